@@ -1,0 +1,209 @@
+"""ctypes access to the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Loads ``oracle/liboracle.so`` (the plain-C restatement of the reference hot
+path) and, where it was built, ``oracle/_ref/libvppref.so`` (the reference's
+own C++ sources compiled unmodified, driven through ``ref_harness.cpp``).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
+``bench.py`` may import this module; the product path never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libvppref.so")
+REF_TREE = os.environ.get("VPP_REFERENCE_TREE", "/root/reference")
+
+_P = C.c_void_p
+_I = C.c_int
+_L = C.c_long
+
+
+def build(with_reference: bool | None = None, jobs: int = 8) -> None:
+    """Compile the oracle (and the reference library when its tree exists)."""
+    subprocess.run(["make", "-s", "-C", HERE, f"-j{jobs}", "liboracle.so"], check=True)
+    if with_reference is None:
+        with_reference = os.path.isdir(os.path.join(REF_TREE, "src"))
+    if with_reference:
+        subprocess.run(["make", "-s", "-C", HERE, f"-j{jobs}", "ref", f"REF={REF_TREE}"], check=True)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+class Oracle:
+    """The C restatement."""
+
+    def __init__(self, path: str = ORACLE_SO):
+        if not os.path.exists(path):
+            build(with_reference=False)
+        self.lib = C.CDLL(path)
+        L = self.lib
+        L.vo_num_mbs.argtypes = [_I, _I]
+        L.vo_me_full.argtypes = [_P, _P, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L)]
+        L.vo_me_full_detail.argtypes = [_P, _P, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L)] + [_P] * 6
+        L.vo_me_full_intpel.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P]
+        L.vo_quarter_read16.argtypes = [_P, _I, _I, _I, _I, _I, _I, _P]
+        L.vo_half.argtypes = [_P, _I, _I, _P]
+        L.vo_fwd4x4.argtypes = [_P, _I, _I, _I, _I, _I]
+        L.vo_inv4x4.argtypes = [_P, _I, _I, _I, _I, _P]
+        L.vo_quantise_value.argtypes = [C.c_short, _I, _I, _I]
+        L.vo_rgb24_to_yuv420.argtypes = [_I, _P, _I, _I, _I, _I, _P, _P, _P]
+        L.vo_bench_me_full.argtypes = [_P, _P, _I, _I, _I, _I, _I, _P]
+
+    def me_full(self, src, ref, motion_range, dist_incl=None, slice_map=None, detail=False):
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = self.lib.vo_num_mbs(w, h)
+        mv = np.zeros((nmb, 2), np.int16)
+        dist = np.zeros(nmb, np.int32)
+        avg = _L(0)
+        incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
+        sl = None if slice_map is None else np.ascontiguousarray(slice_map, dtype=np.int32)
+        if not detail:
+            rc = self.lib.vo_me_full(_ptr(src), _ptr(ref), w, h, motion_range, _ptr(incl), _ptr(sl),
+                                     _ptr(mv), _ptr(dist), C.byref(avg))
+            if rc:
+                raise ValueError(f"vo_me_full rc={rc}")
+            return mv, dist, avg.value
+        extra = {k: np.zeros((nmb, 2) if k.endswith("mv") else nmb, np.int32)
+                 for k in ("int_mv", "sub_mv", "min_d", "zero_d", "pred_mv", "pred_d")}
+        rc = self.lib.vo_me_full_detail(_ptr(src), _ptr(ref), w, h, motion_range, _ptr(incl), _ptr(sl),
+                                        _ptr(mv), _ptr(dist), C.byref(avg),
+                                        *[_ptr(extra[k]) for k in ("int_mv", "sub_mv", "min_d", "zero_d",
+                                                                   "pred_mv", "pred_d")])
+        if rc:
+            raise ValueError(f"vo_me_full_detail rc={rc}")
+        return mv, dist, avg.value, extra
+
+    def me_full_intpel(self, src, ref, motion_range, metric=1):
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = self.lib.vo_num_mbs(w, h)
+        mv = np.zeros((nmb, 2), np.int16)
+        dist = np.zeros(nmb, np.int32)
+        rc = self.lib.vo_me_full_intpel(_ptr(src), _ptr(ref), w, h, motion_range, metric, _ptr(mv), _ptr(dist))
+        if rc:
+            raise ValueError(f"vo_me_full_intpel rc={rc}")
+        return mv, dist
+
+    def quarter_read16(self, plane, x, y, qx, qy):
+        h, w = plane.shape
+        plane = np.ascontiguousarray(plane, dtype=np.int16)
+        out = np.zeros((16, 16), np.int16)
+        self.lib.vo_quarter_read16(_ptr(plane), w, h, x, y, qx, qy, _ptr(out))
+        return out
+
+    def half(self, plane):
+        h, w = plane.shape
+        plane = np.ascontiguousarray(plane, dtype=np.int16)
+        out = np.zeros((h // 2, w // 2), np.int16)
+        self.lib.vo_half(_ptr(plane), w, h, _ptr(out))
+        return out
+
+    def fwd4x4(self, data, layout, mode, qp, intra):
+        d = np.array(data, dtype=np.int16, copy=True, order="C")
+        unit = 16 if layout == 0 else 256
+        self.lib.vo_fwd4x4(_ptr(d), d.size // unit, layout, mode, qp, intra)
+        return d
+
+    def inv4x4(self, data, layout, mode, qp, weight=None):
+        d = np.array(data, dtype=np.int16, copy=True, order="C")
+        unit = 16 if layout == 0 else 256
+        wt = None if weight is None else np.ascontiguousarray(weight, dtype=np.int32)
+        self.lib.vo_inv4x4(_ptr(d), d.size // unit, layout, mode, qp, _ptr(wt))
+        return d
+
+    def quantise_value(self, val, pos, qp, intra):
+        return self.lib.vo_quantise_value(int(val), pos, qp, intra)
+
+    def rgb_to_yuv(self, kind, bgr, chr_off=0, flip=0):
+        h, w, _ = bgr.shape
+        bgr = np.ascontiguousarray(bgr, dtype=np.uint8)
+        y = np.zeros((h, w), np.int16)
+        u = np.zeros((h // 2, w // 2), np.int16)
+        v = np.zeros((h // 2, w // 2), np.int16)
+        rc = self.lib.vo_rgb24_to_yuv420(kind, _ptr(bgr), w, h, chr_off, flip, _ptr(y), _ptr(u), _ptr(v))
+        if rc:
+            raise ValueError(f"vo_rgb24_to_yuv420 rc={rc}")
+        return y, u, v
+
+    def bench_me_full(self, srcs, refs, motion_range, nthreads):
+        h, w = srcs[0].shape
+        n = len(srcs)
+        keep = [np.ascontiguousarray(a, dtype=np.int16) for a in list(srcs) + list(refs)]
+        sp = (_P * n)(*[k.ctypes.data for k in keep[:n]])
+        rp = (_P * n)(*[k.ctypes.data for k in keep[n:]])
+        mv = np.zeros((n, self.lib.vo_num_mbs(w, h), 2), np.int16)
+        rc = self.lib.vo_bench_me_full(sp, rp, n, w, h, motion_range, nthreads, _ptr(mv))
+        if rc:
+            raise ValueError(f"vo_bench_me_full rc={rc}")
+        return mv
+
+
+class Reference:
+    """The reference's own C++ classes (only where oracle/_ref was built)."""
+
+    KIND = {"full": 0, "multires": 1, "multires_cross": 2, "multires_cross_v2": 3}
+
+    def __init__(self, path: str = REF_SO):
+        self.lib = C.CDLL(path)
+        L = self.lib
+        L.ref_me_estimate.argtypes = [_I, _P, _P, _I, _I, _I, _I, _P, _P, _I, _P, C.POINTER(_L)]
+        L.ref_fwd_transform.argtypes = [_I, _P, _I, _I, _I, _I]
+        L.ref_inv_transform.argtypes = [_I, _P, _I, _I, _I, _P]
+        L.ref_quantise_value.argtypes = [C.c_short, _I, _I, _I]
+        L.ref_rgb_to_yuv.argtypes = [_I, _P, _I, _I, _I, _I, _P, _P, _P]
+
+    @staticmethod
+    def available(path: str = REF_SO) -> bool:
+        return os.path.exists(path)
+
+    def me(self, kind, src, ref, motion_range, mode=1, dist_incl=None, lam=None, repeat=1):
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = (w // 16) * (h // 16)
+        mv = np.zeros((nmb, 2), np.int16)
+        avg = _L(0)
+        incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
+        lamv = None if lam is None else np.array([lam], np.float64)
+        rc = self.lib.ref_me_estimate(self.KIND[kind], _ptr(src), _ptr(ref), w, h, motion_range, mode,
+                                      _ptr(incl), _ptr(lamv), repeat, _ptr(mv), C.byref(avg))
+        if rc:
+            raise ValueError(f"ref_me_estimate rc={rc}")
+        return mv, avg.value
+
+    def fwd(self, impl, data, mode, qp, intra):
+        d = np.array(data, dtype=np.int16, copy=True, order="C")
+        unit = 256 if impl == 2 else 16
+        self.lib.ref_fwd_transform(impl, _ptr(d), d.size // unit, mode, qp, intra)
+        return d
+
+    def inv(self, impl, data, mode, qp, weight=None):
+        d = np.array(data, dtype=np.int16, copy=True, order="C")
+        unit = 256 if impl == 1 else 16
+        wt = None if weight is None else np.ascontiguousarray(weight, dtype=np.int32)
+        self.lib.ref_inv_transform(impl, _ptr(d), d.size // unit, mode, qp, _ptr(wt))
+        return d
+
+    def quantise_value(self, val, pos, qp, intra):
+        return self.lib.ref_quantise_value(int(val), pos, qp, intra)
+
+    def rgb_to_yuv(self, kind, bgr, chr_off=0, flip=0):
+        h, w, _ = bgr.shape
+        bgr = np.ascontiguousarray(bgr, dtype=np.uint8)
+        y = np.zeros((h, w), np.int16)
+        u = np.zeros((h // 2, w // 2), np.int16)
+        v = np.zeros((h // 2, w // 2), np.int16)
+        self.lib.ref_rgb_to_yuv(kind, _ptr(bgr), w, h, chr_off, flip, _ptr(y), _ptr(u), _ptr(v))
+        return y, u, v

@@ -1,0 +1,363 @@
+/*
+ * oracle_me_full.c -- TEST INFRASTRUCTURE ONLY (CPU oracle).
+ *
+ * Restatement of MotionEstimatorH264ImplFull::Estimate
+ * (src/CodecUtils/MotionEstimatorH264ImplFull.cpp:330-613) and the median
+ * predictor it drives (H264MotionVectorPredictorImpl1 over MacroBlockH264).
+ * Build without FMA contraction (-ffp-contract=off): GetBestVector is IEEE
+ * double arithmetic and must be evaluated one rounded operation at a time.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include "oracle_internal.h"
+
+#define MB 16
+#define EXT_BORDER (MB + 3) /* macroblock + MEH264IF_PADDING (Full.cpp:71,244) */
+
+int vo_num_mbs(int w, int h) { return (w / MB) * (h / MB); }
+
+/* ------------------------------------------------------------------------ */
+/* Median predictor                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* MacroBlockH264::Median (MacroBlockH264.cpp:923-936). */
+int vo_median3(int x, int y, int z)
+{
+    int lo, hi;
+    if (y - z < 0) { lo = y; hi = z; } else { lo = z; hi = y; }
+    if (x < lo) lo = x;
+    if (x > hi) hi = x;
+    return x + y + z - lo - hi;
+}
+
+int vo_pred_init(vo_pred_state* st, int cols, int rows, const int* slice)
+{
+    st->cols = cols;
+    st->rows = rows;
+    st->slice = slice;
+    st->mvx = (int*)calloc((size_t)cols * rows, sizeof(int));
+    st->mvy = (int*)calloc((size_t)cols * rows, sizeof(int));
+    return (st->mvx && st->mvy) ? 0 : -1;
+}
+
+void vo_pred_free(vo_pred_state* st)
+{
+    free(st->mvx);
+    free(st->mvy);
+    st->mvx = st->mvy = NULL;
+}
+
+static int nb_avail(const vo_pred_state* st, int k, int r, int c)
+{
+    if (r < 0 || c < 0 || c >= st->cols) return -1;
+    int n = r * st->cols + c;
+    if (st->slice && st->slice[n] != st->slice[k]) return -1;
+    return n;
+}
+
+/* MacroBlockH264::GetMbMotionMedianPred (MacroBlockH264.cpp:757-816): A = left,
+ * B = above, C = above-right (D = above-left when C is missing); a missing
+ * neighbour contributes (0,0); with neither B nor C, B and C take A.  Every
+ * neighbour of a macroblock precedes it in raster order, so within one
+ * Estimate() call it has already been given its final vector and is inter. */
+void vo_pred_get(const vo_pred_state* st, int k, int* px, int* py)
+{
+    int r = k / st->cols, c = k % st->cols;
+    int a = nb_avail(st, k, r, c - 1);
+    int b = nb_avail(st, k, r - 1, c);
+    int cc = nb_avail(st, k, r - 1, c + 1);
+    int ax = 0, ay = 0, bx = 0, by = 0, cx = 0, cy = 0;
+    if (a >= 0) { ax = st->mvx[a]; ay = st->mvy[a]; }
+    if (b >= 0) { bx = st->mvx[b]; by = st->mvy[b]; }
+    if (cc >= 0) { cx = st->mvx[cc]; cy = st->mvy[cc]; }
+    else {
+        int d = nb_avail(st, k, r - 1, c - 1);
+        if (d >= 0) { cx = st->mvx[d]; cy = st->mvy[d]; }
+    }
+    if (b < 0 && cc < 0) { bx = cx = ax; by = cy = ay; }
+    *px = vo_median3(ax, bx, cx);
+    *py = vo_median3(ay, by, cy);
+}
+
+/* H264MotionVectorPredictorImpl1::Set16x16MotionVector (…Impl1.h:103-111). */
+void vo_pred_set(vo_pred_state* st, int k, int mvx, int mvy)
+{
+    st->mvx[k] = mvx;
+    st->mvy[k] = mvy;
+}
+
+/* GetBestVector over the Fifo contents (Full.h:140-168): cost = D/norm +
+ * lambda*sqrt(|v-ref|^2), strict improvement, scanning from slot 0. */
+int vo_best_vector5(const int* xs, const int* ys, const int* ds, double lambda, double norm,
+                    int xref, int yref)
+{
+    int pos = 0;
+    double mag = (double)((xs[0] - xref) * (xs[0] - xref) + (ys[0] - yref) * (ys[0] - yref));
+    double cost = ((double)ds[0] / norm) + (lambda * sqrt(mag));
+    for (int i = 1; i < 5; i++) {
+        double m = (double)((xs[i] - xref) * (xs[i] - xref) + (ys[i] - yref) * (ys[i] - yref));
+        double c = ((double)ds[i] / norm) + (lambda * sqrt(m));
+        if (c < cost) { cost = c; pos = i; }
+    }
+    return pos;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Search range                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* MotionEstimatorH264ImplFull::GetMotionRange with zero offset
+ * (Full.cpp:1029-1081): the vector magnitude is limited to vecRange-1 and the
+ * block may reach at most `MB` pels outside the picture. */
+static void full_range(int x, int y, int w, int h, int motion_range, int range,
+                       int* xl, int* xr, int* yu, int* yd)
+{
+    const int boundary = EXT_BORDER - 3;
+    int vec_range = motion_range / 4;
+    int lr = (-range > -vec_range) ? range : vec_range - 1;
+    int rr = (range < vec_range) ? range : vec_range - 1;
+    *xl = (x - lr >= -boundary) ? -lr : -(x + boundary);
+    *xr = (x + rr < w) ? rr : w - x;
+    *yu = (y - lr >= -boundary) ? -lr : -(y + boundary);
+    *yd = (y + rr < h) ? rr : h - y;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Sub-pel window                                                            */
+/* ------------------------------------------------------------------------ */
+/* LoadHalfQuartPelWindow / LoadQuartPelWindow / QuarterRead of the window
+ * (Full.cpp:1095-1255), restated as sample functions.  Coordinates are in
+ * quarter pels relative to the best full-pel block origin (ox, oy) of the
+ * extended reference.  Even positions hold G (full), h (vertical half),
+ * b (horizontal half) and j (centre half) samples; odd positions around the
+ * winning half-pel point are rounded averages of two even neighbours. */
+static int floordiv4(int v) { return v >= 0 ? v / 4 : -((-v + 3) / 4); }
+
+static int win_even(const short* e, int es, int ox, int oy, int qy, int qx)
+{
+    int fy = floordiv4(qy), fx = floordiv4(qx);
+    int ry = qy - 4 * fy, rx = qx - 4 * fx;
+    int x = ox + fx, y = oy + fy;
+    if (ry == 0 && rx == 0) return e[(size_t)y * es + x];
+    if (ry == 2 && rx == 0) return vo_hp_h(e, es, x, y);
+    if (ry == 0 && rx == 2) return vo_hp_b(e, es, x, y);
+    return vo_hp_j(e, es, x, y);
+}
+
+/* Quarter sample at offset (sy, sx) in -1..1 around the even point (cy, cx),
+ * following the eight assignments of LoadQuartPelWindow (Full.cpp:1207-1220). */
+static int win_quarter(const short* e, int es, int ox, int oy, int cy, int cx, int sy, int sx)
+{
+    int a, b;
+    if (sy < 0) {
+        if (sx < 0) { a = win_even(e, es, ox, oy, cy - 2, cx - 2); b = win_even(e, es, ox, oy, cy, cx); }
+        else if (sx == 0) { a = win_even(e, es, ox, oy, cy - 2, cx); b = win_even(e, es, ox, oy, cy, cx); }
+        else { a = win_even(e, es, ox, oy, cy - 2, cx); b = win_even(e, es, ox, oy, cy, cx + 2); }
+    } else if (sy == 0) {
+        if (sx < 0) { a = win_even(e, es, ox, oy, cy, cx - 2); b = win_even(e, es, ox, oy, cy, cx); }
+        else { a = win_even(e, es, ox, oy, cy, cx + 2); b = win_even(e, es, ox, oy, cy, cx); }
+    } else {
+        if (sx < 0) { a = win_even(e, es, ox, oy, cy, cx - 2); b = win_even(e, es, ox, oy, cy + 2, cx); }
+        else if (sx == 0) { a = win_even(e, es, ox, oy, cy + 2, cx); b = win_even(e, es, ox, oy, cy, cx); }
+        else { a = win_even(e, es, ox, oy, cy + 2, cx); b = win_even(e, es, ox, oy, cy, cx + 2); }
+    }
+    return (a + b + 1) >> 1;
+}
+
+/* Neighbour order of the sub-pel passes (MEH264IF_SubPos, Full.cpp:77-81). */
+static const int SUB_X[8] = {-1, 0, 1, -1, 1, -1, 0, 1};
+static const int SUB_Y[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+
+/* Half-pel pass then quarter-pel pass around the full-pel winner at ext
+ * origin (ox, oy) (Full.cpp:452-517).  *min_d enters as the full-pel minimum
+ * and leaves as the refined one; returns the quarter-pel refinement. */
+static void subpel_refine(const short* in, int ins, const short* e, int es, int ox, int oy,
+                          int* min_d, int* qmx, int* qmy)
+{
+    short blk[256];
+    int hmx = 0, hmy = 0, best = *min_d;
+    for (int k = 0; k < 8; k++) {
+        int qx = 2 * SUB_X[k], qy = 2 * SUB_Y[k];
+        for (int r = 0; r < 16; r++)
+            for (int c = 0; c < 16; c++)
+                blk[r * 16 + c] = (short)win_even(e, es, ox, oy, 4 * r + qy, 4 * c + qx);
+        int d = vo_tsd16_lt(in, ins, blk, 16, best);
+        if (d < best) { best = d; hmx = qx; hmy = qy; }
+    }
+    int bx = hmx, by = hmy;
+    for (int k = 0; k < 8; k++) {
+        for (int r = 0; r < 16; r++)
+            for (int c = 0; c < 16; c++)
+                blk[r * 16 + c] = (short)win_quarter(e, es, ox, oy, 4 * r + hmy, 4 * c + hmx, SUB_Y[k], SUB_X[k]);
+        int d = vo_tsd16_lt(in, ins, blk, 16, best);
+        if (d < best) { best = d; bx = hmx + SUB_X[k]; by = hmy + SUB_Y[k]; }
+    }
+    *min_d = best;
+    *qmx = bx;
+    *qmy = by;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Integer-pel scan                                                          */
+/* ------------------------------------------------------------------------ */
+/* Full.cpp:394-446: raster scan of the range; (0,0) is the start point; a
+ * candidate is skipped when, shifted by the current best vector, it would
+ * leave the range; ties go to the candidate nearer the rounded prediction. */
+static int int_scan(const short* in, int ins, const short* e, int es, int w, int h,
+                    int n, int m, int motion_range, int metric, int prx, int pry,
+                    int* zero_d, int* bx, int* by)
+{
+    int xl, xr, yu, yd;
+    int eox = vo_clamp_origin(n + EXT_BORDER, w + 2 * EXT_BORDER, MB);
+    int eoy = vo_clamp_origin(m + EXT_BORDER, h + 2 * EXT_BORDER, MB);
+    const short* blk0 = e + (size_t)eoy * es + eox;
+    int zd = metric ? vo_tad16(in, ins, blk0, es) : vo_tsd16(in, ins, blk0, es);
+    int min_d = zd, mx = 0, my = 0;
+    full_range(n, m, w, h, motion_range, motion_range / 4, &xl, &xr, &yu, &yd);
+    for (int i = yu; i <= yd; i++) {
+        for (int j = xl; j <= xr; j++) {
+            if (i == 0 && j == 0) continue;
+            if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+            int ox = vo_clamp_origin(n + j + EXT_BORDER, w + 2 * EXT_BORDER, MB);
+            int oy = vo_clamp_origin(m + i + EXT_BORDER, h + 2 * EXT_BORDER, MB);
+            const short* cand = e + (size_t)oy * es + ox;
+            int d = metric ? vo_tad16_lt(in, ins, cand, es, min_d) : vo_tsd16_lt(in, ins, cand, es, min_d);
+            if (d > min_d) continue;
+            if (d == min_d) {
+                int cxo = mx - prx, cyo = my - pry, nxo = j - prx, nyo = i - pry;
+                if ((cyo * cyo + cxo * cxo) - (nyo * nyo + nxo * nxo) < 0) continue;
+            }
+            min_d = d;
+            mx = j;
+            my = i;
+        }
+    }
+    *zero_d = zd;
+    *bx = mx;
+    *by = my;
+    return min_d;
+}
+
+/* Nearest full-pel prediction, C integer division (Full.cpp:368-380). */
+static int round_pred(int p) { return p < 0 ? (p - 2) / 4 : (p + 2) / 4; }
+
+int vo_me_full_detail(const short* src, const short* ref, int w, int h, int motion_range,
+                      const unsigned char* dist_incl, const int* slice,
+                      short* mv_out, int* mb_dist, long* avg_dist,
+                      int* int_mv, int* sub_mv, int* min_dv, int* zero_dv,
+                      int* pred_mv, int* pred_dv)
+{
+    if (!src || !ref || !mv_out || w < MB || h < MB || (w % MB) != 0 || motion_range < 4)
+        return -1;
+    int cols = w / MB, rows = h / MB, nmb = cols * rows;
+    int es = w + 2 * EXT_BORDER;
+    short* e = vo_ext_alloc(ref, w, h, EXT_BORDER);
+    vo_pred_state ps;
+    if (!e || vo_pred_init(&ps, cols, rows, slice) != 0) {
+        free(e);
+        vo_pred_free(&ps);
+        return -2;
+    }
+    long total = 0;
+    int included = 0;
+    for (int k = 0; k < nmb; k++) {
+        int n = (k % cols) * MB, m = (k / cols) * MB;
+        const short* in = src + (size_t)vo_clamp_origin(m, h, MB) * w + vo_clamp_origin(n, w, MB);
+
+        int px, py;
+        vo_pred_get(&ps, k, &px, &py);
+        int pxq = px % 4, pyq = py % 4, px0 = px / 4, py0 = py / 4;
+
+        int zd, mx, my;
+        int min_d = int_scan(in, w, e, es, w, h, n, m, motion_range, 0,
+                             round_pred(px), round_pred(py), &zd, &mx, &my);
+        if (int_mv) { int_mv[2 * k] = mx; int_mv[2 * k + 1] = my; }
+
+        int ox = vo_clamp_origin(n + mx + EXT_BORDER, es, MB);
+        int oy = vo_clamp_origin(m + my + EXT_BORDER, h + 2 * EXT_BORDER, MB);
+        int qmx, qmy;
+        subpel_refine(in, w, e, es, ox, oy, &min_d, &qmx, &qmy);
+        int mvx = 4 * mx + qmx, mvy = 4 * my + qmy;
+        if (sub_mv) { sub_mv[2 * k] = mvx; sub_mv[2 * k + 1] = mvy; }
+        if (min_dv) min_dv[k] = min_d;
+        if (zero_dv) zero_dv[k] = zd;
+
+        /* Prediction clamped to one macroblock outside the picture (Full.cpp:532-541). */
+        if (px0 + n > w) px0 = MB;
+        if (px0 + n < -MB) px0 = -MB;
+        if (py0 + m > h) py0 = MB;
+        if (py0 + m < -MB) py0 = -MB;
+        px = 4 * px0 + pxq;
+        py = 4 * py0 + pyq;
+        int pox = vo_clamp_origin(px0 + n + EXT_BORDER, es, MB);
+        int poy = vo_clamp_origin(py0 + m + EXT_BORDER, h + 2 * EXT_BORDER, MB);
+        int pd;
+        if (pxq || pyq) {
+            short blk[256];
+            vo_qread16_ext(e, es, pox, poy, pxq, pyq, blk);
+            pd = vo_tsd16(in, w, blk, 16);
+        } else {
+            pd = vo_tsd16(in, w, e + (size_t)poy * es + pox, es);
+        }
+        if (pred_mv) { pred_mv[2 * k] = px; pred_mv[2 * k + 1] = py; }
+        if (pred_dv) pred_dv[k] = pd;
+
+        /* Fifo after pushing zero, pred, best (Full.cpp:573-576; Fifo.h:74-94). */
+        int xs[5] = {mvx, px, 0, 0, 0}, ys[5] = {mvy, py, 0, 0, 0}, ds[5] = {min_d, pd, zd, zd, zd};
+        int pos = vo_best_vector5(xs, ys, ds, 1.05, 256.0, px, py);
+        mvx = xs[pos];
+        mvy = ys[pos];
+        if (dist_incl && dist_incl[k]) {
+            included++;
+            total += ds[pos];
+        }
+        if (mb_dist) mb_dist[k] = ds[pos];
+        mv_out[2 * k] = (short)mvx;
+        mv_out[2 * k + 1] = (short)mvy;
+        vo_pred_set(&ps, k, mvx, mvy);
+    }
+    if (avg_dist) *avg_dist = included ? total / included : 0;
+    vo_pred_free(&ps);
+    free(e);
+    return 0;
+}
+
+int vo_me_full(const short* src, const short* ref, int w, int h, int motion_range,
+               const unsigned char* dist_incl, const int* slice,
+               short* mv_out, int* mb_dist, long* avg_dist)
+{
+    return vo_me_full_detail(src, ref, w, h, motion_range, dist_incl, slice, mv_out, mb_dist,
+                             avg_dist, NULL, NULL, NULL, NULL, NULL, NULL);
+}
+
+int vo_me_full_intpel(const short* src, const short* ref, int w, int h, int motion_range,
+                      int metric, short* mv_out, int* mb_dist)
+{
+    if (!src || !ref || !mv_out || w < MB || h < MB || (w % MB) != 0 || motion_range < 4)
+        return -1;
+    int cols = w / MB, rows = h / MB, nmb = cols * rows;
+    int es = w + 2 * EXT_BORDER;
+    short* e = vo_ext_alloc(ref, w, h, EXT_BORDER);
+    vo_pred_state ps;
+    if (!e || vo_pred_init(&ps, cols, rows, NULL) != 0) {
+        free(e);
+        vo_pred_free(&ps);
+        return -2;
+    }
+    for (int k = 0; k < nmb; k++) {
+        int n = (k % cols) * MB, m = (k / cols) * MB;
+        const short* in = src + (size_t)vo_clamp_origin(m, h, MB) * w + vo_clamp_origin(n, w, MB);
+        int px, py, zd, mx, my;
+        vo_pred_get(&ps, k, &px, &py);
+        int d = int_scan(in, w, e, es, w, h, n, m, motion_range, metric,
+                         round_pred(px), round_pred(py), &zd, &mx, &my);
+        mv_out[2 * k] = (short)(4 * mx);
+        mv_out[2 * k + 1] = (short)(4 * my);
+        if (mb_dist) mb_dist[k] = d;
+        vo_pred_set(&ps, k, 4 * mx, 4 * my);
+    }
+    vo_pred_free(&ps);
+    free(e);
+    return 0;
+}

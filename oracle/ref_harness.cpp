@@ -1,0 +1,172 @@
+/*
+ * ref_harness.cpp -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A thin extern "C" driver around the reference's own C++ classes, compiled
+ * together with the reference sources (read where they lie) by
+ * oracle/Makefile into oracle/_ref/libvppref.so.  It exists to pin the C
+ * restatement in oracle/*.c and to generate the golden fixtures; it contains
+ * no algorithm of its own, only object set-up in the way a vpp codec does it.
+ */
+#include <math.h>
+#include <string.h>
+#include <stdlib.h>
+
+#include "MacroBlockH264.h"
+#include "H264MotionVectorPredictorImpl1.h"
+#include "MotionEstimatorH264ImplFull.h"
+#include "MotionEstimatorH264ImplMultires.h"
+#include "MotionEstimatorH264ImplMultiresCross.h"
+#include "MotionEstimatorH264ImplMultiresCrossVer2.h"
+#include "VectorStructList.h"
+#include "FastForward4x4ITImpl1.h"
+#include "FastForward4x4ITImpl2.h"
+#include "FastInverse4x4ITImpl1.h"
+#include "FastForward4x4On16x16ITImpl1.h"
+#include "FastInverse4x4On16x16ITImpl1.h"
+#include "FastFixedPointRGB24toYUV420Converter.h"
+#include "RealRGB24toYUV420Converter.h"
+#include "RealRGB24toYUV420ConverterImpl2.h"
+
+namespace {
+
+/* A macroblock array laid out as a codec lays it out: rows x cols with the
+ * neighbourhood wired by MacroBlockH264::Initialise.  Rows are rounded up so
+ * the reference's partial bottom row (h % 16 != 0) reads valid memory.
+ *
+ * Every macroblock of a partial bottom row asks the predictor for index N_MB
+ * (vecPos stops at maxLength, MotionEstimatorH264ImplFull.cpp:594-601) and its
+ * results are dropped.  When that prediction points below the picture,
+ * Full.cpp:536-537 replaces it with +16 rows, which for this row places the
+ * pred-vector QuarterRead (Full.cpp:551) up to 3 rows past the extended
+ * reference (OverlayMem2Dv2.cpp:989-1010; AddressSanitizer reports a heap
+ * overflow there).  Putting the partial row in a slice of its own makes that
+ * prediction (0,0), keeping the reference in bounds without changing any
+ * stored result. */
+struct MbGrid {
+    int rows, cols;
+    MacroBlockH264* flat;
+    MacroBlockH264** rowp;
+    MbGrid(int w, int h) {
+        cols = w / 16;
+        rows = (h + 15) / 16;
+        int full_rows = h / 16;
+        flat = new MacroBlockH264[rows * cols];
+        rowp = new MacroBlockH264*[rows];
+        for (int r = 0; r < rows; r++) rowp[r] = &flat[r * cols];
+        MacroBlockH264::Initialise(rows, cols, 0, full_rows * cols - 1, 0, rowp);
+        if (rows > full_rows)
+            MacroBlockH264::Initialise(rows, cols, full_rows * cols, rows * cols - 1, 1, rowp);
+    }
+    ~MbGrid() { delete[] rowp; delete[] flat; }
+};
+
+/* Flags with one extra trailing `false`: the reference reads the flag at index
+ * N_MB for the macroblocks of a partial bottom row (they are dropped). */
+bool* make_flags(const unsigned char* incl, int nmb) {
+    if (!incl) return NULL;
+    bool* f = new bool[nmb + 1];
+    for (int i = 0; i < nmb; i++) f[i] = incl[i] != 0;
+    f[nmb] = false;
+    return f;
+}
+
+void copy_vectors(VectorStructList* l, int nmb, short* out) {
+    for (int i = 0; i < nmb; i++) {
+        out[2 * i] = (short)l->GetSimpleElement(i, 0);
+        out[2 * i + 1] = (short)l->GetSimpleElement(i, 1);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+/* kind: 0 Full, 1 Multires, 2 MultiresCross, 3 MultiresCrossVer2.
+ * lambda: NULL, or a pointer passed to Estimate(long*, void*) (Ver2 only).
+ * Returns 0 on success. */
+int ref_me_estimate(int kind, const short* src, const short* ref, int w, int h, int motion_range,
+                    int mode, const unsigned char* incl, const double* lambda, int nframes_same_object,
+                    short* mv_out, long* avg_out)
+{
+    int nmb = (w / 16) * (h / 16);
+    MbGrid grid(w, h);
+    H264MotionVectorPredictorImpl1 pred(grid.flat);
+    bool* flags = make_flags(incl, nmb);
+    IMotionEstimator* me = NULL;
+    switch (kind) {
+    case 0: me = new MotionEstimatorH264ImplFull(src, ref, w, h, motion_range, &pred, flags); break;
+    case 1: me = new MotionEstimatorH264ImplMultires(src, ref, w, h, motion_range, &pred, flags); break;
+    case 2: me = new MotionEstimatorH264ImplMultiresCross(src, ref, w, h, motion_range, flags); break;
+    case 3: me = new MotionEstimatorH264ImplMultiresCrossVer2(src, ref, w, h, motion_range, &pred, flags); break;
+    default: delete[] flags; return -1;
+    }
+    if (!me->Create()) { delete me; delete[] flags; return -2; }
+    me->SetMode(mode);
+    long avg = 0;
+    void* res = NULL;
+    for (int f = 0; f < (nframes_same_object > 0 ? nframes_same_object : 1); f++)
+        res = lambda ? me->Estimate(&avg, (void*)lambda) : me->Estimate(&avg);
+    copy_vectors((VectorStructList*)res, nmb, mv_out);
+    if (avg_out) *avg_out = avg;
+    delete me;
+    delete[] flags;
+    return 0;
+}
+
+/* impl: 0 FastForward4x4ITImpl1, 1 FastForward4x4ITImpl2 (16-short blocks),
+ *       2 FastForward4x4On16x16ITImpl1 (256-short macroblocks). */
+int ref_fwd_transform(int impl, short* data, int nunits, int mode, int qp, int intra)
+{
+    IForwardTransform* t = NULL;
+    int unit = 16;
+    if (impl == 0) t = new FastForward4x4ITImpl1();
+    else if (impl == 1) t = new FastForward4x4ITImpl2();
+    else if (impl == 2) { t = new FastForward4x4On16x16ITImpl1(); unit = 256; }
+    else return -1;
+    t->SetMode(mode);
+    t->SetParameter(IForwardTransform::INTRA_FLAG_ID, intra);
+    t->SetParameter(IForwardTransform::QUANT_ID, qp);
+    for (int u = 0; u < nunits; u++) t->Transform(data + (size_t)u * unit);
+    delete t;
+    return 0;
+}
+
+/* impl: 0 FastInverse4x4ITImpl1 (16-short blocks), 1 FastInverse4x4On16x16ITImpl1. */
+int ref_inv_transform(int impl, short* data, int nunits, int mode, int qp, const int* weight16)
+{
+    IInverseTransform* t = NULL;
+    int unit = 16;
+    if (impl == 0) t = new FastInverse4x4ITImpl1();
+    else if (impl == 1) { t = new FastInverse4x4On16x16ITImpl1(); unit = 256; }
+    else return -1;
+    if (weight16) t->SetScale((void*)weight16);
+    t->SetMode(mode);
+    t->SetParameter(IInverseTransform::QUANT_ID, qp);
+    for (int u = 0; u < nunits; u++) t->InverseTransform(data + (size_t)u * unit);
+    delete t;
+    return 0;
+}
+
+int ref_quantise_value(short val, int pos, int qp, int intra)
+{
+    FastForward4x4ITImpl2 t;
+    t.SetParameter(IForwardTransform::INTRA_FLAG_ID, intra);
+    return t.QuantiseValue(val, pos, qp);
+}
+
+/* kind: 0 FastFixedPoint, 1 Real, 2 RealImpl2. */
+int ref_rgb_to_yuv(int kind, const unsigned char* bgr, int w, int h, int chr_off, int flip,
+                   short* y, short* u, short* v)
+{
+    RGBtoYUV420Converter* c = NULL;
+    if (kind == 0) c = new FastFixedPointRGB24toYUV420Converter(w, h, chr_off);
+    else if (kind == 1) c = new RealRGB24toYUV420Converter(w, h, chr_off);
+    else if (kind == 2) c = new RealRGB24toYUV420ConverterImpl2(w, h, chr_off);
+    else return -1;
+    c->SetFlip(flip != 0);
+    c->Convert((void*)bgr, y, u, v);
+    delete c;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+/*
+ * vpp_oracle.h -- CPU oracle for the vpp encoder hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * algorithms (CSIR-RTVC/ImageCodingUtils, "vpp") used as the checker for the
+ * CUDA implementation.  Only tests/, __graft_entry__.smoke() and the CPU
+ * baseline legs of bench.py may load it.  The product path never calls it.
+ *
+ * Parity of this restatement is pinned against the reference's own C++ code,
+ * compiled from its sources by oracle/Makefile into oracle/_ref/ and driven
+ * through oracle/ref_harness.cpp; the golden fixtures under tests/golden/ were
+ * produced by that compiled reference (tests/golden/make_golden.py).
+ *
+ * Conventions shared with the reference:
+ *   - pixel planes are `short` (int16), luma values 0..255;
+ *   - motion vectors are quarter-pel {short x, short y} per 16x16 macroblock,
+ *     raster order (VectorStructList SIMPLE2D, include/CodecUtils/VectorStructList.h:56-60);
+ *   - motion_range is in quarter-pel units (MotionEstimatorH264ImplFull.cpp:125).
+ */
+#ifndef VPP_ORACLE_H
+#define VPP_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Motion estimation                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* Number of macroblocks whose vectors the reference stores for a w x h frame:
+ * (w/16) * (h/16) (MotionEstimatorH264ImplFull.cpp:293).  A partial bottom MB
+ * row (h % 16 != 0) is searched by the reference but its results are dropped
+ * (Full.cpp:594); the oracle skips it. */
+int vo_num_mbs(int w, int h);
+
+/* MotionEstimatorH264ImplFull::Estimate (src/CodecUtils/MotionEstimatorH264ImplFull.cpp:330-613)
+ * with the H264MotionVectorPredictorImpl1 median predictor over a single-slice
+ * (or per-MB `slice`) macroblock array.
+ *   dist_incl : NULL, or one flag per stored MB (reference `pDistortionIncluded`).
+ *   slice     : NULL (one slice), or one slice id per stored MB.
+ *   mv_out    : 2*N_MB shorts (x,y pairs).
+ *   mb_dist   : NULL or N_MB ints: distortion of the selected vector (Fifo item
+ *               chosen by GetBestVector, Full.cpp:579-590).
+ *   avg_dist  : the reference's avgDistortion out-param.
+ * Returns 0 on success, negative on invalid arguments. */
+int vo_me_full(const short* src, const short* ref, int w, int h, int motion_range,
+               const unsigned char* dist_incl, const int* slice,
+               short* mv_out, int* mb_dist, long* avg_dist);
+
+/* Instrumented variant: additionally returns, per MB, the integer-pel winner
+ * (ix, iy), the sub-pel stage winner (mvx, mvy, min_d), the zero-vector and
+ * predicted-vector distortions and the clamped prediction used by
+ * GetBestVector.  Any output pointer may be NULL. */
+int vo_me_full_detail(const short* src, const short* ref, int w, int h, int motion_range,
+                      const unsigned char* dist_incl, const int* slice,
+                      short* mv_out, int* mb_dist, long* avg_dist,
+                      int* int_mv, int* sub_mv, int* min_d, int* zero_d,
+                      int* pred_mv, int* pred_d);
+
+/* Integer-pel full search only (the hot loop of Full.cpp:350-446) with the
+ * sum-of-absolute-differences metric (OverlayMem2Dv2::Tad16x16 /
+ * Tad16x16LessThan) or the squared metric, the same running-best skip and
+ * predictor tie-break, the predictor being fed the integer winner in
+ * quarter-pel units.  metric: 0 = SSD, 1 = SAD. */
+int vo_me_full_intpel(const short* src, const short* ref, int w, int h, int motion_range,
+                      int metric, short* mv_out, int* mb_dist);
+
+/* OverlayMem2Dv2::QuarterRead (src/ImageUtils/OverlayMem2Dv2.cpp:704-1052) of
+ * a 16x16 block whose full-pel origin is (x, y) in a frame extended by edge
+ * replication, at quarter offsets (qx, qy) in -3..3. */
+void vo_quarter_read16(const short* plane, int w, int h, int x, int y, int qx, int qy,
+                       short* dst256);
+
+/* OverlayMem2Dv2::Half 2:1 decimation (OverlayMem2Dv2.cpp:3018-3033). */
+void vo_half(const short* src, int w, int h, short* dst);
+
+/* ------------------------------------------------------------------------ */
+/* 4x4 integer transform + H.264 quantisation                                */
+/* ------------------------------------------------------------------------ */
+/* Modes (IForwardTransform.h:119-125): 0 = transform+quant, 1 = transform only,
+ * 2 = quant only.  `layout`: 0 = contiguous 16-short blocks (FastForward4x4ITImpl1,
+ * FastInverse4x4ITImpl1), 1 = 16x16 raster macroblocks of 256 shorts
+ * (FastForward4x4On16x16ITImpl1, FastInverse4x4On16x16ITImpl1). */
+void vo_fwd4x4(short* data, int nunits, int layout, int mode, int qp, int intra);
+void vo_inv4x4(short* data, int nunits, int layout, int mode, int qp, const int* weight_scale16);
+/* FastForward4x4ITImpl2::QuantiseValue (FastForward4x4ITImpl2.cpp:640-683). */
+int vo_quantise_value(short val, int pos, int qp, int intra);
+
+/* ------------------------------------------------------------------------ */
+/* RGB24 -> YUV420                                                           */
+/* ------------------------------------------------------------------------ */
+/* kind: 0 = FastFixedPointRGB24toYUV420Converter (integer),
+ *       1 = RealRGB24toYUV420Converter (IEEE double),
+ *       2 = RealRGB24toYUV420ConverterImpl2 (IEEE double, other rounding).
+ * flip: bottom-up source rows (Real converters only; FastFixedPoint ignores it). */
+int vo_rgb24_to_yuv420(int kind, const unsigned char* bgr, int w, int h, int chr_off, int flip,
+                       short* y, short* u, short* v);
+
+/* ------------------------------------------------------------------------ */
+/* Multi-threaded CPU baseline drivers (one estimator state per thread over   */
+/* independent frame pairs; the reference has no internal threading).        */
+/* ------------------------------------------------------------------------ */
+int vo_bench_me_full(const short* const* srcs, const short* const* refs, int nframes,
+                     int w, int h, int motion_range, int nthreads, short* mv_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
