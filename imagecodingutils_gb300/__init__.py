@@ -1,0 +1,362 @@
+"""GB300 (sm_103a) encoder hot path of vpp (CSIR-RTVC/ImageCodingUtils).
+
+Python mirror of the reference's C++ plugin interfaces over the C ABI in
+``include/vppgpu.h``.  Class, method and parameter names follow the
+reference so code and tests read like the vpp originals:
+
+* ``MotionEstimatorH264ImplFull`` -- ``IMotionEstimator``
+  (include/CodecUtils/IMotionEstimator.h:51-96): ``Create``, ``Reset``,
+  ``Ready``, ``SetMode``/``GetMode``, ``Estimate``.
+* ``FastForward4x4ITImpl1`` / ``FastForward4x4ITImpl2`` /
+  ``FastForward4x4On16x16ITImpl1`` -- ``IForwardTransform``
+  (include/CodecUtils/IForwardTransform.h:56-127).
+* ``FastInverse4x4ITImpl1`` / ``FastInverse4x4On16x16ITImpl1`` -- ``IInverseTransform``.
+* ``FastGpuRGB24toYUV420Converter`` -- ``RGBtoYUV420Converter``
+  (include/ImageUtils/RGBtoYUV420Converter.h:57-86), the reference's own
+  reserved (empty) GPU slot.
+
+Every call runs the CUDA kernels; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import VppGpuError, check, load
+
+__all__ = [
+    "Context", "get_context", "MotionEstimatorH264ImplFull", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
+    "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1",
+    "FastGpuRGB24toYUV420Converter", "VppGpuError", "load",
+]
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One CUDA device and stream (vppgpu_ctx)."""
+
+    def __init__(self, device: int = 0):
+        lib = load()
+        h = C.c_void_p()
+        check(lib.vppgpu_ctx_create(device, C.byref(h)), "vppgpu_ctx_create")
+        self.handle = h
+        self.device = device
+
+    def synchronize(self):
+        check(load().vppgpu_ctx_synchronize(self.handle), "vppgpu_ctx_synchronize")
+
+    def set_stream(self, stream_ptr: int | None):
+        check(load().vppgpu_ctx_set_stream(self.handle, C.c_void_p(stream_ptr) if stream_ptr else None),
+              "vppgpu_ctx_set_stream")
+
+    def launch_count(self) -> int:
+        n = C.c_ulonglong()
+        check(load().vppgpu_ctx_launch_count(self.handle, C.byref(n)), "vppgpu_ctx_launch_count")
+        return n.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().vppgpu_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: Context | None = None
+
+
+def get_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+# ---------------------------------------------------------------------------
+# Motion estimation
+# ---------------------------------------------------------------------------
+class _MotionEstimatorBase:
+    KIND = _lib.ME_FULL
+
+    def __init__(self, pSrc, pRef, imgWidth: int, imgHeight: int, motionRange: int = 64, pMVPred=None,
+                 pDistortionIncluded=None, mb_slice=None, ctx: Context | None = None):
+        # The planes are captured by reference and re-read on every Estimate(),
+        # as the reference does with its pSrc/pRef constructor arguments.
+        self._src = pSrc
+        self._ref = pRef
+        self._w = int(imgWidth)
+        self._h = int(imgHeight)
+        self._range = int(motionRange)
+        self._pred = pMVPred
+        self._incl = None if pDistortionIncluded is None else np.ascontiguousarray(pDistortionIncluded, np.uint8)
+        self._slice = None if mb_slice is None else np.ascontiguousarray(mb_slice, np.int32)
+        self._ctx = ctx or get_context()
+        self._h_me = None
+        self._mode = 1
+        self.last_mb_distortion = None
+
+    # IMotionEstimator
+    def Create(self) -> int:
+        self._destroy()
+        h = C.c_void_p()
+        rc = load().vppgpu_me_create(self._ctx.handle, self.KIND, self._w, self._h, self._range, C.byref(h))
+        if rc != _lib.OK:
+            return 0
+        self._h_me = h
+        load().vppgpu_me_set_mode(self._h_me, self._mode)
+        return 1
+
+    def Reset(self) -> None:
+        pass
+
+    def Ready(self) -> int:
+        return 1 if self._h_me else 0
+
+    def SetMode(self, mode: int) -> None:
+        self._mode = int(mode)
+        if self._h_me:
+            load().vppgpu_me_set_mode(self._h_me, self._mode)
+
+    def GetMode(self) -> int:
+        return self._mode
+
+    def num_mbs(self) -> int:
+        return (self._w // 16) * (self._h // 16)
+
+    def Estimate(self, *args, want_mb_distortion: bool = True):
+        """Estimate() -> (vectors[N_MB, 2] int16 quarter-pel, avgDistortion).
+
+        Estimate(pSrc, pRef) ignores its arguments and uses the constructor
+        planes, exactly like the reference (MotionEstimatorH264ImplFull.h:109-110)."""
+        if not self._h_me:
+            raise VppGpuError(_lib.ERR_NOT_READY, "Estimate before Create")
+        src = np.ascontiguousarray(self._src, np.int16)
+        ref = np.ascontiguousarray(self._ref, np.int16)
+        if src.size != self._w * self._h or ref.size != self._w * self._h:
+            raise ValueError("source/reference plane size does not match the estimator")
+        n = self.num_mbs()
+        mv = np.empty((n, 2), np.int16)
+        dist = np.empty(n, np.int32) if want_mb_distortion else None
+        avg = C.c_long(0)
+        check(load().vppgpu_me_estimate(self._h_me, _ptr(src), _ptr(ref), _ptr(self._incl), _ptr(self._slice),
+                                        _ptr(mv), _ptr(dist), C.byref(avg)), "vppgpu_me_estimate")
+        self.last_mb_distortion = dist
+        if self._pred is not None:  # side effect of the reference on its predictor
+            for k in range(n):
+                self._pred.Set16x16MotionVector(k, int(mv[k, 0]), int(mv[k, 1]))
+        return mv, avg.value
+
+    def last_sweeps(self) -> int:
+        s = C.c_int()
+        check(load().vppgpu_me_last_sweeps(self._h_me, C.byref(s)), "vppgpu_me_last_sweeps")
+        return s.value
+
+    def _destroy(self):
+        if self._h_me:
+            load().vppgpu_me_destroy(self._h_me)
+            self._h_me = None
+
+    def __del__(self):
+        try:
+            self._destroy()
+        except Exception:
+            pass
+
+
+class MotionEstimatorH264ImplFull(_MotionEstimatorBase):
+    """GPU MotionEstimatorH264ImplFull (src/CodecUtils/MotionEstimatorH264ImplFull.cpp)."""
+
+    KIND = _lib.ME_FULL
+
+
+# ---------------------------------------------------------------------------
+# 4x4 transforms
+# ---------------------------------------------------------------------------
+QUANT_ID = 0
+INTRA_FLAG_ID = 1
+TransformAndQuant, TransformOnly, QuantOnly = 0, 1, 2
+
+
+class _ForwardBase:
+    LAYOUT = _lib.LAYOUT_BLOCKS
+    UNIT = 16
+
+    def __init__(self, ctx: Context | None = None):
+        self._ctx = ctx or get_context()
+        self._mode = TransformAndQuant
+        self._intra = 1
+        self._q = 1
+
+    def SetMode(self, mode):
+        self._mode = int(mode)
+
+    def GetMode(self):
+        return self._mode
+
+    def SetParameter(self, paramID, paramVal):
+        if paramID == QUANT_ID:
+            self._q = int(paramVal)
+        elif paramID == INTRA_FLAG_ID:
+            self._intra = int(paramVal)
+
+    def GetParameter(self, paramID):
+        return self._q if paramID == QUANT_ID else self._intra
+
+    def SetScale(self, pScale):
+        pass
+
+    def GetScale(self):
+        return None
+
+    def Transform(self, ptr, pCoeff=None):
+        """In place on an int16 array holding a whole number of units, or
+        Transform(pIn, pCoeff): copy then transform pCoeff."""
+        if pCoeff is not None:
+            np.copyto(pCoeff, ptr)
+            ptr = pCoeff
+        a = _as_units(ptr, self.UNIT)
+        check(load().vppgpu_fwd4x4(self._ctx.handle, _ptr(a), a.size // self.UNIT, self.LAYOUT, self._mode, self._q,
+                                   self._intra), "vppgpu_fwd4x4")
+        if a is not ptr:
+            np.copyto(ptr, a.reshape(ptr.shape))
+        return ptr
+
+    def QuantiseValue(self, val, pos, qp):
+        self._q = int(qp)
+        return load().vppgpu_quantise_value(int(val), int(pos), int(qp), self._intra)
+
+
+class FastForward4x4ITImpl1(_ForwardBase):
+    LAYOUT, UNIT = _lib.LAYOUT_BLOCKS, 16
+
+
+class FastForward4x4ITImpl2(_ForwardBase):
+    LAYOUT, UNIT = _lib.LAYOUT_BLOCKS, 16
+
+
+class FastForward4x4On16x16ITImpl1(_ForwardBase):
+    LAYOUT, UNIT = _lib.LAYOUT_MB16, 256
+
+
+class _InverseBase:
+    LAYOUT = _lib.LAYOUT_BLOCKS
+    UNIT = 16
+
+    def __init__(self, ctx: Context | None = None):
+        self._ctx = ctx or get_context()
+        self._mode = TransformAndQuant
+        self._q = 1
+        self._weight = np.full(16, 16, np.int32)
+
+    def SetMode(self, mode):
+        self._mode = int(mode)
+
+    def GetMode(self):
+        return self._mode
+
+    def SetParameter(self, paramID, paramVal):
+        if paramID == QUANT_ID:
+            self._q = int(paramVal)
+
+    def GetParameter(self, paramID):
+        return self._q
+
+    def SetScale(self, pScale):
+        self._weight = np.ascontiguousarray(pScale, np.int32).reshape(16).copy()
+
+    def GetScale(self):
+        return self._weight
+
+    def InverseTransform(self, ptr, pOut=None):
+        if pOut is not None:
+            np.copyto(pOut, ptr)
+            ptr = pOut
+        a = _as_units(ptr, self.UNIT)
+        check(load().vppgpu_inv4x4(self._ctx.handle, _ptr(a), a.size // self.UNIT, self.LAYOUT, self._mode, self._q,
+                                   _ptr(self._weight)), "vppgpu_inv4x4")
+        if a is not ptr:
+            np.copyto(ptr, a.reshape(ptr.shape))
+        return ptr
+
+
+class FastInverse4x4ITImpl1(_InverseBase):
+    LAYOUT, UNIT = _lib.LAYOUT_BLOCKS, 16
+
+
+class FastInverse4x4On16x16ITImpl1(_InverseBase):
+    LAYOUT, UNIT = _lib.LAYOUT_MB16, 256
+
+
+def _as_units(a, unit):
+    if not isinstance(a, np.ndarray) or a.dtype != np.int16:
+        raise TypeError("transform data must be an int16 numpy array")
+    if a.size % unit:
+        raise ValueError(f"transform data must hold a whole number of {unit}-sample units")
+    return a if a.flags.c_contiguous else np.ascontiguousarray(a)
+
+
+def tq_roundtrip_plane(residual, qp, intra, inv_order=_lib.INV_ROWS_FIRST, weight16=None, ctx=None):
+    """Levels and reconstruction of a residual plane (BlockH264 forward + quant,
+    dequant + inverse for every 4x4 block)."""
+    ctx = ctx or get_context()
+    res = np.ascontiguousarray(residual, np.int16)
+    h, w = res.shape
+    lev = np.empty_like(res)
+    rec = np.empty_like(res)
+    wt = None if weight16 is None else np.ascontiguousarray(weight16, np.int32)
+    check(load().vppgpu_tq_roundtrip_plane(ctx.handle, _ptr(res), _ptr(lev), _ptr(rec), w, h, w, int(qp), int(intra),
+                                           int(inv_order), _ptr(wt)), "vppgpu_tq_roundtrip_plane")
+    return lev, rec
+
+
+# ---------------------------------------------------------------------------
+# Colour conversion
+# ---------------------------------------------------------------------------
+class FastGpuRGB24toYUV420Converter:
+    """RGBtoYUV420Converter filled in on the GPU.  kind selects the arithmetic
+    of FastFixedPointRGB24toYUV420Converter (default), RealRGB24toYUV420Converter
+    or RealRGB24toYUV420ConverterImpl2."""
+
+    def __init__(self, width=0, height=0, chrOff=0, kind=_lib.RGB_FIXED_POINT, ctx: Context | None = None):
+        self._width, self._height, self._chrOff, self._flip = int(width), int(height), int(chrOff), False
+        self._kind = int(kind)
+        self._ctx = ctx or get_context()
+
+    def GetWidth(self):
+        return self._width
+
+    def GetHeight(self):
+        return self._height
+
+    def GetChrominanceOffset(self):
+        return self._chrOff
+
+    def GetFlip(self):
+        return self._flip
+
+    def SetDimensions(self, width, height):
+        self._width, self._height = int(width), int(height)
+
+    def SetFlip(self, flip):
+        self._flip = bool(flip)
+
+    def SetChrominanceOffset(self, val):
+        self._chrOff = int(val)
+
+    def Convert(self, pRgb, pY, pU, pV):
+        rgb = np.ascontiguousarray(pRgb, np.uint8)
+        for p in (pY, pU, pV):
+            if p.dtype != np.int16 or not p.flags.c_contiguous:
+                raise TypeError("output planes must be contiguous int16 arrays")
+        check(load().vppgpu_rgb24_to_yuv420(self._ctx.handle, self._kind, _ptr(rgb), self._width, self._height,
+                                            self._chrOff, int(self._flip), _ptr(pY), _ptr(pU), _ptr(pV)),
+              "vppgpu_rgb24_to_yuv420")

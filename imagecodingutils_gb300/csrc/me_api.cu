@@ -1,0 +1,342 @@
+// me_api.cu -- the motion-estimation handle of the vppgpu C ABI: the
+// constructor + Create() of an IMotionEstimator implementation (device
+// allocations sized once per frame geometry) and its Estimate() calls.
+#include <stdlib.h>
+#include <string.h>
+
+#include "me_common.cuh"
+#include "me_internal.h"
+
+struct vppgpu_me {
+    vppgpu_ctx* ctx;
+    int kind, W, H, cols, rows, nmb, motion_range, mode;
+    int rstride;
+    short* d_src16;
+    short* d_ref16;
+    unsigned char* d_src8;
+    unsigned char* d_refp;
+    int* spec;  // 5 * nmb: mv, imv, min, zero, flags
+    int* tables;
+    int* state; // 3 * nmb: final_mv, final_dist, pred_used
+    int* d_out_mv;
+    int* d_out_dist;
+    long long* d_out_avg;
+    unsigned char* d_incl;
+    int* d_slice;
+    vppgpu::MeCtrl* ctrl;
+    int* changed;
+    int sweep_limit;
+    int resolve_grid;
+    vppgpu::MeCtrl* h_ctrl;  // pinned
+    int last_status;
+    // per-kernel timing (vppgpu_me_set_timing)
+    int timing;
+    int ring_used;
+    cudaEvent_t (*ring)[4];
+    int timed_n;
+    double timed_ms[3];
+};
+
+namespace {
+constexpr int kRing = 256;
+
+void ring_fold(vppgpu_me* me)
+{
+    for (int i = 0; i < me->ring_used; i++) {
+        cudaEventSynchronize(me->ring[i][3]);
+        for (int k = 0; k < 3; k++) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, me->ring[i][k], me->ring[i][k + 1]) == cudaSuccess) me->timed_ms[k] += ms;
+        }
+        me->timed_n++;
+    }
+    me->ring_used = 0;
+}
+
+void ring_free(vppgpu_me* me)
+{
+    if (!me->ring) return;
+    for (int i = 0; i < kRing; i++)
+        for (int k = 0; k < 4; k++) cudaEventDestroy(me->ring[i][k]);
+    free(me->ring);
+    me->ring = nullptr;
+}
+
+cudaEvent_t* ring_slot(vppgpu_me* me)
+{
+    if (!me->timing || !me->ring) return nullptr;
+    if (me->ring_used == kRing) ring_fold(me);
+    return me->ring[me->ring_used++];
+}
+}  // namespace
+
+namespace {
+
+void me_free(vppgpu_me* me)
+{
+    if (!me) return;
+    cudaSetDevice(me->ctx->device);
+    cudaStreamSynchronize(me->ctx->stream);
+    cudaFree(me->d_src16);
+    cudaFree(me->d_ref16);
+    cudaFree(me->d_src8);
+    cudaFree(me->d_refp);
+    cudaFree(me->spec);
+    cudaFree(me->tables);
+    cudaFree(me->state);
+    cudaFree(me->d_out_mv);
+    cudaFree(me->d_out_dist);
+    cudaFree(me->d_out_avg);
+    cudaFree(me->d_incl);
+    cudaFree(me->d_slice);
+    cudaFree(me->ctrl);
+    cudaFree(me->changed);
+    cudaFreeHost(me->h_ctrl);
+    ring_free(me);
+    free(me);
+}
+
+template <typename T>
+int dalloc(T** p, size_t count)
+{
+    if (cudaMalloc((void**)p, sizeof(T) * (count ? count : 1)) != cudaSuccess) return VPPGPU_ERR_OUT_OF_MEMORY;
+    return VPPGPU_OK;
+}
+
+vppgpu::FullArgs full_args(vppgpu_me* me, const unsigned char* incl, const int* slice, int* out_mv, int* out_dist,
+                           long long* out_avg, double lambda)
+{
+    vppgpu::FullArgs a;
+    a.W = me->W;
+    a.H = me->H;
+    a.cols = me->cols;
+    a.nmb = me->nmb;
+    a.motion_range = me->motion_range;
+    a.rstride = me->rstride;
+    a.src8 = me->d_src8;
+    a.refp = me->d_refp;
+    a.spec_mv = me->spec;
+    a.spec_imv = me->spec + me->nmb;
+    a.spec_min = me->spec + 2 * me->nmb;
+    a.spec_zero = me->spec + 3 * me->nmb;
+    a.spec_flags = me->spec + 4 * me->nmb;
+    a.tables = me->tables;
+    a.final_mv = me->state;
+    a.final_dist = me->state + me->nmb;
+    a.pred_used = me->state + 2 * me->nmb;
+    a.slice = slice;
+    a.incl = incl;
+    a.out_mv = out_mv;
+    a.out_dist = out_dist;
+    a.out_avg = out_avg;
+    a.ctrl = me->ctrl;
+    a.changed = me->changed;
+    a.lambda = lambda;
+    a.sweep_limit = me->sweep_limit;
+    a.spin_limit = 20000000LL;  // ~2 s of polling before a barrier gives up
+    return a;
+}
+
+int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigned char* d_incl, const int* d_slice,
+        int* d_mv, int* d_dist, long long* d_avg, double lambda)
+{
+    vppgpu_ctx* ctx = me->ctx;
+    VPP_CUDA(cudaMemsetAsync(me->ctrl, 0, sizeof(vppgpu::MeCtrl), ctx->stream));
+    VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
+    vppgpu::FullArgs a = full_args(me, d_incl, d_slice, d_mv, d_dist, d_avg, lambda);
+    return vppgpu::full_launch(ctx, a, me->nmb, d_src16, d_ref16, me->resolve_grid, ring_slot(me));
+}
+
+int status_from_ctrl(const vppgpu::MeCtrl& c)
+{
+    if (c.status & vppgpu::ST_PIXEL_RANGE) return VPPGPU_ERR_PIXEL_RANGE;
+    if (c.status & vppgpu::ST_TIMEOUT) return VPPGPU_ERR_TIMEOUT;
+    return VPPGPU_OK;
+}
+
+bool aligned(const void* p, size_t a) { return ((uintptr_t)p & (a - 1)) == 0; }
+
+}  // namespace
+
+extern "C" {
+
+int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motion_range, vppgpu_me** out)
+{
+    if (!ctx || !out) return VPPGPU_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
+    if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
+    if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind != VPPGPU_ME_FULL) return VPPGPU_ERR_UNSUPPORTED;
+    int rc = vppgpu::bind(ctx);
+    if (rc) return rc;
+    vppgpu_me* me = (vppgpu_me*)calloc(1, sizeof(vppgpu_me));
+    if (!me) return VPPGPU_ERR_OUT_OF_MEMORY;
+    me->ctx = ctx;
+    me->kind = kind;
+    me->W = width;
+    me->H = height;
+    me->cols = width / 16;
+    me->rows = height / 16;
+    me->nmb = me->cols * me->rows;
+    me->motion_range = motion_range;
+    me->mode = 1;
+    me->rstride = width + 2 * vppgpu::PAD;
+    me->sweep_limit = me->nmb + 2;
+    size_t npix = (size_t)width * height;
+    size_t npad = (size_t)me->rstride * (height + 2 * vppgpu::PAD);
+    if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) || (rc = dalloc(&me->d_src8, npix)) ||
+        (rc = dalloc(&me->d_refp, npad)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
+        (rc = dalloc(&me->tables, (size_t)me->nmb * 64 * 64)) || (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
+        (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
+        (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||
+        (rc = dalloc(&me->d_slice, me->nmb)) || (rc = dalloc(&me->ctrl, 1)) ||
+        (rc = dalloc(&me->changed, (size_t)me->sweep_limit))) {
+        me_free(me);
+        return rc;
+    }
+    if (cudaMallocHost((void**)&me->h_ctrl, sizeof(vppgpu::MeCtrl)) != cudaSuccess) {
+        me_free(me);
+        return VPPGPU_ERR_OUT_OF_MEMORY;
+    }
+    if ((rc = vppgpu::full_prepare(ctx, me->nmb, &me->resolve_grid))) {
+        me_free(me);
+        return rc;
+    }
+    *out = me;
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_destroy(vppgpu_me* me)
+{
+    if (!me) return VPPGPU_ERR_INVALID_ARG;
+    me_free(me);
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_set_mode(vppgpu_me* me, int mode)
+{
+    if (!me) return VPPGPU_ERR_INVALID_ARG;
+    me->mode = mode;
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_get_mode(vppgpu_me* me, int* mode)
+{
+    if (!me || !mode) return VPPGPU_ERR_INVALID_ARG;
+    *mode = me->mode;
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_num_mbs(vppgpu_me* me, int* n)
+{
+    if (!me || !n) return VPPGPU_ERR_INVALID_ARG;
+    *n = me->nmb;
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_estimate_device(vppgpu_me* me, const short* d_src, const short* d_ref, const unsigned char* d_incl,
+                              const int* d_slice, short* d_mv_out, int* d_mb_dist_out, long long* d_avg_out)
+{
+    if (!me || !d_src || !d_ref || !d_mv_out) return VPPGPU_ERR_INVALID_ARG;
+    if (!aligned(d_src, 4) || !aligned(d_ref, 4) || !aligned(d_mv_out, 4)) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    me->last_status = VPPGPU_OK;
+    return run(me, d_src, d_ref, d_incl, d_slice, (int*)d_mv_out, d_mb_dist_out, d_avg_out, 1.05);
+}
+
+static int estimate_host(vppgpu_me* me, const short* src, const short* ref, const unsigned char* incl,
+                         const int* slice, short* mv_out, int* mb_dist_out, long* avg, double lambda)
+{
+    if (!me || !src || !ref || !mv_out) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    cudaStream_t st = me->ctx->stream;
+    size_t plane = sizeof(short) * (size_t)me->W * me->H;
+    VPP_CUDA(cudaMemcpyAsync(me->d_src16, src, plane, cudaMemcpyHostToDevice, st));
+    VPP_CUDA(cudaMemcpyAsync(me->d_ref16, ref, plane, cudaMemcpyHostToDevice, st));
+    if (incl) VPP_CUDA(cudaMemcpyAsync(me->d_incl, incl, (size_t)me->nmb, cudaMemcpyHostToDevice, st));
+    if (slice) VPP_CUDA(cudaMemcpyAsync(me->d_slice, slice, sizeof(int) * me->nmb, cudaMemcpyHostToDevice, st));
+    rc = run(me, me->d_src16, me->d_ref16, incl ? me->d_incl : nullptr, slice ? me->d_slice : nullptr,
+             me->d_out_mv, mb_dist_out ? me->d_out_dist : nullptr, nullptr, lambda);
+    if (rc) return rc;
+    VPP_CUDA(cudaMemcpyAsync(mv_out, me->d_out_mv, sizeof(int) * me->nmb, cudaMemcpyDeviceToHost, st));
+    if (mb_dist_out)
+        VPP_CUDA(cudaMemcpyAsync(mb_dist_out, me->d_out_dist, sizeof(int) * me->nmb, cudaMemcpyDeviceToHost, st));
+    VPP_CUDA(cudaMemcpyAsync(me->h_ctrl, me->ctrl, sizeof(vppgpu::MeCtrl), cudaMemcpyDeviceToHost, st));
+    VPP_CUDA(cudaStreamSynchronize(st));
+    me->last_status = status_from_ctrl(*me->h_ctrl);
+    if (me->last_status) return me->last_status;
+    if (avg) *avg = me->h_ctrl->count ? (long)(me->h_ctrl->total / me->h_ctrl->count) : 0;
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_estimate(vppgpu_me* me, const short* src, const short* ref, const unsigned char* incl,
+                       const int* slice, short* mv_out, int* mb_dist_out, long* avg)
+{
+    return estimate_host(me, src, ref, incl, slice, mv_out, mb_dist_out, avg, 1.05);
+}
+
+int vppgpu_me_estimate_lambda(vppgpu_me* me, const short* src, const short* ref, const unsigned char* incl,
+                              const int* slice, double lambda, short* mv_out, int* mb_dist_out, long* avg)
+{
+    // The full-search estimator has no lambda overload: IMotionEstimator's
+    // default Estimate(long*, void*) ignores the parameter (IMotionEstimator.h:94).
+    (void)lambda;
+    return estimate_host(me, src, ref, incl, slice, mv_out, mb_dist_out, avg, 1.05);
+}
+
+int vppgpu_me_last_status(vppgpu_me* me)
+{
+    if (!me) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    VPP_CUDA(cudaMemcpyAsync(me->h_ctrl, me->ctrl, sizeof(vppgpu::MeCtrl), cudaMemcpyDeviceToHost, me->ctx->stream));
+    VPP_CUDA(cudaStreamSynchronize(me->ctx->stream));
+    return status_from_ctrl(*me->h_ctrl);
+}
+
+int vppgpu_me_set_timing(vppgpu_me* me, int enable)
+{
+    if (!me) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    if (enable && !me->ring) {
+        me->ring = (cudaEvent_t(*)[4])calloc(kRing, sizeof(*me->ring));
+        if (!me->ring) return VPPGPU_ERR_OUT_OF_MEMORY;
+        for (int i = 0; i < kRing; i++)
+            for (int k = 0; k < 4; k++) VPP_CUDA(cudaEventCreate(&me->ring[i][k]));
+    }
+    me->timing = enable != 0;
+    me->ring_used = 0;
+    me->timed_n = 0;
+    me->timed_ms[0] = me->timed_ms[1] = me->timed_ms[2] = 0.0;
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_timing(vppgpu_me* me, int* n, double* pack_ms, double* search_ms, double* resolve_ms)
+{
+    if (!me || !n || !pack_ms || !search_ms || !resolve_ms) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    if (me->ring) ring_fold(me);
+    *n = me->timed_n;
+    *pack_ms = me->timed_ms[0];
+    *search_ms = me->timed_ms[1];
+    *resolve_ms = me->timed_ms[2];
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
+{
+    if (!me || !sweeps) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    VPP_CUDA(cudaMemcpyAsync(me->h_ctrl, me->ctrl, sizeof(vppgpu::MeCtrl), cudaMemcpyDeviceToHost, me->ctx->stream));
+    VPP_CUDA(cudaStreamSynchronize(me->ctx->stream));
+    *sweeps = me->h_ctrl->sweeps;
+    return VPPGPU_OK;
+}
+
+}  // extern "C"

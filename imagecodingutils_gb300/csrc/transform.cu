@@ -1,0 +1,473 @@
+// transform.cu -- H.264 4x4 forward integer transform + quantisation and
+// dequantisation + inverse transform for sm_103a.
+//
+// Bit-exact with FastForward4x4ITImpl1/Impl2 / FastForward4x4On16x16ITImpl1
+// (src/CodecUtils/FastForward4x4ITImpl1.cpp:100-201, FastForward4x4On16x16ITImpl1.cpp:457-757)
+// and FastInverse4x4ITImpl1 / FastInverse4x4On16x16ITImpl1
+// (src/CodecUtils/FastInverse4x4ITImpl1.cpp:119-244, FastInverse4x4On16x16ITImpl1.cpp:120-361):
+// every intermediate the reference stores to a `short` is truncated to 16
+// bits here at the same point.
+//
+// The work is HBM-bound (32 B read, 32 B written per block and pass), so the
+// kernels are one thread per 4x4 block with each row moved as one 8-byte
+// access; a warp covers 32 horizontally adjacent blocks, i.e. 256 contiguous
+// bytes per row access.
+#include "vppgpu_internal.cuh"
+
+namespace {
+
+// Quantiser multiplication factors MF[qp%6][class] and dequantiser scales
+// V[qp%6][class]; class 0 = (even row, even col), 1 = (odd, odd), 2 = mixed
+// (FastForward4x4ITImpl1.cpp:57-73, FastInverse4x4ITImpl1.cpp:60-74).
+__constant__ int c_fwd_mf[6][3] = {{13107, 5243, 8066}, {11916, 4660, 7490}, {10082, 4194, 6554},
+                                   {9362, 3647, 5825},  {8192, 3355, 5243},  {7282, 2893, 4559}};
+__constant__ int c_inv_v[6][3] = {{10, 16, 13}, {11, 18, 14}, {13, 20, 16},
+                                  {14, 23, 18}, {16, 25, 20}, {18, 29, 23}};
+
+__host__ __device__ constexpr int pos_class(int pos)
+{
+    return (((pos >> 2) & 1) == 0 && (pos & 1) == 0) ? 0 : ((((pos >> 2) & 1) && (pos & 1)) ? 1 : 2);
+}
+
+struct FwdParams {
+    int qm, f, sh;
+};
+
+struct InvParams {
+    int weight[16];  // SetScale() weights (16 = flat)
+    int qm, q, f, right, left;
+};
+
+FwdParams make_fwd(int qp, int intra)
+{
+    FwdParams p;
+    int qe = qp / 6;
+    p.qm = qp % 6;
+    p.sh = 15 + qe;
+    p.f = intra ? (1 << (15 + qe)) / 3 : (1 << (15 + qe)) / 6;
+    return p;
+}
+
+InvParams make_inv(int qp, const int* weight16)
+{
+    InvParams p;
+    int qe = qp / 6;
+    for (int i = 0; i < 16; i++) p.weight[i] = weight16 ? weight16[i] : 16;
+    p.qm = qp % 6;
+    p.q = qp;
+    p.f = qe <= 3 ? (1 << (3 - qe)) : 0;
+    p.right = 4 - qe;
+    p.left = qe - 4;
+    return p;
+}
+
+__device__ __forceinline__ int s16(int x) { return (int)(short)x; }
+
+__device__ __forceinline__ int quant(int x, int mf, const FwdParams& p)
+{
+    // sign-magnitude rounding: negative inputs are negated, never shifted
+    return x < 0 ? s16(-(((-x) * mf + p.f) >> p.sh)) : s16((x * mf + p.f) >> p.sh);
+}
+
+// Forward transform of one block held as 16 ints (row-major), modes 0/1/2.
+__device__ __forceinline__ void fwd_block(int* b, int mode, const FwdParams& p)
+{
+    if (mode == 2) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) b[i] = quant(b[i], c_fwd_mf[p.qm][pos_class(i)], p);
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        int* q = b + 4 * r;
+        int s0 = q[0] + q[3], s3 = q[0] - q[3], s1 = q[1] + q[2], s2 = q[1] - q[2];
+        q[0] = s16(s0 + s1);
+        q[2] = s16(s0 - s1);
+        q[1] = s16(s2 + (s3 << 1));
+        q[3] = s16(s3 - (s2 << 1));
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        int s0 = b[c] + b[12 + c], s3 = b[c] - b[12 + c];
+        int s1 = b[4 + c] + b[8 + c], s2 = b[4 + c] - b[8 + c];
+        int y0 = s0 + s1, y1 = s2 + (s3 << 1), y2 = s0 - s1, y3 = s3 - (s2 << 1);
+        if (mode == 0) {
+            b[c] = quant(y0, c_fwd_mf[p.qm][pos_class(c)], p);
+            b[4 + c] = quant(y1, c_fwd_mf[p.qm][pos_class(4 + c)], p);
+            b[8 + c] = quant(y2, c_fwd_mf[p.qm][pos_class(8 + c)], p);
+            b[12 + c] = quant(y3, c_fwd_mf[p.qm][pos_class(12 + c)], p);
+        } else {
+            b[c] = s16(y0);
+            b[4 + c] = s16(y1);
+            b[8 + c] = s16(y2);
+            b[12 + c] = s16(y3);
+        }
+    }
+}
+
+__device__ __forceinline__ int dequant(int x, int pos, const InvParams& p)
+{
+    int v = x * (c_inv_v[p.qm][pos_class(pos)] * p.weight[pos]);
+    return p.q < 24 ? (v + p.f) >> p.right : v << p.left;
+}
+
+__device__ __forceinline__ void inv_1d(int x0, int x1, int x2, int x3, int& y0, int& y1, int& y2, int& y3)
+{
+    int s0 = x0 + x2, s1 = x0 - x2, s2 = (x1 >> 1) - x3, s3 = x1 + (x3 >> 1);
+    y0 = s0 + s3;
+    y1 = s1 + s2;
+    y2 = s1 - s2;
+    y3 = s0 - s3;
+}
+
+// Inverse of one block: mode 2 = dequant only; modes 0/1 with the pass order
+// of FastInverse4x4ITImpl1 (rows first) or the On16x16 variant (cols first).
+__device__ __forceinline__ void inv_block(int* b, int mode, int cols_first, const InvParams& p)
+{
+    if (mode == 2) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) b[i] = s16(dequant(b[i], i, p));
+        return;
+    }
+    if (mode == 0) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) b[i] = dequant(b[i], i, p);
+    }
+    int y0, y1, y2, y3;
+    if (!cols_first) {
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            int* q = b + 4 * r;
+            inv_1d(q[0], q[1], q[2], q[3], y0, y1, y2, y3);
+            q[0] = s16(y0); q[1] = s16(y1); q[2] = s16(y2); q[3] = s16(y3);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            inv_1d(b[c], b[4 + c], b[8 + c], b[12 + c], y0, y1, y2, y3);
+            b[c] = s16((y0 + 32) >> 6); b[4 + c] = s16((y1 + 32) >> 6);
+            b[8 + c] = s16((y2 + 32) >> 6); b[12 + c] = s16((y3 + 32) >> 6);
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            inv_1d(b[c], b[4 + c], b[8 + c], b[12 + c], y0, y1, y2, y3);
+            b[c] = s16(y0); b[4 + c] = s16(y1); b[8 + c] = s16(y2); b[12 + c] = s16(y3);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            int* q = b + 4 * r;
+            inv_1d(q[0], q[1], q[2], q[3], y0, y1, y2, y3);
+            q[0] = s16((y0 + 32) >> 6); q[1] = s16((y1 + 32) >> 6);
+            q[2] = s16((y2 + 32) >> 6); q[3] = s16((y3 + 32) >> 6);
+        }
+    }
+}
+
+// ---- block addressing ----------------------------------------------------
+// Returns the element offset of block `blk`'s top-left sample and its row
+// stride for the two unit layouts.
+__device__ __forceinline__ long long block_origin(long long blk, int layout, int& rs)
+{
+    if (layout == VPPGPU_LAYOUT_BLOCKS) {
+        rs = 4;
+        return blk * 16;
+    }
+    rs = 16;  // 16x16 raster macroblock: 16 blocks per unit
+    long long mb = blk >> 4;
+    int bi = (int)(blk & 15);
+    return mb * 256 + (bi >> 2) * 64 + (bi & 3) * 4;
+}
+
+__device__ __forceinline__ void load_rows(const short* p, int rs, int* b)
+{
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        uint2 v = *reinterpret_cast<const uint2*>(p + (size_t)r * rs);
+        b[4 * r + 0] = (int)(short)(v.x & 0xffff);
+        b[4 * r + 1] = (int)(short)(v.x >> 16);
+        b[4 * r + 2] = (int)(short)(v.y & 0xffff);
+        b[4 * r + 3] = (int)(short)(v.y >> 16);
+    }
+}
+
+__device__ __forceinline__ void store_rows(short* p, int rs, const int* b)
+{
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        uint2 v;
+        v.x = (unsigned)(b[4 * r + 0] & 0xffff) | ((unsigned)b[4 * r + 1] << 16);
+        v.y = (unsigned)(b[4 * r + 2] & 0xffff) | ((unsigned)b[4 * r + 3] << 16);
+        *reinterpret_cast<uint2*>(p + (size_t)r * rs) = v;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_fwd_units(short* __restrict__ data, long long nblocks, int layout,
+                                                   int mode, FwdParams p)
+{
+    for (long long blk = blockIdx.x * (long long)blockDim.x + threadIdx.x; blk < nblocks;
+         blk += (long long)gridDim.x * blockDim.x) {
+        int rs;
+        short* q = data + block_origin(blk, layout, rs);
+        int b[16];
+        load_rows(q, rs, b);
+        fwd_block(b, mode, p);
+        store_rows(q, rs, b);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_inv_units(short* __restrict__ data, long long nblocks, int layout,
+                                                   int mode, InvParams p)
+{
+    int cols_first = layout == VPPGPU_LAYOUT_MB16;
+    for (long long blk = blockIdx.x * (long long)blockDim.x + threadIdx.x; blk < nblocks;
+         blk += (long long)gridDim.x * blockDim.x) {
+        int rs;
+        short* q = data + block_origin(blk, layout, rs);
+        int b[16];
+        load_rows(q, rs, b);
+        inv_block(b, mode, cols_first, p);
+        store_rows(q, rs, b);
+    }
+}
+
+}  // namespace
+
+// ---- fused plane round trip (also used by the batched/served forms) -------
+namespace vppgpu {
+
+// Same layout as vppgpu_tq_job (include/vppgpu.h).
+struct TqJob {
+    const short* res;
+    short* lev;
+    short* rec;
+    int width, height, stride;
+    int qp, intra;
+};
+static_assert(sizeof(TqJob) == sizeof(vppgpu_tq_job), "TqJob must mirror vppgpu_tq_job");
+
+}  // namespace vppgpu
+
+namespace {
+
+__device__ __forceinline__ void roundtrip_one(const vppgpu::TqJob& j, long long blk, int cols_first,
+                                              const int* weight)
+{
+    int bw = j.width >> 2;
+    int by = (int)(blk / bw), bx = (int)(blk - (long long)by * bw);
+    size_t off = (size_t)by * 4 * j.stride + (size_t)bx * 4;
+    int b[16];
+    load_rows(j.res + off, j.stride, b);
+    FwdParams fp;
+    int qe = j.qp / 6;
+    fp.qm = j.qp % 6;
+    fp.sh = 15 + qe;
+    fp.f = j.intra ? (1 << (15 + qe)) / 3 : (1 << (15 + qe)) / 6;
+    fwd_block(b, 0, fp);
+    store_rows(j.lev + off, j.stride, b);
+    InvParams ip;
+#pragma unroll
+    for (int i = 0; i < 16; i++) ip.weight[i] = weight[i];
+    ip.qm = fp.qm;
+    ip.q = j.qp;
+    ip.f = qe <= 3 ? (1 << (3 - qe)) : 0;
+    ip.right = 4 - qe;
+    ip.left = qe - 4;
+    inv_block(b, 0, cols_first, ip);
+    store_rows(j.rec + off, j.stride, b);
+}
+
+struct Weights {
+    int w[16];
+};
+
+// blockIdx.y selects the job; x covers its blocks with a grid-stride loop.
+__global__ void __launch_bounds__(256) k_tq_roundtrip(const vppgpu::TqJob* __restrict__ jobs, int cols_first,
+                                                      Weights wt)
+{
+    vppgpu::TqJob j = jobs[blockIdx.y];
+    long long nblk = (long long)(j.width >> 2) * (j.height >> 2);
+    for (long long blk = blockIdx.x * (long long)blockDim.x + threadIdx.x; blk < nblk;
+         blk += (long long)gridDim.x * blockDim.x)
+        roundtrip_one(j, blk, cols_first, wt.w);
+}
+
+__global__ void __launch_bounds__(256) k_tq_roundtrip_single(vppgpu::TqJob j, int cols_first, Weights wt)
+{
+    long long nblk = (long long)(j.width >> 2) * (j.height >> 2);
+    for (long long blk = blockIdx.x * (long long)blockDim.x + threadIdx.x; blk < nblk;
+         blk += (long long)gridDim.x * blockDim.x)
+        roundtrip_one(j, blk, cols_first, wt.w);
+}
+
+int grid_for(vppgpu_ctx* ctx, long long nblocks)
+{
+    long long want = (nblocks + 255) / 256;
+    long long cap = (long long)ctx->sm_count * 8;
+    return (int)(want < cap ? (want > 0 ? want : 1) : cap);
+}
+
+int check_common(vppgpu_ctx* ctx, const void* p, long long nunits, int layout, int mode, int qp)
+{
+    if (!ctx || !p || nunits < 0) return VPPGPU_ERR_INVALID_ARG;
+    if (layout != VPPGPU_LAYOUT_BLOCKS && layout != VPPGPU_LAYOUT_MB16) return VPPGPU_ERR_INVALID_ARG;
+    if (mode < 0 || mode > 2 || qp < 0 || qp > 51) return VPPGPU_ERR_INVALID_ARG;
+    return VPPGPU_OK;
+}
+
+}  // namespace
+
+namespace vppgpu {
+
+int launch_tq_jobs(vppgpu_ctx* ctx, const TqJob* d_jobs, int njobs, long long max_blocks, int inv_order,
+                   const int* weight16)
+{
+    Weights wt;
+    for (int i = 0; i < 16; i++) wt.w[i] = weight16 ? weight16[i] : 16;
+    long long want = (max_blocks + 255) / 256;
+    int gx = (int)(want < 4096 ? (want > 0 ? want : 1) : 4096);
+    dim3 grid(gx, njobs);
+    k_tq_roundtrip<<<grid, 256, 0, ctx->stream>>>(d_jobs, inv_order == VPPGPU_INV_COLS_FIRST, wt);
+    VPP_CHECK_LAUNCH(ctx);
+    return VPPGPU_OK;
+}
+
+}  // namespace vppgpu
+
+extern "C" {
+
+int vppgpu_fwd4x4_device(vppgpu_ctx* ctx, short* d, long long nunits, int layout, int mode, int qp, int intra)
+{
+    int rc = check_common(ctx, d, nunits, layout, mode, qp);
+    if (rc) return rc;
+    if ((rc = vppgpu::bind(ctx))) return rc;
+    long long nblocks = layout == VPPGPU_LAYOUT_BLOCKS ? nunits : nunits * 16;
+    if (nblocks == 0) return VPPGPU_OK;
+    k_fwd_units<<<grid_for(ctx, nblocks), 256, 0, ctx->stream>>>(d, nblocks, layout, mode,
+                                                                   make_fwd(qp, intra != 0));
+    VPP_CHECK_LAUNCH(ctx);
+    return VPPGPU_OK;
+}
+
+int vppgpu_inv4x4_device(vppgpu_ctx* ctx, short* d, long long nunits, int layout, int mode, int qp,
+                         const int* weight16)
+{
+    int rc = check_common(ctx, d, nunits, layout, mode, qp);
+    if (rc) return rc;
+    if ((rc = vppgpu::bind(ctx))) return rc;
+    long long nblocks = layout == VPPGPU_LAYOUT_BLOCKS ? nunits : nunits * 16;
+    if (nblocks == 0) return VPPGPU_OK;
+    k_inv_units<<<grid_for(ctx, nblocks), 256, 0, ctx->stream>>>(d, nblocks, layout, mode,
+                                                                   make_inv(qp, weight16));
+    VPP_CHECK_LAUNCH(ctx);
+    return VPPGPU_OK;
+}
+
+static int host_units(vppgpu_ctx* ctx, short* data, long long nunits, int layout, bool fwd, int mode, int qp,
+                      int intra, const int* weight16)
+{
+    int rc = check_common(ctx, data, nunits, layout, mode, qp);
+    if (rc) return rc;
+    if ((rc = vppgpu::bind(ctx))) return rc;
+    size_t bytes = (size_t)nunits * (layout == VPPGPU_LAYOUT_BLOCKS ? 32 : 512);
+    if (bytes == 0) return VPPGPU_OK;
+    short* d = nullptr;
+    VPP_CUDA(cudaMallocAsync((void**)&d, bytes, ctx->stream));
+    cudaError_t e = cudaMemcpyAsync(d, data, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        rc = fwd ? vppgpu_fwd4x4_device(ctx, d, nunits, layout, mode, qp, intra)
+                 : vppgpu_inv4x4_device(ctx, d, nunits, layout, mode, qp, weight16);
+        if (rc == VPPGPU_OK) e = cudaMemcpyAsync(data, d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    }
+    cudaFreeAsync(d, ctx->stream);
+    cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+    if (rc) return rc;
+    if (e != cudaSuccess) return vppgpu::cuda_status(e);
+    if (e2 != cudaSuccess) return vppgpu::cuda_status(e2);
+    return VPPGPU_OK;
+}
+
+int vppgpu_fwd4x4(vppgpu_ctx* ctx, short* data, long long nunits, int layout, int mode, int qp, int intra)
+{
+    return host_units(ctx, data, nunits, layout, true, mode, qp, intra, nullptr);
+}
+
+int vppgpu_inv4x4(vppgpu_ctx* ctx, short* data, long long nunits, int layout, int mode, int qp,
+                  const int* weight16)
+{
+    return host_units(ctx, data, nunits, layout, false, mode, qp, 0, weight16);
+}
+
+int vppgpu_tq_roundtrip_plane_device(vppgpu_ctx* ctx, const short* res, short* lev, short* rec, int width,
+                                     int height, int stride, int qp, int intra, int inv_order,
+                                     const int* weight16)
+{
+    if (!ctx || !res || !lev || !rec || width <= 0 || height <= 0 || (width & 3) || (height & 3) ||
+        stride < width || (stride & 3) || qp < 0 || qp > 51 ||
+        (inv_order != VPPGPU_INV_ROWS_FIRST && inv_order != VPPGPU_INV_COLS_FIRST))
+        return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(ctx);
+    if (rc) return rc;
+    vppgpu::TqJob j{res, lev, rec, width, height, stride, qp, intra != 0};
+    Weights wt;
+    for (int i = 0; i < 16; i++) wt.w[i] = weight16 ? weight16[i] : 16;
+    long long nblk = (long long)(width >> 2) * (height >> 2);
+    k_tq_roundtrip_single<<<grid_for(ctx, nblk), 256, 0, ctx->stream>>>(j, inv_order == VPPGPU_INV_COLS_FIRST,
+                                                                         wt);
+    VPP_CHECK_LAUNCH(ctx);
+    return VPPGPU_OK;
+}
+
+int vppgpu_tq_roundtrip_plane(vppgpu_ctx* ctx, const short* residual, short* levels, short* recon, int width,
+                              int height, int stride, int qp, int intra, int inv_order, const int* weight16)
+{
+    if (!ctx || !residual || !levels || !recon || width <= 0 || height <= 0 || stride < width)
+        return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(ctx);
+    if (rc) return rc;
+    size_t bytes = (size_t)stride * height * sizeof(short);
+    short* d = nullptr;
+    VPP_CUDA(cudaMallocAsync((void**)&d, 3 * bytes, ctx->stream));
+    cudaError_t e = cudaMemcpyAsync(d, residual, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        short* dl = d + (size_t)stride * height;
+        short* dr = dl + (size_t)stride * height;
+        rc = vppgpu_tq_roundtrip_plane_device(ctx, d, dl, dr, width, height, stride, qp, intra, inv_order,
+                                              weight16);
+        if (rc == VPPGPU_OK) e = cudaMemcpyAsync(levels, dl, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+        if (rc == VPPGPU_OK && e == cudaSuccess)
+            e = cudaMemcpyAsync(recon, dr, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    }
+    cudaFreeAsync(d, ctx->stream);
+    cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+    if (rc) return rc;
+    if (e != cudaSuccess) return vppgpu::cuda_status(e);
+    if (e2 != cudaSuccess) return vppgpu::cuda_status(e2);
+    return VPPGPU_OK;
+}
+
+int vppgpu_tq_roundtrip_planes_device(vppgpu_ctx* ctx, const vppgpu_tq_job* d_jobs, int njobs, int inv_order,
+                                      const int* weight16)
+{
+    if (!ctx || !d_jobs || njobs < 1 || njobs > 65535 ||
+        (inv_order != VPPGPU_INV_ROWS_FIRST && inv_order != VPPGPU_INV_COLS_FIRST))
+        return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(ctx);
+    if (rc) return rc;
+    // x extent sized for the largest plane the descriptors may hold (8K luma)
+    return vppgpu::launch_tq_jobs(ctx, reinterpret_cast<const vppgpu::TqJob*>(d_jobs), njobs,
+                                  (long long)(ctx->sm_count) * 8 * 256, inv_order, weight16);
+}
+
+int vppgpu_quantise_value(short val, int pos, int qp, int intra)
+{
+    static const int mf[6][3] = {{13107, 5243, 8066}, {11916, 4660, 7490}, {10082, 4194, 6554},
+                                 {9362, 3647, 5825},  {8192, 3355, 5243},  {7282, 2893, 4559}};
+    if (pos < 0 || pos > 15 || qp < 0 || qp > 51) return 0;
+    int qe = qp / 6;
+    int f = intra ? (1 << (15 + qe)) / 3 : (1 << (15 + qe)) / 6;
+    int m = mf[qp % 6][pos_class(pos)];
+    int x = (int)val;
+    return x < 0 ? (int)(short)(-(((-x) * m + f) >> (15 + qe))) : (int)(short)((x * m + f) >> (15 + qe));
+}
+
+}  // extern "C"

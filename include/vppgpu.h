@@ -1,0 +1,224 @@
+/*
+ * vppgpu.h -- C ABI of the GB300 (sm_103a) encoder hot path for vpp
+ * (CSIR-RTVC/ImageCodingUtils).
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes and returns
+ * an int status (VPPGPU_OK = 0, negative on error); nothing throws across the
+ * boundary.  Host-pointer entry points are synchronous: they copy inputs to
+ * the device, run the kernels on the context's stream and copy results back.
+ * `_device` entry points take device pointers, only enqueue work on the
+ * context's stream and return at once.
+ *
+ * The interfaces each call replaces are cited per declaration (paths inside
+ * the vpp source tree).  Pixel planes are `short` (vpp's yuvType and
+ * OverlayMem2Dv2 element type) holding 0..255 luma; motion vectors are
+ * quarter-pel {short x, short y} pairs per 16x16 macroblock in raster order,
+ * the VectorStructList SIMPLE2D layout (include/CodecUtils/VectorStructList.h:56-60).
+ *
+ * Thread safety: one handle per host thread, as for the vpp classes
+ * (single-threaded, non-reentrant per object).
+ */
+#ifndef VPPGPU_H
+#define VPPGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define VPPGPU_OK                 0
+#define VPPGPU_ERR_INVALID_ARG   -1  /* null pointer, bad size or mode            */
+#define VPPGPU_ERR_CUDA          -2  /* a CUDA runtime call failed                */
+#define VPPGPU_ERR_OUT_OF_MEMORY -3  /* device or pinned allocation failed        */
+#define VPPGPU_ERR_PIXEL_RANGE   -4  /* a luma sample outside 0..255              */
+#define VPPGPU_ERR_TIMEOUT       -5  /* a bounded device-side wait gave up        */
+#define VPPGPU_ERR_UNSUPPORTED   -6  /* configuration outside the supported set   */
+#define VPPGPU_ERR_NOT_READY     -7  /* handle not created / creation failed      */
+#define VPPGPU_ERR_NO_DEVICE     -8  /* no CUDA device, or not an sm_103 part     */
+
+/* Human-readable name of a status code (static storage). */
+const char* vppgpu_status_string(int status);
+
+/* ---- context ------------------------------------------------------------ */
+/* A context binds one CUDA device and one stream.  No vpp counterpart: the
+ * vpp classes run on the calling thread; the context is where their GPU
+ * replacements enqueue work. */
+typedef struct vppgpu_ctx vppgpu_ctx;
+
+int vppgpu_ctx_create(int device, vppgpu_ctx** out);
+int vppgpu_ctx_destroy(vppgpu_ctx* ctx);
+/* Use a caller-owned cudaStream_t (passed as void*) instead of the context's
+ * own stream; NULL restores the context's stream. */
+int vppgpu_ctx_set_stream(vppgpu_ctx* ctx, void* cuda_stream);
+int vppgpu_ctx_get_stream(vppgpu_ctx* ctx, void** cuda_stream);
+int vppgpu_ctx_synchronize(vppgpu_ctx* ctx);
+/* Number of kernels this context has launched so far. */
+int vppgpu_ctx_launch_count(vppgpu_ctx* ctx, unsigned long long* count);
+
+/* ---- motion estimation -------------------------------------------------- */
+/* Estimator kinds: the IMotionEstimator implementations replaced. */
+#define VPPGPU_ME_FULL              0  /* MotionEstimatorH264ImplFull              */
+#define VPPGPU_ME_MULTIRES          1  /* MotionEstimatorH264ImplMultires          */
+#define VPPGPU_ME_MULTIRES_CROSS    2  /* MotionEstimatorH264ImplMultiresCross     */
+#define VPPGPU_ME_MULTIRES_CROSS_V2 3  /* MotionEstimatorH264ImplMultiresCrossVer2 */
+
+typedef struct vppgpu_me vppgpu_me;
+
+/* Constructor + Create() of the estimator (src/CodecUtils/MotionEstimatorH264ImplFull.cpp:132-153,
+ * 216-320; same shape for the other kinds): allocates all device state for a
+ * width x height luma frame and a quarter-pel motion range.  width must be a
+ * multiple of 16; a partial bottom macroblock row (height % 16 != 0) is not
+ * reported, as in the reference (Full.cpp:293, 594).  Supported ranges:
+ * 4 <= motion_range <= 128 (search of at most +-31 pels). */
+int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motion_range,
+                     vppgpu_me** out);
+int vppgpu_me_destroy(vppgpu_me* me);
+/* IMotionEstimator::SetMode / GetMode (include/CodecUtils/IMotionEstimator.h:80-81). */
+int vppgpu_me_set_mode(vppgpu_me* me, int mode);
+int vppgpu_me_get_mode(vppgpu_me* me, int* mode);
+/* Number of vectors an estimate produces: (width/16)*(height/16). */
+int vppgpu_me_num_mbs(vppgpu_me* me, int* n);
+
+/* IMotionEstimator::Estimate(long* avgDistortion) (IMotionEstimator.h:90-93;
+ * MotionEstimatorH264ImplFull::Estimate, Full.cpp:330-613), host buffers.
+ *   src, ref       width*height shorts, luma 0..255 (else VPPGPU_ERR_PIXEL_RANGE)
+ *   dist_included  NULL or one flag per macroblock: the reference's
+ *                  pDistortionIncluded constructor argument
+ *   mb_slice       NULL (one slice) or one slice id per macroblock: the
+ *                  neighbourhood MacroBlockH264::Initialise wires for the
+ *                  median predictor (src/CodecUtils/MacroBlockH264.cpp:319-)
+ *   mv_out         2 shorts per macroblock (the VectorStructList contents)
+ *   mb_dist_out    NULL or one int per macroblock: distortion of the chosen vector
+ *   avg_distortion NULL or the avgDistortion out-parameter
+ * The caller then applies mv_out to its IMotionVectorPredictor with
+ * Set16x16MotionVector(k, x, y) for every k, the side effect the reference has
+ * (include/CodecUtils/H264MotionVectorPredictorImpl1.h:103-111). */
+int vppgpu_me_estimate(vppgpu_me* me, const short* src, const short* ref,
+                       const unsigned char* dist_included, const int* mb_slice,
+                       short* mv_out, int* mb_dist_out, long* avg_distortion);
+
+/* Same with device pointers; enqueued on the context stream.  avg_out is a
+ * device long long. */
+int vppgpu_me_estimate_device(vppgpu_me* me, const short* d_src, const short* d_ref,
+                              const unsigned char* d_dist_included, const int* d_mb_slice,
+                              short* d_mv_out, int* d_mb_dist_out, long long* d_avg_out);
+
+/* IMotionEstimator::Estimate(long*, void* param) with a Lagrange multiplier
+ * (MotionEstimatorH264ImplMultiresCrossVer2.cpp:1162-). */
+int vppgpu_me_estimate_lambda(vppgpu_me* me, const short* src, const short* ref,
+                              const unsigned char* dist_included, const int* mb_slice,
+                              double lambda, short* mv_out, int* mb_dist_out,
+                              long* avg_distortion);
+
+/* Status of the last device-side estimate (pixel-range or timeout flags);
+ * synchronises the context stream. */
+int vppgpu_me_last_status(vppgpu_me* me);
+
+/* Number of resolve sweeps the last estimate needed (predictor fixed point). */
+int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps);
+
+/* Observability, no vpp counterpart.  While enabled, every estimate records
+ * CUDA events around its three kernels on the context stream (no host
+ * synchronisation); vppgpu_me_timing synchronises and returns how many
+ * estimates were timed and the summed milliseconds of the pack, search and
+ * resolve kernels.  Enabling resets the sums. */
+int vppgpu_me_set_timing(vppgpu_me* me, int enable);
+int vppgpu_me_timing(vppgpu_me* me, int* n, double* pack_ms, double* search_ms, double* resolve_ms);
+
+/* Measured dp4a issue rate of the whole device (instructions per second),
+ * the integer-ALU roofline of the motion search.  No vpp counterpart. */
+int vppgpu_calibrate_dp4a(vppgpu_ctx* ctx, double* dp4a_per_second);
+
+/* ---- 4x4 integer transform + H.264 quantisation ------------------------- */
+/* Modes (include/CodecUtils/IForwardTransform.h:119-125). */
+#define VPPGPU_TQ_TRANSFORM_AND_QUANT 0
+#define VPPGPU_TQ_TRANSFORM_ONLY      1
+#define VPPGPU_TQ_QUANT_ONLY          2
+/* Data layouts. */
+#define VPPGPU_LAYOUT_BLOCKS 0  /* contiguous 16-short 4x4 blocks: FastForward4x4ITImpl1/2,
+                                   FastInverse4x4ITImpl1 (one Transform(void*) per block) */
+#define VPPGPU_LAYOUT_MB16   1  /* 256-short 16x16 raster macroblocks:
+                                   FastForward4x4On16x16ITImpl1 / FastInverse4x4On16x16ITImpl1 */
+/* Inverse pass order: rows first (FastInverse4x4ITImpl1) or columns first
+ * (FastInverse4x4On16x16ITImpl1); the int16 stores between the passes make
+ * the two differ. */
+#define VPPGPU_INV_ROWS_FIRST 0
+#define VPPGPU_INV_COLS_FIRST 1
+
+/* IForwardTransform::Transform(void*) over nunits units in place
+ * (src/CodecUtils/FastForward4x4ITImpl1.cpp:100-201; On16x16: FastForward4x4On16x16ITImpl1.cpp:457-757),
+ * with SetMode(mode), SetParameter(QUANT_ID, qp), SetParameter(INTRA_FLAG_ID, intra). */
+int vppgpu_fwd4x4(vppgpu_ctx* ctx, short* data, long long nunits, int layout, int mode, int qp,
+                  int intra);
+int vppgpu_fwd4x4_device(vppgpu_ctx* ctx, short* d_data, long long nunits, int layout, int mode,
+                         int qp, int intra);
+
+/* IInverseTransform::InverseTransform(void*) over nunits units in place
+ * (src/CodecUtils/FastInverse4x4ITImpl1.cpp:119-244; On16x16: FastInverse4x4On16x16ITImpl1.cpp:120-361).
+ * weight16: NULL (flat 16) or the SetScale() array of 16 ints (FastInverse4x4ITImpl1.cpp:251-268).
+ * The blocks layout runs rows first, the mb16 layout columns first. */
+int vppgpu_inv4x4(vppgpu_ctx* ctx, short* data, long long nunits, int layout, int mode, int qp,
+                  const int* weight16);
+int vppgpu_inv4x4_device(vppgpu_ctx* ctx, short* d_data, long long nunits, int layout, int mode,
+                         int qp, const int* weight16);
+
+/* Fused residual round trip over a raster plane (width, height multiples of
+ * 4, row stride in shorts): every 4x4 block goes through forward transform +
+ * quantisation (mode 0), the levels are written to `levels`, then through
+ * dequantisation + inverse transform (mode 0, `inv_order`), written to
+ * `recon`.  This is BlockH264::ForwardTransform/Quantise followed by
+ * InverseQuantise/InverseTransform (src/CodecUtils/BlockH264.cpp:136-196)
+ * for a whole plane in one pass. */
+int vppgpu_tq_roundtrip_plane(vppgpu_ctx* ctx, const short* residual, short* levels, short* recon,
+                              int width, int height, int stride, int qp, int intra,
+                              int inv_order, const int* weight16);
+int vppgpu_tq_roundtrip_plane_device(vppgpu_ctx* ctx, const short* d_residual, short* d_levels,
+                                     short* d_recon, int width, int height, int stride, int qp,
+                                     int intra, int inv_order, const int* weight16);
+
+/* One plane of a batched round trip. */
+typedef struct vppgpu_tq_job {
+    const short* residual; /* device */
+    short* levels;         /* device */
+    short* recon;          /* device */
+    int width, height, stride;
+    int qp, intra;
+} vppgpu_tq_job;
+
+/* Many planes (e.g. the Y, U, V planes of many frames, each at its own QP and
+ * intra/inter rounding) in one launch; `d_jobs` is a device array of njobs
+ * descriptors. */
+int vppgpu_tq_roundtrip_planes_device(vppgpu_ctx* ctx, const vppgpu_tq_job* d_jobs, int njobs, int inv_order,
+                                      const int* weight16);
+
+/* FastForward4x4ITImpl2::QuantiseValue (src/CodecUtils/FastForward4x4ITImpl2.cpp:640-683),
+ * host-side scalar helper kept for API completeness. */
+int vppgpu_quantise_value(short val, int pos, int qp, int intra);
+
+/* ---- RGB24 -> YUV420 ----------------------------------------------------- */
+#define VPPGPU_RGB_FIXED_POINT 0  /* FastFixedPointRGB24toYUV420Converter  */
+#define VPPGPU_RGB_REAL        1  /* RealRGB24toYUV420Converter            */
+#define VPPGPU_RGB_REAL_IMPL2  2  /* RealRGB24toYUV420ConverterImpl2       */
+
+/* RGBtoYUV420Converter::Convert(pRgb, pY, pU, pV) (include/ImageUtils/RGBtoYUV420Converter.h:57-86;
+ * src/ImageUtils/FastFixedPointRGB24toYUV420Converter.cpp:94-169,
+ * src/ImageUtils/RealRGB24toYUV420Converter.cpp:83-242): packed B,G,R bytes in,
+ * planar shorts out (Y width*height, U and V (width/2)*(height/2)).  flip
+ * reads the source bottom-up (Real converters; the fixed-point one ignores
+ * it, as in the reference). */
+int vppgpu_rgb24_to_yuv420(vppgpu_ctx* ctx, int kind, const unsigned char* bgr, int width,
+                           int height, int chr_off, int flip, short* y, short* u, short* v);
+int vppgpu_rgb24_to_yuv420_device(vppgpu_ctx* ctx, int kind, const unsigned char* d_bgr, int width,
+                                  int height, int chr_off, int flip, short* d_y, short* d_u,
+                                  short* d_v);
+
+/* nframes frames stored back to back (BGR, Y, U, V each contiguous per frame)
+ * converted in one launch. */
+int vppgpu_rgb24_to_yuv420_frames_device(vppgpu_ctx* ctx, int kind, const unsigned char* d_bgr, int nframes,
+                                         int width, int height, int chr_off, int flip, short* d_y, short* d_u,
+                                         short* d_v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VPPGPU_H */

@@ -127,40 +127,62 @@ static void full_range(int x, int y, int w, int h, int motion_range, int range,
 /* Sub-pel window                                                            */
 /* ------------------------------------------------------------------------ */
 /* LoadHalfQuartPelWindow / LoadQuartPelWindow / QuarterRead of the window
- * (Full.cpp:1095-1255), restated as sample functions.  Coordinates are in
- * quarter pels relative to the best full-pel block origin (ox, oy) of the
- * extended reference.  Even positions hold G (full), h (vertical half),
- * b (horizontal half) and j (centre half) samples; odd positions around the
- * winning half-pel point are rounded averages of two even neighbours. */
+ * (Full.cpp:1095-1255), restated with explicit sample planes.  Coordinates
+ * are in quarter pels relative to the best full-pel block origin (ox, oy) of
+ * the extended reference.  Even positions hold G (full), h (vertical half),
+ * b (horizontal half) and j (centre half) samples, computed once per
+ * macroblock as the reference's window is; odd positions around the winning
+ * half-pel point are rounded averages of two even neighbours. */
+typedef struct {
+    const short* e;
+    int es, ox, oy;
+    short h[17][18]; /* fy in [-1,15], fx in [-1,16] */
+    short b[18][17]; /* fy in [-1,16], fx in [-1,15] */
+    short j[17][17]; /* fy,fx in [-1,15] */
+} subpel_win;
+
+static void win_load(subpel_win* w, const short* e, int es, int ox, int oy)
+{
+    w->e = e;
+    w->es = es;
+    w->ox = ox;
+    w->oy = oy;
+    for (int fy = -1; fy <= 15; fy++)
+        for (int fx = -1; fx <= 16; fx++) w->h[fy + 1][fx + 1] = (short)vo_hp_h(e, es, ox + fx, oy + fy);
+    for (int fy = -1; fy <= 16; fy++)
+        for (int fx = -1; fx <= 15; fx++) w->b[fy + 1][fx + 1] = (short)vo_hp_b(e, es, ox + fx, oy + fy);
+    for (int fy = -1; fy <= 15; fy++)
+        for (int fx = -1; fx <= 15; fx++) w->j[fy + 1][fx + 1] = (short)vo_hp_j(e, es, ox + fx, oy + fy);
+}
+
 static int floordiv4(int v) { return v >= 0 ? v / 4 : -((-v + 3) / 4); }
 
-static int win_even(const short* e, int es, int ox, int oy, int qy, int qx)
+static int win_even(const subpel_win* w, int qy, int qx)
 {
     int fy = floordiv4(qy), fx = floordiv4(qx);
     int ry = qy - 4 * fy, rx = qx - 4 * fx;
-    int x = ox + fx, y = oy + fy;
-    if (ry == 0 && rx == 0) return e[(size_t)y * es + x];
-    if (ry == 2 && rx == 0) return vo_hp_h(e, es, x, y);
-    if (ry == 0 && rx == 2) return vo_hp_b(e, es, x, y);
-    return vo_hp_j(e, es, x, y);
+    if (ry == 0 && rx == 0) return w->e[(size_t)(w->oy + fy) * w->es + w->ox + fx];
+    if (ry == 2 && rx == 0) return w->h[fy + 1][fx + 1];
+    if (ry == 0 && rx == 2) return w->b[fy + 1][fx + 1];
+    return w->j[fy + 1][fx + 1];
 }
 
 /* Quarter sample at offset (sy, sx) in -1..1 around the even point (cy, cx),
  * following the eight assignments of LoadQuartPelWindow (Full.cpp:1207-1220). */
-static int win_quarter(const short* e, int es, int ox, int oy, int cy, int cx, int sy, int sx)
+static int win_quarter(const subpel_win* w, int cy, int cx, int sy, int sx)
 {
     int a, b;
     if (sy < 0) {
-        if (sx < 0) { a = win_even(e, es, ox, oy, cy - 2, cx - 2); b = win_even(e, es, ox, oy, cy, cx); }
-        else if (sx == 0) { a = win_even(e, es, ox, oy, cy - 2, cx); b = win_even(e, es, ox, oy, cy, cx); }
-        else { a = win_even(e, es, ox, oy, cy - 2, cx); b = win_even(e, es, ox, oy, cy, cx + 2); }
+        if (sx < 0) { a = win_even(w, cy - 2, cx - 2); b = win_even(w, cy, cx); }
+        else if (sx == 0) { a = win_even(w, cy - 2, cx); b = win_even(w, cy, cx); }
+        else { a = win_even(w, cy - 2, cx); b = win_even(w, cy, cx + 2); }
     } else if (sy == 0) {
-        if (sx < 0) { a = win_even(e, es, ox, oy, cy, cx - 2); b = win_even(e, es, ox, oy, cy, cx); }
-        else { a = win_even(e, es, ox, oy, cy, cx + 2); b = win_even(e, es, ox, oy, cy, cx); }
+        if (sx < 0) { a = win_even(w, cy, cx - 2); b = win_even(w, cy, cx); }
+        else { a = win_even(w, cy, cx + 2); b = win_even(w, cy, cx); }
     } else {
-        if (sx < 0) { a = win_even(e, es, ox, oy, cy, cx - 2); b = win_even(e, es, ox, oy, cy + 2, cx); }
-        else if (sx == 0) { a = win_even(e, es, ox, oy, cy + 2, cx); b = win_even(e, es, ox, oy, cy, cx); }
-        else { a = win_even(e, es, ox, oy, cy + 2, cx); b = win_even(e, es, ox, oy, cy, cx + 2); }
+        if (sx < 0) { a = win_even(w, cy, cx - 2); b = win_even(w, cy + 2, cx); }
+        else if (sx == 0) { a = win_even(w, cy + 2, cx); b = win_even(w, cy, cx); }
+        else { a = win_even(w, cy + 2, cx); b = win_even(w, cy, cx + 2); }
     }
     return (a + b + 1) >> 1;
 }
@@ -175,13 +197,15 @@ static const int SUB_Y[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
 static void subpel_refine(const short* in, int ins, const short* e, int es, int ox, int oy,
                           int* min_d, int* qmx, int* qmy)
 {
+    subpel_win w;
+    win_load(&w, e, es, ox, oy);
     short blk[256];
     int hmx = 0, hmy = 0, best = *min_d;
     for (int k = 0; k < 8; k++) {
         int qx = 2 * SUB_X[k], qy = 2 * SUB_Y[k];
         for (int r = 0; r < 16; r++)
             for (int c = 0; c < 16; c++)
-                blk[r * 16 + c] = (short)win_even(e, es, ox, oy, 4 * r + qy, 4 * c + qx);
+                blk[r * 16 + c] = (short)win_even(&w, 4 * r + qy, 4 * c + qx);
         int d = vo_tsd16_lt(in, ins, blk, 16, best);
         if (d < best) { best = d; hmx = qx; hmy = qy; }
     }
@@ -189,7 +213,7 @@ static void subpel_refine(const short* in, int ins, const short* e, int es, int 
     for (int k = 0; k < 8; k++) {
         for (int r = 0; r < 16; r++)
             for (int c = 0; c < 16; c++)
-                blk[r * 16 + c] = (short)win_quarter(e, es, ox, oy, 4 * r + hmy, 4 * c + hmx, SUB_Y[k], SUB_X[k]);
+                blk[r * 16 + c] = (short)win_quarter(&w, 4 * r + hmy, 4 * c + hmx, SUB_Y[k], SUB_X[k]);
         int d = vo_tsd16_lt(in, ins, blk, 16, best);
         if (d < best) { best = d; bx = hmx + SUB_X[k]; by = hmy + SUB_Y[k]; }
     }

@@ -1,0 +1,125 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs the reference's own C++ classes (compiled unmodified from its sources by
+``make -C oracle ref`` into oracle/_ref/libvppref.so) on seeded synthetic
+inputs and stores inputs and outputs:
+
+* me_full.npz     MotionEstimatorH264ImplFull vectors and avgDistortion for
+                  QCIF / CIF / partial-row pairs at motion ranges 64 and 128,
+                  plus per-macroblock distortions for one QCIF pair (one
+                  estimate per macroblock with a single pDistortionIncluded flag)
+* transform.npz   FastForward4x4ITImpl1 / Impl2 / On16x16 levels and
+                  FastInverse4x4ITImpl1 / On16x16 reconstructions over QP 0..51,
+                  intra and inter, modes 0/1/2, a custom SetScale, and
+                  FastForward4x4ITImpl2::QuantiseValue
+* colour.npz      the three RGB24->YUV420 converters, flip and chroma offsets
+
+Usage: python tests/golden/make_golden.py   (needs the reference tree)
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from imagecodingutils_gb300 import synth  # noqa: E402
+from oracle import oracle  # noqa: E402
+
+ME_CASES = [  # (name, w, h, motion_range, seed)
+    ("qcif_r64", 176, 144, 64, 1),
+    ("qcif_r128", 176, 144, 128, 3),
+    ("cif_r128", 352, 288, 128, 2),
+    ("partial_r128", 176, 152, 128, 4),
+    ("shift_r64", 176, 144, 64, 5),
+]
+
+
+def me_fixtures(ref: oracle.Reference) -> dict:
+    out = {}
+    for name, w, h, mr, seed in ME_CASES:
+        if name.startswith("shift"):
+            fr = synth.shift_sequence(seed, w, h, 2)
+        else:
+            fr = synth.pan_sequence(seed, w, h, 2)
+        src, rf = fr[1], fr[0]
+        nmb = (w // 16) * (h // 16)
+        incl = np.ones(nmb, np.uint8)
+        mv, avg = ref.me("full", src, rf, mr, dist_incl=incl)
+        mv0, avg0 = ref.me("full", src, rf, mr)
+        assert np.array_equal(mv, mv0) and avg0 == 0
+        out[f"{name}_src"] = src.astype(np.uint8)
+        out[f"{name}_ref"] = rf.astype(np.uint8)
+        out[f"{name}_meta"] = np.array([w, h, mr], np.int32)
+        out[f"{name}_mv"] = mv
+        out[f"{name}_avg"] = np.array([avg], np.int64)
+        if name == "qcif_r64":
+            d = np.zeros(nmb, np.int64)
+            for k in range(nmb):
+                one = np.zeros(nmb, np.uint8)
+                one[k] = 1
+                _, d[k] = ref.me("full", src, rf, mr, dist_incl=one)
+            out[f"{name}_mbdist"] = d
+    return out
+
+
+def transform_fixtures(ref: oracle.Reference) -> dict:
+    lap = synth.residual_blocks(11, 16 * 64)
+    full = ((synth.splitmix64(12, 16 * 16) % np.uint64(65536)).astype(np.int64) - 32768).astype(np.int16)
+    x = np.concatenate([lap, full])
+    out = {"x": x}
+    weight = (np.arange(16, dtype=np.int32) * 3 + 7)
+    out["weight"] = weight
+    for qp in range(52):
+        for intra in (0, 1):
+            lev = ref.fwd(0, x, 0, qp, intra)
+            assert np.array_equal(lev, ref.fwd(1, x, 0, qp, intra))
+            out[f"fwd_q{qp}_i{intra}"] = lev
+            out[f"fwd16_q{qp}_i{intra}"] = ref.fwd(2, x, 0, qp, intra)
+        lev = out[f"fwd_q{qp}_i1"]
+        out[f"inv_q{qp}"] = ref.inv(0, lev, 0, qp)
+        out[f"inv16_q{qp}"] = ref.inv(1, lev, 0, qp)
+    for qp in (0, 11, 23, 24, 28, 51):
+        for mode in (1, 2):
+            out[f"fwd_m{mode}_q{qp}"] = ref.fwd(0, x, mode, qp, 1)
+            out[f"inv_m{mode}_q{qp}"] = ref.inv(0, x, mode, qp)
+            out[f"inv16_m{mode}_q{qp}"] = ref.inv(1, x, mode, qp)
+        out[f"invw_q{qp}"] = ref.inv(0, out[f"fwd_q{qp}_i0"], 0, qp, weight)
+    qv = []
+    for qp in (0, 7, 28, 51):
+        for pos in range(16):
+            for val in (-32768, -300, -1, 0, 1, 255, 1000, 32767):
+                for intra in (0, 1):
+                    qv.append((val, pos, qp, intra, ref.quantise_value(val, pos, qp, intra)))
+    out["quantise_value"] = np.array(qv, np.int32)
+    return out
+
+
+def colour_fixtures(ref: oracle.Reference) -> dict:
+    bgr = synth.rgb_frame(21, 64, 48)
+    out = {"bgr": bgr}
+    for kind in (0, 1, 2):
+        for flip in (0, 1):
+            for co in (0, 128):
+                y, u, v = ref.rgb_to_yuv(kind, bgr, co, flip)
+                out[f"k{kind}_f{flip}_c{co}_y"] = y
+                out[f"k{kind}_f{flip}_c{co}_u"] = u
+                out[f"k{kind}_f{flip}_c{co}_v"] = v
+    return out
+
+
+def main() -> None:
+    oracle.build(with_reference=True)
+    ref = oracle.Reference()
+    np.savez_compressed(os.path.join(HERE, "me_full.npz"), **me_fixtures(ref))
+    np.savez_compressed(os.path.join(HERE, "transform.npz"), **transform_fixtures(ref))
+    np.savez_compressed(os.path.join(HERE, "colour.npz"), **colour_fixtures(ref))
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

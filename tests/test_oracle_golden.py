@@ -1,0 +1,103 @@
+"""The CPU oracle against the golden fixtures produced by the reference itself
+(tests/golden/make_golden.py), and -- where oracle/_ref was built -- against
+the compiled reference on further seeded cases."""
+import numpy as np
+import pytest
+
+from imagecodingutils_gb300 import synth
+from oracle import oracle as oracle_mod
+
+ME_CASES = ["qcif_r64", "qcif_r128", "cif_r128", "partial_r128", "shift_r64"]
+
+
+@pytest.mark.parametrize("case", ME_CASES)
+def test_me_full_matches_reference_vectors(orc, golden, case):
+    g = golden("me_full.npz")
+    w, h, mr = (int(v) for v in g[f"{case}_meta"])
+    src = g[f"{case}_src"].astype(np.int16)
+    ref = g[f"{case}_ref"].astype(np.int16)
+    incl = np.ones((w // 16) * (h // 16), np.uint8)
+    mv, dist, avg = orc.me_full(src, ref, mr, dist_incl=incl)
+    np.testing.assert_array_equal(mv, g[f"{case}_mv"])
+    assert avg == int(g[f"{case}_avg"][0])
+    # without pDistortionIncluded the reference reports 0
+    mv2, _, avg2 = orc.me_full(src, ref, mr)
+    np.testing.assert_array_equal(mv2, mv)
+    assert avg2 == 0
+
+
+def test_me_full_matches_reference_per_mb_distortion(orc, golden):
+    g = golden("me_full.npz")
+    src = g["qcif_r64_src"].astype(np.int16)
+    ref = g["qcif_r64_ref"].astype(np.int16)
+    _, dist, _ = orc.me_full(src, ref, 64, dist_incl=np.ones(99, np.uint8))
+    np.testing.assert_array_equal(dist, g["qcif_r64_mbdist"])
+
+
+def test_transform_matches_reference(orc, golden):
+    g = golden("transform.npz")
+    x = g["x"]
+    for qp in range(52):
+        for intra in (0, 1):
+            np.testing.assert_array_equal(orc.fwd4x4(x, 0, 0, qp, intra), g[f"fwd_q{qp}_i{intra}"])
+            np.testing.assert_array_equal(orc.fwd4x4(x, 1, 0, qp, intra), g[f"fwd16_q{qp}_i{intra}"])
+        lev = g[f"fwd_q{qp}_i1"]
+        np.testing.assert_array_equal(orc.inv4x4(lev, 0, 0, qp), g[f"inv_q{qp}"])
+        np.testing.assert_array_equal(orc.inv4x4(lev, 1, 0, qp), g[f"inv16_q{qp}"])
+    for qp in (0, 11, 23, 24, 28, 51):
+        for mode in (1, 2):
+            np.testing.assert_array_equal(orc.fwd4x4(x, 0, mode, qp, 1), g[f"fwd_m{mode}_q{qp}"])
+            np.testing.assert_array_equal(orc.inv4x4(x, 0, mode, qp), g[f"inv_m{mode}_q{qp}"])
+            np.testing.assert_array_equal(orc.inv4x4(x, 1, mode, qp), g[f"inv16_m{mode}_q{qp}"])
+        np.testing.assert_array_equal(orc.inv4x4(g[f"fwd_q{qp}_i0"], 0, 0, qp, g["weight"]), g[f"invw_q{qp}"])
+    for val, pos, qp, intra, want in g["quantise_value"]:
+        assert orc.quantise_value(int(val), int(pos), int(qp), int(intra)) == want
+
+
+def test_colour_matches_reference(orc, golden):
+    g = golden("colour.npz")
+    for kind in (0, 1, 2):
+        for flip in (0, 1):
+            for co in (0, 128):
+                y, u, v = orc.rgb_to_yuv(kind, g["bgr"], co, flip)
+                np.testing.assert_array_equal(y, g[f"k{kind}_f{flip}_c{co}_y"])
+                np.testing.assert_array_equal(u, g[f"k{kind}_f{flip}_c{co}_u"])
+                np.testing.assert_array_equal(v, g[f"k{kind}_f{flip}_c{co}_v"])
+
+
+def test_inverse_pass_orders_differ(orc):
+    """The two inverse classes round differently (int16 stores between passes
+    in a different order), so both must be reproduced."""
+    x = synth.residual_blocks(99, 16 * 256)
+    lev = orc.fwd4x4(x, 0, 0, 4, 1)
+    assert not np.array_equal(orc.inv4x4(lev, 0, 0, 4), orc.inv4x4(lev, 1, 0, 4))
+
+
+ref_available = pytest.mark.skipif(not oracle_mod.Reference.available(), reason="reference not built here")
+
+
+@ref_available
+@pytest.mark.parametrize("seed,w,h,mr", [(31, 64, 48, 128), (32, 80, 64, 64), (33, 48, 40, 40), (34, 32, 32, 128)])
+def test_me_full_against_compiled_reference(orc, seed, w, h, mr):
+    ref_lib = oracle_mod.Reference()
+    fr = synth.pan_sequence(seed, w, h, 2)
+    incl = (synth.splitmix64(seed, (w // 16) * (h // 16)) & np.uint64(1)).astype(np.uint8)
+    mv_r, avg_r = ref_lib.me("full", fr[1], fr[0], mr, dist_incl=incl)
+    mv_o, _, avg_o = orc.me_full(fr[1], fr[0], mr, dist_incl=incl)
+    np.testing.assert_array_equal(mv_o, mv_r)
+    assert avg_o == avg_r
+
+
+@ref_available
+def test_me_full_flat_content_ties(orc):
+    """Flat and periodic content makes many exact ties: the prediction-based
+    tie-break decides the vectors."""
+    ref_lib = oracle_mod.Reference()
+    w, h = 96, 64
+    yy, xx = np.mgrid[0:h, 0:w]
+    a = ((xx // 8 + yy // 8) % 2 * 40 + 100).astype(np.int16)
+    b = np.roll(a, (3, 5), axis=(0, 1))
+    b[20:40, 30:60] = 128
+    mv_r, _ = ref_lib.me("full", b, a, 128)
+    mv_o, _, _ = orc.me_full(b, a, 128)
+    np.testing.assert_array_equal(mv_o, mv_r)
