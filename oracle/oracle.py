@@ -50,6 +50,7 @@ class Oracle:
         L.vo_me_full.argtypes = [_P, _P, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L)]
         L.vo_me_full_detail.argtypes = [_P, _P, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L)] + [_P] * 6
         L.vo_me_full_intpel.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P]
+        L.vo_me_multires_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.vo_quarter_read16.argtypes = [_P, _I, _I, _I, _I, _I, _I, _P]
         L.vo_half.argtypes = [_P, _I, _I, _P]
         L.vo_fwd4x4.argtypes = [_P, _I, _I, _I, _I, _I]
@@ -83,6 +84,21 @@ class Oracle:
         if rc:
             raise ValueError(f"vo_me_full_detail rc={rc}")
         return mv, dist, avg.value, extra
+
+    def me_multires_cross(self, src, ref, motion_range, mode=1, dist_incl=None):
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = self.lib.vo_num_mbs(w, h)
+        mv = np.zeros((nmb, 2), np.int16)
+        dist = np.zeros(nmb, np.int32)
+        avg = _L(0)
+        incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
+        rc = self.lib.vo_me_multires_cross(_ptr(src), _ptr(ref), w, h, motion_range, mode, _ptr(incl),
+                                           _ptr(mv), _ptr(dist), C.byref(avg))
+        if rc:
+            raise ValueError(f"vo_me_multires_cross rc={rc}")
+        return mv, dist, avg.value
 
     def me_full_intpel(self, src, ref, motion_range, metric=1):
         h, w = src.shape

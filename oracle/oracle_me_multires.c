@@ -1,0 +1,432 @@
+/*
+ * oracle_me_multires.c -- TEST INFRASTRUCTURE ONLY (CPU oracle).
+ *
+ * Restatement of the multi-resolution H.264 estimators:
+ *   MotionEstimatorH264ImplMultiresCross::Estimate
+ *     (src/CodecUtils/MotionEstimatorH264ImplMultiresCross.cpp:525-1019)
+ *
+ * The reference works on extended-boundary copies of each pyramid level
+ * (borders 19 / 9 / 5 samples for levels 0 / 1 / 2), addresses them through
+ * row-pointer overlays whose origins are clamped (OverlayExtMem2Dv2::SetOrigin,
+ * src/ImageUtils/OverlayExtMem2Dv2.cpp:86-101) and reads beyond an overlay
+ * without checks.  The oracle keeps the same flat buffers and origin clamps
+ * and aborts (returns an error) if a read would leave a buffer, so that the
+ * restatement is exact wherever the reference itself is defined.
+ *
+ * The half-pel window of this estimator (…MultiresCross.cpp:1281-1349) does
+ * not write the full-pel samples of its last column and row, nor scale the
+ * last h column / b row (the full-search estimator does, Full.cpp:1162-1180).
+ * Those never-written samples are taken as 0, the content of the window
+ * buffer when its allocation is fresh zeroed memory; the unscaled edge
+ * samples are reproduced as they are.
+ */
+#include <stdlib.h>
+#include <string.h>
+#include "oracle_internal.h"
+
+typedef struct {
+    short* mem;
+    int w, h;
+} mr_buf;
+
+typedef struct {
+    const mr_buf* b;
+    int bw, bh;  /* block (overlay) dimensions */
+    int x, y;    /* origin in buffer coordinates */
+    int ebx, eby; /* extended border for OverlayExtMem2Dv2 origins (0 for plain overlays) */
+} mr_ov;
+
+static int g_mr_fault;
+
+static inline int mr_read(const mr_buf* b, int r, int c)
+{
+    long long f = (long long)r * b->w + c;
+    if (f < 0 || f >= (long long)b->w * b->h) {
+        g_mr_fault = 1;
+        return 0;
+    }
+    return b->mem[f];
+}
+
+/* OverlayMem2Dv2::SetOrigin / OverlayExtMem2Dv2::SetOrigin. */
+static void ov_origin(mr_ov* o, int x, int y)
+{
+    x += o->ebx;
+    y += o->eby;
+    if (x < 0) x = 0;
+    else if (x > o->b->w - o->bw) x = o->b->w - o->bw;
+    if (y < 0) y = 0;
+    else if (y > o->b->h - o->bh) y = o->b->h - o->bh;
+    o->x = x;
+    o->y = y;
+}
+
+static inline int ov_px(const mr_ov* o, int r, int c) { return mr_read(o->b, o->y + r, o->x + c); }
+
+/* Tsd4x4 / Tsd8x8 / Tsd16x16 (OverlayMem2Dv2.cpp:1523-1700). */
+static int ov_tsd(const mr_ov* a, const mr_ov* b, int n)
+{
+    int acc = 0;
+    for (int r = 0; r < n; r++)
+        for (int c = 0; c < n; c++) {
+            int d = ov_px(a, r, c) - ov_px(b, r, c);
+            acc += d * d;
+        }
+    return acc;
+}
+
+/* Tsd4x4LessThan (OverlayMem2Dv2.cpp:1739-1790). */
+static int ov_tsd4_lt(const mr_ov* a, const mr_ov* b, int min)
+{
+    int acc = 0;
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) {
+            int d = ov_px(a, r, c) - ov_px(b, r, c);
+            acc += d * d;
+            if (c < 3 && acc > min) return acc;
+        }
+    return acc;
+}
+
+/* Tsd8x8PartialLessThan / Tsd16x16PartialLessThan (OverlayMem2Dv2.cpp:1886-1913, 1993-2020). */
+static int ov_tsd_partial_lt(const mr_ov* a, const mr_ov* b, int n, int min)
+{
+    int dp = 0;
+    for (int p = 1; p <= 16; p++) {
+        int pd = 0;
+        for (int i = 0; i < n; i += 4)
+            for (int j = 0; j < n; j += 4) {
+                int d = ov_px(a, vo_phase_row[p] + i, vo_phase_col[p] + j) - ov_px(b, vo_phase_row[p] + i, vo_phase_col[p] + j);
+                pd += d * d;
+            }
+        dp += pd;
+        if ((dp << 4) > p * min) return dp << 4;
+    }
+    return dp;
+}
+
+/* Same partial test against a plain 16x16 block (the sub-pel candidates). */
+static int blk_tsd16_partial_lt(const mr_ov* a, const short* blk, int min)
+{
+    int dp = 0;
+    for (int p = 1; p <= 16; p++) {
+        int pd = 0;
+        for (int i = 0; i < 16; i += 4)
+            for (int j = 0; j < 16; j += 4) {
+                int r = vo_phase_row[p] + i, c = vo_phase_col[p] + j;
+                int d = ov_px(a, r, c) - blk[r * 16 + c];
+                pd += d * d;
+            }
+        dp += pd;
+        if ((dp << 4) > p * min) return dp << 4;
+    }
+    return dp;
+}
+
+static int mr_buf_ext(mr_buf* e, const short* plane, int w, int h, int border)
+{
+    e->w = w + 2 * border;
+    e->h = h + 2 * border;
+    e->mem = vo_ext_alloc(plane, w, h, border);
+    return e->mem ? 0 : -1;
+}
+
+/* Ranged GetMotionRange of the multi-resolution estimators
+ * (…MultiresCross.cpp:1195-1262): vector limits from vecRange of the level,
+ * then the block may reach `boundary` samples outside the level's picture. */
+typedef struct {
+    int boundary, width, height, vec_range;
+} mr_level;
+
+static void mr_range(const mr_level* L, int xpos, int ypos, int xoff, int yoff, int range,
+                     int* xl, int* xr, int* yu, int* yd)
+{
+    int x = xpos + xoff, y = ypos + yoff;
+    int vr = L->vec_range;
+    int xlr = (xoff - range > -vr) ? range : (vr - 1) + xoff;
+    int xrr = (xoff + range < vr) ? range : (vr - 1) - xoff;
+    int yur = (yoff - range > -vr) ? range : (vr - 1) + yoff;
+    int ydr = (yoff + range < vr) ? range : (vr - 1) - yoff;
+    *xl = (x - xlr >= -L->boundary) ? -xlr : -(x + L->boundary);
+    *xr = (x + xrr < L->width) ? xrr : L->width - x;
+    *yu = (y - yur >= -L->boundary) ? -yur : -(y + L->boundary);
+    *yd = (y + ydr < L->height) ? ydr : L->height - y;
+}
+
+/* ---- the 88x88 quarter-pel window ------------------------------------- */
+#define WIN 88
+typedef struct {
+    short w[WIN][WIN];
+} mr_window;
+
+static inline int clip255i(int x) { return x < 0 ? 0 : (x > 255 ? 255 : x); }
+
+/* MotionEstimatorH264ImplMultiresCross::LoadHalfQuartPelWindow (…:1281-1349):
+ * raw h over rows 2..18 x all 22 columns, raw b over all 22 rows x columns
+ * 2..18, j from the raw h, then h/b scaled and G copied over columns and rows
+ * 2..18 only. */
+static void mr_load_half_window(mr_window* W, const mr_ov* ref)
+{
+    const int rx = ref->x, ry = ref->y;
+    for (int fr = 2; fr < 19; fr++)
+        for (int fc = 0; fc < 22; fc++) {
+            int rr = ry + fr - 3, cc = rx + fc - 3;
+            int h = mr_read(ref->b, rr - 2, cc) - 5 * mr_read(ref->b, rr - 1, cc) + 20 * mr_read(ref->b, rr, cc) +
+                    20 * mr_read(ref->b, rr + 1, cc) - 5 * mr_read(ref->b, rr + 2, cc) + mr_read(ref->b, rr + 3, cc);
+            W->w[4 * fr + 2][4 * fc] = (short)h;
+        }
+    for (int fr = 0; fr < 22; fr++)
+        for (int fc = 2; fc < 19; fc++) {
+            int rr = ry + fr - 3, cc = rx + fc - 3;
+            int b = mr_read(ref->b, rr, cc - 2) - 5 * mr_read(ref->b, rr, cc - 1) + 20 * mr_read(ref->b, rr, cc) +
+                    20 * mr_read(ref->b, rr, cc + 1) - 5 * mr_read(ref->b, rr, cc + 2) + mr_read(ref->b, rr, cc + 3);
+            W->w[4 * fr][4 * fc + 2] = (short)b;
+        }
+    for (int fr = 2; fr < 19; fr++)
+        for (int fc = 2; fc < 19; fc++) {
+            int qr = 4 * fr + 2, qc = 4 * fc + 2;
+            int j = ((int)W->w[qr][qc - 10] - 5 * W->w[qr][qc - 6] + 20 * W->w[qr][qc - 2] + 20 * W->w[qr][qc + 2] -
+                     5 * W->w[qr][qc + 6] + W->w[qr][qc + 10] + 512) >> 10;
+            W->w[qr][qc] = (short)clip255i(j);
+        }
+    for (int fr = 2; fr < 19; fr++)
+        for (int fc = 2; fc < 19; fc++) {
+            int qr = 4 * fr, qc = 4 * fc;
+            W->w[qr + 2][qc] = (short)clip255i((W->w[qr + 2][qc] + 16) >> 5);
+            W->w[qr][qc + 2] = (short)clip255i((W->w[qr][qc + 2] + 16) >> 5);
+            W->w[qr][qc] = (short)mr_read(ref->b, ry + fr - 3, rx + fc - 3);
+        }
+}
+
+/* LoadQuartPelWindow (…MultiresCross.cpp:1365-1389): the eight quarter
+ * samples around every point of the winning half-pel grid. */
+static void mr_load_quarter_window(mr_window* W, int hx, int hy)
+{
+    for (int fr = 0; fr < 16; fr++)
+        for (int fc = 0; fc < 16; fc++) {
+            int qr = 12 + hy + 4 * fr, qc = 12 + hx + 4 * fc;
+            short (*w)[WIN] = W->w;
+            w[qr - 1][qc - 1] = (short)((w[qr - 2][qc - 2] + w[qr][qc] + 1) >> 1);
+            w[qr - 1][qc] = (short)((w[qr - 2][qc] + w[qr][qc] + 1) >> 1);
+            w[qr - 1][qc + 1] = (short)((w[qr - 2][qc] + w[qr][qc + 2] + 1) >> 1);
+            w[qr][qc - 1] = (short)((w[qr][qc - 2] + w[qr][qc] + 1) >> 1);
+            w[qr][qc + 1] = (short)((w[qr][qc + 2] + w[qr][qc] + 1) >> 1);
+            w[qr + 1][qc - 1] = (short)((w[qr][qc - 2] + w[qr + 2][qc] + 1) >> 1);
+            w[qr + 1][qc] = (short)((w[qr + 2][qc] + w[qr][qc] + 1) >> 1);
+            w[qr + 1][qc + 1] = (short)((w[qr + 2][qc] + w[qr][qc + 2] + 1) >> 1);
+        }
+}
+
+static void mr_window_read(const mr_window* W, int qx, int qy, short* blk)
+{
+    for (int r = 0; r < 16; r++)
+        for (int c = 0; c < 16; c++) blk[r * 16 + c] = W->w[12 + qy + 4 * r][12 + qx + 4 * c];
+}
+
+static const int SUBX[8] = {-1, 0, 1, -1, 1, -1, 0, 1};
+static const int SUBY[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+static const int CRX[4] = {-1, 1, 0, 0};
+static const int CRY[4] = {0, 0, -1, 1};
+
+#define MRC_NOISE_FLOOR 512
+
+/* ------------------------------------------------------------------------ */
+int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                         const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist)
+{
+    if (!src || !ref || !mv_out || w < 16 || h < 16 || (w % 16) != 0) return -1;
+    g_mr_fault = 0;
+    const int cols = w / 16, nmb = cols * (h / 16), rows_all = (h + 15) / 16;
+    const int w1 = w / 2, h1 = h / 2, w2 = w1 / 2, h2 = h1 / 2;
+    const int l1_range = motion_range / 8, l2_range = l1_range / 2;
+    if (mode == 0) mode = (w * h > 40000) ? 2 : 1; /* SetMode(0) (…:501-513) */
+    const int lcl_l1_range = (mode == 2) ? 2 : l1_range;
+
+    mr_buf in0 = {(short*)src, w, h}, in1 = {0}, in2 = {0}, r1 = {0}, r2 = {0}, e0 = {0}, e1 = {0}, e2 = {0};
+    in1.w = r1.w = w1; in1.h = r1.h = h1;
+    in2.w = r2.w = w2; in2.h = r2.h = h2;
+    in1.mem = (short*)malloc(sizeof(short) * (size_t)w1 * h1);
+    r1.mem = (short*)malloc(sizeof(short) * (size_t)w1 * h1);
+    in2.mem = (short*)malloc(sizeof(short) * (size_t)w2 * h2 + 2);
+    r2.mem = (short*)malloc(sizeof(short) * (size_t)w2 * h2 + 2);
+    mr_window* win = (mr_window*)calloc(1, sizeof(mr_window));
+    int rc = 0;
+    if (!in1.mem || !r1.mem || !in2.mem || !r2.mem || !win) { rc = -2; goto done; }
+    vo_half(ref, w, h, r1.mem);
+    vo_half(src, w, h, in1.mem);
+    if (mode == 2) {
+        vo_half(r1.mem, w1, h1, r2.mem);
+        vo_half(in1.mem, w1, h1, in2.mem);
+    }
+    if (mr_buf_ext(&e0, ref, w, h, 19) || mr_buf_ext(&e1, r1.mem, w1, h1, 9) ||
+        (mode == 2 && mr_buf_ext(&e2, r2.mem, w2, h2, 5))) { rc = -2; goto done; }
+
+    {
+        mr_level L0 = {16, w, h, motion_range / 4}, L1 = {8, w1, h1, l1_range}, L2 = {4, w2, h2, l2_range};
+        mr_ov oin0 = {&in0, 16, 16, 0, 0, 0, 0}, oin1 = {&in1, 8, 8, 0, 0, 0, 0}, oin2 = {&in2, 4, 4, 0, 0, 0, 0};
+        mr_ov oe0 = {&e0, 16, 16, 0, 0, 19, 19}, oe1 = {&e1, 8, 8, 0, 0, 9, 9}, oe2 = {&e2, 4, 4, 0, 0, 5, 5};
+        long total = 0;
+        int included = 0;
+        short blk[256];
+        for (int mbr = 0; mbr < rows_all; mbr++)
+            for (int mbc = 0; mbc < cols; mbc++) {
+                const int m = 16 * mbr, n = 16 * mbc, p = 8 * mbr, q = 8 * mbc, kk = 4 * mbr, ll = 4 * mbc;
+                const int vec_pos = mbr * cols + mbc < nmb ? mbr * cols + mbc : nmb;
+                int mx = 0, my = 0, rmx = 0, rmy = 0, hmx = 0, hmy = 0, qmx, qmy;
+                int xl, xr, yu, yd;
+                ov_origin(&oin0, n, m);
+                ov_origin(&oe0, n, m);
+                int zero_d = ov_tsd(&oin0, &oe0, 16);
+                int min_d = zero_d;
+
+                if (mode == 2) { /* level 2 cross search (…:639-697) */
+                    ov_origin(&oin2, ll, kk);
+                    ov_origin(&oe2, ll, kk);
+                    int min2 = ov_tsd(&oin2, &oe2, 4);
+                    for (int s = l2_range / 2; s > 0; s /= 2) {
+                        mr_range(&L2, ll, kk, 0, 0, l2_range - 1, &xl, &xr, &yu, &yd);
+                        rmx = rmy = 0;
+                        for (int c = 0; c < 4; c++) {
+                            int i = s * CRY[c], j = s * CRX[c];
+                            if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+                            ov_origin(&oe2, j + ll + mx, i + kk + my);
+                            int d = ov_tsd4_lt(&oin2, &oe2, min2);
+                            if (d > min2) continue;
+                            if (d == min2 && (my * my + mx * mx) - (i * i + j * j) < 0) continue;
+                            min2 = d;
+                            rmx = j;
+                            rmy = i;
+                        }
+                        mx += rmx;
+                        my += rmy;
+                    }
+                    mx <<= 1;
+                    my <<= 1;
+                }
+
+                /* level 1 (…:699-816) */
+                ov_origin(&oin1, q, p);
+                ov_origin(&oe1, mx + q, my + p);
+                int min1 = ov_tsd(&oin1, &oe1, 8);
+                rmx = rmy = 0;
+                if (mode == 2) {
+                    mr_range(&L1, q, p, mx, my, lcl_l1_range, &xl, &xr, &yu, &yd);
+                    for (int i = yu; i <= yd; i++)
+                        for (int j = xl; j <= xr; j++) {
+                            if (!(i || j)) continue;
+                            ov_origin(&oe1, j + mx + q, i + my + p);
+                            int d = ov_tsd_partial_lt(&oin1, &oe1, 8, min1);
+                            if (d > min1) continue;
+                            if (d == min1 && ((my + rmy) * (my + rmy) + (mx + rmx) * (mx + rmx)) -
+                                                     ((my + i) * (my + i) + (mx + j) * (mx + j)) < 0)
+                                continue;
+                            min1 = d;
+                            rmx = j;
+                            rmy = i;
+                        }
+                } else {
+                    for (int s = l1_range / 2; s > 0; s /= 2) {
+                        mr_range(&L1, q, p, mx, my, lcl_l1_range - 1, &xl, &xr, &yu, &yd);
+                        rmx = rmy = 0;
+                        for (int c = 0; c < 4; c++) {
+                            int i = s * CRY[c], j = s * CRX[c];
+                            if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+                            ov_origin(&oe1, j + mx + q, i + my + p);
+                            int d = ov_tsd_partial_lt(&oin1, &oe1, 8, min1);
+                            if (d > min1) continue;
+                            if (d == min1 && ((my + rmy) * (my + rmy) + (mx + rmx) * (mx + rmx)) -
+                                                     ((my + i) * (my + i) + (mx + j) * (mx + j)) < 0)
+                                continue;
+                            min1 = d;
+                            rmx = j;
+                            rmy = i;
+                        }
+                        mx += rmx;
+                        my += rmy;
+                    }
+                }
+                /* the last level-1 refinement is added once more here in the
+                 * cross mode (…:815-816) */
+                mx = (mx + rmx) * 2;
+                my = (my + rmy) * 2;
+
+                /* level 0 +-2 refinement (…:819-873) */
+                ov_origin(&oe0, n + mx, m + my);
+                min_d = ov_tsd(&oin0, &oe0, 16);
+                rmx = rmy = 0;
+                mr_range(&L0, n, m, mx, my, 2, &xl, &xr, &yu, &yd);
+                for (int i = yu; i <= yd; i++)
+                    for (int j = xl; j <= xr; j++) {
+                        if (!(i || j)) continue;
+                        ov_origin(&oe0, n + mx + j, m + my + i);
+                        int d = ov_tsd_partial_lt(&oin0, &oe0, 16, min_d);
+                        if (d > min_d) continue;
+                        if (d == min_d && ((my + rmy) * (my + rmy) + (mx + rmx) * (mx + rmx)) -
+                                                  ((my + i) * (my + i) + (mx + j) * (mx + j)) < 0)
+                            continue;
+                        min_d = d;
+                        rmx = j;
+                        rmy = i;
+                    }
+                mx += rmx;
+                my += rmy;
+                int mvx = mx << 2, mvy = my << 2;
+
+                /* half then quarter pel (…:875-941) */
+                ov_origin(&oe0, n + mx, m + my);
+                mr_load_half_window(win, &oe0);
+                for (int c = 0; c < 8; c++) {
+                    int qx = 2 * SUBX[c], qy = 2 * SUBY[c];
+                    mr_window_read(win, qx, qy, blk);
+                    int d = blk_tsd16_partial_lt(&oin0, blk, min_d);
+                    if (d < min_d) { min_d = d; hmx = qx; hmy = qy; }
+                }
+                qmx = hmx;
+                qmy = hmy;
+                mr_load_quarter_window(win, hmx, hmy);
+                for (int c = 0; c < 8; c++) {
+                    int qx = hmx + SUBX[c], qy = hmy + SUBY[c];
+                    mr_window_read(win, qx, qy, blk);
+                    int d = blk_tsd16_partial_lt(&oin0, blk, min_d);
+                    if (d < min_d) { min_d = d; qmx = qx; qmy = qy; }
+                }
+                mvx += qmx;
+                mvy += qmy;
+
+                /* accept-or-zero heuristic (…:943-999) */
+                int weight = 0, diff0 = zero_d - min_d, mag = mvx * mvx + mvy * mvy;
+                if (diff0 < mag) weight++;
+                if (zero_d < MRC_NOISE_FLOOR) weight++;
+                if (diff0 * 10 < min_d) weight++;
+                int do_it = dist_incl ? (vec_pos < nmb ? dist_incl[vec_pos] != 0 : 0) : 1;
+                int chosen;
+                if (min_d < zero_d && weight < 2) {
+                    chosen = min_d;
+                } else {
+                    mvx = mvy = 0;
+                    chosen = zero_d;
+                }
+                if (do_it) {
+                    included++;
+                    total += chosen;
+                }
+                if (vec_pos < nmb) {
+                    mv_out[2 * vec_pos] = (short)mvx;
+                    mv_out[2 * vec_pos + 1] = (short)mvy;
+                    if (mb_dist) mb_dist[vec_pos] = chosen;
+                }
+            }
+        if (avg_dist) *avg_dist = included ? total / included : 0;
+    }
+    if (g_mr_fault) rc = -3;
+done:
+    free(in1.mem);
+    free(r1.mem);
+    free(in2.mem);
+    free(r2.mem);
+    free(e0.mem);
+    free(e1.mem);
+    free(e2.mem);
+    free(win);
+    return rc;
+}

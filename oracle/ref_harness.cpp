@@ -7,6 +7,7 @@
  * restatement in oracle/*.c and to generate the golden fixtures; it contains
  * no algorithm of its own, only object set-up in the way a vpp codec does it.
  */
+#include <malloc.h>
 #include <math.h>
 #include <string.h>
 #include <stdlib.h>
@@ -93,14 +94,21 @@ int ref_me_estimate(int kind, const short* src, const short* ref, int w, int h, 
     H264MotionVectorPredictorImpl1 pred(grid.flat);
     bool* flags = make_flags(incl, nmb);
     IMotionEstimator* me = NULL;
+    /* The multi-resolution estimators read window samples they never write
+     * (see oracle_me_multires.c).  Allocations made while constructing and
+     * creating the estimator are zero-filled (glibc M_PERTURB with 0xff fills
+     * new allocations with 0x00), which pins those samples to 0. */
+    mallopt(M_PERTURB, 0xff);
     switch (kind) {
     case 0: me = new MotionEstimatorH264ImplFull(src, ref, w, h, motion_range, &pred, flags); break;
     case 1: me = new MotionEstimatorH264ImplMultires(src, ref, w, h, motion_range, &pred, flags); break;
     case 2: me = new MotionEstimatorH264ImplMultiresCross(src, ref, w, h, motion_range, flags); break;
     case 3: me = new MotionEstimatorH264ImplMultiresCrossVer2(src, ref, w, h, motion_range, &pred, flags); break;
-    default: delete[] flags; return -1;
+    default: mallopt(M_PERTURB, 0); delete[] flags; return -1;
     }
-    if (!me->Create()) { delete me; delete[] flags; return -2; }
+    int created = me->Create();
+    mallopt(M_PERTURB, 0);
+    if (!created) { delete me; delete[] flags; return -2; }
     me->SetMode(mode);
     long avg = 0;
     void* res = NULL;

@@ -66,6 +66,16 @@ int vo_me_full_detail(const short* src, const short* ref, int w, int h, int moti
 int vo_me_full_intpel(const short* src, const short* ref, int w, int h, int motion_range,
                       int metric, short* mv_out, int* mb_dist);
 
+/* MotionEstimatorH264ImplMultiresCross::Estimate
+ * (src/CodecUtils/MotionEstimatorH264ImplMultiresCross.cpp:525-1019): 3-level
+ * pyramid, cross search at the coarsest level, partial-distortion refinement,
+ * sub-pel window, accept-or-zero heuristic; no predictor.  mode 0 (auto),
+ * 1 or 2 as SetMode.  The partial bottom macroblock row is searched and,
+ * with dist_incl NULL, counted in the average, as in the reference.
+ * Returns -3 if the reference itself would read outside its buffers. */
+int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                         const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist);
+
 /* OverlayMem2Dv2::QuarterRead (src/ImageUtils/OverlayMem2Dv2.cpp:704-1052) of
  * a 16x16 block whose full-pel origin is (x, y) in a frame extended by edge
  * replication, at quarter offsets (qx, qy) in -3..3. */

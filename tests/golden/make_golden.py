@@ -8,6 +8,10 @@ inputs and stores inputs and outputs:
                   QCIF / CIF / partial-row pairs at motion ranges 64 and 128,
                   plus per-macroblock distortions for one QCIF pair (one
                   estimate per macroblock with a single pDistortionIncluded flag)
+* me_mrc.npz      MotionEstimatorH264ImplMultiresCross vectors and
+                  avgDistortion, modes 0/1/2, with and without
+                  pDistortionIncluded (the partial bottom row counts in the
+                  average when it is NULL)
 * transform.npz   FastForward4x4ITImpl1 / Impl2 / On16x16 levels and
                   FastInverse4x4ITImpl1 / On16x16 reconstructions over QP 0..51,
                   intra and inter, modes 0/1/2, a custom SetScale, and
@@ -67,6 +71,32 @@ def me_fixtures(ref: oracle.Reference) -> dict:
     return out
 
 
+MRC_CASES = [  # (name, w, h, motion_range, seed)
+    ("qcif_r64", 176, 144, 64, 21),
+    ("cif_r128", 352, 288, 128, 22),
+    ("partial_r128", 352, 280, 128, 23),
+    ("small_r32", 64, 48, 32, 24),
+]
+
+
+def mrc_fixtures(ref: oracle.Reference) -> dict:
+    out = {}
+    for name, w, h, mr, seed in MRC_CASES:
+        fr = synth.pan_sequence(seed, w, h, 2)
+        src, rf = fr[1], fr[0]
+        nmb = (w // 16) * (h // 16)
+        out[f"{name}_src"] = src.astype(np.uint8)
+        out[f"{name}_ref"] = rf.astype(np.uint8)
+        out[f"{name}_meta"] = np.array([w, h, mr], np.int32)
+        for mode in (0, 1, 2):
+            mv, avg = ref.me("multires_cross", src, rf, mr, mode=mode)
+            mvi, avgi = ref.me("multires_cross", src, rf, mr, mode=mode, dist_incl=np.ones(nmb, np.uint8))
+            assert np.array_equal(mv, mvi)
+            out[f"{name}_m{mode}_mv"] = mv
+            out[f"{name}_m{mode}_avg"] = np.array([avg, avgi], np.int64)
+    return out
+
+
 def transform_fixtures(ref: oracle.Reference) -> dict:
     lap = synth.residual_blocks(11, 16 * 64)
     full = ((synth.splitmix64(12, 16 * 16) % np.uint64(65536)).astype(np.int64) - 32768).astype(np.int16)
@@ -116,6 +146,7 @@ def main() -> None:
     oracle.build(with_reference=True)
     ref = oracle.Reference()
     np.savez_compressed(os.path.join(HERE, "me_full.npz"), **me_fixtures(ref))
+    np.savez_compressed(os.path.join(HERE, "me_mrc.npz"), **mrc_fixtures(ref))
     np.savez_compressed(os.path.join(HERE, "transform.npz"), **transform_fixtures(ref))
     np.savez_compressed(os.path.join(HERE, "colour.npz"), **colour_fixtures(ref))
     print("golden fixtures written to", HERE)
