@@ -1,0 +1,89 @@
+// example_estimate.cpp -- how a vpp codec drives the GPU classes.
+//
+//   example_estimate <pair.bin> <width> <height> <motionRange> <out.bin>
+//
+// pair.bin holds the source then the reference luma plane (int16).  The
+// program estimates with GpuMotionEstimatorH264ImplFull exactly as a codec
+// would with MotionEstimatorH264ImplFull (constructor, Create, Estimate,
+// predictor side effect), then runs the forward/inverse 4x4 transform classes
+// on the motion-compensated-free residual (source - reference) of the first
+// macroblock row.  out.bin receives: the vectors (N x 2 int16), avgDistortion
+// (int64), the predictor's copy of the vectors (N x 2 int32), then the
+// transformed residual levels and reconstruction (int16).
+#include <stdio.h>
+#include <stdlib.h>
+#include <vector>
+
+#include "vppgpu_vpp.hpp"
+
+class RecordingPredictor : public IMotionVectorPredictor {
+public:
+    explicit RecordingPredictor(int n) : mv(2 * (size_t)n, 0) {}
+    virtual int Create(void) { return 1; }
+    virtual int Get16x16Prediction(void*, int, int* x, int* y) { *x = *y = 0; return 1; }
+    virtual void Set16x16MotionVector(int blk, int x, int y) { mv[2 * blk] = x; mv[2 * blk + 1] = y; }
+    std::vector<int> mv;
+};
+
+int main(int argc, char** argv)
+{
+    if (argc != 6) {
+        fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin\n", argv[0]);
+        return 2;
+    }
+    int w = atoi(argv[2]), h = atoi(argv[3]), range = atoi(argv[4]);
+    std::vector<short> src((size_t)w * h), ref((size_t)w * h);
+    FILE* f = fopen(argv[1], "rb");
+    if (!f || fread(src.data(), 2, src.size(), f) != src.size() || fread(ref.data(), 2, ref.size(), f) != ref.size())
+        return 3;
+    fclose(f);
+    int nmb = (w / 16) * (h / 16);
+    bool* incl = new bool[nmb];
+    for (int i = 0; i < nmb; i++) incl[i] = true;
+
+    RecordingPredictor pred(nmb);
+    IMotionEstimator* me = new GpuMotionEstimatorH264ImplFull(src.data(), ref.data(), w, h, range, &pred, incl);
+    if (!me->Create()) {
+        fprintf(stderr, "Create failed\n");
+        return 4;
+    }
+    long avg = 0;
+    VectorStructList* vl = (VectorStructList*)me->Estimate(&avg);
+    if (!vl) {
+        fprintf(stderr, "Estimate failed\n");
+        return 5;
+    }
+
+    // residual of the first macroblock row, 4x4 blocks laid out contiguously
+    int nblk = (w / 4) * 4;
+    std::vector<short> blocks(16 * (size_t)nblk);
+    for (int b = 0; b < nblk; b++)
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 4; c++) {
+                int y = (b / (w / 4)) * 4 + r, x = (b % (w / 4)) * 4 + c;
+                blocks[16 * b + 4 * r + c] = (short)(src[(size_t)y * w + x] - ref[(size_t)y * w + x]);
+            }
+    GpuForward4x4IT fwd;
+    fwd.SetParameter(IForwardTransform::INTRA_FLAG_ID, 0);
+    fwd.SetParameter(IForwardTransform::QUANT_ID, 28);
+    fwd.TransformBlocks(blocks.data(), nblk);
+    std::vector<short> levels = blocks;
+    GpuInverse4x4IT inv;
+    inv.SetParameter(IInverseTransform::QUANT_ID, 28);
+    inv.InverseTransformBlocks(blocks.data(), nblk);
+
+    FILE* o = fopen(argv[5], "wb");
+    for (int k = 0; k < nmb; k++) {
+        short v[2] = {(short)vl->GetSimpleElement(k, 0), (short)vl->GetSimpleElement(k, 1)};
+        fwrite(v, 2, 2, o);
+    }
+    long long a = avg;
+    fwrite(&a, 8, 1, o);
+    fwrite(pred.mv.data(), 4, pred.mv.size(), o);
+    fwrite(levels.data(), 2, levels.size(), o);
+    fwrite(blocks.data(), 2, blocks.size(), o);
+    fclose(o);
+    delete me;
+    delete[] incl;
+    return 0;
+}

@@ -1,0 +1,365 @@
+// vppgpu_vpp.hpp -- drop-in C++ classes for vpp codecs, header only.
+//
+// Each class implements one of vpp's plugin interfaces by calling the C ABI
+// of include/vppgpu.h, so a codec swaps
+//     new MotionEstimatorH264ImplFull(pSrc, pRef, w, h, range, pMVPred, pDistIncl)
+// for
+//     new GpuMotionEstimatorH264ImplFull(pSrc, pRef, w, h, range, pMVPred, pDistIncl)
+// and keeps everything else.
+//
+// Build inside the vpp tree with -DVPPGPU_WITH_VPP: the classes then derive
+// from vpp's own IMotionEstimator, IForwardTransform, IInverseTransform and
+// RGBtoYUV420Converter and return vpp's VectorStructList.  Without that
+// macro, minimal local declarations with the same method signatures are
+// used (for this repository's tests and for codecs that only need the
+// methods).
+#pragma once
+
+#include <stddef.h>
+#include <string.h>
+
+#include "../../include/vppgpu.h"
+
+#ifdef VPPGPU_WITH_VPP
+#include "IForwardTransform.h"
+#include "IInverseTransform.h"
+#include "IMotionEstimator.h"
+#include "IMotionVectorPredictor.h"
+#include "RGBtoYUV420Converter.h"
+#include "VectorStructList.h"
+#else
+// ---- local declarations mirroring the vpp interfaces (same signatures) ----
+class IMotionEstimator {
+public:
+    virtual ~IMotionEstimator() {}
+    virtual int Create(void) = 0;
+    virtual void Reset(void) = 0;
+    virtual int Ready(void) = 0;
+    virtual void SetMode(int mode) = 0;
+    virtual int GetMode(void) = 0;
+    virtual void* Estimate(const void* pSrc, const void* pRef, long* avgDistortion) = 0;
+    virtual void* Estimate(long* avgDistortion) = 0;
+    virtual void* Estimate(long* avgDistortion, void* param) { (void)param; return Estimate(avgDistortion); }
+};
+
+class IMotionVectorPredictor {
+public:
+    virtual ~IMotionVectorPredictor() {}
+    virtual int Create(void) = 0;
+    virtual int Get16x16Prediction(void* pList, int blk, int* predX, int* predY) = 0;
+    virtual void Set16x16MotionVector(int blk, int mvX, int mvY) = 0;
+};
+
+// The SIMPLE2D layout of vpp's VectorStructList: one {short x, short y} per block.
+class VectorStructList {
+public:
+    static const int SIMPLE2D = 0;
+    explicit VectorStructList(int type) : _type(type), _length(0), _pData(NULL) {}
+    virtual ~VectorStructList() { delete[] _pData; }
+    virtual int SetLength(int length) {
+        delete[] _pData;
+        _pData = new short[2 * (size_t)(length > 0 ? length : 1)];
+        _length = length;
+        return 1;
+    }
+    int GetType(void) { return _type; }
+    int GetLength(void) { return _length; }
+    void* GetListPtr(void) { return _pData; }
+    virtual void SetSimpleElement(int pos, int element, int val) { _pData[2 * pos + (element ? 1 : 0)] = (short)val; }
+    virtual int GetSimpleElement(int pos, int element) { return _pData[2 * pos + (element ? 1 : 0)]; }
+
+protected:
+    int _type, _length;
+    short* _pData;
+};
+
+class IForwardTransform {
+public:
+    virtual ~IForwardTransform() {}
+    virtual void Transform(void* ptr) = 0;
+    virtual void Transform(void* pIn, void* pCoeff) = 0;
+    virtual void SetScale(void* pScale) = 0;
+    virtual void* GetScale(void) = 0;
+    virtual void SetMode(int mode) = 0;
+    virtual int GetMode(void) = 0;
+    virtual void SetParameter(int paramID, int paramVal) = 0;
+    virtual int GetParameter(int paramID) = 0;
+    virtual int QuantiseValue(short val, int pos, int qp) = 0;
+    static const int QUANT_ID = 0;
+    static const int INTRA_FLAG_ID = 1;
+    static const int TransformAndQuant = 0;
+    static const int TransformOnly = 1;
+    static const int QuantOnly = 2;
+};
+
+class IInverseTransform {
+public:
+    virtual ~IInverseTransform() {}
+    virtual void InverseTransform(void* ptr) = 0;
+    virtual void InverseTransform(void* pCoeff, void* pOut) = 0;
+    virtual void SetScale(void* pScale) = 0;
+    virtual void* GetScale(void) = 0;
+    virtual void SetMode(int mode) = 0;
+    virtual int GetMode(void) = 0;
+    virtual void SetParameter(int paramID, int paramVal) = 0;
+    virtual int GetParameter(int paramID) = 0;
+    static const int QUANT_ID = 0;
+    static const int TransformAndQuant = 0;
+    static const int TransformOnly = 1;
+    static const int QuantOnly = 2;
+};
+
+typedef short yuvType;
+class RGBtoYUV420Converter {
+public:
+    RGBtoYUV420Converter(void) { _width = 0; _height = 0; _chrOff = 0; _flip = false; }
+    RGBtoYUV420Converter(int width, int height) { _width = width; _height = height; _chrOff = 0; _flip = false; }
+    RGBtoYUV420Converter(int width, int height, int chrOff) { _width = width; _height = height; _chrOff = chrOff; _flip = false; }
+    virtual ~RGBtoYUV420Converter(void) {}
+    virtual void Convert(void* pRgb, void* pY, void* pU, void* pV) = 0;
+    int GetWidth(void) { return _width; }
+    int GetHeight(void) { return _height; }
+    int GetChrominanceOffset() const { return _chrOff; }
+    bool GetFlip() const { return _flip; }
+    void SetDimensions(int width, int height) { _width = width; _height = height; }
+    void SetFlip(bool flip) { _flip = flip; }
+    void SetChrominanceOffset(int val) { _chrOff = val; }
+
+protected:
+    int _width, _height, _chrOff;
+    bool _flip;
+};
+#endif  // VPPGPU_WITH_VPP
+
+namespace vppgpu_vpp {
+
+// One CUDA context per process unless the codec installs its own.
+inline vppgpu_ctx*& default_context()
+{
+    static vppgpu_ctx* ctx = NULL;
+    return ctx;
+}
+
+inline vppgpu_ctx* context()
+{
+    vppgpu_ctx*& c = default_context();
+    if (!c && vppgpu_ctx_create(0, &c) != VPPGPU_OK) c = NULL;
+    return c;
+}
+
+}  // namespace vppgpu_vpp
+
+// ---------------------------------------------------------------------------
+// IMotionEstimator replacements.  Constructor arguments, Create()/Ready()
+// two-stage set-up, SetMode/GetMode and the returned VectorStructList follow
+// MotionEstimatorH264ImplFull (src/CodecUtils/MotionEstimatorH264ImplFull.cpp:111-320).
+// Every Estimate() re-reads the planes given at construction and, as the
+// reference does, hands each final vector to the predictor
+// (Set16x16MotionVector) so later frames and stages see them.
+// ---------------------------------------------------------------------------
+class GpuMotionEstimatorH264Base : public IMotionEstimator {
+public:
+    GpuMotionEstimatorH264Base(int kind, const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                               int motionRange, IMotionVectorPredictor* pMVPred, void* pDistortionIncluded)
+        : _kind(kind), _pSrc(pSrc), _pRef(pRef), _w(imgWidth), _h(imgHeight), _range(motionRange),
+          _pMVPred(pMVPred), _pIncl((bool*)pDistortionIncluded), _mode(1), _me(NULL), _list(NULL),
+          _incl(NULL), _last(VPPGPU_OK)
+    {
+    }
+    virtual ~GpuMotionEstimatorH264Base() { Destroy(); }
+
+    virtual int Create(void)
+    {
+        Destroy();
+        vppgpu_ctx* ctx = vppgpu_vpp::context();
+        if (!ctx || vppgpu_me_create(ctx, _kind, _w, _h, _range, &_me) != VPPGPU_OK) {
+            _me = NULL;
+            return 0;
+        }
+        vppgpu_me_set_mode(_me, _mode);
+        int n = 0;
+        vppgpu_me_num_mbs(_me, &n);
+        _list = new VectorStructList(VectorStructList::SIMPLE2D);
+        _list->SetLength(n);
+        _incl = new unsigned char[n > 0 ? n : 1];
+        return 1;
+    }
+    virtual void Reset(void) {}
+    virtual int Ready(void) { return _me ? 1 : 0; }
+    virtual void SetMode(int mode)
+    {
+        _mode = mode;
+        if (_me) vppgpu_me_set_mode(_me, mode);
+    }
+    virtual int GetMode(void) { return _mode; }
+    virtual void* Estimate(const void* pSrc, const void* pRef, long* avgDistortion)
+    {
+        (void)pSrc;
+        (void)pRef;
+        return Estimate(avgDistortion);
+    }
+    virtual void* Estimate(long* avgDistortion) { return Run(avgDistortion, false, 0.0); }
+    virtual void* Estimate(long* avgDistortion, void* param)
+    {
+        return param ? Run(avgDistortion, true, *(double*)param) : Estimate(avgDistortion);
+    }
+
+    // Status of the last Estimate() (vppgpu status code); the vpp interface
+    // itself has no error channel.
+    int LastStatus(void) const { return _last; }
+
+protected:
+    void* Run(long* avg, bool with_lambda, double lambda)
+    {
+        if (!_me) return NULL;
+        int n = _list->GetLength();
+        const unsigned char* incl = NULL;
+        if (_pIncl) {
+            for (int i = 0; i < n; i++) _incl[i] = _pIncl[i] ? 1 : 0;
+            incl = _incl;
+        }
+        short* mv = (short*)_list->GetListPtr();
+        long a = 0;
+        _last = with_lambda ? vppgpu_me_estimate_lambda(_me, (const short*)_pSrc, (const short*)_pRef, incl, NULL,
+                                                        lambda, mv, NULL, &a)
+                            : vppgpu_me_estimate(_me, (const short*)_pSrc, (const short*)_pRef, incl, NULL, mv,
+                                                 NULL, &a);
+        if (avg) *avg = _last == VPPGPU_OK ? a : 0;
+        if (_last != VPPGPU_OK) return NULL;
+        if (_pMVPred)
+            for (int k = 0; k < n; k++) _pMVPred->Set16x16MotionVector(k, mv[2 * k], mv[2 * k + 1]);
+        return (void*)_list;
+    }
+    void Destroy(void)
+    {
+        if (_me) vppgpu_me_destroy(_me);
+        _me = NULL;
+        delete _list;
+        _list = NULL;
+        delete[] _incl;
+        _incl = NULL;
+    }
+
+    int _kind;
+    const void* _pSrc;
+    const void* _pRef;
+    int _w, _h, _range;
+    IMotionVectorPredictor* _pMVPred;
+    bool* _pIncl;
+    int _mode;
+    vppgpu_me* _me;
+    VectorStructList* _list;
+    unsigned char* _incl;
+    int _last;
+};
+
+class GpuMotionEstimatorH264ImplFull : public GpuMotionEstimatorH264Base {
+public:
+    GpuMotionEstimatorH264ImplFull(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int motionRange,
+                                   IMotionVectorPredictor* pMVPred)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_FULL, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred, NULL)
+    {
+    }
+    GpuMotionEstimatorH264ImplFull(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int motionRange,
+                                   IMotionVectorPredictor* pMVPred, void* pDistortionIncluded)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_FULL, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred,
+                                     pDistortionIncluded)
+    {
+    }
+};
+
+// ---------------------------------------------------------------------------
+// IForwardTransform / IInverseTransform replacements (FastForward4x4ITImpl1,
+// FastInverse4x4ITImpl1 and their On16x16 variants).  Transform(void*) takes
+// one unit like the reference; TransformBlocks() takes many at once, which is
+// where the GPU pays off.
+// ---------------------------------------------------------------------------
+class GpuForward4x4IT : public IForwardTransform {
+public:
+    explicit GpuForward4x4IT(int layout = VPPGPU_LAYOUT_BLOCKS)
+        : _layout(layout), _mode(TransformAndQuant), _q(1), _intra(1) {}
+    virtual void Transform(void* ptr) { TransformBlocks(ptr, 1); }
+    virtual void Transform(void* pIn, void* pCoeff)
+    {
+        memcpy(pCoeff, pIn, sizeof(short) * Unit());
+        Transform(pCoeff);
+    }
+    void TransformBlocks(void* ptr, long long nunits)
+    {
+        vppgpu_fwd4x4(vppgpu_vpp::context(), (short*)ptr, nunits, _layout, _mode, _q, _intra);
+    }
+    virtual void SetScale(void* pScale) { (void)pScale; }
+    virtual void* GetScale(void) { return NULL; }
+    virtual void SetMode(int mode) { _mode = mode; }
+    virtual int GetMode(void) { return _mode; }
+    virtual void SetParameter(int paramID, int paramVal)
+    {
+        if (paramID == QUANT_ID) _q = paramVal;
+        else if (paramID == INTRA_FLAG_ID) _intra = paramVal;
+    }
+    virtual int GetParameter(int paramID) { return paramID == QUANT_ID ? _q : _intra; }
+    virtual int QuantiseValue(short val, int pos, int qp)
+    {
+        _q = qp;
+        return vppgpu_quantise_value(val, pos, qp, _intra);
+    }
+
+protected:
+    size_t Unit() const { return _layout == VPPGPU_LAYOUT_BLOCKS ? 16 : 256; }
+    int _layout, _mode, _q, _intra;
+};
+
+class GpuInverse4x4IT : public IInverseTransform {
+public:
+    explicit GpuInverse4x4IT(int layout = VPPGPU_LAYOUT_BLOCKS) : _layout(layout), _mode(TransformAndQuant), _q(1)
+    {
+        for (int i = 0; i < 16; i++) _weight[i] = 16;
+    }
+    virtual void InverseTransform(void* ptr) { InverseTransformBlocks(ptr, 1); }
+    virtual void InverseTransform(void* pCoeff, void* pOut)
+    {
+        memcpy(pOut, pCoeff, sizeof(short) * (_layout == VPPGPU_LAYOUT_BLOCKS ? 16 : 256));
+        InverseTransform(pOut);
+    }
+    void InverseTransformBlocks(void* ptr, long long nunits)
+    {
+        vppgpu_inv4x4(vppgpu_vpp::context(), (short*)ptr, nunits, _layout, _mode, _q, _weight);
+    }
+    virtual void SetScale(void* pScale) { memcpy(_weight, pScale, sizeof(_weight)); }
+    virtual void* GetScale(void) { return (void*)_weight; }
+    virtual void SetMode(int mode) { _mode = mode; }
+    virtual int GetMode(void) { return _mode; }
+    virtual void SetParameter(int paramID, int paramVal)
+    {
+        if (paramID == QUANT_ID) _q = paramVal;
+    }
+    virtual int GetParameter(int paramID) { (void)paramID; return _q; }
+
+protected:
+    int _layout, _mode, _q;
+    int _weight[16];
+};
+
+// ---------------------------------------------------------------------------
+// The GPU slot vpp reserves for colour conversion (an empty class in the
+// reference, include/ImageUtils/FastGpuRGB24toYUV420Converter.h).
+// ---------------------------------------------------------------------------
+class FastGpuRGB24toYUV420Converter : public RGBtoYUV420Converter {
+public:
+    FastGpuRGB24toYUV420Converter(void) : _kind(VPPGPU_RGB_FIXED_POINT) {}
+    FastGpuRGB24toYUV420Converter(int width, int height) : RGBtoYUV420Converter(width, height), _kind(VPPGPU_RGB_FIXED_POINT) {}
+    FastGpuRGB24toYUV420Converter(int width, int height, int chrOff)
+        : RGBtoYUV420Converter(width, height, chrOff), _kind(VPPGPU_RGB_FIXED_POINT)
+    {
+        _flip = false;
+    }
+    void SetArithmetic(int kind) { _kind = kind; }
+    virtual void Convert(void* pRgb, void* pY, void* pU, void* pV)
+    {
+        vppgpu_rgb24_to_yuv420(vppgpu_vpp::context(), _kind, (const unsigned char*)pRgb, _width, _height, _chrOff,
+                               _flip ? 1 : 0, (short*)pY, (short*)pU, (short*)pV);
+    }
+
+protected:
+    int _kind;
+};

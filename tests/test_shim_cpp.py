@@ -1,0 +1,66 @@
+"""The C++ drop-in classes (imagecodingutils_gb300/shim/vppgpu_vpp.hpp): they
+compile standalone and against vpp's own interface headers, and a codec-style
+program built on them gives the oracle's results on the GPU."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from imagecodingutils_gb300 import synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SHIM = os.path.join(ROOT, "imagecodingutils_gb300", "shim")
+REF_INC = "/root/reference/include"
+
+
+def gxx(args):
+    return subprocess.run(["g++", "-std=c++11", "-Wall", "-Wno-pragma-once-outside-header", *args],
+                          capture_output=True, text=True)
+
+
+def test_shim_compiles_standalone():
+    r = gxx(["-fsyntax-only", "-I", SHIM, os.path.join(SHIM, "example_estimate.cpp")])
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_INC), reason="vpp headers not present on this host")
+def test_shim_compiles_against_vpp_interfaces():
+    r = gxx(["-fsyntax-only", "-DVPPGPU_WITH_VPP", "-include", "math.h", "-x", "c++",
+             *[f"-I{REF_INC}/{d}" for d in ("CodecUtils", "GeneralUtils", "ImageUtils")],
+             os.path.join(SHIM, "vppgpu_vpp.hpp")])
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.gpu
+def test_codec_style_program_on_gpu(tmp_path, vpp, orc):
+    from imagecodingutils_gb300 import build
+    exe = tmp_path / "example_estimate"
+    r = subprocess.run(["g++", "-std=c++11", "-O2", "-I", SHIM, os.path.join(SHIM, "example_estimate.cpp"),
+                        "-L", os.path.dirname(build.LIB), "-lvppgpu", f"-Wl,-rpath,{os.path.dirname(build.LIB)}",
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    w, h, mr = 176, 144, 128
+    fr = synth.pan_sequence(77, w, h, 2)
+    pair = tmp_path / "pair.bin"
+    pair.write_bytes(fr[1].astype(np.int16).tobytes() + fr[0].astype(np.int16).tobytes())
+    out = tmp_path / "out.bin"
+    r = subprocess.run([str(exe), str(pair), str(w), str(h), str(mr), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    nmb = (w // 16) * (h // 16)
+    raw = out.read_bytes()
+    mv = np.frombuffer(raw[:4 * nmb], np.int16).reshape(nmb, 2)
+    avg = np.frombuffer(raw[4 * nmb:4 * nmb + 8], np.int64)[0]
+    pred = np.frombuffer(raw[4 * nmb + 8:12 * nmb + 8], np.int32).reshape(nmb, 2)
+    rest = np.frombuffer(raw[12 * nmb + 8:], np.int16)
+    nblk = (w // 4) * 4
+    levels, recon = rest[:16 * nblk], rest[16 * nblk:]
+    mv_o, _, avg_o = orc.me_full(fr[1], fr[0], mr, dist_incl=np.ones(nmb, np.uint8))
+    np.testing.assert_array_equal(mv, mv_o)
+    assert avg == avg_o
+    np.testing.assert_array_equal(pred, mv_o.astype(np.int32))
+    res = (fr[1][:16].astype(np.int32) - fr[0][:16]).astype(np.int16)
+    blocks = res.reshape(4, 4, w // 4, 4).transpose(0, 2, 1, 3).reshape(-1, 16)
+    lev_o = orc.fwd4x4(blocks, 0, 0, 28, 0)
+    np.testing.assert_array_equal(levels.reshape(-1, 16), lev_o)
+    np.testing.assert_array_equal(recon.reshape(-1, 16), orc.inv4x4(lev_o, 0, 0, 28))
