@@ -129,6 +129,27 @@ int vppgpu_me_timing(vppgpu_me* me, int* n, double* pack_ms, double* search_ms, 
  * the integer-ALU roofline of the motion search.  No vpp counterpart. */
 int vppgpu_calibrate_dp4a(vppgpu_ctx* ctx, double* dp4a_per_second);
 
+/* Full search without any device allocation.  No counterpart in the
+ * reference: it exists for callers that must not allocate device memory once
+ * running (real-time encoders with a fixed budget, plugins inside a host
+ * that owns all allocations, code paths that forbid allocator calls after
+ * start-up).  Same kernels and results as vppgpu_me_estimate_device, but all
+ * intermediate buffers live in one 7 MiB static device array held by every
+ * GPU that loads the library until the process exits.  Limits: at most
+ * VPPGPU_NOALLOC_MAX_MBS stored macroblocks and width, height at most
+ * VPPGPU_NOALLOC_MAX_DIM, else VPPGPU_ERR_UNSUPPORTED.  Inputs and outputs are
+ * the caller's device buffers; cuda_stream is a cudaStream_t (NULL: default
+ * stream); the call returns when the results are written.  All calls share
+ * the array, so calls that overlap on the GPU race and must be serialised.
+ * The first call on a device (with that device current) looks up the array's
+ * address; make it before any stream capture. */
+#define VPPGPU_NOALLOC_MAX_MBS 396
+#define VPPGPU_NOALLOC_MAX_DIM 1024
+int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* d_ref, int width, int height,
+                                    int motion_range, const unsigned char* d_dist_included,
+                                    const int* d_mb_slice, short* d_mv_out, int* d_mb_dist_out,
+                                    long* avg_distortion, void* cuda_stream);
+
 /* ---- 4x4 integer transform + H.264 quantisation ------------------------- */
 /* Modes (include/CodecUtils/IForwardTransform.h:119-125). */
 #define VPPGPU_TQ_TRANSFORM_AND_QUANT 0
