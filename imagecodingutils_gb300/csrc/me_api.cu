@@ -15,8 +15,10 @@ struct vppgpu_me {
     short* d_ref16;
     unsigned char* d_src8;
     unsigned char* d_refp;
-    int* spec;  // 5 * nmb: mv, imv, min, zero, flags
+    int* spec;  // 5 * nmb: {vector, distortion, zero distortion, flags} per MB, then full-pel winners
     int* tables;
+    int2* cache;
+    int* dict;
     int* state; // 3 * nmb: final_mv, final_dist, pred_used
     int* d_out_mv;
     int* d_out_dist;
@@ -83,6 +85,8 @@ void me_free(vppgpu_me* me)
     cudaFree(me->d_refp);
     cudaFree(me->spec);
     cudaFree(me->tables);
+    cudaFree(me->cache);
+    cudaFree(me->dict);
     cudaFree(me->state);
     cudaFree(me->d_out_mv);
     cudaFree(me->d_out_dist);
@@ -115,11 +119,10 @@ vppgpu::FullArgs full_args(vppgpu_me* me, const unsigned char* incl, const int* 
     a.rstride = me->rstride;
     a.src8 = me->d_src8;
     a.refp = me->d_refp;
-    a.spec_mv = me->spec;
-    a.spec_imv = me->spec + me->nmb;
-    a.spec_min = me->spec + 2 * me->nmb;
-    a.spec_zero = me->spec + 3 * me->nmb;
-    a.spec_flags = me->spec + 4 * me->nmb;
+    a.spec4 = reinterpret_cast<int4*>(me->spec);
+    a.spec_imv = me->spec + 4 * (size_t)me->nmb;
+    a.cache = me->cache;
+    a.dict = me->dict;
     a.tables = me->tables;
     a.final_mv = me->state;
     a.final_dist = me->state + me->nmb;
@@ -188,6 +191,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) || (rc = dalloc(&me->d_src8, npix)) ||
         (rc = dalloc(&me->d_refp, npad)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
         (rc = dalloc(&me->tables, (size_t)me->nmb * 64 * 64)) || (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
+        (rc = dalloc(&me->cache, (size_t)me->nmb * vppgpu::KCACHE)) || (rc = dalloc(&me->dict, vppgpu::NDICT)) ||
         (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
         (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||
         (rc = dalloc(&me->d_slice, me->nmb)) || (rc = dalloc(&me->ctrl, 1)) ||
@@ -340,3 +344,16 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 }
 
 }  // extern "C"
+
+extern "C" int vppgpu_me_last_stats(vppgpu_me* me, int* stats8)
+{
+    if (!me || !stats8) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    VPP_CUDA(cudaMemcpyAsync(me->h_ctrl, me->ctrl, sizeof(vppgpu::MeCtrl), cudaMemcpyDeviceToHost, me->ctx->stream));
+    VPP_CUDA(cudaStreamSynchronize(me->ctx->stream));
+    const vppgpu::MeCtrl& c = *me->h_ctrl;
+    int v[8] = {c.sweeps, c.converged, c.relax_evals, c.relax_miss, c.wave_miss, c.status, c.count, 0};
+    for (int i = 0; i < 8; i++) stats8[i] = v[i];
+    return VPPGPU_OK;
+}

@@ -225,12 +225,104 @@ __device__ __forceinline__ int qread_ssd_warp(const unsigned char (*patch)[24], 
     return warp_sum(acc);
 }
 
+// Planar form of the same distortion: the half-pel planes the fractional
+// case needs are computed once into per-warp scratch (b: 17x16, h: 16x17,
+// j from 16x21 unrounded vertical taps), then every pixel is a lookup or a
+// rounded mean of two lookups -- about 20x fewer taps than per-pixel j.
+struct PdScratch {
+    unsigned char patch[22][24];
+    int rawv[16][21];
+    unsigned char b[17][16];
+    unsigned char h[16][17];
+    unsigned char j[16][16];
+};
+
+__device__ __forceinline__ int pd_planar_warp(PdScratch& s, const unsigned char* cur, int fx, int fy, int lane)
+{
+    const int sel = fx | (fy << 2);
+    // which planes: b for x-half and the b-based quarter cases, h likewise, j for the centre cases
+    const bool need_b = sel == 2 || sel == 1 || sel == 3 || sel == 6 || sel == 14 || sel == 5 || sel == 7 ||
+                        sel == 13 || sel == 15;
+    const bool need_h = sel == 8 || sel == 4 || sel == 12 || sel == 9 || sel == 11 || sel == 5 || sel == 7 ||
+                        sel == 13 || sel == 15;
+    const bool need_j = sel == 10 || sel == 6 || sel == 14 || sel == 9 || sel == 11;
+    if (need_b)
+        for (int i = lane; i < 17 * 16; i += 32) {
+            int r = i >> 4, c = i & 15;  // b at (r, c): row r, cols c-2..c+3 -> patch [r+3][c+1..c+6]
+            const unsigned char* q = &s.patch[r + 3][c + 1];
+            s.b[r][c] = (unsigned char)clip255((tap6(q[0], q[1], q[2], q[3], q[4], q[5]) + 16) >> 5);
+        }
+    if (need_h)
+        for (int i = lane; i < 16 * 17; i += 32) {
+            int r = i / 17, c = i - r * 17;  // h at (r, c): rows r-2..r+3 -> patch [r+1..r+6][c+3]
+            s.h[r][c] = (unsigned char)clip255((tap6(s.patch[r + 1][c + 3], s.patch[r + 2][c + 3], s.patch[r + 3][c + 3],
+                                                     s.patch[r + 4][c + 3], s.patch[r + 5][c + 3], s.patch[r + 6][c + 3]) +
+                                                16) >> 5);
+        }
+    if (need_j) {
+        for (int i = lane; i < 16 * 21; i += 32) {
+            int r = i / 21, c = i - r * 21;  // vertical taps at col c-2 -> patch col c+1
+            s.rawv[r][c] = tap6(s.patch[r + 1][c + 1], s.patch[r + 2][c + 1], s.patch[r + 3][c + 1], s.patch[r + 4][c + 1],
+                                s.patch[r + 5][c + 1], s.patch[r + 6][c + 1]);
+        }
+        __syncwarp();
+        for (int i = lane; i < 256; i += 32) {
+            int r = i >> 4, c = i & 15;
+            const int* q = &s.rawv[r][c];  // cols c-2..c+3
+            s.j[r][c] = (unsigned char)clip255((tap6(q[0], q[1], q[2], q[3], q[4], q[5]) + 512) >> 10);
+        }
+    }
+    __syncwarp();
+    // each case reads one plane sample or the rounded mean of two; the case
+    // is uniform across the warp, so pick base pointers and strides once
+    const unsigned char* G0 = &s.patch[3][3];
+    const unsigned char *p1 = G0, *p2 = G0;
+    int st1 = 24, st2 = 24;
+    bool two = true;
+    switch (sel) {
+    case 0: two = false; break;
+    case 2: p1 = &s.b[0][0]; st1 = 16; two = false; break;                   // b
+    case 8: p1 = &s.h[0][0]; st1 = 17; two = false; break;                   // h
+    case 10: p1 = &s.j[0][0]; st1 = 16; two = false; break;                  // j
+    case 1: p2 = &s.b[0][0]; st2 = 16; break;                                // a = (G + b)
+    case 3: p1 = G0 + 1; p2 = &s.b[0][0]; st2 = 16; break;                   // c = (G[x+1] + b)
+    case 4: p2 = &s.h[0][0]; st2 = 17; break;                                // d = (G + h)
+    case 12: p1 = G0 + 24; p2 = &s.h[0][0]; st2 = 17; break;                 // n = (G[y+1] + h)
+    case 6: p1 = &s.j[0][0]; st1 = 16; p2 = &s.b[0][0]; st2 = 16; break;     // f = (j + b)
+    case 14: p1 = &s.j[0][0]; st1 = 16; p2 = &s.b[1][0]; st2 = 16; break;    // q = (j + b[y+1])
+    case 9: p1 = &s.j[0][0]; st1 = 16; p2 = &s.h[0][0]; st2 = 17; break;     // i = (j + h)
+    case 11: p1 = &s.j[0][0]; st1 = 16; p2 = &s.h[0][1]; st2 = 17; break;    // k = (j + h[x+1])
+    case 5: p1 = &s.b[0][0]; st1 = 16; p2 = &s.h[0][0]; st2 = 17; break;     // e = (b + h)
+    case 7: p1 = &s.b[0][0]; st1 = 16; p2 = &s.h[0][1]; st2 = 17; break;     // g = (b + h[x+1])
+    case 13: p1 = &s.h[0][0]; st1 = 17; p2 = &s.b[1][0]; st2 = 16; break;    // p = (h + b[y+1])
+    default: p1 = &s.h[0][1]; st1 = 17; p2 = &s.b[1][0]; st2 = 16; break;    // r = (h[x+1] + b[y+1])
+    }
+    int acc = 0;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        int px = lane + 32 * t, r = px >> 4, c = px & 15;
+        int v = p1[r * st1 + c];
+        if (two) v = (v + p2[r * st2 + c] + 1) >> 1;
+        int d = (int)cur[px] - v;
+        acc += d * d;
+    }
+    return warp_sum(acc);
+}
+
 // Copy a 22x22 full-pel patch (rows/cols -3..18 around (x, y)) from a padded plane.
 __device__ __forceinline__ void load_patch22(unsigned char (*dst)[24], const Plane8& pl, int x, int y, int lane)
 {
-    for (int i = lane; i < 22 * 22; i += 32) {
+    unsigned char v[16];
+#pragma unroll
+    for (int t = 0; t < 16; t++) {  // all loads in flight before any store
+        int i = lane + 32 * t;
         int r = i / 22, c = i - r * 22;
-        dst[r][c] = *pl.at(x - 3 + c, y - 3 + r);
+        v[t] = i < 22 * 22 ? __ldg(pl.at(x - 3 + c, y - 3 + r)) : 0;
+    }
+#pragma unroll
+    for (int t = 0; t < 16; t++) {
+        int i = lane + 32 * t;
+        if (i < 22 * 22) dst[i / 22][i % 22] = v[t];
     }
     __syncwarp();
 }
@@ -250,33 +342,46 @@ __device__ __forceinline__ int median3(int x, int y, int z)
     return x + y + z - lo - hi;
 }
 
-__device__ __forceinline__ int load_mv_relaxed(const int* p)
-{
-    return __ldcg(p);
-}
+// Neighbour availability bits kept in the per-macroblock flags (position
+// and slice membership, MacroBlockH264::Initialise, MacroBlockH264.cpp:319-).
+constexpr int AV_A = 1 << 1;   // left
+constexpr int AV_B = 1 << 2;   // above
+constexpr int AV_C = 1 << 3;   // above-right
+constexpr int AV_D = 1 << 4;   // above-left
 
-__device__ __forceinline__ void median_pred(const int* final_mv, const int* slice, int k, int cols, int* px, int* py)
+__device__ __forceinline__ int neighbour_mask(const int* slice, int k, int cols, int rows)
 {
     int r = k / cols, c = k - r * cols;
     int sk = slice ? slice[k] : 0;
-    auto avail = [&](int rr, int cc) -> int {
-        if (rr < 0 || cc < 0 || cc >= cols) return -1;
-        int n = rr * cols + cc;
-        if (slice && slice[n] != sk) return -1;
-        return n;
-    };
-    int a = avail(r, c - 1), b = avail(r - 1, c), cn = avail(r - 1, c + 1);
-    int A = a >= 0 ? load_mv_relaxed(final_mv + a) : 0;
-    int B = b >= 0 ? load_mv_relaxed(final_mv + b) : 0;
-    int C = 0;
-    if (cn >= 0) C = load_mv_relaxed(final_mv + cn);
-    else {
-        int d = avail(r - 1, c - 1);
-        if (d >= 0) C = load_mv_relaxed(final_mv + d);
+    auto ok = [&](int rr, int cc) { return rr >= 0 && rr < rows && cc >= 0 && cc < cols && (!slice || slice[rr * cols + cc] == sk); };
+    return (ok(r, c - 1) ? AV_A : 0) | (ok(r - 1, c) ? AV_B : 0) | (ok(r - 1, c + 1) ? AV_C : 0) |
+           (ok(r - 1, c - 1) ? AV_D : 0);
+}
+
+// Median of the packed neighbour vectors under the availability mask.
+__device__ __forceinline__ void median_from(int av, int A, int B, int C, int D, int* px, int* py)
+{
+    if (!(av & AV_A)) A = 0;
+    if (!(av & AV_B)) B = 0;
+    if (av & AV_C) {
+    } else if (av & AV_D) {
+        C = D;
+    } else {
+        C = 0;
     }
-    if (b < 0 && cn < 0) B = C = A;
+    if (!(av & AV_B) && !(av & AV_C)) B = C = A;
     *px = median3(mv_x(A), mv_x(B), mv_x(C));
     *py = median3(mv_y(A), mv_y(B), mv_y(C));
+}
+
+// From the current vectors in global memory (L2, bypassing L1: other SMs update them).
+__device__ __forceinline__ void median_pred(const int* final_mv, int av, int k, int cols, int* px, int* py)
+{
+    int A = (av & AV_A) ? __ldcg(final_mv + k - 1) : 0;
+    int B = (av & AV_B) ? __ldcg(final_mv + k - cols) : 0;
+    int C = (av & AV_C) ? __ldcg(final_mv + k - cols + 1) : 0;
+    int D = (!(av & AV_C) && (av & AV_D)) ? __ldcg(final_mv + k - cols - 1) : 0;
+    median_from(av, A, B, C, D, px, py);
 }
 
 // Nearest full-pel prediction with C division (Full.cpp:368-380).
@@ -286,7 +391,7 @@ __device__ __forceinline__ int round_pred(int p) { return p < 0 ? (p - 2) / 4 : 
 // (include/CodecUtils/MotionEstimatorH264ImplFull.h:140-168): cost =
 // D/norm + lambda*sqrt(|v-ref|^2) in IEEE double, one rounding per
 // operation, strict improvement.  Returns the winning slot 0..2.
-__device__ __forceinline__ int best_of3(int bx, int by, int bd, int px, int py, int pd, int zd, double lambda,
+static __device__ __noinline__ int best_of3(int bx, int by, int bd, int px, int py, int pd, int zd, double lambda,
                                         double norm, int xref, int yref)
 {
     auto cost = [&](int x, int y, int d) {
@@ -302,6 +407,32 @@ __device__ __forceinline__ int best_of3(int bx, int by, int bd, int px, int py, 
     }
     double c2 = cost(0, 0, zd);
     if (c2 < c0) pos = 2;
+    return pos;
+}
+
+// Same decision, float first: each float cost is within a few ulp of the
+// exact real value and the double costs within 2^-50 relative, so when every
+// compared pair differs by more than 2^-18 relative both orderings agree with
+// the exact one.  Near-ties (including exact ones) take the double path.
+__device__ __forceinline__ int best_of3_fast(int bx, int by, int bd, int px, int py, int pd, int zd, double lambda,
+                                             int xref, int yref)
+{
+    const float lf = (float)lambda, inv = 1.0f / 256.0f;
+    float m0 = (float)((bx - xref) * (bx - xref) + (by - yref) * (by - yref));
+    float m2 = (float)(xref * xref + yref * yref);
+    float c0 = (float)bd * inv + lf * sqrtf(m0);
+    float c1 = (float)pd * inv;  // the prediction is the reference vector itself
+    float c2 = (float)zd * inv + lf * sqrtf(m2);
+    auto close = [](float a, float b) { return fabsf(a - b) <= 4e-6f * fmaxf(fabsf(a), fabsf(b)) + 1e-30f; };
+    if (close(c0, c1) || close(c0, c2) || close(c1, c2))
+        return best_of3(bx, by, bd, px, py, pd, zd, lambda, 256.0, xref, yref);
+    int pos = 0;
+    float c = c0;
+    if (c1 < c) {
+        c = c1;
+        pos = 1;
+    }
+    if (c2 < c) pos = 2;
     return pos;
 }
 

@@ -31,18 +31,11 @@
 //                   in practice a handful, instead of a ~250-step wavefront.
 #include <string.h>
 
-#include "me_common.cuh"
-#include "me_internal.h"
+#include "me_full_common.cuh"
 
 namespace vppgpu {
 namespace {
-
-constexpr int RMAX = 31;       // table geometry: i in [-31,31] -> ii = i+31, j -> jj = j+32
-constexpr int WROWS = 84;      // window rows m-34 .. m+49
-constexpr int WSTRIDE = 112;   // window cols n-48 .. n+63
-constexpr int H2STRIDE = 81;   // odd stride: conflict-free column walks
-constexpr int TAB = 64;        // SSD table is TAB x TAB ints
-constexpr int FLAG_TIE = 1;
+using namespace full;
 
 struct SearchSmem {
     alignas(16) unsigned char win[WROWS][WSTRIDE];
@@ -94,73 +87,6 @@ __global__ void __launch_bounds__(256) k_full_pack(const short* __restrict__ src
     }
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(status, ST_PIXEL_RANGE);
 }
-
-// GetMotionRange with zero offset (Full.cpp:1029-1081).
-__device__ __forceinline__ void full_range(int n, int m, int W, int H, int motion_range, int& xl, int& xr, int& yu,
-                                           int& yd)
-{
-    // Estimate asks for range = vecRange = motion_range/4 with zero offset, so
-    // both vector limits resolve to vecRange - 1 (Full.cpp:1046-1061).
-    int vr = motion_range / 4;
-    int lr = vr - 1, rr = vr - 1;
-    const int boundary = 16;
-    xl = (n - lr >= -boundary) ? -lr : -(n + boundary);
-    xr = (n + rr < W) ? rr : W - n;
-    yu = (m - lr >= -boundary) ? -lr : -(m + boundary);
-    yd = (m + rr < H) ? rr : H - m;
-}
-
-// Sequential raster replay of the integer search over tab (ii = i+31,
-// jj = j+32), one warp.  prx/pry: rounded prediction used at ties.  Returns
-// the winner and sets *tie when any exact tie was decided.
-template <typename TabT>
-__device__ __forceinline__ void scan_table(const TabT& tab, int xl, int xr, int yu, int yd, int prx, int pry,
-                                           int lane, int* omx, int* omy, int* omin, int* tie)
-{
-    int minD = tab(RMAX, RMAX + 1), mx = 0, my = 0, t = 0;
-    for (int i = yu; i <= yd; i++) {
-        for (int base = xl; base <= xr; base += 32) {
-            int j = base + lane;
-            bool valid = (j <= xr) && !(i == 0 && j == 0);
-            int d = valid ? tab(i + RMAX, j + RMAX + 1) : 0x7fffffff;
-            unsigned pending = 0xffffffffu;
-            while (true) {
-                bool ok = valid && d <= minD && (i + my >= yu) && (i + my <= yd) && (j + mx >= xl) && (j + mx <= xr);
-                unsigned m = __ballot_sync(0xffffffffu, ok) & pending;
-                if (!m) break;
-                int f = __ffs(m) - 1;
-                int df = __shfl_sync(0xffffffffu, d, f);
-                int jf = base + f;
-                bool accept = true;
-                if (df == minD) {
-                    t = 1;
-                    int cx = mx - prx, cy = my - pry, nx = jf - prx, ny = i - pry;
-                    accept = (cy * cy + cx * cx) - (ny * ny + nx * nx) >= 0;
-                }
-                if (accept) {
-                    minD = df;
-                    mx = jf;
-                    my = i;
-                }
-                pending &= ~((2u << f) - 1u);
-                if (f == 31) break;
-            }
-        }
-    }
-    *omx = mx;
-    *omy = my;
-    *omin = minD;
-    *tie = t;
-}
-
-struct SmemTab {
-    const int (*t)[TAB];
-    __device__ int operator()(int r, int c) const { return t[r][c]; }
-};
-struct GlobalTab {
-    const int* t;
-    __device__ int operator()(int r, int c) const { return __ldcg(t + r * TAB + c); }
-};
 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128, 4) k_full_search(FullArgs a)
@@ -328,166 +254,11 @@ __global__ void __launch_bounds__(128, 4) k_full_search(FullArgs a)
         subpel_refine_warp(sp, S.cur, lane, &minD, &qmx, &qmy);
         if (lane == 0) {
             int mvx = 4 * mx + qmx, mvy = 4 * my + qmy;
-            a.spec_mv[k] = pack_mv(mvx, mvy);
+            int av = neighbour_mask(a.slice, k, a.cols, a.nmb / a.cols);
+            a.spec4[k] = make_int4(pack_mv(mvx, mvy), minD, zero_d, flags | av);
             a.spec_imv[k] = pack_mv(mx, my);
-            a.spec_min[k] = minD;
-            a.spec_zero[k] = zero_d;
-            a.spec_flags[k] = flags;
             __stcg(a.final_mv + k, pack_mv(mvx, mvy));
         }
-    }
-}
-
-// ---------------------------------------------------------------------------
-struct ResolveSmem {
-    SubpelScratch sp[8];
-    alignas(16) unsigned char cur[8][256];
-    long long red_total[8];
-    int red_count[8];
-};
-
-__device__ __forceinline__ void warp_load_cur(unsigned char* cur, const FullArgs& a, int n, int m, int lane)
-{
-    if (lane < 16)
-        *reinterpret_cast<uint4*>(cur + 16 * lane) =
-            *reinterpret_cast<const uint4*>(a.src8 + (size_t)(m + lane) * a.W + n);
-    __syncwarp();
-}
-
-// One macroblock's dependent tail for a given prediction (Full.cpp:368-380,
-// 401-446 rescan on ties, 452-517 sub-pel when the full-pel winner moved,
-// 532-590 prediction distortion and Lagrangian pick).
-__device__ void evaluate_mb(const FullArgs& a, int k, int px, int py, SubpelScratch& sp, unsigned char* cur, int lane,
-                           int* out_mv, int* out_d)
-{
-    const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
-    warp_load_cur(cur, a, n, m, lane);
-    int mv = a.spec_mv[k];
-    int mvx = mv_x(mv), mvy = mv_y(mv);
-    int minD = a.spec_min[k];
-    const int zd = a.spec_zero[k];
-    if (a.spec_flags[k] & FLAG_TIE) {
-        int prx = round_pred(px), pry = round_pred(py);
-        if (prx != 0 || pry != 0) {
-            int xl, xr, yu, yd, mx, my, md, tie;
-            full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
-            scan_table(GlobalTab{a.tables + (size_t)k * TAB * TAB}, xl, xr, yu, yd, prx, pry, lane, &mx, &my, &md,
-                       &tie);
-            int imv = a.spec_imv[k];
-            if (mx != mv_x(imv) || my != mv_y(imv)) {
-                Plane8 rp{a.refp, a.rstride};
-                load_patch22(sp.patch, rp, n + mx, m + my, lane);
-                int qmx, qmy;
-                subpel_refine_warp(sp, cur, lane, &md, &qmx, &qmy);
-                mvx = 4 * mx + qmx;
-                mvy = 4 * my + qmy;
-                minD = md;
-            }
-        }
-    }
-    // prediction clamped to one macroblock outside the picture (Full.cpp:532-541)
-    int pxq = px % 4, pyq = py % 4, px0 = px / 4, py0 = py / 4;
-    if (px0 + n > a.W) px0 = 16;
-    if (px0 + n < -16) px0 = -16;
-    if (py0 + m > a.H) py0 = 16;
-    if (py0 + m < -16) py0 = -16;
-    int pcx = 4 * px0 + pxq, pcy = 4 * py0 + pyq;
-    int fx = pxq < 0 ? pxq + 4 : pxq, fy = pyq < 0 ? pyq + 4 : pyq;
-    int ox = n + px0 + (pxq < 0 ? -1 : 0), oy = m + py0 + (pyq < 0 ? -1 : 0);
-    Plane8 rp{a.refp, a.rstride};
-    load_patch22(sp.patch, rp, ox, oy, lane);
-    int pd = qread_ssd_warp(sp.patch, cur, fx, fy, lane);
-    int pos = best_of3(mvx, mvy, minD, pcx, pcy, pd, zd, a.lambda, 256.0, pcx, pcy);
-    if (pos == 0) {
-        *out_mv = pack_mv(mvx, mvy);
-        *out_d = minD;
-    } else if (pos == 1) {
-        *out_mv = pack_mv(pcx, pcy);
-        *out_d = pd;
-    } else {
-        *out_mv = pack_mv(0, 0);
-        *out_d = zd;
-    }
-}
-
-__global__ void __launch_bounds__(256) k_full_resolve(FullArgs a)
-{
-    __shared__ ResolveSmem S;
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int gwarp = blockIdx.x * 8 + wib, nwarps = gridDim.x * 8;
-    SubpelScratch& sp = S.sp[wib];
-    unsigned char* cur = S.cur[wib];
-    int sweep = 0;
-    bool ok = true;
-    for (;; sweep++) {
-        int changed = 0;
-        for (int k = gwarp; k < a.nmb; k += nwarps) {
-            int px, py;
-            median_pred(a.final_mv, a.slice, k, a.cols, &px, &py);
-            int pp = pack_mv(px, py);
-            if (sweep > 0 && a.pred_used[k] == pp) continue;
-            int fmv, fd;
-            evaluate_mb(a, k, px, py, sp, cur, lane, &fmv, &fd);
-            if (lane == 0) {
-                a.pred_used[k] = pp;
-                a.final_dist[k] = fd;
-                if (__ldcg(a.final_mv + k) != fmv) {
-                    __stcg(a.final_mv + k, fmv);
-                    changed = 1;
-                }
-            }
-            __syncwarp();
-        }
-        // one counter per sweep (zeroed before launch): no reset races
-        if (lane == 0 && changed) atomicAdd(&a.changed[sweep], 1);
-        ok = grid_sync(a.ctrl->bar, &a.ctrl->status, gridDim.x, a.spin_limit);
-        if (!ok) break;
-        if (*((volatile int*)&a.changed[sweep]) == 0) break;
-        if (sweep + 1 >= a.sweep_limit) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.ctrl->status, ST_TIMEOUT);
-            ok = false;
-            break;
-        }
-    }
-    // outputs and the included-distortion average (Full.cpp:581-611)
-    long long tot = 0;
-    int cnt = 0;
-    for (int k = gwarp; k < a.nmb; k += nwarps) {
-        if (lane == 0) {
-            int fmv = __ldcg(a.final_mv + k);
-            a.out_mv[k] = fmv;
-            int d = a.final_dist[k];
-            if (a.out_dist) a.out_dist[k] = d;
-            if (a.incl && a.incl[k]) {
-                tot += d;
-                cnt++;
-            }
-        }
-    }
-    if (lane == 0) {
-        S.red_total[wib] = tot;
-        S.red_count[wib] = cnt;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        long long t = 0;
-        int c = 0;
-        for (int w = 0; w < 8; w++) {
-            t += S.red_total[w];
-            c += S.red_count[w];
-        }
-        if (c) {
-            atomicAdd(reinterpret_cast<unsigned long long*>(&a.ctrl->total), (unsigned long long)t);
-            atomicAdd(&a.ctrl->count, c);
-        }
-    }
-    if (!ok) return;
-    if (!grid_sync(a.ctrl->bar, &a.ctrl->status, gridDim.x, a.spin_limit)) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        long long t = *((volatile long long*)&a.ctrl->total);
-        int c = *((volatile int*)&a.ctrl->count);
-        if (a.out_avg) *a.out_avg = c ? t / c : 0;
-        a.ctrl->sweeps = sweep + 1;
     }
 }
 
@@ -511,12 +282,8 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, const short* d_s
     k_full_search<<<nmb, 128, sizeof(SearchSmem), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     if (ev) VPP_CUDA(cudaEventRecord(ev[2], ctx->stream));
-    {
-        void* params[] = {(void*)&args};
-        VPP_CUDA(cudaLaunchCooperativeKernel((const void*)k_full_resolve, dim3(resolve_grid), dim3(256), params, 0,
-                                             ctx->stream));
-        ctx->launches++;
-    }
+    int rc = full_resolve_launch(ctx, args, resolve_grid);
+    if (rc) return rc;
     if (ev) VPP_CUDA(cudaEventRecord(ev[3], ctx->stream));
     return VPPGPU_OK;
 }
@@ -525,11 +292,10 @@ int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid)
 {
     VPP_CUDA(cudaFuncSetAttribute(k_full_search, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(SearchSmem)));
-    int per_sm = 0;
-    VPP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_full_resolve, 256, 0));
-    if (per_sm < 1) return VPPGPU_ERR_UNSUPPORTED;
+    int cap = 0;
+    int rc = full_resolve_prepare(ctx, &cap);
+    if (rc) return rc;
     int want = (nmb + 7) / 8;
-    int cap = per_sm * ctx->sm_count;
     *resolve_grid = want < cap ? want : cap;
     return VPPGPU_OK;
 }

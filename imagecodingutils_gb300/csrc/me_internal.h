@@ -9,9 +9,13 @@ namespace vppgpu {
 struct MeCtrl {
     int status;      // ST_* bits
     unsigned bar[2]; // grid barrier: arrivals, generation
-    int sweeps;      // resolve sweeps used
+    int sweeps;      // relaxation sweeps used (+1000 when the wavefront finished the frame)
     long long total; // sum of included distortions
     int count;       // number of included macroblocks
+    int converged;   // relaxation reached the fixed point
+    int relax_evals; // MB evaluations in the relaxation sweeps
+    int relax_miss;  // ... of which computed the prediction distortion
+    int wave_miss;   // MBs the wavefront had to evaluate in full
     int pad;
 };
 
@@ -19,17 +23,18 @@ struct FullArgs {
     int W, H, cols, nmb, motion_range, rstride;
     const unsigned char* src8;  // W x H input, unpadded
     const unsigned char* refp;  // padded reference (PAD samples each side)
-    // speculative (prediction-independent) results of k_full_search
-    int* spec_mv;    // packed quarter-pel vector after sub-pel refinement
+    // speculative (prediction-independent) results of k_full_search, per MB:
+    // {packed quarter-pel vector after sub-pel refinement, its distortion,
+    //  zero-vector distortion, flags (FLAG_TIE | neighbour availability)}
+    int4* spec4;
     int* spec_imv;   // packed full-pel winner
-    int* spec_min;   // distortion of spec_mv
-    int* spec_zero;  // distortion of the zero vector
-    int* spec_flags; // FLAG_TIE: the scan met an exact tie
     int* tables;     // 64x64 SSD table per macroblock (kept for tie macroblocks)
-    // fixed-point state of k_full_resolve
+    // resolve state
     int* final_mv;
     int* final_dist;
     int* pred_used;
+    int2* cache;     // KCACHE (prediction, distortion at it) pairs per MB
+    int* dict;       // dominant vectors of the frame (NDICT)
     const int* slice;          // nullable
     const unsigned char* incl; // nullable
     int* out_mv;               // packed short2 per macroblock
@@ -42,7 +47,14 @@ struct FullArgs {
     long long spin_limit;
 };
 
+constexpr int KCACHE = 12;  // cache entries per macroblock
+constexpr int NDICT = 8;    // dictionary vectors
+
 size_t full_search_smem();
+// Launch the prediction-dependent tail (sweep 0, relaxation, dictionary
+// precompute, exact wavefront) of an estimate whose search has run.
+int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid);
+int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap);
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid);
 // ev: nullptr, or 4 events recorded before the pack kernel, before the
 // search kernel, before the resolve kernel and after it.

@@ -38,6 +38,8 @@ constexpr size_t kSpecBytes = 8192;                        // 5 ints per macrobl
 constexpr size_t kStateBytes = 4864;                       // 3 ints per macroblock
 constexpr size_t kCtrlBytes = 256;                         // vppgpu::MeCtrl
 constexpr size_t kChangedBytes = 1792;                     // (N + 2) ints
+constexpr size_t kCacheBytes = 38144;                      // KCACHE (vector, distortion) pairs per macroblock
+constexpr size_t kDictBytes = 256;                         // NDICT vectors
 constexpr size_t kTableBytes = (size_t)VPPGPU_NOALLOC_MAX_MBS * 64 * 64 * 4;
 constexpr size_t kOffSrc = 0;
 constexpr size_t kOffRef = kOffSrc + kSrcBytes;
@@ -45,7 +47,12 @@ constexpr size_t kOffSpec = kOffRef + kRefBytes;
 constexpr size_t kOffState = kOffSpec + kSpecBytes;
 constexpr size_t kOffCtrl = kOffState + kStateBytes;
 constexpr size_t kOffChanged = kOffCtrl + kCtrlBytes;
-constexpr size_t kOffTables = kOffChanged + kChangedBytes;
+constexpr size_t kOffCache = kOffChanged + kChangedBytes;
+constexpr size_t kOffDict = kOffCache + kCacheBytes;
+constexpr size_t kOffTables = kOffDict + kDictBytes;
+static_assert(8 * vppgpu::KCACHE * VPPGPU_NOALLOC_MAX_MBS <= kCacheBytes && 4 * vppgpu::NDICT <= kDictBytes,
+              "resolve caches do not fit");
+static_assert(kOffSpec % 16 == 0 && kOffCache % 16 == 0, "vector records need 16-byte alignment");
 constexpr size_t kScratchBytes = 7u << 20;
 static_assert(kOffTables + kTableBytes <= kScratchBytes, "scratch layout exceeds the array");
 static_assert(sizeof(vppgpu::MeCtrl) <= kCtrlBytes, "control block does not fit");
@@ -135,12 +142,11 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     a.src8 = base + kOffSrc;
     a.refp = base + kOffRef;
     int* spec = (int*)(base + kOffSpec);
-    a.spec_mv = spec;
-    a.spec_imv = spec + nmb;
-    a.spec_min = spec + 2 * nmb;
-    a.spec_zero = spec + 3 * nmb;
-    a.spec_flags = spec + 4 * nmb;
+    a.spec4 = reinterpret_cast<int4*>(spec);
+    a.spec_imv = spec + 4 * nmb;
     a.tables = (int*)(base + kOffTables);
+    a.cache = (int2*)(base + kOffCache);
+    a.dict = (int*)(base + kOffDict);
     int* state = (int*)(base + kOffState);
     a.final_mv = state;
     a.final_dist = state + nmb;

@@ -117,6 +117,12 @@ int vppgpu_me_last_status(vppgpu_me* me);
 /* Number of resolve sweeps the last estimate needed (predictor fixed point). */
 int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps);
 
+/* Counters of the last estimate's prediction-dependent stage: {sweeps,
+ * converged-by-relaxation, relaxation evaluations, of which distortion
+ * computations, MBs the wavefront evaluated in full, status bits, included
+ * MBs, 0}.  Synchronises the context stream.  No vpp counterpart. */
+int vppgpu_me_last_stats(vppgpu_me* me, int* stats8);
+
 /* Observability, no vpp counterpart.  While enabled, every estimate records
  * CUDA events around its three kernels on the context stream (no host
  * synchronisation); vppgpu_me_timing synchronises and returns how many
