@@ -15,9 +15,14 @@ struct vppgpu_me {
     short* d_ref16;
     unsigned char* d_src8;
     unsigned char* d_refp;
+    unsigned char* d_hpel;  // b, h, j planes of the padded reference
+    size_t plane_size;
+    void* d_wave_scratch;
+    vppgpu::WaveRec* d_wave_rec;
+    int* d_wave_choice;
     int* spec;  // 5 * nmb: {vector, distortion, zero distortion, flags} per MB, then full-pel winners
     int* tables;
-    int2* cache;
+    int4* cache;
     int* dict;
     int* state; // 3 * nmb: final_mv, final_dist, pred_used
     int* d_out_mv;
@@ -83,6 +88,10 @@ void me_free(vppgpu_me* me)
     cudaFree(me->d_ref16);
     cudaFree(me->d_src8);
     cudaFree(me->d_refp);
+    cudaFree(me->d_hpel);
+    cudaFree(me->d_wave_scratch);
+    cudaFree(me->d_wave_rec);
+    cudaFree(me->d_wave_choice);
     cudaFree(me->spec);
     cudaFree(me->tables);
     cudaFree(me->cache);
@@ -119,6 +128,11 @@ vppgpu::FullArgs full_args(vppgpu_me* me, const unsigned char* incl, const int* 
     a.rstride = me->rstride;
     a.src8 = me->d_src8;
     a.refp = me->d_refp;
+    a.hpel = me->d_hpel;
+    a.plane_size = me->plane_size;
+    a.wave_scratch = me->d_wave_scratch;
+    a.wave_rec = me->d_wave_rec;
+    a.wave_choice = me->d_wave_choice;
     a.spec4 = reinterpret_cast<int4*>(me->spec);
     a.spec_imv = me->spec + 4 * (size_t)me->nmb;
     a.cache = me->cache;
@@ -188,8 +202,11 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     me->sweep_limit = me->nmb + 2;
     size_t npix = (size_t)width * height;
     size_t npad = (size_t)me->rstride * (height + 2 * vppgpu::PAD);
+    me->plane_size = npad;
     if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) || (rc = dalloc(&me->d_src8, npix)) ||
-        (rc = dalloc(&me->d_refp, npad)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
+        (rc = dalloc(&me->d_refp, npad)) || (rc = dalloc(&me->d_hpel, 3 * npad)) ||
+        (rc = dalloc((unsigned char**)&me->d_wave_scratch, vppgpu::full_wave_scratch_bytes())) ||
+        (rc = dalloc(&me->d_wave_rec, me->nmb)) || (rc = dalloc(&me->d_wave_choice, me->nmb)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
         (rc = dalloc(&me->tables, (size_t)me->nmb * 64 * 64)) || (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
         (rc = dalloc(&me->cache, (size_t)me->nmb * vppgpu::KCACHE)) || (rc = dalloc(&me->dict, vppgpu::NDICT)) ||
         (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||

@@ -119,16 +119,20 @@ __device__ __forceinline__ void subpel_planes(SubpelScratch& s, int lane)
 
 // cur: 16x16 input block (row stride 16).  Enters with the full-pel minimum
 // in *min_d; leaves with the refined minimum and quarter offsets (qmx, qmy).
+// kLean: loops kept rolled, for callers where registers matter more than
+// speed (the rare tie rescans inside the prediction-dependent kernels).
+template <bool kLean = false>
 __device__ __forceinline__ void subpel_refine_warp(SubpelScratch& s, const unsigned char* cur, int lane, int* min_d,
                                                    int* qmx, int* qmy)
 {
     subpel_planes(s, lane);
     int best = *min_d, hmx = 0, hmy = 0;
     // lane handles pixels lane + 32*t, t = 0..7
+#pragma unroll(kLean ? 1 : 8)
     for (int k = 0; k < 8; k++) {
         int qx = 2 * kSubX[k], qy = 2 * kSubY[k];
         int acc = 0;
-#pragma unroll
+#pragma unroll(kLean ? 1 : 8)
         for (int t = 0; t < 8; t++) {
             int px = lane + 32 * t, r = px >> 4, c = px & 15;
             int d = (int)cur[px] - lattice(s, 4 * r + qy, 4 * c + qx);
@@ -142,10 +146,11 @@ __device__ __forceinline__ void subpel_refine_warp(SubpelScratch& s, const unsig
         }
     }
     int bx = hmx, by = hmy;
+#pragma unroll(kLean ? 1 : 8)
     for (int k = 0; k < 8; k++) {
         int sx = kSubX[k], sy = kSubY[k];
         int acc = 0;
-#pragma unroll
+#pragma unroll(kLean ? 1 : 8)
         for (int t = 0; t < 8; t++) {
             int px = lane + 32 * t, r = px >> 4, c = px & 15;
             int d = (int)cur[px] - quarter_sample(s, 4 * r + hmy, 4 * c + hmx, sy, sx);
@@ -410,30 +415,37 @@ static __device__ __noinline__ int best_of3(int bx, int by, int bd, int px, int 
     return pos;
 }
 
-// Same decision, float first: each float cost is within a few ulp of the
-// exact real value and the double costs within 2^-50 relative, so when every
-// compared pair differs by more than 2^-18 relative both orderings agree with
-// the exact one.  Near-ties (including exact ones) take the double path.
+// Same decision without FP64 in the common cases.  Two costs with the same
+// sqrt argument differ only in D/norm, and D/256 is exact; with |lambda| <
+// 2^20 every sum stays below 2^40, where costs 1/256 apart never round
+// together, so their double order is the order of the integers D.  This
+// covers the most frequent near-tie, the prediction slot against a searched
+// vector equal to it.  Other pairs compare in float: each float cost is
+// within a few ulp of the exact real value and the double costs within 2^-50
+// relative, so when a pair differs by more than 2^-18 relative both orderings
+// agree with the exact one; closer pairs take the double path.
 __device__ __forceinline__ int best_of3_fast(int bx, int by, int bd, int px, int py, int pd, int zd, double lambda,
                                              int xref, int yref)
 {
+    const int m0 = (bx - xref) * (bx - xref) + (by - yref) * (by - yref);
+    const int m1 = (px - xref) * (px - xref) + (py - yref) * (py - yref);
+    const int m2 = xref * xref + yref * yref;
     const float lf = (float)lambda, inv = 1.0f / 256.0f;
-    float m0 = (float)((bx - xref) * (bx - xref) + (by - yref) * (by - yref));
-    float m2 = (float)(xref * xref + yref * yref);
-    float c0 = (float)bd * inv + lf * sqrtf(m0);
-    float c1 = (float)pd * inv;  // the prediction is the reference vector itself
-    float c2 = (float)zd * inv + lf * sqrtf(m2);
-    auto close = [](float a, float b) { return fabsf(a - b) <= 4e-6f * fmaxf(fabsf(a), fabsf(b)) + 1e-30f; };
-    if (close(c0, c1) || close(c0, c2) || close(c1, c2))
-        return best_of3(bx, by, bd, px, py, pd, zd, lambda, 256.0, xref, yref);
-    int pos = 0;
-    float c = c0;
-    if (c1 < c) {
-        c = c1;
-        pos = 1;
-    }
-    if (c2 < c) pos = 2;
-    return pos;
+    const float c0 = (float)bd * inv + lf * sqrtf((float)m0);
+    const float c1 = (float)pd * inv + lf * sqrtf((float)m1);
+    const float c2 = (float)zd * inv + lf * sqrtf((float)m2);
+    bool slow = false;
+    const bool small_lambda = fabs(lambda) < 1048576.0;
+    // strict "cost a < cost b" in the double arithmetic of best_of3
+    auto less = [&](int da, int ma, float ca, int db, int mb, float cb) {
+        if (ma == mb && small_lambda) return da < db;
+        if (fabsf(ca - cb) <= 4e-6f * fmaxf(fabsf(ca), fabsf(cb)) + 1e-30f) slow = true;
+        return ca < cb;
+    };
+    int pos = less(pd, m1, c1, bd, m0, c0) ? 1 : 0;
+    const bool z = pos == 0 ? less(zd, m2, c2, bd, m0, c0) : less(zd, m2, c2, pd, m1, c1);
+    if (slow) return best_of3(bx, by, bd, px, py, pd, zd, lambda, 256.0, xref, yref);
+    return z ? 2 : pos;
 }
 
 // ---------------------------------------------------------------------------

@@ -21,14 +21,11 @@
 //                   looked at), and runs the sub-pel stages.  None of this
 //                   depends on the predictor except exact ties in the scan,
 //                   which are flagged and the table kept for a rescan.
-//   k_full_resolve  cooperative kernel.  A macroblock's final vector depends
-//                   on its left/above/above-right neighbours' final vectors
-//                   through the median predictor (a DAG in raster order).
-//                   Each sweep recomputes every macroblock whose prediction
-//                   changed, in place; a sweep with no change is the unique
-//                   fixed point, i.e. the sequential result.  On a DAG this
-//                   needs at most (longest dependency chain + 2) sweeps and
-//                   in practice a handful, instead of a ~250-step wavefront.
+//   k_full_halfpel  b / h / j half-pel planes of the padded reference, used
+//                   by every distortion at a predicted vector.
+//   resolve         (me_full_resolve.cu) the prediction-dependent tail:
+//                   median prediction, tie rescans, prediction distortion
+//                   and the Lagrangian pick, in the reference's raster order.
 #include <string.h>
 
 #include "me_full_common.cuh"
@@ -48,6 +45,7 @@ struct SearchSmem {
     } u;
     int a2;
     int state[4];  // mx, my, minD, flags broadcast
+    int tie_nev[TIE_RUNS];
 };
 
 // ---------------------------------------------------------------------------
@@ -86,6 +84,61 @@ __global__ void __launch_bounds__(256) k_full_pack(const short* __restrict__ src
         }
     }
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(status, ST_PIXEL_RANGE);
+}
+
+// ---------------------------------------------------------------------------
+// Half-pel planes of the padded reference (the H.264 6-tap b, h and j
+// samples QuarterRead combines, OverlayMem2Dv2.cpp): b(x,y) between x and
+// x+1, h(x,y) between y and y+1, j from the unrounded vertical taps.  Four
+// samples per thread; tap coordinates are clamped to the padded buffer, which
+// only changes samples within three of its border, never read (a prediction
+// stays within 17 samples of the picture, the padding is 48).
+__device__ __forceinline__ unsigned char clip_tap(int v, int round, int shift)
+{
+    return (unsigned char)clip255((v + round) >> shift);
+}
+
+__global__ void __launch_bounds__(256) k_full_halfpel(const unsigned char* __restrict__ refp, int rstride, int PW,
+                                                      int PH, unsigned char* __restrict__ hpel, size_t plane_size)
+{
+    const int qw = PW / 4;
+    const long long total = (long long)qw * PH;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int Y = (int)(i / qw), X = 4 * (int)(i - (long long)Y * qw);
+        // columns X-4 .. X+7 of rows Y-2 .. Y+3 as three words per row
+        int g[6][12];
+#pragma unroll
+        for (int dy = 0; dy < 6; dy++) {
+            const int yy = min(max(Y - 2 + dy, 0), PH - 1);
+            const unsigned* row = reinterpret_cast<const unsigned*>(refp + (size_t)yy * rstride);
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                const int wq = min(max(X / 4 - 1 + q, 0), qw - 1);
+                const unsigned w = __ldg(row + wq);
+#pragma unroll
+                for (int b = 0; b < 4; b++) g[dy][4 * q + b] = (w >> (8 * b)) & 0xff;
+            }
+        }
+        // unrounded vertical taps at columns X-2 .. X+6 (g index 2 .. 10)
+        int v[9];
+#pragma unroll
+        for (int c = 0; c < 9; c++) v[c] = tap6(g[0][c + 2], g[1][c + 2], g[2][c + 2], g[3][c + 2], g[4][c + 2], g[5][c + 2]);
+        unsigned ob = 0, oh = 0, oj = 0;
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            const int x = t + 4;  // g index of column X + t
+            const int bv = tap6(g[2][x - 2], g[2][x - 1], g[2][x], g[2][x + 1], g[2][x + 2], g[2][x + 3]);
+            ob |= (unsigned)clip_tap(bv, 16, 5) << (8 * t);
+            oh |= (unsigned)clip_tap(v[t + 2], 16, 5) << (8 * t);
+            const int jv = tap6(v[t], v[t + 1], v[t + 2], v[t + 3], v[t + 4], v[t + 5]);
+            oj |= (unsigned)clip_tap(jv, 512, 10) << (8 * t);
+        }
+        const size_t o = (size_t)Y * rstride + X;
+        *reinterpret_cast<unsigned*>(hpel + o) = ob;
+        *reinterpret_cast<unsigned*>(hpel + plane_size + o) = oh;
+        *reinterpret_cast<unsigned*>(hpel + 2 * plane_size + o) = oj;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -218,9 +271,11 @@ __global__ void __launch_bounds__(128, 4) k_full_search(FullArgs a)
     }
     __syncthreads();
 
-    // 5. sequential scan replay (warp 0)
+    // 5. row minima, then the sequential scan replay (warp 0)
     int xl, xr, yu, yd;
     full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
+    table_row_minima(S.tab, xl, xr, yu, yd, warp, 4, lane);
+    __syncthreads();
     if (warp == 0) {
         int mx, my, minD, tie;
         scan_table(SmemTab{S.tab}, xl, xr, yu, yd, 0, 0, lane, &mx, &my, &minD, &tie);
@@ -236,7 +291,7 @@ __global__ void __launch_bounds__(128, 4) k_full_search(FullArgs a)
     int minD = S.state[2];
     if (flags & FLAG_TIE) {
         int* dst = a.tables + (size_t)k * TAB * TAB;
-        for (int i = tid; i < TAB * TAB / 4; i += 128)
+        for (int i = tid; i < TIE_ROW * TAB / 4; i += 128)
             __stcg(reinterpret_cast<int4*>(dst) + i, reinterpret_cast<const int4*>(&S.tab[0][0])[i]);
     }
     const int zero_d = S.tab[RMAX][RMAX + 1];
@@ -252,12 +307,54 @@ __global__ void __launch_bounds__(128, 4) k_full_search(FullArgs a)
         __syncwarp();
         int qmx, qmy;
         subpel_refine_warp(sp, S.cur, lane, &minD, &qmx, &qmy);
+        const int qmv = pack_mv(4 * mx + qmx, 4 * my + qmy);
+        int deep = 0;
+        if (flags & FLAG_TIE) {
+            // 7. tie tree: the runs reachable by some prediction
+            int* tree = a.tables + (size_t)k * TAB * TAB + TIE_ROW * TAB;
+            for (int p = 0; p < TIE_RUNS; p++) {
+                if (p > 0) {
+                    const int hb = 31 - __clz(p);
+                    if (S.tie_nev[p & ~(1 << hb)] <= hb) {  // tie hb never met on that path
+                        if (lane == 0) S.tie_nev[p] = 0;
+                        __syncwarp();
+                        continue;
+                    }
+                }
+                int rmx, rmy, rmin, rt, nev, ev[TIE_DEPTH] = {0, 0, 0};
+                scan_table_t<true>(SmemTab{S.tab}, xl, xr, yu, yd, 0, 0, p, lane, &rmx, &rmy, &rmin, &rt, &nev, ev);
+                int rq = qmv, rqmin = minD;
+                if (rmx != mx || rmy != my) {
+                    __syncwarp();
+                    for (int i = lane; i < 22 * 22; i += 32) {
+                        int r = i / 22, c = i - r * 22;
+                        sp.patch[r][c] = S.win[rmy + 34 - 3 + r][rmx + 48 - 3 + c];
+                    }
+                    __syncwarp();
+                    int sx, sy;
+                    subpel_refine_warp(sp, S.cur, lane, &rmin, &sx, &sy);
+                    rq = pack_mv(4 * rmx + sx, 4 * rmy + sy);
+                    rqmin = rmin;
+                }
+                if (lane == 0) {
+                    int* run = tree + p * (int)(sizeof(TieRun) / sizeof(int));
+                    run[0] = ev[0];
+                    run[1] = ev[1];
+                    run[2] = ev[2];
+                    run[3] = nev;
+                    run[4] = rq;
+                    run[5] = rqmin;
+                    S.tie_nev[p] = nev < 0 ? TIE_DEPTH + 1 : nev;
+                }
+                deep |= nev < 0;
+                __syncwarp();
+            }
+        }
         if (lane == 0) {
-            int mvx = 4 * mx + qmx, mvy = 4 * my + qmy;
             int av = neighbour_mask(a.slice, k, a.cols, a.nmb / a.cols);
-            a.spec4[k] = make_int4(pack_mv(mvx, mvy), minD, zero_d, flags | av);
+            a.spec4[k] = make_int4(qmv, minD, zero_d, flags | av | (deep ? FLAG_DEEP : 0));
             a.spec_imv[k] = pack_mv(mx, my);
-            __stcg(a.final_mv + k, pack_mv(mvx, mvy));
+            __stcg(a.final_mv + k, qmv);
         }
     }
 }
@@ -276,6 +373,15 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, const short* d_s
         if (grid > ctx->sm_count * 16) grid = ctx->sm_count * 16;
         k_full_pack<<<grid, 256, 0, ctx->stream>>>(d_src16, d_ref16, args.W, args.H, (unsigned char*)args.src8,
                                                    (unsigned char*)args.refp, args.rstride, &args.ctrl->status);
+        VPP_CHECK_LAUNCH(ctx);
+    }
+    {
+        const int PW = args.W + 2 * PAD, PH = args.H + 2 * PAD;
+        long long work = (long long)(PW / 4) * PH;
+        int grid = (int)((work + 255) / 256);
+        if (grid > ctx->sm_count * 16) grid = ctx->sm_count * 16;
+        k_full_halfpel<<<grid, 256, 0, ctx->stream>>>(args.refp, args.rstride, PW, PH, (unsigned char*)args.hpel,
+                                                      args.plane_size);
         VPP_CHECK_LAUNCH(ctx);
     }
     if (ev) VPP_CUDA(cudaEventRecord(ev[1], ctx->stream));

@@ -14,7 +14,27 @@ constexpr int WROWS = 84;      // window rows m-34 .. m+49
 constexpr int WSTRIDE = 112;   // window cols n-48 .. n+63
 constexpr int H2STRIDE = 81;   // odd stride: conflict-free column walks
 constexpr int TAB = 64;        // SSD table is TAB x TAB ints
-constexpr int FLAG_TIE = 1;
+constexpr int FLAG_TIE = 1;   // the scan met an exact tie: its result may depend on the prediction
+constexpr int FLAG_DEEP = 32; // ... and more ties than the tie tree holds: rescan the kept table
+
+// Tie tree of a FLAG_TIE macroblock.  The prediction enters the integer
+// search only through exact ties (Full.cpp:424-441): tie e is decided by
+// whether the new candidate is not farther from the rounded prediction than
+// the running best.  Run p of the tree is the scan with tie e decided by bit
+// e of p; it keeps the geometry of its ties and its result after the sub-pel
+// stage, so the result for any prediction is a walk down the runs: decide
+// tie 0 with run 0's geometry, tie 1 with the geometry of the run that made
+// decision 0, and so on.  Stored in the unused last row of the MB's table.
+constexpr int TIE_DEPTH = 3;
+constexpr int TIE_RUNS = 1 << TIE_DEPTH;
+struct TieRun {
+    int ev[TIE_DEPTH];  // per tie: running best (x, y), candidate (x, y) as signed bytes
+    int nev;            // ties met (<= TIE_DEPTH), -1 for more
+    int qmv;            // packed quarter-pel vector after sub-pel refinement
+    int qmin;           // its distortion
+};
+constexpr int TIE_ROW = 63;  // table row (ii = 2*RMAX + 1) free for the tree
+static_assert(sizeof(TieRun) * TIE_RUNS <= 64 * sizeof(int), "tie tree exceeds one table row");
 
 
 // GetMotionRange with zero offset (Full.cpp:1029-1081).
@@ -35,19 +55,51 @@ __device__ __forceinline__ void full_range(int n, int m, int W, int H, int motio
 // Sequential raster replay of the integer search over tab (ii = i+31,
 // jj = j+32), one warp.  prx/pry: rounded prediction used at ties.  Returns
 // the winner and sets *tie when any exact tie was decided.
-template <typename TabT>
-__device__ __forceinline__ void scan_table(const TabT& tab, int xl, int xr, int yu, int yd, int prx, int pry,
-                                           int lane, int* omx, int* omy, int* omin, int* tie)
+//
+// Column 0 of the table (jj = 0, outside every range) holds each row's
+// minimum over the searched columns.  A row whose minimum is above the
+// running minimum cannot accept any candidate (acceptance needs d <= min and
+// the minimum only falls), so only the rows that can are visited, found with
+// a ballot over the row minima.
+//
+// kForced: instead of the distance rule, exact tie e (in scan order) takes
+// bit e of `path`; the geometry of the first TIE_DEPTH ties goes to ev[] and
+// their count to *nev (-1 when there were more).
+template <bool kForced, typename TabT>
+__device__ __forceinline__ void scan_table_t(const TabT& tab, int xl, int xr, int yu, int yd, int prx, int pry,
+                                             int path, int lane, int* omx, int* omy, int* omin, int* tie, int* nev,
+                                             int* ev)
 {
+    int ne = 0;
+    constexpr int kNone = 0x7fffffff;  // above any 16x16 SSD
     int minD = tab(RMAX, RMAX + 1), mx = 0, my = 0, t = 0;
-    for (int i = yu; i <= yd; i++) {
-        for (int base = xl; base <= xr; base += 32) {
-            int j = base + lane;
-            bool valid = (j <= xr) && !(i == 0 && j == 0);
-            int d = valid ? tab(i + RMAX, j + RMAX + 1) : 0x7fffffff;
+    const int rm0 = yu + lane <= yd ? tab(yu + lane + RMAX, 0) : kNone;
+    const int rm1 = yu + lane + 32 <= yd ? tab(yu + lane + 32 + RMAX, 0) : kNone;
+    int done = 0;  // rows yu .. yu+done-1 are behind the scan
+    while (true) {
+        const unsigned m0 = __ballot_sync(0xffffffffu, rm0 <= minD && lane >= done);
+        const unsigned m1 = __ballot_sync(0xffffffffu, rm1 <= minD && lane + 32 >= done);
+        if (!m0 && !m1) break;
+        const int off = m0 ? __ffs(m0) - 1 : 32 + __ffs(m1) - 1;
+        const int i = yu + off;
+        done = off + 1;
+        int v[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int j = xl + 32 * h + lane;
+            const bool valid = j <= xr && !(i == 0 && j == 0);
+            v[h] = valid ? tab(i + RMAX, j + RMAX + 1) : kNone;
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int base = xl + 32 * h;
+            if (base > xr) break;
+            const int j = base + lane;
+            const int d = v[h];
             unsigned pending = 0xffffffffu;
             while (true) {
-                bool ok = valid && d <= minD && (i + my >= yu) && (i + my <= yd) && (j + mx >= xl) && (j + mx <= xr);
+                bool ok = d != kNone && d <= minD && (i + my >= yu) && (i + my <= yd) && (j + mx >= xl) &&
+                          (j + mx <= xr);
                 unsigned m = __ballot_sync(0xffffffffu, ok) & pending;
                 if (!m) break;
                 int f = __ffs(m) - 1;
@@ -56,8 +108,17 @@ __device__ __forceinline__ void scan_table(const TabT& tab, int xl, int xr, int 
                 bool accept = true;
                 if (df == minD) {
                     t = 1;
-                    int cx = mx - prx, cy = my - pry, nx = jf - prx, ny = i - pry;
-                    accept = (cy * cy + cx * cx) - (ny * ny + nx * nx) >= 0;
+                    if (kForced) {
+                        const int g = (mx & 0xff) | ((my & 0xff) << 8) | ((jf & 0xff) << 16) | ((i & 0xff) << 24);
+                        if (ne == 0) ev[0] = g;
+                        if (ne == 1) ev[1] = g;
+                        if (ne == 2) ev[2] = g;
+                        accept = ne < TIE_DEPTH ? ((path >> ne) & 1) != 0 : true;
+                        ne++;
+                    } else {
+                        int cx = mx - prx, cy = my - pry, nx = jf - prx, ny = i - pry;
+                        accept = (cy * cy + cx * cx) - (ny * ny + nx * nx) >= 0;
+                    }
                 }
                 if (accept) {
                     minD = df;
@@ -73,6 +134,31 @@ __device__ __forceinline__ void scan_table(const TabT& tab, int xl, int xr, int 
     *omy = my;
     *omin = minD;
     *tie = t;
+    if (kForced) *nev = ne <= TIE_DEPTH ? ne : -1;
+}
+
+template <typename TabT>
+__device__ __forceinline__ void scan_table(const TabT& tab, int xl, int xr, int yu, int yd, int prx, int pry,
+                                           int lane, int* omx, int* omy, int* omin, int* tie)
+{
+    scan_table_t<false>(tab, xl, xr, yu, yd, prx, pry, 0, lane, omx, omy, omin, tie, nullptr, nullptr);
+}
+
+// Row minima of the searched columns into column 0 (see scan_table), one
+// warp per row.
+__device__ __forceinline__ void table_row_minima(int (*tab)[TAB], int xl, int xr, int yu, int yd, int warp,
+                                                 int nwarps, int lane)
+{
+    for (int i = yu + warp; i <= yd; i += nwarps) {
+        int* row = tab[i + RMAX];
+        const int j0 = xl + lane, j1 = xl + 32 + lane;
+        int v = j0 <= xr ? row[j0 + RMAX + 1] : 0x7fffffff;
+        if (j1 <= xr) v = min(v, row[j1 + RMAX + 1]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+        __syncwarp();
+        if (lane == 0) row[0] = v;
+    }
 }
 
 struct SmemTab {
@@ -84,6 +170,12 @@ struct GlobalTab {
     __device__ int operator()(int r, int c) const { return __ldcg(t + r * TAB + c); }
 };
 
+// Per-warp scratch of the prediction-dependent stage: the sub-pel stage of a
+// tie rescan and the macroblock's input samples.
+struct WarpScratch {
+    SubpelScratch sp;
+    alignas(16) unsigned char cur[256];
+};
 
 }  // namespace full
 }  // namespace vppgpu

@@ -7,21 +7,29 @@
 // prediction depends on the left / above / above-right (else above-left)
 // neighbours' final vectors: a DAG in raster order.
 //
-//   k_full_sweep0    every MB at once, prediction from the current vectors
-//                    (initially the searched ones); caches the distortion at
-//                    the prediction it saw.
-//   k_full_relax     cooperative: up to kRelaxSweeps sweeps re-evaluating the
-//                    MBs whose prediction changed (cache first).  A sweep
-//                    without change is the unique fixed point of the DAG,
-//                    i.e. the sequential result; most frames stop here.
-//                    Otherwise (long copy chains: the prediction wins and is
-//                    copied along rows and columns) block 0 builds a
-//                    dictionary of the frame's dominant vectors.
-//   k_full_precompute  distortion of every MB at every dictionary vector.
-//   k_full_wave      one CTA: the exact sequential order as anti-diagonal
-//                    steps (t = col + 2*row), vectors in shared memory,
-//                    cached distortions prefetched two diagonals ahead with
-//                    cp.async; misses are computed by whole warps.
+// Every evaluation of a macroblock at a prediction is kept as a record
+// {prediction, distortion at it, final vector, final distortion} in a small
+// per-MB cache, so a later visit with the same prediction is a lookup.  The
+// distortion at a prediction reads the frame's precomputed half-pel planes
+// (two byte loads per sample at most).
+//
+//   k_full_sweep0      every MB at once, prediction from the current vectors
+//                      (initially the searched ones).
+//   k_full_relax       cooperative: up to kRelaxSweeps sweeps re-evaluating
+//                      the MBs whose prediction changed.  A sweep without
+//                      change is the unique fixed point of the DAG, i.e. the
+//                      sequential result.  Otherwise (long copy chains: the
+//                      prediction wins and is copied along rows and columns)
+//                      block 0 builds a dictionary of the frame's dominant
+//                      vectors.
+//   k_full_precompute  records of every MB at every dictionary vector.
+//   k_full_wave        one CTA replays the exact sequential order, pipelined
+//                      by rows: warp w owns rows w, w+32, ...; a row advances
+//                      one MB per step once the row above has finished the
+//                      MB above-right, signalled through shared-memory
+//                      progress counters.  A step is a median, a key match
+//                      against the MB's records (prefetched with cp.async)
+//                      and, on a miss only, a full evaluation by the warp.
 #include "me_full_common.cuh"
 
 namespace vppgpu {
@@ -33,13 +41,7 @@ constexpr int kRelaxSweeps = 8;
 constexpr int kCacheRelax = 1;      // entries 1..3 round robin in relaxation
 constexpr int kCacheDict = 4;       // entries 4..11 dictionary
 
-struct WarpScratch {
-    union {
-        SubpelScratch sp;
-        PdScratch pd;
-    } u;
-    alignas(16) unsigned char cur[256];
-};
+__device__ __forceinline__ int4 empty_record() { return make_int4(kEmpty, 0, 0, 0); }
 
 __device__ __forceinline__ void load_cur(unsigned char* cur, const FullArgs& a, int n, int m, int lane)
 {
@@ -72,78 +74,156 @@ __device__ __forceinline__ PredGeom pred_geom(int n, int m, int W, int H, int px
     return g;
 }
 
-// Distortion at the prediction, one warp (cur already loaded).
-__device__ __forceinline__ int warp_pred_distortion(const FullArgs& a, const PredGeom& g, WarpScratch& ws, int lane)
+// Eight consecutive bytes from any address: three aligned words and two
+// funnel shifts (little endian).
+__device__ __forceinline__ uint2 load8(const unsigned char* p)
 {
-    Plane8 rp{a.refp, a.rstride};
-    load_patch22(ws.u.pd.patch, rp, g.ox, g.oy, lane);
-    return pd_planar_warp(ws.u.pd, ws.cur, g.fx, g.fy, lane);
+    const uintptr_t u = reinterpret_cast<uintptr_t>(p);
+    const unsigned* w = reinterpret_cast<const unsigned*>(u & ~(uintptr_t)3);
+    const unsigned sh = (unsigned)(u & 3) * 8;
+    const unsigned w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2);
+    return make_uint2(__funnelshift_r(w0, w1, sh), __funnelshift_r(w1, w2, sh));
 }
 
-// Exact-tie macroblocks: the integer scan depends on the rounded prediction;
-// replay it from the kept table and redo the sub-pel stage if the full-pel
-// winner moved.  Rare, so kept out of line.
-__device__ __noinline__ void tie_path(const FullArgs& a, int k, int px, int py, WarpScratch& ws, int lane, int* mvx,
-                                      int* mvy, int* minD)
+// Distortion at the prediction, one warp: QuarterRead's sixteen cases
+// (OverlayMem2Dv2::QuarterRead) as one sample of the full-pel, b, h or j
+// plane, or the rounded mean of two.  Lane l covers row l/2, columns
+// 8*(l&1) .. +7; squared differences with dp4a on per-byte |differences|.
+__device__ __forceinline__ int plane_pred_distortion(const FullArgs& a, int n, int m, const PredGeom& g, int lane)
+{
+    const int r = lane >> 1, c0 = (lane & 1) * 8, st = a.rstride;
+    const size_t o = (size_t)(g.oy + r + PAD) * st + (size_t)(g.ox + c0 + PAD);
+    const unsigned char* G = a.refp;
+    const unsigned char* Bp = a.hpel;
+    const unsigned char* Hp = a.hpel + a.plane_size;
+    const unsigned char* Jp = a.hpel + 2 * a.plane_size;
+    const unsigned char *p1 = G + o, *p2 = G + o;
+    bool two = true;
+    switch (g.fx | (g.fy << 2)) {
+    case 0: two = false; break;                          // G
+    case 2: p1 = Bp + o; two = false; break;             // b
+    case 8: p1 = Hp + o; two = false; break;             // h
+    case 10: p1 = Jp + o; two = false; break;            // j
+    case 1: p2 = Bp + o; break;                          // a = (G + b)
+    case 3: p1 = G + o + 1; p2 = Bp + o; break;          // c = (G[x+1] + b)
+    case 4: p2 = Hp + o; break;                          // d = (G + h)
+    case 12: p1 = G + o + st; p2 = Hp + o; break;        // n = (G[y+1] + h)
+    case 6: p1 = Jp + o; p2 = Bp + o; break;             // f = (j + b)
+    case 14: p1 = Jp + o; p2 = Bp + o + st; break;       // q = (j + b[y+1])
+    case 9: p1 = Jp + o; p2 = Hp + o; break;             // i = (j + h)
+    case 11: p1 = Jp + o; p2 = Hp + o + 1; break;        // k = (j + h[x+1])
+    case 5: p1 = Bp + o; p2 = Hp + o; break;             // e = (b + h)
+    case 7: p1 = Bp + o; p2 = Hp + o + 1; break;         // g = (b + h[x+1])
+    case 13: p1 = Hp + o; p2 = Bp + o + st; break;       // p = (h + b[y+1])
+    default: p1 = Hp + o + 1; p2 = Bp + o + st; break;   // r = (h[x+1] + b[y+1])
+    }
+    uint2 v = load8(p1);
+    if (two) {
+        const uint2 w = load8(p2);
+        v.x = __vavgu4(v.x, w.x);  // (p + q + 1) >> 1 per byte
+        v.y = __vavgu4(v.y, w.y);
+    }
+    const uint2 cur = __ldg(reinterpret_cast<const uint2*>(a.src8 + (size_t)(m + r) * a.W + n + c0));
+    const unsigned d0 = __vabsdiffu4(cur.x, v.x), d1 = __vabsdiffu4(cur.y, v.y);
+    return warp_sum((int)__dp4a(d0, d0, __dp4a(d1, d1, 0u)));
+}
+
+// Exact-tie macroblocks: the integer scan depends on the rounded prediction.
+// Walk the tie tree the search kernel kept (one load per lane), or, for the
+// rare macroblock with more ties than the tree holds, replay the scan from
+// the kept table and redo the sub-pel stage if the full-pel winner moved.
+// Kept out of line.
+__device__ __noinline__ void tie_path(const FullArgs& a, int k, int px, int py, int flags, WarpScratch& ws,
+                                      int lane, int* mvx, int* mvy, int* minD)
 {
     int prx = round_pred(px), pry = round_pred(py);
     if (prx == 0 && pry == 0) return;  // the search kernel already decided ties with (0,0)
+    const int* tab = a.tables + (size_t)k * TAB * TAB;
+    if (!(flags & FLAG_DEEP)) {
+        constexpr int RW = sizeof(TieRun) / sizeof(int), TW = TIE_RUNS * RW;
+        const int* tree = tab + TIE_ROW * TAB;
+        const int t0 = __ldcg(tree + lane);
+        const int t1 = lane < TW - 32 ? __ldcg(tree + 32 + lane) : 0;
+        auto get = [&](int idx) {
+            const int v0 = __shfl_sync(0xffffffffu, t0, idx & 31), v1 = __shfl_sync(0xffffffffu, t1, idx & 31);
+            return idx < 32 ? v0 : v1;
+        };
+        int path = 0;
+        for (int e = 0; e < TIE_DEPTH; e++) {
+            if (e >= get(path * RW + TIE_DEPTH)) break;
+            const int g = get(path * RW + e);
+            const int cx = (int)(signed char)(g & 0xff) - prx, cy = (int)(signed char)((g >> 8) & 0xff) - pry;
+            const int nx = (int)(signed char)((g >> 16) & 0xff) - prx, ny = (int)(signed char)((g >> 24) & 0xff) - pry;
+            if ((cy * cy + cx * cx) - (ny * ny + nx * nx) >= 0) path |= 1 << e;
+        }
+        const int q = get(path * RW + TIE_DEPTH + 1);
+        *mvx = mv_x(q);
+        *mvy = mv_y(q);
+        *minD = get(path * RW + TIE_DEPTH + 2);
+        return;
+    }
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
     int xl, xr, yu, yd, mx, my, md, tie;
     full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
-    scan_table(GlobalTab{a.tables + (size_t)k * TAB * TAB}, xl, xr, yu, yd, prx, pry, lane, &mx, &my, &md, &tie);
+    scan_table(GlobalTab{tab}, xl, xr, yu, yd, prx, pry, lane, &mx, &my, &md, &tie);
     int imv = a.spec_imv[k];
     if (mx != mv_x(imv) || my != mv_y(imv)) {
+        load_cur(ws.cur, a, n, m, lane);
         Plane8 rp{a.refp, a.rstride};
-        load_patch22(ws.u.sp.patch, rp, n + mx, m + my, lane);
+        load_patch22(ws.sp.patch, rp, n + mx, m + my, lane);
         int qmx, qmy;
-        subpel_refine_warp(ws.u.sp, ws.cur, lane, &md, &qmx, &qmy);
+        subpel_refine_warp<true>(ws.sp, ws.cur, lane, &md, &qmx, &qmy);
         *mvx = 4 * mx + qmx;
         *mvy = 4 * my + qmy;
         *minD = md;
     }
 }
 
-// Warp-level cache probe: lanes 0..KCACHE-1 each hold one entry.
-__device__ __forceinline__ bool cache_probe(const int2* c, int key, int lane, int* pd)
+// Warp-level record lookup: lanes 0..KCACHE-1 each hold one record.
+__device__ __forceinline__ bool cache_probe(const int4* c, int key, int lane, int4* rec)
 {
-    int2 e = lane < KCACHE ? __ldcg(c + lane) : make_int2(kEmpty, 0);
+    int4 e = lane < KCACHE ? __ldcg(c + lane) : empty_record();
     unsigned hit = __ballot_sync(0xffffffffu, e.x == key);
     if (!hit) return false;
-    *pd = __shfl_sync(0xffffffffu, e.y, __ffs(hit) - 1);
+    const int f = __ffs(hit) - 1;
+    rec->x = key;
+    rec->y = __shfl_sync(0xffffffffu, e.y, f);
+    rec->z = __shfl_sync(0xffffffffu, e.z, f);
+    rec->w = __shfl_sync(0xffffffffu, e.w, f);
     return true;
 }
 
-// Full evaluation of MB k for raw prediction (px, py).  pd_known >= 0 skips
-// the distortion computation.  Returns the packed final vector and distance.
-__device__ __noinline__ void evaluate(const FullArgs& a, int k, int px, int py, int pd, WarpScratch& ws, int lane, int* out_mv,
-                         int* out_d, int* out_pd)
+// Full evaluation of MB k for raw prediction (px, py), one warp: the record
+// {prediction, distortion at it, final vector, final distortion}.
+__device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, WarpScratch& ws, int lane)
 {
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
     const int4 sp = a.spec4[k];
     int mvx = mv_x(sp.x), mvy = mv_y(sp.x), minD = sp.y;
     const int zd = sp.z;
-    bool tie = (sp.w & FLAG_TIE) && (round_pred(px) != 0 || round_pred(py) != 0);
-    PredGeom g = pred_geom(n, m, a.W, a.H, px, py);
-    if (pd < 0 || tie) load_cur(ws.cur, a, n, m, lane);
-    if (tie) tie_path(a, k, px, py, ws, lane, &mvx, &mvy, &minD);
-    if (pd < 0) pd = warp_pred_distortion(a, g, ws, lane);
-    int pos = best_of3_fast(mvx, mvy, minD, g.pcx, g.pcy, pd, zd, a.lambda, g.pcx, g.pcy);
-    *out_pd = pd;
+    const bool tie = (sp.w & FLAG_TIE) && (round_pred(px) != 0 || round_pred(py) != 0);
+    const PredGeom g = pred_geom(n, m, a.W, a.H, px, py);
+    if (tie) tie_path(a, k, px, py, sp.w, ws, lane, &mvx, &mvy, &minD);
+    const int pd = plane_pred_distortion(a, n, m, g, lane);
+    const int pos = best_of3_fast(mvx, mvy, minD, g.pcx, g.pcy, pd, zd, a.lambda, g.pcx, g.pcy);
+    int4 rec;
+    rec.x = pack_mv(px, py);
+    rec.y = pd;
     if (pos == 0) {
-        *out_mv = pack_mv(mvx, mvy);
-        *out_d = minD;
+        rec.z = pack_mv(mvx, mvy);
+        rec.w = minD;
     } else if (pos == 1) {
-        *out_mv = pack_mv(g.pcx, g.pcy);
-        *out_d = pd;
+        rec.z = pack_mv(g.pcx, g.pcy);
+        rec.w = pd;
     } else {
-        *out_mv = pack_mv(0, 0);
-        *out_d = zd;
+        rec.z = pack_mv(0, 0);
+        rec.w = zd;
     }
+    return rec;
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_full_sweep0(FullArgs a)
+__global__ void __launch_bounds__(256, 4) k_full_sweep0(FullArgs a)
 {
     __shared__ WarpScratch S[8];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -151,14 +231,12 @@ __global__ void __launch_bounds__(256) k_full_sweep0(FullArgs a)
     if (k >= a.nmb) return;
     int px, py;
     median_pred(a.final_mv, a.spec4[k].w, k, a.cols, &px, &py);
-    int fmv, fd, pd;
-    evaluate(a, k, px, py, -1, S[wib], lane, &fmv, &fd, &pd);
-    int key = pack_mv(px, py);
-    if (lane < KCACHE) __stcg(a.cache + (size_t)k * KCACHE + lane, lane == 0 ? make_int2(key, pd) : make_int2(kEmpty, 0));
+    const int4 rec = evaluate(a, k, px, py, S[wib], lane);
+    if (lane < KCACHE) __stcg(a.cache + (size_t)k * KCACHE + lane, lane == 0 ? rec : empty_record());
     if (lane == 0) {
-        a.pred_used[k] = key;
-        a.final_dist[k] = fd;
-        __stcg(a.final_mv + k, fmv);
+        a.pred_used[k] = rec.x;
+        a.final_dist[k] = rec.w;
+        __stcg(a.final_mv + k, rec.z);
     }
 }
 
@@ -218,7 +296,7 @@ __global__ void __launch_bounds__(256, 2) k_full_relax(FullArgs a)
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gwarp = blockIdx.x * 8 + wib, nwarps = gridDim.x * 8;
     WarpScratch& ws = S.u.w[wib];
-    bool converged = false, ok = true;
+    bool converged = false;
     int sweep = 1;
     for (; sweep <= kRelaxSweeps; sweep++) {
         int changed = 0;
@@ -226,29 +304,29 @@ __global__ void __launch_bounds__(256, 2) k_full_relax(FullArgs a)
             const int av = __ldcg(&a.spec4[k].w);
             int px, py;
             median_pred(a.final_mv, av, k, a.cols, &px, &py);
-            int key = pack_mv(px, py);
+            const int key = pack_mv(px, py);
             if (a.pred_used[k] == key) continue;
-            int2* cache = a.cache + (size_t)k * KCACHE;
-            int pd = -1;
-            bool hit = cache_probe(cache, key, lane, &pd);
-            int fmv, fd, npd;
-            evaluate(a, k, px, py, hit ? pd : -1, ws, lane, &fmv, &fd, &npd);
+            int4* cache = a.cache + (size_t)k * KCACHE;
+            int4 rec;
+            const bool hit = cache_probe(cache, key, lane, &rec);
+            if (!hit) rec = evaluate(a, k, px, py, ws, lane);
             if (lane == 0) {
                 atomicAdd(&a.ctrl->relax_evals, 1);
-                if (!hit) atomicAdd(&a.ctrl->relax_miss, 1);
-                if (!hit) __stcg(cache + kCacheRelax + (sweep % 3), make_int2(key, npd));
+                if (!hit) {
+                    atomicAdd(&a.ctrl->relax_miss, 1);
+                    __stcg(cache + kCacheRelax + (sweep % 3), rec);
+                }
                 a.pred_used[k] = key;
-                a.final_dist[k] = fd;
-                if (__ldcg(a.final_mv + k) != fmv) {
-                    __stcg(a.final_mv + k, fmv);
+                a.final_dist[k] = rec.w;
+                if (__ldcg(a.final_mv + k) != rec.z) {
+                    __stcg(a.final_mv + k, rec.z);
                     changed = 1;
                 }
             }
             __syncwarp();
         }
         if (lane == 0 && changed) atomicAdd(&a.changed[sweep], 1);
-        ok = grid_sync(a.ctrl->bar, &a.ctrl->status, gridDim.x, a.spin_limit);
-        if (!ok) return;
+        if (!grid_sync(a.ctrl->bar, &a.ctrl->status, gridDim.x, a.spin_limit)) return;
         if (*((volatile int*)&a.changed[sweep]) == 0) {
             converged = true;
             break;
@@ -321,41 +399,45 @@ __global__ void __launch_bounds__(256, 2) k_full_relax(FullArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// One warp per (MB, dictionary vector): distortion at that vector, unless the
-// MB's cache already holds it.
-__global__ void __launch_bounds__(256) k_full_precompute(FullArgs a)
+// One warp per MB: records at every dictionary vector the MB's cache lacks,
+// then the MB's wavefront record.
+__global__ void __launch_bounds__(256, 2) k_full_precompute(FullArgs a)
 {
     if (*((volatile int*)&a.ctrl->converged)) return;
     __shared__ WarpScratch S[8];
+    __shared__ int dict[NDICT];
+    if (threadIdx.x < NDICT) dict[threadIdx.x] = a.dict[threadIdx.x];
+    __syncthreads();
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    for (int task = blockIdx.x * 8 + wib; task < a.nmb * NDICT; task += gridDim.x * 8) {
-        const int k = task / NDICT, d = task - k * NDICT;
-        const int v = a.dict[d];
-        if (v == kEmpty) continue;
-        int2* cache = a.cache + (size_t)k * KCACHE;
-        int pd;
-        if (cache_probe(cache, v, lane, &pd)) continue;
-        const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
-        load_cur(S[wib].cur, a, n, m, lane);
-        PredGeom g = pred_geom(n, m, a.W, a.H, mv_x(v), mv_y(v));
-        pd = warp_pred_distortion(a, g, S[wib], lane);
-        if (lane == 0) __stcg(cache + kCacheDict + d, make_int2(v, pd));
-        __syncwarp();
+    for (int k = blockIdx.x * 8 + wib; k < a.nmb; k += gridDim.x * 8) {
+        int4* cache = a.cache + (size_t)k * KCACHE;
+        int4 mine = lane < KCACHE ? __ldcg(cache + lane) : empty_record();
+        for (int d = 0; d < NDICT; d++) {
+            const int v = dict[d];
+            if (v == kEmpty || __any_sync(0xffffffffu, mine.x == v)) continue;
+            const int4 rec = evaluate(a, k, mv_x(v), mv_y(v), S[wib], lane);
+            if (lane == kCacheDict + d) mine = rec;
+            if (lane == 0) __stcg(cache + kCacheDict + d, rec);
+            __syncwarp();
+        }
+        WaveRec* wr = a.wave_rec + k;
+        if (lane < KCACHE) wr->kv[lane] = make_int2(mine.x, mine.z);
+        if (lane == KCACHE) wr->av = __ldcg(&a.spec4[k].w);
     }
 }
 
 // ---------------------------------------------------------------------------
-// Exact wavefront in one CTA.  Diagonal t holds the MBs with col + 2*row == t;
-// every MB's neighbours lie on earlier diagonals.
-constexpr int kWaveThreads = 512;
-constexpr int kWaveMaxDiag = 256;   // MBs on one diagonal: min(rows, ceil(cols/2))
-constexpr int kWaveMissWarps = 8;   // warps that evaluate cache misses
-constexpr int kWaveRing = 3;
-
-struct WaveEntry {
-    int2 cache[KCACHE];  // 96 B
-    int4 spec;           // 16 B
-};
+// Exact order in one CTA.  Lane l of warp w owns row 32w + l and handles
+// column t - 2l at step t: its left neighbour is its own previous output,
+// above / above-right / above-left are lane l-1's outputs of steps t-2, t-1
+// and t-3 (shuffles), so a warp advances 32 rows in lock step with no
+// synchronisation.  Lane 0 takes the row above from warp w-1's lane 31
+// through shared memory: each vector is its own flag (the array starts as
+// kEmpty, which no vector packs to), so no fence sits in the loop.  Each lane prefetches its own wavefront records kRing columns
+// ahead with cp.async; a step is a median, twelve key compares and, only for
+// a lane whose prediction is in none of its records, a full evaluation by
+// the whole warp.
+constexpr int kWaveMaxWarps = WAVE_WARPS;  // 32 rows each: 512 rows
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
 {
@@ -366,127 +448,125 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-__device__ __forceinline__ void diag_range(int t, int cols, int rows, int* r_lo, int* cnt)
+__device__ __forceinline__ void fetch_wave_rec(WaveRec* dst, const WaveRec* src)
 {
-    int lo = t - (cols - 1);
-    lo = lo > 0 ? (lo + 1) / 2 : 0;
-    int hi = t / 2 < rows - 1 ? t / 2 : rows - 1;
-    *r_lo = lo;
-    *cnt = hi >= lo ? hi - lo + 1 : 0;
+#pragma unroll
+    for (int q = 0; q < 7; q++)
+        cp_async16(reinterpret_cast<int4*>(dst) + q, reinterpret_cast<const int4*>(src) + q);
 }
 
-__device__ __forceinline__ void prefetch_diag(const FullArgs& a, WaveEntry* slot, int t)
-{
-    int r_lo, cnt;
-    diag_range(t, a.cols, a.nmb / a.cols, &r_lo, &cnt);
-    for (int i = threadIdx.x; i < cnt * 7; i += blockDim.x) {
-        int e = i / 7, part = i - e * 7;
-        int r = r_lo + e, c = t - 2 * r, k = r * a.cols + c;
-        if (part < 6)
-            cp_async16(&slot[e].cache[2 * part], a.cache + (size_t)k * KCACHE + 2 * part);
-        else
-            cp_async16(&slot[e].spec, a.spec4 + k);
-    }
-}
-
-template <bool kSmemVectors>
-__global__ void __launch_bounds__(kWaveThreads, 1) k_full_wave(FullArgs a)
+template <int kRing, int kMaxThreads>
+__global__ void __launch_bounds__(kMaxThreads, 1) k_full_wave(FullArgs a)
 {
     if (*((volatile int*)&a.ctrl->converged)) return;
     extern __shared__ __align__(16) unsigned char wave_smem[];
-    WaveEntry* ring = reinterpret_cast<WaveEntry*>(wave_smem);                   // kWaveRing x kWaveMaxDiag
-    WarpScratch* ws = reinterpret_cast<WarpScratch*>(ring + kWaveRing * kWaveMaxDiag);  // miss warps
-    int* miss = reinterpret_cast<int*>(ws + kWaveMissWarps);                                  // kWaveMaxDiag + 1
-    int* fin = kSmemVectors ? miss + kWaveMaxDiag + 1 : a.final_mv;              // vectors in raster order
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int cols = a.cols, rows = a.nmb / a.cols;
-    const int tmax = (cols - 1) + 2 * (rows - 1);
+    const int cols = a.cols, rows = a.nmb / a.cols, nw = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    WaveRec* ring = reinterpret_cast<WaveRec*>(wave_smem);             // [nw][kRing][32]
+    volatile int* edge = reinterpret_cast<int*>(ring + nw * kRing * 32);  // [nw][cols]: row 32w+31
+    __shared__ int abort_flag;
+    for (int i = threadIdx.x; i < nw * cols; i += blockDim.x) edge[i] = kEmpty;
+    if (threadIdx.x == 0) abort_flag = 0;
+    __syncthreads();
 
-    prefetch_diag(a, ring + 0 * kWaveMaxDiag, 0);
-    cp_async_commit();
-    prefetch_diag(a, ring + 1 * kWaveMaxDiag, 1);
-    cp_async_commit();
-    if (threadIdx.x == 0) miss[kWaveMaxDiag] = 0;
+    WarpScratch& ws = reinterpret_cast<WarpScratch*>(a.wave_scratch)[w];
+    const int r = 32 * w + lane;
+    const bool row_ok = r < rows;
+    const int lanes_used = min(32, rows - 32 * w);
+    const int nsteps = cols + 2 * (lanes_used - 1);
+    WaveRec* mine = ring + (w * kRing) * 32 + lane;      // slot s at mine[32 * s]
+    const WaveRec* src = a.wave_rec + (size_t)r * cols;
+    const volatile int* above = edge + (w - 1) * cols;   // used by lane 0 of warps > 0
 
-    for (int t = 0; t <= tmax; t++) {
-        prefetch_diag(a, ring + ((t + 2) % kWaveRing) * kWaveMaxDiag, t + 2);
-        cp_async_commit();
-        cp_async_wait<2>();
-        __syncthreads();  // diagonal t's entries and diagonal t-1's vectors visible
-        WaveEntry* slot = ring + (t % kWaveRing) * kWaveMaxDiag;
-        int r_lo, cnt;
-        diag_range(t, cols, rows, &r_lo, &cnt);
-        for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-            int r = r_lo + e, c = t - 2 * r, k = r * cols + c;
-            const WaveEntry& we = slot[e];
-            const int av = we.spec.w;
-            int A = (av & AV_A) ? fin[k - 1] : 0;
-            int B = (av & AV_B) ? fin[k - cols] : 0;
-            int C = (av & AV_C) ? fin[k - cols + 1] : 0;
-            int D = (!(av & AV_C) && (av & AV_D)) ? fin[k - cols - 1] : 0;
-            int px, py;
-            median_from(av, A, B, C, D, &px, &py);
-            int key = pack_mv(px, py);
-            bool tie = (av & FLAG_TIE) && (round_pred(px) != 0 || round_pred(py) != 0);
-            int pd = -1;
-#pragma unroll
-            for (int q = 0; q < KCACHE; q++)
-                if (pd < 0 && we.cache[q].x == key) pd = we.cache[q].y;
-            if (pd < 0 || tie) {
-                int idx = atomicAdd(&miss[kWaveMaxDiag], 1);
-                miss[idx] = (k << 1);  // resolved below by a warp
-                continue;
-            }
-            const int n = c * 16, m = r * 16;
-            PredGeom g = pred_geom(n, m, a.W, a.H, px, py);
-            int mvx = mv_x(we.spec.x), mvy = mv_y(we.spec.x);
-            int pos = best_of3_fast(mvx, mvy, we.spec.y, g.pcx, g.pcy, pd, we.spec.z, a.lambda, g.pcx, g.pcy);
-            int fmv = pos == 0 ? we.spec.x : (pos == 1 ? pack_mv(g.pcx, g.pcy) : 0);
-            int fd = pos == 0 ? we.spec.y : (pos == 1 ? pd : we.spec.z);
-            fin[k] = fmv;
-            a.final_dist[k] = fd;
-        }
-        __syncthreads();
-        const int nmiss = miss[kWaveMaxDiag];
-        if (nmiss) {
-            if (threadIdx.x == 0) atomicAdd(&a.ctrl->wave_miss, nmiss);
-            for (int i = wid; wid < kWaveMissWarps && i < nmiss; i += kWaveMissWarps) {
-                int k = miss[i] >> 1;
-                int r = k / cols, c = k - r * cols;
-                int av = a.spec4[k].w;
-                int A = (av & AV_A) ? fin[k - 1] : 0;
-                int B = (av & AV_B) ? fin[k - cols] : 0;
-                int C = (av & AV_C) ? fin[k - cols + 1] : 0;
-                int D = (!(av & AV_C) && (av & AV_D)) ? fin[k - cols - 1] : 0;
-                int px, py;
-                median_from(av, A, B, C, D, &px, &py);
-                int fmv, fd, pd;
-                evaluate(a, k, px, py, -1, ws[wid], lane, &fmv, &fd, &pd);
-                (void)r;
-                (void)c;
-                if (lane == 0) {
-                    fin[k] = fmv;
-                    a.final_dist[k] = fd;
-                }
-                __syncwarp();
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) miss[kWaveMaxDiag] = 0;
+    if (row_ok) {
+        for (int c = 0; c < kRing - 1; c++) {
+            if (c < cols) fetch_wave_rec(mine + 32 * c, src + c);
+            cp_async_commit();
         }
     }
+    int o1 = 0, o2 = 0, o3 = 0;  // this lane's outputs of steps t-1, t-2, t-3
+    int misses = 0;
+    for (int t = 0; t < nsteps; t++) {
+        const int c = t - 2 * lane;
+        const bool active = row_ok && c >= 0 && c < cols;
+        int B = __shfl_up_sync(0xffffffffu, o2, 1);
+        int C = __shfl_up_sync(0xffffffffu, o1, 1);
+        int D = __shfl_up_sync(0xffffffffu, o3, 1);
+        bool stop = false;
+        if (lane == 0 && w > 0 && active) {
+            // the row above, columns c-1 .. c+1, as warp w-1's lane 31 stores them
+            long long it = 0;
+            while (true) {
+                B = above[c];
+                C = c + 1 < cols ? above[c + 1] : 0;
+                D = c >= 1 ? above[c - 1] : 0;
+                if (B != kEmpty && C != kEmpty && D != kEmpty) break;
+                if (++it > a.spin_limit || *((volatile int*)&abort_flag)) {
+                    stop = true;
+                    break;
+                }
+            }
+        }
+        if (__any_sync(0xffffffffu, stop)) {
+            if (lane == 0) {
+                abort_flag = 1;
+                atomicOr(&a.ctrl->status, ST_TIMEOUT);
+            }
+            break;
+        }
+        int out = 0, px = 0, py = 0, q = -1;
+        if (active) {
+            if (c + kRing - 1 < cols) fetch_wave_rec(mine + 32 * ((c + kRing - 1) % kRing), src + c + kRing - 1);
+            cp_async_commit();
+            cp_async_wait<kRing - 1>();
+            const WaveRec& rec = mine[32 * (c % kRing)];
+            median_from(rec.av, o1, B, C, D, &px, &py);
+            const int key = pack_mv(px, py);
+#pragma unroll
+            for (int e = KCACHE - 1; e >= 0; e--) {
+                const int2 kv = rec.kv[e];
+                if (kv.x == key) {
+                    q = e;
+                    out = kv.y;
+                }
+            }
+        }
+        unsigned miss = __ballot_sync(0xffffffffu, active && q < 0);
+        misses += __popc(miss);
+        while (miss) {
+            const int f = __ffs(miss) - 1;
+            miss &= miss - 1;
+            const int fx = __shfl_sync(0xffffffffu, px, f), fy = __shfl_sync(0xffffffffu, py, f);
+            const int fk = (32 * w + f) * cols + (t - 2 * f);
+            const int4 rec = evaluate(a, fk, fx, fy, ws, lane);
+            if (lane == f) {
+                out = rec.z;
+                a.final_dist[fk] = rec.w;
+            }
+        }
+        if (active) {
+            const int k = r * cols + c;
+            a.final_mv[k] = out;
+            a.wave_choice[k] = q;
+            if (lane == 31) edge[w * cols + c] = out;
+        }
+        o3 = o2;
+        o2 = o1;
+        o1 = out;
+    }
+    if (row_ok) cp_async_wait<0>();
+    if (lane == 0 && misses) atomicAdd(&a.ctrl->wave_miss, misses);
     __syncthreads();
+    if (abort_flag) return;
     // outputs and the included-distortion average (Full.cpp:581-611)
     long long tot = 0;
     int cnt = 0;
     for (int k = threadIdx.x; k < a.nmb; k += blockDim.x) {
-        int fmv = fin[k];
+        const int fmv = a.final_mv[k];
         a.out_mv[k] = fmv;
-        if (!kSmemVectors) continue;
-        __stcg(a.final_mv + k, fmv);
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < a.nmb; k += blockDim.x) {
-        int d = a.final_dist[k];
+        const int q = a.wave_choice[k];
+        const int d = q >= 0 ? __ldcg(&a.cache[(size_t)k * KCACHE + q].w) : a.final_dist[k];
+        a.final_dist[k] = d;
         if (a.out_dist) a.out_dist[k] = d;
         if (a.incl && a.incl[k]) {
             tot += d;
@@ -497,19 +577,19 @@ __global__ void __launch_bounds__(kWaveThreads, 1) k_full_wave(FullArgs a)
         tot += __shfl_xor_sync(0xffffffffu, tot, o);
         cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     }
-    __shared__ long long wt[32];
-    __shared__ int wc[32];
+    __shared__ long long wt[kWaveMaxWarps];
+    __shared__ int wc[kWaveMaxWarps];
     if (lane == 0) {
-        wt[wid] = tot;
-        wc[wid] = cnt;
+        wt[w] = tot;
+        wc[w] = cnt;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         long long T = 0;
         int Cn = 0;
-        for (int w = 0; w < kWaveThreads / 32; w++) {
-            T += wt[w];
-            Cn += wc[w];
+        for (int i = 0; i < nw; i++) {
+            T += wt[i];
+            Cn += wc[i];
         }
         a.ctrl->total = T;
         a.ctrl->count = Cn;
@@ -518,17 +598,16 @@ __global__ void __launch_bounds__(kWaveThreads, 1) k_full_wave(FullArgs a)
     }
 }
 
-size_t wave_smem_bytes(int nmb, bool smem_vectors)
+size_t wave_smem_bytes(int nw, int cols, int ring)
 {
-    size_t b = sizeof(WaveEntry) * kWaveRing * kWaveMaxDiag + sizeof(WarpScratch) * kWaveMissWarps +
-               sizeof(int) * (kWaveMaxDiag + 1);
-    if (smem_vectors) b += sizeof(int) * (size_t)nmb;
-    return b;
+    return sizeof(WaveRec) * (size_t)nw * ring * 32 + sizeof(int) * (size_t)nw * cols;
 }
 
-constexpr int kWaveSmemVectorsMax = 24000;  // MBs whose vectors fit in shared memory next to the ring
+constexpr int kWaveMaxCols = 512;  // 8192 / 16
 
 }  // namespace
+
+size_t full_wave_scratch_bytes() { return sizeof(WarpScratch) * WAVE_WARPS; }
 
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
 {
@@ -536,18 +615,17 @@ int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
     VPP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_full_relax, 256, 0));
     if (per_sm < 1) return VPPGPU_ERR_UNSUPPORTED;
     *resolve_cap = per_sm * ctx->sm_count;
-    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)wave_smem_bytes(kWaveSmemVectorsMax, true)));
-    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)wave_smem_bytes(0, false)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<8, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(4, kWaveMaxCols, 8)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<3, kWaveMaxWarps * 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 3)));
     return VPPGPU_OK;
 }
 
 int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid)
 {
-    const int rows = args.nmb / args.cols;
-    const int diag = rows < (args.cols + 1) / 2 ? rows : (args.cols + 1) / 2;
-    if (diag > kWaveMaxDiag) return VPPGPU_ERR_UNSUPPORTED;
+    const int rows = args.nmb / args.cols, nw = (rows + 31) / 32;
+    if (nw > kWaveMaxWarps || args.cols > kWaveMaxCols) return VPPGPU_ERR_UNSUPPORTED;
     k_full_sweep0<<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     {
@@ -557,14 +635,14 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid)
         ctx->launches++;
     }
     {
-        int tasks_blocks = (args.nmb * NDICT + 7) / 8, cap = ctx->sm_count * 8;
-        k_full_precompute<<<tasks_blocks < cap ? tasks_blocks : cap, 256, 0, ctx->stream>>>(args);
+        int blocks = (args.nmb + 7) / 8, cap = ctx->sm_count * 8;
+        k_full_precompute<<<blocks < cap ? blocks : cap, 256, 0, ctx->stream>>>(args);
     }
     VPP_CHECK_LAUNCH(ctx);
-    if (args.nmb <= kWaveSmemVectorsMax)
-        k_full_wave<true><<<1, kWaveThreads, wave_smem_bytes(args.nmb, true), ctx->stream>>>(args);
+    if (nw <= 4)
+        k_full_wave<8, 128><<<1, nw * 32, wave_smem_bytes(nw, args.cols, 8), ctx->stream>>>(args);
     else
-        k_full_wave<false><<<1, kWaveThreads, wave_smem_bytes(0, false), ctx->stream>>>(args);
+        k_full_wave<3, kWaveMaxWarps * 32><<<1, nw * 32, wave_smem_bytes(nw, args.cols, 3), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     return VPPGPU_OK;
 }

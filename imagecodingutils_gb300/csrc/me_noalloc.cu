@@ -13,7 +13,7 @@
 //
 // Limits: at most VPPGPU_NOALLOC_MAX_MBS (396) stored macroblocks, e.g. CIF
 // 352x288, width and height at most VPPGPU_NOALLOC_MAX_DIM (1024); larger
-// frames are rejected with VPPGPU_ERR_UNSUPPORTED.  The array takes 7 MiB on
+// frames are rejected with VPPGPU_ERR_UNSUPPORTED.  The array takes 8 MiB on
 // every GPU that loads the library, for as long as the process runs.
 //
 // Sharing: all calls use the same array and it keeps the previous call's
@@ -27,8 +27,7 @@
 // kernels.  Make that first call before any stream capture begins.
 #include <mutex>
 
-#include "me_common.cuh"
-#include "me_internal.h"
+#include "me_full_common.cuh"
 
 namespace {
 
@@ -38,8 +37,12 @@ constexpr size_t kSpecBytes = 8192;                        // 5 ints per macrobl
 constexpr size_t kStateBytes = 4864;                       // 3 ints per macroblock
 constexpr size_t kCtrlBytes = 256;                         // vppgpu::MeCtrl
 constexpr size_t kChangedBytes = 1792;                     // (N + 2) ints
-constexpr size_t kCacheBytes = 38144;                      // KCACHE (vector, distortion) pairs per macroblock
+constexpr size_t kCacheBytes = 76032;                      // KCACHE 16-byte records per macroblock
 constexpr size_t kDictBytes = 256;                         // NDICT vectors
+constexpr size_t kHpelBytes = 3 * kRefBytes;               // b, h, j planes of the padded reference
+constexpr size_t kWaveScratchBytes = 102400;               // WAVE_WARPS per-warp scratch areas
+constexpr size_t kWaveRecBytes = 44352;                    // one 112-byte wavefront record per macroblock
+constexpr size_t kChoiceBytes = 1584;                      // one int per macroblock
 constexpr size_t kTableBytes = (size_t)VPPGPU_NOALLOC_MAX_MBS * 64 * 64 * 4;
 constexpr size_t kOffSrc = 0;
 constexpr size_t kOffRef = kOffSrc + kSrcBytes;
@@ -49,11 +52,22 @@ constexpr size_t kOffCtrl = kOffState + kStateBytes;
 constexpr size_t kOffChanged = kOffCtrl + kCtrlBytes;
 constexpr size_t kOffCache = kOffChanged + kChangedBytes;
 constexpr size_t kOffDict = kOffCache + kCacheBytes;
-constexpr size_t kOffTables = kOffDict + kDictBytes;
-static_assert(8 * vppgpu::KCACHE * VPPGPU_NOALLOC_MAX_MBS <= kCacheBytes && 4 * vppgpu::NDICT <= kDictBytes,
+constexpr size_t kOffHpel = kOffDict + kDictBytes;
+constexpr size_t kOffWave = kOffHpel + kHpelBytes;
+constexpr size_t kOffWaveRec = kOffWave + kWaveScratchBytes;
+constexpr size_t kOffChoice = kOffWaveRec + kWaveRecBytes;
+constexpr size_t kOffTables = kOffChoice + kChoiceBytes;
+static_assert(16 * vppgpu::KCACHE * VPPGPU_NOALLOC_MAX_MBS <= kCacheBytes && 4 * vppgpu::NDICT <= kDictBytes,
               "resolve caches do not fit");
-static_assert(kOffSpec % 16 == 0 && kOffCache % 16 == 0, "vector records need 16-byte alignment");
-constexpr size_t kScratchBytes = 7u << 20;
+static_assert(sizeof(vppgpu::full::WarpScratch) * vppgpu::WAVE_WARPS <= kWaveScratchBytes,
+              "wavefront scratch does not fit");
+static_assert(sizeof(vppgpu::WaveRec) * VPPGPU_NOALLOC_MAX_MBS <= kWaveRecBytes &&
+                  4 * VPPGPU_NOALLOC_MAX_MBS <= kChoiceBytes,
+              "wavefront records do not fit");
+static_assert(kOffSpec % 16 == 0 && kOffCache % 16 == 0 && kOffHpel % 16 == 0 && kOffWave % 16 == 0 &&
+                  kOffWaveRec % 16 == 0 && kOffTables % 16 == 0,
+              "vector records and planes need 16-byte alignment");
+constexpr size_t kScratchBytes = 8u << 20;
 static_assert(kOffTables + kTableBytes <= kScratchBytes, "scratch layout exceeds the array");
 static_assert(sizeof(vppgpu::MeCtrl) <= kCtrlBytes, "control block does not fit");
 static_assert(5 * 4 * VPPGPU_NOALLOC_MAX_MBS <= kSpecBytes && 3 * 4 * VPPGPU_NOALLOC_MAX_MBS <= kStateBytes &&
@@ -141,11 +155,16 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     a.rstride = width + 2 * vppgpu::PAD;
     a.src8 = base + kOffSrc;
     a.refp = base + kOffRef;
+    a.hpel = base + kOffHpel;
+    a.plane_size = (size_t)a.rstride * (height + 2 * vppgpu::PAD);
+    a.wave_scratch = base + kOffWave;
+    a.wave_rec = (vppgpu::WaveRec*)(base + kOffWaveRec);
+    a.wave_choice = (int*)(base + kOffChoice);
     int* spec = (int*)(base + kOffSpec);
     a.spec4 = reinterpret_cast<int4*>(spec);
     a.spec_imv = spec + 4 * nmb;
     a.tables = (int*)(base + kOffTables);
-    a.cache = (int2*)(base + kOffCache);
+    a.cache = (int4*)(base + kOffCache);
     a.dict = (int*)(base + kOffDict);
     int* state = (int*)(base + kOffState);
     a.final_mv = state;
