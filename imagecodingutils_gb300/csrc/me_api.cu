@@ -206,7 +206,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) || (rc = dalloc(&me->d_src8, npix)) ||
         (rc = dalloc(&me->d_refp, npad)) || (rc = dalloc(&me->d_hpel, 3 * npad)) ||
         (rc = dalloc((unsigned char**)&me->d_wave_scratch, vppgpu::full_wave_scratch_bytes())) ||
-        (rc = dalloc(&me->d_wave_rec, me->nmb)) || (rc = dalloc(&me->d_wave_choice, me->nmb)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
+        (rc = dalloc(&me->d_wave_rec, vppgpu::wave_rec_count(me->cols, me->rows))) || (rc = dalloc(&me->d_wave_choice, me->nmb)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
         (rc = dalloc(&me->tables, (size_t)me->nmb * 64 * 64)) || (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
         (rc = dalloc(&me->cache, (size_t)me->nmb * vppgpu::KCACHE)) || (rc = dalloc(&me->dict, vppgpu::NDICT)) ||
         (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||

@@ -379,6 +379,18 @@ __device__ __forceinline__ void median_from(int av, int A, int B, int C, int D, 
     *py = median3(mv_y(A), mv_y(B), mv_y(C));
 }
 
+// Same median on packed vectors (x in the low, y in the high signed 16-bit
+// half): per-half min/max, the packed result equals pack_mv(px, py).
+__device__ __forceinline__ int median_packed(int av, int A, int B, int C, int D)
+{
+    if (!(av & AV_A)) A = 0;
+    if (!(av & AV_B)) B = 0;
+    C = (av & AV_C) ? C : ((av & AV_D) ? D : 0);
+    if (!(av & AV_B) && !(av & AV_C)) B = C = A;
+    const unsigned a = (unsigned)A, b = (unsigned)B, c = (unsigned)C;
+    return (int)__vmaxs2(__vmins2(a, b), __vmins2(__vmaxs2(a, b), c));
+}
+
 // From the current vectors in global memory (L2, bypassing L1: other SMs update them).
 __device__ __forceinline__ void median_pred(const int* final_mv, int av, int k, int cols, int* px, int* py)
 {

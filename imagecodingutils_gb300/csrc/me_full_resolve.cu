@@ -40,6 +40,8 @@ constexpr int kEmpty = 0x7fffffff;  // no vector packs to this (|y| < 32767 quar
 constexpr int kRelaxSweeps = 8;
 constexpr int kCacheRelax = 1;      // entries 1..3 round robin in relaxation
 constexpr int kCacheDict = 4;       // entries 4..11 dictionary
+constexpr int kCacheClosure = 12;   // entries 12..31 neighbour closure
+constexpr int kSetMax = 6;          // possible final vectors kept per neighbour
 
 __device__ __forceinline__ int4 empty_record() { return make_int4(kEmpty, 0, 0, 0); }
 
@@ -198,13 +200,13 @@ __device__ __forceinline__ bool cache_probe(const int4* c, int key, int lane, in
 __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, WarpScratch& ws, int lane)
 {
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
-    const int4 sp = a.spec4[k];
+    const PredGeom g = pred_geom(n, m, a.W, a.H, px, py);
+    const int4 sp = a.spec4[k];  // loads of spec and planes are independent: one round trip
+    const int pd = plane_pred_distortion(a, n, m, g, lane);
     int mvx = mv_x(sp.x), mvy = mv_y(sp.x), minD = sp.y;
     const int zd = sp.z;
     const bool tie = (sp.w & FLAG_TIE) && (round_pred(px) != 0 || round_pred(py) != 0);
-    const PredGeom g = pred_geom(n, m, a.W, a.H, px, py);
     if (tie) tie_path(a, k, px, py, sp.w, ws, lane, &mvx, &mvy, &minD);
-    const int pd = plane_pred_distortion(a, n, m, g, lane);
     const int pos = best_of3_fast(mvx, mvy, minD, g.pcx, g.pcy, pd, zd, a.lambda, g.pcx, g.pcy);
     int4 rec;
     rec.x = pack_mv(px, py);
@@ -300,30 +302,42 @@ __global__ void __launch_bounds__(256, 2) k_full_relax(FullArgs a)
     int sweep = 1;
     for (; sweep <= kRelaxSweeps; sweep++) {
         int changed = 0;
-        for (int k = gwarp; k < a.nmb; k += nwarps) {
-            const int av = __ldcg(&a.spec4[k].w);
-            int px, py;
-            median_pred(a.final_mv, av, k, a.cols, &px, &py);
-            const int key = pack_mv(px, py);
-            if (a.pred_used[k] == key) continue;
-            int4* cache = a.cache + (size_t)k * KCACHE;
-            int4 rec;
-            const bool hit = cache_probe(cache, key, lane, &rec);
-            if (!hit) rec = evaluate(a, k, px, py, ws, lane);
-            if (lane == 0) {
-                atomicAdd(&a.ctrl->relax_evals, 1);
-                if (!hit) {
-                    atomicAdd(&a.ctrl->relax_miss, 1);
-                    __stcg(cache + kCacheRelax + (sweep % 3), rec);
-                }
-                a.pred_used[k] = key;
-                a.final_dist[k] = rec.w;
-                if (__ldcg(a.final_mv + k) != rec.z) {
-                    __stcg(a.final_mv + k, rec.z);
-                    changed = 1;
-                }
+        // lane per MB (MBs gwarp + lane*nwarps ...) to find the MBs whose
+        // prediction moved, then the warp on each
+        for (int base = gwarp; base < a.nmb; base += 32 * nwarps) {
+            const int k = base + lane * nwarps;
+            int px = 0, py = 0, key = 0;
+            bool moved = false;
+            if (k < a.nmb) {
+                median_pred(a.final_mv, __ldcg(&a.spec4[k].w), k, a.cols, &px, &py);
+                key = pack_mv(px, py);
+                moved = __ldcg(a.pred_used + k) != key;
             }
-            __syncwarp();
+            unsigned todo = __ballot_sync(0xffffffffu, moved);
+            while (todo) {
+                const int f = __ffs(todo) - 1;
+                todo &= todo - 1;
+                const int kk = base + f * nwarps, fkey = __shfl_sync(0xffffffffu, key, f);
+                const int fx = __shfl_sync(0xffffffffu, px, f), fy = __shfl_sync(0xffffffffu, py, f);
+                int4* cache = a.cache + (size_t)kk * KCACHE;
+                int4 rec;
+                const bool hit = cache_probe(cache, fkey, lane, &rec);
+                if (!hit) rec = evaluate(a, kk, fx, fy, ws, lane);
+                if (lane == 0) {
+                    atomicAdd(&a.ctrl->relax_evals, 1);
+                    if (!hit) {
+                        atomicAdd(&a.ctrl->relax_miss, 1);
+                        __stcg(cache + kCacheRelax + (sweep % 3), rec);
+                    }
+                    __stcg(a.pred_used + kk, fkey);
+                    a.final_dist[kk] = rec.w;
+                    if (__ldcg(a.final_mv + kk) != rec.z) {
+                        __stcg(a.final_mv + kk, rec.z);
+                        changed = 1;
+                    }
+                }
+                __syncwarp();
+            }
         }
         if (lane == 0 && changed) atomicAdd(&a.changed[sweep], 1);
         if (!grid_sync(a.ctrl->bar, &a.ctrl->status, gridDim.x, a.spin_limit)) return;
@@ -399,8 +413,7 @@ __global__ void __launch_bounds__(256, 2) k_full_relax(FullArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// One warp per MB: records at every dictionary vector the MB's cache lacks,
-// then the MB's wavefront record.
+// One warp per MB: records at every dictionary vector the MB's cache lacks.
 __global__ void __launch_bounds__(256, 2) k_full_precompute(FullArgs a)
 {
     if (*((volatile int*)&a.ctrl->converged)) return;
@@ -411,162 +424,459 @@ __global__ void __launch_bounds__(256, 2) k_full_precompute(FullArgs a)
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     for (int k = blockIdx.x * 8 + wib; k < a.nmb; k += gridDim.x * 8) {
         int4* cache = a.cache + (size_t)k * KCACHE;
-        int4 mine = lane < KCACHE ? __ldcg(cache + lane) : empty_record();
+        const int4 mine = __ldcg(cache + lane);
         for (int d = 0; d < NDICT; d++) {
             const int v = dict[d];
             if (v == kEmpty || __any_sync(0xffffffffu, mine.x == v)) continue;
             const int4 rec = evaluate(a, k, mv_x(v), mv_y(v), S[wib], lane);
-            if (lane == kCacheDict + d) mine = rec;
             if (lane == 0) __stcg(cache + kCacheDict + d, rec);
             __syncwarp();
         }
-        WaveRec* wr = a.wave_rec + k;
-        if (lane < KCACHE) wr->kv[lane] = make_int2(mine.x, mine.z);
-        if (lane == KCACHE) wr->av = __ldcg(&a.spec4[k].w);
     }
 }
 
 // ---------------------------------------------------------------------------
-// Exact order in one CTA.  Lane l of warp w owns row 32w + l and handles
-// column t - 2l at step t: its left neighbour is its own previous output,
-// above / above-right / above-left are lane l-1's outputs of steps t-2, t-1
-// and t-3 (shuffles), so a warp advances 32 rows in lock step with no
-// synchronisation.  Lane 0 takes the row above from warp w-1's lane 31
-// through shared memory: each vector is its own flag (the array starts as
-// kEmpty, which no vector packs to), so no fence sits in the loop.  Each lane prefetches its own wavefront records kRing columns
-// ahead with cp.async; a step is a median, twelve key compares and, only for
-// a lane whose prediction is in none of its records, a full evaluation by
-// the whole warp.
-constexpr int kWaveMaxWarps = WAVE_WARPS;  // 32 rows each: 512 rows
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+// Neighbour closure, one warp per MB.  The prediction of MB k is the median
+// of the final vectors of A, B and C (or D); each of those is one of a few
+// values: its current vector, its searched vector, zero, or the outcome of
+// one of its records.  Medians of those per-neighbour sets, taken in order of
+// plausibility (index sum), that MB k has no record for yet become records
+// 12..31, evaluated here.  Then MB k's wavefront record is written.
+// Wavefront record hashing: a prediction whose halves fit in signed 11 bits
+// encodes to 22 bits; two distinct buckets of 4 per encoding.
+__device__ __forceinline__ bool wave_encode(int key, unsigned* e)
 {
-    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+    const int x = mv_x(key), y = mv_y(key);
+    *e = (unsigned)(x & 0x7ff) | ((unsigned)(y & 0x7ff) << 11);
+    return (unsigned)(x + 1024) < 2048u && (unsigned)(y + 1024) < 2048u;
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-__device__ __forceinline__ void fetch_wave_rec(WaveRec* dst, const WaveRec* src)
+__device__ __forceinline__ void wave_buckets(unsigned e, int* h1, int* h2)
 {
-#pragma unroll
-    for (int q = 0; q < 7; q++)
-        cp_async16(reinterpret_cast<int4*>(dst) + q, reinterpret_cast<const int4*>(src) + q);
+    *h1 = (int)((e * 0x9e3779b1u) >> 28);
+    *h2 = *h1 ^ (1 + (int)((e * 0xc2b2ae3du) >> 29));  // differs from h1
 }
 
-template <int kRing, int kMaxThreads>
-__global__ void __launch_bounds__(kMaxThreads, 1) k_full_wave(FullArgs a)
+// Index triples (ia, ib, ic) < kSetMax^3 by index sum, then lexicographic,
+// packed as ia | ib << 3 | ic << 6.
+constexpr int kCombos = kSetMax * kSetMax * kSetMax;
+struct ClosureOrder {
+    short v[kCombos];
+};
+constexpr ClosureOrder make_closure_order()
+{
+    ClosureOrder o{};
+    int n = 0;
+    for (int sum = 0; sum <= 3 * (kSetMax - 1); sum++)
+        for (int ia = 0; ia < kSetMax; ia++)
+            for (int ib = 0; ib < kSetMax; ib++) {
+                const int ic = sum - ia - ib;
+                if (ic >= 0 && ic < kSetMax) o.v[n++] = (short)(ia | (ib << 3) | (ic << 6));
+            }
+    return o;
+}
+__constant__ const ClosureOrder kClosureOrder = make_closure_order();
+
+struct ClosureSmem {
+    unsigned tab[8][64];
+    int cnt[8][16];
+    int set[8][3][kSetMax];
+    int nset[8][3];
+    int fresh[8][KCACHE - kCacheClosure];
+    WarpScratch ws[8];
+};
+
+// Ordered, de-duplicated possible final vectors of MB x into set[0..n).
+__device__ __forceinline__ int neighbour_set(const FullArgs& a, int x, int lane, int* set)
+{
+    int v = kEmpty;
+    if (lane == 0) v = __ldcg(a.final_mv + x);
+    else if (lane == 1) v = __ldcg(&a.spec4[x].x);
+    else if (lane == 2) v = 0;
+    else if (lane < 3 + kCacheClosure) {
+        const int4 r = __ldcg(a.cache + (size_t)x * KCACHE + (lane - 3));
+        if (r.x != kEmpty) v = r.z;
+    }
+    const bool valid = v != kEmpty;
+    const unsigned vm = __ballot_sync(0xffffffffu, valid);
+    const unsigned same = __match_any_sync(0xffffffffu, v);
+    const bool keep = valid && (__ffs(same) - 1) == lane;
+    const unsigned km = __ballot_sync(0xffffffffu, keep);
+    const int rank = __popc(km & ((1u << lane) - 1u));
+    if (keep && rank < kSetMax) set[rank] = v;
+    (void)vm;
+    __syncwarp();
+    return min(__popc(km), kSetMax);
+}
+
+__global__ void __launch_bounds__(256, 2) k_full_closure(FullArgs a)
+{
+    if (*((volatile int*)&a.ctrl->converged)) return;
+    __shared__ ClosureSmem S;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int cols = a.cols, rows = a.nmb / cols;
+    for (int k = blockIdx.x * 8 + wib; k < a.nmb; k += gridDim.x * 8) {
+        int4* cache = a.cache + (size_t)k * KCACHE;
+        int4 mine = __ldcg(cache + lane);
+        const int av = __ldcg(&a.spec4[k].w);
+        // neighbour sets (an unavailable neighbour contributes zero, as in the median)
+        const int r = k / cols, c = k - r * cols;
+        (void)rows;
+        const int nb[3] = {(av & AV_A) ? k - 1 : -1, (av & AV_B) ? k - cols : -1,
+                           (av & AV_C) ? k - cols + 1 : ((av & AV_D) ? k - cols - 1 : -1)};
+        for (int s = 0; s < 3; s++) {
+            if (nb[s] >= 0) {
+                const int n = neighbour_set(a, nb[s], lane, S.set[wib][s]);
+                if (lane == 0) S.nset[wib][s] = n;
+            } else if (lane == 0) {
+                S.set[wib][s][0] = 0;
+                S.nset[wib][s] = 1;
+            }
+        }
+        __syncwarp();
+        if (!(av & AV_B) && !(av & AV_C)) {
+            // neither above nor above-right: B and C take A (median_from)
+            for (int i = lane; i < kSetMax; i += 32) S.set[wib][1][i] = S.set[wib][2][i] = S.set[wib][0][i];
+            if (lane == 0) S.nset[wib][1] = S.nset[wib][2] = S.nset[wib][0];
+            __syncwarp();
+        }
+        const int nA = S.nset[wib][0], nB = S.nset[wib][1], nC = S.nset[wib][2];
+        // combinations by index sum, 32 at a time
+        int fresh = 0;
+        for (int base = 0; base < kCombos && fresh < KCACHE - kCacheClosure; base += 32) {
+            const int idx = base + lane;
+            int ia = 0, ib = 0, ic = 0;
+            bool ok = false;
+            if (idx < kCombos) {
+                const int code = kClosureOrder.v[idx];
+                ia = code & 7;
+                ib = (code >> 3) & 7;
+                ic = (code >> 6) & 7;
+                ok = ia < nA && ib < nB && ic < nC;
+            }
+            if (!__any_sync(0xffffffffu, ok)) continue;
+            int key = kEmpty;
+            if (ok) {
+                const int A = S.set[wib][0][ia], B = S.set[wib][1][ib], C = S.set[wib][2][ic];
+                key = pack_mv(median3(mv_x(A), mv_x(B), mv_x(C)), median3(mv_y(A), mv_y(B), mv_y(C)));
+            }
+            // new: not among the MB's records (including those added so far), first of its kind in the batch
+            bool dup = !ok;
+            for (int e = 0; e < KCACHE; e++) dup |= __shfl_sync(0xffffffffu, mine.x, e) == key;
+            const unsigned same = __match_any_sync(0xffffffffu, key);
+            const bool take = !dup && (__ffs(same) - 1) == lane;
+            const unsigned tm = __ballot_sync(0xffffffffu, take);
+            const int slot = fresh + __popc(tm & ((1u << lane) - 1u));
+            if (take && slot < KCACHE - kCacheClosure) S.fresh[wib][slot] = key;
+            __syncwarp();
+            const int added = min(__popc(tm), KCACHE - kCacheClosure - fresh);
+            if (lane >= kCacheClosure + fresh && lane < kCacheClosure + fresh + added)
+                mine.x = S.fresh[wib][lane - kCacheClosure];
+            fresh += added;
+            __syncwarp();
+        }
+        // evaluate the new records
+        for (int i = 0; i < fresh; i++) {
+            const int key = S.fresh[wib][i];
+            const int4 rec = evaluate(a, k, mv_x(key), mv_y(key), S.ws[wib], lane);
+            if (lane == kCacheClosure + i) mine = rec;
+        }
+        if (lane >= kCacheClosure) {
+            if (lane < kCacheClosure + fresh) __stcg(cache + lane, mine);
+        }
+        // the wavefront record: entries hashed into 16 buckets of 4, each to
+        // the emptier of its two buckets, in slot order (a record that does not
+        // fit, or whose outcome is a clamped prediction, is left out: the
+        // wavefront then evaluates that prediction itself)
+        const int spec = __ldcg(&a.spec4[k].x);
+        unsigned entry = 0xffffffffu;
+        int h1 = 0, h2 = 0;
+        if (mine.x != kEmpty) {
+            const int code = mine.z == spec ? 0 : (mine.z == mine.x ? 1 : (mine.z == 0 ? 2 : 3));
+            unsigned e;
+            if (code < 3 && wave_encode(mine.x, &e)) {
+                entry = e | ((unsigned)code << 22);
+                wave_buckets(e, &h1, &h2);
+            }
+        }
+        unsigned* tab = S.tab[wib];
+        int* cnt = S.cnt[wib];
+        tab[lane] = 0xffffffffu;
+        tab[lane + 32] = 0xffffffffu;
+        if (lane < 16) cnt[lane] = 0;
+        __syncwarp();
+        for (int i = 0; i < 32; i++) {
+            if (lane == i && entry != 0xffffffffu) {
+                const int c1 = cnt[h1], c2 = cnt[h2];
+                const int b = c1 <= c2 ? h1 : h2, cb = c1 <= c2 ? c1 : c2;
+                if (cb < 4) {
+                    tab[4 * b + cb] = entry;
+                    cnt[b] = cb + 1;
+                }
+            }
+            __syncwarp();
+        }
+        WaveRec* wr = a.wave_rec + wave_rec_index(cols, r, c);
+        reinterpret_cast<uint2*>(wr->slot)[lane] = make_uint2(tab[2 * lane], tab[2 * lane + 1]);
+        if (lane == 0) {
+            wr->spec = spec;
+            wr->av = av;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exact order, one CTA per group of up to WAVE_WARPS bands of 32 rows.
+// Lane l of warp w owns row 32(band0+w) + l and handles column t - 2l at step
+// t: its left neighbour is its own previous output, above / above-right /
+// above-left are lane l-1's outputs of steps t-2, t-1 and t-3 (shuffles), so
+// a warp advances 32 rows in lock step with no synchronisation.  Lane 0 takes
+// the row above from warp w-1's lane 31 through shared memory, where each
+// vector is its own flag (the array starts as kEmpty, which no vector packs
+// to), or, for the first band of a launch, from the vectors the previous
+// launch stored.  The 32 wavefront records of a step are contiguous (diagonal
+// layout) and arrive by one bulk copy, kRing-1 steps ahead.  A step is a
+// median, 32 key compares and, only for a lane whose prediction is in none of
+// its records, a full evaluation by the whole warp.
+constexpr int kWaveMaxWarps = WAVE_WARPS;
+constexpr unsigned kWaveStepBytes = 32 * sizeof(WaveRec);
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// One bulk copy global -> shared, completion counted on `bar` (16-byte
+// aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar)
+{
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <int kChunk>
+__global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a, int band0, int last)
 {
     if (*((volatile int*)&a.ctrl->converged)) return;
     extern __shared__ __align__(16) unsigned char wave_smem[];
     const int cols = a.cols, rows = a.nmb / a.cols, nw = blockDim.x >> 5;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    WaveRec* ring = reinterpret_cast<WaveRec*>(wave_smem);             // [nw][kRing][32]
-    volatile int* edge = reinterpret_cast<int*>(ring + nw * kRing * 32);  // [nw][cols]: row 32w+31
+    // per warp: two buffers of kChunk steps (32 records a step), a barrier each
+    WaveRec* ring = reinterpret_cast<WaveRec*>(wave_smem);                                // [nw][2][kChunk][32]
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(ring + nw * 2 * kChunk * 32);  // [nw][2]
+    volatile int* edge = reinterpret_cast<int*>(bars + nw * 2);                           // [nw][cols]
     __shared__ int abort_flag;
     for (int i = threadIdx.x; i < nw * cols; i += blockDim.x) edge[i] = kEmpty;
+    if (threadIdx.x < nw * 2) mbar_init(bars + threadIdx.x, 1);
     if (threadIdx.x == 0) abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     __syncthreads();
 
     WarpScratch& ws = reinterpret_cast<WarpScratch*>(a.wave_scratch)[w];
-    const int r = 32 * w + lane;
+    const int band = band0 + w;
+    const int r = 32 * band + lane;
     const bool row_ok = r < rows;
-    const int lanes_used = min(32, rows - 32 * w);
+    const int lanes_used = min(32, rows - 32 * band);
     const int nsteps = cols + 2 * (lanes_used - 1);
-    WaveRec* mine = ring + (w * kRing) * 32 + lane;      // slot s at mine[32 * s]
-    const WaveRec* src = a.wave_rec + (size_t)r * cols;
-    const volatile int* above = edge + (w - 1) * cols;   // used by lane 0 of warps > 0
+    const int nchunks = (nsteps + kChunk - 1) / kChunk;
+    const WaveRec* src = a.wave_rec + (size_t)band * (cols + 62) * 32;  // step t: src[32t .. 32t+31]
+    WaveRec* mybuf = ring + w * 2 * kChunk * 32;
+    unsigned long long* mybars = bars + w * 2;
+    const volatile int* above = edge + (w - 1) * cols;                 // lane 0 of warps > 0
+    const int* above_g = a.final_mv + (size_t)(32 * band - 1) * cols;  // lane 0 of warp 0 when band0 > 0
 
-    if (row_ok) {
-        for (int c = 0; c < kRing - 1; c++) {
-            if (c < cols) fetch_wave_rec(mine + 32 * c, src + c);
-            cp_async_commit();
-        }
+    auto issue = [&](int ci) {  // chunk ci into buffer ci & 1 (lane 0)
+        const int steps = min(kChunk, nsteps - ci * kChunk);
+        const unsigned bytes = (unsigned)steps * kWaveStepBytes;
+        mbar_expect_tx(mybars + (ci & 1), bytes);
+        bulk_load(mybuf + (ci & 1) * kChunk * 32, src + (size_t)ci * kChunk * 32, bytes, mybars + (ci & 1));
+    };
+    if (lane == 0) {
+        issue(0);
+        if (nchunks > 1) issue(1);
     }
+    int issued = min(2, nchunks), consumed = 0;  // chunks of this warp
     int o1 = 0, o2 = 0, o3 = 0;  // this lane's outputs of steps t-1, t-2, t-3
+    int pb = 0, pc = 0;          // lane 0: row above at columns c-1 and c (previous step's B and C)
     int misses = 0;
+    bool stop = false;
     for (int t = 0; t < nsteps; t++) {
+        const int ci = t / kChunk, ti = t - ci * kChunk;
+        if (ti == 0) {
+            long long it = 0;
+            while (!mbar_try_wait(mybars + (ci & 1), (unsigned)(ci >> 1) & 1u))
+                if (++it > a.spin_limit) {
+                    stop = true;
+                    break;
+                }
+            if (__any_sync(0xffffffffu, stop)) {
+                if (lane == 0) {
+                    abort_flag = 1;
+                    atomicOr(&a.ctrl->status, ST_TIMEOUT);
+                }
+                break;
+            }
+            consumed = ci + 1;
+            // the other buffer held chunk ci-1, finished: refill it with chunk ci+1
+            if (ci >= 1 && ci + 1 < nchunks) {
+                if (lane == 0) issue(ci + 1);
+                issued++;
+            }
+        }
         const int c = t - 2 * lane;
         const bool active = row_ok && c >= 0 && c < cols;
         int B = __shfl_up_sync(0xffffffffu, o2, 1);
         int C = __shfl_up_sync(0xffffffffu, o1, 1);
         int D = __shfl_up_sync(0xffffffffu, o3, 1);
-        bool stop = false;
-        if (lane == 0 && w > 0 && active) {
-            // the row above, columns c-1 .. c+1, as warp w-1's lane 31 stores them
-            long long it = 0;
-            while (true) {
-                B = above[c];
-                C = c + 1 < cols ? above[c + 1] : 0;
-                D = c >= 1 ? above[c - 1] : 0;
-                if (B != kEmpty && C != kEmpty && D != kEmpty) break;
-                if (++it > a.spin_limit || *((volatile int*)&abort_flag)) {
-                    stop = true;
-                    break;
+        if (lane == 0 && active) {
+            if (w > 0) {
+                // warp w-1's lane 31 stores the row above: only column c+1 is new
+                if (c == 0) {
+                    long long it = 0;
+                    while ((pc = above[0]) == kEmpty)
+                        if (++it > a.spin_limit || *((volatile int*)&abort_flag)) {
+                            stop = true;
+                            break;
+                        }
+                    pb = 0;
                 }
+                int nc = 0;
+                if (c + 1 < cols) {
+                    long long it = 0;
+                    while ((nc = above[c + 1]) == kEmpty)
+                        if (++it > a.spin_limit || *((volatile int*)&abort_flag)) {
+                            stop = true;
+                            break;
+                        }
+                }
+                D = pb;
+                B = pc;
+                C = nc;
+                pb = pc;
+                pc = nc;
+            } else if (band0 > 0) {
+                B = __ldcg(above_g + c);
+                C = c + 1 < cols ? __ldcg(above_g + c + 1) : 0;
+                D = c >= 1 ? __ldcg(above_g + c - 1) : 0;
             }
         }
-        if (__any_sync(0xffffffffu, stop)) {
+        if (w > 0 && __any_sync(0xffffffffu, stop)) {
             if (lane == 0) {
                 abort_flag = 1;
                 atomicOr(&a.ctrl->status, ST_TIMEOUT);
             }
             break;
         }
-        int out = 0, px = 0, py = 0, q = -1;
+        int out = 0, key = 0;
+        bool hit = false;
         if (active) {
-            if (c + kRing - 1 < cols) fetch_wave_rec(mine + 32 * ((c + kRing - 1) % kRing), src + c + kRing - 1);
-            cp_async_commit();
-            cp_async_wait<kRing - 1>();
-            const WaveRec& rec = mine[32 * (c % kRing)];
-            median_from(rec.av, o1, B, C, D, &px, &py);
-            const int key = pack_mv(px, py);
-#pragma unroll
-            for (int e = KCACHE - 1; e >= 0; e--) {
-                const int2 kv = rec.kv[e];
-                if (kv.x == key) {
-                    q = e;
-                    out = kv.y;
+            const WaveRec& rec = mybuf[((ci & 1) * kChunk + ti) * 32 + lane];
+            key = median_packed(rec.av, o1, B, C, D);
+            unsigned e;
+            const bool inr = wave_encode(key, &e);
+            int h1, h2;
+            wave_buckets(e, &h1, &h2);
+            const uint4 b1 = reinterpret_cast<const uint4*>(rec.slot)[h1];
+            const uint4 b2 = reinterpret_cast<const uint4*>(rec.slot)[h2];
+            int code = -1;
+            const unsigned m = 0xff3fffffu;
+            if ((b1.x & m) == e) code = (int)((b1.x >> 22) & 3u);
+            if ((b1.y & m) == e) code = (int)((b1.y >> 22) & 3u);
+            if ((b1.z & m) == e) code = (int)((b1.z >> 22) & 3u);
+            if ((b1.w & m) == e) code = (int)((b1.w >> 22) & 3u);
+            if ((b2.x & m) == e) code = (int)((b2.x >> 22) & 3u);
+            if ((b2.y & m) == e) code = (int)((b2.y >> 22) & 3u);
+            if ((b2.z & m) == e) code = (int)((b2.z >> 22) & 3u);
+            if ((b2.w & m) == e) code = (int)((b2.w >> 22) & 3u);
+            hit = inr && code >= 0;
+            out = code == 0 ? rec.spec : (code == 1 ? key : 0);
+        }
+        unsigned miss = __ballot_sync(0xffffffffu, active && !hit);
+        if (miss) {
+            misses += __popc(miss);
+            do {
+                const int f = __ffs(miss) - 1;
+                miss &= miss - 1;
+                const int fkey = __shfl_sync(0xffffffffu, key, f);
+                const int fk = (32 * band + f) * cols + (t - 2 * f);
+                const int4 rec = evaluate(a, fk, mv_x(fkey), mv_y(fkey), ws, lane);
+                if (lane == f) {
+                    out = rec.z;
+                    a.final_mv[fk] = rec.z;
+                    a.final_dist[fk] = rec.w;
                 }
-            }
-        }
-        unsigned miss = __ballot_sync(0xffffffffu, active && q < 0);
-        misses += __popc(miss);
-        while (miss) {
-            const int f = __ffs(miss) - 1;
-            miss &= miss - 1;
-            const int fx = __shfl_sync(0xffffffffu, px, f), fy = __shfl_sync(0xffffffffu, py, f);
-            const int fk = (32 * w + f) * cols + (t - 2 * f);
-            const int4 rec = evaluate(a, fk, fx, fy, ws, lane);
-            if (lane == f) {
-                out = rec.z;
-                a.final_dist[fk] = rec.w;
-            }
+            } while (miss);
         }
         if (active) {
-            const int k = r * cols + c;
-            a.final_mv[k] = out;
-            a.wave_choice[k] = q;
-            if (lane == 31) edge[w * cols + c] = out;
+            a.wave_choice[r * cols + c] = hit ? key : kEmpty;
+            if (lane == 31) {
+                edge[w * cols + c] = out;
+                a.final_mv[r * cols + c] = out;  // the next launch's first band reads this row
+            }
         }
         o3 = o2;
         o2 = o1;
         o1 = out;
     }
-    if (row_ok) cp_async_wait<0>();
+    // copies still in flight after an abort land before the CTA leaves
+    for (int ci = consumed; ci < issued; ci++) {
+        long long it = 0;
+        while (!mbar_try_wait(mybars + (ci & 1), (unsigned)(ci >> 1) & 1u))
+            if (++it > a.spin_limit) break;
+    }
     if (lane == 0 && misses) atomicAdd(&a.ctrl->wave_miss, misses);
     __syncthreads();
-    if (abort_flag) return;
-    // outputs and the included-distortion average (Full.cpp:581-611)
+    if (threadIdx.x == 0 && !abort_flag && last) a.ctrl->sweeps = kRelaxSweeps + 1000;
+}
+
+// Outputs of a wavefront-resolved frame, one thread per MB: the record each
+// MB took (or the vector and distortion the wavefront evaluated), and the
+// included-distortion average (Full.cpp:581-611).
+__global__ void __launch_bounds__(256) k_full_wave_outputs(FullArgs a)
+{
+    if (*((volatile int*)&a.ctrl->converged) || (*((volatile int*)&a.ctrl->status) & ST_TIMEOUT)) return;
     long long tot = 0;
     int cnt = 0;
-    for (int k = threadIdx.x; k < a.nmb; k += blockDim.x) {
-        const int fmv = a.final_mv[k];
-        a.out_mv[k] = fmv;
-        const int q = a.wave_choice[k];
-        const int d = q >= 0 ? __ldcg(&a.cache[(size_t)k * KCACHE + q].w) : a.final_dist[k];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmb; k += gridDim.x * blockDim.x) {
+        const int key = a.wave_choice[k];
+        int fmv = 0, d = 0;
+        if (key != kEmpty) {
+            const int4* cache = a.cache + (size_t)k * KCACHE;
+            for (int e = 0; e < KCACHE; e++) {
+                const int4 rec = __ldcg(cache + e);
+                if (rec.x == key) {
+                    fmv = rec.z;
+                    d = rec.w;
+                    break;
+                }
+            }
+        } else {
+            fmv = a.final_mv[k];
+            d = a.final_dist[k];
+        }
+        a.final_mv[k] = fmv;
         a.final_dist[k] = d;
+        a.out_mv[k] = fmv;
         if (a.out_dist) a.out_dist[k] = d;
         if (a.incl && a.incl[k]) {
             tot += d;
@@ -577,30 +887,24 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_full_wave(FullArgs a)
         tot += __shfl_xor_sync(0xffffffffu, tot, o);
         cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     }
-    __shared__ long long wt[kWaveMaxWarps];
-    __shared__ int wc[kWaveMaxWarps];
-    if (lane == 0) {
-        wt[w] = tot;
-        wc[w] = cnt;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        long long T = 0;
-        int Cn = 0;
-        for (int i = 0; i < nw; i++) {
-            T += wt[i];
-            Cn += wc[i];
-        }
-        a.ctrl->total = T;
-        a.ctrl->count = Cn;
-        if (a.out_avg) *a.out_avg = Cn ? T / Cn : 0;
-        a.ctrl->sweeps = kRelaxSweeps + 1000;
+    if ((threadIdx.x & 31) == 0 && cnt) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&a.ctrl->total), (unsigned long long)tot);
+        atomicAdd(&a.ctrl->count, cnt);
     }
 }
 
-size_t wave_smem_bytes(int nw, int cols, int ring)
+// The average, once every output block has added its sums.
+__global__ void k_full_wave_average(FullArgs a)
 {
-    return sizeof(WaveRec) * (size_t)nw * ring * 32 + sizeof(int) * (size_t)nw * cols;
+    if (*((volatile int*)&a.ctrl->converged) || (*((volatile int*)&a.ctrl->status) & ST_TIMEOUT)) return;
+    const long long t = a.ctrl->total;
+    const int c = a.ctrl->count;
+    if (a.out_avg) *a.out_avg = c ? t / c : 0;
+}
+
+size_t wave_smem_bytes(int nw, int cols, int chunk)
+{
+    return (size_t)kWaveStepBytes * nw * 2 * chunk + sizeof(unsigned long long) * nw * 2 + sizeof(int) * (size_t)nw * cols;
 }
 
 constexpr int kWaveMaxCols = 512;  // 8192 / 16
@@ -615,17 +919,17 @@ int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
     VPP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_full_relax, 256, 0));
     if (per_sm < 1) return VPPGPU_ERR_UNSUPPORTED;
     *resolve_cap = per_sm * ctx->sm_count;
-    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<8, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)wave_smem_bytes(4, kWaveMaxCols, 8)));
-    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<3, kWaveMaxWarps * 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 3)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 2)));
     return VPPGPU_OK;
 }
 
 int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid)
 {
-    const int rows = args.nmb / args.cols, nw = (rows + 31) / 32;
-    if (nw > kWaveMaxWarps || args.cols > kWaveMaxCols) return VPPGPU_ERR_UNSUPPORTED;
+    const int rows = args.nmb / args.cols, nbands = (rows + 31) / 32;
+    if (args.cols > kWaveMaxCols) return VPPGPU_ERR_UNSUPPORTED;
     k_full_sweep0<<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     {
@@ -635,15 +939,28 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid)
         ctx->launches++;
     }
     {
-        int blocks = (args.nmb + 7) / 8, cap = ctx->sm_count * 8;
-        k_full_precompute<<<blocks < cap ? blocks : cap, 256, 0, ctx->stream>>>(args);
+        const int blocks = (args.nmb + 7) / 8, cap = ctx->sm_count * 8, grid = blocks < cap ? blocks : cap;
+        k_full_precompute<<<grid, 256, 0, ctx->stream>>>(args);
+        VPP_CHECK_LAUNCH(ctx);
+        k_full_closure<<<grid, 256, 0, ctx->stream>>>(args);
+        VPP_CHECK_LAUNCH(ctx);
     }
-    VPP_CHECK_LAUNCH(ctx);
-    if (nw <= 4)
-        k_full_wave<8, 128><<<1, nw * 32, wave_smem_bytes(nw, args.cols, 8), ctx->stream>>>(args);
-    else
-        k_full_wave<3, kWaveMaxWarps * 32><<<1, nw * 32, wave_smem_bytes(nw, args.cols, 3), ctx->stream>>>(args);
-    VPP_CHECK_LAUNCH(ctx);
+    for (int b0 = 0; b0 < nbands; b0 += kWaveMaxWarps) {
+        const int nw = nbands - b0 < kWaveMaxWarps ? nbands - b0 : kWaveMaxWarps;
+        const int last = b0 + nw == nbands;
+        if (nw <= 3)
+            k_full_wave<4><<<1, nw * 32, wave_smem_bytes(nw, args.cols, 4), ctx->stream>>>(args, b0, last);
+        else
+            k_full_wave<2><<<1, nw * 32, wave_smem_bytes(nw, args.cols, 2), ctx->stream>>>(args, b0, last);
+        VPP_CHECK_LAUNCH(ctx);
+    }
+    {
+        const int blocks = (args.nmb + 255) / 256, cap = ctx->sm_count * 4;
+        k_full_wave_outputs<<<blocks < cap ? blocks : cap, 256, 0, ctx->stream>>>(args);
+        VPP_CHECK_LAUNCH(ctx);
+        k_full_wave_average<<<1, 1, 0, ctx->stream>>>(args);
+        VPP_CHECK_LAUNCH(ctx);
+    }
     return VPPGPU_OK;
 }
 

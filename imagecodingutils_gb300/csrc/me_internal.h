@@ -19,14 +19,31 @@ struct MeCtrl {
     int pad;
 };
 
-// What the wavefront needs of one macroblock, 112 bytes (seven 16-byte
-// copies): its records as {prediction, final vector} pairs and its
-// neighbour-availability word.
+constexpr int KCACHE = 32;  // records per macroblock
+
+// What the wavefront needs of one macroblock, 272 bytes: its records as a
+// hash table of 64 four-byte entries (16 buckets of 4; an entry is the
+// prediction as two signed 11-bit halves, bits 0..21, and how the final
+// vector follows from it, bits 22..23: 0 the searched vector, 1 the
+// prediction itself, 2 zero; 0xffffffff is empty), the searched vector and
+// the neighbour-availability word.  Stored along the wavefront's diagonals:
+// band b (rows 32b..32b+31), step t, lane l (row 32b+l, column t-2l) at
+// (b*(cols+62) + t)*32 + l, so the 32 records one warp needs at one step are
+// contiguous.
 struct WaveRec {
-    int2 kv[12];
+    unsigned slot[64];
+    int spec;
     int av;
-    int pad[3];
+    int pad[2];
 };
+__host__ __device__ inline size_t wave_rec_count(int cols, int rows)
+{
+    return (size_t)((rows + 31) / 32) * (cols + 62) * 32;
+}
+__host__ __device__ inline size_t wave_rec_index(int cols, int r, int c)
+{
+    return ((size_t)(r >> 5) * (cols + 62) + c + 2 * (r & 31)) * 32 + (r & 31);
+}
 
 struct FullArgs {
     int W, H, cols, nmb, motion_range, rstride;
@@ -56,16 +73,16 @@ struct FullArgs {
     MeCtrl* ctrl;
     int* changed;              // one counter per sweep
     void* wave_scratch;        // WAVE_WARPS per-warp scratch areas of the wavefront
-    WaveRec* wave_rec;         // per MB
-    int* wave_choice;          // per MB: record the wavefront took, or -1 (evaluated, final_dist holds it)
+    WaveRec* wave_rec;         // wave_rec_count(cols, rows) records
+    int* wave_choice;          // per MB: the prediction the wavefront found a record for, or 0x7fffffff
+                               // (evaluated there; final_mv / final_dist hold the result)
     double lambda;
     int sweep_limit;
     long long spin_limit;
 };
 
-constexpr int KCACHE = 12;  // cache entries per macroblock
 constexpr int NDICT = 8;    // dictionary vectors
-constexpr int WAVE_WARPS = 16;  // most warps of the single-CTA wavefront (32 rows each)
+constexpr int WAVE_WARPS = 5;   // most warps (bands of 32 rows) of one wavefront launch
 
 size_t full_search_smem();
 // Launch the prediction-dependent tail (sweep 0, relaxation, dictionary

@@ -13,7 +13,7 @@
 //
 // Limits: at most VPPGPU_NOALLOC_MAX_MBS (396) stored macroblocks, e.g. CIF
 // 352x288, width and height at most VPPGPU_NOALLOC_MAX_DIM (1024); larger
-// frames are rejected with VPPGPU_ERR_UNSUPPORTED.  The array takes 8 MiB on
+// frames are rejected with VPPGPU_ERR_UNSUPPORTED.  The array takes 10 MiB on
 // every GPU that loads the library, for as long as the process runs.
 //
 // Sharing: all calls use the same array and it keeps the previous call's
@@ -37,12 +37,15 @@ constexpr size_t kSpecBytes = 8192;                        // 5 ints per macrobl
 constexpr size_t kStateBytes = 4864;                       // 3 ints per macroblock
 constexpr size_t kCtrlBytes = 256;                         // vppgpu::MeCtrl
 constexpr size_t kChangedBytes = 1792;                     // (N + 2) ints
-constexpr size_t kCacheBytes = 76032;                      // KCACHE 16-byte records per macroblock
+constexpr size_t kCacheBytes = 202752;                     // KCACHE 16-byte records per macroblock
 constexpr size_t kDictBytes = 256;                         // NDICT vectors
 constexpr size_t kHpelBytes = 3 * kRefBytes;               // b, h, j planes of the padded reference
-constexpr size_t kWaveScratchBytes = 102400;               // WAVE_WARPS per-warp scratch areas
-constexpr size_t kWaveRecBytes = 44352;                    // one 112-byte wavefront record per macroblock
-constexpr size_t kChoiceBytes = 1584;                      // one int per macroblock
+constexpr size_t kWaveScratchBytes = 16384;                // WAVE_WARPS per-warp scratch areas
+// Wavefront records, wave_rec_count(cols, rows): at most 2*(12+62)*32 = 4736
+// for 396 macroblocks no wider or taller than 64 (rows 33..64 leave at most
+// 12 columns; 32 rows or fewer at most 64 columns, 4032).
+constexpr size_t kWaveRecBytes = 4736 * sizeof(vppgpu::WaveRec);
+constexpr size_t kChoiceBytes = 1600;                      // one int per macroblock
 constexpr size_t kTableBytes = (size_t)VPPGPU_NOALLOC_MAX_MBS * 64 * 64 * 4;
 constexpr size_t kOffSrc = 0;
 constexpr size_t kOffRef = kOffSrc + kSrcBytes;
@@ -67,7 +70,7 @@ static_assert(sizeof(vppgpu::WaveRec) * VPPGPU_NOALLOC_MAX_MBS <= kWaveRecBytes 
 static_assert(kOffSpec % 16 == 0 && kOffCache % 16 == 0 && kOffHpel % 16 == 0 && kOffWave % 16 == 0 &&
                   kOffWaveRec % 16 == 0 && kOffTables % 16 == 0,
               "vector records and planes need 16-byte alignment");
-constexpr size_t kScratchBytes = 8u << 20;
+constexpr size_t kScratchBytes = 10u << 20;
 static_assert(kOffTables + kTableBytes <= kScratchBytes, "scratch layout exceeds the array");
 static_assert(sizeof(vppgpu::MeCtrl) <= kCtrlBytes, "control block does not fit");
 static_assert(5 * 4 * VPPGPU_NOALLOC_MAX_MBS <= kSpecBytes && 3 * 4 * VPPGPU_NOALLOC_MAX_MBS <= kStateBytes &&
@@ -130,7 +133,8 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     const int cols = width / 16, nmb = cols * (height / 16);
     if (width > VPPGPU_NOALLOC_MAX_DIM || height > VPPGPU_NOALLOC_MAX_DIM || nmb > VPPGPU_NOALLOC_MAX_MBS ||
         motion_range > 128 || (size_t)width * height > kSrcBytes ||
-        (size_t)(width + 2 * vppgpu::PAD) * (height + 2 * vppgpu::PAD) > kRefBytes)
+        (size_t)(width + 2 * vppgpu::PAD) * (height + 2 * vppgpu::PAD) > kRefBytes ||
+        vppgpu::wave_rec_count(cols, height / 16) * sizeof(vppgpu::WaveRec) > kWaveRecBytes)
         return VPPGPU_ERR_UNSUPPORTED;
 
     int dev = 0;
