@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(256) k_dp4a_peak(unsigned seed, int iters, uns
 extern "C" {
 
 // Not part of the vpp interface: measures the dp4a rate (instructions per
-// second over the whole device) against which k_full_search is reported.
+// second over the whole device) against which the full-search table kernel is reported.
 int vppgpu_calibrate_dp4a(vppgpu_ctx* ctx, double* dp4a_per_second)
 {
     if (!ctx || !dp4a_per_second) return VPPGPU_ERR_INVALID_ARG;

@@ -17,11 +17,11 @@ struct vppgpu_me {
     unsigned char* d_refp;
     unsigned char* d_hpel;  // b, h, j planes of the padded reference
     size_t plane_size;
-    void* d_wave_scratch;
     vppgpu::WaveRec* d_wave_rec;
     int* d_wave_choice;
     int* spec;  // 5 * nmb: {vector, distortion, zero distortion, flags} per MB, then full-pel winners
     int* tables;
+    int* tie_list;
     int4* cache;
     int* dict;
     int* state; // 3 * nmb: final_mv, final_dist, pred_used
@@ -89,11 +89,11 @@ void me_free(vppgpu_me* me)
     cudaFree(me->d_src8);
     cudaFree(me->d_refp);
     cudaFree(me->d_hpel);
-    cudaFree(me->d_wave_scratch);
     cudaFree(me->d_wave_rec);
     cudaFree(me->d_wave_choice);
     cudaFree(me->spec);
     cudaFree(me->tables);
+    cudaFree(me->tie_list);
     cudaFree(me->cache);
     cudaFree(me->dict);
     cudaFree(me->state);
@@ -130,7 +130,6 @@ vppgpu::FullArgs full_args(vppgpu_me* me, const unsigned char* incl, const int* 
     a.refp = me->d_refp;
     a.hpel = me->d_hpel;
     a.plane_size = me->plane_size;
-    a.wave_scratch = me->d_wave_scratch;
     a.wave_rec = me->d_wave_rec;
     a.wave_choice = me->d_wave_choice;
     a.spec4 = reinterpret_cast<int4*>(me->spec);
@@ -138,6 +137,7 @@ vppgpu::FullArgs full_args(vppgpu_me* me, const unsigned char* incl, const int* 
     a.cache = me->cache;
     a.dict = me->dict;
     a.tables = me->tables;
+    a.tie_list = me->tie_list;
     a.final_mv = me->state;
     a.final_dist = me->state + me->nmb;
     a.pred_used = me->state + 2 * me->nmb;
@@ -205,9 +205,8 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     me->plane_size = npad;
     if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) || (rc = dalloc(&me->d_src8, npix)) ||
         (rc = dalloc(&me->d_refp, npad)) || (rc = dalloc(&me->d_hpel, 3 * npad)) ||
-        (rc = dalloc((unsigned char**)&me->d_wave_scratch, vppgpu::full_wave_scratch_bytes())) ||
         (rc = dalloc(&me->d_wave_rec, vppgpu::wave_rec_count(me->cols, me->rows))) || (rc = dalloc(&me->d_wave_choice, me->nmb)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
-        (rc = dalloc(&me->tables, (size_t)me->nmb * 64 * 64)) || (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
+        (rc = dalloc(&me->tables, (size_t)me->nmb * 64 * 64)) || (rc = dalloc(&me->tie_list, me->nmb)) || (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
         (rc = dalloc(&me->cache, (size_t)me->nmb * vppgpu::KCACHE)) || (rc = dalloc(&me->dict, vppgpu::NDICT)) ||
         (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
         (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||

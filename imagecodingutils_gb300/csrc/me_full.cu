@@ -10,17 +10,21 @@
 // GB300 design
 //   k_full_pack     int16 -> u8 (with a 0..255 check) and an edge-replicated
 //                   padded reference, one pass over the planes.
-//   k_full_search   one CTA per macroblock.  The whole (2R+1)^2 SSD table is
-//                   computed as A2 + B2 - 2*sum(a*b): sum(a*b) with dp4a on
-//                   four byte-shifted, zero-padded copies of each template
-//                   row against word-aligned window rows held in registers
-//                   (5 dp4a per 16-pixel row, no byte alignment work), B2 by
-//                   separable sliding sums.  A warp then replays the
-//                   reference's sequential raster scan over the table with
-//                   ballots (only lanes that beat the running minimum are
-//                   looked at), and runs the sub-pel stages.  None of this
-//                   depends on the predictor except exact ties in the scan,
-//                   which are flagged and the table kept for a rescan.
+//   k_full_table    one CTA per macroblock, every warp busy.  The whole
+//                   (2R+1)^2 SSD table is computed as A2 + B2 - 2*sum(a*b):
+//                   sum(a*b) with dp4a on four byte-shifted, zero-padded
+//                   copies of each template row against word-aligned window
+//                   rows held in registers (5 dp4a per 16-pixel row, no byte
+//                   alignment work), B2 by separable sliding sums in 16-wide
+//                   runs; row minima; the table goes to global memory.
+//   k_full_refine   one warp per macroblock, many per SM: the reference's
+//                   sequential raster scan over the table (ballots; rows whose
+//                   minimum cannot win are skipped) and the sub-pel stages.
+//                   None of this depends on the predictor except exact ties
+//                   in the scan, which are listed.
+//   k_full_tietree  for the listed MBs, the scan outcome of every tie
+//                   decision pattern (the tie tree), read by the
+//                   prediction-dependent stage.
 //   k_full_halfpel  b / h / j half-pel planes of the padded reference, used
 //                   by every distortion at a predicted vector.
 //   resolve         (me_full_resolve.cu) the prediction-dependent tail:
@@ -34,18 +38,18 @@ namespace vppgpu {
 namespace {
 using namespace full;
 
-struct SearchSmem {
+struct TableSmem {
     alignas(16) unsigned char win[WROWS][WSTRIDE];
     alignas(16) unsigned ash[16][4][8];  // [y][shift][word]: template row y shifted right by `shift` bytes
     alignas(16) unsigned char cur[256];
     alignas(16) int tab[TAB][TAB];
-    union {
-        int h2t[TAB][H2STRIDE];  // h2t[jj][r] = sum_x win(r, jj+x)^2
-        SubpelScratch sp;
-    } u;
+    int h2t[TAB][H2STRIDE];  // h2t[jj][r] = sum_x win(r+3, 16+jj+x)^2
     int a2;
-    int state[4];  // mx, my, minD, flags broadcast
-    int tie_nev[TIE_RUNS];
+};
+
+struct TieSmem {
+    alignas(16) int tab[TAB][TAB];
+    int run[TIE_RUNS][sizeof(TieRun) / sizeof(int)];
 };
 
 // ---------------------------------------------------------------------------
@@ -142,10 +146,12 @@ __global__ void __launch_bounds__(256) k_full_halfpel(const unsigned char* __res
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128, 4) k_full_search(FullArgs a)
+// Table stage, one CTA per macroblock, every warp busy: the SSD of all
+// (2R+1)^2 full-pel candidates, its row minima, to the MB's global table.
+__global__ void __launch_bounds__(128, 4) k_full_table(FullArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SearchSmem& S = *reinterpret_cast<SearchSmem*>(smem_raw);
+    TableSmem& S = *reinterpret_cast<TableSmem*>(smem_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int k = blockIdx.x;
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
@@ -164,7 +170,8 @@ __global__ void __launch_bounds__(128, 4) k_full_search(FullArgs a)
     }
     __syncthreads();
 
-    // 2. shifted template rows, template energy, horizontal window energies
+    // 2. shifted template rows, template energy; horizontal 16-sample window
+    //    energies in 16-column runs (task: window row r, run jb)
     if (tid < 64) {
         int y = tid >> 2, s = tid & 3;
         unsigned wds[8];
@@ -191,31 +198,37 @@ __global__ void __launch_bounds__(128, 4) k_full_search(FullArgs a)
         acc = warp_sum(acc);
         if (l == 0) S.a2 = acc;
     }
-    if (tid < 78) {
-        // row r of the dp4a geometry is window row r+3; columns jj+x -> smem col 16+jj+x
-        const unsigned char* row = &S.win[tid + 3][16];
+    for (int task = tid; task < 78 * 4; task += 128) {
+        const int jb = task / 78, r = task - jb * 78;  // consecutive threads: consecutive rows
+        const uint4* p = reinterpret_cast<const uint4*>(&S.win[r + 3][16 + 16 * jb]);
+        const uint4 q0 = p[0], q1 = p[1];
+        const unsigned wv[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+        auto px = [&](int x) { return (int)((wv[x >> 2] >> (8 * (x & 3))) & 0xffu); };
         int sum = 0;
 #pragma unroll
-        for (int x = 0; x < 16; x++) sum += (int)row[x] * row[x];
-        S.u.h2t[0][tid] = sum;
-        for (int jj = 1; jj < TAB; jj++) {
-            int o = row[jj - 1], nw = row[jj + 15];
+        for (int x = 0; x < 16; x++) sum += px(x) * px(x);
+        S.h2t[16 * jb][r] = sum;
+#pragma unroll
+        for (int j = 1; j < 16; j++) {
+            const int o = px(j - 1), nw = px(j + 15);
             sum += nw * nw - o * o;
-            S.u.h2t[jj][tid] = sum;
+            S.h2t[16 * jb + j][r] = sum;
         }
     }
     __syncthreads();
 
-    // 3. vertical window energies -> tab
-    if (tid < TAB) {
-        const int* col = S.u.h2t[tid];
+    // 3. vertical 16-row sums of the horizontal energies -> tab (task: column jj, run ib)
+    for (int task = tid; task < TAB * 4; task += 128) {
+        const int jj = task & (TAB - 1), ib = task >> 6;
+        const int* col = S.h2t[jj];
+        const int ii0 = 16 * ib, ii1 = min(ii0 + 16, 2 * RMAX + 1);
         int sum = 0;
 #pragma unroll
-        for (int y = 0; y < 16; y++) sum += col[y];
-        S.tab[0][tid] = sum;
-        for (int ii = 1; ii < 2 * RMAX + 1; ii++) {
+        for (int y = 0; y < 16; y++) sum += col[ii0 + y];
+        S.tab[ii0][jj] = sum;
+        for (int ii = ii0 + 1; ii < ii1; ii++) {
             sum += col[ii + 15] - col[ii - 1];
-            S.tab[ii][tid] = sum;
+            S.tab[ii][jj] = sum;
         }
     }
     __syncthreads();
@@ -271,97 +284,107 @@ __global__ void __launch_bounds__(128, 4) k_full_search(FullArgs a)
     }
     __syncthreads();
 
-    // 5. row minima, then the sequential scan replay (warp 0)
+    // 5. row minima, then the table (rows 0 .. 2R) to global memory
     int xl, xr, yu, yd;
     full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
     table_row_minima(S.tab, xl, xr, yu, yd, warp, 4, lane);
     __syncthreads();
-    if (warp == 0) {
-        int mx, my, minD, tie;
-        scan_table(SmemTab{S.tab}, xl, xr, yu, yd, 0, 0, lane, &mx, &my, &minD, &tie);
-        if (lane == 0) {
-            S.state[0] = mx;
-            S.state[1] = my;
-            S.state[2] = minD;
-            S.state[3] = tie ? FLAG_TIE : 0;
-        }
-    }
-    __syncthreads();
-    const int mx = S.state[0], my = S.state[1], flags = S.state[3];
-    int minD = S.state[2];
-    if (flags & FLAG_TIE) {
-        int* dst = a.tables + (size_t)k * TAB * TAB;
-        for (int i = tid; i < TIE_ROW * TAB / 4; i += 128)
-            __stcg(reinterpret_cast<int4*>(dst) + i, reinterpret_cast<const int4*>(&S.tab[0][0])[i]);
-    }
-    const int zero_d = S.tab[RMAX][RMAX + 1];
-    __syncthreads();  // tab / h2t no longer needed: sub-pel scratch may overwrite the union
+    int4* dst = reinterpret_cast<int4*>(a.tables + (size_t)k * TAB * TAB);
+    for (int i = tid; i < (2 * RMAX + 1) * TAB / 4; i += 128) __stcg(dst + i, reinterpret_cast<const int4*>(&S.tab[0][0])[i]);
+}
 
-    // 6. sub-pel refinement (warp 0)
-    if (warp == 0) {
-        SubpelScratch& sp = S.u.sp;
-        for (int i = lane; i < 22 * 22; i += 32) {
-            int r = i / 22, c = i - r * 22;
-            sp.patch[r][c] = S.win[my + 34 - 3 + r][mx + 48 - 3 + c];
-        }
-        __syncwarp();
-        int qmx, qmy;
-        subpel_refine_warp(sp, S.cur, lane, &minD, &qmx, &qmy);
+// ---------------------------------------------------------------------------
+// Refine stage, one warp per macroblock: the reference's sequential scan
+// over the table (prediction (0,0) for ties), then the half/quarter-pel
+// stages around the winner.  MBs whose scan met an exact tie go to the tie
+// list for their tie tree.
+__global__ void __launch_bounds__(256, 4) k_full_refine(FullArgs a)
+{
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int k = blockIdx.x * 8 + wib;
+    if (k >= a.nmb) return;
+    const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
+    const int* gt = a.tables + (size_t)k * TAB * TAB;
+    const uint2 cur = load_cur8(a, n, m, lane);
+    int xl, xr, yu, yd, mx, my, minD, tie;
+    full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
+    scan_table(GlobalTab{gt}, xl, xr, yu, yd, 0, 0, lane, &mx, &my, &minD, &tie);
+    const int zero_d = __ldcg(gt + RMAX * TAB + RMAX + 1);
+    int qmx, qmy;
+    subpel_refine_planes(a, n + mx, m + my, cur, lane, &minD, &qmx, &qmy);
+    if (lane == 0) {
         const int qmv = pack_mv(4 * mx + qmx, 4 * my + qmy);
-        int deep = 0;
-        if (flags & FLAG_TIE) {
-            // 7. tie tree: the runs reachable by some prediction
-            int* tree = a.tables + (size_t)k * TAB * TAB + TIE_ROW * TAB;
-            for (int p = 0; p < TIE_RUNS; p++) {
-                if (p > 0) {
-                    const int hb = 31 - __clz(p);
-                    if (S.tie_nev[p & ~(1 << hb)] <= hb) {  // tie hb never met on that path
-                        if (lane == 0) S.tie_nev[p] = 0;
-                        __syncwarp();
-                        continue;
-                    }
-                }
-                int rmx, rmy, rmin, rt, nev, ev[TIE_DEPTH] = {0, 0, 0};
-                scan_table_t<true>(SmemTab{S.tab}, xl, xr, yu, yd, 0, 0, p, lane, &rmx, &rmy, &rmin, &rt, &nev, ev);
-                int rq = qmv, rqmin = minD;
-                if (rmx != mx || rmy != my) {
-                    __syncwarp();
-                    for (int i = lane; i < 22 * 22; i += 32) {
-                        int r = i / 22, c = i - r * 22;
-                        sp.patch[r][c] = S.win[rmy + 34 - 3 + r][rmx + 48 - 3 + c];
-                    }
-                    __syncwarp();
-                    int sx, sy;
-                    subpel_refine_warp(sp, S.cur, lane, &rmin, &sx, &sy);
-                    rq = pack_mv(4 * rmx + sx, 4 * rmy + sy);
-                    rqmin = rmin;
-                }
-                if (lane == 0) {
-                    int* run = tree + p * (int)(sizeof(TieRun) / sizeof(int));
-                    run[0] = ev[0];
-                    run[1] = ev[1];
-                    run[2] = ev[2];
-                    run[3] = nev;
-                    run[4] = rq;
-                    run[5] = rqmin;
-                    S.tie_nev[p] = nev < 0 ? TIE_DEPTH + 1 : nev;
-                }
-                deep |= nev < 0;
-                __syncwarp();
-            }
+        const int av = neighbour_mask(a.slice, k, a.cols, a.nmb / a.cols);
+        a.spec4[k] = make_int4(qmv, minD, zero_d, (tie ? FLAG_TIE : 0) | av);
+        a.spec_imv[k] = pack_mv(mx, my);
+        __stcg(a.final_mv + k, qmv);
+        if (tie) a.tie_list[atomicAdd(&a.ctrl->ntie, 1)] = k;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tie trees of the listed macroblocks (see TieRun), one CTA per MB: the table
+// in shared memory, warp p computes run p (forced scan, then the sub-pel
+// stage of its winner when that is not the searched one).  FLAG_DEEP when a
+// run reachable by some prediction met more ties than the tree holds (the
+// prediction-dependent stage then rescans).
+__global__ void __launch_bounds__(TIE_RUNS * 32) k_full_tietree(FullArgs a)
+{
+    extern __shared__ __align__(16) unsigned char tie_smem[];
+    TieSmem& S = *reinterpret_cast<TieSmem*>(tie_smem);
+    const int tid = threadIdx.x, lane = tid & 31, p = tid >> 5;
+    const int ntie = *((volatile int*)&a.ctrl->ntie);
+    for (int t = blockIdx.x; t < ntie; t += gridDim.x) {
+        const int k = a.tie_list[t];
+        const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
+        int* gt = a.tables + (size_t)k * TAB * TAB;
+        for (int i = tid; i < (2 * RMAX + 1) * TAB / 4; i += blockDim.x)
+            reinterpret_cast<int4*>(&S.tab[0][0])[i] = __ldcg(reinterpret_cast<const int4*>(gt) + i);
+        __syncthreads();
+        int xl, xr, yu, yd;
+        full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
+        const int4 sp = a.spec4[k];
+        const int imv = a.spec_imv[k];
+        int rmx, rmy, rmin, rt, nev, ev[TIE_DEPTH] = {0, 0, 0};
+        scan_table_t<true>(SmemTab{S.tab}, xl, xr, yu, yd, 0, 0, p, lane, &rmx, &rmy, &rmin, &rt, &nev, ev);
+        int rq = sp.x, rqmin = sp.y;
+        if (rmx != mv_x(imv) || rmy != mv_y(imv)) {
+            int sx, sy;
+            subpel_refine_planes(a, n + rmx, m + rmy, load_cur8(a, n, m, lane), lane, &rmin, &sx, &sy);
+            rq = pack_mv(4 * rmx + sx, 4 * rmy + sy);
+            rqmin = rmin;
         }
         if (lane == 0) {
-            int av = neighbour_mask(a.slice, k, a.cols, a.nmb / a.cols);
-            a.spec4[k] = make_int4(qmv, minD, zero_d, flags | av | (deep ? FLAG_DEEP : 0));
-            a.spec_imv[k] = pack_mv(mx, my);
-            __stcg(a.final_mv + k, qmv);
+            S.run[p][0] = ev[0];
+            S.run[p][1] = ev[1];
+            S.run[p][2] = ev[2];
+            S.run[p][3] = nev;
+            S.run[p][4] = rq;
+            S.run[p][5] = rqmin;
         }
+        __syncthreads();
+        constexpr int RW = sizeof(TieRun) / sizeof(int);
+        if (tid < TIE_RUNS * RW) gt[TIE_ROW * TAB + tid] = S.run[tid / RW][tid % RW];
+        if (tid == 0) {
+            // runs a prediction can reach: run p needs tie hb(p) met on the path of p without that bit
+            bool reach[TIE_RUNS];
+            bool deep = S.run[0][3] < 0;
+            reach[0] = true;
+            for (int q = 1; q < TIE_RUNS; q++) {
+                const int hb = 31 - __clz(q), par = q & ~(1 << hb);
+                const int pn = S.run[par][3] < 0 ? TIE_DEPTH + 1 : S.run[par][3];
+                reach[q] = reach[par] && pn > hb;
+                deep |= reach[q] && S.run[q][3] < 0;
+            }
+            if (deep) a.spec4[k].w = sp.w | FLAG_DEEP;
+        }
+        __syncthreads();
     }
 }
 
 }  // namespace
 
-size_t full_search_smem() { return sizeof(SearchSmem); }
+size_t full_search_smem() { return sizeof(TableSmem); }
 
 int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, const short* d_src16, const short* d_ref16,
                 int resolve_grid, cudaEvent_t* ev)
@@ -385,7 +408,11 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, const short* d_s
         VPP_CHECK_LAUNCH(ctx);
     }
     if (ev) VPP_CUDA(cudaEventRecord(ev[1], ctx->stream));
-    k_full_search<<<nmb, 128, sizeof(SearchSmem), ctx->stream>>>(args);
+    k_full_table<<<nmb, 128, sizeof(TableSmem), ctx->stream>>>(args);
+    VPP_CHECK_LAUNCH(ctx);
+    k_full_refine<<<(nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
+    VPP_CHECK_LAUNCH(ctx);
+    k_full_tietree<<<ctx->sm_count, TIE_RUNS * 32, sizeof(TieSmem), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     if (ev) VPP_CUDA(cudaEventRecord(ev[2], ctx->stream));
     int rc = full_resolve_launch(ctx, args, resolve_grid);
@@ -396,8 +423,10 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, const short* d_s
 
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid)
 {
-    VPP_CUDA(cudaFuncSetAttribute(k_full_search, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sizeof(SearchSmem)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_table, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(TableSmem)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_tietree, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(TieSmem)));
     int cap = 0;
     int rc = full_resolve_prepare(ctx, &cap);
     if (rc) return rc;

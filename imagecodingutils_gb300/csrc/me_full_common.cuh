@@ -65,7 +65,7 @@ __device__ __forceinline__ void full_range(int n, int m, int W, int H, int motio
 // kForced: instead of the distance rule, exact tie e (in scan order) takes
 // bit e of `path`; the geometry of the first TIE_DEPTH ties goes to ev[] and
 // their count to *nev (-1 when there were more).
-template <bool kForced, typename TabT>
+template <bool kForced, int kBatch = 1, typename TabT>
 __device__ __forceinline__ void scan_table_t(const TabT& tab, int xl, int xr, int yu, int yd, int prx, int pry,
                                              int path, int lane, int* omx, int* omy, int* omin, int* tie, int* nev,
                                              int* ev)
@@ -77,56 +77,77 @@ __device__ __forceinline__ void scan_table_t(const TabT& tab, int xl, int xr, in
     const int rm1 = yu + lane + 32 <= yd ? tab(yu + lane + 32 + RMAX, 0) : kNone;
     int done = 0;  // rows yu .. yu+done-1 are behind the scan
     while (true) {
-        const unsigned m0 = __ballot_sync(0xffffffffu, rm0 <= minD && lane >= done);
-        const unsigned m1 = __ballot_sync(0xffffffffu, rm1 <= minD && lane + 32 >= done);
+        // the next kBatch rows that can accept, read together
+        unsigned m0 = __ballot_sync(0xffffffffu, rm0 <= minD && lane >= done);
+        unsigned m1 = __ballot_sync(0xffffffffu, rm1 <= minD && lane + 32 >= done);
         if (!m0 && !m1) break;
-        const int off = m0 ? __ffs(m0) - 1 : 32 + __ffs(m1) - 1;
-        const int i = yu + off;
-        done = off + 1;
-        int v[2];
+        int offs[kBatch];
+        int vals[kBatch][2];
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int j = xl + 32 * h + lane;
-            const bool valid = j <= xr && !(i == 0 && j == 0);
-            v[h] = valid ? tab(i + RMAX, j + RMAX + 1) : kNone;
+        for (int q = 0; q < kBatch; q++) {
+            int off = -1;
+            if (m0) {
+                off = __ffs(m0) - 1;
+                m0 &= m0 - 1;
+            } else if (m1) {
+                off = 32 + __ffs(m1) - 1;
+                m1 &= m1 - 1;
+            }
+            offs[q] = off;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int i = yu + off, j = xl + 32 * h + lane;
+                const bool valid = off >= 0 && j <= xr && !(i == 0 && j == 0);
+                vals[q][h] = valid ? tab(i + RMAX, j + RMAX + 1) : kNone;
+            }
         }
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int base = xl + 32 * h;
-            if (base > xr) break;
-            const int j = base + lane;
-            const int d = v[h];
-            unsigned pending = 0xffffffffu;
-            while (true) {
-                bool ok = d != kNone && d <= minD && (i + my >= yu) && (i + my <= yd) && (j + mx >= xl) &&
-                          (j + mx <= xr);
-                unsigned m = __ballot_sync(0xffffffffu, ok) & pending;
-                if (!m) break;
-                int f = __ffs(m) - 1;
-                int df = __shfl_sync(0xffffffffu, d, f);
-                int jf = base + f;
-                bool accept = true;
-                if (df == minD) {
-                    t = 1;
-                    if (kForced) {
-                        const int g = (mx & 0xff) | ((my & 0xff) << 8) | ((jf & 0xff) << 16) | ((i & 0xff) << 24);
-                        if (ne == 0) ev[0] = g;
-                        if (ne == 1) ev[1] = g;
-                        if (ne == 2) ev[2] = g;
-                        accept = ne < TIE_DEPTH ? ((path >> ne) & 1) != 0 : true;
-                        ne++;
-                    } else {
-                        int cx = mx - prx, cy = my - pry, nx = jf - prx, ny = i - pry;
-                        accept = (cy * cy + cx * cx) - (ny * ny + nx * nx) >= 0;
+        for (int q = 0; q < kBatch; q++) {
+            const int off = offs[q];
+            if (off < 0) break;
+            done = off + 1;
+            const int rmin = __shfl_sync(0xffffffffu, off < 32 ? rm0 : rm1, off & 31);
+            if (rmin > minD) continue;  // the minimum fell below this row's within the batch
+            const int i = yu + off;
+            int v[2] = {vals[q][0], vals[q][1]};
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int base = xl + 32 * h;
+                if (base > xr) break;
+                const int j = base + lane;
+                const int d = v[h];
+                unsigned pending = 0xffffffffu;
+                while (true) {
+                    bool ok = d != kNone && d <= minD && (i + my >= yu) && (i + my <= yd) && (j + mx >= xl) &&
+                              (j + mx <= xr);
+                    unsigned m = __ballot_sync(0xffffffffu, ok) & pending;
+                    if (!m) break;
+                    int f = __ffs(m) - 1;
+                    int df = __shfl_sync(0xffffffffu, d, f);
+                    int jf = base + f;
+                    bool accept = true;
+                    if (df == minD) {
+                        t = 1;
+                        if (kForced) {
+                            const int g = (mx & 0xff) | ((my & 0xff) << 8) | ((jf & 0xff) << 16) | ((i & 0xff) << 24);
+                            if (ne == 0) ev[0] = g;
+                            if (ne == 1) ev[1] = g;
+                            if (ne == 2) ev[2] = g;
+                            accept = ne < TIE_DEPTH ? ((path >> ne) & 1) != 0 : true;
+                            ne++;
+                        } else {
+                            int cx = mx - prx, cy = my - pry, nx = jf - prx, ny = i - pry;
+                            accept = (cy * cy + cx * cx) - (ny * ny + nx * nx) >= 0;
+                        }
                     }
+                    if (accept) {
+                        minD = df;
+                        mx = jf;
+                        my = i;
+                    }
+                    pending &= ~((2u << f) - 1u);
+                    if (f == 31) break;
                 }
-                if (accept) {
-                    minD = df;
-                    mx = jf;
-                    my = i;
-                }
-                pending &= ~((2u << f) - 1u);
-                if (f == 31) break;
             }
         }
     }
@@ -141,7 +162,7 @@ template <typename TabT>
 __device__ __forceinline__ void scan_table(const TabT& tab, int xl, int xr, int yu, int yd, int prx, int pry,
                                            int lane, int* omx, int* omy, int* omin, int* tie)
 {
-    scan_table_t<false>(tab, xl, xr, yu, yd, prx, pry, 0, lane, omx, omy, omin, tie, nullptr, nullptr);
+    scan_table_t<false, TabT::kBatch>(tab, xl, xr, yu, yd, prx, pry, 0, lane, omx, omy, omin, tie, nullptr, nullptr);
 }
 
 // Row minima of the searched columns into column 0 (see scan_table), one
@@ -162,20 +183,100 @@ __device__ __forceinline__ void table_row_minima(int (*tab)[TAB], int xl, int xr
 }
 
 struct SmemTab {
+    static constexpr int kBatch = 1;
     const int (*t)[TAB];
     __device__ int operator()(int r, int c) const { return t[r][c]; }
 };
 struct GlobalTab {
+    static constexpr int kBatch = 4;  // rows per round trip
     const int* t;
     __device__ int operator()(int r, int c) const { return __ldcg(t + r * TAB + c); }
 };
 
-// Per-warp scratch of the prediction-dependent stage: the sub-pel stage of a
-// tie rescan and the macroblock's input samples.
-struct WarpScratch {
-    SubpelScratch sp;
-    alignas(16) unsigned char cur[256];
-};
+// Eight consecutive bytes from any address: three aligned words and two
+// funnel shifts (little endian).
+__device__ __forceinline__ uint2 load8(const unsigned char* p)
+{
+    const uintptr_t u = reinterpret_cast<uintptr_t>(p);
+    const unsigned* w = reinterpret_cast<const unsigned*>(u & ~(uintptr_t)3);
+    const unsigned sh = (unsigned)(u & 3) * 8;
+    const unsigned w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2);
+    return make_uint2(__funnelshift_r(w0, w1, sh), __funnelshift_r(w1, w2, sh));
+}
+
+// Sum of squared byte differences of 8 samples.
+__device__ __forceinline__ int ssd8(uint2 a, uint2 b)
+{
+    const unsigned d0 = __vabsdiffu4(a.x, b.x), d1 = __vabsdiffu4(a.y, b.y);
+    return (int)__dp4a(d0, d0, __dp4a(d1, d1, 0u));
+}
+
+// This lane's 8 samples (row lane/2, columns 8*(lane&1)..+7 of the 16x16
+// block) of the even quarter-pel lattice at quarter offset (qy, qx) from the
+// full-pel block origin (x0, y0): the full-pel plane, b (x half), h (y half)
+// or j (centre) at a whole-sample shift, which is what the sub-pel window of
+// LoadHalfQuartPelWindow (Full.cpp:1095-1182) holds at those offsets.
+__device__ __forceinline__ const unsigned char* even_block(const FullArgs& a, int x0, int y0, int qy, int qx, int lane)
+{
+    const int ry = qy & 3, rx = qx & 3;
+    const unsigned char* pl = ry == 0 ? (rx == 0 ? a.refp : a.hpel)
+                                      : (rx == 0 ? a.hpel + a.plane_size : a.hpel + 2 * a.plane_size);
+    return pl + (size_t)(y0 + (qy >> 2) + (lane >> 1) + PAD) * a.rstride + (x0 + (qx >> 2) + 8 * (lane & 1) + PAD);
+}
+
+// Half-pel then quarter-pel refinement around the full-pel winner at
+// (x0, y0) (Full.cpp:452-517), one warp, samples from the frame's planes:
+// eight half-pel neighbours in MEH264IF_SubPos order, then eight quarter-pel
+// neighbours of the half-pel winner, each the rounded mean of the two
+// lattice samples LoadQuartPelWindow pairs (Full.cpp:1207-1220); strict
+// improvement.  cur: this lane's 8 input samples.
+__device__ __forceinline__ void subpel_refine_planes(const FullArgs& a, int x0, int y0, uint2 cur, int lane, int* min_d,
+                                                     int* qmx, int* qmy)
+{
+    constexpr int SX[8] = {-1, 0, 1, -1, 1, -1, 0, 1};
+    constexpr int SY[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+    // quarter pass: lattice offsets (dy, dx) of the two averaged samples
+    constexpr int AY[8] = {-2, -2, -2, 0, 0, 0, 2, 2}, AX[8] = {-2, 0, 0, -2, 2, -2, 0, 0};
+    constexpr int BY[8] = {0, 0, 0, 0, 0, 2, 0, 0}, BX[8] = {0, 0, 2, 0, 0, 0, 0, 2};
+    int part[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) part[k] = ssd8(cur, load8(even_block(a, x0, y0, 2 * SY[k], 2 * SX[k], lane)));
+    int best = *min_d, hmx = 0, hmy = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int acc = warp_sum(part[k]);
+        if (acc < best) {
+            best = acc;
+            hmx = 2 * SX[k];
+            hmy = 2 * SY[k];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint2 va = load8(even_block(a, x0, y0, hmy + AY[k], hmx + AX[k], lane));
+        const uint2 vb = load8(even_block(a, x0, y0, hmy + BY[k], hmx + BX[k], lane));
+        part[k] = ssd8(cur, make_uint2(__vavgu4(va.x, vb.x), __vavgu4(va.y, vb.y)));
+    }
+    int bx = hmx, by = hmy;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int acc = warp_sum(part[k]);
+        if (acc < best) {
+            best = acc;
+            bx = hmx + SX[k];
+            by = hmy + SY[k];
+        }
+    }
+    *min_d = best;
+    *qmx = bx;
+    *qmy = by;
+}
+
+// This lane's 8 input samples of macroblock (n, m).
+__device__ __forceinline__ uint2 load_cur8(const FullArgs& a, int n, int m, int lane)
+{
+    return __ldg(reinterpret_cast<const uint2*>(a.src8 + (size_t)(m + (lane >> 1)) * a.W + n + 8 * (lane & 1)));
+}
 
 }  // namespace full
 }  // namespace vppgpu

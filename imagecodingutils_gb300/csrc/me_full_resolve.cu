@@ -1,6 +1,6 @@
 // me_full_resolve.cu -- prediction-dependent tail of MotionEstimatorH264ImplFull.
 //
-// After k_full_search every macroblock has its prediction-independent results
+// After the search every macroblock has its prediction-independent results
 // (sub-pel vector and distortion, zero-vector distortion).  What is left is a
 // function of the median prediction (Full.cpp:368-380 rounding, 401-446 tie
 // rescan, 532-590 prediction distortion and GetBestVector), and the
@@ -45,14 +45,6 @@ constexpr int kSetMax = 6;          // possible final vectors kept per neighbour
 
 __device__ __forceinline__ int4 empty_record() { return make_int4(kEmpty, 0, 0, 0); }
 
-__device__ __forceinline__ void load_cur(unsigned char* cur, const FullArgs& a, int n, int m, int lane)
-{
-    if (lane < 16)
-        *reinterpret_cast<uint4*>(cur + 16 * lane) =
-            *reinterpret_cast<const uint4*>(a.src8 + (size_t)(m + lane) * a.W + n);
-    __syncwarp();
-}
-
 // Prediction clamped to one macroblock outside the picture (Full.cpp:532-541)
 // and the folded full-pel origin / fraction of its QuarterRead.
 struct PredGeom {
@@ -74,17 +66,6 @@ __device__ __forceinline__ PredGeom pred_geom(int n, int m, int W, int H, int px
     g.ox = n + px0 + (pxq < 0 ? -1 : 0);
     g.oy = m + py0 + (pyq < 0 ? -1 : 0);
     return g;
-}
-
-// Eight consecutive bytes from any address: three aligned words and two
-// funnel shifts (little endian).
-__device__ __forceinline__ uint2 load8(const unsigned char* p)
-{
-    const uintptr_t u = reinterpret_cast<uintptr_t>(p);
-    const unsigned* w = reinterpret_cast<const unsigned*>(u & ~(uintptr_t)3);
-    const unsigned sh = (unsigned)(u & 3) * 8;
-    const unsigned w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2);
-    return make_uint2(__funnelshift_r(w0, w1, sh), __funnelshift_r(w1, w2, sh));
 }
 
 // Distortion at the prediction, one warp: QuarterRead's sixteen cases
@@ -125,9 +106,7 @@ __device__ __forceinline__ int plane_pred_distortion(const FullArgs& a, int n, i
         v.x = __vavgu4(v.x, w.x);  // (p + q + 1) >> 1 per byte
         v.y = __vavgu4(v.y, w.y);
     }
-    const uint2 cur = __ldg(reinterpret_cast<const uint2*>(a.src8 + (size_t)(m + r) * a.W + n + c0));
-    const unsigned d0 = __vabsdiffu4(cur.x, v.x), d1 = __vabsdiffu4(cur.y, v.y);
-    return warp_sum((int)__dp4a(d0, d0, __dp4a(d1, d1, 0u)));
+    return warp_sum(ssd8(load_cur8(a, n, m, lane), v));
 }
 
 // Exact-tie macroblocks: the integer scan depends on the rounded prediction.
@@ -135,8 +114,8 @@ __device__ __forceinline__ int plane_pred_distortion(const FullArgs& a, int n, i
 // rare macroblock with more ties than the tree holds, replay the scan from
 // the kept table and redo the sub-pel stage if the full-pel winner moved.
 // Kept out of line.
-__device__ __noinline__ void tie_path(const FullArgs& a, int k, int px, int py, int flags, WarpScratch& ws,
-                                      int lane, int* mvx, int* mvy, int* minD)
+__device__ __noinline__ void tie_path(const FullArgs& a, int k, int px, int py, int flags, int lane, int* mvx,
+                                      int* mvy, int* minD)
 {
     int prx = round_pred(px), pry = round_pred(py);
     if (prx == 0 && pry == 0) return;  // the search kernel already decided ties with (0,0)
@@ -170,11 +149,8 @@ __device__ __noinline__ void tie_path(const FullArgs& a, int k, int px, int py, 
     scan_table(GlobalTab{tab}, xl, xr, yu, yd, prx, pry, lane, &mx, &my, &md, &tie);
     int imv = a.spec_imv[k];
     if (mx != mv_x(imv) || my != mv_y(imv)) {
-        load_cur(ws.cur, a, n, m, lane);
-        Plane8 rp{a.refp, a.rstride};
-        load_patch22(ws.sp.patch, rp, n + mx, m + my, lane);
         int qmx, qmy;
-        subpel_refine_warp<true>(ws.sp, ws.cur, lane, &md, &qmx, &qmy);
+        subpel_refine_planes(a, n + mx, m + my, load_cur8(a, n, m, lane), lane, &md, &qmx, &qmy);
         *mvx = 4 * mx + qmx;
         *mvy = 4 * my + qmy;
         *minD = md;
@@ -197,7 +173,7 @@ __device__ __forceinline__ bool cache_probe(const int4* c, int key, int lane, in
 
 // Full evaluation of MB k for raw prediction (px, py), one warp: the record
 // {prediction, distortion at it, final vector, final distortion}.
-__device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, WarpScratch& ws, int lane)
+__device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, int lane)
 {
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
     const PredGeom g = pred_geom(n, m, a.W, a.H, px, py);
@@ -206,7 +182,7 @@ __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, 
     int mvx = mv_x(sp.x), mvy = mv_y(sp.x), minD = sp.y;
     const int zd = sp.z;
     const bool tie = (sp.w & FLAG_TIE) && (round_pred(px) != 0 || round_pred(py) != 0);
-    if (tie) tie_path(a, k, px, py, sp.w, ws, lane, &mvx, &mvy, &minD);
+    if (tie) tie_path(a, k, px, py, sp.w, lane, &mvx, &mvy, &minD);
     const int pos = best_of3_fast(mvx, mvy, minD, g.pcx, g.pcy, pd, zd, a.lambda, g.pcx, g.pcy);
     int4 rec;
     rec.x = pack_mv(px, py);
@@ -227,13 +203,12 @@ __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256, 4) k_full_sweep0(FullArgs a)
 {
-    __shared__ WarpScratch S[8];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int k = blockIdx.x * 8 + wib;
     if (k >= a.nmb) return;
     int px, py;
     median_pred(a.final_mv, a.spec4[k].w, k, a.cols, &px, &py);
-    const int4 rec = evaluate(a, k, px, py, S[wib], lane);
+    const int4 rec = evaluate(a, k, px, py, lane);
     if (lane < KCACHE) __stcg(a.cache + (size_t)k * KCACHE + lane, lane == 0 ? rec : empty_record());
     if (lane == 0) {
         a.pred_used[k] = rec.x;
@@ -245,7 +220,6 @@ __global__ void __launch_bounds__(256, 4) k_full_sweep0(FullArgs a)
 // ---------------------------------------------------------------------------
 struct RelaxSmem {
     union {
-        WarpScratch w[8];
         struct {
             int keys[2048];
             int counts[2048];
@@ -297,7 +271,6 @@ __global__ void __launch_bounds__(256, 2) k_full_relax(FullArgs a)
     __shared__ RelaxSmem S;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gwarp = blockIdx.x * 8 + wib, nwarps = gridDim.x * 8;
-    WarpScratch& ws = S.u.w[wib];
     bool converged = false;
     int sweep = 1;
     for (; sweep <= kRelaxSweeps; sweep++) {
@@ -322,7 +295,7 @@ __global__ void __launch_bounds__(256, 2) k_full_relax(FullArgs a)
                 int4* cache = a.cache + (size_t)kk * KCACHE;
                 int4 rec;
                 const bool hit = cache_probe(cache, fkey, lane, &rec);
-                if (!hit) rec = evaluate(a, kk, fx, fy, ws, lane);
+                if (!hit) rec = evaluate(a, kk, fx, fy, lane);
                 if (lane == 0) {
                     atomicAdd(&a.ctrl->relax_evals, 1);
                     if (!hit) {
@@ -417,7 +390,6 @@ __global__ void __launch_bounds__(256, 2) k_full_relax(FullArgs a)
 __global__ void __launch_bounds__(256, 2) k_full_precompute(FullArgs a)
 {
     if (*((volatile int*)&a.ctrl->converged)) return;
-    __shared__ WarpScratch S[8];
     __shared__ int dict[NDICT];
     if (threadIdx.x < NDICT) dict[threadIdx.x] = a.dict[threadIdx.x];
     __syncthreads();
@@ -428,7 +400,7 @@ __global__ void __launch_bounds__(256, 2) k_full_precompute(FullArgs a)
         for (int d = 0; d < NDICT; d++) {
             const int v = dict[d];
             if (v == kEmpty || __any_sync(0xffffffffu, mine.x == v)) continue;
-            const int4 rec = evaluate(a, k, mv_x(v), mv_y(v), S[wib], lane);
+            const int4 rec = evaluate(a, k, mv_x(v), mv_y(v), lane);
             if (lane == 0) __stcg(cache + kCacheDict + d, rec);
             __syncwarp();
         }
@@ -482,7 +454,6 @@ struct ClosureSmem {
     int set[8][3][kSetMax];
     int nset[8][3];
     int fresh[8][KCACHE - kCacheClosure];
-    WarpScratch ws[8];
 };
 
 // Ordered, de-duplicated possible final vectors of MB x into set[0..n).
@@ -577,7 +548,7 @@ __global__ void __launch_bounds__(256, 2) k_full_closure(FullArgs a)
         // evaluate the new records
         for (int i = 0; i < fresh; i++) {
             const int key = S.fresh[wib][i];
-            const int4 rec = evaluate(a, k, mv_x(key), mv_y(key), S.ws[wib], lane);
+            const int4 rec = evaluate(a, k, mv_x(key), mv_y(key), lane);
             if (lane == kCacheClosure + i) mine = rec;
         }
         if (lane >= kCacheClosure) {
@@ -692,7 +663,6 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     __syncthreads();
 
-    WarpScratch& ws = reinterpret_cast<WarpScratch*>(a.wave_scratch)[w];
     const int band = band0 + w;
     const int r = 32 * band + lane;
     const bool row_ok = r < rows;
@@ -819,7 +789,7 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
                 miss &= miss - 1;
                 const int fkey = __shfl_sync(0xffffffffu, key, f);
                 const int fk = (32 * band + f) * cols + (t - 2 * f);
-                const int4 rec = evaluate(a, fk, mv_x(fkey), mv_y(fkey), ws, lane);
+                const int4 rec = evaluate(a, fk, mv_x(fkey), mv_y(fkey), lane);
                 if (lane == f) {
                     out = rec.z;
                     a.final_mv[fk] = rec.z;
@@ -910,8 +880,6 @@ size_t wave_smem_bytes(int nw, int cols, int chunk)
 constexpr int kWaveMaxCols = 512;  // 8192 / 16
 
 }  // namespace
-
-size_t full_wave_scratch_bytes() { return sizeof(WarpScratch) * WAVE_WARPS; }
 
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
 {

@@ -16,7 +16,7 @@ struct MeCtrl {
     int relax_evals; // MB evaluations in the relaxation sweeps
     int relax_miss;  // ... of which computed the prediction distortion
     int wave_miss;   // MBs the wavefront had to evaluate in full
-    int pad;
+    int ntie;        // entries of FullArgs::tie_list
 };
 
 constexpr int KCACHE = 32;  // records per macroblock
@@ -53,12 +53,13 @@ struct FullArgs {
     // after the other: b (horizontal), h (vertical), j (centre)
     const unsigned char* hpel;
     size_t plane_size;          // bytes of one padded plane
-    // speculative (prediction-independent) results of k_full_search, per MB:
+    // speculative (prediction-independent) results of the search, per MB:
     // {packed quarter-pel vector after sub-pel refinement, its distortion,
     //  zero-vector distortion, flags (FLAG_TIE | neighbour availability)}
     int4* spec4;
     int* spec_imv;   // packed full-pel winner
-    int* tables;     // 64x64 SSD table per macroblock (kept for tie macroblocks)
+    int* tables;     // 64x64 SSD table per macroblock (row minima in column 0, tie tree in row 63)
+    int* tie_list;   // macroblocks whose scan met an exact tie (MeCtrl::ntie of them)
     // resolve state
     int* final_mv;
     int* final_dist;
@@ -72,7 +73,6 @@ struct FullArgs {
     long long* out_avg;        // nullable
     MeCtrl* ctrl;
     int* changed;              // one counter per sweep
-    void* wave_scratch;        // WAVE_WARPS per-warp scratch areas of the wavefront
     WaveRec* wave_rec;         // wave_rec_count(cols, rows) records
     int* wave_choice;          // per MB: the prediction the wavefront found a record for, or 0x7fffffff
                                // (evaluated there; final_mv / final_dist hold the result)
@@ -89,7 +89,6 @@ size_t full_search_smem();
 // precompute, exact wavefront) of an estimate whose search has run.
 int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid);
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap);
-size_t full_wave_scratch_bytes();  // bytes behind FullArgs::wave_scratch
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid);
 // ev: nullptr, or 4 events recorded before the pack kernel, before the
 // search kernel, before the resolve kernel and after it.

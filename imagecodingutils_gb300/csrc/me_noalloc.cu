@@ -40,12 +40,12 @@ constexpr size_t kChangedBytes = 1792;                     // (N + 2) ints
 constexpr size_t kCacheBytes = 202752;                     // KCACHE 16-byte records per macroblock
 constexpr size_t kDictBytes = 256;                         // NDICT vectors
 constexpr size_t kHpelBytes = 3 * kRefBytes;               // b, h, j planes of the padded reference
-constexpr size_t kWaveScratchBytes = 16384;                // WAVE_WARPS per-warp scratch areas
 // Wavefront records, wave_rec_count(cols, rows): at most 2*(12+62)*32 = 4736
 // for 396 macroblocks no wider or taller than 64 (rows 33..64 leave at most
 // 12 columns; 32 rows or fewer at most 64 columns, 4032).
 constexpr size_t kWaveRecBytes = 4736 * sizeof(vppgpu::WaveRec);
 constexpr size_t kChoiceBytes = 1600;                      // one int per macroblock
+constexpr size_t kTieListBytes = 1600;                     // one int per macroblock
 constexpr size_t kTableBytes = (size_t)VPPGPU_NOALLOC_MAX_MBS * 64 * 64 * 4;
 constexpr size_t kOffSrc = 0;
 constexpr size_t kOffRef = kOffSrc + kSrcBytes;
@@ -56,18 +56,16 @@ constexpr size_t kOffChanged = kOffCtrl + kCtrlBytes;
 constexpr size_t kOffCache = kOffChanged + kChangedBytes;
 constexpr size_t kOffDict = kOffCache + kCacheBytes;
 constexpr size_t kOffHpel = kOffDict + kDictBytes;
-constexpr size_t kOffWave = kOffHpel + kHpelBytes;
-constexpr size_t kOffWaveRec = kOffWave + kWaveScratchBytes;
+constexpr size_t kOffWaveRec = kOffHpel + kHpelBytes;
 constexpr size_t kOffChoice = kOffWaveRec + kWaveRecBytes;
-constexpr size_t kOffTables = kOffChoice + kChoiceBytes;
+constexpr size_t kOffTieList = kOffChoice + kChoiceBytes;
+constexpr size_t kOffTables = kOffTieList + kTieListBytes;
 static_assert(16 * vppgpu::KCACHE * VPPGPU_NOALLOC_MAX_MBS <= kCacheBytes && 4 * vppgpu::NDICT <= kDictBytes,
               "resolve caches do not fit");
-static_assert(sizeof(vppgpu::full::WarpScratch) * vppgpu::WAVE_WARPS <= kWaveScratchBytes,
-              "wavefront scratch does not fit");
 static_assert(sizeof(vppgpu::WaveRec) * VPPGPU_NOALLOC_MAX_MBS <= kWaveRecBytes &&
                   4 * VPPGPU_NOALLOC_MAX_MBS <= kChoiceBytes,
               "wavefront records do not fit");
-static_assert(kOffSpec % 16 == 0 && kOffCache % 16 == 0 && kOffHpel % 16 == 0 && kOffWave % 16 == 0 &&
+static_assert(kOffSpec % 16 == 0 && kOffCache % 16 == 0 && kOffHpel % 16 == 0 &&
                   kOffWaveRec % 16 == 0 && kOffTables % 16 == 0,
               "vector records and planes need 16-byte alignment");
 constexpr size_t kScratchBytes = 10u << 20;
@@ -161,9 +159,9 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     a.refp = base + kOffRef;
     a.hpel = base + kOffHpel;
     a.plane_size = (size_t)a.rstride * (height + 2 * vppgpu::PAD);
-    a.wave_scratch = base + kOffWave;
     a.wave_rec = (vppgpu::WaveRec*)(base + kOffWaveRec);
     a.wave_choice = (int*)(base + kOffChoice);
+    a.tie_list = (int*)(base + kOffTieList);
     int* spec = (int*)(base + kOffSpec);
     a.spec4 = reinterpret_cast<int4*>(spec);
     a.spec_imv = spec + 4 * nmb;
