@@ -12,11 +12,11 @@
 //                   padded reference, one pass over the planes.
 //   k_full_table    one CTA per macroblock, every warp busy.  The whole
 //                   (2R+1)^2 SSD table is computed as A2 + B2 - 2*sum(a*b):
-//                   sum(a*b) with dp4a on four byte-shifted, zero-padded
-//                   copies of each template row against word-aligned window
-//                   rows held in registers (5 dp4a per 16-pixel row, no byte
-//                   alignment work), B2 by separable sliding sums in 16-wide
-//                   runs; row minima; the table goes to global memory.
+//                   sum(a*b) with dp4a, window rows byte-aligned once per
+//                   thread (funnel shifts) and held in a register ring, 4
+//                   dp4a per 16-pixel row product; B2 by separable sliding
+//                   sums in 16-wide runs; row minima; the table goes to
+//                   global memory.
 //   k_full_refine   one warp per macroblock, many per SM: the reference's
 //                   sequential raster scan over the table (ballots; rows whose
 //                   minimum cannot win are skipped) and the sub-pel stages.
@@ -40,10 +40,9 @@ using namespace full;
 
 struct TableSmem {
     alignas(16) unsigned char win[WROWS][WSTRIDE];
-    alignas(16) unsigned ash[16][4][8];  // [y][shift][word]: template row y shifted right by `shift` bytes
     alignas(16) unsigned char cur[256];
     alignas(16) int tab[TAB][TAB];
-    int h2t[TAB][H2STRIDE];  // h2t[jj][r] = sum_x win(r+3, 16+jj+x)^2
+    int h2t[TAB][H2STRIDE];  // h2t[jj][r] = sum_x win(r, jj+x)^2
     int a2;
 };
 
@@ -148,7 +147,7 @@ __global__ void __launch_bounds__(256) k_full_halfpel(const unsigned char* __res
 // ---------------------------------------------------------------------------
 // Table stage, one CTA per macroblock, every warp busy: the SSD of all
 // (2R+1)^2 full-pel candidates, its row minima, to the MB's global table.
-__global__ void __launch_bounds__(128, 4) k_full_table(FullArgs a)
+__global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TableSmem& S = *reinterpret_cast<TableSmem*>(smem_raw);
@@ -156,9 +155,9 @@ __global__ void __launch_bounds__(128, 4) k_full_table(FullArgs a)
     const int k = blockIdx.x;
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
 
-    // 1. window (rows m-34.., cols n-48..) and input block
+    // 1. window (rows m-31.., cols n-32..) and input block
     {
-        const unsigned char* wbase = a.refp + (size_t)(m - 34 + PAD) * a.rstride + (n - 48 + PAD);
+        const unsigned char* wbase = a.refp + (size_t)(m - 31 + PAD) * a.rstride + (n - 32 + PAD);
         for (int i = tid; i < WROWS * (WSTRIDE / 16); i += 128) {
             int r = i / (WSTRIDE / 16), c = i - r * (WSTRIDE / 16);
             *reinterpret_cast<uint4*>(&S.win[r][16 * c]) =
@@ -170,37 +169,21 @@ __global__ void __launch_bounds__(128, 4) k_full_table(FullArgs a)
     }
     __syncthreads();
 
-    // 2. shifted template rows, template energy; horizontal 16-sample window
-    //    energies in 16-column runs (task: window row r, run jb)
-    if (tid < 64) {
-        int y = tid >> 2, s = tid & 3;
-        unsigned wds[8];
-#pragma unroll
-        for (int w = 0; w < 8; w++) {
-            unsigned v = 0;
-#pragma unroll
-            for (int b = 0; b < 4; b++) {
-                int x = 4 * w + b - s;
-                unsigned px = (x >= 0 && x < 16) ? S.cur[16 * y + x] : 0u;
-                v |= px << (8 * b);
-            }
-            wds[w] = v;
-        }
-        *reinterpret_cast<uint4*>(&S.ash[y][s][0]) = make_uint4(wds[0], wds[1], wds[2], wds[3]);
-        *reinterpret_cast<uint4*>(&S.ash[y][s][4]) = make_uint4(wds[4], wds[5], wds[6], wds[7]);
-    } else if (tid < 96) {
-        int l = tid - 64, acc = 0;
+    // 2. template energy; horizontal 16-sample window energies in 16-column
+    //    runs (task: window row r, run jb)
+    if (tid < 32) {
+        int acc = 0;
 #pragma unroll
         for (int t = 0; t < 8; t++) {
-            int v = S.cur[l + 32 * t];
+            const int v = S.cur[tid + 32 * t];
             acc += v * v;
         }
         acc = warp_sum(acc);
-        if (l == 0) S.a2 = acc;
+        if (tid == 0) S.a2 = acc;
     }
     for (int task = tid; task < 78 * 4; task += 128) {
         const int jb = task / 78, r = task - jb * 78;  // consecutive threads: consecutive rows
-        const uint4* p = reinterpret_cast<const uint4*>(&S.win[r + 3][16 + 16 * jb]);
+        const uint4* p = reinterpret_cast<const uint4*>(&S.win[r][16 * jb]);
         const uint4 q0 = p[0], q1 = p[1];
         const unsigned wv[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
         auto px = [&](int x) { return (int)((wv[x >> 2] >> (8 * (x & 3))) & 0xffu); };
@@ -233,19 +216,23 @@ __global__ void __launch_bounds__(128, 4) k_full_table(FullArgs a)
     }
     __syncthreads();
 
-    // 4. cross terms with dp4a; each thread: 8 candidate rows x 4 word offsets, one byte shift
+    // 4. cross terms with dp4a; each thread: 8 candidate rows x 4 word offsets, one byte shift s.
+    //    Each window row is byte-aligned once for the thread's shift (funnel shifts: word i
+    //    holds bytes 4i+s .. 4i+s+3 of the thread's 32-byte slice) and kept in a ring of 8
+    //    rows; then every 16-pixel row product is 4 dp4a against the template row.
     {
         const int s = lane & 3, qg = (lane >> 2) & 3, ig = 2 * warp + (lane >> 4);
         const int ii0 = 8 * ig;
-        unsigned bw[8][8];
+        unsigned al[8][7];
         auto load_row = [&](unsigned* dst, int r) {
-            const uint4* p = reinterpret_cast<const uint4*>(&S.win[r + 3][16 + 16 * qg]);
-            uint4 x0 = p[0], x1 = p[1];
-            dst[0] = x0.x; dst[1] = x0.y; dst[2] = x0.z; dst[3] = x0.w;
-            dst[4] = x1.x; dst[5] = x1.y; dst[6] = x1.z; dst[7] = x1.w;
+            const uint4* p = reinterpret_cast<const uint4*>(&S.win[r][16 * qg]);
+            const uint4 x0 = p[0], x1 = p[1];
+            const unsigned w[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+            for (int i = 0; i < 7; i++) dst[i] = __funnelshift_r(w[i], w[i + 1], 8 * s);
         };
 #pragma unroll
-        for (int r = 0; r < 8; r++) load_row(bw[r], ii0 + r);
+        for (int r = 0; r < 8; r++) load_row(al[r], ii0 + r);
         unsigned acc[8][4];
 #pragma unroll
         for (int r = 0; r < 8; r++)
@@ -253,21 +240,20 @@ __global__ void __launch_bounds__(128, 4) k_full_table(FullArgs a)
             for (int q = 0; q < 4; q++) acc[r][q] = 0u;
 #pragma unroll
         for (int y = 0; y < 16; y++) {
-            uint4 a0 = *reinterpret_cast<const uint4*>(&S.ash[y][s][0]);
-            unsigned a4 = S.ash[y][s][4];
-            const unsigned A[5] = {a0.x, a0.y, a0.z, a0.w, a4};
+            const uint4 t = *reinterpret_cast<const uint4*>(&S.cur[16 * y]);
+            const unsigned A[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
             for (int r = 0; r < 8; r++) {
-                const unsigned* B = bw[(r + y) & 7];
+                const unsigned* B = al[(r + y) & 7];
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     unsigned c = acc[r][q];
 #pragma unroll
-                    for (int w = 0; w < 5; w++) c = __dp4a(A[w], B[q + w], c);
+                    for (int w = 0; w < 4; w++) c = __dp4a(A[w], B[q + w], c);
                     acc[r][q] = c;
                 }
             }
-            if (y < 15) load_row(bw[y & 7], ii0 + y + 8);
+            if (y < 15) load_row(al[y & 7], ii0 + y + 8);
         }
         const int a2 = S.a2;
 #pragma unroll

@@ -10,8 +10,8 @@ namespace vppgpu {
 namespace full {
 
 constexpr int RMAX = 31;       // table geometry: i in [-31,31] -> ii = i+31, j -> jj = j+32
-constexpr int WROWS = 84;      // window rows m-34 .. m+49
-constexpr int WSTRIDE = 112;   // window cols n-48 .. n+63
+constexpr int WROWS = 78;      // window rows m-31 .. m+46 (candidate rows -31..31, plus 15)
+constexpr int WSTRIDE = 80;    // window cols n-32 .. n+47 (candidate cols -32..31, plus 15; 16-aligned)
 constexpr int H2STRIDE = 81;   // odd stride: conflict-free column walks
 constexpr int TAB = 64;        // SSD table is TAB x TAB ints
 constexpr int FLAG_TIE = 1;   // the scan met an exact tie: its result may depend on the prediction
