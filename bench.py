@@ -54,9 +54,10 @@ def frames_for(rank: int):
     return synth.pan_sequence(1234 + 97 * rank, W, H, NFRAMES)
 
 
-def algorithmic_px_ops():
+def algorithmic_px_ops(subpel: bool = True):
     """Candidates of GetMotionRange per macroblock (full range, zero vector
-    included) plus the 16 sub-pel candidates, x 256 pixels (one SSD term each)."""
+    included), plus the 16 sub-pel candidates when `subpel`, x 256 pixels (one
+    SSD term each)."""
     total = 0
     vr = MOTION_RANGE // 4
     lr = rr = vr - 1
@@ -66,7 +67,7 @@ def algorithmic_px_ops():
         xr = rr if n + rr < W else W - n
         yu = -lr if m - lr >= -16 else -(m + 16)
         yd = rr if m + rr < H else H - m
-        total += (xr - xl + 1) * (yd - yu + 1) + 16
+        total += (xr - xl + 1) * (yd - yu + 1) + (16 if subpel else 0)
     return total * 256
 
 
@@ -128,8 +129,8 @@ def peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per k_full_search launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_full_search_1080p.json")
+    """DRAM bytes per k_full_table launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_full_table_1080p.json")
     if os.path.exists(path):
         return json.load(open(path)).get("dram_bytes_per_launch")
     return None
@@ -259,19 +260,20 @@ def main():
     barrier()
     launches0 = ctx.launch_count()
     _lib.check(L.vppgpu_me_set_timing(h, 1), "vppgpu_me_set_timing")
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     with ClockSampler(local) as clk:
         barrier()
-        ev0.record(stream)
+        evs[0].record(stream)
         for t in range(args.steps):
             step_device(t)
-        ev1.record(stream)
+            evs[t + 1].record(stream)
         barrier()
     launches = ctx.launch_count() - launches0
-    dev_ms = ev0.elapsed_time(ev1)
+    dev_ms = evs[0].elapsed_time(evs[-1])
+    per_frame = sorted(evs[t].elapsed_time(evs[t + 1]) for t in range(args.steps))
     n = C.c_int()
-    kms = [C.c_double(), C.c_double(), C.c_double()]
-    _lib.check(L.vppgpu_me_timing(h, C.byref(n), *[C.byref(x) for x in kms]), "vppgpu_me_timing")
+    stage = (C.c_double * 4)()
+    _lib.check(L.vppgpu_me_timing_stages(h, C.byref(n), stage), "vppgpu_me_timing_stages")
     _lib.check(L.vppgpu_me_set_timing(h, 0), "vppgpu_me_set_timing")
     sweeps = C.c_int()
     L.vppgpu_me_last_sweeps(h, C.byref(sweeps))
@@ -302,9 +304,9 @@ def main():
     if rank == 0:
         dp4a = C.c_double()
         _lib.check(L.vppgpu_calibrate_dp4a(ctx.handle, C.byref(dp4a)), "vppgpu_calibrate_dp4a")
-        px_ops = algorithmic_px_ops()
-        search_s = kms[1].value * 1e-3 / max(n.value, 1)
-        achieved = px_ops / search_s / 1e12           # Tpx/s (one squared-difference term per pixel)
+        px_ops = algorithmic_px_ops(subpel=False)
+        table_s = stage[1] * 1e-3 / max(n.value, 1)
+        achieved = px_ops / table_s / 1e12            # Tpx/s (one squared-difference term per pixel)
         peak = 4.0 * dp4a.value / 1e12                # 4 byte products per dp4a
         cpu = None
         if not args.no_cpu:
@@ -322,12 +324,15 @@ def main():
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * W * H * 2,
                     "d2h_bytes_per_step": NMB * 4 + 32},
-            "roofline": {"bound": "int-alu", "kernel": "k_full_search", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "int-alu", "kernel": "k_full_table", "achieved": achieved, "peak": peak,
                          "unit": "Tpx/s", "frac": achieved / peak, "traffic": profile_traffic(),
                          "peak_source": "measured dp4a rate x 4 px (vppgpu_calibrate_dp4a, this run)",
                          "algorithmic_px_per_launch": px_ops},
-            "kernel_ms_per_frame": {"pack": kms[0].value / max(n.value, 1), "search": kms[1].value / max(n.value, 1),
-                                    "resolve": kms[2].value / max(n.value, 1)},
+            "kernel_ms_per_frame": {k: stage[i] / max(n.value, 1)
+                                    for i, k in enumerate(("pack_halfpel", "table", "refine_tietree", "resolve"))},
+            "latency_ms": {"p50": per_frame[len(per_frame) // 2],
+                           "p99": per_frame[min(len(per_frame) - 1, int(0.99 * len(per_frame)))],
+                           "max": per_frame[-1], "unit": "device ms per frame, plain per-frame form"},
             "resolve_sweeps_last_frame": sweeps.value,
             "hbm_peak_gbs": pk.get("hbm_gbs"), "peaks_source": pk_kind,
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check,

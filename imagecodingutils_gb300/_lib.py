@@ -54,6 +54,7 @@ SIGNATURES = {
     "vppgpu_me_set_timing": (_I, [_P, _I]),
     "vppgpu_me_timing": (_I, [_P, C.POINTER(_I), C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_double)]),
+    "vppgpu_me_timing_stages": (_I, [_P, C.POINTER(_I), _P]),
     "vppgpu_calibrate_dp4a": (_I, [_P, C.POINTER(C.c_double)]),
     "vppgpu_me_full_estimate_noalloc": (_I, [_P, _P, _I, _I, _I, _P, _P, _P, _P, C.POINTER(C.c_long), _P]),
     "vppgpu_fwd4x4": (_I, [_P, _P, _LL, _I, _I, _I, _I]),

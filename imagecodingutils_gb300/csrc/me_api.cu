@@ -39,9 +39,9 @@ struct vppgpu_me {
     // per-kernel timing (vppgpu_me_set_timing)
     int timing;
     int ring_used;
-    cudaEvent_t (*ring)[4];
+    cudaEvent_t (*ring)[5];
     int timed_n;
-    double timed_ms[3];
+    double timed_ms[4];  // pack + half-pel planes, table, refine + tie trees, resolve
 };
 
 namespace {
@@ -50,8 +50,8 @@ constexpr int kRing = 256;
 void ring_fold(vppgpu_me* me)
 {
     for (int i = 0; i < me->ring_used; i++) {
-        cudaEventSynchronize(me->ring[i][3]);
-        for (int k = 0; k < 3; k++) {
+        cudaEventSynchronize(me->ring[i][4]);
+        for (int k = 0; k < 4; k++) {
             float ms = 0.f;
             if (cudaEventElapsedTime(&ms, me->ring[i][k], me->ring[i][k + 1]) == cudaSuccess) me->timed_ms[k] += ms;
         }
@@ -64,7 +64,7 @@ void ring_free(vppgpu_me* me)
 {
     if (!me->ring) return;
     for (int i = 0; i < kRing; i++)
-        for (int k = 0; k < 4; k++) cudaEventDestroy(me->ring[i][k]);
+        for (int k = 0; k < 5; k++) cudaEventDestroy(me->ring[i][k]);
     free(me->ring);
     me->ring = nullptr;
 }
@@ -323,15 +323,15 @@ int vppgpu_me_set_timing(vppgpu_me* me, int enable)
     int rc = vppgpu::bind(me->ctx);
     if (rc) return rc;
     if (enable && !me->ring) {
-        me->ring = (cudaEvent_t(*)[4])calloc(kRing, sizeof(*me->ring));
+        me->ring = (cudaEvent_t(*)[5])calloc(kRing, sizeof(*me->ring));
         if (!me->ring) return VPPGPU_ERR_OUT_OF_MEMORY;
         for (int i = 0; i < kRing; i++)
-            for (int k = 0; k < 4; k++) VPP_CUDA(cudaEventCreate(&me->ring[i][k]));
+            for (int k = 0; k < 5; k++) VPP_CUDA(cudaEventCreate(&me->ring[i][k]));
     }
     me->timing = enable != 0;
     me->ring_used = 0;
     me->timed_n = 0;
-    me->timed_ms[0] = me->timed_ms[1] = me->timed_ms[2] = 0.0;
+    for (int k = 0; k < 4; k++) me->timed_ms[k] = 0.0;
     return VPPGPU_OK;
 }
 
@@ -343,8 +343,19 @@ int vppgpu_me_timing(vppgpu_me* me, int* n, double* pack_ms, double* search_ms, 
     if (me->ring) ring_fold(me);
     *n = me->timed_n;
     *pack_ms = me->timed_ms[0];
-    *search_ms = me->timed_ms[1];
-    *resolve_ms = me->timed_ms[2];
+    *search_ms = me->timed_ms[1] + me->timed_ms[2];
+    *resolve_ms = me->timed_ms[3];
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_timing_stages(vppgpu_me* me, int* n, double* stage_ms4)
+{
+    if (!me || !n || !stage_ms4) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    if (me->ring) ring_fold(me);
+    *n = me->timed_n;
+    for (int k = 0; k < 4; k++) stage_ms4[k] = me->timed_ms[k];
     return VPPGPU_OK;
 }
 

@@ -396,14 +396,15 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, const short* d_s
     if (ev) VPP_CUDA(cudaEventRecord(ev[1], ctx->stream));
     k_full_table<<<nmb, 128, sizeof(TableSmem), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
+    if (ev) VPP_CUDA(cudaEventRecord(ev[2], ctx->stream));
     k_full_refine<<<(nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     k_full_tietree<<<ctx->sm_count, TIE_RUNS * 32, sizeof(TieSmem), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
-    if (ev) VPP_CUDA(cudaEventRecord(ev[2], ctx->stream));
+    if (ev) VPP_CUDA(cudaEventRecord(ev[3], ctx->stream));
     int rc = full_resolve_launch(ctx, args, resolve_grid);
     if (rc) return rc;
-    if (ev) VPP_CUDA(cudaEventRecord(ev[3], ctx->stream));
+    if (ev) VPP_CUDA(cudaEventRecord(ev[4], ctx->stream));
     return VPPGPU_OK;
 }
 

@@ -90,8 +90,8 @@ size_t full_search_smem();
 int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid);
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap);
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid);
-// ev: nullptr, or 4 events recorded before the pack kernel, before the
-// search kernel, before the resolve kernel and after it.
+// ev: nullptr, or 5 events recorded before the pack kernel, before the
+// table kernel, before the refine kernel, before the resolve and after it.
 int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, const short* d_src16, const short* d_ref16,
                 int resolve_grid, cudaEvent_t* ev);
 

@@ -130,6 +130,9 @@ int vppgpu_me_last_stats(vppgpu_me* me, int* stats8);
  * resolve kernels.  Enabling resets the sums. */
 int vppgpu_me_set_timing(vppgpu_me* me, int enable);
 int vppgpu_me_timing(vppgpu_me* me, int* n, double* pack_ms, double* search_ms, double* resolve_ms);
+/* The same sums split by stage: {pack + half-pel planes, SSD table, scan +
+ * sub-pel + tie trees, prediction-dependent resolve}. */
+int vppgpu_me_timing_stages(vppgpu_me* me, int* n, double* stage_ms4);
 
 /* Measured dp4a issue rate of the whole device (instructions per second),
  * the integer-ALU roofline of the motion search.  No vpp counterpart. */
