@@ -172,37 +172,4 @@ __device__ __forceinline__ int best_of3_fast(int bx, int by, int bd, int px, int
     return z ? 2 : pos;
 }
 
-// ---------------------------------------------------------------------------
-// Grid-wide barrier for cooperative launches with a bounded wait: a block
-// that waits longer than `limit` polls sets ST_TIMEOUT and leaves.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ bool grid_sync(unsigned* bar, int* status, unsigned nblocks, long long limit)
-{
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* vgen = bar + 1;
-        unsigned gen = *vgen;
-        __threadfence();
-        unsigned arrived = atomicAdd(bar, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            long long it = 0;
-            while (*vgen == gen) {
-                __nanosleep(100);
-                if (++it > limit) {
-                    atomicOr(status, ST_TIMEOUT);
-                    break;
-                }
-                if (*((volatile int*)status) & ST_TIMEOUT) break;
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return (*((volatile int*)status) & ST_TIMEOUT) == 0;
-}
-
 }  // namespace vppgpu

@@ -15,13 +15,14 @@
 //
 //   k_full_sweep0      every MB at once, prediction from the current vectors
 //                      (initially the searched ones).
-//   k_full_relax       cooperative: up to kRelaxSweeps sweeps re-evaluating
-//                      the MBs whose prediction changed.  A sweep without
-//                      change is the unique fixed point of the DAG, i.e. the
-//                      sequential result.  Otherwise (long copy chains: the
-//                      prediction wins and is copied along rows and columns)
-//                      block 0 builds a dictionary of the frame's dominant
-//                      vectors.
+//   k_full_relax_sweep up to kRelaxSweeps launches, each re-evaluating the
+//                      MBs whose prediction moved.  A sweep without change
+//                      is the unique fixed point of the DAG, i.e. the
+//                      sequential result; most frames stop here
+//                      (k_full_relax_outcome writes their outputs).
+//                      Otherwise (long copy chains: the prediction wins and
+//                      is copied along rows and columns) k_full_relax_outcome
+//                      builds a dictionary of the frame's dominant vectors.
 //   k_full_precompute  records of every MB at every dictionary vector.
 //   k_full_wave        one CTA replays the exact sequential order, pipelined
 //                      by rows: warp w owns rows w, w+32, ...; a row advances
@@ -231,122 +232,118 @@ struct RelaxSmem {
     int red_val[8];
 };
 
-__device__ void write_outputs_and_average(const FullArgs& a, RelaxSmem& S, int gwarp, int nwarps, int lane, int wib)
+// One relaxation sweep: lane per MB (MBs gwarp + lane*nwarps ...) to find the
+// MBs whose prediction moved, then the warp on each.  Skipped once an earlier
+// sweep changed no vector (the fixed point is reached).
+__global__ void __launch_bounds__(256, 4) k_full_relax_sweep(FullArgs a, int sweep)
 {
-    long long tot = 0;
-    int cnt = 0;
-    for (int k = gwarp; k < a.nmb; k += nwarps) {
-        if (lane == 0) {
-            int fmv = __ldcg(a.final_mv + k);
+    if (sweep > 1 && *((volatile int*)&a.changed[sweep - 1]) == 0) return;
+    for (int s = 1; s < sweep - 1; s++)
+        if (*((volatile int*)&a.changed[s]) == 0) return;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gwarp = blockIdx.x * 8 + wib, nwarps = gridDim.x * 8;
+    int changed = 0;
+    for (int base = gwarp; base < a.nmb; base += 32 * nwarps) {
+        const int k = base + lane * nwarps;
+        int px = 0, py = 0, key = 0;
+        bool moved = false;
+        if (k < a.nmb) {
+            median_pred(a.final_mv, __ldcg(&a.spec4[k].w), k, a.cols, &px, &py);
+            key = pack_mv(px, py);
+            moved = __ldcg(a.pred_used + k) != key;
+        }
+        unsigned todo = __ballot_sync(0xffffffffu, moved);
+        while (todo) {
+            const int f = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int kk = base + f * nwarps, fkey = __shfl_sync(0xffffffffu, key, f);
+            const int fx = __shfl_sync(0xffffffffu, px, f), fy = __shfl_sync(0xffffffffu, py, f);
+            int4* cache = a.cache + (size_t)kk * KCACHE;
+            int4 rec;
+            const bool hit = cache_probe(cache, fkey, lane, &rec);
+            if (!hit) rec = evaluate(a, kk, fx, fy, lane);
+            if (lane == 0) {
+                atomicAdd(&a.ctrl->relax_evals, 1);
+                if (!hit) {
+                    atomicAdd(&a.ctrl->relax_miss, 1);
+                    __stcg(cache + kCacheRelax + (sweep % 3), rec);
+                }
+                __stcg(a.pred_used + kk, fkey);
+                a.final_dist[kk] = rec.w;
+                if (__ldcg(a.final_mv + kk) != rec.z) {
+                    __stcg(a.final_mv + kk, rec.z);
+                    changed = 1;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    if (lane == 0 && changed) atomicAdd(&a.changed[sweep], 1);
+}
+
+// After the sweeps: a sweep that changed nothing means the vectors are the
+// sequential result -- every block writes its MBs' outputs and adds their
+// included distortions; otherwise block 0 finds the frame's dominant vectors
+// for the wavefront's records.
+__global__ void __launch_bounds__(256) k_full_relax_outcome(FullArgs a)
+{
+    __shared__ RelaxSmem S;
+    int sweeps = 0;
+    for (int s = 1; s <= kRelaxSweeps && !sweeps; s++)
+        if (*((volatile int*)&a.changed[s]) == 0) sweeps = s;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    if (sweeps) {
+        long long tot = 0;
+        int cnt = 0;
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmb; k += gridDim.x * blockDim.x) {
+            const int fmv = __ldcg(a.final_mv + k);
             a.out_mv[k] = fmv;
-            int d = a.final_dist[k];
+            const int d = a.final_dist[k];
             if (a.out_dist) a.out_dist[k] = d;
             if (a.incl && a.incl[k]) {
                 tot += d;
                 cnt++;
             }
         }
-    }
-    if (lane == 0) {
-        S.red_total[wib] = tot;
-        S.red_count[wib] = cnt;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        long long t = 0;
-        int c = 0;
-        for (int w = 0; w < 8; w++) {
-            t += S.red_total[w];
-            c += S.red_count[w];
+        for (int o = 16; o > 0; o >>= 1) {
+            tot += __shfl_xor_sync(0xffffffffu, tot, o);
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
         }
-        if (c) {
-            atomicAdd(reinterpret_cast<unsigned long long*>(&a.ctrl->total), (unsigned long long)t);
-            atomicAdd(&a.ctrl->count, c);
+        if (lane == 0 && cnt) {
+            atomicAdd(reinterpret_cast<unsigned long long*>(&a.ctrl->total), (unsigned long long)tot);
+            atomicAdd(&a.ctrl->count, cnt);
         }
-    }
-}
-
-__global__ void __launch_bounds__(256, 2) k_full_relax(FullArgs a)
-{
-    __shared__ RelaxSmem S;
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int gwarp = blockIdx.x * 8 + wib, nwarps = gridDim.x * 8;
-    bool converged = false;
-    int sweep = 1;
-    for (; sweep <= kRelaxSweeps; sweep++) {
-        int changed = 0;
-        // lane per MB (MBs gwarp + lane*nwarps ...) to find the MBs whose
-        // prediction moved, then the warp on each
-        for (int base = gwarp; base < a.nmb; base += 32 * nwarps) {
-            const int k = base + lane * nwarps;
-            int px = 0, py = 0, key = 0;
-            bool moved = false;
-            if (k < a.nmb) {
-                median_pred(a.final_mv, __ldcg(&a.spec4[k].w), k, a.cols, &px, &py);
-                key = pack_mv(px, py);
-                moved = __ldcg(a.pred_used + k) != key;
-            }
-            unsigned todo = __ballot_sync(0xffffffffu, moved);
-            while (todo) {
-                const int f = __ffs(todo) - 1;
-                todo &= todo - 1;
-                const int kk = base + f * nwarps, fkey = __shfl_sync(0xffffffffu, key, f);
-                const int fx = __shfl_sync(0xffffffffu, px, f), fy = __shfl_sync(0xffffffffu, py, f);
-                int4* cache = a.cache + (size_t)kk * KCACHE;
-                int4 rec;
-                const bool hit = cache_probe(cache, fkey, lane, &rec);
-                if (!hit) rec = evaluate(a, kk, fx, fy, lane);
-                if (lane == 0) {
-                    atomicAdd(&a.ctrl->relax_evals, 1);
-                    if (!hit) {
-                        atomicAdd(&a.ctrl->relax_miss, 1);
-                        __stcg(cache + kCacheRelax + (sweep % 3), rec);
-                    }
-                    __stcg(a.pred_used + kk, fkey);
-                    a.final_dist[kk] = rec.w;
-                    if (__ldcg(a.final_mv + kk) != rec.z) {
-                        __stcg(a.final_mv + kk, rec.z);
-                        changed = 1;
-                    }
-                }
-                __syncwarp();
-            }
-        }
-        if (lane == 0 && changed) atomicAdd(&a.changed[sweep], 1);
-        if (!grid_sync(a.ctrl->bar, &a.ctrl->status, gridDim.x, a.spin_limit)) return;
-        if (*((volatile int*)&a.changed[sweep]) == 0) {
-            converged = true;
-            break;
-        }
-    }
-    if (converged) {
-        write_outputs_and_average(a, S, gwarp, nwarps, lane, wib);
-        if (!grid_sync(a.ctrl->bar, &a.ctrl->status, gridDim.x, a.spin_limit)) return;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
-            long long t = *((volatile long long*)&a.ctrl->total);
-            int c = *((volatile int*)&a.ctrl->count);
-            if (a.out_avg) *a.out_avg = c ? t / c : 0;
-            a.ctrl->sweeps = sweep;
+            a.ctrl->sweeps = sweeps;
             a.ctrl->converged = 1;
         }
         return;
     }
-    // Not converged: block 0 finds the frame's dominant vectors.
     if (blockIdx.x != 0) return;
     for (int i = threadIdx.x; i < 2048; i += blockDim.x) {
         S.u.hist.keys[i] = kEmpty;
         S.u.hist.counts[i] = 0;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < a.nmb; k += blockDim.x) {
-        int v = __ldcg(a.final_mv + k);
-        unsigned h = ((unsigned)v * 2654435761u) >> 21;  // 11 bits
-        for (int probe = 0; probe < 32; probe++) {
-            int slot = (h + probe) & 2047;
-            int prev = atomicCAS(&S.u.hist.keys[slot], kEmpty, v);
-            if (prev == kEmpty || prev == v) {
-                atomicAdd(&S.u.hist.counts[slot], 1);
-                break;
+    for (int k0 = threadIdx.x; k0 < a.nmb; k0 += 8 * blockDim.x) {
+        int vals[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {  // eight loads in flight per thread
+            const int k = k0 + u * blockDim.x;
+            vals[u] = k < a.nmb ? __ldcg(a.final_mv + k) : kEmpty;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int v = vals[u];
+            if (v == kEmpty) continue;
+            unsigned h = ((unsigned)v * 2654435761u) >> 21;  // 11 bits
+            for (int probe = 0; probe < 32; probe++) {
+                int slot = (h + probe) & 2047;
+                int prev = atomicCAS(&S.u.hist.keys[slot], kEmpty, v);
+                if (prev == kEmpty || prev == v) {
+                    atomicAdd(&S.u.hist.counts[slot], 1);
+                    break;
+                }
             }
         }
     }
@@ -863,10 +860,10 @@ __global__ void __launch_bounds__(256) k_full_wave_outputs(FullArgs a)
     }
 }
 
-// The average, once every output block has added its sums.
-__global__ void k_full_wave_average(FullArgs a)
+// The included-distortion average, once every output block has added its sums.
+__global__ void k_full_average(FullArgs a)
 {
-    if (*((volatile int*)&a.ctrl->converged) || (*((volatile int*)&a.ctrl->status) & ST_TIMEOUT)) return;
+    if (*((volatile int*)&a.ctrl->status) & ST_TIMEOUT) return;
     const long long t = a.ctrl->total;
     const int c = a.ctrl->count;
     if (a.out_avg) *a.out_avg = c ? t / c : 0;
@@ -883,10 +880,7 @@ constexpr int kWaveMaxCols = 512;  // 8192 / 16
 
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
 {
-    int per_sm = 0;
-    VPP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_full_relax, 256, 0));
-    if (per_sm < 1) return VPPGPU_ERR_UNSUPPORTED;
-    *resolve_cap = per_sm * ctx->sm_count;
+    *resolve_cap = ctx->sm_count * 8;
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -901,10 +895,15 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid)
     k_full_sweep0<<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     {
-        void* params[] = {(void*)&args};
-        VPP_CUDA(cudaLaunchCooperativeKernel((const void*)k_full_relax, dim3(resolve_grid), dim3(256), params, 0,
-                                             ctx->stream));
-        ctx->launches++;
+        // many warps, few MBs each: a sweep's latency is its busiest warp's evaluations
+        const int want = (args.nmb + 7) / 8, cap = ctx->sm_count * 4, blocks = want < cap ? want : cap;
+        for (int sweep = 1; sweep <= kRelaxSweeps; sweep++) {
+            k_full_relax_sweep<<<blocks, 256, 0, ctx->stream>>>(args, sweep);
+            VPP_CHECK_LAUNCH(ctx);
+        }
+        const int ob = (args.nmb + 255) / 256, ocap = ctx->sm_count * 4;
+        k_full_relax_outcome<<<ob < ocap ? ob : ocap, 256, 0, ctx->stream>>>(args);
+        VPP_CHECK_LAUNCH(ctx);
     }
     {
         const int blocks = (args.nmb + 7) / 8, cap = ctx->sm_count * 8, grid = blocks < cap ? blocks : cap;
@@ -926,7 +925,7 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid)
         const int blocks = (args.nmb + 255) / 256, cap = ctx->sm_count * 4;
         k_full_wave_outputs<<<blocks < cap ? blocks : cap, 256, 0, ctx->stream>>>(args);
         VPP_CHECK_LAUNCH(ctx);
-        k_full_wave_average<<<1, 1, 0, ctx->stream>>>(args);
+        k_full_average<<<1, 1, 0, ctx->stream>>>(args);
         VPP_CHECK_LAUNCH(ctx);
     }
     return VPPGPU_OK;
