@@ -150,6 +150,90 @@ def cpu_baseline(frames, nthreads: int, nframes: int):
     return nframes * NMB / dt, dt
 
 
+BATCH_SIZES = [(176, 144), (352, 288), (1280, 720), (1920, 1080), (3840, 2160)]
+BATCH_SEQS, BATCH_FRAMES, BATCH_BASES = 64, 8, 2
+
+
+def batched_workload(torch, dev):
+    """The mixed-resolution batch: 64 sequences, uniform over QCIF, CIF, 720p,
+    1080p and 4K, 8 frames each (7 frame pairs per sequence).  Generating 4K
+    content on the host costs ~15 s per sequence, so each size has 2 seeded
+    base sequences and sequence i uses base (i // 5) % 2 of size i % 5; every
+    job is still estimated on its own."""
+    from imagecodingutils_gb300 import synth
+    bases = {}
+    for si, (w, h) in enumerate(BATCH_SIZES):
+        for b in range(BATCH_BASES):
+            fr = synth.pan_sequence(5000 + 10 * si + b, w, h, BATCH_FRAMES)
+            bases[(si, b)] = torch.from_numpy(np.stack(fr)).to(dev)
+    jobs = []
+    for i in range(BATCH_SEQS):
+        si, b = i % len(BATCH_SIZES), (i // len(BATCH_SIZES)) % BATCH_BASES
+        w, h = BATCH_SIZES[si]
+        for t in range(BATCH_FRAMES - 1):
+            jobs.append((si, b, t, w, h))
+    return bases, jobs
+
+
+def run_batched(args, torch, vpp, _lib, L, ctx, stream, dev):
+    bases, spec = batched_workload(torch, dev)
+    outs = [torch.empty(((w // 16) * (h // 16), 2), dtype=torch.int16, device=dev) for (_, _, _, w, h) in spec]
+    outs_plain = [torch.empty_like(o) for o in outs]
+    mbs = sum((w // 16) * (h // 16) for (_, _, _, w, h) in spec)
+
+    def job(i, dst):
+        si, b, t, w, h = spec[i]
+        fr = bases[(si, b)]
+        return (fr[t + 1].data_ptr(), fr[t].data_ptr(), w, h, MOTION_RANGE, dst[i].data_ptr())
+
+    jobs = [job(i, outs) for i in range(len(spec))]
+    batch = vpp.MotionEstimatorBatch(streams=args.batch_streams, ctx=ctx)
+    plain_me = {}
+    for (_, _, _, w, h) in spec:
+        if (w, h) not in plain_me:
+            hh = C.c_void_p()
+            _lib.check(L.vppgpu_me_create(ctx.handle, _lib.ME_FULL, w, h, MOTION_RANGE, C.byref(hh)), "vppgpu_me_create")
+            plain_me[(w, h)] = hh
+
+    def plain_pass():
+        for i in range(len(spec)):
+            si, b, t, w, h = spec[i]
+            fr = bases[(si, b)]
+            _lib.check(L.vppgpu_me_estimate_device(plain_me[(w, h)], C.c_void_p(fr[t + 1].data_ptr()),
+                                                   C.c_void_p(fr[t].data_ptr()), None, None,
+                                                   C.c_void_p(outs_plain[i].data_ptr()), None, None),
+                       "vppgpu_me_estimate_device")
+
+    def timed(fn, reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        fn()  # warm-up (creates the per-geometry estimators)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def batched_pass():
+        st, _ = batch.run(jobs)
+        assert all(x == 0 for x in st), st
+
+    ms_plain = timed(plain_pass, args.batch_reps)
+    ms_batch = timed(batched_pass, args.batch_reps)
+    same = all(torch.equal(a, b) for a, b in zip(outs, outs_plain))
+    for hh in plain_me.values():
+        L.vppgpu_me_destroy(hh)
+    batch.close()
+    return {
+        "value": mbs / (ms_batch * 1e-3), "unit": UNIT, "plain_value": mbs / (ms_plain * 1e-3),
+        "ratio_vs_plain": ms_plain / ms_batch, "ms_per_batch": ms_batch, "plain_ms_per_batch": ms_plain,
+        "jobs": len(spec), "macroblocks": mbs, "streams": args.batch_streams, "identical_to_plain": bool(same),
+        "workload": "64 sequences x 7 frame pairs, uniform over 176x144, 352x288, 1280x720, 1920x1080, 3840x2160; "
+                    "Full ME motionRange 128; device-resident",
+    }
+
+
 def run_reference(args, rank, world):
     """One step = one frame-pair estimate, as in the GPU arm; the K steps are
     spread over all host threads (one estimator per thread)."""
@@ -189,6 +273,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-frames", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-streams", type=int, default=8)
+    ap.add_argument("--batch-reps", type=int, default=3)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -314,6 +401,7 @@ def main():
             v_cpu, dt_cpu = cpu_baseline(frames, nth, min(args.cpu_frames, NFRAMES - 1))
             cpu = {"value": v_cpu, "unit": UNIT, "cores": nth, "kind": "port",
                    "sample": f"{min(args.cpu_frames, NFRAMES - 1)} 1080p frame pairs, {nth} threads, {dt_cpu:.1f} s"}
+        batched = None if args.no_batch else run_batched(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}")
         pk, pk_kind = peaks()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -335,7 +423,7 @@ def main():
                            "max": per_frame[-1], "unit": "device ms per frame, plain per-frame form"},
             "resolve_sweeps_last_frame": sweeps.value,
             "hbm_peak_gbs": pk.get("hbm_gbs"), "peaks_source": pk_kind,
-            "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check,
+            "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

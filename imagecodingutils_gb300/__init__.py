@@ -186,6 +186,48 @@ INTRA_FLAG_ID = 1
 TransformAndQuant, TransformOnly, QuantOnly = 0, 1, 2
 
 
+class MotionEstimatorBatch:
+    """Many independent frame pairs of mixed sizes in one call
+    (vppgpu_me_batch_*; no vpp counterpart).  Jobs are dicts or tuples of
+    device pointers: (src, ref, width, height, motion_range, mv_out[,
+    mb_dist_out[, dist_included]]); run() returns (statuses, avgDistortions)."""
+
+    def __init__(self, streams: int = 4, kind: int = _lib.ME_FULL, ctx: Context | None = None):
+        self._ctx = ctx or get_context()
+        h = C.c_void_p()
+        check(load().vppgpu_me_batch_create(self._ctx.handle, kind, int(streams), C.byref(h)), "vppgpu_me_batch_create")
+        self.handle = h
+
+    def run(self, jobs):
+        n = len(jobs)
+        arr = (_lib.MeJob * max(n, 1))()
+        for i, j in enumerate(jobs):
+            src, ref, w, hgt, mr, mv = j[:6]
+            dist = j[6] if len(j) > 6 else None
+            incl = j[7] if len(j) > 7 else None
+            arr[i] = _lib.MeJob(src, ref, w, hgt, mr, incl, mv, dist)
+        st = (C.c_int * max(n, 1))()
+        avg = (C.c_long * max(n, 1))()
+        load().vppgpu_me_batch_run(self.handle, arr, n, st, avg)
+        return list(st)[:n], list(avg)[:n]
+
+    def launch_count(self) -> int:
+        c = C.c_ulonglong()
+        check(load().vppgpu_me_batch_launch_count(self.handle, C.byref(c)), "vppgpu_me_batch_launch_count")
+        return c.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().vppgpu_me_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class _ForwardBase:
     LAYOUT = _lib.LAYOUT_BLOCKS
     UNIT = 16

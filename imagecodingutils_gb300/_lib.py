@@ -55,6 +55,10 @@ SIGNATURES = {
     "vppgpu_me_timing": (_I, [_P, C.POINTER(_I), C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_double)]),
     "vppgpu_me_timing_stages": (_I, [_P, C.POINTER(_I), _P]),
+    "vppgpu_me_batch_create": (_I, [_P, _I, _I, C.POINTER(_P)]),
+    "vppgpu_me_batch_destroy": (_I, [_P]),
+    "vppgpu_me_batch_run": (_I, [_P, _P, _I, _P, _P]),
+    "vppgpu_me_batch_launch_count": (_I, [_P, C.POINTER(C.c_ulonglong)]),
     "vppgpu_calibrate_dp4a": (_I, [_P, C.POINTER(C.c_double)]),
     "vppgpu_me_full_estimate_noalloc": (_I, [_P, _P, _I, _I, _I, _P, _P, _P, _P, C.POINTER(C.c_long), _P]),
     "vppgpu_fwd4x4": (_I, [_P, _P, _LL, _I, _I, _I, _I]),
@@ -105,3 +109,10 @@ def status_string(s: int) -> str:
 def check(status: int, what: str) -> None:
     if status != OK:
         raise VppGpuError(status, what)
+
+
+class MeJob(C.Structure):
+    """vppgpu_me_job (include/vppgpu.h)."""
+    _fields_ = [("src", C.c_void_p), ("ref", C.c_void_p), ("width", C.c_int), ("height", C.c_int),
+                ("motion_range", C.c_int), ("dist_included", C.c_void_p), ("mv_out", C.c_void_p),
+                ("mb_dist_out", C.c_void_p)]

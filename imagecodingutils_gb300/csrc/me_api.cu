@@ -4,6 +4,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <new>
+
 #include "me_common.cuh"
 #include "me_internal.h"
 
@@ -384,3 +386,197 @@ extern "C" int vppgpu_me_last_stats(vppgpu_me* me, int* stats8)
     for (int i = 0; i < 8; i++) stats8[i] = v[i];
     return VPPGPU_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batched estimation: many independent frame pairs, any mix of sizes, spread
+// over several streams so that one frame's latency-bound stages run beside
+// another frame's search.  Jobs go to streams longest first (by macroblock
+// count), each to the stream with the least work so far; each stream keeps
+// one estimator per frame geometry, created on first use and reused by later
+// batches.  The batch is ordered after the work already on the context's
+// stream and before work enqueued there later.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kBatchMaxStreams = 16;
+
+struct BatchSlot {
+    vppgpu_ctx* ctx = nullptr;  // own stream
+    struct Entry {
+        int W, H, range;
+        vppgpu_me* me;
+    };
+    Entry pool[8];
+    int npool = 0;
+    long long load = 0;
+};
+}  // namespace
+
+struct vppgpu_me_batch {
+    vppgpu_ctx* parent;
+    int kind;
+    int nslots;
+    BatchSlot slot[kBatchMaxStreams];
+    vppgpu::MeCtrl* h_ctrl;  // pinned, one per job of the current batch
+    int cap;
+    int* order;
+    int* where;
+    cudaEvent_t start, done[kBatchMaxStreams];
+};
+
+namespace {
+
+void batch_free(vppgpu_me_batch* b)
+{
+    if (!b) return;
+    cudaSetDevice(b->parent->device);
+    for (int s = 0; s < b->nslots; s++) {
+        BatchSlot& sl = b->slot[s];
+        for (int i = 0; i < sl.npool; i++) vppgpu_me_destroy(sl.pool[i].me);
+        if (sl.ctx) vppgpu_ctx_destroy(sl.ctx);
+        if (b->done[s]) cudaEventDestroy(b->done[s]);
+    }
+    if (b->start) cudaEventDestroy(b->start);
+    if (b->h_ctrl) cudaFreeHost(b->h_ctrl);
+    free(b->order);
+    free(b->where);
+    free(b);
+}
+
+int slot_estimator(vppgpu_me_batch* b, BatchSlot& sl, int W, int H, int range, vppgpu_me** out)
+{
+    for (int i = 0; i < sl.npool; i++)
+        if (sl.pool[i].W == W && sl.pool[i].H == H && sl.pool[i].range == range) {
+            *out = sl.pool[i].me;
+            return VPPGPU_OK;
+        }
+    if (sl.npool == 8) {  // evict the oldest geometry
+        vppgpu_me_destroy(sl.pool[0].me);
+        for (int i = 1; i < 8; i++) sl.pool[i - 1] = sl.pool[i];
+        sl.npool--;
+    }
+    vppgpu_me* me = nullptr;
+    int rc = vppgpu_me_create(sl.ctx, b->kind, W, H, range, &me);
+    if (rc) return rc;
+    sl.pool[sl.npool++] = {W, H, range, me};
+    *out = me;
+    return VPPGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vppgpu_me_batch_create(vppgpu_ctx* ctx, int kind, int streams, vppgpu_me_batch** out)
+{
+    if (!ctx || !out || streams < 1) return VPPGPU_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (kind != VPPGPU_ME_FULL) return VPPGPU_ERR_UNSUPPORTED;
+    int rc = vppgpu::bind(ctx);
+    if (rc) return rc;
+    vppgpu_me_batch* b = (vppgpu_me_batch*)calloc(1, sizeof(vppgpu_me_batch));
+    if (!b) return VPPGPU_ERR_OUT_OF_MEMORY;
+    b->parent = ctx;
+    b->kind = kind;
+    b->nslots = streams < kBatchMaxStreams ? streams : kBatchMaxStreams;
+    for (int s = 0; s < b->nslots; s++) {
+        new (&b->slot[s]) BatchSlot();
+        if ((rc = vppgpu_ctx_create(ctx->device, &b->slot[s].ctx)) ||
+            cudaEventCreateWithFlags(&b->done[s], cudaEventDisableTiming) != cudaSuccess) {
+            batch_free(b);
+            return rc ? rc : VPPGPU_ERR_CUDA;
+        }
+    }
+    if (cudaEventCreateWithFlags(&b->start, cudaEventDisableTiming) != cudaSuccess) {
+        batch_free(b);
+        return VPPGPU_ERR_CUDA;
+    }
+    *out = b;
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_batch_destroy(vppgpu_me_batch* b)
+{
+    if (!b) return VPPGPU_ERR_INVALID_ARG;
+    batch_free(b);
+    return VPPGPU_OK;
+}
+
+int vppgpu_me_batch_run(vppgpu_me_batch* b, const vppgpu_me_job* jobs, int n, int* status_out, long* avg_out)
+{
+    if (!b || (n > 0 && !jobs) || n < 0) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(b->parent);
+    if (rc) return rc;
+    for (int j = 0; j < n; j++) {
+        const vppgpu_me_job& J = jobs[j];
+        if (!J.src || !J.ref || !J.mv_out || J.width < 16 || J.height < 16 || J.width % 16) return VPPGPU_ERR_INVALID_ARG;
+    }
+    if (n > b->cap) {
+        if (b->h_ctrl) cudaFreeHost(b->h_ctrl);
+        free(b->order);
+        free(b->where);
+        b->h_ctrl = nullptr;
+        b->order = (int*)malloc(sizeof(int) * (size_t)n);
+        b->where = (int*)malloc(sizeof(int) * (size_t)n);
+        b->cap = 0;
+        if (!b->order || !b->where || cudaMallocHost((void**)&b->h_ctrl, sizeof(vppgpu::MeCtrl) * (size_t)n) != cudaSuccess)
+            return VPPGPU_ERR_OUT_OF_MEMORY;
+        b->cap = n;
+    }
+    // longest job first, each to the least-loaded stream
+    for (int j = 0; j < n; j++) b->order[j] = j;
+    auto mbs = [&](int j) { return (long long)(jobs[j].width / 16) * (jobs[j].height / 16); };
+    for (int i = 1; i < n; i++) {  // insertion sort, descending
+        int v = b->order[i], k = i - 1;
+        while (k >= 0 && mbs(b->order[k]) < mbs(v)) {
+            b->order[k + 1] = b->order[k];
+            k--;
+        }
+        b->order[k + 1] = v;
+    }
+    for (int s = 0; s < b->nslots; s++) b->slot[s].load = 0;
+    for (int i = 0; i < n; i++) {
+        int best = 0;
+        for (int s = 1; s < b->nslots; s++)
+            if (b->slot[s].load < b->slot[best].load) best = s;
+        b->where[b->order[i]] = best;
+        b->slot[best].load += mbs(b->order[i]);
+    }
+    VPP_CUDA(cudaEventRecord(b->start, b->parent->stream));
+    for (int s = 0; s < b->nslots; s++) VPP_CUDA(cudaStreamWaitEvent(b->slot[s].ctx->stream, b->start, 0));
+    for (int i = 0; i < n; i++) {
+        const int j = b->order[i];
+        const vppgpu_me_job& J = jobs[j];
+        BatchSlot& sl = b->slot[b->where[j]];
+        vppgpu_me* me = nullptr;
+        if ((rc = slot_estimator(b, sl, J.width, J.height, J.motion_range, &me))) return rc;
+        if ((rc = vppgpu_me_estimate_device(me, J.src, J.ref, J.dist_included, nullptr, J.mv_out, J.mb_dist_out,
+                                            nullptr)))
+            return rc;
+        VPP_CUDA(cudaMemcpyAsync(b->h_ctrl + j, me->ctrl, sizeof(vppgpu::MeCtrl), cudaMemcpyDeviceToHost,
+                                 sl.ctx->stream));
+    }
+    for (int s = 0; s < b->nslots; s++) {
+        VPP_CUDA(cudaEventRecord(b->done[s], b->slot[s].ctx->stream));
+        VPP_CUDA(cudaStreamWaitEvent(b->parent->stream, b->done[s], 0));
+    }
+    VPP_CUDA(cudaStreamSynchronize(b->parent->stream));
+    int first = VPPGPU_OK;
+    for (int j = 0; j < n; j++) {
+        const int st = status_from_ctrl(b->h_ctrl[j]);
+        if (status_out) status_out[j] = st;
+        if (avg_out) avg_out[j] = b->h_ctrl[j].count ? (long)(b->h_ctrl[j].total / b->h_ctrl[j].count) : 0;
+        if (st && !first) first = st;
+    }
+    return first;
+}
+
+int vppgpu_me_batch_launch_count(vppgpu_me_batch* b, unsigned long long* count)
+{
+    if (!b || !count) return VPPGPU_ERR_INVALID_ARG;
+    unsigned long long c = 0;
+    for (int s = 0; s < b->nslots; s++) c += b->slot[s].ctx->launches;
+    *count = c;
+    return VPPGPU_OK;
+}
+
+}  // extern "C"

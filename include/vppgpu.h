@@ -134,6 +134,30 @@ int vppgpu_me_timing(vppgpu_me* me, int* n, double* pack_ms, double* search_ms, 
  * sub-pel + tie trees, prediction-dependent resolve}. */
 int vppgpu_me_timing_stages(vppgpu_me* me, int* n, double* stage_ms4);
 
+/* Batched estimation, no vpp counterpart (the codecs estimate one frame at a
+ * time).  A batch runs many independent frame pairs of any mix of sizes on
+ * `streams` streams of its own, so that the latency-bound stages of one
+ * frame overlap the search of others; outputs are identical to estimating
+ * each job alone.  Device pointers; a job's planes are W x H luma 0..255.
+ * vppgpu_me_batch_run enqueues after the work on the context's stream,
+ * waits for the batch, and returns per job its status and avgDistortion
+ * (either array may be NULL); the return value is the first non-zero job
+ * status.  Estimators are created per stream and frame geometry on first
+ * use and kept for later batches. */
+typedef struct vppgpu_me_batch vppgpu_me_batch;
+typedef struct {
+    const short* src;                    /* device, W x H */
+    const short* ref;                    /* device, W x H */
+    int width, height, motion_range;
+    const unsigned char* dist_included;  /* device, one flag per MB, or NULL */
+    short* mv_out;                       /* device, 2 shorts per MB */
+    int* mb_dist_out;                    /* device, one int per MB, or NULL */
+} vppgpu_me_job;
+int vppgpu_me_batch_create(vppgpu_ctx* ctx, int kind, int streams, vppgpu_me_batch** out);
+int vppgpu_me_batch_destroy(vppgpu_me_batch* b);
+int vppgpu_me_batch_run(vppgpu_me_batch* b, const vppgpu_me_job* jobs, int n, int* status_out, long* avg_out);
+int vppgpu_me_batch_launch_count(vppgpu_me_batch* b, unsigned long long* count);
+
 /* Measured dp4a issue rate of the whole device (instructions per second),
  * the integer-ALU roofline of the motion search.  No vpp counterpart. */
 int vppgpu_calibrate_dp4a(vppgpu_ctx* ctx, double* dp4a_per_second);
