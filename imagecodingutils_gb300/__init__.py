@@ -178,6 +178,21 @@ class MotionEstimatorH264ImplFull(_MotionEstimatorBase):
     KIND = _lib.ME_FULL
 
 
+class MotionEstimatorH264ImplMultiresCross(_MotionEstimatorBase):
+    """GPU MotionEstimatorH264ImplMultiresCross (src/CodecUtils/MotionEstimatorH264ImplMultiresCross.cpp).
+    No predictor; avgDistortion counts every macroblock (the partial bottom row
+    too) when pDistortionIncluded is None, as the reference does."""
+
+    KIND = _lib.ME_MULTIRES_CROSS
+
+    def GetMode(self) -> int:
+        if self._h_me:  # SetMode(0) resolves by picture area
+            m = C.c_int()
+            check(load().vppgpu_me_get_mode(self._h_me, C.byref(m)), "vppgpu_me_get_mode")
+            return m.value
+        return self._mode
+
+
 # ---------------------------------------------------------------------------
 # 4x4 transforms
 # ---------------------------------------------------------------------------

@@ -21,6 +21,7 @@ struct vppgpu_me {
     size_t plane_size;
     vppgpu::WaveRec* d_wave_rec;
     int* d_wave_choice;
+    unsigned char* d_mrc;  // MultiresCross level planes (mrc_scratch_bytes)
     int* spec;  // 5 * nmb: {vector, distortion, zero distortion, flags} per MB, then full-pel winners
     int* tables;
     int* tie_list;
@@ -93,6 +94,7 @@ void me_free(vppgpu_me* me)
     cudaFree(me->d_hpel);
     cudaFree(me->d_wave_rec);
     cudaFree(me->d_wave_choice);
+    cudaFree(me->d_mrc);
     cudaFree(me->spec);
     cudaFree(me->tables);
     cudaFree(me->tie_list);
@@ -161,6 +163,9 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
 {
     vppgpu_ctx* ctx = me->ctx;
     VPP_CUDA(cudaMemsetAsync(me->ctrl, 0, sizeof(vppgpu::MeCtrl), ctx->stream));
+    if (me->kind == VPPGPU_ME_MULTIRES_CROSS)
+        return vppgpu::mrc_launch(ctx, me->W, me->H, me->motion_range, me->mode, d_src16, d_ref16, me->d_mrc, d_incl,
+                                  d_mv, d_dist, d_avg, me->ctrl);
     VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
     vppgpu::FullArgs a = full_args(me, d_incl, d_slice, d_mv, d_dist, d_avg, lambda);
     return vppgpu::full_launch(ctx, a, me->nmb, d_src16, d_ref16, me->resolve_grid, ring_slot(me));
@@ -170,6 +175,7 @@ int status_from_ctrl(const vppgpu::MeCtrl& c)
 {
     if (c.status & vppgpu::ST_PIXEL_RANGE) return VPPGPU_ERR_PIXEL_RANGE;
     if (c.status & vppgpu::ST_TIMEOUT) return VPPGPU_ERR_TIMEOUT;
+    if (c.status & vppgpu::ST_OUT_OF_BOUNDS) return VPPGPU_ERR_UNSUPPORTED;
     return VPPGPU_OK;
 }
 
@@ -186,7 +192,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
     if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
     if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
-    if (kind != VPPGPU_ME_FULL) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind != VPPGPU_ME_FULL && kind != VPPGPU_ME_MULTIRES_CROSS) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me* me = (vppgpu_me*)calloc(1, sizeof(vppgpu_me));
@@ -205,6 +211,23 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     size_t npix = (size_t)width * height;
     size_t npad = (size_t)me->rstride * (height + 2 * vppgpu::PAD);
     me->plane_size = npad;
+    if (kind == VPPGPU_ME_MULTIRES_CROSS) {
+        // MotionEstimatorH264ImplMultiresCross(…) + Create(): the level planes and outputs only
+        if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
+            (rc = dalloc(&me->d_mrc, vppgpu::mrc_scratch_bytes(width, height))) ||
+            (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
+            (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||
+            (rc = dalloc(&me->d_slice, me->nmb)) || (rc = dalloc(&me->ctrl, 1))) {
+            me_free(me);
+            return rc;
+        }
+        if (cudaMallocHost((void**)&me->h_ctrl, sizeof(vppgpu::MeCtrl)) != cudaSuccess) {
+            me_free(me);
+            return VPPGPU_ERR_OUT_OF_MEMORY;
+        }
+        *out = me;
+        return VPPGPU_OK;
+    }
     if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) || (rc = dalloc(&me->d_src8, npix)) ||
         (rc = dalloc(&me->d_refp, npad)) || (rc = dalloc(&me->d_hpel, 3 * npad)) ||
         (rc = dalloc(&me->d_wave_rec, vppgpu::wave_rec_count(me->cols, me->rows))) || (rc = dalloc(&me->d_wave_choice, me->nmb)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
@@ -239,6 +262,8 @@ int vppgpu_me_destroy(vppgpu_me* me)
 int vppgpu_me_set_mode(vppgpu_me* me, int mode)
 {
     if (!me) return VPPGPU_ERR_INVALID_ARG;
+    // SetMode(0) picks by picture area (MultiresCross.cpp:501-513)
+    if (mode == 0 && me->kind == VPPGPU_ME_MULTIRES_CROSS) mode = (me->W * me->H > 40000) ? 2 : 1;
     me->mode = mode;
     return VPPGPU_OK;
 }
@@ -470,7 +495,7 @@ int vppgpu_me_batch_create(vppgpu_ctx* ctx, int kind, int streams, vppgpu_me_bat
 {
     if (!ctx || !out || streams < 1) return VPPGPU_ERR_INVALID_ARG;
     *out = nullptr;
-    if (kind != VPPGPU_ME_FULL) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind != VPPGPU_ME_FULL && kind != VPPGPU_ME_MULTIRES_CROSS) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me_batch* b = (vppgpu_me_batch*)calloc(1, sizeof(vppgpu_me_batch));

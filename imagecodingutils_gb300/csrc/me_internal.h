@@ -84,6 +84,13 @@ struct FullArgs {
 constexpr int NDICT = 8;    // dictionary vectors
 constexpr int WAVE_WARPS = 5;   // most warps (bands of 32 rows) of one wavefront launch
 
+// MultiresCross (me_mrc.cu): level planes in one scratch buffer.
+constexpr int ST_OUT_OF_BOUNDS = 4;  // a read the reference would make outside its buffer
+size_t mrc_scratch_bytes(int W, int H);
+int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const short* d_src16, const short* d_ref16,
+               unsigned char* scratch, const unsigned char* incl, int* out_mv, int* out_dist, long long* out_avg,
+               MeCtrl* ctrl);
+
 size_t full_search_smem();
 // Launch the prediction-dependent tail (sweep 0, relaxation, dictionary
 // precompute, exact wavefront) of an estimate whose search has run.
