@@ -234,6 +234,134 @@ def run_batched(args, torch, vpp, _lib, L, ctx, stream, dev):
     }
 
 
+def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with_cpu):
+    """MotionEstimatorH264ImplMultiresCross (mode 0 -> 2 at 1080p) on the same
+    1080p sequence: device-resident MB/s over the frame rotation, and the
+    oracle port on all host threads as its CPU baseline."""
+    h = C.c_void_p()
+    _lib.check(L.vppgpu_me_create(ctx.handle, _lib.ME_MULTIRES_CROSS, W, H, MOTION_RANGE, C.byref(h)), "vppgpu_me_create")
+    _lib.check(L.vppgpu_me_set_mode(h, 0), "vppgpu_me_set_mode")
+    mode = C.c_int()
+    L.vppgpu_me_get_mode(h, C.byref(mode))
+    dev_frames = torch.from_numpy(np.stack(frames)).to(dev)
+    d_mv = torch.empty((NMB, 2), dtype=torch.int16, device=dev)
+
+    def step(t):
+        i = t % (NFRAMES - 1)
+        _lib.check(L.vppgpu_me_estimate_device(h, C.c_void_p(dev_frames[i + 1].data_ptr()),
+                                               C.c_void_p(dev_frames[i].data_ptr()), None, None,
+                                               C.c_void_p(d_mv.data_ptr()), None, None), "vppgpu_me_estimate_device")
+
+    for t in range(args.warmup):
+        step(t)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(args.steps, 50)
+    e0.record(stream)
+    for t in range(steps):
+        step(t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    step(0)
+    torch.cuda.synchronize()
+    out = {"value": NMB / (ms * 1e-3), "unit": UNIT, "ms_per_frame": ms, "mode": mode.value,
+           "workload": f"MotionEstimatorH264ImplMultiresCross plain per-frame, {W}x{H}, motionRange {MOTION_RANGE}"}
+    if with_cpu:
+        from concurrent.futures import ThreadPoolExecutor
+        from oracle.oracle import Oracle
+        orc = Oracle()
+        mv_o, _, _ = orc.me_multires_cross(frames[1], frames[0], MOTION_RANGE, mode=mode.value)
+        out["parity_first_frame"] = bool(np.array_equal(d_mv.cpu().numpy(), mv_o))
+        nth = os.cpu_count() or 1
+        npairs = min(4 * nth, NFRAMES - 1)
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(nth) as ex:  # ctypes calls release the GIL: one estimate per thread
+            list(ex.map(lambda i: orc.me_multires_cross(frames[i + 1], frames[i], MOTION_RANGE, mode=mode.value),
+                        range(npairs)))
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": npairs * NMB / dt, "unit": UNIT, "cores": nth, "kind": "port",
+                               "sample": f"{npairs} 1080p frame pairs, {nth} threads, {dt:.1f} s"}
+    L.vppgpu_me_destroy(h)
+    return out
+
+
+class TqJob(C.Structure):
+    _fields_ = [("residual", C.c_void_p), ("levels", C.c_void_p), ("recon", C.c_void_p), ("width", C.c_int),
+                ("height", C.c_int), ("stride", C.c_int), ("qp", C.c_int), ("intra", C.c_int)]
+
+
+def run_hbm_paths(torch, _lib, L, ctx, stream, dev, pk):
+    """The HBM-bound rows: 4x4 transform + quantisation + dequantisation +
+    inverse on 1920x1080 4:2:0 residual frames (96 B of algorithmic traffic
+    per 4x4 block: residual in, levels and reconstruction out; QP 28 inter),
+    and fixed-point RGB24 -> YUV420 on 1920x1080 frames (6 B per pixel:
+    3 B in, 2 B luma and 1 B of chroma out as int16).  Working sets larger
+    than L2; CUDA events on the launching stream."""
+    from imagecodingutils_gb300 import synth
+    out = {}
+    nfr = 16
+    planes = []
+    for f in range(nfr):
+        yv, uv, vv = synth.residual_frame_420(900 + f)
+        for pl in (yv, uv, vv):
+            r = torch.from_numpy(np.ascontiguousarray(pl)).to(dev)
+            planes.append((r, torch.empty_like(r), torch.empty_like(r)))
+    jobs = (TqJob * len(planes))()
+    for i, (r, lv, rc) in enumerate(planes):
+        h, w = r.shape
+        jobs[i] = TqJob(r.data_ptr(), lv.data_ptr(), rc.data_ptr(), w, h, w, 28, 0)
+    d_jobs = torch.empty(C.sizeof(jobs), dtype=torch.uint8, device=dev)
+    d_jobs.copy_(torch.frombuffer(bytearray(bytes(jobs)), dtype=torch.uint8))
+    blocks = sum(r.numel() // 16 for r, _, _ in planes)
+
+    def tq():
+        _lib.check(L.vppgpu_tq_roundtrip_planes_device(ctx.handle, C.c_void_p(d_jobs.data_ptr()), len(planes),
+                                                       _lib.INV_ROWS_FIRST, None), "vppgpu_tq_roundtrip_planes_device")
+
+    def timed(fn, reps=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms = timed(tq)
+    gbs = blocks * 96 / (ms * 1e-3) / 1e9
+    out["transform_quant_roundtrip"] = {
+        "value": nfr / (ms * 1e-3), "unit": "frames/s", "ms_per_launch": ms, "frames_per_launch": nfr,
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": gbs / pk["hbm_gbs"] if pk.get("hbm_gbs") else None,
+                     "algorithmic_bytes_per_launch": blocks * 96},
+        "workload": "1920x1080 4:2:0 Laplacian(6) residual frames, T+Q / dequant + inverse, QP 28 inter"}
+    nrgb = 32
+    bgr = torch.from_numpy(np.stack([synth.rgb_frame(950 + f, W, H) for f in range(nrgb)])).to(dev)
+    ys = torch.empty((nrgb, H, W), dtype=torch.int16, device=dev)
+    us = torch.empty((nrgb, H // 2, W // 2), dtype=torch.int16, device=dev)
+    vs = torch.empty_like(us)
+
+    def conv():
+        _lib.check(L.vppgpu_rgb24_to_yuv420_frames_device(ctx.handle, _lib.RGB_FIXED_POINT, C.c_void_p(bgr.data_ptr()),
+                                                          nrgb, W, H, 0, 0, C.c_void_p(ys.data_ptr()),
+                                                          C.c_void_p(us.data_ptr()), C.c_void_p(vs.data_ptr())),
+                   "vppgpu_rgb24_to_yuv420_frames_device")
+
+    ms = timed(conv)
+    gbs = nrgb * W * H * 6 / (ms * 1e-3) / 1e9
+    out["rgb24_to_yuv420"] = {
+        "value": nrgb / (ms * 1e-3), "unit": "frames/s", "ms_per_launch": ms, "frames_per_launch": nrgb,
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": gbs / pk["hbm_gbs"] if pk.get("hbm_gbs") else None,
+                     "algorithmic_bytes_per_launch": nrgb * W * H * 6},
+        "workload": "FastFixedPointRGB24toYUV420Converter, 1920x1080 uniform BGR frames"}
+    return out
+
+
 def run_reference(args, rank, world):
     """One step = one frame-pair estimate, as in the GPU arm; the K steps are
     spread over all host threads (one estimator per thread)."""
@@ -402,7 +530,9 @@ def main():
             cpu = {"value": v_cpu, "unit": UNIT, "cores": nth, "kind": "port",
                    "sample": f"{min(args.cpu_frames, NFRAMES - 1)} 1080p frame pairs, {nth} threads, {dt_cpu:.1f} s"}
         batched = None if args.no_batch else run_batched(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}")
+        mrc = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu)
         pk, pk_kind = peaks()
+        hbm_rows = run_hbm_paths(torch, _lib, L, ctx, stream, f"cuda:{local}", pk)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -424,6 +554,7 @@ def main():
             "resolve_sweeps_last_frame": sweeps.value,
             "hbm_peak_gbs": pk.get("hbm_gbs"), "peaks_source": pk_kind,
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
+            "multires_cross": mrc, **hbm_rows,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
