@@ -474,7 +474,6 @@ def main():
         step_device(t)
     barrier()
     launches0 = ctx.launch_count()
-    _lib.check(L.vppgpu_me_set_timing(h, 1), "vppgpu_me_set_timing")
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     with ClockSampler(local) as clk:
         barrier()
@@ -486,6 +485,12 @@ def main():
     launches = ctx.launch_count() - launches0
     dev_ms = evs[0].elapsed_time(evs[-1])
     per_frame = sorted(evs[t].elapsed_time(evs[t + 1]) for t in range(args.steps))
+    # per-stage breakdown: the library's events around its stages (direct
+    # launches instead of the captured graph while timing is on)
+    _lib.check(L.vppgpu_me_set_timing(h, 1), "vppgpu_me_set_timing")
+    for t in range(min(args.steps, 200)):
+        step_device(t)
+    barrier()
     n = C.c_int()
     stage = (C.c_double * 4)()
     _lib.check(L.vppgpu_me_timing_stages(h, C.byref(n), stage), "vppgpu_me_timing_stages")

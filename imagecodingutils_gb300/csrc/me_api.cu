@@ -22,6 +22,11 @@ struct vppgpu_me {
     vppgpu::WaveRec* d_wave_rec;
     int* d_wave_choice;
     unsigned char* d_mrc;  // MultiresCross level planes (mrc_scratch_bytes)
+    vppgpu::JobDesc* d_job;  // this estimate's pointers, read by the kernels
+    // the Full estimator's kernel sequence, captured once per handle
+    cudaGraphExec_t graph;
+    unsigned long long graph_kernels;
+    int graph_state;  // 0 not tried, 1 captured, -1 unavailable (direct launches)
     int* spec;  // 5 * nmb: {vector, distortion, zero distortion, flags} per MB, then full-pel winners
     int* tables;
     int* tie_list;
@@ -95,6 +100,8 @@ void me_free(vppgpu_me* me)
     cudaFree(me->d_wave_rec);
     cudaFree(me->d_wave_choice);
     cudaFree(me->d_mrc);
+    cudaFree(me->d_job);
+    if (me->graph) cudaGraphExecDestroy(me->graph);
     cudaFree(me->spec);
     cudaFree(me->tables);
     cudaFree(me->tie_list);
@@ -120,8 +127,7 @@ int dalloc(T** p, size_t count)
     return VPPGPU_OK;
 }
 
-vppgpu::FullArgs full_args(vppgpu_me* me, const unsigned char* incl, const int* slice, int* out_mv, int* out_dist,
-                           long long* out_avg, double lambda)
+vppgpu::FullArgs full_args(vppgpu_me* me, double lambda)
 {
     vppgpu::FullArgs a;
     a.W = me->W;
@@ -145,11 +151,7 @@ vppgpu::FullArgs full_args(vppgpu_me* me, const unsigned char* incl, const int* 
     a.final_mv = me->state;
     a.final_dist = me->state + me->nmb;
     a.pred_used = me->state + 2 * me->nmb;
-    a.slice = slice;
-    a.incl = incl;
-    a.out_mv = out_mv;
-    a.out_dist = out_dist;
-    a.out_avg = out_avg;
+    a.job = me->d_job;
     a.ctrl = me->ctrl;
     a.changed = me->changed;
     a.lambda = lambda;
@@ -166,9 +168,37 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS)
         return vppgpu::mrc_launch(ctx, me->W, me->H, me->motion_range, me->mode, d_src16, d_ref16, me->d_mrc, d_incl,
                                   d_mv, d_dist, d_avg, me->ctrl);
+    int rc = vppgpu::set_job(ctx, me->d_job, vppgpu::JobDesc{d_src16, d_ref16, d_incl, d_slice, d_mv, d_dist, d_avg});
+    if (rc) return rc;
+    const vppgpu::FullArgs a = full_args(me, lambda);
+    cudaEvent_t* ev = ring_slot(me);
+    if (!ev && me->graph_state == 0) {
+        // capture the per-estimate sequence once; every later estimate is one graph launch
+        me->graph_state = -1;
+        cudaGraph_t g = nullptr;
+        const unsigned long long before = ctx->launches;
+        if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            int crc = VPPGPU_OK;
+            if (cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream) != cudaSuccess)
+                crc = VPPGPU_ERR_CUDA;
+            if (!crc) crc = vppgpu::full_launch(ctx, a, me->nmb, me->resolve_grid, nullptr);
+            const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+            if (!crc && e == cudaSuccess && g && cudaGraphInstantiate(&me->graph, g, 0) == cudaSuccess) {
+                me->graph_state = 1;
+                me->graph_kernels = ctx->launches - before;
+            }
+            if (g) cudaGraphDestroy(g);
+        }
+        ctx->launches = before;
+        cudaGetLastError();  // a failed capture leaves no sticky error: fall back to direct launches
+    }
+    if (!ev && me->graph_state == 1) {
+        VPP_CUDA(cudaGraphLaunch(me->graph, ctx->stream));
+        ctx->launches += me->graph_kernels;
+        return VPPGPU_OK;
+    }
     VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
-    vppgpu::FullArgs a = full_args(me, d_incl, d_slice, d_mv, d_dist, d_avg, lambda);
-    return vppgpu::full_launch(ctx, a, me->nmb, d_src16, d_ref16, me->resolve_grid, ring_slot(me));
+    return vppgpu::full_launch(ctx, a, me->nmb, me->resolve_grid, ev);
 }
 
 int status_from_ctrl(const vppgpu::MeCtrl& c)
@@ -231,7 +261,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) || (rc = dalloc(&me->d_src8, npix)) ||
         (rc = dalloc(&me->d_refp, npad)) || (rc = dalloc(&me->d_hpel, 3 * npad)) ||
         (rc = dalloc(&me->d_wave_rec, vppgpu::wave_rec_count(me->cols, me->rows))) || (rc = dalloc(&me->d_wave_choice, me->nmb)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
-        (rc = dalloc(&me->tables, (size_t)me->nmb * 64 * 64)) || (rc = dalloc(&me->tie_list, me->nmb)) || (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
+        (rc = dalloc(&me->tables, (size_t)me->nmb * 64 * 64)) || (rc = dalloc(&me->d_job, 1)) || (rc = dalloc(&me->tie_list, me->nmb)) || (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
         (rc = dalloc(&me->cache, (size_t)me->nmb * vppgpu::KCACHE)) || (rc = dalloc(&me->dict, vppgpu::NDICT)) ||
         (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
         (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||

@@ -52,10 +52,12 @@ struct TieSmem {
 };
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_full_pack(const short* __restrict__ src16, const short* __restrict__ ref16,
-                                                  int W, int H, unsigned char* __restrict__ src8,
-                                                  unsigned char* __restrict__ refp, int rstride, int* status)
+__global__ void __launch_bounds__(256) k_full_pack(const JobDesc* __restrict__ job, int W, int H,
+                                                  unsigned char* __restrict__ src8, unsigned char* __restrict__ refp,
+                                                  int rstride, int* status)
 {
+    const short* __restrict__ src16 = job->src16;
+    const short* __restrict__ ref16 = job->ref16;
     // padded reference: 4 bytes per thread; source: 4 samples per thread
     const int PW = W + 2 * PAD, PH = H + 2 * PAD;
     const long long nref = (long long)(PW / 4) * PH;  // PW is a multiple of 16
@@ -300,7 +302,7 @@ __global__ void __launch_bounds__(256, 4) k_full_refine(FullArgs a)
     subpel_refine_planes(a, n + mx, m + my, cur, lane, &minD, &qmx, &qmy);
     if (lane == 0) {
         const int qmv = pack_mv(4 * mx + qmx, 4 * my + qmy);
-        const int av = neighbour_mask(a.slice, k, a.cols, a.nmb / a.cols);
+        const int av = neighbour_mask(a.job->slice, k, a.cols, a.nmb / a.cols);
         a.spec4[k] = make_int4(qmv, minD, zero_d, (tie ? FLAG_TIE : 0) | av);
         a.spec_imv[k] = pack_mv(mx, my);
         __stcg(a.final_mv + k, qmv);
@@ -368,19 +370,27 @@ __global__ void __launch_bounds__(TIE_RUNS * 32) k_full_tietree(FullArgs a)
     }
 }
 
+__global__ void k_set_job(JobDesc* dst, JobDesc v) { *dst = v; }
+
 }  // namespace
+
+int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v)
+{
+    k_set_job<<<1, 1, 0, ctx->stream>>>(d_job, v);
+    VPP_CHECK_LAUNCH(ctx);
+    return VPPGPU_OK;
+}
 
 size_t full_search_smem() { return sizeof(TableSmem); }
 
-int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, const short* d_src16, const short* d_ref16,
-                int resolve_grid, cudaEvent_t* ev)
+int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid, cudaEvent_t* ev)
 {
     if (ev) VPP_CUDA(cudaEventRecord(ev[0], ctx->stream));
     {
         long long work = (long long)((args.W + 2 * PAD) / 4) * (args.H + 2 * PAD) + (long long)args.W * args.H / 4;
         int grid = (int)((work + 255) / 256);
         if (grid > ctx->sm_count * 16) grid = ctx->sm_count * 16;
-        k_full_pack<<<grid, 256, 0, ctx->stream>>>(d_src16, d_ref16, args.W, args.H, (unsigned char*)args.src8,
+        k_full_pack<<<grid, 256, 0, ctx->stream>>>(args.job, args.W, args.H, (unsigned char*)args.src8,
                                                    (unsigned char*)args.refp, args.rstride, &args.ctrl->status);
         VPP_CHECK_LAUNCH(ctx);
     }

@@ -297,10 +297,10 @@ __global__ void __launch_bounds__(256) k_full_relax_outcome(FullArgs a)
         int cnt = 0;
         for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmb; k += gridDim.x * blockDim.x) {
             const int fmv = __ldcg(a.final_mv + k);
-            a.out_mv[k] = fmv;
+            a.job->out_mv[k] = fmv;
             const int d = a.final_dist[k];
-            if (a.out_dist) a.out_dist[k] = d;
-            if (a.incl && a.incl[k]) {
+            if (a.job->out_dist) a.job->out_dist[k] = d;
+            if (a.job->incl && a.job->incl[k]) {
                 tot += d;
                 cnt++;
             }
@@ -843,9 +843,9 @@ __global__ void __launch_bounds__(256) k_full_wave_outputs(FullArgs a)
         }
         a.final_mv[k] = fmv;
         a.final_dist[k] = d;
-        a.out_mv[k] = fmv;
-        if (a.out_dist) a.out_dist[k] = d;
-        if (a.incl && a.incl[k]) {
+        a.job->out_mv[k] = fmv;
+        if (a.job->out_dist) a.job->out_dist[k] = d;
+        if (a.job->incl && a.job->incl[k]) {
             tot += d;
             cnt++;
         }
@@ -866,7 +866,7 @@ __global__ void k_full_average(FullArgs a)
     if (*((volatile int*)&a.ctrl->status) & ST_TIMEOUT) return;
     const long long t = a.ctrl->total;
     const int c = a.ctrl->count;
-    if (a.out_avg) *a.out_avg = c ? t / c : 0;
+    if (a.job->out_avg) *a.job->out_avg = c ? t / c : 0;
 }
 
 size_t wave_smem_bytes(int nw, int cols, int chunk)

@@ -45,6 +45,18 @@ __host__ __device__ inline size_t wave_rec_index(int cols, int r, int c)
     return ((size_t)(r >> 5) * (cols + 62) + c + 2 * (r & 31)) * 32 + (r & 31);
 }
 
+// The per-estimate pointers, read by the kernels from device memory so that a
+// captured kernel sequence (CUDA graph) serves every estimate of a handle.
+struct JobDesc {
+    const short* src16;        // input luma, W x H int16
+    const short* ref16;        // reference luma
+    const unsigned char* incl; // nullable: pDistortionIncluded
+    const int* slice;          // nullable: macroblock slice map
+    int* out_mv;               // packed short2 per macroblock
+    int* out_dist;             // nullable
+    long long* out_avg;        // nullable
+};
+
 struct FullArgs {
     int W, H, cols, nmb, motion_range, rstride;
     const unsigned char* src8;  // W x H input, unpadded
@@ -66,11 +78,7 @@ struct FullArgs {
     int* pred_used;
     int4* cache;     // KCACHE records per MB: {prediction, distortion at it, final vector, final distortion}
     int* dict;       // dominant vectors of the frame (NDICT)
-    const int* slice;          // nullable
-    const unsigned char* incl; // nullable
-    int* out_mv;               // packed short2 per macroblock
-    int* out_dist;             // nullable
-    long long* out_avg;        // nullable
+    const JobDesc* job;        // device
     MeCtrl* ctrl;
     int* changed;              // one counter per sweep
     WaveRec* wave_rec;         // wave_rec_count(cols, rows) records
@@ -91,6 +99,10 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
                unsigned char* scratch, const unsigned char* incl, int* out_mv, int* out_dist, long long* out_avg,
                MeCtrl* ctrl);
 
+// Write this estimate's pointers to the device descriptor (a one-thread
+// kernel with the descriptor as its parameter: stream-ordered, no host copy).
+int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v);
+
 size_t full_search_smem();
 // Launch the prediction-dependent tail (sweep 0, relaxation, dictionary
 // precompute, exact wavefront) of an estimate whose search has run.
@@ -99,7 +111,6 @@ int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap);
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid);
 // ev: nullptr, or 5 events recorded before the pack kernel, before the
 // table kernel, before the refine kernel, before the resolve and after it.
-int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, const short* d_src16, const short* d_ref16,
-                int resolve_grid, cudaEvent_t* ev);
+int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid, cudaEvent_t* ev);
 
 }  // namespace vppgpu

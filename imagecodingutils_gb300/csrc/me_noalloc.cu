@@ -46,6 +46,7 @@ constexpr size_t kHpelBytes = 3 * kRefBytes;               // b, h, j planes of 
 constexpr size_t kWaveRecBytes = 4736 * sizeof(vppgpu::WaveRec);
 constexpr size_t kChoiceBytes = 1600;                      // one int per macroblock
 constexpr size_t kTieListBytes = 1600;                     // one int per macroblock
+constexpr size_t kJobBytes = 64;                           // vppgpu::JobDesc
 constexpr size_t kTableBytes = (size_t)VPPGPU_NOALLOC_MAX_MBS * 64 * 64 * 4;
 constexpr size_t kOffSrc = 0;
 constexpr size_t kOffRef = kOffSrc + kSrcBytes;
@@ -59,7 +60,9 @@ constexpr size_t kOffHpel = kOffDict + kDictBytes;
 constexpr size_t kOffWaveRec = kOffHpel + kHpelBytes;
 constexpr size_t kOffChoice = kOffWaveRec + kWaveRecBytes;
 constexpr size_t kOffTieList = kOffChoice + kChoiceBytes;
-constexpr size_t kOffTables = kOffTieList + kTieListBytes;
+constexpr size_t kOffJob = kOffTieList + kTieListBytes;
+constexpr size_t kOffTables = kOffJob + kJobBytes;
+static_assert(sizeof(vppgpu::JobDesc) <= kJobBytes && kOffJob % 16 == 0, "job descriptor does not fit");
 static_assert(16 * vppgpu::KCACHE * VPPGPU_NOALLOC_MAX_MBS <= kCacheBytes && 4 * vppgpu::NDICT <= kDictBytes,
               "resolve caches do not fit");
 static_assert(sizeof(vppgpu::WaveRec) * VPPGPU_NOALLOC_MAX_MBS <= kWaveRecBytes &&
@@ -172,11 +175,7 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     a.final_mv = state;
     a.final_dist = state + nmb;
     a.pred_used = state + 2 * nmb;
-    a.slice = d_mb_slice;
-    a.incl = d_dist_included;
-    a.out_mv = (int*)d_mv_out;
-    a.out_dist = d_mb_dist_out;
-    a.out_avg = nullptr;
+    a.job = (const vppgpu::JobDesc*)(base + kOffJob);
     a.ctrl = (vppgpu::MeCtrl*)(base + kOffCtrl);
     a.changed = (int*)(base + kOffChanged);
     a.lambda = 1.05;
@@ -188,7 +187,10 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     VPP_CUDA(cudaMemsetAsync(a.changed, 0, sizeof(int) * (size_t)a.sweep_limit, ctx.stream));
     int grid = (nmb + 7) / 8;
     if (grid > s->resolve_cap) grid = s->resolve_cap;
-    rc = vppgpu::full_launch(&ctx, a, nmb, d_src, d_ref, grid, nullptr);
+    rc = vppgpu::set_job(&ctx, (vppgpu::JobDesc*)(base + kOffJob),
+                         vppgpu::JobDesc{d_src, d_ref, d_dist_included, d_mb_slice, (int*)d_mv_out, d_mb_dist_out, nullptr});
+    if (rc) return rc;
+    rc = vppgpu::full_launch(&ctx, a, nmb, grid, nullptr);
     if (rc) return rc;
 
     vppgpu::MeCtrl h = {};
