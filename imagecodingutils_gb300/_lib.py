@@ -55,6 +55,7 @@ SIGNATURES = {
     "vppgpu_me_timing": (_I, [_P, C.POINTER(_I), C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_double)]),
     "vppgpu_me_timing_stages": (_I, [_P, C.POINTER(_I), _P]),
+    "vppgpu_me_residual_device": (_I, [_P, _P, _P]),
     "vppgpu_me_batch_create": (_I, [_P, _I, _I, C.POINTER(_P)]),
     "vppgpu_me_batch_destroy": (_I, [_P]),
     "vppgpu_me_batch_run": (_I, [_P, _P, _I, _P, _P]),

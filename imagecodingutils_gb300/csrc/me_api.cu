@@ -429,6 +429,16 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 
 }  // extern "C"
 
+extern "C" int vppgpu_me_residual_device(vppgpu_me* me, const short* d_mv, short* d_residual)
+{
+    if (!me || !d_mv || !d_residual) return VPPGPU_ERR_INVALID_ARG;
+    if (me->kind != VPPGPU_ME_FULL) return VPPGPU_ERR_UNSUPPORTED;
+    if (!aligned(d_mv, 4) || !aligned(d_residual, 16)) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    return vppgpu::full_residual_launch(me->ctx, full_args(me, 1.05), (const int*)d_mv, d_residual);
+}
+
 extern "C" int vppgpu_me_last_stats(vppgpu_me* me, int* stats8)
 {
     if (!me || !stats8) return VPPGPU_ERR_INVALID_ARG;

@@ -73,17 +73,19 @@ __device__ __forceinline__ PredGeom pred_geom(int n, int m, int W, int H, int px
 // (OverlayMem2Dv2::QuarterRead) as one sample of the full-pel, b, h or j
 // plane, or the rounded mean of two.  Lane l covers row l/2, columns
 // 8*(l&1) .. +7; squared differences with dp4a on per-byte |differences|.
-__device__ __forceinline__ int plane_pred_distortion(const FullArgs& a, int n, int m, const PredGeom& g, int lane)
+// This lane's 8 quarter-pel samples (row lane/2, columns 8*(lane&1)..+7) of
+// the 16x16 block at full-pel origin (ox, oy) and fraction (fx, fy) in 0..3.
+__device__ __forceinline__ uint2 qpel_block8(const FullArgs& a, int ox, int oy, int fx, int fy, int lane)
 {
     const int r = lane >> 1, c0 = (lane & 1) * 8, st = a.rstride;
-    const size_t o = (size_t)(g.oy + r + PAD) * st + (size_t)(g.ox + c0 + PAD);
+    const size_t o = (size_t)(oy + r + PAD) * st + (size_t)(ox + c0 + PAD);
     const unsigned char* G = a.refp;
     const unsigned char* Bp = a.hpel;
     const unsigned char* Hp = a.hpel + a.plane_size;
     const unsigned char* Jp = a.hpel + 2 * a.plane_size;
     const unsigned char *p1 = G + o, *p2 = G + o;
     bool two = true;
-    switch (g.fx | (g.fy << 2)) {
+    switch (fx | (fy << 2)) {
     case 0: two = false; break;                          // G
     case 2: p1 = Bp + o; two = false; break;             // b
     case 8: p1 = Hp + o; two = false; break;             // h
@@ -107,7 +109,12 @@ __device__ __forceinline__ int plane_pred_distortion(const FullArgs& a, int n, i
         v.x = __vavgu4(v.x, w.x);  // (p + q + 1) >> 1 per byte
         v.y = __vavgu4(v.y, w.y);
     }
-    return warp_sum(ssd8(load_cur8(a, n, m, lane), v));
+    return v;
+}
+
+__device__ __forceinline__ int plane_pred_distortion(const FullArgs& a, int n, int m, const PredGeom& g, int lane)
+{
+    return warp_sum(ssd8(load_cur8(a, n, m, lane), qpel_block8(a, g.ox, g.oy, g.fx, g.fy, lane)));
 }
 
 // Exact-tie macroblocks: the integer scan depends on the rounded prediction.
@@ -869,6 +876,32 @@ __global__ void k_full_average(FullArgs a)
     if (a.job->out_avg) *a.job->out_avg = c ? t / c : 0;
 }
 
+// Motion-compensated luma residual (MotionCompensatorH264ImplStd::Compensate,
+// MotionCompensatorH264ImplStd.cpp:413-431: QuarterRead of the reference at
+// the vector, a copy for full-pel vectors; then OverlayMem2Dv2::Sub16x16):
+// one warp per macroblock, samples from the estimate's planes.
+__global__ void __launch_bounds__(256) k_full_residual(FullArgs a, const int* __restrict__ mv, short* __restrict__ res)
+{
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (k >= a.nmb) return;
+    const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
+    const int v = mv[k], mvx = mv_x(v), mvy = mv_y(v);
+    const int qx = mvx % 4, qy = mvy % 4;  // C remainders, folded as QuarterRead does
+    const int fx = qx < 0 ? qx + 4 : qx, fy = qy < 0 ? qy + 4 : qy;
+    const int ox = n + mvx / 4 + (qx < 0 ? -1 : 0), oy = m + mvy / 4 + (qy < 0 ? -1 : 0);
+    const uint2 p = qpel_block8(a, ox, oy, fx, fy, lane);
+    const uint2 c = load_cur8(a, n, m, lane);
+    short* dst = res + (size_t)(m + (lane >> 1)) * a.W + n + 8 * (lane & 1);
+    short vals[8];
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+        vals[b] = (short)((int)((c.x >> (8 * b)) & 0xff) - (int)((p.x >> (8 * b)) & 0xff));
+        vals[4 + b] = (short)((int)((c.y >> (8 * b)) & 0xff) - (int)((p.y >> (8 * b)) & 0xff));
+    }
+    *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(vals);
+}
+
 size_t wave_smem_bytes(int nw, int cols, int chunk)
 {
     return (size_t)kWaveStepBytes * nw * 2 * chunk + sizeof(unsigned long long) * nw * 2 + sizeof(int) * (size_t)nw * cols;
@@ -928,6 +961,13 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid)
         k_full_average<<<1, 1, 0, ctx->stream>>>(args);
         VPP_CHECK_LAUNCH(ctx);
     }
+    return VPPGPU_OK;
+}
+
+int full_residual_launch(vppgpu_ctx* ctx, const FullArgs& args, const int* d_mv, short* d_res)
+{
+    k_full_residual<<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(args, d_mv, d_res);
+    VPP_CHECK_LAUNCH(ctx);
     return VPPGPU_OK;
 }
 

@@ -103,6 +103,9 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
 // kernel with the descriptor as its parameter: stream-ordered, no host copy).
 int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v);
 
+// Motion-compensated luma residual of the last estimate's planes at vectors d_mv.
+int full_residual_launch(vppgpu_ctx* ctx, const FullArgs& args, const int* d_mv, short* d_res);
+
 size_t full_search_smem();
 // Launch the prediction-dependent tail (sweep 0, relaxation, dictionary
 // precompute, exact wavefront) of an estimate whose search has run.

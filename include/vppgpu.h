@@ -134,6 +134,15 @@ int vppgpu_me_timing(vppgpu_me* me, int* n, double* pack_ms, double* search_ms, 
  * sub-pel + tie trees, prediction-dependent resolve}. */
 int vppgpu_me_timing_stages(vppgpu_me* me, int* n, double* stage_ms4);
 
+/* Motion-compensated luma residual of the last estimate of a Full estimator:
+ * for every macroblock, input minus the reference read at its vector
+ * (MotionCompensatorH264ImplStd::Compensate luma, MotionCompensatorH264ImplStd.cpp:413-431:
+ * QuarterRead at the quarter-pel vector, a copy for a full-pel one; then
+ * OverlayMem2Dv2::Sub16x16), as int16 W x H (16-byte aligned).  d_mv: 2 shorts
+ * per macroblock, e.g. the estimate's own output.  Enqueued on the context
+ * stream after the estimate. */
+int vppgpu_me_residual_device(vppgpu_me* me, const short* d_mv, short* d_residual);
+
 /* Batched estimation, no vpp counterpart (the codecs estimate one frame at a
  * time).  A batch runs many independent frame pairs of any mix of sizes on
  * `streams` streams of its own, so that the latency-bound stages of one
