@@ -243,6 +243,66 @@ class MotionEstimatorBatch:
             pass
 
 
+class Server:
+    """Continuous-batching request loop (vppgpu_server_*; no vpp counterpart).
+    submit(frames[nframes, H, W] int16, motion_range, qp) -> ticket; the
+    result arrays (vectors, digests) are filled when poll()/wait_idle() report
+    the ticket done."""
+
+    def __init__(self, slots: int = 4, hbm_budget: int = 0, ctx: Context | None = None):
+        self._ctx = ctx or get_context()
+        h = C.c_void_p()
+        check(load().vppgpu_server_create(self._ctx.handle, int(slots), int(hbm_budget), C.byref(h)),
+              "vppgpu_server_create")
+        self.handle = h
+        self._live = {}
+
+    def submit(self, frames, motion_range: int = 128, qp: int = 28, want_vectors: bool = True):
+        f = np.ascontiguousarray(frames, np.int16)
+        nfr, h, w = f.shape
+        nmb = (w // 16) * (h // 16)
+        mv = np.zeros((max(nfr - 1, 0), nmb, 2), np.int16) if want_vectors else None
+        dig = np.zeros(max(nfr - 1, 0), np.uint64)
+        req = _lib.SeqRequest(w, h, nfr, int(motion_range), int(qp), f.ctypes.data,
+                              mv.ctypes.data if mv is not None else None, dig.ctypes.data)
+        t = C.c_ulonglong()
+        check(load().vppgpu_server_submit(self.handle, C.byref(req), C.byref(t)), "vppgpu_server_submit")
+        self._live[t.value] = (f, mv, dig)  # keep the buffers alive until done
+        return t.value, mv, dig
+
+    def poll(self, max_n: int = 1024):
+        tk = (C.c_ulonglong * max_n)()
+        st = (C.c_int * max_n)()
+        lat = (C.c_double * max_n)()
+        n = C.c_int()
+        check(load().vppgpu_server_poll(self.handle, max_n, tk, st, lat, C.byref(n)), "vppgpu_server_poll")
+        out = []
+        for i in range(n.value):
+            self._live.pop(tk[i], None)
+            out.append((tk[i], st[i], lat[i]))
+        return out
+
+    def wait_idle(self):
+        check(load().vppgpu_server_wait_idle(self.handle), "vppgpu_server_wait_idle")
+
+    def stats(self):
+        b = C.c_ulonglong()
+        r = C.c_int()
+        check(load().vppgpu_server_stats(self.handle, C.byref(b), C.byref(r)), "vppgpu_server_stats")
+        return {"reserved_peak_bytes": b.value, "running_peak": r.value}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().vppgpu_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class _ForwardBase:
     LAYOUT = _lib.LAYOUT_BLOCKS
     UNIT = 16

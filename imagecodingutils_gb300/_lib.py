@@ -56,6 +56,12 @@ SIGNATURES = {
                               C.POINTER(C.c_double)]),
     "vppgpu_me_timing_stages": (_I, [_P, C.POINTER(_I), _P]),
     "vppgpu_me_residual_device": (_I, [_P, _P, _P]),
+    "vppgpu_server_create": (_I, [_P, _I, C.c_ulonglong, C.POINTER(_P)]),
+    "vppgpu_server_submit": (_I, [_P, _P, C.POINTER(C.c_ulonglong)]),
+    "vppgpu_server_poll": (_I, [_P, _I, _P, _P, _P, C.POINTER(_I)]),
+    "vppgpu_server_wait_idle": (_I, [_P]),
+    "vppgpu_server_stats": (_I, [_P, C.POINTER(C.c_ulonglong), C.POINTER(_I)]),
+    "vppgpu_server_destroy": (_I, [_P]),
     "vppgpu_me_batch_create": (_I, [_P, _I, _I, C.POINTER(_P)]),
     "vppgpu_me_batch_destroy": (_I, [_P]),
     "vppgpu_me_batch_run": (_I, [_P, _P, _I, _P, _P]),
@@ -117,3 +123,9 @@ class MeJob(C.Structure):
     _fields_ = [("src", C.c_void_p), ("ref", C.c_void_p), ("width", C.c_int), ("height", C.c_int),
                 ("motion_range", C.c_int), ("dist_included", C.c_void_p), ("mv_out", C.c_void_p),
                 ("mb_dist_out", C.c_void_p)]
+
+
+class SeqRequest(C.Structure):
+    """vppgpu_seq_request (include/vppgpu.h)."""
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("nframes", C.c_int), ("motion_range", C.c_int),
+                ("qp", C.c_int), ("frames", C.c_void_p), ("mv_out", C.c_void_p), ("digest_out", C.c_void_p)]

@@ -201,17 +201,25 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
     return vppgpu::full_launch(ctx, a, me->nmb, me->resolve_grid, ev);
 }
 
-int status_from_ctrl(const vppgpu::MeCtrl& c)
-{
-    if (c.status & vppgpu::ST_PIXEL_RANGE) return VPPGPU_ERR_PIXEL_RANGE;
-    if (c.status & vppgpu::ST_TIMEOUT) return VPPGPU_ERR_TIMEOUT;
-    if (c.status & vppgpu::ST_OUT_OF_BOUNDS) return VPPGPU_ERR_UNSUPPORTED;
-    return VPPGPU_OK;
-}
+int status_from_ctrl(const vppgpu::MeCtrl& c) { return vppgpu::status_from_bits(c.status); }
 
 bool aligned(const void* p, size_t a) { return ((uintptr_t)p & (a - 1)) == 0; }
 
 }  // namespace
+
+namespace vppgpu {
+
+int status_from_bits(int bits)
+{
+    if (bits & ST_PIXEL_RANGE) return VPPGPU_ERR_PIXEL_RANGE;
+    if (bits & ST_TIMEOUT) return VPPGPU_ERR_TIMEOUT;
+    if (bits & ST_OUT_OF_BOUNDS) return VPPGPU_ERR_UNSUPPORTED;
+    return VPPGPU_OK;
+}
+
+const int* me_status_word(vppgpu_me* me) { return &me->ctrl->status; }
+
+}  // namespace vppgpu
 
 extern "C" {
 

@@ -890,9 +890,16 @@ __global__ void __launch_bounds__(256) k_full_residual(FullArgs a, const int* __
     const int qx = mvx % 4, qy = mvy % 4;  // C remainders, folded as QuarterRead does
     const int fx = qx < 0 ? qx + 4 : qx, fy = qy < 0 ? qy + 4 : qy;
     const int ox = n + mvx / 4 + (qx < 0 ? -1 : 0), oy = m + mvy / 4 + (qy < 0 ? -1 : 0);
+    short* dst = res + (size_t)(m + (lane >> 1)) * a.W + n + 8 * (lane & 1);
+    // a prediction more than 32 samples outside the picture would leave the
+    // padded planes: flagged, residual zero
+    if (ox < -32 || oy < -32 || ox > a.W + 16 || oy > a.H + 16) {
+        *reinterpret_cast<uint4*>(dst) = make_uint4(0, 0, 0, 0);
+        if (lane == 0) atomicOr(&a.ctrl->status, ST_OUT_OF_BOUNDS);
+        return;
+    }
     const uint2 p = qpel_block8(a, ox, oy, fx, fy, lane);
     const uint2 c = load_cur8(a, n, m, lane);
-    short* dst = res + (size_t)(m + (lane >> 1)) * a.W + n + 8 * (lane & 1);
     short vals[8];
 #pragma unroll
     for (int b = 0; b < 4; b++) {

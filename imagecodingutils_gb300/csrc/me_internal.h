@@ -99,6 +99,11 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
                unsigned char* scratch, const unsigned char* incl, int* out_mv, int* out_dist, long long* out_avg,
                MeCtrl* ctrl);
 
+// Device address of the status word (ST_* bits) of a handle's current
+// estimate, and the C ABI status those bits stand for.
+const int* me_status_word(vppgpu_me* me);
+int status_from_bits(int bits);
+
 // Write this estimate's pointers to the device descriptor (a one-thread
 // kernel with the descriptor as its parameter: stream-ordered, no host copy).
 int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v);

@@ -140,7 +140,9 @@ int vppgpu_me_timing_stages(vppgpu_me* me, int* n, double* stage_ms4);
  * QuarterRead at the quarter-pel vector, a copy for a full-pel one; then
  * OverlayMem2Dv2::Sub16x16), as int16 W x H (16-byte aligned).  d_mv: 2 shorts
  * per macroblock, e.g. the estimate's own output.  Enqueued on the context
- * stream after the estimate. */
+ * stream after the estimate.  A vector whose prediction lies more than 32
+ * samples outside the picture (never one the estimator returns) gets a zero
+ * residual and makes vppgpu_me_last_status return VPPGPU_ERR_UNSUPPORTED. */
 int vppgpu_me_residual_device(vppgpu_me* me, const short* d_mv, short* d_residual);
 
 /* Batched estimation, no vpp counterpart (the codecs estimate one frame at a
@@ -166,6 +168,36 @@ int vppgpu_me_batch_create(vppgpu_ctx* ctx, int kind, int streams, vppgpu_me_bat
 int vppgpu_me_batch_destroy(vppgpu_me_batch* b);
 int vppgpu_me_batch_run(vppgpu_me_batch* b, const vppgpu_me_job* jobs, int n, int* status_out, long* avg_out);
 int vppgpu_me_batch_launch_count(vppgpu_me_batch* b, unsigned long long* count);
+
+/* Serving, no vpp counterpart: a continuous-batching request loop for
+ * sequence jobs.  A request is nframes host luma planes (W x H, back to back;
+ * kept valid until the request completes); for every frame pair the server
+ * estimates the Full-search vectors (motion_range), forms the
+ * motion-compensated luma residual and runs the 4x4 transform + quantisation
+ * round trip on it (inter rounding, qp), returning the vectors
+ * ((nframes-1) x N_MB x 2 shorts, nullable) and per pair a digest
+ * sum(levels + 3*reconstruction) (nullable).  Frames are uploaded once and
+ * stay on the device as the next pair's reference.  `slots` worker threads
+ * with their own streams take the oldest queued request whose device buffers
+ * fit under `hbm_budget` bytes (0: half of the free memory), so requests
+ * arriving while others run are admitted as slots and memory free up and
+ * overlap on the device.  Results are identical to running each request
+ * alone.  poll() returns completed tickets with status and submit-to-done
+ * latency. */
+typedef struct vppgpu_server vppgpu_server;
+typedef struct {
+    int width, height, nframes, motion_range, qp;
+    const short* frames;               /* host */
+    short* mv_out;                     /* host, nullable */
+    unsigned long long* digest_out;    /* host, nframes-1 values, nullable */
+} vppgpu_seq_request;
+int vppgpu_server_create(vppgpu_ctx* ctx, int slots, unsigned long long hbm_budget, vppgpu_server** out);
+int vppgpu_server_submit(vppgpu_server* s, const vppgpu_seq_request* r, unsigned long long* ticket);
+int vppgpu_server_poll(vppgpu_server* s, int max, unsigned long long* tickets, int* status, double* latency_ms,
+                       int* n);
+int vppgpu_server_wait_idle(vppgpu_server* s);
+int vppgpu_server_stats(vppgpu_server* s, unsigned long long* reserved_peak, int* running_peak);
+int vppgpu_server_destroy(vppgpu_server* s);
 
 /* Measured dp4a issue rate of the whole device (instructions per second),
  * the integer-ALU roofline of the motion search.  No vpp counterpart. */
