@@ -154,18 +154,24 @@ BATCH_SIZES = [(176, 144), (352, 288), (1280, 720), (1920, 1080), (3840, 2160)]
 BATCH_SEQS, BATCH_FRAMES, BATCH_BASES = 64, 8, 2
 
 
-def batched_workload(torch, dev):
-    """The mixed-resolution batch: 64 sequences, uniform over QCIF, CIF, 720p,
-    1080p and 4K, 8 frames each (7 frame pairs per sequence).  Generating 4K
-    content on the host costs ~15 s per sequence, so each size has 2 seeded
-    base sequences and sequence i uses base (i // 5) % 2 of size i % 5; every
-    job is still estimated on its own."""
+def sequence_bases(torch, dev):
+    """Seeded base sequences of the resolution mix: 2 per size, 8 frames each,
+    on the device.  Generating 4K content on the host costs ~15 s per
+    sequence, so the batched and the serving workloads draw their sequences
+    from these."""
     from imagecodingutils_gb300 import synth
     bases = {}
     for si, (w, h) in enumerate(BATCH_SIZES):
         for b in range(BATCH_BASES):
             fr = synth.pan_sequence(5000 + 10 * si + b, w, h, BATCH_FRAMES)
             bases[(si, b)] = torch.from_numpy(np.stack(fr)).to(dev)
+    return bases
+
+
+def batched_workload(bases):
+    """The mixed-resolution batch: 64 sequences, uniform over QCIF, CIF, 720p,
+    1080p and 4K, 8 frames each (7 frame pairs per sequence); sequence i uses
+    base (i // 5) % 2 of size i % 5, every job is still estimated on its own."""
     jobs = []
     for i in range(BATCH_SEQS):
         si, b = i % len(BATCH_SIZES), (i // len(BATCH_SIZES)) % BATCH_BASES
@@ -175,8 +181,8 @@ def batched_workload(torch, dev):
     return bases, jobs
 
 
-def run_batched(args, torch, vpp, _lib, L, ctx, stream, dev):
-    bases, spec = batched_workload(torch, dev)
+def run_batched(args, torch, vpp, _lib, L, ctx, stream, dev, bases):
+    bases, spec = batched_workload(bases)
     outs = [torch.empty(((w // 16) * (h // 16), 2), dtype=torch.int16, device=dev) for (_, _, _, w, h) in spec]
     outs_plain = [torch.empty_like(o) for o in outs]
     mbs = sum((w // 16) * (h // 16) for (_, _, _, w, h) in spec)
@@ -231,6 +237,81 @@ def run_batched(args, torch, vpp, _lib, L, ctx, stream, dev):
         "jobs": len(spec), "macroblocks": mbs, "streams": args.batch_streams, "identical_to_plain": bool(same),
         "workload": "64 sequences x 7 frame pairs, uniform over 176x144, 352x288, 1280x720, 1920x1080, 3840x2160; "
                     "Full ME motionRange 128; device-resident",
+    }
+
+
+SERVE_QP = 28
+SERVE_SPAN = 24  # frames of the ping-pong host sequence a request is cut from
+
+
+def serving_workload(args, torch, bases):
+    """Requests of the serving form: Poisson arrivals (mean args.serve_rate
+    per second), each a 4..16-frame sequence of a size drawn uniformly from
+    the resolution mix, cut at a seeded offset from a pinned host sequence
+    that plays its 8-frame base forwards and backwards (0..7, 6..1, 0..7, ...)."""
+    rng = np.random.default_rng(2000)
+    hosts = {}
+    for key, fr in bases.items():
+        idx = [t % 14 if t % 14 < 8 else 14 - t % 14 for t in range(SERVE_SPAN)]
+        hosts[key] = fr[idx].cpu().pin_memory().numpy()
+    reqs, t = [], 0.0
+    for _ in range(args.serve_jobs):
+        t += rng.exponential(1.0 / args.serve_rate)
+        si = int(rng.integers(len(BATCH_SIZES)))
+        b = int(rng.integers(BATCH_BASES))
+        n = int(rng.integers(4, 17))
+        start = int(rng.integers(SERVE_SPAN - n + 1))
+        reqs.append((t, si, b, start, n))
+    return hosts, reqs
+
+
+def serve_pass(vpp, ctx, hosts, reqs, slots, budget):
+    """Submit every request at its arrival time (busy-wait on the host clock)
+    to a server with `slots` worker slots; returns per-request latencies,
+    outputs and the wall time from the first arrival to the last completion."""
+    srv = vpp.Server(slots=slots, hbm_budget=budget, ctx=ctx)
+    for (w, h) in BATCH_SIZES:
+        srv.prepare(w, h, MOTION_RANGE)
+    outs = []
+    t0 = time.perf_counter()
+    for (ta, si, b, start, n) in reqs:
+        while time.perf_counter() - t0 < ta:
+            pass
+        outs.append(srv.submit(hosts[(si, b)][start:start + n], MOTION_RANGE, SERVE_QP))
+    srv.wait_idle()
+    wall = time.perf_counter() - t0
+    done = srv.poll(max_n=len(reqs) + 16)
+    stats = srv.stats()
+    srv.close()
+    assert len(done) == len(reqs) and all(st == 0 for _, st, _ in done), [st for _, st, _ in done if st]
+    lat = {tk: ms for tk, _, ms in done}
+    return np.array([lat[o[0]] for o in outs]), [(o[1], o[2]) for o in outs], wall, stats
+
+
+def run_serving(args, vpp, torch, ctx, bases):
+    hosts, reqs = serving_workload(args, torch, bases)
+    mbs = sum((n - 1) * (BATCH_SIZES[si][0] // 16) * (BATCH_SIZES[si][1] // 16) for (_, si, _, _, n) in reqs)
+    res = {}
+    for name, slots in (("plain", 1), ("served", args.serve_slots)):
+        lat, outs, wall, stats = serve_pass(vpp, ctx, hosts, reqs, slots, args.serve_budget)
+        res[name] = {"value": mbs / wall, "unit": UNIT, "wall_s": wall, "slots": slots,
+                     "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                                    "p99.9": float(np.percentile(lat, 99.9)), "max": float(lat.max())},
+                     "running_peak": stats["running_peak"], "reserved_peak_bytes": stats["reserved_peak_bytes"],
+                     "_outs": outs}
+    same = all(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+               for a, b in zip(res["plain"].pop("_outs"), res["served"].pop("_outs")))
+    span = reqs[-1][0]
+    return {
+        **res["served"], "plain": res["plain"], "ratio_vs_plain": res["plain"]["wall_s"] / res["served"]["wall_s"],
+        "requests": len(reqs), "macroblocks": mbs, "frame_pairs": sum(n - 1 for (*_, n) in reqs),
+        "offered_rate_per_s": args.serve_rate, "arrival_span_s": span, "identical_to_plain": bool(same),
+        "workload": f"{len(reqs)} requests, Poisson arrivals mean {args.serve_rate:g}/s, 4..16-frame sequences "
+                    "uniform over 176x144, 352x288, 1280x720, 1920x1080, 3840x2160; per frame pair Full ME "
+                    f"motionRange {MOTION_RANGE}, motion-compensated residual, 4x4 transform + quant round trip "
+                    f"QP {SERVE_QP}; frames from pinned host memory, uploaded once and kept as the next reference; "
+                    "plain = one slot (requests one after another)",
+        "latency": "submit to completion of the request's last device->host copy",
     }
 
 
@@ -404,6 +485,11 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-streams", type=int, default=8)
     ap.add_argument("--batch-reps", type=int, default=3)
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-jobs", type=int, default=1000)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-budget", type=int, default=0, help="bytes of request buffers (0: half the free HBM)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -534,7 +620,10 @@ def main():
             v_cpu, dt_cpu = cpu_baseline(frames, nth, min(args.cpu_frames, NFRAMES - 1))
             cpu = {"value": v_cpu, "unit": UNIT, "cores": nth, "kind": "port",
                    "sample": f"{min(args.cpu_frames, NFRAMES - 1)} 1080p frame pairs, {nth} threads, {dt_cpu:.1f} s"}
-        batched = None if args.no_batch else run_batched(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}")
+        bases = None if args.no_batch and args.no_serve else sequence_bases(torch, f"cuda:{local}")
+        batched = None if args.no_batch else run_batched(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}",
+                                                         bases)
+        serving = None if args.no_serve else run_serving(args, vpp, torch, ctx, bases)
         mrc = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu)
         pk, pk_kind = peaks()
         hbm_rows = run_hbm_paths(torch, _lib, L, ctx, stream, f"cuda:{local}", pk)
@@ -559,6 +648,7 @@ def main():
             "resolve_sweeps_last_frame": sweeps.value,
             "hbm_peak_gbs": pk.get("hbm_gbs"), "peaks_source": pk_kind,
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
+            "serving": serving,
             "multires_cross": mrc, **hbm_rows,
             "clocks": clk.summary(),
         }

@@ -257,6 +257,10 @@ class Server:
         self.handle = h
         self._live = {}
 
+    def prepare(self, width: int, height: int, motion_range: int = 128):
+        check(load().vppgpu_server_prepare(self.handle, int(width), int(height), int(motion_range)),
+              "vppgpu_server_prepare")
+
     def submit(self, frames, motion_range: int = 128, qp: int = 28, want_vectors: bool = True):
         f = np.ascontiguousarray(frames, np.int16)
         nfr, h, w = f.shape

@@ -57,6 +57,7 @@ SIGNATURES = {
     "vppgpu_me_timing_stages": (_I, [_P, C.POINTER(_I), _P]),
     "vppgpu_me_residual_device": (_I, [_P, _P, _P]),
     "vppgpu_server_create": (_I, [_P, _I, C.c_ulonglong, C.POINTER(_P)]),
+    "vppgpu_server_prepare": (_I, [_P, _I, _I, _I]),
     "vppgpu_server_submit": (_I, [_P, _P, C.POINTER(C.c_ulonglong)]),
     "vppgpu_server_poll": (_I, [_P, _I, _P, _P, _P, C.POINTER(_I)]),
     "vppgpu_server_wait_idle": (_I, [_P]),

@@ -20,6 +20,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <thread>
@@ -85,6 +86,7 @@ struct vppgpu_server {
     struct Slot {
         vppgpu_ctx* ctx = nullptr;
         int* h_status = nullptr;  // pinned
+        std::unique_ptr<std::mutex> pool_mu{new std::mutex};  // the worker vs vppgpu_server_prepare
         struct Entry {
             int W, H, range;
             vppgpu_me* me;
@@ -98,6 +100,7 @@ namespace {
 
 int slot_estimator(vppgpu_server::Slot& sl, int W, int H, int range, vppgpu_me** out)
 {
+    std::lock_guard<std::mutex> lk(*sl.pool_mu);
     for (auto& e : sl.pool)
         if (e.W == W && e.H == H && e.range == range) {
             *out = e.me;
@@ -217,6 +220,14 @@ int vppgpu_server_create(vppgpu_ctx* ctx, int slots, unsigned long long hbm_budg
         VPP_CUDA(cudaMemGetInfo(&fr, &tot));
         hbm_budget = fr / 2;
     }
+    {
+        // keep freed request buffers in the stream-ordered pool up to the
+        // budget instead of returning them at every synchronisation
+        cudaMemPool_t pool;
+        VPP_CUDA(cudaDeviceGetDefaultMemPool(&pool, ctx->device));
+        uint64_t keep = hbm_budget;
+        VPP_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    }
     vppgpu_server* s = new (std::nothrow) vppgpu_server();
     if (!s) return VPPGPU_ERR_OUT_OF_MEMORY;
     s->parent = ctx;
@@ -240,6 +251,18 @@ int vppgpu_server_create(vppgpu_ctx* ctx, int slots, unsigned long long hbm_budg
     }
     for (int i = 0; i < slots; i++) s->workers.emplace_back(worker, s, i);
     *out = s;
+    return VPPGPU_OK;
+}
+
+int vppgpu_server_prepare(vppgpu_server* s, int width, int height, int motion_range)
+{
+    if (!s || width < 16 || height < 16 || (width % 16) || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(s->parent);
+    if (rc) return rc;
+    for (auto& sl : s->slots) {
+        vppgpu_me* me = nullptr;
+        if ((rc = slot_estimator(sl, width, height, motion_range, &me))) return rc;
+    }
     return VPPGPU_OK;
 }
 

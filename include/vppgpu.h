@@ -192,6 +192,9 @@ typedef struct {
     unsigned long long* digest_out;    /* host, nframes-1 values, nullable */
 } vppgpu_seq_request;
 int vppgpu_server_create(vppgpu_ctx* ctx, int slots, unsigned long long hbm_budget, vppgpu_server** out);
+/* Create every slot's estimator for one frame geometry now (otherwise the
+ * first request of that geometry on a slot creates it). */
+int vppgpu_server_prepare(vppgpu_server* s, int width, int height, int motion_range);
 int vppgpu_server_submit(vppgpu_server* s, const vppgpu_seq_request* r, unsigned long long* ticket);
 int vppgpu_server_poll(vppgpu_server* s, int max, unsigned long long* tickets, int* status, double* latency_ms,
                        int* n);
