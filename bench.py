@@ -136,18 +136,22 @@ def profile_traffic():
     return None
 
 
-def cpu_baseline(frames, nthreads: int, nframes: int):
+def cpu_baseline(frames, nthreads: int, nframes: int, seconds: float):
     """The oracle restatement of the reference on host threads, one estimator
-    per thread over independent frame pairs."""
+    per thread over independent frame pairs: passes over `nframes` pairs of
+    the rotation until `seconds` of wall time have been spent."""
     from oracle.oracle import Oracle
     orc = Oracle()
     srcs = [frames[i + 1] for i in range(nframes)]
     refs = [frames[i] for i in range(nframes)]
     orc.bench_me_full(srcs[:1], refs[:1], MOTION_RANGE, 1)  # warm caches
-    t0 = time.perf_counter()
-    orc.bench_me_full(srcs, refs, MOTION_RANGE, nthreads)
-    dt = time.perf_counter() - t0
-    return nframes * NMB / dt, dt
+    done, t0 = 0, time.perf_counter()
+    while True:
+        orc.bench_me_full(srcs, refs, MOTION_RANGE, nthreads)
+        done += nframes
+        dt = time.perf_counter() - t0
+        if dt >= seconds:
+            return done * NMB / dt, dt, done
 
 
 BATCH_SIZES = [(176, 144), (352, 288), (1280, 720), (1920, 1080), (3840, 2160)]
@@ -355,14 +359,16 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
         mv_o, _, _ = orc.me_multires_cross(frames[1], frames[0], MOTION_RANGE, mode=mode.value)
         out["parity_first_frame"] = bool(np.array_equal(d_mv.cpu().numpy(), mv_o))
         nth = os.cpu_count() or 1
-        npairs = min(4 * nth, NFRAMES - 1)
-        t0 = time.perf_counter()
+        npairs, t0 = 0, time.perf_counter()
         with ThreadPoolExecutor(nth) as ex:  # ctypes calls release the GIL: one estimate per thread
-            list(ex.map(lambda i: orc.me_multires_cross(frames[i + 1], frames[i], MOTION_RANGE, mode=mode.value),
-                        range(npairs)))
+            while time.perf_counter() - t0 < args.cpu_seconds:
+                list(ex.map(lambda i: orc.me_multires_cross(frames[i + 1], frames[i], MOTION_RANGE,
+                                                            mode=mode.value), range(NFRAMES - 1)))
+                npairs += NFRAMES - 1
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": npairs * NMB / dt, "unit": UNIT, "cores": nth, "kind": "port",
-                               "sample": f"{npairs} 1080p frame pairs, {nth} threads, {dt:.1f} s"}
+                               "sample": f"{npairs} 1080p frame pairs (passes over the 32-pair rotation), "
+                                         f"{nth} threads, {dt:.1f} s"}
     L.vppgpu_me_destroy(h)
     return out
 
@@ -480,7 +486,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-frames", type=int, default=16)
+    ap.add_argument("--cpu-frames", type=int, default=32)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="wall time of each CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-streams", type=int, default=8)
@@ -617,9 +624,9 @@ def main():
         cpu = None
         if not args.no_cpu:
             nth = os.cpu_count() or 1
-            v_cpu, dt_cpu = cpu_baseline(frames, nth, min(args.cpu_frames, NFRAMES - 1))
+            v_cpu, dt_cpu, n_cpu = cpu_baseline(frames, nth, min(args.cpu_frames, NFRAMES - 1), args.cpu_seconds)
             cpu = {"value": v_cpu, "unit": UNIT, "cores": nth, "kind": "port",
-                   "sample": f"{min(args.cpu_frames, NFRAMES - 1)} 1080p frame pairs, {nth} threads, {dt_cpu:.1f} s"}
+                   "sample": f"{n_cpu} 1080p frame pairs (passes over the rotation), {nth} threads, {dt_cpu:.1f} s"}
         bases = None if args.no_batch and args.no_serve else sequence_bases(torch, f"cuda:{local}")
         batched = None if args.no_batch else run_batched(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}",
                                                          bases)
