@@ -193,6 +193,16 @@ class MotionEstimatorH264ImplMultiresCross(_MotionEstimatorBase):
         return self._mode
 
 
+class MotionEstimatorH264ImplMultiresCrossVer2(MotionEstimatorH264ImplMultiresCross):
+    """GPU MotionEstimatorH264ImplMultiresCrossVer2
+    (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp): the
+    MultiresCross search with ties towards the median prediction, the
+    pred-vector check and GetBestVector (lambda 0.9); Estimate(long*) only
+    (its lambda overload is not built)."""
+
+    KIND = _lib.ME_MULTIRES_CROSS_V2
+
+
 # ---------------------------------------------------------------------------
 # 4x4 transforms
 # ---------------------------------------------------------------------------

@@ -42,6 +42,7 @@ struct vppgpu_me {
     int* changed;
     int sweep_limit;
     int resolve_grid;
+    int relax_sweeps;  // MultiresCrossVer2: 0 = default
     vppgpu::MeCtrl* h_ctrl;  // pinned
     int last_status;
     // per-kernel timing (vppgpu_me_set_timing)
@@ -170,6 +171,19 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
                                   d_mv, d_dist, d_avg, me->ctrl);
     int rc = vppgpu::set_job(ctx, me->d_job, vppgpu::JobDesc{d_src16, d_ref16, d_incl, d_slice, d_mv, d_dist, d_avg});
     if (rc) return rc;
+    if (me->kind == VPPGPU_ME_MULTIRES_CROSS_V2) {
+        vppgpu::V2State v;
+        v.scratch = me->d_mrc;
+        v.spec = reinterpret_cast<int4*>(me->spec);
+        v.final_mv = me->state;
+        v.final_dist = me->state + me->nmb;
+        v.pred_used = me->state + 2 * me->nmb;
+        v.changed = me->changed;
+        v.done = me->d_wave_choice;
+        v.sweeps = me->relax_sweeps ? me->relax_sweeps : vppgpu::V2_SWEEPS;
+        return vppgpu::mrc2_launch(ctx, me->mode, v, full_args(me, 0.9), d_src16, d_ref16, d_incl, d_slice, d_mv,
+                                   d_dist, d_avg);
+    }
     const vppgpu::FullArgs a = full_args(me, lambda);
     cudaEvent_t* ev = ring_slot(me);
     if (!ev && me->graph_state == 0) {
@@ -230,7 +244,8 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
     if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
     if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
-    if (kind != VPPGPU_ME_FULL && kind != VPPGPU_ME_MULTIRES_CROSS) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind != VPPGPU_ME_FULL && kind != VPPGPU_ME_MULTIRES_CROSS && kind != VPPGPU_ME_MULTIRES_CROSS_V2)
+        return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me* me = (vppgpu_me*)calloc(1, sizeof(vppgpu_me));
@@ -256,6 +271,29 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
             (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
             (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||
             (rc = dalloc(&me->d_slice, me->nmb)) || (rc = dalloc(&me->ctrl, 1))) {
+            me_free(me);
+            return rc;
+        }
+        if (cudaMallocHost((void**)&me->h_ctrl, sizeof(vppgpu::MeCtrl)) != cudaSuccess) {
+            me_free(me);
+            return VPPGPU_ERR_OUT_OF_MEMORY;
+        }
+        *out = me;
+        return VPPGPU_OK;
+    }
+    if (kind == VPPGPU_ME_MULTIRES_CROSS_V2) {
+        // MotionEstimatorH264ImplMultiresCrossVer2(…) + Create(): level planes, the
+        // padded reference with its half-pel planes, per-MB prediction state
+        if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
+            (rc = dalloc(&me->d_src8, npix)) || (rc = dalloc(&me->d_refp, npad)) ||
+            (rc = dalloc(&me->d_hpel, 3 * npad)) ||
+            (rc = dalloc(&me->d_mrc, vppgpu::mrc_scratch_bytes(width, height))) ||
+            (rc = dalloc(&me->d_job, 1)) || (rc = dalloc(&me->spec, 4 * (size_t)me->nmb)) ||
+            (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) || (rc = dalloc(&me->d_wave_choice, me->nmb)) ||
+            (rc = dalloc(&me->changed, vppgpu::V2_SWEEPS)) || (rc = dalloc(&me->d_out_mv, me->nmb)) ||
+            (rc = dalloc(&me->d_out_dist, me->nmb)) || (rc = dalloc(&me->d_out_avg, 1)) ||
+            (rc = dalloc(&me->d_incl, me->nmb)) || (rc = dalloc(&me->d_slice, me->nmb)) ||
+            (rc = dalloc(&me->ctrl, 1))) {
             me_free(me);
             return rc;
         }
@@ -301,7 +339,8 @@ int vppgpu_me_set_mode(vppgpu_me* me, int mode)
 {
     if (!me) return VPPGPU_ERR_INVALID_ARG;
     // SetMode(0) picks by picture area (MultiresCross.cpp:501-513)
-    if (mode == 0 && me->kind == VPPGPU_ME_MULTIRES_CROSS) mode = (me->W * me->H > 40000) ? 2 : 1;
+    if (mode == 0 && (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_MULTIRES_CROSS_V2))
+        mode = (me->W * me->H > 40000) ? 2 : 1;
     me->mode = mode;
     return VPPGPU_OK;
 }
@@ -366,9 +405,12 @@ int vppgpu_me_estimate(vppgpu_me* me, const short* src, const short* ref, const 
 int vppgpu_me_estimate_lambda(vppgpu_me* me, const short* src, const short* ref, const unsigned char* incl,
                               const int* slice, double lambda, short* mv_out, int* mb_dist_out, long* avg)
 {
-    // The full-search estimator has no lambda overload: IMotionEstimator's
-    // default Estimate(long*, void*) ignores the parameter (IMotionEstimator.h:94).
+    // The full-search and MultiresCross estimators have no lambda overload:
+    // IMotionEstimator's default Estimate(long*, void*) ignores the parameter
+    // (IMotionEstimator.h:94).  Ver2's overload (per-level GetBestVector,
+    // MultiresCrossVer2.cpp:1162-1722) is not built.
     (void)lambda;
+    if (me && me->kind == VPPGPU_ME_MULTIRES_CROSS_V2) return VPPGPU_ERR_UNSUPPORTED;
     return estimate_host(me, src, ref, incl, slice, mv_out, mb_dist_out, avg, 1.05);
 }
 
@@ -436,6 +478,14 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 }
 
 }  // extern "C"
+
+extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
+{
+    if (!me || sweeps < 0 || sweeps > vppgpu::V2_SWEEPS) return VPPGPU_ERR_INVALID_ARG;
+    if (me->kind != VPPGPU_ME_MULTIRES_CROSS_V2) return VPPGPU_ERR_UNSUPPORTED;
+    me->relax_sweeps = sweeps;
+    return VPPGPU_OK;
+}
 
 extern "C" int vppgpu_me_residual_device(vppgpu_me* me, const short* d_mv, short* d_residual)
 {
@@ -543,7 +593,8 @@ int vppgpu_me_batch_create(vppgpu_ctx* ctx, int kind, int streams, vppgpu_me_bat
 {
     if (!ctx || !out || streams < 1) return VPPGPU_ERR_INVALID_ARG;
     *out = nullptr;
-    if (kind != VPPGPU_ME_FULL && kind != VPPGPU_ME_MULTIRES_CROSS) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind != VPPGPU_ME_FULL && kind != VPPGPU_ME_MULTIRES_CROSS && kind != VPPGPU_ME_MULTIRES_CROSS_V2)
+        return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me_batch* b = (vppgpu_me_batch*)calloc(1, sizeof(vppgpu_me_batch));

@@ -113,6 +113,18 @@ __device__ __forceinline__ void median_pred(const int* final_mv, int av, int k, 
     median_from(av, A, B, C, D, px, py);
 }
 
+// Flag word accesses ordered against the data they publish (device scope).
+__device__ __forceinline__ int ld_acquire(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // Nearest full-pel prediction with C division (Full.cpp:368-380).
 __device__ __forceinline__ int round_pred(int p) { return p < 0 ? (p - 2) / 4 : (p + 2) / 4; }
 

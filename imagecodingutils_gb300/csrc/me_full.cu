@@ -383,9 +383,8 @@ int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v)
 
 size_t full_search_smem() { return sizeof(TableSmem); }
 
-int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid, cudaEvent_t* ev)
+int full_planes_launch(vppgpu_ctx* ctx, const FullArgs& args)
 {
-    if (ev) VPP_CUDA(cudaEventRecord(ev[0], ctx->stream));
     {
         long long work = (long long)((args.W + 2 * PAD) / 4) * (args.H + 2 * PAD) + (long long)args.W * args.H / 4;
         int grid = (int)((work + 255) / 256);
@@ -403,6 +402,14 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid
                                                       args.plane_size);
         VPP_CHECK_LAUNCH(ctx);
     }
+    return VPPGPU_OK;
+}
+
+int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid, cudaEvent_t* ev)
+{
+    if (ev) VPP_CUDA(cudaEventRecord(ev[0], ctx->stream));
+    int rc = full_planes_launch(ctx, args);
+    if (rc) return rc;
     if (ev) VPP_CUDA(cudaEventRecord(ev[1], ctx->stream));
     k_full_table<<<nmb, 128, sizeof(TableSmem), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
@@ -412,7 +419,7 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid
     k_full_tietree<<<ctx->sm_count, TIE_RUNS * 32, sizeof(TieSmem), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     if (ev) VPP_CUDA(cudaEventRecord(ev[3], ctx->stream));
-    int rc = full_resolve_launch(ctx, args, resolve_grid);
+    rc = full_resolve_launch(ctx, args, resolve_grid);
     if (rc) return rc;
     if (ev) VPP_CUDA(cudaEventRecord(ev[4], ctx->stream));
     return VPPGPU_OK;

@@ -278,5 +278,76 @@ __device__ __forceinline__ uint2 load_cur8(const FullArgs& a, int n, int m, int 
     return __ldg(reinterpret_cast<const uint2*>(a.src8 + (size_t)(m + (lane >> 1)) * a.W + n + 8 * (lane & 1)));
 }
 
+// Prediction clamped to one macroblock outside the picture (Full.cpp:532-541)
+// and the folded full-pel origin / fraction of its QuarterRead.
+struct PredGeom {
+    int pcx, pcy, ox, oy, fx, fy;
+};
+
+__device__ __forceinline__ PredGeom pred_geom(int n, int m, int W, int H, int px, int py)
+{
+    int pxq = px % 4, pyq = py % 4, px0 = px / 4, py0 = py / 4;
+    if (px0 + n > W) px0 = 16;
+    if (px0 + n < -16) px0 = -16;
+    if (py0 + m > H) py0 = 16;
+    if (py0 + m < -16) py0 = -16;
+    PredGeom g;
+    g.pcx = 4 * px0 + pxq;
+    g.pcy = 4 * py0 + pyq;
+    g.fx = pxq < 0 ? pxq + 4 : pxq;
+    g.fy = pyq < 0 ? pyq + 4 : pyq;
+    g.ox = n + px0 + (pxq < 0 ? -1 : 0);
+    g.oy = m + py0 + (pyq < 0 ? -1 : 0);
+    return g;
+}
+
+// Distortion at the prediction, one warp: QuarterRead's sixteen cases
+// (OverlayMem2Dv2::QuarterRead) as one sample of the full-pel, b, h or j
+// plane, or the rounded mean of two.  Lane l covers row l/2, columns
+// 8*(l&1) .. +7; squared differences with dp4a on per-byte |differences|.
+// This lane's 8 quarter-pel samples (row lane/2, columns 8*(lane&1)..+7) of
+// the 16x16 block at full-pel origin (ox, oy) and fraction (fx, fy) in 0..3.
+__device__ __forceinline__ uint2 qpel_block8(const FullArgs& a, int ox, int oy, int fx, int fy, int lane)
+{
+    const int r = lane >> 1, c0 = (lane & 1) * 8, st = a.rstride;
+    const size_t o = (size_t)(oy + r + PAD) * st + (size_t)(ox + c0 + PAD);
+    const unsigned char* G = a.refp;
+    const unsigned char* Bp = a.hpel;
+    const unsigned char* Hp = a.hpel + a.plane_size;
+    const unsigned char* Jp = a.hpel + 2 * a.plane_size;
+    const unsigned char *p1 = G + o, *p2 = G + o;
+    bool two = true;
+    switch (fx | (fy << 2)) {
+    case 0: two = false; break;                          // G
+    case 2: p1 = Bp + o; two = false; break;             // b
+    case 8: p1 = Hp + o; two = false; break;             // h
+    case 10: p1 = Jp + o; two = false; break;            // j
+    case 1: p2 = Bp + o; break;                          // a = (G + b)
+    case 3: p1 = G + o + 1; p2 = Bp + o; break;          // c = (G[x+1] + b)
+    case 4: p2 = Hp + o; break;                          // d = (G + h)
+    case 12: p1 = G + o + st; p2 = Hp + o; break;        // n = (G[y+1] + h)
+    case 6: p1 = Jp + o; p2 = Bp + o; break;             // f = (j + b)
+    case 14: p1 = Jp + o; p2 = Bp + o + st; break;       // q = (j + b[y+1])
+    case 9: p1 = Jp + o; p2 = Hp + o; break;             // i = (j + h)
+    case 11: p1 = Jp + o; p2 = Hp + o + 1; break;        // k = (j + h[x+1])
+    case 5: p1 = Bp + o; p2 = Hp + o; break;             // e = (b + h)
+    case 7: p1 = Bp + o; p2 = Hp + o + 1; break;         // g = (b + h[x+1])
+    case 13: p1 = Hp + o; p2 = Bp + o + st; break;       // p = (h + b[y+1])
+    default: p1 = Hp + o + 1; p2 = Bp + o + st; break;   // r = (h[x+1] + b[y+1])
+    }
+    uint2 v = load8(p1);
+    if (two) {
+        const uint2 w = load8(p2);
+        v.x = __vavgu4(v.x, w.x);  // (p + q + 1) >> 1 per byte
+        v.y = __vavgu4(v.y, w.y);
+    }
+    return v;
+}
+
+__device__ __forceinline__ int plane_pred_distortion(const FullArgs& a, int n, int m, const PredGeom& g, int lane)
+{
+    return warp_sum(ssd8(load_cur8(a, n, m, lane), qpel_block8(a, g.ox, g.oy, g.fx, g.fy, lane)));
+}
+
 }  // namespace full
 }  // namespace vppgpu

@@ -17,6 +17,7 @@ struct MeCtrl {
     int relax_miss;  // ... of which computed the prediction distortion
     int wave_miss;   // MBs the wavefront had to evaluate in full
     int ntie;        // entries of FullArgs::tie_list
+    int ticket;      // MultiresCrossVer2 dataflow pass: next macroblock
 };
 
 constexpr int KCACHE = 32;  // records per macroblock
@@ -104,6 +105,24 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
 const int* me_status_word(vppgpu_me* me);
 int status_from_bits(int bits);
 
+// MultiresCrossVer2 (me_mrc.cu): level planes plus the per-MB state of the
+// prediction-dependent pass; `planes` carries the Full geometry and buffers
+// used for the distortion at the prediction (src8, refp, hpel, job, ctrl).
+constexpr int V2_SWEEPS = 8;
+struct V2State {
+    unsigned char* scratch;  // mrc_scratch_bytes
+    int4* spec;              // nmb
+    int* final_mv;           // nmb
+    int* final_dist;         // nmb
+    int* pred_used;          // nmb
+    int* changed;            // V2_SWEEPS
+    int* done;               // nmb
+    int sweeps;              // relaxation sweeps before the dataflow pass, 1..V2_SWEEPS
+};
+int mrc2_launch(vppgpu_ctx* ctx, int mode, const V2State& st, const FullArgs& planes, const short* d_src16,
+                const short* d_ref16, const unsigned char* incl, const int* slice, int* out_mv, int* out_dist,
+                long long* out_avg);
+
 // Write this estimate's pointers to the device descriptor (a one-thread
 // kernel with the descriptor as its parameter: stream-ordered, no host copy).
 int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v);
@@ -112,6 +131,9 @@ int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v);
 int full_residual_launch(vppgpu_ctx* ctx, const FullArgs& args, const int* d_mv, short* d_res);
 
 size_t full_search_smem();
+// Byte-packed input (args.src8), padded reference and its half-pel planes
+// from the int16 planes of args.job.
+int full_planes_launch(vppgpu_ctx* ctx, const FullArgs& args);
 // Launch the prediction-dependent tail (sweep 0, relaxation, dictionary
 // precompute, exact wavefront) of an estimate whose search has run.
 int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid);

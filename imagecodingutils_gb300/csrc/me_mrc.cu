@@ -30,7 +30,7 @@
 //                  minimum.  The sub-pel window's lattice (G, h, b,
 //                  j at 22x22 points, with the window's unwritten and
 //                  unscaled edge samples) is built per warp in shared memory.
-#include "me_common.cuh"
+#include "me_full_common.cuh"
 #include "me_internal.h"
 
 namespace vppgpu {
@@ -234,6 +234,7 @@ __device__ __forceinline__ int lat(const Lattice& L, int qr, int qc)
     return (qc & 3) == 0 ? L.h[fr][fc] : L.j[fr][fc];
 }
 
+template <bool kVer2>
 __device__ void build_lattice(Lattice& L, const Buf& e0, Org o, int lane, bool& bad)
 {
     for (int i = lane; i < 22 * 22; i += 32) {
@@ -271,6 +272,20 @@ __device__ void build_lattice(Lattice& L, const Buf& e0, Org o, int lane, bool& 
         L.b[fr][fc] = (short)clip255((L.b[fr][fc] + 16) >> 5);
         L.g[fr][fc] = (short)rd(e0, o.y + fr - 3, o.x + fc - 3, bad);
     }
+    if (kVer2 && lane < 18) {
+        // Ver2 completes column and row 19 (…MultiresCrossVer2.cpp:2075-2093):
+        // scaled h and G at column 19 of rows 2..18, scaled b and G at row 19
+        // of columns 2..18, G at (19, 19)
+        if (lane < 17) {
+            const int f = 2 + lane;
+            L.h[f][19] = (short)clip255((L.h[f][19] + 16) >> 5);
+            L.g[f][19] = (short)rd(e0, o.y + f - 3, o.x + 16, bad);
+            L.b[19][f] = (short)clip255((L.b[19][f] + 16) >> 5);
+            L.g[19][f] = (short)rd(e0, o.y + 16, o.x + f - 3, bad);
+        } else {
+            L.g[19][19] = (short)rd(e0, o.y + 16, o.x + 16, bad);
+        }
+    }
     __syncwarp();
 }
 
@@ -293,33 +308,48 @@ __device__ __forceinline__ int quarter(const Lattice& L, int qr, int qc, int sy,
 }
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
+struct MbSearch {
+    int zero_d, min_d, mvx, mvy;
+    bool tie;  // an integer stage met a candidate equal to its running minimum
+};
+
+// Tie rule of the integer stages: an equal distortion replaces the current
+// best (offset (rmx, rmy) from the centre (mx, my)) unless the candidate at
+// (j, i) is farther from (px, py): (0, 0) for MultiresCross
+// (…MultiresCross.cpp:741-746, 794, 857), the level's rounded prediction for
+// Ver2 (…MultiresCrossVer2.cpp:778-786, 834-842, 906-914).
+__device__ __forceinline__ bool farther(int mx, int my, int rmx, int rmy, int j, int i, int px, int py)
 {
-    __shared__ Lattice lattice[8];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int k = blockIdx.x * 8 + wib;
-    if (k >= a.cols * a.rows_all) return;
-    Lattice& LT = lattice[wib];
-    bool bad = false;
-    const int mbr = k / a.cols, mbc = k - mbr * a.cols;
+    const int cx = mx + rmx - px, cy = my + rmy - py, nx = mx + j - px, ny = my + i - py;
+    return (cy * cy + cx * cx) - (ny * ny + nx * nx) < 0;
+}
+
+// The search of one macroblock, one warp, from the zero vector to the
+// quarter-pel winner (…MultiresCross.cpp:612-941; …MultiresCrossVer2.cpp:643-992).
+// kVer2: ties towards pl = {level-2 x, y, level-1 x, y, level-0 rounded x, y}
+// of the prediction and the completed sub-pel window.
+template <bool kVer2>
+__device__ MbSearch search_mb(const MrcArgs& a, Lattice& LT, int mbr, int mbc, const int* pl, int lane, bool& bad)
+{
     const int m = 16 * mbr, n = 16 * mbc, p = 8 * mbr, q = 8 * mbc, kk = 4 * mbr, ll = 4 * mbc;
-    const int vec_pos = k < a.nmb ? k : a.nmb;
     const int w1 = a.W / 2, h1 = a.H / 2, w2 = w1 / 2, h2 = h1 / 2;
     const int l1_range = a.motion_range / 8, l2_range = l1_range / 2;
     const int lcl_l1_range = a.mode == 2 ? 2 : l1_range;
     const Level L0{16, a.W, a.H, a.motion_range / 4}, L1{8, w1, h1, l1_range}, L2{4, w2, h2, l2_range};
     constexpr int CRX[4] = {-1, 1, 0, 0}, CRY[4] = {0, 0, -1, 1};
     constexpr int SX[8] = {-1, 0, 1, -1, 1, -1, 0, 1}, SY[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+    MbSearch out;
+    out.tie = false;
 
     const Org oin0 = origin(a.in0, 16, 16, 0, n, m);
-    const int zero_d = full_ssd(a.in0, oin0, a.e0, origin(a.e0, 16, 16, 19, n, m), 16, lane, bad);
+    out.zero_d = full_ssd(a.in0, oin0, a.e0, origin(a.e0, 16, 16, 19, n, m), 16, lane, bad);
     int mx = 0, my = 0, rmx = 0, rmy = 0, xl, xr, yu, yd;
 
-    if (a.mode == 2) {  // level 2 cross search (…:639-697)
+    if (a.mode == 2) {  // level 2 cross search (…MultiresCross.cpp:639-697)
         const Org oin2 = origin(a.in2, 4, 4, 0, ll, kk);
         int min2 = full_ssd(a.in2, oin2, a.e2, origin(a.e2, 4, 4, 5, ll, kk), 4, lane, bad);
+        mr_range(L2, ll, kk, 0, 0, l2_range - 1, xl, xr, yu, yd);
         for (int s = l2_range / 2; s > 0; s /= 2) {
-            mr_range(L2, ll, kk, 0, 0, l2_range - 1, xl, xr, yu, yd);
             rmx = rmy = 0;
             for (int c = 0; c < 4; c++) {
                 const int i = s * CRY[c], j = s * CRX[c];
@@ -327,7 +357,12 @@ __global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
                 // Tsd4x4LessThan stops early only on a sum already above min: a full SSD decides the same
                 const int d = full_ssd(a.in2, oin2, a.e2, origin(a.e2, 4, 4, 5, j + ll + mx, i + kk + my), 4, lane, bad);
                 if (d > min2) continue;
-                if (d == min2 && (my * my + mx * mx) - (i * i + j * j) < 0) continue;
+                if (d == min2) {
+                    out.tie = true;
+                    // MultiresCross compares the centre with the offset (…MultiresCross.cpp:673-679)
+                    if (kVer2 ? farther(mx, my, rmx, rmy, j, i, pl[0], pl[1]) : (my * my + mx * mx) - (i * i + j * j) < 0)
+                        continue;
+                }
                 min2 = d;
                 rmx = j;
                 rmy = i;
@@ -339,7 +374,8 @@ __global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
         my <<= 1;
     }
 
-    // level 1 (…:699-816): input samples of this lane's phase share, kept
+    // level 1 (…MultiresCross.cpp:699-816): input samples of this lane's phase share, kept
+    const int p1x = kVer2 ? pl[2] : 0, p1y = kVer2 ? pl[3] : 0;
     const Org oin1 = origin(a.in1, 8, 8, 0, q, p);
     int r1, c1;
     phase_coords<8>(lane, r1, c1);
@@ -360,9 +396,10 @@ __global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
     auto consider1 = [&](int i, int j) {
         const int d = partial_value(part8(origin(a.e1, 8, 8, 9, j + mx + q, i + my + p)), min1, lane);
         if (d > min1) return;
-        if (d == min1 &&
-            ((my + rmy) * (my + rmy) + (mx + rmx) * (mx + rmx)) - ((my + i) * (my + i) + (mx + j) * (mx + j)) < 0)
-            return;
+        if (d == min1) {
+            out.tie = true;
+            if (farther(mx, my, rmx, rmy, j, i, p1x, p1y)) return;
+        }
         min1 = d;
         rmx = j;
         rmy = i;
@@ -385,11 +422,12 @@ __global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
             my += rmy;
         }
     }
-    // the last level-1 refinement is added once more (…:815-816)
+    // the last level-1 refinement is added once more (…MultiresCross.cpp:815-816)
     mx = (mx + rmx) * 2;
     my = (my + rmy) * 2;
 
-    // level 0 +-2 refinement (…:819-873)
+    // level 0 +-2 refinement (…MultiresCross.cpp:819-873)
+    const int p0x = kVer2 ? pl[4] : 0, p0y = kVer2 ? pl[5] : 0;
     int r0, c0;
     phase_coords<16>(lane, r0, c0);
     int cur0[8];
@@ -416,9 +454,10 @@ __global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
             if (!(i || j)) continue;
             const int d = partial_value(part16(origin(a.e0, 16, 16, 19, n + mx + j, m + my + i)), min_d, lane);
             if (d > min_d) continue;
-            if (d == min_d &&
-                ((my + rmy) * (my + rmy) + (mx + rmx) * (mx + rmx)) - ((my + i) * (my + i) + (mx + j) * (mx + j)) < 0)
-                continue;
+            if (d == min_d) {
+                out.tie = true;
+                if (farther(mx, my, rmx, rmy, j, i, p0x, p0y)) continue;
+            }
             min_d = d;
             rmx = j;
             rmy = i;
@@ -427,8 +466,8 @@ __global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
     my += rmy;
     int mvx = mx * 4, mvy = my * 4;
 
-    // half then quarter pel in the estimator's window (…:875-941)
-    build_lattice(LT, a.e0, origin(a.e0, 16, 16, 19, n + mx, m + my), lane, bad);
+    // half then quarter pel in the estimator's window (…MultiresCross.cpp:875-941), strict improvements
+    build_lattice<kVer2>(LT, a.e0, origin(a.e0, 16, 16, 19, n + mx, m + my), lane, bad);
     int hmx = 0, hmy = 0;
     for (int c = 0; c < 8; c++) {
         const int qx = 2 * SX[c], qy = 2 * SY[c];
@@ -465,21 +504,37 @@ __global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
             qmy = hmy + SY[c];
         }
     }
-    mvx += qmx;
-    mvy += qmy;
+    __syncwarp();  // the lattice is reused by this warp's next search
+    out.min_d = min_d;
+    out.mvx = mvx + qmx;
+    out.mvy = mvy + qmy;
+    return out;
+}
 
-    // accept-or-zero heuristic (…:943-999)
+__global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
+{
+    __shared__ Lattice lattice[8];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int k = blockIdx.x * 8 + wib;
+    if (k >= a.cols * a.rows_all) return;
+    bool bad = false;
+    const int mbr = k / a.cols, mbc = k - mbr * a.cols;
+    const int vec_pos = k < a.nmb ? k : a.nmb;
+    const MbSearch r = search_mb<false>(a, lattice[wib], mbr, mbc, nullptr, lane, bad);
+    int mvx = r.mvx, mvy = r.mvy;
+
+    // accept-or-zero heuristic (…MultiresCross.cpp:943-999)
     int weight = 0;
-    const int diff0 = zero_d - min_d, mag = mvx * mvx + mvy * mvy;
+    const int diff0 = r.zero_d - r.min_d, mag = mvx * mvx + mvy * mvy;
     if (diff0 < mag) weight++;
-    if (zero_d < MRC_NOISE_FLOOR) weight++;
-    if (diff0 * 10 < min_d) weight++;
+    if (r.zero_d < MRC_NOISE_FLOOR) weight++;
+    if (diff0 * 10 < r.min_d) weight++;
     int chosen;
-    if (min_d < zero_d && weight < 2) {
-        chosen = min_d;
+    if (r.min_d < r.zero_d && weight < 2) {
+        chosen = r.min_d;
     } else {
         mvx = mvy = 0;
-        chosen = zero_d;
+        chosen = r.zero_d;
     }
     const bool do_it = a.incl ? (vec_pos < a.nmb ? a.incl[vec_pos] != 0 : false) : true;
     bad = __any_sync(0xffffffffu, bad);
@@ -503,6 +558,191 @@ __global__ void k_mrc_average(long long* out_avg, MeCtrl* ctrl)
     if (out_avg) *out_avg = c ? t / c : 0;
 }
 
+// ---------------------------------------------------------------------------
+// MultiresCrossVer2 (…MultiresCrossVer2.cpp:537-1151).  The search depends on
+// the median prediction only through its tie rules, so every macroblock is
+// searched once with the prediction (0, 0) and remembers whether a tie
+// occurred; the result is the search at any prediction unless it did.  The
+// rest is a function of the prediction (distortion at the prediction through
+// the half-pel planes, GetBestVector with lambda 0.9) and the predictions form
+// the raster-order DAG of the full-search estimator: relaxation sweeps reach
+// its unique fixed point on most frames; otherwise a ticket-ordered dataflow
+// pass replays the exact order.
+constexpr int kV2Empty = 0x7fffffff;
+
+struct V2Args {
+    MrcArgs m;
+    FullArgs f;        // byte input, padded reference and half-pel planes (distortion at the prediction)
+    int4* spec;        // per MB {searched vector at prediction (0,0), its distortion, zero-vector distortion, flags}
+    int* final_mv;
+    int* final_dist;
+    int* pred_used;    // prediction of the last evaluation, kV2Empty before the first
+    int* changed;      // MBs whose vector changed, per sweep
+    int* done;         // dataflow pass: MB final
+    const int* slice;
+    long long spin_limit;
+};
+
+constexpr int V2_TIE = 1;
+
+__global__ void __launch_bounds__(256) k_v2_search(V2Args a)
+{
+    __shared__ Lattice lattice[8];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int k = blockIdx.x * 8 + wib;
+    if (k >= a.m.nmb) return;
+    bool bad = false;
+    const int mbr = k / a.m.cols, mbc = k - mbr * a.m.cols;
+    const int zero6[6] = {0, 0, 0, 0, 0, 0};
+    const MbSearch r = search_mb<true>(a.m, lattice[wib], mbr, mbc, zero6, lane, bad);
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        if (bad) atomicOr(&a.m.ctrl->status, ST_OUT_OF_BOUNDS);
+        const int flags = (r.tie ? V2_TIE : 0) | neighbour_mask(a.slice, k, a.m.cols, a.m.nmb / a.m.cols);
+        a.spec[k] = make_int4(pack_mv(r.mvx, r.mvy), r.min_d, r.zero_d, flags);
+        a.final_mv[k] = pack_mv(r.mvx, r.mvy);
+        a.pred_used[k] = kV2Empty;
+    }
+}
+
+// Final vector and distortion of macroblock k at prediction (px, py), one warp.
+__device__ void v2_evaluate(const V2Args& a, Lattice& LT, int k, int px, int py, int lane, int* fmv, int* fd,
+                            bool& bad)
+{
+    const int4 s = __ldg(a.spec + k);
+    const int mbr = k / a.m.cols, mbc = k - mbr * a.m.cols, n = 16 * mbc, m = 16 * mbr;
+    int mvx = mv_x(s.x), mvy = mv_y(s.x), md = s.y;
+    const int p0x = round_pred(px), p0y = round_pred(py);
+    if ((s.w & V2_TIE) && (p0x | p0y)) {  // the searched result holds for prediction levels (0, 0) only
+        const int pl[6] = {p0x / 2 / 2, p0y / 2 / 2, p0x / 2, p0y / 2, p0x, p0y};
+        const MbSearch r = search_mb<true>(a.m, LT, mbr, mbc, pl, lane, bad);
+        mvx = r.mvx;
+        mvy = r.mvy;
+        md = r.min_d;
+    }
+    // pred-vector check and GetBestVector (…MultiresCrossVer2.cpp:1008-1064)
+    const full::PredGeom g = full::pred_geom(n, m, a.m.W, a.m.H, px, py);
+    const int pd = full::plane_pred_distortion(a.f, n, m, g, lane);
+    const int pos = best_of3_fast(mvx, mvy, md, g.pcx, g.pcy, pd, s.z, 0.9, g.pcx, g.pcy);
+    *fmv = pos == 0 ? pack_mv(mvx, mvy) : (pos == 1 ? pack_mv(g.pcx, g.pcy) : 0);
+    *fd = pos == 0 ? md : (pos == 1 ? pd : s.z);
+}
+
+// Relaxation sweep s: every MB (s = 0) or those whose prediction moved.  A
+// sweep that changes nothing leaves the fixed point; later sweeps exit.
+__global__ void __launch_bounds__(256) k_v2_sweep(V2Args a, int s)
+{
+    __shared__ Lattice lattice[8];
+    if (s > 0 && __ldcg(a.changed + s - 1) == 0) return;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int k = blockIdx.x * 8 + wib;
+    if (k >= a.m.nmb) return;
+    const int av = __ldg(&a.spec[k].w);
+    int px, py;
+    median_pred(a.final_mv, av, k, a.m.cols, &px, &py);
+    const int key = pack_mv(px, py);
+    if (s > 0 && key == __ldcg(a.pred_used + k)) return;
+    bool bad = false;
+    int fmv, fd;
+    v2_evaluate(a, lattice[wib], k, px, py, lane, &fmv, &fd, bad);
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        if (bad) atomicOr(&a.m.ctrl->status, ST_OUT_OF_BOUNDS);
+        a.pred_used[k] = key;
+        a.final_dist[k] = fd;
+        if (fmv != __ldcg(a.final_mv + k)) {
+            a.final_mv[k] = fmv;
+            atomicAdd(a.changed + s, 1);
+        }
+    }
+}
+
+// Lane 0: wait until MB j is final (bounded).
+__device__ __forceinline__ void v2_wait(const V2Args& a, int j)
+{
+    long long spins = 0;
+    while (ld_acquire(a.done + j) == 0) {
+        if (++spins > a.spin_limit) {
+            atomicOr(&a.m.ctrl->status, ST_TIMEOUT);
+            return;
+        }
+        __nanosleep(32);
+    }
+}
+
+// Exact raster order when the sweeps did not converge: warps take MBs in
+// raster order from a ticket counter and wait for the neighbours the
+// prediction reads; every earlier ticket is held by a running warp, so the
+// waits end.  An MB whose prediction equals the one of its last evaluation
+// keeps that result.
+__global__ void __launch_bounds__(256) k_v2_wave(V2Args a, int last_sweep)
+{
+    __shared__ Lattice lattice[8];
+    if (__ldcg(a.changed + last_sweep) == 0) return;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int cols = a.m.cols;
+    for (;;) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(&a.m.ctrl->ticket, 1);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= a.m.nmb) return;
+        const int av = __ldg(&a.spec[k].w);
+        int px = 0, py = 0;
+        if (lane == 0) {
+            if (av & AV_A) v2_wait(a, k - 1);
+            if (av & AV_B) v2_wait(a, k - cols);
+            if (av & AV_C) v2_wait(a, k - cols + 1);
+            else if (av & AV_D) v2_wait(a, k - cols - 1);
+            median_pred(a.final_mv, av, k, cols, &px, &py);
+        }
+        px = __shfl_sync(0xffffffffu, px, 0);
+        py = __shfl_sync(0xffffffffu, py, 0);
+        const int key = pack_mv(px, py);
+        if (key != __ldcg(a.pred_used + k)) {
+            bool bad = false;
+            int fmv, fd;
+            v2_evaluate(a, lattice[wib], k, px, py, lane, &fmv, &fd, bad);
+            bad = __any_sync(0xffffffffu, bad);
+            if (lane == 0) {
+                if (bad) atomicOr(&a.m.ctrl->status, ST_OUT_OF_BOUNDS);
+                a.pred_used[k] = key;
+                a.final_dist[k] = fd;
+                a.final_mv[k] = fmv;
+            }
+        }
+        __syncwarp();
+        if (lane == 0) st_release(a.done + k, 1);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_v2_outputs(V2Args a, int sweeps)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) {  // sweeps to the fixed point, or 1000 + sweeps when the dataflow pass ran
+        int s = 0;
+        while (s < sweeps && __ldcg(a.changed + s) != 0) s++;
+        a.m.ctrl->sweeps = s < sweeps ? s + 1 : 1000 + sweeps;
+        a.m.ctrl->converged = s < sweeps;
+    }
+    bool inc = false;
+    int d = 0;
+    if (k < a.m.nmb) {
+        const int v = __ldcg(a.final_mv + k);
+        d = __ldcg(a.final_dist + k);
+        a.m.out_mv[k] = v;
+        if (a.m.out_dist) a.m.out_dist[k] = d;
+        inc = a.m.incl && a.m.incl[k];
+    }
+    // avgDistortion counts included MBs only; none without pDistortionIncluded (…:1053-1062)
+    const unsigned mask = __ballot_sync(0xffffffffu, inc);
+    long long sum = inc ? d : 0;
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0 && mask) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&a.m.ctrl->total), (unsigned long long)sum);
+        atomicAdd(&a.m.ctrl->count, __popc(mask));
+    }
+}
+
 }  // namespace
 
 size_t mrc_scratch_bytes(int W, int H)
@@ -512,12 +752,12 @@ size_t mrc_scratch_bytes(int W, int H)
            (w2 + 10) * (h2 + 10) + 64;
 }
 
-int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const short* d_src16, const short* d_ref16,
-               unsigned char* scratch, const unsigned char* incl, int* out_mv, int* out_dist, long long* out_avg,
-               MeCtrl* ctrl)
+namespace {
+
+MrcArgs mrc_args(int W, int H, int motion_range, int mode, unsigned char* scratch)
 {
     const int w1 = W / 2, h1 = H / 2, w2 = w1 / 2, h2 = h1 / 2;
-    if (mode == 0) mode = (W * H > 40000) ? 2 : 1;  // SetMode(0) (…:501-513)
+    if (mode == 0) mode = (W * H > 40000) ? 2 : 1;  // SetMode(0) (…MultiresCross.cpp:501-513)
     MrcArgs a;
     a.W = W;
     a.H = H;
@@ -544,31 +784,96 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
     a.e1 = Buf{e1, w1 + 18, h1 + 18};
     a.in2 = Buf{in2, w2, h2};
     a.e2 = Buf{e2, w2 + 10, h2 + 10};
-    a.incl = incl;
-    a.out_mv = out_mv;
-    a.out_dist = out_dist;
-    a.out_avg = out_avg;
-    a.ctrl = ctrl;
+    a.incl = nullptr;
+    a.out_mv = nullptr;
+    a.out_dist = nullptr;
+    a.out_avg = nullptr;
+    a.ctrl = nullptr;
+    return a;
+}
+
+int levels_launch(vppgpu_ctx* ctx, const MrcArgs& a, const short* d_src16, const short* d_ref16)
+{
+    const int W = a.W, H = a.H, w1 = W / 2, h1 = H / 2, w2 = w1 / 2, h2 = h1 / 2;
     const int cap = ctx->sm_count * 8;
     auto grid = [&](long long work) {
         long long g = (work + 255) / 256;
         return (int)(g < cap ? g : cap);
     };
     k_mrc_level0<<<grid((long long)W * H + (long long)(W + 38) * (H + 38)), 256, 0, ctx->stream>>>(
-        d_src16, d_ref16, W, H, in0, e0, &ctrl->status);
+        d_src16, d_ref16, W, H, (unsigned char*)a.in0.p, (unsigned char*)a.e0.p, &a.ctrl->status);
     VPP_CHECK_LAUNCH(ctx);
     k_mrc_level1<<<grid((long long)w1 * h1 + (long long)(w1 + 18) * (h1 + 18)), 256, 0, ctx->stream>>>(
-        d_src16, d_ref16, W, H, in1, e1);
+        d_src16, d_ref16, W, H, (unsigned char*)a.in1.p, (unsigned char*)a.e1.p);
     VPP_CHECK_LAUNCH(ctx);
-    if (mode == 2) {
+    if (a.mode == 2) {
         k_mrc_level2<<<grid((long long)w2 * h2 + (long long)(w2 + 10) * (h2 + 10)), 256, 0, ctx->stream>>>(
-            in1, e1, W, H, in2, e2);
+            a.in1.p, a.e1.p, W, H, (unsigned char*)a.in2.p, (unsigned char*)a.e2.p);
         VPP_CHECK_LAUNCH(ctx);
     }
+    return VPPGPU_OK;
+}
+
+}  // namespace
+
+int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const short* d_src16, const short* d_ref16,
+               unsigned char* scratch, const unsigned char* incl, int* out_mv, int* out_dist, long long* out_avg,
+               MeCtrl* ctrl)
+{
+    MrcArgs a = mrc_args(W, H, motion_range, mode, scratch);
+    a.incl = incl;
+    a.out_mv = out_mv;
+    a.out_dist = out_dist;
+    a.out_avg = out_avg;
+    a.ctrl = ctrl;
+    int rc = levels_launch(ctx, a, d_src16, d_ref16);
+    if (rc) return rc;
     const int warps = a.cols * a.rows_all;
     k_mrc_search<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(a);
     VPP_CHECK_LAUNCH(ctx);
     k_mrc_average<<<1, 1, 0, ctx->stream>>>(out_avg, ctrl);
+    VPP_CHECK_LAUNCH(ctx);
+    return VPPGPU_OK;
+}
+
+int mrc2_launch(vppgpu_ctx* ctx, int mode, const V2State& st, const FullArgs& planes, const short* d_src16,
+                const short* d_ref16, const unsigned char* incl, const int* slice, int* out_mv, int* out_dist,
+                long long* out_avg)
+{
+    V2Args a;
+    a.m = mrc_args(planes.W, planes.H, planes.motion_range, mode, st.scratch);
+    a.m.incl = incl;
+    a.m.out_mv = out_mv;
+    a.m.out_dist = out_dist;
+    a.m.out_avg = out_avg;
+    a.m.ctrl = planes.ctrl;
+    a.f = planes;
+    a.spec = st.spec;
+    a.final_mv = st.final_mv;
+    a.final_dist = st.final_dist;
+    a.pred_used = st.pred_used;
+    a.changed = st.changed;
+    a.done = st.done;
+    a.slice = slice;
+    a.spin_limit = planes.spin_limit;
+    int rc = full_planes_launch(ctx, planes);
+    if (rc) return rc;
+    if ((rc = levels_launch(ctx, a.m, d_src16, d_ref16))) return rc;
+    const int nmb = a.m.nmb, blocks = (nmb + 7) / 8;
+    const int sweeps = st.sweeps < 1 ? 1 : (st.sweeps > V2_SWEEPS ? V2_SWEEPS : st.sweeps);
+    VPP_CUDA(cudaMemsetAsync(st.changed, 0, sizeof(int) * V2_SWEEPS, ctx->stream));
+    VPP_CUDA(cudaMemsetAsync(st.done, 0, sizeof(int) * (size_t)nmb, ctx->stream));
+    k_v2_search<<<blocks, 256, 0, ctx->stream>>>(a);
+    VPP_CHECK_LAUNCH(ctx);
+    for (int s = 0; s < sweeps; s++) {
+        k_v2_sweep<<<blocks, 256, 0, ctx->stream>>>(a, s);
+        VPP_CHECK_LAUNCH(ctx);
+    }
+    k_v2_wave<<<ctx->sm_count * 4, 256, 0, ctx->stream>>>(a, sweeps - 1);
+    VPP_CHECK_LAUNCH(ctx);
+    k_v2_outputs<<<(nmb + 255) / 256, 256, 0, ctx->stream>>>(a, sweeps);
+    VPP_CHECK_LAUNCH(ctx);
+    k_mrc_average<<<1, 1, 0, ctx->stream>>>(out_avg, planes.ctrl);
     VPP_CHECK_LAUNCH(ctx);
     return VPPGPU_OK;
 }

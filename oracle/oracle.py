@@ -51,6 +51,7 @@ class Oracle:
         L.vo_me_full_detail.argtypes = [_P, _P, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L)] + [_P] * 6
         L.vo_me_full_intpel.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P]
         L.vo_me_multires_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
+        L.vo_me_multires_cross_v2.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_quarter_read16.argtypes = [_P, _I, _I, _I, _I, _I, _I, _P]
         L.vo_half.argtypes = [_P, _I, _I, _P]
         L.vo_fwd4x4.argtypes = [_P, _I, _I, _I, _I, _I]
@@ -99,6 +100,24 @@ class Oracle:
         if rc:
             raise ValueError(f"vo_me_multires_cross rc={rc}")
         return mv, dist, avg.value
+
+    def me_multires_cross_v2(self, src, ref, motion_range, mode=1, dist_incl=None, slice_map=None,
+                             with_ties=False):
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = self.lib.vo_num_mbs(w, h)
+        mv = np.zeros((nmb, 2), np.int16)
+        dist = np.zeros(nmb, np.int32)
+        ties = np.zeros(nmb, np.int32)
+        avg = _L(0)
+        incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
+        sl = None if slice_map is None else np.ascontiguousarray(slice_map, dtype=np.int32)
+        rc = self.lib.vo_me_multires_cross_v2(_ptr(src), _ptr(ref), w, h, motion_range, mode, _ptr(incl),
+                                              _ptr(sl), _ptr(mv), _ptr(dist), C.byref(avg), _ptr(ties))
+        if rc:
+            raise ValueError(f"vo_me_multires_cross_v2 rc={rc}")
+        return (mv, dist, avg.value, ties) if with_ties else (mv, dist, avg.value)
 
     def me_full_intpel(self, src, ref, motion_range, metric=1):
         h, w = src.shape

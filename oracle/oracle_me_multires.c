@@ -4,6 +4,8 @@
  * Restatement of the multi-resolution H.264 estimators:
  *   MotionEstimatorH264ImplMultiresCross::Estimate
  *     (src/CodecUtils/MotionEstimatorH264ImplMultiresCross.cpp:525-1019)
+ *   MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*)
+ *     (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:537-1151)
  *
  * The reference works on extended-boundary copies of each pyramid level
  * (borders 19 / 9 / 5 samples for levels 0 / 1 / 2), addresses them through
@@ -13,9 +15,10 @@
  * and aborts (returns an error) if a read would leave a buffer, so that the
  * restatement is exact wherever the reference itself is defined.
  *
- * The half-pel window of this estimator (…MultiresCross.cpp:1281-1349) does
+ * The half-pel window of MultiresCross (…MultiresCross.cpp:1281-1349) does
  * not write the full-pel samples of its last column and row, nor scale the
- * last h column / b row (the full-search estimator does, Full.cpp:1162-1180).
+ * last h column / b row (the full-search estimator and Ver2 do, Full.cpp:1162-1180,
+ * …MultiresCrossVer2.cpp:2075-2093).
  * Those never-written samples are taken as 0, the content of the window
  * buffer when its allocation is fresh zeroed memory; the unscaled edge
  * samples are reproduced as they are.
@@ -165,7 +168,7 @@ static inline int clip255i(int x) { return x < 0 ? 0 : (x > 255 ? 255 : x); }
  * raw h over rows 2..18 x all 22 columns, raw b over all 22 rows x columns
  * 2..18, j from the raw h, then h/b scaled and G copied over columns and rows
  * 2..18 only. */
-static void mr_load_half_window(mr_window* W, const mr_ov* ref)
+static void mr_load_half_window(mr_window* W, const mr_ov* ref, int ver2)
 {
     const int rx = ref->x, ry = ref->y;
     for (int fr = 2; fr < 19; fr++)
@@ -196,6 +199,20 @@ static void mr_load_half_window(mr_window* W, const mr_ov* ref)
             W->w[qr][qc + 2] = (short)clip255i((W->w[qr][qc + 2] + 16) >> 5);
             W->w[qr][qc] = (short)mr_read(ref->b, ry + fr - 3, rx + fc - 3);
         }
+    if (ver2) {
+        /* Ver2 also completes column and row 19: scaled h and G at column 19
+         * of rows 2..18, scaled b and G at row 19 of columns 2..18, and G at
+         * (19, 19) (…MultiresCrossVer2.cpp:2075-2093) */
+        for (int fr = 2; fr < 19; fr++) {
+            W->w[4 * fr + 2][76] = (short)clip255i((W->w[4 * fr + 2][76] + 16) >> 5);
+            W->w[4 * fr][76] = (short)mr_read(ref->b, ry + fr - 3, rx + 16);
+        }
+        for (int fc = 2; fc < 19; fc++) {
+            W->w[76][4 * fc + 2] = (short)clip255i((W->w[76][4 * fc + 2] + 16) >> 5);
+            W->w[76][4 * fc] = (short)mr_read(ref->b, ry + 16, rx + fc - 3);
+        }
+        W->w[76][76] = (short)mr_read(ref->b, ry + 16, rx + 16);
+    }
 }
 
 /* LoadQuartPelWindow (…MultiresCross.cpp:1365-1389): the eight quarter
@@ -231,202 +248,354 @@ static const int CRY[4] = {0, 0, -1, 1};
 #define MRC_NOISE_FLOOR 512
 
 /* ------------------------------------------------------------------------ */
+/* The pyramid one estimate works on. */
+typedef struct {
+    int w, h, cols, nmb, rows_all, mode, l1_range, l2_range, lcl_l1_range;
+    mr_buf in0, in1, in2, r1, r2, e0, e1, e2;
+    mr_level L0, L1, L2;
+    mr_window* win;
+} mr_ctx;
+
+static void mr_ctx_free(mr_ctx* c)
+{
+    free(c->in1.mem);
+    free(c->r1.mem);
+    free(c->in2.mem);
+    free(c->r2.mem);
+    free(c->e0.mem);
+    free(c->e1.mem);
+    free(c->e2.mem);
+    free(c->win);
+}
+
+/* Level copies as Estimate builds them before its macroblock loop
+ * (…MultiresCross.cpp:539-601; …MultiresCrossVer2.cpp:552-611). */
+static int mr_ctx_init(mr_ctx* c, const short* src, const short* ref, int w, int h, int motion_range, int mode)
+{
+    memset(c, 0, sizeof(*c));
+    c->w = w;
+    c->h = h;
+    c->cols = w / 16;
+    c->nmb = c->cols * (h / 16);
+    c->rows_all = (h + 15) / 16;
+    const int w1 = w / 2, h1 = h / 2, w2 = w1 / 2, h2 = h1 / 2;
+    c->l1_range = motion_range / 8;
+    c->l2_range = c->l1_range / 2;
+    if (mode == 0) mode = (w * h > 40000) ? 2 : 1; /* SetMode(0) (…MultiresCross.cpp:501-513) */
+    c->mode = mode;
+    c->lcl_l1_range = (mode == 2) ? 2 : c->l1_range;
+    c->in0.mem = (short*)src;
+    c->in0.w = w;
+    c->in0.h = h;
+    c->in1.w = c->r1.w = w1;
+    c->in1.h = c->r1.h = h1;
+    c->in2.w = c->r2.w = w2;
+    c->in2.h = c->r2.h = h2;
+    c->in1.mem = (short*)malloc(sizeof(short) * (size_t)w1 * h1);
+    c->r1.mem = (short*)malloc(sizeof(short) * (size_t)w1 * h1);
+    c->in2.mem = (short*)malloc(sizeof(short) * (size_t)w2 * h2 + 2);
+    c->r2.mem = (short*)malloc(sizeof(short) * (size_t)w2 * h2 + 2);
+    c->win = (mr_window*)calloc(1, sizeof(mr_window));
+    if (!c->in1.mem || !c->r1.mem || !c->in2.mem || !c->r2.mem || !c->win) return -2;
+    vo_half(ref, w, h, c->r1.mem);
+    vo_half(src, w, h, c->in1.mem);
+    if (mode == 2) {
+        vo_half(c->r1.mem, w1, h1, c->r2.mem);
+        vo_half(c->in1.mem, w1, h1, c->in2.mem);
+    }
+    if (mr_buf_ext(&c->e0, ref, w, h, 19) || mr_buf_ext(&c->e1, c->r1.mem, w1, h1, 9) ||
+        (mode == 2 && mr_buf_ext(&c->e2, c->r2.mem, w2, h2, 5)))
+        return -2;
+    c->L0 = (mr_level){16, w, h, motion_range / 4};
+    c->L1 = (mr_level){8, w1, h1, c->l1_range};
+    c->L2 = (mr_level){4, w2, h2, c->l2_range};
+    return 0;
+}
+
+/* Tie rule of the integer stages: an equal distortion replaces the current
+ * best (offset (rmx, rmy) from the centre (mx, my)) unless the candidate at
+ * (j, i) is farther from the reference point (px, py): MultiresCross measures
+ * from (0, 0) (…MultiresCross.cpp:741-746, 794, 857), MultiresCrossVer2 from
+ * the rounded prediction of the level (…MultiresCrossVer2.cpp:778-786,
+ * 834-842, 906-914). */
+static inline int mr_farther(int mx, int my, int rmx, int rmy, int j, int i, int px, int py)
+{
+    const int cx = mx + rmx - px, cy = my + rmy - py, nx = mx + j - px, ny = my + i - py;
+    return (cy * cy + cx * cx) - (ny * ny + nx * nx) < 0;
+}
+
+/* Result of the search of one macroblock. */
+typedef struct {
+    int zero_d, min_d, mvx, mvy;
+    int tie; /* an integer stage met a candidate equal to its running minimum */
+} mr_result;
+
+/* The search of macroblock (mbr, mbc) of both estimators, from the zero
+ * vector to the quarter-pel winner (…MultiresCross.cpp:612-941;
+ * …MultiresCrossVer2.cpp:643-992).  pred == NULL: MultiresCross's tie rules;
+ * else Ver2's, pred = {level-2 x, y, level-1 x, y, level-0 rounded x, y}. */
+static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result* out)
+{
+    const int m = 16 * mbr, n = 16 * mbc, p = 8 * mbr, q = 8 * mbc, kk = 4 * mbr, ll = 4 * mbc;
+    mr_ov oin0 = {&c->in0, 16, 16, 0, 0, 0, 0}, oin1 = {&c->in1, 8, 8, 0, 0, 0, 0}, oin2 = {&c->in2, 4, 4, 0, 0, 0, 0};
+    mr_ov oe0 = {&c->e0, 16, 16, 0, 0, 19, 19}, oe1 = {&c->e1, 8, 8, 0, 0, 9, 9}, oe2 = {&c->e2, 4, 4, 0, 0, 5, 5};
+    int mx = 0, my = 0, rmx = 0, rmy = 0, hmx = 0, hmy = 0, qmx, qmy, xl, xr, yu, yd, tie = 0;
+    short blk[256];
+    ov_origin(&oin0, n, m);
+    ov_origin(&oe0, n, m);
+    const int zero_d = ov_tsd(&oin0, &oe0, 16);
+    int min_d;
+
+    if (c->mode == 2) { /* level 2 cross search (…MultiresCross.cpp:639-697) */
+        ov_origin(&oin2, ll, kk);
+        ov_origin(&oe2, ll, kk);
+        int min2 = ov_tsd(&oin2, &oe2, 4);
+        mr_range(&c->L2, ll, kk, 0, 0, c->l2_range - 1, &xl, &xr, &yu, &yd);
+        for (int s = c->l2_range / 2; s > 0; s /= 2) {
+            rmx = rmy = 0;
+            for (int k = 0; k < 4; k++) {
+                int i = s * CRY[k], j = s * CRX[k];
+                if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+                ov_origin(&oe2, j + ll + mx, i + kk + my);
+                int d = ov_tsd4_lt(&oin2, &oe2, min2);
+                if (d > min2) continue;
+                if (d == min2) {
+                    tie = 1;
+                    /* MultiresCross compares the centre with the offset (…:673-679) */
+                    if (pred ? mr_farther(mx, my, rmx, rmy, j, i, pred[0], pred[1])
+                             : (my * my + mx * mx) - (i * i + j * j) < 0)
+                        continue;
+                }
+                min2 = d;
+                rmx = j;
+                rmy = i;
+            }
+            mx += rmx;
+            my += rmy;
+        }
+        mx <<= 1;
+        my <<= 1;
+    }
+
+    /* level 1 (…MultiresCross.cpp:699-816) */
+    const int p1x = pred ? pred[2] : 0, p1y = pred ? pred[3] : 0;
+    ov_origin(&oin1, q, p);
+    ov_origin(&oe1, mx + q, my + p);
+    int min1 = ov_tsd(&oin1, &oe1, 8);
+    rmx = rmy = 0;
+    if (c->mode == 2) {
+        mr_range(&c->L1, q, p, mx, my, c->lcl_l1_range, &xl, &xr, &yu, &yd);
+        for (int i = yu; i <= yd; i++)
+            for (int j = xl; j <= xr; j++) {
+                if (!(i || j)) continue;
+                ov_origin(&oe1, j + mx + q, i + my + p);
+                int d = ov_tsd_partial_lt(&oin1, &oe1, 8, min1);
+                if (d > min1) continue;
+                if (d == min1) {
+                    tie = 1;
+                    if (mr_farther(mx, my, rmx, rmy, j, i, p1x, p1y)) continue;
+                }
+                min1 = d;
+                rmx = j;
+                rmy = i;
+            }
+    } else {
+        for (int s = c->l1_range / 2; s > 0; s /= 2) {
+            mr_range(&c->L1, q, p, mx, my, c->lcl_l1_range - 1, &xl, &xr, &yu, &yd);
+            rmx = rmy = 0;
+            for (int k = 0; k < 4; k++) {
+                int i = s * CRY[k], j = s * CRX[k];
+                if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+                ov_origin(&oe1, j + mx + q, i + my + p);
+                int d = ov_tsd_partial_lt(&oin1, &oe1, 8, min1);
+                if (d > min1) continue;
+                if (d == min1) {
+                    tie = 1;
+                    if (mr_farther(mx, my, rmx, rmy, j, i, p1x, p1y)) continue;
+                }
+                min1 = d;
+                rmx = j;
+                rmy = i;
+            }
+            mx += rmx;
+            my += rmy;
+        }
+    }
+    /* the last level-1 refinement is added once more here in the cross mode
+     * (…MultiresCross.cpp:815-816) */
+    mx = (mx + rmx) * 2;
+    my = (my + rmy) * 2;
+
+    /* level 0 +-2 refinement (…MultiresCross.cpp:819-873) */
+    const int p0x = pred ? pred[4] : 0, p0y = pred ? pred[5] : 0;
+    ov_origin(&oe0, n + mx, m + my);
+    min_d = ov_tsd(&oin0, &oe0, 16);
+    rmx = rmy = 0;
+    mr_range(&c->L0, n, m, mx, my, 2, &xl, &xr, &yu, &yd);
+    for (int i = yu; i <= yd; i++)
+        for (int j = xl; j <= xr; j++) {
+            if (!(i || j)) continue;
+            ov_origin(&oe0, n + mx + j, m + my + i);
+            int d = ov_tsd_partial_lt(&oin0, &oe0, 16, min_d);
+            if (d > min_d) continue;
+            if (d == min_d) {
+                tie = 1;
+                if (mr_farther(mx, my, rmx, rmy, j, i, p0x, p0y)) continue;
+            }
+            min_d = d;
+            rmx = j;
+            rmy = i;
+        }
+    mx += rmx;
+    my += rmy;
+    int mvx = mx << 2, mvy = my << 2;
+
+    /* half then quarter pel (…MultiresCross.cpp:875-941), strict improvements */
+    ov_origin(&oe0, n + mx, m + my);
+    mr_load_half_window(c->win, &oe0, pred != NULL);
+    for (int k = 0; k < 8; k++) {
+        int qx = 2 * SUBX[k], qy = 2 * SUBY[k];
+        mr_window_read(c->win, qx, qy, blk);
+        int d = blk_tsd16_partial_lt(&oin0, blk, min_d);
+        if (d < min_d) { min_d = d; hmx = qx; hmy = qy; }
+    }
+    qmx = hmx;
+    qmy = hmy;
+    mr_load_quarter_window(c->win, hmx, hmy);
+    for (int k = 0; k < 8; k++) {
+        int qx = hmx + SUBX[k], qy = hmy + SUBY[k];
+        mr_window_read(c->win, qx, qy, blk);
+        int d = blk_tsd16_partial_lt(&oin0, blk, min_d);
+        if (d < min_d) { min_d = d; qmx = qx; qmy = qy; }
+    }
+    out->zero_d = zero_d;
+    out->min_d = min_d;
+    out->mvx = mvx + qmx;
+    out->mvy = mvy + qmy;
+    out->tie = tie;
+}
+
 int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
                          const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist)
 {
     if (!src || !ref || !mv_out || w < 16 || h < 16 || (w % 16) != 0) return -1;
     g_mr_fault = 0;
-    const int cols = w / 16, nmb = cols * (h / 16), rows_all = (h + 15) / 16;
-    const int w1 = w / 2, h1 = h / 2, w2 = w1 / 2, h2 = h1 / 2;
-    const int l1_range = motion_range / 8, l2_range = l1_range / 2;
-    if (mode == 0) mode = (w * h > 40000) ? 2 : 1; /* SetMode(0) (…:501-513) */
-    const int lcl_l1_range = (mode == 2) ? 2 : l1_range;
-
-    mr_buf in0 = {(short*)src, w, h}, in1 = {0}, in2 = {0}, r1 = {0}, r2 = {0}, e0 = {0}, e1 = {0}, e2 = {0};
-    in1.w = r1.w = w1; in1.h = r1.h = h1;
-    in2.w = r2.w = w2; in2.h = r2.h = h2;
-    in1.mem = (short*)malloc(sizeof(short) * (size_t)w1 * h1);
-    r1.mem = (short*)malloc(sizeof(short) * (size_t)w1 * h1);
-    in2.mem = (short*)malloc(sizeof(short) * (size_t)w2 * h2 + 2);
-    r2.mem = (short*)malloc(sizeof(short) * (size_t)w2 * h2 + 2);
-    mr_window* win = (mr_window*)calloc(1, sizeof(mr_window));
-    int rc = 0;
-    if (!in1.mem || !r1.mem || !in2.mem || !r2.mem || !win) { rc = -2; goto done; }
-    vo_half(ref, w, h, r1.mem);
-    vo_half(src, w, h, in1.mem);
-    if (mode == 2) {
-        vo_half(r1.mem, w1, h1, r2.mem);
-        vo_half(in1.mem, w1, h1, in2.mem);
-    }
-    if (mr_buf_ext(&e0, ref, w, h, 19) || mr_buf_ext(&e1, r1.mem, w1, h1, 9) ||
-        (mode == 2 && mr_buf_ext(&e2, r2.mem, w2, h2, 5))) { rc = -2; goto done; }
-
-    {
-        mr_level L0 = {16, w, h, motion_range / 4}, L1 = {8, w1, h1, l1_range}, L2 = {4, w2, h2, l2_range};
-        mr_ov oin0 = {&in0, 16, 16, 0, 0, 0, 0}, oin1 = {&in1, 8, 8, 0, 0, 0, 0}, oin2 = {&in2, 4, 4, 0, 0, 0, 0};
-        mr_ov oe0 = {&e0, 16, 16, 0, 0, 19, 19}, oe1 = {&e1, 8, 8, 0, 0, 9, 9}, oe2 = {&e2, 4, 4, 0, 0, 5, 5};
+    mr_ctx c;
+    int rc = mr_ctx_init(&c, src, ref, w, h, motion_range, mode);
+    if (rc == 0) {
         long total = 0;
         int included = 0;
-        short blk[256];
-        for (int mbr = 0; mbr < rows_all; mbr++)
-            for (int mbc = 0; mbc < cols; mbc++) {
-                const int m = 16 * mbr, n = 16 * mbc, p = 8 * mbr, q = 8 * mbc, kk = 4 * mbr, ll = 4 * mbc;
-                const int vec_pos = mbr * cols + mbc < nmb ? mbr * cols + mbc : nmb;
-                int mx = 0, my = 0, rmx = 0, rmy = 0, hmx = 0, hmy = 0, qmx, qmy;
-                int xl, xr, yu, yd;
-                ov_origin(&oin0, n, m);
-                ov_origin(&oe0, n, m);
-                int zero_d = ov_tsd(&oin0, &oe0, 16);
-                int min_d = zero_d;
-
-                if (mode == 2) { /* level 2 cross search (…:639-697) */
-                    ov_origin(&oin2, ll, kk);
-                    ov_origin(&oe2, ll, kk);
-                    int min2 = ov_tsd(&oin2, &oe2, 4);
-                    for (int s = l2_range / 2; s > 0; s /= 2) {
-                        mr_range(&L2, ll, kk, 0, 0, l2_range - 1, &xl, &xr, &yu, &yd);
-                        rmx = rmy = 0;
-                        for (int c = 0; c < 4; c++) {
-                            int i = s * CRY[c], j = s * CRX[c];
-                            if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
-                            ov_origin(&oe2, j + ll + mx, i + kk + my);
-                            int d = ov_tsd4_lt(&oin2, &oe2, min2);
-                            if (d > min2) continue;
-                            if (d == min2 && (my * my + mx * mx) - (i * i + j * j) < 0) continue;
-                            min2 = d;
-                            rmx = j;
-                            rmy = i;
-                        }
-                        mx += rmx;
-                        my += rmy;
-                    }
-                    mx <<= 1;
-                    my <<= 1;
-                }
-
-                /* level 1 (…:699-816) */
-                ov_origin(&oin1, q, p);
-                ov_origin(&oe1, mx + q, my + p);
-                int min1 = ov_tsd(&oin1, &oe1, 8);
-                rmx = rmy = 0;
-                if (mode == 2) {
-                    mr_range(&L1, q, p, mx, my, lcl_l1_range, &xl, &xr, &yu, &yd);
-                    for (int i = yu; i <= yd; i++)
-                        for (int j = xl; j <= xr; j++) {
-                            if (!(i || j)) continue;
-                            ov_origin(&oe1, j + mx + q, i + my + p);
-                            int d = ov_tsd_partial_lt(&oin1, &oe1, 8, min1);
-                            if (d > min1) continue;
-                            if (d == min1 && ((my + rmy) * (my + rmy) + (mx + rmx) * (mx + rmx)) -
-                                                     ((my + i) * (my + i) + (mx + j) * (mx + j)) < 0)
-                                continue;
-                            min1 = d;
-                            rmx = j;
-                            rmy = i;
-                        }
-                } else {
-                    for (int s = l1_range / 2; s > 0; s /= 2) {
-                        mr_range(&L1, q, p, mx, my, lcl_l1_range - 1, &xl, &xr, &yu, &yd);
-                        rmx = rmy = 0;
-                        for (int c = 0; c < 4; c++) {
-                            int i = s * CRY[c], j = s * CRX[c];
-                            if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
-                            ov_origin(&oe1, j + mx + q, i + my + p);
-                            int d = ov_tsd_partial_lt(&oin1, &oe1, 8, min1);
-                            if (d > min1) continue;
-                            if (d == min1 && ((my + rmy) * (my + rmy) + (mx + rmx) * (mx + rmx)) -
-                                                     ((my + i) * (my + i) + (mx + j) * (mx + j)) < 0)
-                                continue;
-                            min1 = d;
-                            rmx = j;
-                            rmy = i;
-                        }
-                        mx += rmx;
-                        my += rmy;
-                    }
-                }
-                /* the last level-1 refinement is added once more here in the
-                 * cross mode (…:815-816) */
-                mx = (mx + rmx) * 2;
-                my = (my + rmy) * 2;
-
-                /* level 0 +-2 refinement (…:819-873) */
-                ov_origin(&oe0, n + mx, m + my);
-                min_d = ov_tsd(&oin0, &oe0, 16);
-                rmx = rmy = 0;
-                mr_range(&L0, n, m, mx, my, 2, &xl, &xr, &yu, &yd);
-                for (int i = yu; i <= yd; i++)
-                    for (int j = xl; j <= xr; j++) {
-                        if (!(i || j)) continue;
-                        ov_origin(&oe0, n + mx + j, m + my + i);
-                        int d = ov_tsd_partial_lt(&oin0, &oe0, 16, min_d);
-                        if (d > min_d) continue;
-                        if (d == min_d && ((my + rmy) * (my + rmy) + (mx + rmx) * (mx + rmx)) -
-                                                  ((my + i) * (my + i) + (mx + j) * (mx + j)) < 0)
-                            continue;
-                        min_d = d;
-                        rmx = j;
-                        rmy = i;
-                    }
-                mx += rmx;
-                my += rmy;
-                int mvx = mx << 2, mvy = my << 2;
-
-                /* half then quarter pel (…:875-941) */
-                ov_origin(&oe0, n + mx, m + my);
-                mr_load_half_window(win, &oe0);
-                for (int c = 0; c < 8; c++) {
-                    int qx = 2 * SUBX[c], qy = 2 * SUBY[c];
-                    mr_window_read(win, qx, qy, blk);
-                    int d = blk_tsd16_partial_lt(&oin0, blk, min_d);
-                    if (d < min_d) { min_d = d; hmx = qx; hmy = qy; }
-                }
-                qmx = hmx;
-                qmy = hmy;
-                mr_load_quarter_window(win, hmx, hmy);
-                for (int c = 0; c < 8; c++) {
-                    int qx = hmx + SUBX[c], qy = hmy + SUBY[c];
-                    mr_window_read(win, qx, qy, blk);
-                    int d = blk_tsd16_partial_lt(&oin0, blk, min_d);
-                    if (d < min_d) { min_d = d; qmx = qx; qmy = qy; }
-                }
-                mvx += qmx;
-                mvy += qmy;
-
-                /* accept-or-zero heuristic (…:943-999) */
-                int weight = 0, diff0 = zero_d - min_d, mag = mvx * mvx + mvy * mvy;
+        for (int mbr = 0; mbr < c.rows_all; mbr++)
+            for (int mbc = 0; mbc < c.cols; mbc++) {
+                const int vec_pos = mbr * c.cols + mbc < c.nmb ? mbr * c.cols + mbc : c.nmb;
+                mr_result r;
+                mr_search_mb(&c, mbr, mbc, NULL, &r);
+                int mvx = r.mvx, mvy = r.mvy;
+                /* accept-or-zero heuristic (…MultiresCross.cpp:943-999) */
+                int weight = 0, diff0 = r.zero_d - r.min_d, mag = mvx * mvx + mvy * mvy;
                 if (diff0 < mag) weight++;
-                if (zero_d < MRC_NOISE_FLOOR) weight++;
-                if (diff0 * 10 < min_d) weight++;
-                int do_it = dist_incl ? (vec_pos < nmb ? dist_incl[vec_pos] != 0 : 0) : 1;
+                if (r.zero_d < MRC_NOISE_FLOOR) weight++;
+                if (diff0 * 10 < r.min_d) weight++;
+                int do_it = dist_incl ? (vec_pos < c.nmb ? dist_incl[vec_pos] != 0 : 0) : 1;
                 int chosen;
-                if (min_d < zero_d && weight < 2) {
-                    chosen = min_d;
+                if (r.min_d < r.zero_d && weight < 2) {
+                    chosen = r.min_d;
                 } else {
                     mvx = mvy = 0;
-                    chosen = zero_d;
+                    chosen = r.zero_d;
                 }
                 if (do_it) {
                     included++;
                     total += chosen;
                 }
-                if (vec_pos < nmb) {
+                if (vec_pos < c.nmb) {
                     mv_out[2 * vec_pos] = (short)mvx;
                     mv_out[2 * vec_pos + 1] = (short)mvy;
                     if (mb_dist) mb_dist[vec_pos] = chosen;
                 }
             }
         if (avg_dist) *avg_dist = included ? total / included : 0;
+        if (g_mr_fault) rc = -3;
     }
-    if (g_mr_fault) rc = -3;
-done:
-    free(in1.mem);
-    free(r1.mem);
-    free(in2.mem);
-    free(r2.mem);
-    free(e0.mem);
-    free(e1.mem);
-    free(e2.mem);
-    free(win);
+    mr_ctx_free(&c);
+    return rc;
+}
+
+/* MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*)
+ * (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:537-1151): the
+ * MultiresCross search with ties resolved towards the rounded median
+ * prediction of each level (…:627-642), then the pred-vector check and the
+ * Lagrangian choice among {search winner, prediction, zero} with lambda 0.9
+ * (…:1008-1064; GetBestVector at level 2 weighs every item with lambda,
+ * MultiresCrossVer2.h:168-197).  Only full macroblock rows are estimated: the
+ * reference drops the partial bottom row's vectors (…:1137) and asks the
+ * predictor for an index past its array for it.  tie_out (nullable): per MB,
+ * 1 if an integer stage met an equal distortion (the search then depends on
+ * the prediction). */
+int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                            const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist,
+                            long* avg_dist, int* tie_out)
+{
+    if (!src || !ref || !mv_out || w < 16 || h < 16 || (w % 16) != 0) return -1;
+    g_mr_fault = 0;
+    mr_ctx c;
+    vo_pred_state ps;
+    const int rows = h / 16;
+    int rc = mr_ctx_init(&c, src, ref, w, h, motion_range, mode);
+    if (rc == 0 && vo_pred_init(&ps, c.cols, rows, slice) != 0) {
+        vo_pred_free(&ps);
+        rc = -2;
+    }
+    if (rc == 0) {
+        const int es = w + 38;
+        long total = 0;
+        int included = 0;
+        for (int k = 0; k < c.nmb; k++) {
+            const int mbr = k / c.cols, mbc = k % c.cols, n = 16 * mbc, m = 16 * mbr;
+            int px, py;
+            vo_pred_get(&ps, k, &px, &py);
+            const int pxq = px % 4, pyq = py % 4;
+            int px0 = px / 4, py0 = py / 4;
+            const int px0r = px < 0 ? (px - 2) / 4 : (px + 2) / 4, py0r = py < 0 ? (py - 2) / 4 : (py + 2) / 4;
+            const int pl[6] = {px0r / 2 / 2, py0r / 2 / 2, px0r / 2, py0r / 2, px0r, py0r};
+            mr_result r;
+            mr_search_mb(&c, mbr, mbc, pl, &r);
+            if (tie_out) tie_out[k] = r.tie;
+
+            /* pred-vector check, clamped to one macroblock outside (…:1008-1045) */
+            if (px0 + n > w) px0 = 16;
+            if (px0 + n < -16) px0 = -16;
+            if (py0 + m > h) py0 = 16;
+            if (py0 + m < -16) py0 = -16;
+            px = 4 * px0 + pxq;
+            py = 4 * py0 + pyq;
+            const int pox = vo_clamp_origin(px0 + n + 19, es, 16), poy = vo_clamp_origin(py0 + m + 19, h + 38, 16);
+            const short* in = src + (size_t)m * w + n;
+            int pd;
+            if (pxq || pyq) {
+                short blk[256];
+                vo_qread16_ext(c.e0.mem, es, pox, poy, pxq, pyq, blk);
+                pd = vo_tsd16(in, w, blk, 16);
+            } else {
+                pd = vo_tsd16(in, w, c.e0.mem + (size_t)poy * es + pox, es);
+            }
+            /* Fifo after pushing zero, pred, best (…:1047-1050) */
+            int xs[5] = {r.mvx, px, 0, 0, 0}, ys[5] = {r.mvy, py, 0, 0, 0};
+            int ds[5] = {r.min_d, pd, r.zero_d, r.zero_d, r.zero_d};
+            const int pos = vo_best_vector5(xs, ys, ds, 0.9, 256.0, px, py);
+            if (dist_incl && dist_incl[k]) {
+                included++;
+                total += ds[pos];
+            }
+            if (mb_dist) mb_dist[k] = ds[pos];
+            mv_out[2 * k] = (short)xs[pos];
+            mv_out[2 * k + 1] = (short)ys[pos];
+            vo_pred_set(&ps, k, xs[pos], ys[pos]);
+        }
+        if (avg_dist) *avg_dist = included ? total / included : 0;
+        vo_pred_free(&ps);
+        if (g_mr_fault) rc = -3;
+    }
+    mr_ctx_free(&c);
     return rc;
 }

@@ -76,6 +76,16 @@ int vo_me_full_intpel(const short* src, const short* ref, int w, int h, int moti
 int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
                          const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist);
 
+/* MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*)
+ * (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:537-1151): the
+ * MultiresCross search with ties towards the rounded median prediction of
+ * each level, the pred-vector check and GetBestVector (lambda 0.9).  Full
+ * macroblock rows only.  slice: NULL or one slice id per MB.  tie_out: NULL
+ * or per MB 1 when an integer stage met an equal distortion. */
+int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                            const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist,
+                            long* avg_dist, int* tie_out);
+
 /* OverlayMem2Dv2::QuarterRead (src/ImageUtils/OverlayMem2Dv2.cpp:704-1052) of
  * a 16x16 block whose full-pel origin is (x, y) in a frame extended by edge
  * replication, at quarter offsets (qx, qy) in -3..3. */

@@ -12,13 +12,17 @@ inputs and stores inputs and outputs:
                   avgDistortion, modes 0/1/2, with and without
                   pDistortionIncluded (the partial bottom row counts in the
                   average when it is NULL)
+* me_mrc2.npz     MotionEstimatorH264ImplMultiresCrossVer2 vectors and
+                  avgDistortion, modes 0/1/2, with and without
+                  pDistortionIncluded (pan and integer-shift content)
 * transform.npz   FastForward4x4ITImpl1 / Impl2 / On16x16 levels and
                   FastInverse4x4ITImpl1 / On16x16 reconstructions over QP 0..51,
                   intra and inter, modes 0/1/2, a custom SetScale, and
                   FastForward4x4ITImpl2::QuantiseValue
 * colour.npz      the three RGB24->YUV420 converters, flip and chroma offsets
 
-Usage: python tests/golden/make_golden.py   (needs the reference tree)
+Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
+names: me_full me_mrc me_mrc2 transform colour, default all)
 """
 from __future__ import annotations
 
@@ -97,6 +101,35 @@ def mrc_fixtures(ref: oracle.Reference) -> dict:
     return out
 
 
+MRC2_CASES = [  # (name, w, h, motion_range, seed, generator)
+    ("qcif_r64", 176, 144, 64, 41, "pan"),
+    ("cif_r128", 352, 288, 128, 42, "pan"),
+    ("partial_r128", 352, 280, 128, 43, "pan"),
+    ("small_r32", 64, 48, 32, 44, "pan"),
+    ("shift_r128", 352, 288, 128, 45, "shift"),
+]
+
+
+def mrc2_fixtures(ref: oracle.Reference) -> dict:
+    out = {}
+    for name, w, h, mr, seed, gen in MRC2_CASES:
+        fr = (synth.shift_sequence if gen == "shift" else synth.pan_sequence)(seed, w, h, 2)
+        src, rf = fr[1], fr[0]
+        nmb = (w // 16) * (h // 16)
+        incl = (np.arange(nmb) % 3 != 0).astype(np.uint8)
+        out[f"{name}_src"] = src.astype(np.uint8)
+        out[f"{name}_ref"] = rf.astype(np.uint8)
+        out[f"{name}_meta"] = np.array([w, h, mr], np.int32)
+        out[f"{name}_incl"] = incl
+        for mode in (0, 1, 2):
+            mv, avg = ref.me("multires_cross_v2", src, rf, mr, mode=mode)
+            mvi, avgi = ref.me("multires_cross_v2", src, rf, mr, mode=mode, dist_incl=incl)
+            assert np.array_equal(mv, mvi) and avg == 0
+            out[f"{name}_m{mode}_mv"] = mv
+            out[f"{name}_m{mode}_avg"] = np.array([avgi], np.int64)
+    return out
+
+
 def transform_fixtures(ref: oracle.Reference) -> dict:
     lap = synth.residual_blocks(11, 16 * 64)
     full = ((synth.splitmix64(12, 16 * 16) % np.uint64(65536)).astype(np.int64) - 32768).astype(np.int16)
@@ -145,11 +178,12 @@ def colour_fixtures(ref: oracle.Reference) -> dict:
 def main() -> None:
     oracle.build(with_reference=True)
     ref = oracle.Reference()
-    np.savez_compressed(os.path.join(HERE, "me_full.npz"), **me_fixtures(ref))
-    np.savez_compressed(os.path.join(HERE, "me_mrc.npz"), **mrc_fixtures(ref))
-    np.savez_compressed(os.path.join(HERE, "transform.npz"), **transform_fixtures(ref))
-    np.savez_compressed(os.path.join(HERE, "colour.npz"), **colour_fixtures(ref))
-    print("golden fixtures written to", HERE)
+    makers = {"me_full": me_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
+              "transform": transform_fixtures, "colour": colour_fixtures}
+    names = sys.argv[1:] or list(makers)
+    for name in names:
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **makers[name](ref))
+    print("golden fixtures", ", ".join(names), "written to", HERE)
 
 
 if __name__ == "__main__":

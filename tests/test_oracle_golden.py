@@ -101,3 +101,69 @@ def test_me_full_flat_content_ties(orc):
     mv_r, _ = ref_lib.me("full", b, a, 128)
     mv_o, _, _ = orc.me_full(b, a, 128)
     np.testing.assert_array_equal(mv_o, mv_r)
+
+
+MRC_CASES = ["qcif_r64", "cif_r128", "partial_r128", "small_r32"]
+
+
+@pytest.mark.parametrize("case", MRC_CASES)
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_me_multires_cross_matches_reference(orc, golden, case, mode):
+    g = golden("me_mrc.npz")
+    w, h, mr = (int(v) for v in g[f"{case}_meta"])
+    src = g[f"{case}_src"].astype(np.int16)
+    ref = g[f"{case}_ref"].astype(np.int16)
+    mv, _, avg = orc.me_multires_cross(src, ref, mr, mode=mode)
+    np.testing.assert_array_equal(mv, g[f"{case}_m{mode}_mv"])
+    assert avg == int(g[f"{case}_m{mode}_avg"][0])
+    mvi, _, avgi = orc.me_multires_cross(src, ref, mr, mode=mode, dist_incl=np.ones((w // 16) * (h // 16), np.uint8))
+    np.testing.assert_array_equal(mvi, mv)
+    assert avgi == int(g[f"{case}_m{mode}_avg"][1])
+
+
+MRC2_CASES = ["qcif_r64", "cif_r128", "partial_r128", "small_r32", "shift_r128"]
+
+
+@pytest.mark.parametrize("case", MRC2_CASES)
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_me_multires_cross_v2_matches_reference(orc, golden, case, mode):
+    g = golden("me_mrc2.npz")
+    w, h, mr = (int(v) for v in g[f"{case}_meta"])
+    src = g[f"{case}_src"].astype(np.int16)
+    ref = g[f"{case}_ref"].astype(np.int16)
+    mv, _, avg = orc.me_multires_cross_v2(src, ref, mr, mode=mode)
+    np.testing.assert_array_equal(mv, g[f"{case}_m{mode}_mv"])
+    assert avg == 0  # no pDistortionIncluded: nothing is counted
+    mvi, _, avgi = orc.me_multires_cross_v2(src, ref, mr, mode=mode, dist_incl=g[f"{case}_incl"])
+    np.testing.assert_array_equal(mvi, mv)
+    assert avgi == int(g[f"{case}_m{mode}_avg"][0])
+
+
+@ref_available
+@pytest.mark.parametrize("seed,w,h,mr,mode", [(51, 176, 144, 128, 0), (52, 352, 288, 128, 1), (53, 208, 120, 96, 2),
+                                              (54, 96, 64, 64, 2), (55, 640, 360, 128, 0)])
+def test_me_multires_cross_v2_against_compiled_reference(orc, seed, w, h, mr, mode):
+    ref_lib = oracle_mod.Reference()
+    fr = synth.pan_sequence(seed, w, h, 2)
+    incl = (synth.splitmix64(seed, (w // 16) * (h // 16)) & np.uint64(1)).astype(np.uint8)
+    mv_r, avg_r = ref_lib.me("multires_cross_v2", fr[1], fr[0], mr, mode=mode, dist_incl=incl)
+    mv_o, _, avg_o = orc.me_multires_cross_v2(fr[1], fr[0], mr, mode=mode, dist_incl=incl)
+    np.testing.assert_array_equal(mv_o, mv_r)
+    assert avg_o == avg_r
+
+
+@ref_available
+def test_me_multires_cross_v2_flat_content_ties(orc):
+    """Periodic content with flat patches: many exact ties, decided by the
+    distance to each level's rounded prediction."""
+    ref_lib = oracle_mod.Reference()
+    w, h = 128, 96
+    yy, xx = np.mgrid[0:h, 0:w]
+    a = ((xx // 8 + yy // 8) % 2 * 40 + 100).astype(np.int16)
+    b = np.roll(a, (3, 5), axis=(0, 1))
+    b[20:40, 30:60] = 128
+    for mode in (1, 2):
+        mv_r, _ = ref_lib.me("multires_cross_v2", b, a, 128, mode=mode)
+        mv_o, _, _, ties = orc.me_multires_cross_v2(b, a, 128, mode=mode, with_ties=True)
+        np.testing.assert_array_equal(mv_o, mv_r)
+        assert ties.sum() > 0
