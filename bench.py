@@ -319,12 +319,20 @@ def run_serving(args, vpp, torch, ctx, bases):
     }
 
 
-def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with_cpu):
-    """MotionEstimatorH264ImplMultiresCross (mode 0 -> 2 at 1080p) on the same
-    1080p sequence: device-resident MB/s over the frame rotation, and the
-    oracle port on all host threads as its CPU baseline."""
+MULTIRES = {  # kind -> (class name, oracle method)
+    "multires_cross": ("MotionEstimatorH264ImplMultiresCross", "me_multires_cross"),
+    "multires_cross_v2": ("MotionEstimatorH264ImplMultiresCrossVer2", "me_multires_cross_v2"),
+}
+
+
+def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with_cpu, kind="multires_cross"):
+    """A multi-resolution estimator (mode 0 -> 2 at 1080p) on the same 1080p
+    sequence: device-resident MB/s over the frame rotation, and the oracle
+    port on all host threads as its CPU baseline."""
+    cls, ofn = MULTIRES[kind]
+    code = _lib.ME_MULTIRES_CROSS if kind == "multires_cross" else _lib.ME_MULTIRES_CROSS_V2
     h = C.c_void_p()
-    _lib.check(L.vppgpu_me_create(ctx.handle, _lib.ME_MULTIRES_CROSS, W, H, MOTION_RANGE, C.byref(h)), "vppgpu_me_create")
+    _lib.check(L.vppgpu_me_create(ctx.handle, code, W, H, MOTION_RANGE, C.byref(h)), "vppgpu_me_create")
     _lib.check(L.vppgpu_me_set_mode(h, 0), "vppgpu_me_set_mode")
     mode = C.c_int()
     L.vppgpu_me_get_mode(h, C.byref(mode))
@@ -348,22 +356,38 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
+    out = {"value": NMB / (ms * 1e-3), "unit": UNIT, "ms_per_frame": ms, "mode": mode.value,
+           "workload": f"{cls} plain per-frame, {W}x{H}, motionRange {MOTION_RANGE}"}
+    if kind == "multires_cross_v2":
+        # per-frame device time and how each frame's predictions were decided
+        per, exact = [], 0
+        for t in range(NFRAMES - 1):
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            step(t)
+            f1.record(stream)
+            sw = C.c_int()
+            L.vppgpu_me_last_sweeps(h, C.byref(sw))
+            exact += sw.value >= 1000
+            per.append(f0.elapsed_time(f1))
+        per.sort()
+        out["latency_ms"] = {"p50": per[len(per) // 2], "p99": per[min(len(per) - 1, int(0.99 * len(per)))],
+                             "max": per[-1], "unit": "device ms per frame"}
+        out["frames_needing_wavefront"] = f"{exact}/{NFRAMES - 1}"
     step(0)
     torch.cuda.synchronize()
-    out = {"value": NMB / (ms * 1e-3), "unit": UNIT, "ms_per_frame": ms, "mode": mode.value,
-           "workload": f"MotionEstimatorH264ImplMultiresCross plain per-frame, {W}x{H}, motionRange {MOTION_RANGE}"}
     if with_cpu:
         from concurrent.futures import ThreadPoolExecutor
         from oracle.oracle import Oracle
         orc = Oracle()
-        mv_o, _, _ = orc.me_multires_cross(frames[1], frames[0], MOTION_RANGE, mode=mode.value)
+        mv_o = getattr(orc, ofn)(frames[1], frames[0], MOTION_RANGE, mode=mode.value)[0]
         out["parity_first_frame"] = bool(np.array_equal(d_mv.cpu().numpy(), mv_o))
         nth = os.cpu_count() or 1
         npairs, t0 = 0, time.perf_counter()
         with ThreadPoolExecutor(nth) as ex:  # ctypes calls release the GIL: one estimate per thread
             while time.perf_counter() - t0 < args.cpu_seconds:
-                list(ex.map(lambda i: orc.me_multires_cross(frames[i + 1], frames[i], MOTION_RANGE,
-                                                            mode=mode.value), range(NFRAMES - 1)))
+                list(ex.map(lambda i: getattr(orc, ofn)(frames[i + 1], frames[i], MOTION_RANGE, mode=mode.value),
+                            range(NFRAMES - 1)))
                 npairs += NFRAMES - 1
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": npairs * NMB / dt, "unit": UNIT, "cores": nth, "kind": "port",
@@ -632,6 +656,8 @@ def main():
                                                          bases)
         serving = None if args.no_serve else run_serving(args, vpp, torch, ctx, bases)
         mrc = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu)
+        mrc2 = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
+                                  kind="multires_cross_v2")
         pk, pk_kind = peaks()
         hbm_rows = run_hbm_paths(torch, _lib, L, ctx, stream, f"cuda:{local}", pk)
         line = {
@@ -656,7 +682,7 @@ def main():
             "hbm_peak_gbs": pk.get("hbm_gbs"), "peaks_source": pk_kind,
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
             "serving": serving,
-            "multires_cross": mrc, **hbm_rows,
+            "multires_cross": mrc, "multires_cross_v2": mrc2, **hbm_rows,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

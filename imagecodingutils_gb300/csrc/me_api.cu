@@ -42,7 +42,11 @@ struct vppgpu_me {
     int* changed;
     int sweep_limit;
     int resolve_grid;
-    int relax_sweeps;  // MultiresCrossVer2: 0 = default
+    int relax_sweeps;  // relaxation sweeps before the wavefront (0..RELAX_SWEEPS)
+    void* d_mrc_args;  // MultiresCrossVer2: device mrc::MrcArgs
+    void* d_lattice;   // MultiresCrossVer2: one sub-pel lattice per MB
+    int4* d_search_cache;  // MultiresCrossVer2: searches of tie MBs at other predictions
+    void* d_tie_runs;      // MultiresCrossVer2: tie trees
     vppgpu::MeCtrl* h_ctrl;  // pinned
     int last_status;
     // per-kernel timing (vppgpu_me_set_timing)
@@ -101,6 +105,10 @@ void me_free(vppgpu_me* me)
     cudaFree(me->d_wave_rec);
     cudaFree(me->d_wave_choice);
     cudaFree(me->d_mrc);
+    cudaFree(me->d_mrc_args);
+    cudaFree(me->d_lattice);
+    cudaFree(me->d_search_cache);
+    cudaFree(me->d_tie_runs);
     cudaFree(me->d_job);
     if (me->graph) cudaGraphExecDestroy(me->graph);
     cudaFree(me->spec);
@@ -157,6 +165,11 @@ vppgpu::FullArgs full_args(vppgpu_me* me, double lambda)
     a.changed = me->changed;
     a.lambda = lambda;
     a.sweep_limit = me->sweep_limit;
+    a.relax_sweeps = me->relax_sweeps;
+    a.mrc = me->d_mrc_args;
+    a.lattice = me->d_lattice;
+    a.search_cache = me->d_search_cache;
+    a.tie_runs = me->d_tie_runs;
     a.spin_limit = 20000000LL;  // ~2 s of polling before a barrier gives up
     return a;
 }
@@ -172,17 +185,8 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
     int rc = vppgpu::set_job(ctx, me->d_job, vppgpu::JobDesc{d_src16, d_ref16, d_incl, d_slice, d_mv, d_dist, d_avg});
     if (rc) return rc;
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS_V2) {
-        vppgpu::V2State v;
-        v.scratch = me->d_mrc;
-        v.spec = reinterpret_cast<int4*>(me->spec);
-        v.final_mv = me->state;
-        v.final_dist = me->state + me->nmb;
-        v.pred_used = me->state + 2 * me->nmb;
-        v.changed = me->changed;
-        v.done = me->d_wave_choice;
-        v.sweeps = me->relax_sweeps ? me->relax_sweeps : vppgpu::V2_SWEEPS;
-        return vppgpu::mrc2_launch(ctx, me->mode, v, full_args(me, 0.9), d_src16, d_ref16, d_incl, d_slice, d_mv,
-                                   d_dist, d_avg);
+        VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
+        return vppgpu::mrc2_launch(ctx, me->mode, me->d_mrc, full_args(me, 0.9), d_src16, d_ref16);
     }
     const vppgpu::FullArgs a = full_args(me, lambda);
     cudaEvent_t* ev = ring_slot(me);
@@ -261,6 +265,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     me->mode = 1;
     me->rstride = width + 2 * vppgpu::PAD;
     me->sweep_limit = me->nmb + 2;
+    me->relax_sweeps = vppgpu::RELAX_SWEEPS;
     size_t npix = (size_t)width * height;
     size_t npad = (size_t)me->rstride * (height + 2 * vppgpu::PAD);
     me->plane_size = npad;
@@ -288,18 +293,29 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
             (rc = dalloc(&me->d_src8, npix)) || (rc = dalloc(&me->d_refp, npad)) ||
             (rc = dalloc(&me->d_hpel, 3 * npad)) ||
             (rc = dalloc(&me->d_mrc, vppgpu::mrc_scratch_bytes(width, height))) ||
-            (rc = dalloc(&me->d_job, 1)) || (rc = dalloc(&me->spec, 4 * (size_t)me->nmb)) ||
-            (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) || (rc = dalloc(&me->d_wave_choice, me->nmb)) ||
-            (rc = dalloc(&me->changed, vppgpu::V2_SWEEPS)) || (rc = dalloc(&me->d_out_mv, me->nmb)) ||
-            (rc = dalloc(&me->d_out_dist, me->nmb)) || (rc = dalloc(&me->d_out_avg, 1)) ||
-            (rc = dalloc(&me->d_incl, me->nmb)) || (rc = dalloc(&me->d_slice, me->nmb)) ||
-            (rc = dalloc(&me->ctrl, 1))) {
+            (rc = dalloc((unsigned char**)&me->d_mrc_args, vppgpu::mrc_args_bytes())) ||
+            (rc = dalloc((unsigned char**)&me->d_lattice, vppgpu::mrc_lattice_bytes() * (size_t)me->nmb)) ||
+            (rc = dalloc(&me->d_search_cache, (size_t)me->nmb * vppgpu::V2_SEARCH_CACHE)) ||
+            (rc = dalloc((unsigned char**)&me->d_tie_runs, vppgpu::mrc_tie_runs_bytes() * (size_t)me->nmb)) ||
+            (rc = dalloc(&me->tie_list, me->nmb)) ||
+            (rc = dalloc(&me->d_job, 1)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
+            (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
+            (rc = dalloc(&me->cache, (size_t)me->nmb * vppgpu::KCACHE)) || (rc = dalloc(&me->dict, vppgpu::NDICT)) ||
+            (rc = dalloc(&me->d_wave_rec, vppgpu::wave_rec_count(me->cols, me->rows))) ||
+            (rc = dalloc(&me->d_wave_choice, me->nmb)) || (rc = dalloc(&me->changed, (size_t)me->sweep_limit)) ||
+            (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
+            (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||
+            (rc = dalloc(&me->d_slice, me->nmb)) || (rc = dalloc(&me->ctrl, 1))) {
             me_free(me);
             return rc;
         }
         if (cudaMallocHost((void**)&me->h_ctrl, sizeof(vppgpu::MeCtrl)) != cudaSuccess) {
             me_free(me);
             return VPPGPU_ERR_OUT_OF_MEMORY;
+        }
+        if ((rc = vppgpu::full_prepare(ctx, me->nmb, &me->resolve_grid))) {
+            me_free(me);
+            return rc;
         }
         *out = me;
         return VPPGPU_OK;
@@ -481,9 +497,18 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 
 extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
 {
-    if (!me || sweeps < 0 || sweeps > vppgpu::V2_SWEEPS) return VPPGPU_ERR_INVALID_ARG;
-    if (me->kind != VPPGPU_ME_MULTIRES_CROSS_V2) return VPPGPU_ERR_UNSUPPORTED;
+    if (!me || sweeps < 0 || sweeps > vppgpu::RELAX_SWEEPS) return VPPGPU_ERR_INVALID_ARG;
+    if (me->kind != VPPGPU_ME_FULL && me->kind != VPPGPU_ME_MULTIRES_CROSS_V2) return VPPGPU_ERR_UNSUPPORTED;
+    if (sweeps == me->relax_sweeps) return VPPGPU_OK;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
     me->relax_sweeps = sweeps;
+    if (me->graph) {  // the captured sequence has the old number of sweep launches
+        VPP_CUDA(cudaStreamSynchronize(me->ctx->stream));
+        cudaGraphExecDestroy(me->graph);
+        me->graph = nullptr;
+    }
+    me->graph_state = 0;
     return VPPGPU_OK;
 }
 

@@ -419,7 +419,7 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid
     k_full_tietree<<<ctx->sm_count, TIE_RUNS * 32, sizeof(TieSmem), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     if (ev) VPP_CUDA(cudaEventRecord(ev[3], ctx->stream));
-    rc = full_resolve_launch(ctx, args, resolve_grid);
+    rc = full_resolve_launch(ctx, args, resolve_grid, 0);
     if (rc) return rc;
     if (ev) VPP_CUDA(cudaEventRecord(ev[4], ctx->stream));
     return VPPGPU_OK;

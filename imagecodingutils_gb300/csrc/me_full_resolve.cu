@@ -32,6 +32,7 @@
 //                      against the MB's records (prefetched with cp.async)
 //                      and, on a miss only, a full evaluation by the warp.
 #include "me_full_common.cuh"
+#include "me_mrc_search.cuh"
 
 namespace vppgpu {
 namespace {
@@ -108,8 +109,55 @@ __device__ __forceinline__ bool cache_probe(const int4* c, int key, int lane, in
     return true;
 }
 
+// MultiresCrossVer2: the searched vector and distortion of tie MB k at
+// rounded level-0 prediction (p0x, p0y): from its tie tree, else a kept
+// search whose tie decisions agree, else a new search (kept in slots 1..3;
+// slot 0 holds the search at prediction (0, 0)).  One warp.
+__device__ __noinline__ void v2_search_at(const FullArgs& a, int k, int p0x, int p0y, int lane, int* mvx, int* mvy,
+                                          int* minD)
+{
+    int tv, td;
+    if (mrc::tie_tree_result(static_cast<const mrc::V2TieRun*>(a.tie_runs) + (size_t)k * mrc::V2_TIE_RUNS, p0x, p0y,
+                             &tv, &td)) {
+        *mvx = mv_x(tv);
+        *mvy = mv_y(tv);
+        *minD = td;
+        return;
+    }
+    int4* sc = a.search_cache + (size_t)k * V2_SEARCH_CACHE;
+    const int4 e = lane < V2_SEARCH_CACHE ? __ldcg(sc + lane) : make_int4(0, 0, 0, -1);
+    const unsigned hit =
+        __ballot_sync(0xffffffffu, e.w >= 0 && mrc::search_reusable(e.w, mv_x(e.x), mv_y(e.x), p0x, p0y));
+    if (hit) {
+        const int f = __ffs(hit) - 1;
+        const int v = __shfl_sync(0xffffffffu, e.y, f);
+        *mvx = mv_x(v);
+        *mvy = mv_y(v);
+        *minD = __shfl_sync(0xffffffffu, e.z, f);
+        return;
+    }
+    const int pl[6] = {p0x / 2 / 2, p0y / 2 / 2, p0x / 2, p0y / 2, p0x, p0y};
+    bool bad = false;
+    const mrc::MrcArgs& m = *static_cast<const mrc::MrcArgs*>(a.mrc);
+    mrc::Lattice& LT = static_cast<mrc::Lattice*>(a.lattice)[k];
+    const mrc::MbSearch r = mrc::search_mb_ver2(m, LT, k / a.cols, k % a.cols, pl, lane, bad);
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&a.ctrl->status, ST_OUT_OF_BOUNDS);
+    *mvx = r.mvx;
+    *mvy = r.mvy;
+    *minD = r.min_d;
+    const unsigned slot = 1 + ((unsigned)pack_mv(p0x, p0y) * 2654435761u >> 30) % (V2_SEARCH_CACHE - 1);
+    if (lane == 0) __stcg(sc + slot, make_int4(pack_mv(p0x, p0y), pack_mv(r.mvx, r.mvy), r.min_d, r.tie));
+    __syncwarp();
+}
+
 // Full evaluation of MB k for raw prediction (px, py), one warp: the record
-// {prediction, distortion at it, final vector, final distortion}.
+// {prediction, distortion at it, final vector, final distortion}.  kEst 0:
+// MotionEstimatorH264ImplFull, a tie MB's scan from its table / tie tree;
+// kEst 1: MotionEstimatorH264ImplMultiresCrossVer2, whose searched result
+// (at prediction (0, 0)) holds for any prediction unless the search met a
+// tie; for such an MB the search at the prediction's level vectors
+// (…MultiresCrossVer2.cpp:627-642) comes from v2_search_at.
+template <int kEst>
 __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, int lane)
 {
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
@@ -119,7 +167,13 @@ __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, 
     int mvx = mv_x(sp.x), mvy = mv_y(sp.x), minD = sp.y;
     const int zd = sp.z;
     const bool tie = (sp.w & FLAG_TIE) && (round_pred(px) != 0 || round_pred(py) != 0);
-    if (tie) tie_path(a, k, px, py, sp.w, lane, &mvx, &mvy, &minD);
+    if (tie) {
+        if constexpr (kEst == 0) {
+            tie_path(a, k, px, py, sp.w, lane, &mvx, &mvy, &minD);
+        } else {
+            v2_search_at(a, k, round_pred(px), round_pred(py), lane, &mvx, &mvy, &minD);
+        }
+    }
     const int pos = best_of3_fast(mvx, mvy, minD, g.pcx, g.pcy, pd, zd, a.lambda, g.pcx, g.pcy);
     int4 rec;
     rec.x = pack_mv(px, py);
@@ -138,6 +192,7 @@ __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, 
 }
 
 // ---------------------------------------------------------------------------
+template <int kEst>
 __global__ void __launch_bounds__(256, 4) k_full_sweep0(FullArgs a)
 {
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -145,7 +200,7 @@ __global__ void __launch_bounds__(256, 4) k_full_sweep0(FullArgs a)
     if (k >= a.nmb) return;
     int px, py;
     median_pred(a.final_mv, a.spec4[k].w, k, a.cols, &px, &py);
-    const int4 rec = evaluate(a, k, px, py, lane);
+    const int4 rec = evaluate<kEst>(a, k, px, py, lane);
     if (lane < KCACHE) __stcg(a.cache + (size_t)k * KCACHE + lane, lane == 0 ? rec : empty_record());
     if (lane == 0) {
         a.pred_used[k] = rec.x;
@@ -171,6 +226,7 @@ struct RelaxSmem {
 // One relaxation sweep: lane per MB (MBs gwarp + lane*nwarps ...) to find the
 // MBs whose prediction moved, then the warp on each.  Skipped once an earlier
 // sweep changed no vector (the fixed point is reached).
+template <int kEst>
 __global__ void __launch_bounds__(256, 4) k_full_relax_sweep(FullArgs a, int sweep)
 {
     if (sweep > 1 && *((volatile int*)&a.changed[sweep - 1]) == 0) return;
@@ -197,7 +253,7 @@ __global__ void __launch_bounds__(256, 4) k_full_relax_sweep(FullArgs a, int swe
             int4* cache = a.cache + (size_t)kk * KCACHE;
             int4 rec;
             const bool hit = cache_probe(cache, fkey, lane, &rec);
-            if (!hit) rec = evaluate(a, kk, fx, fy, lane);
+            if (!hit) rec = evaluate<kEst>(a, kk, fx, fy, lane);
             if (lane == 0) {
                 atomicAdd(&a.ctrl->relax_evals, 1);
                 if (!hit) {
@@ -225,7 +281,7 @@ __global__ void __launch_bounds__(256) k_full_relax_outcome(FullArgs a)
 {
     __shared__ RelaxSmem S;
     int sweeps = 0;
-    for (int s = 1; s <= kRelaxSweeps && !sweeps; s++)
+    for (int s = 1; s <= a.relax_sweeps && !sweeps; s++)
         if (*((volatile int*)&a.changed[s]) == 0) sweeps = s;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     if (sweeps) {
@@ -315,11 +371,12 @@ __global__ void __launch_bounds__(256) k_full_relax_outcome(FullArgs a)
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) a.ctrl->sweeps = kRelaxSweeps;
+    if (threadIdx.x == 0) a.ctrl->sweeps = a.relax_sweeps;
 }
 
 // ---------------------------------------------------------------------------
 // One warp per MB: records at every dictionary vector the MB's cache lacks.
+template <int kEst>
 __global__ void __launch_bounds__(256, 2) k_full_precompute(FullArgs a)
 {
     if (*((volatile int*)&a.ctrl->converged)) return;
@@ -333,7 +390,7 @@ __global__ void __launch_bounds__(256, 2) k_full_precompute(FullArgs a)
         for (int d = 0; d < NDICT; d++) {
             const int v = dict[d];
             if (v == kEmpty || __any_sync(0xffffffffu, mine.x == v)) continue;
-            const int4 rec = evaluate(a, k, mv_x(v), mv_y(v), lane);
+            const int4 rec = evaluate<kEst>(a, k, mv_x(v), mv_y(v), lane);
             if (lane == 0) __stcg(cache + kCacheDict + d, rec);
             __syncwarp();
         }
@@ -412,6 +469,7 @@ __device__ __forceinline__ int neighbour_set(const FullArgs& a, int x, int lane,
     return min(__popc(km), kSetMax);
 }
 
+template <int kEst>
 __global__ void __launch_bounds__(256, 2) k_full_closure(FullArgs a)
 {
     if (*((volatile int*)&a.ctrl->converged)) return;
@@ -481,7 +539,7 @@ __global__ void __launch_bounds__(256, 2) k_full_closure(FullArgs a)
         // evaluate the new records
         for (int i = 0; i < fresh; i++) {
             const int key = S.fresh[wib][i];
-            const int4 rec = evaluate(a, k, mv_x(key), mv_y(key), lane);
+            const int4 rec = evaluate<kEst>(a, k, mv_x(key), mv_y(key), lane);
             if (lane == kCacheClosure + i) mine = rec;
         }
         if (lane >= kCacheClosure) {
@@ -578,7 +636,7 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
         : "memory");
 }
 
-template <int kChunk>
+template <int kChunk, int kEst>
 __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a, int band0, int last)
 {
     if (*((volatile int*)&a.ctrl->converged)) return;
@@ -722,7 +780,7 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
                 miss &= miss - 1;
                 const int fkey = __shfl_sync(0xffffffffu, key, f);
                 const int fk = (32 * band + f) * cols + (t - 2 * f);
-                const int4 rec = evaluate(a, fk, mv_x(fkey), mv_y(fkey), lane);
+                const int4 rec = evaluate<kEst>(a, fk, mv_x(fkey), mv_y(fkey), lane);
                 if (lane == f) {
                     out = rec.z;
                     a.final_mv[fk] = rec.z;
@@ -749,7 +807,7 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
     }
     if (lane == 0 && misses) atomicAdd(&a.ctrl->wave_miss, misses);
     __syncthreads();
-    if (threadIdx.x == 0 && !abort_flag && last) a.ctrl->sweeps = kRelaxSweeps + 1000;
+    if (threadIdx.x == 0 && !abort_flag && last) a.ctrl->sweeps = a.relax_sweeps + 1000;
 }
 
 // Outputs of a wavefront-resolved frame, one thread per MB: the record each
@@ -850,24 +908,31 @@ constexpr int kWaveMaxCols = 512;  // 8192 / 16
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
 {
     *resolve_cap = ctx->sm_count * 8;
-    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
-    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 2)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 2)));
     return VPPGPU_OK;
 }
 
-int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid)
+namespace {
+
+template <int kEst>
+int resolve_launch(vppgpu_ctx* ctx, const FullArgs& args)
 {
     const int rows = args.nmb / args.cols, nbands = (rows + 31) / 32;
     if (args.cols > kWaveMaxCols) return VPPGPU_ERR_UNSUPPORTED;
-    k_full_sweep0<<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
+    k_full_sweep0<kEst><<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     {
         // many warps, few MBs each: a sweep's latency is its busiest warp's evaluations
         const int want = (args.nmb + 7) / 8, cap = ctx->sm_count * 4, blocks = want < cap ? want : cap;
-        for (int sweep = 1; sweep <= kRelaxSweeps; sweep++) {
-            k_full_relax_sweep<<<blocks, 256, 0, ctx->stream>>>(args, sweep);
+        for (int sweep = 1; sweep <= args.relax_sweeps; sweep++) {
+            k_full_relax_sweep<kEst><<<blocks, 256, 0, ctx->stream>>>(args, sweep);
             VPP_CHECK_LAUNCH(ctx);
         }
         const int ob = (args.nmb + 255) / 256, ocap = ctx->sm_count * 4;
@@ -876,18 +941,18 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid)
     }
     {
         const int blocks = (args.nmb + 7) / 8, cap = ctx->sm_count * 8, grid = blocks < cap ? blocks : cap;
-        k_full_precompute<<<grid, 256, 0, ctx->stream>>>(args);
+        k_full_precompute<kEst><<<grid, 256, 0, ctx->stream>>>(args);
         VPP_CHECK_LAUNCH(ctx);
-        k_full_closure<<<grid, 256, 0, ctx->stream>>>(args);
+        k_full_closure<kEst><<<grid, 256, 0, ctx->stream>>>(args);
         VPP_CHECK_LAUNCH(ctx);
     }
     for (int b0 = 0; b0 < nbands; b0 += kWaveMaxWarps) {
         const int nw = nbands - b0 < kWaveMaxWarps ? nbands - b0 : kWaveMaxWarps;
         const int last = b0 + nw == nbands;
         if (nw <= 3)
-            k_full_wave<4><<<1, nw * 32, wave_smem_bytes(nw, args.cols, 4), ctx->stream>>>(args, b0, last);
+            k_full_wave<4, kEst><<<1, nw * 32, wave_smem_bytes(nw, args.cols, 4), ctx->stream>>>(args, b0, last);
         else
-            k_full_wave<2><<<1, nw * 32, wave_smem_bytes(nw, args.cols, 2), ctx->stream>>>(args, b0, last);
+            k_full_wave<2, kEst><<<1, nw * 32, wave_smem_bytes(nw, args.cols, 2), ctx->stream>>>(args, b0, last);
         VPP_CHECK_LAUNCH(ctx);
     }
     {
@@ -898,6 +963,14 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid)
         VPP_CHECK_LAUNCH(ctx);
     }
     return VPPGPU_OK;
+}
+
+}  // namespace
+
+int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid, int est)
+{
+    (void)resolve_grid;
+    return est == 0 ? resolve_launch<0>(ctx, args) : resolve_launch<1>(ctx, args);
 }
 
 int full_residual_launch(vppgpu_ctx* ctx, const FullArgs& args, const int* d_mv, short* d_res)

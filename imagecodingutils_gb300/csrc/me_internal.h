@@ -87,8 +87,16 @@ struct FullArgs {
                                // (evaluated there; final_mv / final_dist hold the result)
     double lambda;
     int sweep_limit;
+    int relax_sweeps;          // relaxation sweeps before the wavefront (0..8)
     long long spin_limit;
+    // MultiresCrossVer2 only: the search's level planes (device mrc::MrcArgs)
+    // and one sub-pel lattice per macroblock for searches at a prediction
+    const void* mrc;
+    void* lattice;
+    int4* search_cache;  // V2_SEARCH_CACHE per MB: {rounded prediction, vector, distortion, tie levels or -1}
+    void* tie_runs;      // 8 tie-tree runs (mrc::V2TieRun, 32 bytes) per MB
 };
+constexpr int V2_SEARCH_CACHE = 4;
 
 constexpr int NDICT = 8;    // dictionary vectors
 constexpr int WAVE_WARPS = 5;   // most warps (bands of 32 rows) of one wavefront launch
@@ -105,23 +113,17 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
 const int* me_status_word(vppgpu_me* me);
 int status_from_bits(int bits);
 
-// MultiresCrossVer2 (me_mrc.cu): level planes plus the per-MB state of the
-// prediction-dependent pass; `planes` carries the Full geometry and buffers
-// used for the distortion at the prediction (src8, refp, hpel, job, ctrl).
-constexpr int V2_SWEEPS = 8;
-struct V2State {
-    unsigned char* scratch;  // mrc_scratch_bytes
-    int4* spec;              // nmb
-    int* final_mv;           // nmb
-    int* final_dist;         // nmb
-    int* pred_used;          // nmb
-    int* changed;            // V2_SWEEPS
-    int* done;               // nmb
-    int sweeps;              // relaxation sweeps before the dataflow pass, 1..V2_SWEEPS
-};
-int mrc2_launch(vppgpu_ctx* ctx, int mode, const V2State& st, const FullArgs& planes, const short* d_src16,
-                const short* d_ref16, const unsigned char* incl, const int* slice, int* out_mv, int* out_dist,
-                long long* out_avg);
+// MultiresCrossVer2 (me_mrc.cu): level planes in `scratch`, the search at
+// prediction (0, 0) into args.spec4 / final_mv, then the full-search
+// estimator's prediction-dependent resolve with the Ver2 evaluation.
+// args.mrc points to mrc_args_bytes() of device memory; args.lattice to
+// nmb * mrc_lattice_bytes().
+constexpr int RELAX_SWEEPS = 8;
+size_t mrc_args_bytes();
+size_t mrc_lattice_bytes();
+size_t mrc_tie_runs_bytes();  // per macroblock
+int mrc2_launch(vppgpu_ctx* ctx, int mode, unsigned char* scratch, const FullArgs& args, const short* d_src16,
+                const short* d_ref16);
 
 // Write this estimate's pointers to the device descriptor (a one-thread
 // kernel with the descriptor as its parameter: stream-ordered, no host copy).
@@ -136,7 +138,8 @@ size_t full_search_smem();
 int full_planes_launch(vppgpu_ctx* ctx, const FullArgs& args);
 // Launch the prediction-dependent tail (sweep 0, relaxation, dictionary
 // precompute, exact wavefront) of an estimate whose search has run.
-int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid);
+// est: 0 MotionEstimatorH264ImplFull, 1 MotionEstimatorH264ImplMultiresCrossVer2.
+int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid, int est);
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap);
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid);
 // ev: nullptr, or 5 events recorded before the pack kernel, before the

@@ -180,6 +180,11 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     a.changed = (int*)(base + kOffChanged);
     a.lambda = 1.05;
     a.sweep_limit = nmb + 2;
+    a.relax_sweeps = vppgpu::RELAX_SWEEPS;
+    a.mrc = nullptr;
+    a.lattice = nullptr;
+    a.search_cache = nullptr;
+    a.tie_runs = nullptr;
     a.spin_limit = 20000000LL;
 
     // the words that must start at zero on every call

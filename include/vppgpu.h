@@ -117,9 +117,9 @@ int vppgpu_me_last_status(vppgpu_me* me);
 /* Number of resolve sweeps the last estimate needed (predictor fixed point). */
 int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps);
 
-/* MultiresCrossVer2 only, no vpp counterpart: relaxation sweeps (1..8, 0 =
- * the default 8) run before the exact dataflow pass decides the macroblocks
- * whose predictions have not settled.  Results do not depend on it. */
+/* Full and MultiresCrossVer2, no vpp counterpart: relaxation sweeps (0..8,
+ * default 8) run before the exact wavefront decides the macroblocks whose
+ * predictions have not settled.  Results do not depend on it. */
 int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps);
 
 /* Counters of the last estimate's prediction-dependent stage: {sweeps,

@@ -327,7 +327,7 @@ static inline int mr_farther(int mx, int my, int rmx, int rmy, int j, int i, int
 /* Result of the search of one macroblock. */
 typedef struct {
     int zero_d, min_d, mvx, mvy;
-    int tie; /* an integer stage met a candidate equal to its running minimum */
+    int tie; /* integer stages that met a candidate equal to their running minimum: 1 level 2, 2 level 1, 4 level 0 */
 } mr_result;
 
 /* The search of macroblock (mbr, mbc) of both estimators, from the zero
@@ -360,7 +360,7 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
                 int d = ov_tsd4_lt(&oin2, &oe2, min2);
                 if (d > min2) continue;
                 if (d == min2) {
-                    tie = 1;
+                    tie |= 1;
                     /* MultiresCross compares the centre with the offset (…:673-679) */
                     if (pred ? mr_farther(mx, my, rmx, rmy, j, i, pred[0], pred[1])
                              : (my * my + mx * mx) - (i * i + j * j) < 0)
@@ -392,7 +392,7 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
                 int d = ov_tsd_partial_lt(&oin1, &oe1, 8, min1);
                 if (d > min1) continue;
                 if (d == min1) {
-                    tie = 1;
+                    tie |= 2;
                     if (mr_farther(mx, my, rmx, rmy, j, i, p1x, p1y)) continue;
                 }
                 min1 = d;
@@ -410,7 +410,7 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
                 int d = ov_tsd_partial_lt(&oin1, &oe1, 8, min1);
                 if (d > min1) continue;
                 if (d == min1) {
-                    tie = 1;
+                    tie |= 2;
                     if (mr_farther(mx, my, rmx, rmy, j, i, p1x, p1y)) continue;
                 }
                 min1 = d;
@@ -439,7 +439,7 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
             int d = ov_tsd_partial_lt(&oin0, &oe0, 16, min_d);
             if (d > min_d) continue;
             if (d == min_d) {
-                tie = 1;
+                tie |= 4;
                 if (mr_farther(mx, my, rmx, rmy, j, i, p0x, p0y)) continue;
             }
             min_d = d;
@@ -530,8 +530,8 @@ int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int m
  * MultiresCrossVer2.h:168-197).  Only full macroblock rows are estimated: the
  * reference drops the partial bottom row's vectors (…:1137) and asks the
  * predictor for an index past its array for it.  tie_out (nullable): per MB,
- * 1 if an integer stage met an equal distortion (the search then depends on
- * the prediction). */
+ * the integer stages that met an equal distortion (1 level 2, 2 level 1,
+ * 4 level 0; the search then depends on the prediction). */
 int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, int motion_range, int mode,
                             const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist,
                             long* avg_dist, int* tie_out)

@@ -81,7 +81,8 @@ int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int m
  * MultiresCross search with ties towards the rounded median prediction of
  * each level, the pred-vector check and GetBestVector (lambda 0.9).  Full
  * macroblock rows only.  slice: NULL or one slice id per MB.  tie_out: NULL
- * or per MB 1 when an integer stage met an equal distortion. */
+ * or per MB the integer stages that met an equal distortion (bits: 1 level 2,
+ * 2 level 1, 4 level 0). */
 int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, int motion_range, int mode,
                             const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist,
                             long* avg_dist, int* tie_out);

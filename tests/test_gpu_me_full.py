@@ -153,3 +153,25 @@ def test_1080p_against_oracle(vpp, ctx, orc, h):
     np.testing.assert_array_equal(dist, dist_o)
     assert avg == avg_o
     assert me.last_sweeps() >= 1
+
+
+@pytest.mark.parametrize("sweeps", [0, 2])
+def test_wavefront_after_few_relaxation_sweeps(vpp, ctx, orc, sweeps):
+    """With no or two relaxation sweeps the exact wavefront decides most of
+    the frame; the result is the sequential one either way (the captured
+    kernel sequence is rebuilt after the change)."""
+    w, h = 640, 368
+    fr = synth.pan_sequence(90 + sweeps, w, h, 3)
+    me = vpp.MotionEstimatorH264ImplFull(fr[1], fr[0], w, h, 128, ctx=ctx)
+    assert me.Create() == 1
+    me.Estimate()  # captured with the default 8 sweeps
+    L = vpp.load()
+    assert L.vppgpu_me_set_relax_sweeps(me._h_me, sweeps) == 0
+    for t in (1, 2):
+        me._src, me._ref = fr[t], fr[t - 1]
+        mv, _ = me.Estimate()
+        mv_o, dist_o, _ = orc.me_full(fr[t], fr[t - 1], 128)
+        np.testing.assert_array_equal(mv, mv_o)
+        np.testing.assert_array_equal(me.last_mb_distortion, dist_o)
+        if sweeps == 0:
+            assert me.last_sweeps() == 1000

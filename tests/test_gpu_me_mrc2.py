@@ -4,7 +4,7 @@ with and without pDistortionIncluded, a partial bottom row, integer-shift
 content), and vectors, per-macroblock distortions and averages bit-exact with
 the CPU oracle on further seeded sizes, slice maps, tie-rich content and a
 1080p sequence whose predictions do not settle in the relaxation sweeps (the
-exact dataflow pass then decides)."""
+exact wavefront then decides)."""
 import ctypes as C
 
 import numpy as np
@@ -86,11 +86,11 @@ def test_tie_rich_content(vpp, ctx, orc):
         np.testing.assert_array_equal(dist, dist_o)
 
 
-@pytest.mark.parametrize("sweeps", [0, 1, 3])
-def test_1080p_sequence_and_dataflow_pass(vpp, ctx, orc, sweeps):
-    """Frame pairs of the 1080p benchmark sequence with the default 8 sweeps
-    and with 1 or 3 relaxation sweeps, after which the exact dataflow pass
-    decides the macroblocks that have not settled; every result matches."""
+@pytest.mark.parametrize("sweeps", [8, 0, 3])
+def test_1080p_sequence_and_wavefront(vpp, ctx, orc, sweeps):
+    """Frame pairs of the 1080p benchmark sequence with the default 8 sweeps,
+    none, or 3 relaxation sweeps, after which the exact wavefront decides the
+    macroblocks that have not settled; every result matches."""
     L = vpp.load()
     fr = synth.pan_sequence(1234, 1920, 1080, 4)
     used = []
@@ -107,8 +107,8 @@ def test_1080p_sequence_and_dataflow_pass(vpp, ctx, orc, sweeps):
         s = C.c_int()
         L.vppgpu_me_last_sweeps(me._h_me, C.byref(s))
         used.append(s.value)
-    if sweeps == 1:
-        assert any(u >= 1000 for u in used), used  # the dataflow pass ran
+    if sweeps == 0:
+        assert all(u >= 1000 for u in used), used  # no relaxation: the wavefront decided every frame
 
 
 def test_pixel_range_rejected(vpp, ctx):
