@@ -27,7 +27,9 @@ from . import _lib
 from ._lib import VppGpuError, check, load
 
 __all__ = [
-    "Context", "get_context", "MotionEstimatorH264ImplFull", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
+    "Context", "get_context", "MotionEstimatorH264ImplFull", "MotionEstimatorH264ImplMultires",
+    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorBatch",
+    "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
     "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1",
     "FastGpuRGB24toYUV420Converter", "VppGpuError", "load",
 ]
@@ -191,6 +193,15 @@ class MotionEstimatorH264ImplMultiresCross(_MotionEstimatorBase):
             check(load().vppgpu_me_get_mode(self._h_me, C.byref(m)), "vppgpu_me_get_mode")
             return m.value
         return self._mode
+
+
+class MotionEstimatorH264ImplMultires(MotionEstimatorH264ImplMultiresCross):
+    """GPU MotionEstimatorH264ImplMultires (src/CodecUtils/MotionEstimatorH264ImplMultires.cpp):
+    full searches at levels 2 and 1, +-2 at level 0, sub-pel, ties towards the
+    prediction rounded to each level, the pred-vector check and GetBestVector
+    (lambda 1.1).  The reference needs its pMVPred constructor argument."""
+
+    KIND = _lib.ME_MULTIRES
 
 
 class MotionEstimatorH264ImplMultiresCrossVer2(MotionEstimatorH264ImplMultiresCross):

@@ -184,9 +184,12 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
                                   d_mv, d_dist, d_avg, me->ctrl);
     int rc = vppgpu::set_job(ctx, me->d_job, vppgpu::JobDesc{d_src16, d_ref16, d_incl, d_slice, d_mv, d_dist, d_avg});
     if (rc) return rc;
-    if (me->kind == VPPGPU_ME_MULTIRES_CROSS_V2) {
+    if (me->kind == VPPGPU_ME_MULTIRES_CROSS_V2 || me->kind == VPPGPU_ME_MULTIRES) {
+        // GetBestVector's lambda: 0.9 (MultiresCrossVer2.cpp:1050), 1.1 (Multires.cpp:958)
+        const bool v2 = me->kind == VPPGPU_ME_MULTIRES_CROSS_V2;
         VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
-        return vppgpu::mrc2_launch(ctx, me->mode, me->d_mrc, full_args(me, 0.9), d_src16, d_ref16);
+        return vppgpu::mrc2_launch(ctx, v2 ? 1 : 2, me->mode, me->d_mrc, full_args(me, v2 ? 0.9 : 1.1), d_src16,
+                                   d_ref16);
     }
     const vppgpu::FullArgs a = full_args(me, lambda);
     cudaEvent_t* ev = ring_slot(me);
@@ -248,8 +251,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
     if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
     if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
-    if (kind != VPPGPU_ME_FULL && kind != VPPGPU_ME_MULTIRES_CROSS && kind != VPPGPU_ME_MULTIRES_CROSS_V2)
-        return VPPGPU_ERR_UNSUPPORTED;
+    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_MULTIRES_CROSS_V2) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me* me = (vppgpu_me*)calloc(1, sizeof(vppgpu_me));
@@ -286,8 +288,8 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
         *out = me;
         return VPPGPU_OK;
     }
-    if (kind == VPPGPU_ME_MULTIRES_CROSS_V2) {
-        // MotionEstimatorH264ImplMultiresCrossVer2(…) + Create(): level planes, the
+    if (kind == VPPGPU_ME_MULTIRES_CROSS_V2 || kind == VPPGPU_ME_MULTIRES) {
+        // MotionEstimatorH264ImplMultiresCrossVer2 / Multires (…, pMVPred, …) + Create(): level planes, the
         // padded reference with its half-pel planes, per-MB prediction state
         if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
             (rc = dalloc(&me->d_src8, npix)) || (rc = dalloc(&me->d_refp, npad)) ||
@@ -355,7 +357,7 @@ int vppgpu_me_set_mode(vppgpu_me* me, int mode)
 {
     if (!me) return VPPGPU_ERR_INVALID_ARG;
     // SetMode(0) picks by picture area (MultiresCross.cpp:501-513)
-    if (mode == 0 && (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_MULTIRES_CROSS_V2))
+    if (mode == 0 && me->kind != VPPGPU_ME_FULL)
         mode = (me->W * me->H > 40000) ? 2 : 1;
     me->mode = mode;
     return VPPGPU_OK;
@@ -498,7 +500,7 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
 {
     if (!me || sweeps < 0 || sweeps > vppgpu::RELAX_SWEEPS) return VPPGPU_ERR_INVALID_ARG;
-    if (me->kind != VPPGPU_ME_FULL && me->kind != VPPGPU_ME_MULTIRES_CROSS_V2) return VPPGPU_ERR_UNSUPPORTED;
+    if (me->kind == VPPGPU_ME_MULTIRES_CROSS) return VPPGPU_ERR_UNSUPPORTED;
     if (sweeps == me->relax_sweeps) return VPPGPU_OK;
     int rc = vppgpu::bind(me->ctx);
     if (rc) return rc;
@@ -618,8 +620,7 @@ int vppgpu_me_batch_create(vppgpu_ctx* ctx, int kind, int streams, vppgpu_me_bat
 {
     if (!ctx || !out || streams < 1) return VPPGPU_ERR_INVALID_ARG;
     *out = nullptr;
-    if (kind != VPPGPU_ME_FULL && kind != VPPGPU_ME_MULTIRES_CROSS && kind != VPPGPU_ME_MULTIRES_CROSS_V2)
-        return VPPGPU_ERR_UNSUPPORTED;
+    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_MULTIRES_CROSS_V2) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me_batch* b = (vppgpu_me_batch*)calloc(1, sizeof(vppgpu_me_batch));

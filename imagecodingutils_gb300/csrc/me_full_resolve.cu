@@ -109,16 +109,17 @@ __device__ __forceinline__ bool cache_probe(const int4* c, int key, int lane, in
     return true;
 }
 
-// MultiresCrossVer2: the searched vector and distortion of tie MB k at
-// rounded level-0 prediction (p0x, p0y): from its tie tree, else a kept
-// search whose tie decisions agree, else a new search (kept in slots 1..3;
-// slot 0 holds the search at prediction (0, 0)).  One warp.
-__device__ __noinline__ void v2_search_at(const FullArgs& a, int k, int p0x, int p0y, int lane, int* mvx, int* mvy,
-                                          int* minD)
+// The predictor multi-resolution estimators (kEst 1 Ver2, 2 Multires): the
+// searched vector and distortion of tie MB k at prediction (px, py): from its
+// tie tree, else a kept search whose tie decisions agree, else a new search
+// (kept in slots 1..3; slot 0 holds the search at prediction (0, 0)).  One warp.
+template <int kEst>
+__device__ __noinline__ void pred_search_at(const FullArgs& a, int k, int px, int py, int lane, int* mvx, int* mvy,
+                                            int* minD)
 {
     int tv, td;
-    if (mrc::tie_tree_result(static_cast<const mrc::V2TieRun*>(a.tie_runs) + (size_t)k * mrc::V2_TIE_RUNS, p0x, p0y,
-                             &tv, &td)) {
+    if (mrc::tie_tree_result(kEst, static_cast<const mrc::V2TieRun*>(a.tie_runs) + (size_t)k * mrc::V2_TIE_RUNS, px,
+                             py, &tv, &td)) {
         *mvx = mv_x(tv);
         *mvy = mv_y(tv);
         *minD = td;
@@ -127,7 +128,7 @@ __device__ __noinline__ void v2_search_at(const FullArgs& a, int k, int p0x, int
     int4* sc = a.search_cache + (size_t)k * V2_SEARCH_CACHE;
     const int4 e = lane < V2_SEARCH_CACHE ? __ldcg(sc + lane) : make_int4(0, 0, 0, -1);
     const unsigned hit =
-        __ballot_sync(0xffffffffu, e.w >= 0 && mrc::search_reusable(e.w, mv_x(e.x), mv_y(e.x), p0x, p0y));
+        __ballot_sync(0xffffffffu, e.w >= 0 && mrc::search_reusable(kEst, e.w, mv_x(e.x), mv_y(e.x), px, py));
     if (hit) {
         const int f = __ffs(hit) - 1;
         const int v = __shfl_sync(0xffffffffu, e.y, f);
@@ -136,17 +137,16 @@ __device__ __noinline__ void v2_search_at(const FullArgs& a, int k, int p0x, int
         *minD = __shfl_sync(0xffffffffu, e.z, f);
         return;
     }
-    const int pl[6] = {p0x / 2 / 2, p0y / 2 / 2, p0x / 2, p0y / 2, p0x, p0y};
     bool bad = false;
     const mrc::MrcArgs& m = *static_cast<const mrc::MrcArgs*>(a.mrc);
     mrc::Lattice& LT = static_cast<mrc::Lattice*>(a.lattice)[k];
-    const mrc::MbSearch r = mrc::search_mb_ver2(m, LT, k / a.cols, k % a.cols, pl, lane, bad);
+    const mrc::MbSearch r = mrc::search_pred<kEst>(m, LT, k / a.cols, k % a.cols, px, py, lane, bad);
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&a.ctrl->status, ST_OUT_OF_BOUNDS);
     *mvx = r.mvx;
     *mvy = r.mvy;
     *minD = r.min_d;
-    const unsigned slot = 1 + ((unsigned)pack_mv(p0x, p0y) * 2654435761u >> 30) % (V2_SEARCH_CACHE - 1);
-    if (lane == 0) __stcg(sc + slot, make_int4(pack_mv(p0x, p0y), pack_mv(r.mvx, r.mvy), r.min_d, r.tie));
+    const unsigned slot = 1 + ((unsigned)pack_mv(px, py) * 2654435761u >> 30) % (V2_SEARCH_CACHE - 1);
+    if (lane == 0) __stcg(sc + slot, make_int4(pack_mv(px, py), pack_mv(r.mvx, r.mvy), r.min_d, r.tie));
     __syncwarp();
 }
 
@@ -156,7 +156,8 @@ __device__ __noinline__ void v2_search_at(const FullArgs& a, int k, int p0x, int
 // kEst 1: MotionEstimatorH264ImplMultiresCrossVer2, whose searched result
 // (at prediction (0, 0)) holds for any prediction unless the search met a
 // tie; for such an MB the search at the prediction's level vectors
-// (…MultiresCrossVer2.cpp:627-642) comes from v2_search_at.
+// (…MultiresCrossVer2.cpp:627-642) comes from pred_search_at.  kEst 2:
+// MotionEstimatorH264ImplMultires, the same with its own search.
 template <int kEst>
 __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, int lane)
 {
@@ -166,13 +167,11 @@ __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, 
     const int pd = plane_pred_distortion(a, n, m, g, lane);
     int mvx = mv_x(sp.x), mvy = mv_y(sp.x), minD = sp.y;
     const int zd = sp.z;
-    const bool tie = (sp.w & FLAG_TIE) && (round_pred(px) != 0 || round_pred(py) != 0);
-    if (tie) {
-        if constexpr (kEst == 0) {
+    if constexpr (kEst == 0) {
+        if ((sp.w & FLAG_TIE) && (round_pred(px) != 0 || round_pred(py) != 0))
             tie_path(a, k, px, py, sp.w, lane, &mvx, &mvy, &minD);
-        } else {
-            v2_search_at(a, k, round_pred(px), round_pred(py), lane, &mvx, &mvy, &minD);
-        }
+    } else {
+        if (sp.w & FLAG_TIE) pred_search_at<kEst>(a, k, px, py, lane, &mvx, &mvy, &minD);
     }
     const int pos = best_of3_fast(mvx, mvy, minD, g.pcx, g.pcy, pd, zd, a.lambda, g.pcx, g.pcy);
     int4 rec;
@@ -916,6 +915,10 @@ int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
                                   (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 2)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 2)));
     return VPPGPU_OK;
 }
 
@@ -970,7 +973,7 @@ int resolve_launch(vppgpu_ctx* ctx, const FullArgs& args)
 int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid, int est)
 {
     (void)resolve_grid;
-    return est == 0 ? resolve_launch<0>(ctx, args) : resolve_launch<1>(ctx, args);
+    return est == 0 ? resolve_launch<0>(ctx, args) : (est == 1 ? resolve_launch<1>(ctx, args) : resolve_launch<2>(ctx, args));
 }
 
 int full_residual_launch(vppgpu_ctx* ctx, const FullArgs& args, const int* d_mv, short* d_res)

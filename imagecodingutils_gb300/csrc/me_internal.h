@@ -122,8 +122,9 @@ constexpr int RELAX_SWEEPS = 8;
 size_t mrc_args_bytes();
 size_t mrc_lattice_bytes();
 size_t mrc_tie_runs_bytes();  // per macroblock
-int mrc2_launch(vppgpu_ctx* ctx, int mode, unsigned char* scratch, const FullArgs& args, const short* d_src16,
-                const short* d_ref16);
+// est: 1 MultiresCrossVer2, 2 Multires (the same pipeline, their own search).
+int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, const FullArgs& args,
+                const short* d_src16, const short* d_ref16);
 
 // Write this estimate's pointers to the device descriptor (a one-thread
 // kernel with the descriptor as its parameter: stream-ordered, no host copy).
@@ -138,7 +139,8 @@ size_t full_search_smem();
 int full_planes_launch(vppgpu_ctx* ctx, const FullArgs& args);
 // Launch the prediction-dependent tail (sweep 0, relaxation, dictionary
 // precompute, exact wavefront) of an estimate whose search has run.
-// est: 0 MotionEstimatorH264ImplFull, 1 MotionEstimatorH264ImplMultiresCrossVer2.
+// est: 0 MotionEstimatorH264ImplFull, 1 MotionEstimatorH264ImplMultiresCrossVer2,
+// 2 MotionEstimatorH264ImplMultires.
 int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid, int est);
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap);
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid);

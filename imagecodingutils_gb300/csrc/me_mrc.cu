@@ -160,24 +160,25 @@ __global__ void k_mrc_average(long long* out_avg, MeCtrl* ctrl)
 }
 
 // ---------------------------------------------------------------------------
-// MultiresCrossVer2 (…MultiresCrossVer2.cpp:537-1151).  The search depends on
-// the median prediction only through its tie rules, so every macroblock is
-// searched once at prediction (0, 0) and remembers whether a tie occurred: its
-// result then holds for any prediction unless it did.  What follows is a
-// function of the prediction (distortion at the prediction through the
-// half-pel planes, GetBestVector with lambda 0.9) over the raster-order DAG of
-// predictions, the same as the full-search estimator's, and is resolved by
-// its kernels (me_full_resolve.cu) with the Ver2 evaluation.
-__global__ void __launch_bounds__(256) k_v2_search(MrcArgs m, FullArgs f)
+// The predictor estimators, MultiresCrossVer2 (…MultiresCrossVer2.cpp:537-1151)
+// and Multires (…Multires.cpp:557-1024).  Their searches depend on the median
+// prediction only through tie rules, so every macroblock is searched once at
+// prediction (0, 0) and remembers whether a tie occurred: the result then
+// holds for any prediction unless it did, and for those MBs eight runs with
+// the first three ties decided both ways (the tie tree) give it for any
+// prediction.  What follows is a function of the prediction (distortion at
+// the prediction through the half-pel planes, GetBestVector) over the
+// raster-order DAG of predictions, the same as the full-search estimator's,
+// and is resolved by its kernels (me_full_resolve.cu).
+template <int kEst>
+__global__ void __launch_bounds__(256) k_pred_search(MrcArgs m, FullArgs f)
 {
     __shared__ Lattice lattice[8];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int k = blockIdx.x * 8 + wib;
     if (k >= f.nmb) return;
     bool bad = false;
-    const int mbr = k / f.cols, mbc = k - mbr * f.cols;
-    const int zero6[6] = {0, 0, 0, 0, 0, 0};
-    const MbSearch r = search_mb_ver2(m, lattice[wib], mbr, mbc, zero6, lane, bad);
+    const MbSearch r = search_pred<kEst>(m, lattice[wib], k / f.cols, k % f.cols, 0, 0, lane, bad);
     bad = __any_sync(0xffffffffu, bad);
     if (lane == 0) {
         if (bad) atomicOr(&f.ctrl->status, ST_OUT_OF_BOUNDS);
@@ -195,7 +196,8 @@ __global__ void __launch_bounds__(256) k_v2_search(MrcArgs m, FullArgs f)
 
 // The tie tree of every MB whose search met a tie: warp r of a block makes
 // run r (its first three ties decided by the bits of r).
-__global__ void __launch_bounds__(V2_TIE_RUNS * 32) k_v2_tietree(MrcArgs m, FullArgs f)
+template <int kEst>
+__global__ void __launch_bounds__(V2_TIE_RUNS * 32) k_pred_tietree(MrcArgs m, FullArgs f)
 {
     __shared__ Lattice lattice[V2_TIE_RUNS];
     const int lane = threadIdx.x & 31, run = threadIdx.x >> 5;
@@ -204,7 +206,8 @@ __global__ void __launch_bounds__(V2_TIE_RUNS * 32) k_v2_tietree(MrcArgs m, Full
     for (int i = blockIdx.x; i < ntie; i += gridDim.x) {
         const int k = __ldcg(f.tie_list + i);
         bool bad = false;
-        search_mb_run(m, lattice[run], k / f.cols, k % f.cols, run, runs + (size_t)k * V2_TIE_RUNS + run, lane, bad);
+        search_run<kEst>(m, lattice[run], k / f.cols, k % f.cols, run, runs + (size_t)k * V2_TIE_RUNS + run, lane,
+                         bad);
         if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&f.ctrl->status, ST_OUT_OF_BOUNDS);
     }
 }
@@ -308,8 +311,8 @@ size_t mrc_args_bytes() { return sizeof(MrcArgs); }
 size_t mrc_lattice_bytes() { return sizeof(Lattice); }
 size_t mrc_tie_runs_bytes() { return sizeof(V2TieRun) * V2_TIE_RUNS; }
 
-int mrc2_launch(vppgpu_ctx* ctx, int mode, unsigned char* scratch, const FullArgs& args, const short* d_src16,
-                const short* d_ref16)
+int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, const FullArgs& args,
+                const short* d_src16, const short* d_ref16)
 {
     MrcArgs m = mrc_args(args.W, args.H, args.motion_range, mode, scratch);
     m.ctrl = args.ctrl;
@@ -318,11 +321,17 @@ int mrc2_launch(vppgpu_ctx* ctx, int mode, unsigned char* scratch, const FullArg
     int rc = full_planes_launch(ctx, args);
     if (rc) return rc;
     if ((rc = levels_launch(ctx, m, d_src16, d_ref16))) return rc;
-    k_v2_search<<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(m, args);
+    if (est == EST_MULTIRES) {
+        k_pred_search<EST_MULTIRES><<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(m, args);
+        VPP_CHECK_LAUNCH(ctx);
+        k_pred_tietree<EST_MULTIRES><<<ctx->sm_count * 2, V2_TIE_RUNS * 32, 0, ctx->stream>>>(m, args);
+    } else {
+        k_pred_search<EST_VER2><<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(m, args);
+        VPP_CHECK_LAUNCH(ctx);
+        k_pred_tietree<EST_VER2><<<ctx->sm_count * 2, V2_TIE_RUNS * 32, 0, ctx->stream>>>(m, args);
+    }
     VPP_CHECK_LAUNCH(ctx);
-    k_v2_tietree<<<ctx->sm_count * 2, V2_TIE_RUNS * 32, 0, ctx->stream>>>(m, args);
-    VPP_CHECK_LAUNCH(ctx);
-    return full_resolve_launch(ctx, args, 0, 1);
+    return full_resolve_launch(ctx, args, 0, est);
 }
 
 }  // namespace vppgpu

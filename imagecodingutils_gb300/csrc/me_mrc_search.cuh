@@ -219,16 +219,18 @@ __device__ __forceinline__ int quarter(const Lattice& L, int qr, int qc, int sy,
 // ---------------------------------------------------------------------------
 constexpr int TIE_L2 = 1, TIE_L1 = 2, TIE_L0 = 4;
 
+
 // A search decides ties only with the prediction's vectors at the levels
-// where its own trajectory met them, so a search made for rounded level-0
-// prediction (ex, ey) whose trajectory tied at levels `tie` has the same
-// trajectory, and result, for every prediction (p0x, p0y) with the same
-// vectors at those levels (level 1 and 2 vectors are level 0 halved).
-__device__ __forceinline__ bool search_reusable(int tie, int ex, int ey, int p0x, int p0y)
+// where its own trajectory met them, so a search made for prediction
+// (ex, ey) whose trajectory tied at levels `tie` has the same trajectory, and
+// result, for every prediction with the same vectors at those levels.
+__device__ __forceinline__ int level_pred(int est, int p, int lvl);
+__device__ __forceinline__ bool search_reusable(int est, int tie, int ex, int ey, int px, int py)
 {
-    if ((tie & TIE_L0) && (ex != p0x || ey != p0y)) return false;
-    if ((tie & TIE_L1) && (ex / 2 != p0x / 2 || ey / 2 != p0y / 2)) return false;
-    if ((tie & TIE_L2) && (ex / 2 / 2 != p0x / 2 / 2 || ey / 2 / 2 != p0y / 2 / 2)) return false;
+    for (int l = 0; l < 3; l++)
+        if ((tie & (TIE_L0 >> l)) &&
+            (level_pred(est, ex, l) != level_pred(est, px, l) || level_pred(est, ey, l) != level_pred(est, py, l)))
+            return false;
     return true;
 }
 
@@ -433,6 +435,168 @@ __device__ MbSearch search_mb_with(const MrcArgs& a, Lattice& LT, int mbr, int m
     return out;
 }
 
+// The search of MotionEstimatorH264ImplMultires (…Multires.cpp:644-906): full
+// searches at level 2 (+-(range/16 - 1)) and level 1 (+-2 after level 2, else
+// +-range/8), +-2 at level 0, half and quarter pel in the MultiresCross-style
+// window; LessThan distortions, which decide exactly as full SSDs do.  Each
+// integer level evaluates 32 candidates at a time, one per lane, then every
+// lane applies them in raster order (the same decisions in every lane).
+template <typename Skip>
+__device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int mbc, Skip&& skip, int lane, bool& bad)
+{
+    const int m = 16 * mbr, n = 16 * mbc, p = 8 * mbr, q = 8 * mbc, kk = 4 * mbr, ll = 4 * mbc;
+    const int w1 = a.W / 2, h1 = a.H / 2, w2 = w1 / 2, h2 = h1 / 2;
+    const int l1_range = a.motion_range / 8, l2_range = l1_range / 2;
+    const int lcl_l1_range = a.mode == 2 ? 2 : l1_range;
+    const Level L0{16, a.W, a.H, a.motion_range / 4}, L1{8, w1, h1, l1_range}, L2{4, w2, h2, l2_range};
+    constexpr int SX[8] = {-1, 0, 1, -1, 1, -1, 0, 1}, SY[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+    MbSearch out;
+    out.tie = 0;
+    const Org oin0 = origin(a.in0, 16, 16, 0, n, m);
+    out.zero_d = full_ssd(a.in0, oin0, a.e0, origin(a.e0, 16, 16, 19, n, m), 16, lane, bad);
+    int mx = 0, my = 0, xl, xr, yu, yd;
+
+    // one lane's SSD of an N x N block against the reference copy at origin o
+    auto lane_ssd = [&](const Buf& in, Org oi, const Buf& e, Org o, int N) {
+        int acc = 0;
+        for (int r = 0; r < N; r++)
+            for (int c = 0; c < N; c++) {
+                const int d = rd(in, oi.y + r, oi.x + c, bad) - rd(e, o.y + r, o.x + c, bad);
+                acc += d * d;
+            }
+        return acc;
+    };
+    // candidates (i, j) of [yu, yd] x [xl, xr] in raster order, (0, 0) skipped,
+    // 32 at a time; apply(i, j, d) in every lane in order
+    auto scan = [&](auto&& dist, auto&& apply) {
+        const int wdt = xr - xl + 1, cnt = (wdt > 0 && yd >= yu) ? (yd - yu + 1) * wdt : 0;
+        for (int base = 0; base < cnt; base += 32) {
+            const int c = base + lane;
+            int d = 0;
+            if (c < cnt) {
+                const int i = yu + c / wdt, j = xl + c % wdt;
+                if (i || j) d = dist(i, j);
+            }
+            const int lim = cnt - base < 32 ? cnt - base : 32;
+            for (int t = 0; t < lim; t++) {
+                const int dt = __shfl_sync(0xffffffffu, d, t);
+                const int cc = base + t, i = yu + cc / wdt, j = xl + cc % wdt;
+                if (i || j) apply(i, j, dt);
+            }
+        }
+    };
+
+    if (a.mode == 2) {  // level 2 full search around (0, 0) (…Multires.cpp:667-731)
+        const Org oin2 = origin(a.in2, 4, 4, 0, ll, kk);
+        int min2 = full_ssd(a.in2, oin2, a.e2, origin(a.e2, 4, 4, 5, ll, kk), 4, lane, bad);
+        mr_range(L2, ll, kk, 0, 0, l2_range - 1, xl, xr, yu, yd);
+        scan([&](int i, int j) { return lane_ssd(a.in2, oin2, a.e2, origin(a.e2, 4, 4, 5, ll + j, kk + i), 4); },
+             [&](int i, int j, int d) {
+                 if (d > min2) return;
+                 if (d == min2) {
+                     out.tie |= TIE_L2;
+                     if (skip(2, 0, 0, mx, my, j, i)) return;
+                 }
+                 min2 = d;
+                 mx = j;
+                 my = i;
+             });
+        mx <<= 1;
+        my <<= 1;
+    }
+
+    // level 1 around (mx, my) (…Multires.cpp:735-790)
+    const Org oin1 = origin(a.in1, 8, 8, 0, q, p);
+    int min1 = full_ssd(a.in1, oin1, a.e1, origin(a.e1, 8, 8, 9, mx + q, my + p), 8, lane, bad);
+    int rmx = 0, rmy = 0;
+    mr_range(L1, q, p, mx, my, lcl_l1_range, xl, xr, yu, yd);
+    scan([&](int i, int j) { return lane_ssd(a.in1, oin1, a.e1, origin(a.e1, 8, 8, 9, j + mx + q, i + my + p), 8); },
+         [&](int i, int j, int d) {
+             if (d > min1) return;
+             if (d == min1) {
+                 out.tie |= TIE_L1;
+                 if (skip(1, mx, my, rmx, rmy, j, i)) return;
+             }
+             min1 = d;
+             rmx = j;
+             rmy = i;
+         });
+    mx = (mx + rmx) * 2;
+    my = (my + rmy) * 2;
+
+    // level 0 +-2 (…Multires.cpp:792-849)
+    int min_d = full_ssd(a.in0, oin0, a.e0, origin(a.e0, 16, 16, 19, n + mx, m + my), 16, lane, bad);
+    rmx = rmy = 0;
+    mr_range(L0, n, m, mx, my, 2, xl, xr, yu, yd);
+    scan([&](int i, int j) {
+             return lane_ssd(a.in0, oin0, a.e0, origin(a.e0, 16, 16, 19, n + mx + j, m + my + i), 16);
+         },
+         [&](int i, int j, int d) {
+             if (d > min_d) return;
+             if (d == min_d) {
+                 out.tie |= TIE_L0;
+                 if (skip(0, mx, my, rmx, rmy, j, i)) return;
+             }
+             min_d = d;
+             rmx = j;
+             rmy = i;
+         });
+    mx += rmx;
+    my += rmy;
+    int mvx = mx * 4, mvy = my * 4;
+
+    // half then quarter pel (…Multires.cpp:851-917), strict improvements, full distortions
+    int r0, c0;
+    phase_coords<16>(lane, r0, c0);
+    int cur0[8];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) cur0[4 * i + j] = rd(a.in0, oin0.y + r0 + 4 * i, oin0.x + c0 + 4 * j, bad);
+    build_lattice<false>(LT, a.e0, origin(a.e0, 16, 16, 19, n + mx, m + my), lane, bad);
+    int hmx = 0, hmy = 0;
+    for (int c = 0; c < 8; c++) {
+        const int qx = 2 * SX[c], qy = 2 * SY[c];
+        int acc = 0;
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int d = cur0[4 * i + j] - lat(LT, 12 + qy + 4 * (r0 + 4 * i), 12 + qx + 4 * (c0 + 4 * j));
+                acc += d * d;
+            }
+        const int d = warp_sum(acc);
+        if (d < min_d) {
+            min_d = d;
+            hmx = qx;
+            hmy = qy;
+        }
+    }
+    int qmx = hmx, qmy = hmy;
+    for (int c = 0; c < 8; c++) {
+        int acc = 0;
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int d = cur0[4 * i + j] -
+                              quarter(LT, 12 + hmy + 4 * (r0 + 4 * i), 12 + hmx + 4 * (c0 + 4 * j), SY[c], SX[c]);
+                acc += d * d;
+            }
+        const int d = warp_sum(acc);
+        if (d < min_d) {
+            min_d = d;
+            qmx = hmx + SX[c];
+            qmy = hmy + SY[c];
+        }
+    }
+    __syncwarp();
+    out.min_d = min_d;
+    out.mvx = mvx + qmx;
+    out.mvy = mvy + qmy;
+    return out;
+}
+
 // MultiresCross's tie rules: at level 2 the centre against the offset
 // (…MultiresCross.cpp:673-679), elsewhere distances from (0, 0) (…:741-746, 857).
 __device__ __forceinline__ MbSearch search_mb_mrc(const MrcArgs& a, Lattice& LT, int mbr, int mbc, int lane,
@@ -443,14 +607,37 @@ __device__ __forceinline__ MbSearch search_mb_mrc(const MrcArgs& a, Lattice& LT,
     }, lane, bad);
 }
 
-// Ver2's: distances from the prediction's vector at the level, pl = {level-2
-// x, y, level-1 x, y, level-0 rounded x, y} (…MultiresCrossVer2.cpp:627-642).
-__device__ __forceinline__ MbSearch search_mb_ver2(const MrcArgs& a, Lattice& LT, int mbr, int mbc, const int* pl,
-                                                   int lane, bool& bad)
+// The prediction's vector at a pyramid level (quarter-pel component p):
+// Ver2 rounds to level 0 and halves (…MultiresCrossVer2.cpp:627-642),
+// Multires rounds to every level (…Multires.cpp:646-655).
+constexpr int EST_VER2 = 1, EST_MULTIRES = 2;
+__device__ __forceinline__ int level_pred(int est, int p, int lvl)
 {
-    return search_mb_with<true>(a, LT, mbr, mbc, [pl](int lvl, int mx, int my, int rmx, int rmy, int j, int i) {
-        return farther(mx, my, rmx, rmy, j, i, pl[4 - 2 * lvl], pl[5 - 2 * lvl]);
-    }, lane, bad);
+    if (est == EST_MULTIRES) {
+        const int h = 2 << lvl;  // 2, 4, 8
+        return p < 0 ? (p - h) / (2 * h) : (p + h) / (2 * h);
+    }
+    int v = p < 0 ? (p - 2) / 4 : (p + 2) / 4;
+    for (int l = 0; l < lvl; l++) v /= 2;
+    return v;
+}
+
+// Search of a predictor estimator (est) with ties decided by the distances
+// from prediction (px, py) at each level.
+template <int kEst>
+__device__ __forceinline__ MbSearch search_pred(const MrcArgs& a, Lattice& LT, int mbr, int mbc, int px, int py,
+                                                int lane, bool& bad)
+{
+    int pl[6];
+    for (int l = 0; l < 3; l++) {
+        pl[2 * l] = level_pred(kEst, px, l);
+        pl[2 * l + 1] = level_pred(kEst, py, l);
+    }
+    auto skip = [&pl](int lvl, int mx, int my, int rmx, int rmy, int j, int i) {
+        return farther(mx, my, rmx, rmy, j, i, pl[2 * lvl], pl[2 * lvl + 1]);
+    };
+    if constexpr (kEst == EST_MULTIRES) return search_mr_with(a, LT, mbr, mbc, skip, lane, bad);
+    else return search_mb_with<true>(a, LT, mbr, mbc, skip, lane, bad);
 }
 
 // Tie tree of a Ver2 macroblock: run r of eight decides its t-th tie (t < 3)
@@ -468,12 +655,13 @@ struct V2TieRun {
     int pad;
 };
 
-__device__ __forceinline__ MbSearch search_mb_run(const MrcArgs& a, Lattice& LT, int mbr, int mbc, int run,
-                                                  V2TieRun* rec, int lane, bool& bad)
+template <int kEst>
+__device__ __forceinline__ MbSearch search_run(const MrcArgs& a, Lattice& LT, int mbr, int mbc, int run,
+                                               V2TieRun* rec, int lane, bool& bad)
 {
     int t = 0, lvls = 0, geo[V2_TIE_BITS] = {0, 0, 0};
     bool wide = false;
-    const MbSearch r = search_mb_with<true>(a, LT, mbr, mbc, [&](int lvl, int mx, int my, int rmx, int rmy, int j, int i) {
+    auto skip = [&](int lvl, int mx, int my, int rmx, int rmy, int j, int i) {
         const int cx = mx + rmx, cy = my + rmy, nx = mx + j, ny = my + i;
         const bool take = t < V2_TIE_BITS ? ((run >> t) & 1) : true;
         if (t < V2_TIE_BITS) {
@@ -484,7 +672,10 @@ __device__ __forceinline__ MbSearch search_mb_run(const MrcArgs& a, Lattice& LT,
         }
         t++;
         return !take;
-    }, lane, bad);
+    };
+    MbSearch r;
+    if constexpr (kEst == EST_MULTIRES) r = search_mr_with(a, LT, mbr, mbc, skip, lane, bad);
+    else r = search_mb_with<true>(a, LT, mbr, mbc, skip, lane, bad);
     if (lane == 0) {
         for (int e = 0; e < V2_TIE_BITS; e++) rec->geo[e] = geo[e];
         rec->lvl = lvls;
@@ -495,9 +686,9 @@ __device__ __forceinline__ MbSearch search_mb_run(const MrcArgs& a, Lattice& LT,
     return r;
 }
 
-// The searched vector and distortion of a tie MB for rounded level-0
-// prediction (p0x, p0y) from its tie tree; false when the tree is too deep.
-__device__ __forceinline__ bool tie_tree_result(const V2TieRun* runs, int p0x, int p0y, int* mv, int* min_d)
+// The searched vector and distortion of a tie MB for prediction (px, py)
+// from its tie tree; false when the tree is too deep.
+__device__ __forceinline__ bool tie_tree_result(int est, const V2TieRun* runs, int ppx, int ppy, int* mv, int* min_d)
 {
     int run = 0;
     for (int t = 0; t < V2_TIE_BITS; t++) {
@@ -507,8 +698,7 @@ __device__ __forceinline__ bool tie_tree_result(const V2TieRun* runs, int p0x, i
         const int g = __ldcg(&r.geo[t]), lvl = (__ldcg(&r.lvl) >> (2 * t)) & 3;
         const int cx = (signed char)(g & 0xff), cy = (signed char)((g >> 8) & 0xff);
         const int nx = (signed char)((g >> 16) & 0xff), ny = (signed char)(g >> 24);
-        const int px = lvl == 2 ? p0x / 2 / 2 : (lvl == 1 ? p0x / 2 : p0x);
-        const int py = lvl == 2 ? p0y / 2 / 2 : (lvl == 1 ? p0y / 2 : p0y);
+        const int px = level_pred(est, ppx, lvl), py = level_pred(est, ppy, lvl);
         const bool skip = (cy - py) * (cy - py) + (cx - px) * (cx - px) < (ny - py) * (ny - py) + (nx - px) * (nx - px);
         run |= (skip ? 0 : 1) << t;
     }

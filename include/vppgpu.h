@@ -117,7 +117,7 @@ int vppgpu_me_last_status(vppgpu_me* me);
 /* Number of resolve sweeps the last estimate needed (predictor fixed point). */
 int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps);
 
-/* Full and MultiresCrossVer2, no vpp counterpart: relaxation sweeps (0..8,
+/* Estimators with a predictor, no vpp counterpart: relaxation sweeps (0..8,
  * default 8) run before the exact wavefront decides the macroblocks whose
  * predictions have not settled.  Results do not depend on it. */
 int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps);

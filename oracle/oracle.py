@@ -52,6 +52,7 @@ class Oracle:
         L.vo_me_full_intpel.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P]
         L.vo_me_multires_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.vo_me_multires_cross_v2.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
+        L.vo_me_multires.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_quarter_read16.argtypes = [_P, _I, _I, _I, _I, _I, _I, _P]
         L.vo_half.argtypes = [_P, _I, _I, _P]
         L.vo_fwd4x4.argtypes = [_P, _I, _I, _I, _I, _I]
@@ -101,8 +102,15 @@ class Oracle:
             raise ValueError(f"vo_me_multires_cross rc={rc}")
         return mv, dist, avg.value
 
+    def me_multires(self, src, ref, motion_range, mode=1, dist_incl=None, slice_map=None, with_ties=False):
+        return self._me_pred(self.lib.vo_me_multires, src, ref, motion_range, mode, dist_incl, slice_map, with_ties)
+
     def me_multires_cross_v2(self, src, ref, motion_range, mode=1, dist_incl=None, slice_map=None,
                              with_ties=False):
+        return self._me_pred(self.lib.vo_me_multires_cross_v2, src, ref, motion_range, mode, dist_incl, slice_map,
+                             with_ties)
+
+    def _me_pred(self, fn, src, ref, motion_range, mode, dist_incl, slice_map, with_ties):
         h, w = src.shape
         src = np.ascontiguousarray(src, dtype=np.int16)
         ref = np.ascontiguousarray(ref, dtype=np.int16)
@@ -113,10 +121,10 @@ class Oracle:
         avg = _L(0)
         incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
         sl = None if slice_map is None else np.ascontiguousarray(slice_map, dtype=np.int32)
-        rc = self.lib.vo_me_multires_cross_v2(_ptr(src), _ptr(ref), w, h, motion_range, mode, _ptr(incl),
-                                              _ptr(sl), _ptr(mv), _ptr(dist), C.byref(avg), _ptr(ties))
+        rc = fn(_ptr(src), _ptr(ref), w, h, motion_range, mode, _ptr(incl), _ptr(sl), _ptr(mv), _ptr(dist),
+                C.byref(avg), _ptr(ties))
         if rc:
-            raise ValueError(f"vo_me_multires_cross_v2 rc={rc}")
+            raise ValueError(f"{fn.__name__} rc={rc}")
         return (mv, dist, avg.value, ties) if with_ties else (mv, dist, avg.value)
 
     def me_full_intpel(self, src, ref, motion_range, metric=1):

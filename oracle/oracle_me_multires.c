@@ -6,6 +6,8 @@
  *     (src/CodecUtils/MotionEstimatorH264ImplMultiresCross.cpp:525-1019)
  *   MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*)
  *     (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:537-1151)
+ *   MotionEstimatorH264ImplMultires::Estimate
+ *     (src/CodecUtils/MotionEstimatorH264ImplMultires.cpp:557-1024)
  *
  * The reference works on extended-boundary copies of each pyramid level
  * (borders 19 / 9 / 5 samples for levels 0 / 1 / 2), addresses them through
@@ -521,6 +523,118 @@ int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int m
     return rc;
 }
 
+/* The search of MotionEstimatorH264ImplMultires::Estimate
+ * (src/CodecUtils/MotionEstimatorH264ImplMultires.cpp:644-917) for macroblock
+ * (mbr, mbc): full searches at level 2 (around (0, 0)) and level 1 (around
+ * the level-2 winner), +-2 at level 0, then half and quarter pel in the
+ * MultiresCross-style window.  Its LessThan distortions (…:701, 764, 822, 873,
+ * 899) stop early only on a sum above the running minimum, so full SSDs give
+ * the same decisions.  Ties are measured from the prediction rounded to each
+ * level, pl = {level-2 x, y, level-1 x, y, level-0 x, y} (…:646-655). */
+static void mr_search_mb_multires(mr_ctx* c, int mbr, int mbc, const int* pl, mr_result* out)
+{
+    const int m = 16 * mbr, n = 16 * mbc, p = 8 * mbr, q = 8 * mbc, kk = 4 * mbr, ll = 4 * mbc;
+    mr_ov oin0 = {&c->in0, 16, 16, 0, 0, 0, 0}, oin1 = {&c->in1, 8, 8, 0, 0, 0, 0}, oin2 = {&c->in2, 4, 4, 0, 0, 0, 0};
+    mr_ov oe0 = {&c->e0, 16, 16, 0, 0, 19, 19}, oe1 = {&c->e1, 8, 8, 0, 0, 9, 9}, oe2 = {&c->e2, 4, 4, 0, 0, 5, 5};
+    int mx = 0, my = 0, rmx = 0, rmy = 0, hmx = 0, hmy = 0, qmx, qmy, xl, xr, yu, yd, tie = 0;
+    short blk[256];
+    ov_origin(&oin0, n, m);
+    ov_origin(&oe0, n, m);
+    const int zero_d = ov_tsd(&oin0, &oe0, 16);
+
+    if (c->mode == 2) { /* level 2 full search (…:667-731) */
+        ov_origin(&oin2, ll, kk);
+        ov_origin(&oe2, ll, kk);
+        int min2 = ov_tsd(&oin2, &oe2, 4);
+        mr_range(&c->L2, ll, kk, 0, 0, c->l2_range - 1, &xl, &xr, &yu, &yd);
+        for (int i = yu; i <= yd; i++)
+            for (int j = xl; j <= xr; j++) {
+                if (!(i || j)) continue;
+                ov_origin(&oe2, ll + j, kk + i);
+                int d = ov_tsd(&oin2, &oe2, 4);
+                if (d > min2) continue;
+                if (d == min2) {
+                    tie |= 1;
+                    if (mr_farther(0, 0, mx, my, j, i, pl[0], pl[1])) continue;
+                }
+                min2 = d;
+                mx = j;
+                my = i;
+            }
+        mx <<= 1;
+        my <<= 1;
+    }
+
+    /* level 1 around (mx, my) (…:735-790) */
+    ov_origin(&oin1, q, p);
+    ov_origin(&oe1, mx + q, my + p);
+    int min1 = ov_tsd(&oin1, &oe1, 8);
+    mr_range(&c->L1, q, p, mx, my, c->lcl_l1_range, &xl, &xr, &yu, &yd);
+    for (int i = yu; i <= yd; i++)
+        for (int j = xl; j <= xr; j++) {
+            if (!(i || j)) continue;
+            ov_origin(&oe1, j + mx + q, i + my + p);
+            int d = ov_tsd(&oin1, &oe1, 8);
+            if (d > min1) continue;
+            if (d == min1) {
+                tie |= 2;
+                if (mr_farther(mx, my, rmx, rmy, j, i, pl[2], pl[3])) continue;
+            }
+            min1 = d;
+            rmx = j;
+            rmy = i;
+        }
+    mx = (mx + rmx) * 2;
+    my = (my + rmy) * 2;
+
+    /* level 0 +-2 (…:792-849) */
+    ov_origin(&oe0, n + mx, m + my);
+    int min_d = ov_tsd(&oin0, &oe0, 16);
+    rmx = rmy = 0;
+    mr_range(&c->L0, n, m, mx, my, 2, &xl, &xr, &yu, &yd);
+    for (int i = yu; i <= yd; i++)
+        for (int j = xl; j <= xr; j++) {
+            if (!(i || j)) continue;
+            ov_origin(&oe0, n + mx + j, m + my + i);
+            int d = ov_tsd(&oin0, &oe0, 16);
+            if (d > min_d) continue;
+            if (d == min_d) {
+                tie |= 4;
+                if (mr_farther(mx, my, rmx, rmy, j, i, pl[4], pl[5])) continue;
+            }
+            min_d = d;
+            rmx = j;
+            rmy = i;
+        }
+    mx += rmx;
+    my += rmy;
+    int mvx = mx << 2, mvy = my << 2;
+
+    /* half then quarter pel (…:851-917), strict improvements */
+    ov_origin(&oe0, n + mx, m + my);
+    mr_load_half_window(c->win, &oe0, 0);
+    for (int k = 0; k < 8; k++) {
+        int qx = 2 * SUBX[k], qy = 2 * SUBY[k];
+        mr_window_read(c->win, qx, qy, blk);
+        int d = vo_tsd16(oin0.b->mem + (size_t)oin0.y * oin0.b->w + oin0.x, oin0.b->w, blk, 16);
+        if (d < min_d) { min_d = d; hmx = qx; hmy = qy; }
+    }
+    qmx = hmx;
+    qmy = hmy;
+    mr_load_quarter_window(c->win, hmx, hmy);
+    for (int k = 0; k < 8; k++) {
+        int qx = hmx + SUBX[k], qy = hmy + SUBY[k];
+        mr_window_read(c->win, qx, qy, blk);
+        int d = vo_tsd16(oin0.b->mem + (size_t)oin0.y * oin0.b->w + oin0.x, oin0.b->w, blk, 16);
+        if (d < min_d) { min_d = d; qmx = qx; qmy = qy; }
+    }
+    out->zero_d = zero_d;
+    out->min_d = min_d;
+    out->mvx = mvx + qmx;
+    out->mvy = mvy + qmy;
+    out->tie = tie;
+}
+
 /* MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*)
  * (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:537-1151): the
  * MultiresCross search with ties resolved towards the rounded median
@@ -532,8 +646,8 @@ int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int m
  * predictor for an index past its array for it.  tie_out (nullable): per MB,
  * the integer stages that met an equal distortion (1 level 2, 2 level 1,
  * 4 level 0; the search then depends on the prediction). */
-int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, int motion_range, int mode,
-                            const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist,
+static int me_multires_pred(int multires, const short* src, const short* ref, int w, int h, int motion_range,
+                            int mode, const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist,
                             long* avg_dist, int* tie_out)
 {
     if (!src || !ref || !mv_out || w < 16 || h < 16 || (w % 16) != 0) return -1;
@@ -557,9 +671,17 @@ int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, in
             const int pxq = px % 4, pyq = py % 4;
             int px0 = px / 4, py0 = py / 4;
             const int px0r = px < 0 ? (px - 2) / 4 : (px + 2) / 4, py0r = py < 0 ? (py - 2) / 4 : (py + 2) / 4;
-            const int pl[6] = {px0r / 2 / 2, py0r / 2 / 2, px0r / 2, py0r / 2, px0r, py0r};
             mr_result r;
-            mr_search_mb(&c, mbr, mbc, pl, &r);
+            if (multires) {
+                /* Multires rounds to every level (…Multires.cpp:646-655) */
+                const int pl[6] = {px < 0 ? (px - 8) / 16 : (px + 8) / 16, py < 0 ? (py - 8) / 16 : (py + 8) / 16,
+                                   px < 0 ? (px - 4) / 8 : (px + 4) / 8,   py < 0 ? (py - 4) / 8 : (py + 4) / 8,
+                                   px0r, py0r};
+                mr_search_mb_multires(&c, mbr, mbc, pl, &r);
+            } else {
+                const int pl[6] = {px0r / 2 / 2, py0r / 2 / 2, px0r / 2, py0r / 2, px0r, py0r};
+                mr_search_mb(&c, mbr, mbc, pl, &r);
+            }
             if (tie_out) tie_out[k] = r.tie;
 
             /* pred-vector check, clamped to one macroblock outside (…:1008-1045) */
@@ -582,7 +704,7 @@ int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, in
             /* Fifo after pushing zero, pred, best (…:1047-1050) */
             int xs[5] = {r.mvx, px, 0, 0, 0}, ys[5] = {r.mvy, py, 0, 0, 0};
             int ds[5] = {r.min_d, pd, r.zero_d, r.zero_d, r.zero_d};
-            const int pos = vo_best_vector5(xs, ys, ds, 0.9, 256.0, px, py);
+            const int pos = vo_best_vector5(xs, ys, ds, multires ? 1.1 : 0.9, 256.0, px, py);
             if (dist_incl && dist_incl[k]) {
                 included++;
                 total += ds[pos];
@@ -598,4 +720,24 @@ int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, in
     }
     mr_ctx_free(&c);
     return rc;
+}
+
+int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                            const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist,
+                            long* avg_dist, int* tie_out)
+{
+    return me_multires_pred(0, src, ref, w, h, motion_range, mode, dist_incl, slice, mv_out, mb_dist, avg_dist,
+                            tie_out);
+}
+
+/* MotionEstimatorH264ImplMultires::Estimate (src/CodecUtils/MotionEstimatorH264ImplMultires.cpp:557-1024):
+ * the search above with the prediction rounded to each level, the pred-vector
+ * check and GetBestVector with lambda 1.1 (…:958).  Full macroblock rows only,
+ * as for Ver2. */
+int vo_me_multires(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                   const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist, long* avg_dist,
+                   int* tie_out)
+{
+    return me_multires_pred(1, src, ref, w, h, motion_range, mode, dist_incl, slice, mv_out, mb_dist, avg_dist,
+                            tie_out);
 }

@@ -87,6 +87,15 @@ int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, in
                             const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist,
                             long* avg_dist, int* tie_out);
 
+/* MotionEstimatorH264ImplMultires::Estimate
+ * (src/CodecUtils/MotionEstimatorH264ImplMultires.cpp:557-1024): full searches
+ * at levels 2 and 1, +-2 at level 0, sub-pel in the MultiresCross-style
+ * window, ties towards the prediction rounded to each level, the pred-vector
+ * check and GetBestVector (lambda 1.1).  Arguments as for Ver2. */
+int vo_me_multires(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                   const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist, long* avg_dist,
+                   int* tie_out);
+
 /* OverlayMem2Dv2::QuarterRead (src/ImageUtils/OverlayMem2Dv2.cpp:704-1052) of
  * a 16x16 block whose full-pel origin is (x, y) in a frame extended by edge
  * replication, at quarter offsets (qx, qy) in -3..3. */

@@ -15,6 +15,7 @@ inputs and stores inputs and outputs:
 * me_mrc2.npz     MotionEstimatorH264ImplMultiresCrossVer2 vectors and
                   avgDistortion, modes 0/1/2, with and without
                   pDistortionIncluded (pan and integer-shift content)
+* me_mr.npz       MotionEstimatorH264ImplMultires, the same cases as me_mrc2
 * transform.npz   FastForward4x4ITImpl1 / Impl2 / On16x16 levels and
                   FastInverse4x4ITImpl1 / On16x16 reconstructions over QP 0..51,
                   intra and inter, modes 0/1/2, a custom SetScale, and
@@ -22,7 +23,7 @@ inputs and stores inputs and outputs:
 * colour.npz      the three RGB24->YUV420 converters, flip and chroma offsets
 
 Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
-names: me_full me_mrc me_mrc2 transform colour, default all)
+names: me_full me_mrc me_mrc2 me_mr transform colour, default all)
 """
 from __future__ import annotations
 
@@ -110,7 +111,7 @@ MRC2_CASES = [  # (name, w, h, motion_range, seed, generator)
 ]
 
 
-def mrc2_fixtures(ref: oracle.Reference) -> dict:
+def mrc2_fixtures(ref: oracle.Reference, kind: str = "multires_cross_v2") -> dict:
     out = {}
     for name, w, h, mr, seed, gen in MRC2_CASES:
         fr = (synth.shift_sequence if gen == "shift" else synth.pan_sequence)(seed, w, h, 2)
@@ -122,8 +123,8 @@ def mrc2_fixtures(ref: oracle.Reference) -> dict:
         out[f"{name}_meta"] = np.array([w, h, mr], np.int32)
         out[f"{name}_incl"] = incl
         for mode in (0, 1, 2):
-            mv, avg = ref.me("multires_cross_v2", src, rf, mr, mode=mode)
-            mvi, avgi = ref.me("multires_cross_v2", src, rf, mr, mode=mode, dist_incl=incl)
+            mv, avg = ref.me(kind, src, rf, mr, mode=mode)
+            mvi, avgi = ref.me(kind, src, rf, mr, mode=mode, dist_incl=incl)
             assert np.array_equal(mv, mvi) and avg == 0
             out[f"{name}_m{mode}_mv"] = mv
             out[f"{name}_m{mode}_avg"] = np.array([avgi], np.int64)
@@ -179,6 +180,7 @@ def main() -> None:
     oracle.build(with_reference=True)
     ref = oracle.Reference()
     makers = {"me_full": me_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
+              "me_mr": lambda r: mrc2_fixtures(r, "multires"),
               "transform": transform_fixtures, "colour": colour_fixtures}
     names = sys.argv[1:] or list(makers)
     for name in names:

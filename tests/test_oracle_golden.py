@@ -167,3 +167,31 @@ def test_me_multires_cross_v2_flat_content_ties(orc):
         mv_o, _, _, ties = orc.me_multires_cross_v2(b, a, 128, mode=mode, with_ties=True)
         np.testing.assert_array_equal(mv_o, mv_r)
         assert ties.sum() > 0
+
+
+@pytest.mark.parametrize("case", MRC2_CASES)
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_me_multires_matches_reference(orc, golden, case, mode):
+    g = golden("me_mr.npz")
+    w, h, mr = (int(v) for v in g[f"{case}_meta"])
+    src = g[f"{case}_src"].astype(np.int16)
+    ref = g[f"{case}_ref"].astype(np.int16)
+    mv, _, avg = orc.me_multires(src, ref, mr, mode=mode)
+    np.testing.assert_array_equal(mv, g[f"{case}_m{mode}_mv"])
+    assert avg == 0
+    mvi, _, avgi = orc.me_multires(src, ref, mr, mode=mode, dist_incl=g[f"{case}_incl"])
+    np.testing.assert_array_equal(mvi, mv)
+    assert avgi == int(g[f"{case}_m{mode}_avg"][0])
+
+
+@ref_available
+@pytest.mark.parametrize("seed,w,h,mr,mode", [(56, 176, 144, 128, 0), (57, 352, 288, 128, 1), (58, 208, 120, 96, 2),
+                                              (59, 640, 360, 128, 0)])
+def test_me_multires_against_compiled_reference(orc, seed, w, h, mr, mode):
+    ref_lib = oracle_mod.Reference()
+    fr = synth.pan_sequence(seed, w, h, 2)
+    incl = (synth.splitmix64(seed, (w // 16) * (h // 16)) & np.uint64(1)).astype(np.uint8)
+    mv_r, avg_r = ref_lib.me("multires", fr[1], fr[0], mr, mode=mode, dist_incl=incl)
+    mv_o, _, avg_o = orc.me_multires(fr[1], fr[0], mr, mode=mode, dist_incl=incl)
+    np.testing.assert_array_equal(mv_o, mv_r)
+    assert avg_o == avg_r
