@@ -320,9 +320,11 @@ def run_serving(args, vpp, torch, ctx, bases):
 
 
 MULTIRES = {  # kind -> (class name, oracle method)
+    "multires": ("MotionEstimatorH264ImplMultires", "me_multires"),
     "multires_cross": ("MotionEstimatorH264ImplMultiresCross", "me_multires_cross"),
     "multires_cross_v2": ("MotionEstimatorH264ImplMultiresCrossVer2", "me_multires_cross_v2"),
 }
+MULTIRES_CODE = {"multires": 1, "multires_cross": 2, "multires_cross_v2": 3}  # VPPGPU_ME_*
 
 
 def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with_cpu, kind="multires_cross"):
@@ -330,7 +332,7 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
     sequence: device-resident MB/s over the frame rotation, and the oracle
     port on all host threads as its CPU baseline."""
     cls, ofn = MULTIRES[kind]
-    code = _lib.ME_MULTIRES_CROSS if kind == "multires_cross" else _lib.ME_MULTIRES_CROSS_V2
+    code = MULTIRES_CODE[kind]
     h = C.c_void_p()
     _lib.check(L.vppgpu_me_create(ctx.handle, code, W, H, MOTION_RANGE, C.byref(h)), "vppgpu_me_create")
     _lib.check(L.vppgpu_me_set_mode(h, 0), "vppgpu_me_set_mode")
@@ -358,7 +360,7 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
     ms = e0.elapsed_time(e1) / steps
     out = {"value": NMB / (ms * 1e-3), "unit": UNIT, "ms_per_frame": ms, "mode": mode.value,
            "workload": f"{cls} plain per-frame, {W}x{H}, motionRange {MOTION_RANGE}"}
-    if kind == "multires_cross_v2":
+    if kind != "multires_cross":
         # per-frame device time and how each frame's predictions were decided
         per, exact = [], 0
         for t in range(NFRAMES - 1):
@@ -658,6 +660,8 @@ def main():
         mrc = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu)
         mrc2 = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
                                   kind="multires_cross_v2")
+        mr = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
+                                kind="multires")
         pk, pk_kind = peaks()
         hbm_rows = run_hbm_paths(torch, _lib, L, ctx, stream, f"cuda:{local}", pk)
         line = {
@@ -682,7 +686,7 @@ def main():
             "hbm_peak_gbs": pk.get("hbm_gbs"), "peaks_source": pk_kind,
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
             "serving": serving,
-            "multires_cross": mrc, "multires_cross_v2": mrc2, **hbm_rows,
+            "multires": mr, "multires_cross": mrc, "multires_cross_v2": mrc2, **hbm_rows,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
