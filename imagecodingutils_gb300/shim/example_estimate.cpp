@@ -1,17 +1,20 @@
 // example_estimate.cpp -- how a vpp codec drives the GPU classes.
 //
-//   example_estimate <pair.bin> <width> <height> <motionRange> <out.bin>
+//   example_estimate <pair.bin> <width> <height> <motionRange> <out.bin> [estimator]
 //
 // pair.bin holds the source then the reference luma plane (int16).  The
-// program estimates with GpuMotionEstimatorH264ImplFull exactly as a codec
-// would with MotionEstimatorH264ImplFull (constructor, Create, Estimate,
-// predictor side effect), then runs the forward/inverse 4x4 transform classes
+// program estimates with GpuMotionEstimatorH264ImplFull (or, by the optional
+// last argument, ...Multires, ...MultiresCross or ...MultiresCrossVer2:
+// "multires", "mrc", "mrc2") exactly as a codec would with the vpp class
+// (constructor, Create, SetMode(0), Estimate, predictor side effect), then
+// runs the forward/inverse 4x4 transform classes
 // on the motion-compensated-free residual (source - reference) of the first
 // macroblock row.  out.bin receives: the vectors (N x 2 int16), avgDistortion
 // (int64), the predictor's copy of the vectors (N x 2 int32), then the
 // transformed residual levels and reconstruction (int16).
 #include <stdio.h>
 #include <stdlib.h>
+#include <string>
 #include <vector>
 
 #include "vppgpu_vpp.hpp"
@@ -27,10 +30,11 @@ public:
 
 int main(int argc, char** argv)
 {
-    if (argc != 6) {
-        fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin\n", argv[0]);
+    if (argc != 6 && argc != 7) {
+        fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin [full|multires|mrc|mrc2]\n", argv[0]);
         return 2;
     }
+    const std::string kind = argc == 7 ? argv[6] : "full";
     int w = atoi(argv[2]), h = atoi(argv[3]), range = atoi(argv[4]);
     std::vector<short> src((size_t)w * h), ref((size_t)w * h);
     FILE* f = fopen(argv[1], "rb");
@@ -42,11 +46,20 @@ int main(int argc, char** argv)
     for (int i = 0; i < nmb; i++) incl[i] = true;
 
     RecordingPredictor pred(nmb);
-    IMotionEstimator* me = new GpuMotionEstimatorH264ImplFull(src.data(), ref.data(), w, h, range, &pred, incl);
+    IMotionEstimator* me;
+    if (kind == "multires")
+        me = new GpuMotionEstimatorH264ImplMultires(src.data(), ref.data(), w, h, range, &pred, incl);
+    else if (kind == "mrc")
+        me = new GpuMotionEstimatorH264ImplMultiresCross(src.data(), ref.data(), w, h, range, incl);
+    else if (kind == "mrc2")
+        me = new GpuMotionEstimatorH264ImplMultiresCrossVer2(src.data(), ref.data(), w, h, range, &pred, incl);
+    else
+        me = new GpuMotionEstimatorH264ImplFull(src.data(), ref.data(), w, h, range, &pred, incl);
     if (!me->Create()) {
         fprintf(stderr, "Create failed\n");
         return 4;
     }
+    me->SetMode(0);
     long avg = 0;
     VectorStructList* vl = (VectorStructList*)me->Estimate(&avg);
     if (!vl) {

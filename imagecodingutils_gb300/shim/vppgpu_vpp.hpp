@@ -268,6 +268,53 @@ public:
     }
 };
 
+// The multi-resolution estimators, with the constructors of the reference
+// classes (…MultiresCross.h:77-88, …MultiresCrossVer2.cpp:111-153,
+// …Multires.cpp:107-171).  MultiresCross has no predictor; the reference's
+// Multires estimates only through its constructor with pMVPred.
+class GpuMotionEstimatorH264ImplMultiresCross : public GpuMotionEstimatorH264Base {
+public:
+    GpuMotionEstimatorH264ImplMultiresCross(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                            int motionRange)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_MULTIRES_CROSS, pSrc, pRef, imgWidth, imgHeight, motionRange, NULL,
+                                     NULL)
+    {
+    }
+    GpuMotionEstimatorH264ImplMultiresCross(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                            int motionRange, void* pDistortionIncluded)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_MULTIRES_CROSS, pSrc, pRef, imgWidth, imgHeight, motionRange, NULL,
+                                     pDistortionIncluded)
+    {
+    }
+};
+
+class GpuMotionEstimatorH264ImplMultiresCrossVer2 : public GpuMotionEstimatorH264Base {
+public:
+    GpuMotionEstimatorH264ImplMultiresCrossVer2(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                                int motionRange, IMotionVectorPredictor* pMVPred)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_MULTIRES_CROSS_V2, pSrc, pRef, imgWidth, imgHeight, motionRange,
+                                     pMVPred, NULL)
+    {
+    }
+    GpuMotionEstimatorH264ImplMultiresCrossVer2(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                                int motionRange, IMotionVectorPredictor* pMVPred,
+                                                void* pDistortionIncluded)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_MULTIRES_CROSS_V2, pSrc, pRef, imgWidth, imgHeight, motionRange,
+                                     pMVPred, pDistortionIncluded)
+    {
+    }
+};
+
+class GpuMotionEstimatorH264ImplMultires : public GpuMotionEstimatorH264Base {
+public:
+    GpuMotionEstimatorH264ImplMultires(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                       int motionRange, IMotionVectorPredictor* pMVPred, void* pDistortionIncluded)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_MULTIRES, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred,
+                                     pDistortionIncluded)
+    {
+    }
+};
+
 // ---------------------------------------------------------------------------
 // IForwardTransform / IInverseTransform replacements (FastForward4x4ITImpl1,
 // FastInverse4x4ITImpl1 and their On16x16 variants).  Transform(void*) takes

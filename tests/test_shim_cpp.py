@@ -33,7 +33,8 @@ def test_shim_compiles_against_vpp_interfaces():
 
 
 @pytest.mark.gpu
-def test_codec_style_program_on_gpu(tmp_path, vpp, orc):
+@pytest.mark.parametrize("kind", ["full", "multires", "mrc", "mrc2"])
+def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
     from imagecodingutils_gb300 import build
     exe = tmp_path / "example_estimate"
     r = subprocess.run(["g++", "-std=c++11", "-O2", "-I", SHIM, os.path.join(SHIM, "example_estimate.cpp"),
@@ -45,7 +46,7 @@ def test_codec_style_program_on_gpu(tmp_path, vpp, orc):
     pair = tmp_path / "pair.bin"
     pair.write_bytes(fr[1].astype(np.int16).tobytes() + fr[0].astype(np.int16).tobytes())
     out = tmp_path / "out.bin"
-    r = subprocess.run([str(exe), str(pair), str(w), str(h), str(mr), str(out)], capture_output=True, text=True)
+    r = subprocess.run([str(exe), str(pair), str(w), str(h), str(mr), str(out), kind], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     nmb = (w // 16) * (h // 16)
     raw = out.read_bytes()
@@ -55,10 +56,19 @@ def test_codec_style_program_on_gpu(tmp_path, vpp, orc):
     rest = np.frombuffer(raw[12 * nmb + 8:], np.int16)
     nblk = (w // 4) * 4
     levels, recon = rest[:16 * nblk], rest[16 * nblk:]
-    mv_o, _, avg_o = orc.me_full(fr[1], fr[0], mr, dist_incl=np.ones(nmb, np.uint8))
+    ones = np.ones(nmb, np.uint8)
+    if kind == "full":
+        mv_o, _, avg_o = orc.me_full(fr[1], fr[0], mr, dist_incl=ones)
+    elif kind == "multires":
+        mv_o, _, avg_o = orc.me_multires(fr[1], fr[0], mr, mode=0, dist_incl=ones)
+    elif kind == "mrc":
+        mv_o, _, avg_o = orc.me_multires_cross(fr[1], fr[0], mr, mode=0, dist_incl=ones)
+    else:
+        mv_o, _, avg_o = orc.me_multires_cross_v2(fr[1], fr[0], mr, mode=0, dist_incl=ones)
     np.testing.assert_array_equal(mv, mv_o)
     assert avg == avg_o
-    np.testing.assert_array_equal(pred, mv_o.astype(np.int32))
+    if kind != "mrc":  # MultiresCross has no predictor
+        np.testing.assert_array_equal(pred, mv_o.astype(np.int32))
     res = (fr[1][:16].astype(np.int32) - fr[0][:16]).astype(np.int16)
     blocks = res.reshape(4, 4, w // 4, 4).transpose(0, 2, 1, 3).reshape(-1, 16)
     lev_o = orc.fwd4x4(blocks, 0, 0, 28, 0)
