@@ -171,8 +171,7 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
     }
     __syncthreads();
 
-    // 2. template energy; horizontal 16-sample window energies in 16-column
-    //    runs (task: window row r, run jb)
+    // 2. template energy
     if (tid < 32) {
         int acc = 0;
 #pragma unroll
@@ -183,48 +182,19 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
         acc = warp_sum(acc);
         if (tid == 0) S.a2 = acc;
     }
-    for (int task = tid; task < 78 * 4; task += 128) {
-        const int jb = task / 78, r = task - jb * 78;  // consecutive threads: consecutive rows
-        const uint4* p = reinterpret_cast<const uint4*>(&S.win[r][16 * jb]);
-        const uint4 q0 = p[0], q1 = p[1];
-        const unsigned wv[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
-        auto px = [&](int x) { return (int)((wv[x >> 2] >> (8 * (x & 3))) & 0xffu); };
-        int sum = 0;
-#pragma unroll
-        for (int x = 0; x < 16; x++) sum += px(x) * px(x);
-        S.h2t[16 * jb][r] = sum;
-#pragma unroll
-        for (int j = 1; j < 16; j++) {
-            const int o = px(j - 1), nw = px(j + 15);
-            sum += nw * nw - o * o;
-            S.h2t[16 * jb + j][r] = sum;
-        }
-    }
-    __syncthreads();
 
-    // 3. vertical 16-row sums of the horizontal energies -> tab (task: column jj, run ib)
-    for (int task = tid; task < TAB * 4; task += 128) {
-        const int jj = task & (TAB - 1), ib = task >> 6;
-        const int* col = S.h2t[jj];
-        const int ii0 = 16 * ib, ii1 = min(ii0 + 16, 2 * RMAX + 1);
-        int sum = 0;
-#pragma unroll
-        for (int y = 0; y < 16; y++) sum += col[ii0 + y];
-        S.tab[ii0][jj] = sum;
-        for (int ii = ii0 + 1; ii < ii1; ii++) {
-            sum += col[ii + 15] - col[ii - 1];
-            S.tab[ii][jj] = sum;
-        }
-    }
-    __syncthreads();
-
-    // 4. cross terms with dp4a; each thread: 8 candidate rows x 4 word offsets, one byte shift s.
+    // 3. cross terms with dp4a; each thread: 8 candidate rows x 4 word offsets, one byte shift s.
     //    Each window row is byte-aligned once for the thread's shift (funnel shifts: word i
     //    holds bytes 4i+s .. 4i+s+3 of the thread's 32-byte slice) and kept in a ring of 8
-    //    rows; then every 16-pixel row product is 4 dp4a against the template row.
+    //    rows; then every 16-pixel row product is 4 dp4a against the template row.  The
+    //    horizontal 16-sample energies of the thread's 4 columns come from the same aligned
+    //    words (a self-dp4a per word and a sliding sum), for the window rows the thread owns
+    //    (its first 8; rows 64..77 after the loop); they fill the issue slots the dp4a pipe
+    //    leaves.
+    unsigned acc[8][4];
+    const int s = lane & 3, qg = (lane >> 2) & 3, ig = 2 * warp + (lane >> 4);
+    const int ii0 = 8 * ig;
     {
-        const int s = lane & 3, qg = (lane >> 2) & 3, ig = 2 * warp + (lane >> 4);
-        const int ii0 = 8 * ig;
         unsigned al[8][7];
         auto load_row = [&](unsigned* dst, int r) {
             const uint4* p = reinterpret_cast<const uint4*>(&S.win[r][16 * qg]);
@@ -233,9 +203,22 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
 #pragma unroll
             for (int i = 0; i < 7; i++) dst[i] = __funnelshift_r(w[i], w[i + 1], 8 * s);
         };
+        auto row_energy = [&](const unsigned* w, int r) {
+            unsigned sq[7];
 #pragma unroll
-        for (int r = 0; r < 8; r++) load_row(al[r], ii0 + r);
-        unsigned acc[8][4];
+            for (int i = 0; i < 7; i++) sq[i] = __dp4a(w[i], w[i], 0u);
+            unsigned e = sq[0] + sq[1] + sq[2] + sq[3];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if (q) e += sq[q + 3] - sq[q - 1];
+                S.h2t[16 * qg + 4 * q + s][r] = (int)e;
+            }
+        };
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+            load_row(al[r], ii0 + r);
+            row_energy(al[r], ii0 + r);
+        }
 #pragma unroll
         for (int r = 0; r < 8; r++)
 #pragma unroll
@@ -257,6 +240,45 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
             }
             if (y < 15) load_row(al[y & 7], ii0 + y + 8);
         }
+    }
+    // energies of window rows 64..77 (below every row group's own rows): 14 rows x 16 slices
+    for (int task = tid; task < (WROWS - 64) * 16; task += 128) {
+        const int r = 64 + (task >> 4), c = task & 15, ts = c & 3, tq = c >> 2;
+        const uint4* p = reinterpret_cast<const uint4*>(&S.win[r][16 * tq]);
+        const uint4 x0 = p[0], x1 = p[1];
+        const unsigned w[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+        unsigned sq[7];
+#pragma unroll
+        for (int i = 0; i < 7; i++) {
+            const unsigned v = __funnelshift_r(w[i], w[i + 1], 8 * ts);
+            sq[i] = __dp4a(v, v, 0u);
+        }
+        unsigned e = sq[0] + sq[1] + sq[2] + sq[3];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (q) e += sq[q + 3] - sq[q - 1];
+            S.h2t[16 * tq + 4 * q + ts][r] = (int)e;
+        }
+    }
+    __syncthreads();
+
+    // 4. vertical 16-row sums of the horizontal energies (task: column jj, run ib), then
+    //    SSD = A^2 + B^2 - 2 sum(ab) for every candidate
+    for (int task = tid; task < TAB * 4; task += 128) {
+        const int jj = task & (TAB - 1), ib = task >> 6;
+        const int* col = S.h2t[jj];
+        const int r0 = 16 * ib, r1 = min(r0 + 16, 2 * RMAX + 1);
+        int sum = 0;
+#pragma unroll
+        for (int y = 0; y < 16; y++) sum += col[r0 + y];
+        S.tab[r0][jj] = sum;
+        for (int ii = r0 + 1; ii < r1; ii++) {
+            sum += col[ii + 15] - col[ii - 1];
+            S.tab[ii][jj] = sum;
+        }
+    }
+    __syncthreads();
+    {
         const int a2 = S.a2;
 #pragma unroll
         for (int r = 0; r < 8; r++) {

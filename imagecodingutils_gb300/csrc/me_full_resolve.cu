@@ -209,11 +209,12 @@ __global__ void __launch_bounds__(256, 4) k_full_sweep0(FullArgs a)
 }
 
 // ---------------------------------------------------------------------------
+constexpr int kHist = 4096;  // dictionary histogram slots
 struct RelaxSmem {
     union {
         struct {
-            int keys[2048];
-            int counts[2048];
+            int keys[kHist];
+            int counts[kHist];
         } hist;
     } u;
     long long red_total[8];
@@ -311,12 +312,13 @@ __global__ void __launch_bounds__(256) k_full_relax_outcome(FullArgs a)
         return;
     }
     if (blockIdx.x != 0) return;
-    for (int i = threadIdx.x; i < 2048; i += blockDim.x) {
+    for (int i = threadIdx.x; i < kHist; i += blockDim.x) {
         S.u.hist.keys[i] = kEmpty;
         S.u.hist.counts[i] = 0;
     }
     __syncthreads();
-    for (int k0 = threadIdx.x; k0 < a.nmb; k0 += 8 * blockDim.x) {
+    for (int base = 0; base < a.nmb; base += 8 * blockDim.x) {  // uniform trip count: every lane shuffles
+        const int k0 = base + threadIdx.x;
         int vals[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) {  // eight loads in flight per thread
@@ -325,14 +327,20 @@ __global__ void __launch_bounds__(256) k_full_relax_outcome(FullArgs a)
         }
 #pragma unroll
         for (int u = 0; u < 8; u++) {
+            // one insert per distinct vector of the warp (a pan makes most vectors equal:
+            // per-lane atomics on one slot would serialise)
             const int v = vals[u];
-            if (v == kEmpty) continue;
-            unsigned h = ((unsigned)v * 2654435761u) >> 21;  // 11 bits
-            for (int probe = 0; probe < 32; probe++) {
-                int slot = (h + probe) & 2047;
+            const unsigned same = __match_any_sync(0xffffffffu, v);
+            if (v == kEmpty || (__ffs(same) - 1) != (int)(threadIdx.x & 31)) continue;
+            // counts only steer which records are precomputed: a vector that finds
+            // no slot within a few probes (frames with thousands of distinct
+            // vectors) is left out
+            unsigned h = ((unsigned)v * 2654435761u) >> 20;  // 12 bits
+            for (int probe = 0; probe < 8; probe++) {
+                int slot = (h + probe) & (kHist - 1);
                 int prev = atomicCAS(&S.u.hist.keys[slot], kEmpty, v);
                 if (prev == kEmpty || prev == v) {
-                    atomicAdd(&S.u.hist.counts[slot], 1);
+                    atomicAdd(&S.u.hist.counts[slot], __popc(same));
                     break;
                 }
             }
@@ -341,7 +349,7 @@ __global__ void __launch_bounds__(256) k_full_relax_outcome(FullArgs a)
     __syncthreads();
     for (int d = 0; d < NDICT; d++) {
         int best_c = 0, best_k = kEmpty;
-        for (int i = threadIdx.x; i < 2048; i += blockDim.x)
+        for (int i = threadIdx.x; i < kHist; i += blockDim.x)
             if (S.u.hist.counts[i] > best_c) {
                 best_c = S.u.hist.counts[i];
                 best_k = i;
@@ -469,7 +477,7 @@ __device__ __forceinline__ int neighbour_set(const FullArgs& a, int x, int lane,
 }
 
 template <int kEst>
-__global__ void __launch_bounds__(256, 2) k_full_closure(FullArgs a)
+__global__ void __launch_bounds__(256, kEst == 0 ? 3 : 2) k_full_closure(FullArgs a)
 {
     if (*((volatile int*)&a.ctrl->converged)) return;
     __shared__ ClosureSmem S;
