@@ -115,7 +115,7 @@ __device__ __forceinline__ bool cache_probe(const int4* c, int key, int lane, in
 // (kept in slots 1..3; slot 0 holds the search at prediction (0, 0)).  One warp.
 template <int kEst>
 __device__ __noinline__ void pred_search_at(const FullArgs& a, int k, int px, int py, int lane, int* mvx, int* mvy,
-                                            int* minD)
+                                            int* minD, mrc::Lattice* lt)
 {
     int tv, td;
     if (mrc::tie_tree_result(kEst, static_cast<const mrc::V2TieRun*>(a.tie_runs) + (size_t)k * mrc::V2_TIE_RUNS, px,
@@ -139,7 +139,7 @@ __device__ __noinline__ void pred_search_at(const FullArgs& a, int k, int px, in
     }
     bool bad = false;
     const mrc::MrcArgs& m = *static_cast<const mrc::MrcArgs*>(a.mrc);
-    mrc::Lattice& LT = static_cast<mrc::Lattice*>(a.lattice)[k];
+    mrc::Lattice& LT = lt ? *lt : static_cast<mrc::Lattice*>(a.lattice)[k];
     const mrc::MbSearch r = mrc::search_pred<kEst>(m, LT, k / a.cols, k % a.cols, px, py, lane, bad);
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&a.ctrl->status, ST_OUT_OF_BOUNDS);
     *mvx = r.mvx;
@@ -150,6 +150,22 @@ __device__ __noinline__ void pred_search_at(const FullArgs& a, int k, int px, in
     __syncwarp();
 }
 
+// Per-warp shared sub-pel lattices for the predictor estimators' searches at
+// a prediction (8 warps per block); none for the full-search estimator.  The
+// wavefront, which evaluates rarely, uses the per-MB scratch in global memory.
+template <int kEst>
+struct LatticeSlots {
+    __device__ static mrc::Lattice* get(int warp)
+    {
+        __shared__ mrc::Lattice slots[8];
+        return &slots[warp];
+    }
+};
+template <>
+struct LatticeSlots<0> {
+    __device__ static mrc::Lattice* get(int) { return nullptr; }
+};
+
 // Full evaluation of MB k for raw prediction (px, py), one warp: the record
 // {prediction, distortion at it, final vector, final distortion}.  kEst 0:
 // MotionEstimatorH264ImplFull, a tie MB's scan from its table / tie tree;
@@ -159,7 +175,7 @@ __device__ __noinline__ void pred_search_at(const FullArgs& a, int k, int px, in
 // (…MultiresCrossVer2.cpp:627-642) comes from pred_search_at.  kEst 2:
 // MotionEstimatorH264ImplMultires, the same with its own search.
 template <int kEst>
-__device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, int lane)
+__device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, int lane, mrc::Lattice* lt = nullptr)
 {
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
     const PredGeom g = pred_geom(n, m, a.W, a.H, px, py);
@@ -171,7 +187,7 @@ __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, 
         if ((sp.w & FLAG_TIE) && (round_pred(px) != 0 || round_pred(py) != 0))
             tie_path(a, k, px, py, sp.w, lane, &mvx, &mvy, &minD);
     } else {
-        if (sp.w & FLAG_TIE) pred_search_at<kEst>(a, k, px, py, lane, &mvx, &mvy, &minD);
+        if (sp.w & FLAG_TIE) pred_search_at<kEst>(a, k, px, py, lane, &mvx, &mvy, &minD, lt);
     }
     const int pos = best_of3_fast(mvx, mvy, minD, g.pcx, g.pcy, pd, zd, a.lambda, g.pcx, g.pcy);
     int4 rec;
@@ -199,7 +215,7 @@ __global__ void __launch_bounds__(256, 4) k_full_sweep0(FullArgs a)
     if (k >= a.nmb) return;
     int px, py;
     median_pred(a.final_mv, a.spec4[k].w, k, a.cols, &px, &py);
-    const int4 rec = evaluate<kEst>(a, k, px, py, lane);
+    const int4 rec = evaluate<kEst>(a, k, px, py, lane, LatticeSlots<kEst>::get(wib));
     if (lane < KCACHE) __stcg(a.cache + (size_t)k * KCACHE + lane, lane == 0 ? rec : empty_record());
     if (lane == 0) {
         a.pred_used[k] = rec.x;
@@ -253,7 +269,7 @@ __global__ void __launch_bounds__(256, 4) k_full_relax_sweep(FullArgs a, int swe
             int4* cache = a.cache + (size_t)kk * KCACHE;
             int4 rec;
             const bool hit = cache_probe(cache, fkey, lane, &rec);
-            if (!hit) rec = evaluate<kEst>(a, kk, fx, fy, lane);
+            if (!hit) rec = evaluate<kEst>(a, kk, fx, fy, lane, LatticeSlots<kEst>::get(wib));
             if (lane == 0) {
                 atomicAdd(&a.ctrl->relax_evals, 1);
                 if (!hit) {
@@ -397,7 +413,7 @@ __global__ void __launch_bounds__(256, 2) k_full_precompute(FullArgs a)
         for (int d = 0; d < NDICT; d++) {
             const int v = dict[d];
             if (v == kEmpty || __any_sync(0xffffffffu, mine.x == v)) continue;
-            const int4 rec = evaluate<kEst>(a, k, mv_x(v), mv_y(v), lane);
+            const int4 rec = evaluate<kEst>(a, k, mv_x(v), mv_y(v), lane, LatticeSlots<kEst>::get(wib));
             if (lane == 0) __stcg(cache + kCacheDict + d, rec);
             __syncwarp();
         }
@@ -546,7 +562,7 @@ __global__ void __launch_bounds__(256, kEst == 0 ? 3 : 2) k_full_closure(FullArg
         // evaluate the new records
         for (int i = 0; i < fresh; i++) {
             const int key = S.fresh[wib][i];
-            const int4 rec = evaluate<kEst>(a, k, mv_x(key), mv_y(key), lane);
+            const int4 rec = evaluate<kEst>(a, k, mv_x(key), mv_y(key), lane, LatticeSlots<kEst>::get(wib));
             if (lane == kCacheClosure + i) mine = rec;
         }
         if (lane >= kCacheClosure) {

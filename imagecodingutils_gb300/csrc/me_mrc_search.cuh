@@ -57,8 +57,10 @@ __device__ __forceinline__ Org origin(const Buf& b, int bw, int bh, int eb, int 
 // Flat read, as the reference addresses its buffers.
 __device__ __forceinline__ int rd(const Buf& b, int r, int c, bool& bad)
 {
-    const long long f = (long long)r * b.w + c;
-    if (f < 0 || f >= (long long)b.w * b.h) {
+    // level copies hold fewer than 2^31 samples; reads stay within a few rows of a
+    // copy, so the flat index cannot overflow and a negative one compares as huge
+    const unsigned f = (unsigned)(r * b.w + c);
+    if (f >= (unsigned)(b.w * b.h)) {
         bad = true;
         return 0;
     }
@@ -438,9 +440,10 @@ __device__ MbSearch search_mb_with(const MrcArgs& a, Lattice& LT, int mbr, int m
 // The search of MotionEstimatorH264ImplMultires (…Multires.cpp:644-906): full
 // searches at level 2 (+-(range/16 - 1)) and level 1 (+-2 after level 2, else
 // +-range/8), +-2 at level 0, half and quarter pel in the MultiresCross-style
-// window; LessThan distortions, which decide exactly as full SSDs do.  Each
-// integer level evaluates 32 candidates at a time, one per lane, then every
-// lane applies them in raster order (the same decisions in every lane).
+// window; LessThan distortions, which decide exactly as full SSDs do.  The
+// warp scores candidates in raster order: level 0 and 1 one candidate at a
+// time, each lane holding a fixed share of the input block; level 2 (4x4)
+// two at a time, one per half-warp.
 template <typename Skip>
 __device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int mbc, Skip&& skip, int lane, bool& bad)
 {
@@ -456,96 +459,79 @@ __device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int m
     out.zero_d = full_ssd(a.in0, oin0, a.e0, origin(a.e0, 16, 16, 19, n, m), 16, lane, bad);
     int mx = 0, my = 0, xl, xr, yu, yd;
 
-    // one lane's SSD of an N x N block against the reference copy at origin o
-    auto lane_ssd = [&](const Buf& in, Org oi, const Buf& e, Org o, int N) {
-        int acc = 0;
-        for (int r = 0; r < N; r++)
-            for (int c = 0; c < N; c++) {
-                const int d = rd(in, oi.y + r, oi.x + c, bad) - rd(e, o.y + r, o.x + c, bad);
-                acc += d * d;
-            }
-        return acc;
-    };
-    // candidates (i, j) of [yu, yd] x [xl, xr] in raster order, (0, 0) skipped,
-    // 32 at a time; apply(i, j, d) in every lane in order
-    auto scan = [&](auto&& dist, auto&& apply) {
-        const int wdt = xr - xl + 1, cnt = (wdt > 0 && yd >= yu) ? (yd - yu + 1) * wdt : 0;
-        for (int base = 0; base < cnt; base += 32) {
-            const int c = base + lane;
-            int d = 0;
-            if (c < cnt) {
-                const int i = yu + c / wdt, j = xl + c % wdt;
-                if (i || j) d = dist(i, j);
-            }
-            const int lim = cnt - base < 32 ? cnt - base : 32;
-            for (int t = 0; t < lim; t++) {
-                const int dt = __shfl_sync(0xffffffffu, d, t);
-                const int cc = base + t, i = yu + cc / wdt, j = xl + cc % wdt;
-                if (i || j) apply(i, j, dt);
-            }
-        }
-    };
-
     if (a.mode == 2) {  // level 2 full search around (0, 0) (…Multires.cpp:667-731)
+        // 8 candidates of a row at a time, 4 lanes each (one block row per lane)
         const Org oin2 = origin(a.in2, 4, 4, 0, ll, kk);
+        const int sub = lane >> 2, br = lane & 3;
+        int cur2[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) cur2[c] = rd(a.in2, oin2.y + br, oin2.x + c, bad);
         int min2 = full_ssd(a.in2, oin2, a.e2, origin(a.e2, 4, 4, 5, ll, kk), 4, lane, bad);
         mr_range(L2, ll, kk, 0, 0, l2_range - 1, xl, xr, yu, yd);
-        scan([&](int i, int j) { return lane_ssd(a.in2, oin2, a.e2, origin(a.e2, 4, 4, 5, ll + j, kk + i), 4); },
-             [&](int i, int j, int d) {
-                 if (d > min2) return;
-                 if (d == min2) {
-                     out.tie |= TIE_L2;
-                     if (skip(2, 0, 0, mx, my, j, i)) return;
-                 }
-                 min2 = d;
-                 mx = j;
-                 my = i;
-             });
+        for (int i = yu; i <= yd; i++)
+            for (int j0 = xl; j0 <= xr; j0 += 8) {
+                int d = 0;
+                if (j0 + sub <= xr) {
+                    const Org o = origin(a.e2, 4, 4, 5, ll + j0 + sub, kk + i);
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const int e = cur2[c] - rd(a.e2, o.y + br, o.x + c, bad);
+                        d += e * e;
+                    }
+                }
+                d += __shfl_xor_sync(0xffffffffu, d, 1);
+                d += __shfl_xor_sync(0xffffffffu, d, 2);
+                const int nj = xr - j0 + 1 < 8 ? xr - j0 + 1 : 8;
+                for (int t = 0; t < nj; t++) {
+                    const int j = j0 + t, dt = __shfl_sync(0xffffffffu, d, 4 * t);
+                    if (!(i || j) || dt > min2) continue;
+                    if (dt == min2) {
+                        out.tie |= TIE_L2;
+                        if (skip(2, 0, 0, mx, my, j, i)) continue;
+                    }
+                    min2 = dt;
+                    mx = j;
+                    my = i;
+                }
+            }
         mx <<= 1;
         my <<= 1;
     }
 
-    // level 1 around (mx, my) (…Multires.cpp:735-790)
+    // level 1 around (mx, my) (…Multires.cpp:735-790): this lane's 2 samples of the 8x8 block
     const Org oin1 = origin(a.in1, 8, 8, 0, q, p);
+    int r1, c1;
+    phase_coords<8>(lane, r1, c1);
+    int cur1[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) cur1[j] = rd(a.in1, oin1.y + r1, oin1.x + c1 + 4 * j, bad);
     int min1 = full_ssd(a.in1, oin1, a.e1, origin(a.e1, 8, 8, 9, mx + q, my + p), 8, lane, bad);
     int rmx = 0, rmy = 0;
     mr_range(L1, q, p, mx, my, lcl_l1_range, xl, xr, yu, yd);
-    scan([&](int i, int j) { return lane_ssd(a.in1, oin1, a.e1, origin(a.e1, 8, 8, 9, j + mx + q, i + my + p), 8); },
-         [&](int i, int j, int d) {
-             if (d > min1) return;
-             if (d == min1) {
-                 out.tie |= TIE_L1;
-                 if (skip(1, mx, my, rmx, rmy, j, i)) return;
-             }
-             min1 = d;
-             rmx = j;
-             rmy = i;
-         });
+    for (int i = yu; i <= yd; i++)
+        for (int j = xl; j <= xr; j++) {
+            if (!(i || j)) continue;
+            const Org o = origin(a.e1, 8, 8, 9, j + mx + q, i + my + p);
+            int acc = 0;
+#pragma unroll
+            for (int t = 0; t < 2; t++) {
+                const int e = cur1[t] - rd(a.e1, o.y + r1, o.x + c1 + 4 * t, bad);
+                acc += e * e;
+            }
+            const int d = warp_sum(acc);
+            if (d > min1) continue;
+            if (d == min1) {
+                out.tie |= TIE_L1;
+                if (skip(1, mx, my, rmx, rmy, j, i)) continue;
+            }
+            min1 = d;
+            rmx = j;
+            rmy = i;
+        }
     mx = (mx + rmx) * 2;
     my = (my + rmy) * 2;
 
-    // level 0 +-2 (…Multires.cpp:792-849)
-    int min_d = full_ssd(a.in0, oin0, a.e0, origin(a.e0, 16, 16, 19, n + mx, m + my), 16, lane, bad);
-    rmx = rmy = 0;
-    mr_range(L0, n, m, mx, my, 2, xl, xr, yu, yd);
-    scan([&](int i, int j) {
-             return lane_ssd(a.in0, oin0, a.e0, origin(a.e0, 16, 16, 19, n + mx + j, m + my + i), 16);
-         },
-         [&](int i, int j, int d) {
-             if (d > min_d) return;
-             if (d == min_d) {
-                 out.tie |= TIE_L0;
-                 if (skip(0, mx, my, rmx, rmy, j, i)) return;
-             }
-             min_d = d;
-             rmx = j;
-             rmy = i;
-         });
-    mx += rmx;
-    my += rmy;
-    int mvx = mx * 4, mvy = my * 4;
-
-    // half then quarter pel (…Multires.cpp:851-917), strict improvements, full distortions
+    // level 0 +-2 (…Multires.cpp:792-849): this lane's 8 samples of the 16x16 block
     int r0, c0;
     phase_coords<16>(lane, r0, c0);
     int cur0[8];
@@ -553,6 +539,38 @@ __device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int m
     for (int i = 0; i < 2; i++)
 #pragma unroll
         for (int j = 0; j < 4; j++) cur0[4 * i + j] = rd(a.in0, oin0.y + r0 + 4 * i, oin0.x + c0 + 4 * j, bad);
+    auto ssd16 = [&](Org o) {
+        int acc = 0;
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int e = cur0[4 * i + j] - rd(a.e0, o.y + r0 + 4 * i, o.x + c0 + 4 * j, bad);
+                acc += e * e;
+            }
+        return warp_sum(acc);
+    };
+    int min_d = ssd16(origin(a.e0, 16, 16, 19, n + mx, m + my));
+    rmx = rmy = 0;
+    mr_range(L0, n, m, mx, my, 2, xl, xr, yu, yd);
+    for (int i = yu; i <= yd; i++)
+        for (int j = xl; j <= xr; j++) {
+            if (!(i || j)) continue;
+            const int d = ssd16(origin(a.e0, 16, 16, 19, n + mx + j, m + my + i));
+            if (d > min_d) continue;
+            if (d == min_d) {
+                out.tie |= TIE_L0;
+                if (skip(0, mx, my, rmx, rmy, j, i)) continue;
+            }
+            min_d = d;
+            rmx = j;
+            rmy = i;
+        }
+    mx += rmx;
+    my += rmy;
+    int mvx = mx * 4, mvy = my * 4;
+
+    // half then quarter pel (…Multires.cpp:851-917), strict improvements, full distortions
     build_lattice<false>(LT, a.e0, origin(a.e0, 16, 16, 19, n + mx, m + my), lane, bad);
     int hmx = 0, hmy = 0;
     for (int c = 0; c < 8; c++) {
