@@ -15,7 +15,7 @@
 //
 //   k_full_sweep0      every MB at once, prediction from the current vectors
 //                      (initially the searched ones).
-//   k_full_relax_sweep up to kRelaxSweeps launches, each re-evaluating the
+//   k_full_relax_sweep up to FullArgs::relax_sweeps launches, each re-evaluating the
 //                      MBs whose prediction moved.  A sweep without change
 //                      is the unique fixed point of the DAG, i.e. the
 //                      sequential result; most frames stop here
@@ -39,7 +39,6 @@ namespace {
 using namespace full;
 
 constexpr int kEmpty = 0x7fffffff;  // no vector packs to this (|y| < 32767 quarter pels)
-constexpr int kRelaxSweeps = 8;
 constexpr int kCacheRelax = 1;      // entries 1..3 round robin in relaxation
 constexpr int kCacheDict = 4;       // entries 4..11 dictionary
 constexpr int kCacheClosure = 12;   // entries 12..31 neighbour closure
@@ -225,6 +224,45 @@ __global__ void __launch_bounds__(256, 4) k_full_sweep0(FullArgs a)
 }
 
 // ---------------------------------------------------------------------------
+// The MBs whose median prediction reads MB k (left of the right neighbour,
+// above of the MB below, above-right of the MB below-left, above-left of the
+// MB below-right), set in a bitmap of one bit per MB.
+__device__ __forceinline__ void mark_dependents(const FullArgs& a, int k, unsigned* bits)
+{
+    const int cols = a.cols, rows = a.nmb / cols, r = k / cols, c = k - r * cols;
+    auto set = [&](int j) { atomicOr(bits + (j >> 5), 1u << (j & 31)); };
+    if (c + 1 < cols) set(k + 1);
+    if (r + 1 < rows) {
+        set(k + cols);
+        if (c > 0) set(k + cols - 1);
+        if (c + 1 < cols) set(k + cols + 1);
+    }
+}
+
+// State of the relaxation before sweep `upto` from the change counts of sweeps
+// 1 .. upto-1: s > 0 when sweep s changed nothing (the fixed point), -1 when
+// more than a few MBs still change and the counts stopped falling fast enough
+// to reach zero within `limit` sweeps (they fall about geometrically while
+// copy chains shorten; a ratio above 7/8, or a projection past the limit,
+// gives up to the wavefront), 0 while
+// the sweeps go on.  The sweep kernels and the outcome kernel evaluate the
+// same counts with this one function, so they agree.
+__device__ __forceinline__ int relax_status(const int* changed, int upto, int limit)
+{
+    int prev = 0;
+    for (int s = 1; s < upto; s++) {
+        const int c = *((const volatile int*)&changed[s]);
+        if (c == 0) return s;
+        if (s >= 3 && c > 32) {  // a few changes settle within a sweep or two: never give up on them
+            const float r = (float)c / (float)prev;
+            if (r >= 0.875f) return -1;
+            if ((float)s + logf((float)c + 1.0f) / -logf(r) > (float)limit + 1.0f) return -1;
+        }
+        prev = c;
+    }
+    return 0;
+}
+
 constexpr int kHist = 4096;  // dictionary histogram slots
 struct RelaxSmem {
     union {
@@ -243,11 +281,9 @@ struct RelaxSmem {
 // MBs whose prediction moved, then the warp on each.  Skipped once an earlier
 // sweep changed no vector (the fixed point is reached).
 template <int kEst>
-__global__ void __launch_bounds__(256, 4) k_full_relax_sweep(FullArgs a, int sweep)
+__global__ void __launch_bounds__(256, 4) k_full_relax_sweep(FullArgs a, int sweep, int mark)
 {
-    if (sweep > 1 && *((volatile int*)&a.changed[sweep - 1]) == 0) return;
-    for (int s = 1; s < sweep - 1; s++)
-        if (*((volatile int*)&a.changed[s]) == 0) return;
+    if (relax_status(a.changed, sweep, a.relax_sweeps) != 0) return;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gwarp = blockIdx.x * 8 + wib, nwarps = gridDim.x * 8;
     int changed = 0;
@@ -280,13 +316,80 @@ __global__ void __launch_bounds__(256, 4) k_full_relax_sweep(FullArgs a, int swe
                 a.final_dist[kk] = rec.w;
                 if (__ldcg(a.final_mv + kk) != rec.z) {
                     __stcg(a.final_mv + kk, rec.z);
-                    changed = 1;
+                    changed++;
+                    if (mark) mark_dependents(a, kk, a.dirty);
                 }
             }
             __syncwarp();
         }
     }
-    if (lane == 0 && changed) atomicAdd(&a.changed[sweep], 1);
+    if (lane == 0 && changed) atomicAdd(&a.changed[sweep], changed);
+}
+
+// The remaining sweeps (3 ..) by one block: only the MBs whose prediction
+// inputs changed in the previous sweep (dependents of changed MBs, kept as
+// bitmaps in shared memory) are visited, 32 warps at a time, with a block
+// barrier between sweeps.  A frame that settled in the grid sweeps costs one
+// short launch here instead of a grid launch per remaining sweep.
+template <int kEst>
+__global__ void __launch_bounds__(1024, 1) k_full_relax_tail(FullArgs a, int first)
+{
+    extern __shared__ unsigned tail_bits[];  // current and next dirty sets, one bit per MB
+    __shared__ int s_changed;
+    if (relax_status(a.changed, first, a.relax_sweeps) != 0) return;
+    const int words = (a.nmb + 31) >> 5;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned* cur = tail_bits;
+    unsigned* nxt = tail_bits + words;
+    for (int i = threadIdx.x; i < words; i += blockDim.x) {
+        cur[i] = __ldcg(a.dirty + i);
+        nxt[i] = 0u;
+    }
+    __syncthreads();
+    for (int sweep = first; sweep <= a.relax_sweeps; sweep++) {
+        if (threadIdx.x == 0) s_changed = 0;
+        __syncthreads();
+        int changes = 0;
+        for (int w = wib; w < words; w += nw) {
+            unsigned bits = cur[w];
+            while (bits) {
+                const int k = 32 * w + __ffs(bits) - 1;
+                bits &= bits - 1;
+                int px, py;
+                median_pred(a.final_mv, __ldcg(&a.spec4[k].w), k, a.cols, &px, &py);
+                const int key = pack_mv(px, py);
+                if (__ldcg(a.pred_used + k) == key) continue;
+                int4* cache = a.cache + (size_t)k * KCACHE;
+                int4 rec;
+                const bool hit = cache_probe(cache, key, lane, &rec);
+                if (!hit) rec = evaluate<kEst>(a, k, px, py, lane, nullptr);
+                if (lane == 0) {
+                    atomicAdd(&a.ctrl->relax_evals, 1);
+                    if (!hit) {
+                        atomicAdd(&a.ctrl->relax_miss, 1);
+                        __stcg(cache + kCacheRelax + (sweep % 3), rec);
+                    }
+                    __stcg(a.pred_used + k, key);
+                    a.final_dist[k] = rec.w;
+                    if (__ldcg(a.final_mv + k) != rec.z) {
+                        __stcg(a.final_mv + k, rec.z);
+                        changes++;
+                        mark_dependents(a, k, nxt);
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (lane == 0 && changes) atomicAdd(&s_changed, changes);
+        __syncthreads();
+        for (int i = threadIdx.x; i < words; i += blockDim.x) cur[i] = 0u;
+        if (threadIdx.x == 0) a.changed[sweep] = s_changed;
+        __syncthreads();
+        unsigned* t = cur;
+        cur = nxt;
+        nxt = t;
+        if (relax_status(a.changed, sweep + 1, a.relax_sweeps) != 0) break;
+    }
 }
 
 // After the sweeps: a sweep that changed nothing means the vectors are the
@@ -296,9 +399,8 @@ __global__ void __launch_bounds__(256, 4) k_full_relax_sweep(FullArgs a, int swe
 __global__ void __launch_bounds__(256) k_full_relax_outcome(FullArgs a)
 {
     __shared__ RelaxSmem S;
-    int sweeps = 0;
-    for (int s = 1; s <= a.relax_sweeps && !sweeps; s++)
-        if (*((volatile int*)&a.changed[s]) == 0) sweeps = s;
+    const int status = relax_status(a.changed, a.relax_sweeps + 1, a.relax_sweeps);
+    const int sweeps = status > 0 ? status : 0;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     if (sweeps) {
         long long tot = 0;
@@ -931,6 +1033,11 @@ constexpr int kWaveMaxCols = 512;  // 8192 / 16
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
 {
     *resolve_cap = ctx->sm_count * 8;
+    // dirty bitmaps of the largest picture (8192 x 8192)
+    const int tail_smem = 2 * (512 * 512 / 32) * (int)sizeof(unsigned);
+    VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tail_smem));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tail_smem));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tail_smem));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -958,8 +1065,16 @@ int resolve_launch(vppgpu_ctx* ctx, const FullArgs& args)
     {
         // many warps, few MBs each: a sweep's latency is its busiest warp's evaluations
         const int want = (args.nmb + 7) / 8, cap = ctx->sm_count * 4, blocks = want < cap ? want : cap;
-        for (int sweep = 1; sweep <= args.relax_sweeps; sweep++) {
-            k_full_relax_sweep<kEst><<<blocks, 256, 0, ctx->stream>>>(args, sweep);
+        // the first sweeps over every MB, the rest (if any) over the dirty sets by one block
+        const int grid_sweeps = args.relax_sweeps < args.grid_sweeps ? args.relax_sweeps : args.grid_sweeps;
+        const bool tail = args.relax_sweeps > grid_sweeps;
+        for (int sweep = 1; sweep <= grid_sweeps; sweep++) {
+            k_full_relax_sweep<kEst><<<blocks, 256, 0, ctx->stream>>>(args, sweep, tail && sweep == grid_sweeps);
+            VPP_CHECK_LAUNCH(ctx);
+        }
+        if (tail) {
+            const size_t words = (size_t)(args.nmb + 31) / 32;
+            k_full_relax_tail<kEst><<<1, 1024, 2 * words * sizeof(unsigned), ctx->stream>>>(args, grid_sweeps + 1);
             VPP_CHECK_LAUNCH(ctx);
         }
         const int ob = (args.nmb + 255) / 256, ocap = ctx->sm_count * 4;

@@ -81,13 +81,15 @@ struct FullArgs {
     int* dict;       // dominant vectors of the frame (NDICT)
     const JobDesc* job;        // device
     MeCtrl* ctrl;
-    int* changed;              // one counter per sweep
+    int* changed;              // MBs changed per sweep
+    unsigned* dirty;           // one bit per MB: dependents of the MBs the last grid sweep changed
     WaveRec* wave_rec;         // wave_rec_count(cols, rows) records
     int* wave_choice;          // per MB: the prediction the wavefront found a record for, or 0x7fffffff
                                // (evaluated there; final_mv / final_dist hold the result)
     double lambda;
     int sweep_limit;
-    int relax_sweeps;          // relaxation sweeps before the wavefront (0..8)
+    int relax_sweeps;          // relaxation sweeps before the wavefront (0..RELAX_SWEEPS)
+    int grid_sweeps;           // ... of which over every MB (the rest visit the dirty sets)
     long long spin_limit;
     // MultiresCrossVer2 only: the search's level planes (device mrc::MrcArgs)
     // and one sub-pel lattice per macroblock for searches at a prediction
@@ -118,7 +120,7 @@ int status_from_bits(int bits);
 // estimator's prediction-dependent resolve with the Ver2 evaluation.
 // args.mrc points to mrc_args_bytes() of device memory; args.lattice to
 // nmb * mrc_lattice_bytes().
-constexpr int RELAX_SWEEPS = 8;
+constexpr int RELAX_SWEEPS = 14;
 size_t mrc_args_bytes();
 size_t mrc_lattice_bytes();
 size_t mrc_tie_runs_bytes();  // per macroblock

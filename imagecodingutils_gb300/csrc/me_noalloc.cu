@@ -36,7 +36,7 @@ constexpr size_t kRefBytes = 327680;                       // padded reference, 
 constexpr size_t kSpecBytes = 8192;                        // 5 ints per macroblock
 constexpr size_t kStateBytes = 4864;                       // 3 ints per macroblock
 constexpr size_t kCtrlBytes = 256;                         // vppgpu::MeCtrl
-constexpr size_t kChangedBytes = 1792;                     // (N + 2) ints
+constexpr size_t kChangedBytes = 1792;                     // sweep counters + dirty bitmap
 constexpr size_t kCacheBytes = 202752;                     // KCACHE 16-byte records per macroblock
 constexpr size_t kDictBytes = 256;                         // NDICT vectors
 constexpr size_t kHpelBytes = 3 * kRefBytes;               // b, h, j planes of the padded reference
@@ -75,7 +75,7 @@ constexpr size_t kScratchBytes = 10u << 20;
 static_assert(kOffTables + kTableBytes <= kScratchBytes, "scratch layout exceeds the array");
 static_assert(sizeof(vppgpu::MeCtrl) <= kCtrlBytes, "control block does not fit");
 static_assert(5 * 4 * VPPGPU_NOALLOC_MAX_MBS <= kSpecBytes && 3 * 4 * VPPGPU_NOALLOC_MAX_MBS <= kStateBytes &&
-                  4 * (VPPGPU_NOALLOC_MAX_MBS + 2) <= kChangedBytes,
+                  4 * (vppgpu::RELAX_SWEEPS + 2 + (VPPGPU_NOALLOC_MAX_MBS + 31) / 32) <= kChangedBytes,
               "per-macroblock arrays do not fit");
 
 // The only device memory this entry point uses.
@@ -179,8 +179,10 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     a.ctrl = (vppgpu::MeCtrl*)(base + kOffCtrl);
     a.changed = (int*)(base + kOffChanged);
     a.lambda = 1.05;
-    a.sweep_limit = nmb + 2;
-    a.relax_sweeps = vppgpu::RELAX_SWEEPS;
+    a.sweep_limit = vppgpu::RELAX_SWEEPS + 2 + (nmb + 31) / 32;  // sweep counters, then the dirty bitmap
+    a.dirty = reinterpret_cast<unsigned*>(a.changed + vppgpu::RELAX_SWEEPS + 2);
+    a.relax_sweeps = 8;
+    a.grid_sweeps = 8;
     a.mrc = nullptr;
     a.lattice = nullptr;
     a.search_cache = nullptr;
