@@ -271,11 +271,12 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     me->rstride = width + 2 * vppgpu::PAD;
     me->sweep_limit = vppgpu::RELAX_SWEEPS + 2 + (me->nmb + 31) / 32;  // sweep counters, then the dirty bitmap
     // Sweep policy by how the estimator's predictions settle on moving content
-    // (measured over 1080p pans): the full-search estimator settles within 8
-    // sweeps or not at all; Multires keeps settling with more sweeps, cheaply
-    // over the dirty sets; Ver2 rarely settles, so its wavefront starts early.
-    me->relax_sweeps = kind == VPPGPU_ME_MULTIRES ? vppgpu::RELAX_SWEEPS : (kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : 8);
-    me->grid_sweeps = kind == VPPGPU_ME_MULTIRES ? 4 : me->relax_sweeps;
+    // (measured over 1080p pans): the full-search estimator mostly settles
+    // within 8 sweeps over every MB, a few more over the dirty sets; Multires
+    // keeps settling with more sweeps, cheaply over the dirty sets; Ver2
+    // rarely settles, so its wavefront starts early.
+    me->relax_sweeps = kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : vppgpu::RELAX_SWEEPS;
+    me->grid_sweeps = kind == VPPGPU_ME_MULTIRES ? 4 : (kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : 8);
     size_t npix = (size_t)width * height;
     size_t npad = (size_t)me->rstride * (height + 2 * vppgpu::PAD);
     me->plane_size = npad;
