@@ -327,6 +327,22 @@ MULTIRES = {  # kind -> (class name, oracle method)
 MULTIRES_CODE = {"multires": 1, "multires_cross": 2, "multires_cross_v2": 3}  # VPPGPU_ME_*
 
 
+TUNE_PAIRS = 8
+
+
+def autotune(L, _lib, h, dev_frames, npairs):
+    """vppgpu_me_autotune_pairs over the first frame pairs of the rotation
+    (untimed set-up, as a codec would call it once per stream)."""
+    src = (C.c_void_p * npairs)(*[dev_frames[i + 1].data_ptr() for i in range(npairs)])
+    ref = (C.c_void_p * npairs)(*[dev_frames[i].data_ptr() for i in range(npairs)])
+    idx = C.c_int()
+    _lib.check(L.vppgpu_me_autotune_pairs(h, src, ref, npairs, 1, C.byref(idx)), "vppgpu_me_autotune_pairs")
+    t = (C.c_int * 4)()
+    L.vppgpu_me_get_tuning(h, t)
+    return {"pairs": npairs, "choice": idx.value, "relax_sweeps": t[0], "grid_sweeps": t[1],
+            "sweep_ctas_per_sm": t[2], "search_mbs_per_cta": t[3]}
+
+
 def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with_cpu, kind="multires_cross"):
     """A multi-resolution estimator (mode 0 -> 2 at 1080p) on the same 1080p
     sequence: device-resident MB/s over the frame rotation, and the oracle
@@ -339,6 +355,7 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
     mode = C.c_int()
     L.vppgpu_me_get_mode(h, C.byref(mode))
     dev_frames = torch.from_numpy(np.stack(frames)).to(dev)
+    tuning = None if args.no_autotune else autotune(L, _lib, h, dev_frames, TUNE_PAIRS)
     d_mv = torch.empty((NMB, 2), dtype=torch.int16, device=dev)
 
     def step(t):
@@ -358,7 +375,7 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
-    out = {"value": NMB / (ms * 1e-3), "unit": UNIT, "ms_per_frame": ms, "mode": mode.value,
+    out = {"value": NMB / (ms * 1e-3), "unit": UNIT, "ms_per_frame": ms, "mode": mode.value, "autotune": tuning,
            "workload": f"{cls} plain per-frame, {W}x{H}, motionRange {MOTION_RANGE}"}
     if kind != "multires_cross":
         # per-frame device time and how each frame's predictions were decided
@@ -519,6 +536,7 @@ def main():
     ap.add_argument("--batch-streams", type=int, default=8)
     ap.add_argument("--batch-reps", type=int, default=3)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes and sweep policy")
     ap.add_argument("--serve-jobs", type=int, default=1000)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-slots", type=int, default=4)
@@ -558,6 +576,7 @@ def main():
 
     h = C.c_void_p()
     _lib.check(L.vppgpu_me_create(ctx.handle, _lib.ME_FULL, W, H, MOTION_RANGE, C.byref(h)), "vppgpu_me_create")
+    tuning = None if args.no_autotune else autotune(L, _lib, h, dev, TUNE_PAIRS)
 
     def step_device(t):
         i = t % (NFRAMES - 1)
@@ -682,7 +701,7 @@ def main():
             "latency_ms": {"p50": per_frame[len(per_frame) // 2],
                            "p99": per_frame[min(len(per_frame) - 1, int(0.99 * len(per_frame)))],
                            "max": per_frame[-1], "unit": "device ms per frame, plain per-frame form"},
-            "resolve_sweeps_last_frame": sweeps.value,
+            "resolve_sweeps_last_frame": sweeps.value, "autotune": tuning,
             "hbm_peak_gbs": pk.get("hbm_gbs"), "peaks_source": pk_kind,
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
             "serving": serving,

@@ -157,6 +157,24 @@ class _MotionEstimatorBase:
                 self._pred.Set16x16MotionVector(k, int(mv[k, 0]), int(mv[k, 1]))
         return mv, avg.value
 
+    def Autotune(self, reps: int = 2) -> dict:
+        """Time the estimator's launch shapes and relaxation policy on the
+        constructor planes and keep the fastest (vppgpu_me_autotune; results
+        are the same for every choice).  Returns the chosen tuning."""
+        if not self._h_me:
+            raise VppGpuError(_lib.ERR_NOT_READY, "Autotune before Create")
+        src = np.ascontiguousarray(self._src, np.int16)
+        ref = np.ascontiguousarray(self._ref, np.int16)
+        idx = C.c_int()
+        check(load().vppgpu_me_autotune_host(self._h_me, _ptr(src), _ptr(ref), int(reps), C.byref(idx)),
+              "vppgpu_me_autotune_host")
+        return dict(self.tuning(), choice=idx.value)
+
+    def tuning(self) -> dict:
+        t = (C.c_int * 4)()
+        check(load().vppgpu_me_get_tuning(self._h_me, t), "vppgpu_me_get_tuning")
+        return {"relax_sweeps": t[0], "grid_sweeps": t[1], "sweep_ctas_per_sm": t[2], "search_mbs_per_cta": t[3]}
+
     def last_sweeps(self) -> int:
         s = C.c_int()
         check(load().vppgpu_me_last_sweeps(self._h_me, C.byref(s)), "vppgpu_me_last_sweeps")

@@ -50,6 +50,10 @@ SIGNATURES = {
     "vppgpu_me_estimate_lambda": (_I, [_P, _P, _P, _P, _P, C.c_double, _P, _P, C.POINTER(C.c_long)]),
     "vppgpu_me_last_status": (_I, [_P]),
     "vppgpu_me_set_relax_sweeps": (_I, [_P, _I]),
+    "vppgpu_me_autotune": (_I, [_P, _P, _P, _I, C.POINTER(_I)]),
+    "vppgpu_me_get_tuning": (_I, [_P, _P]),
+    "vppgpu_me_autotune_host": (_I, [_P, _P, _P, _I, C.POINTER(_I)]),
+    "vppgpu_me_autotune_pairs": (_I, [_P, _P, _P, _I, _I, C.POINTER(_I)]),
     "vppgpu_me_last_sweeps": (_I, [_P, C.POINTER(_I)]),
     "vppgpu_me_last_stats": (_I, [_P, _P]),
     "vppgpu_me_set_timing": (_I, [_P, _I]),

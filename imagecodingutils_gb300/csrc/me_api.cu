@@ -1,6 +1,7 @@
 // me_api.cu -- the motion-estimation handle of the vppgpu C ABI: the
 // constructor + Create() of an IMotionEstimator implementation (device
 // allocations sized once per frame geometry) and its Estimate() calls.
+#include <vector>
 #include <stdlib.h>
 #include <string.h>
 
@@ -44,6 +45,8 @@ struct vppgpu_me {
     int resolve_grid;
     int relax_sweeps;  // relaxation sweeps before the wavefront (0..RELAX_SWEEPS)
     int grid_sweeps;   // ... of which over every MB
+    int relax_blocks_per_sm;  // grid of a sweep over every MB
+    int mrc_warps;     // MultiresCross: macroblocks (warps) per search CTA
     void* d_mrc_args;  // MultiresCrossVer2: device mrc::MrcArgs
     void* d_lattice;   // MultiresCrossVer2: one sub-pel lattice per MB
     int4* d_search_cache;  // MultiresCrossVer2: searches of tie MBs at other predictions
@@ -169,6 +172,7 @@ vppgpu::FullArgs full_args(vppgpu_me* me, double lambda)
     a.sweep_limit = me->sweep_limit;
     a.relax_sweeps = me->relax_sweeps;
     a.grid_sweeps = me->grid_sweeps;
+    a.relax_blocks_per_sm = me->relax_blocks_per_sm;
     a.mrc = me->d_mrc_args;
     a.lattice = me->d_lattice;
     a.search_cache = me->d_search_cache;
@@ -184,7 +188,7 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
     VPP_CUDA(cudaMemsetAsync(me->ctrl, 0, sizeof(vppgpu::MeCtrl), ctx->stream));
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS)
         return vppgpu::mrc_launch(ctx, me->W, me->H, me->motion_range, me->mode, d_src16, d_ref16, me->d_mrc, d_incl,
-                                  d_mv, d_dist, d_avg, me->ctrl);
+                                  d_mv, d_dist, d_avg, me->ctrl, me->mrc_warps);
     int rc = vppgpu::set_job(ctx, me->d_job, vppgpu::JobDesc{d_src16, d_ref16, d_incl, d_slice, d_mv, d_dist, d_avg});
     if (rc) return rc;
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS_V2 || me->kind == VPPGPU_ME_MULTIRES) {
@@ -277,6 +281,8 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     // rarely settles, so its wavefront starts early.
     me->relax_sweeps = kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : vppgpu::RELAX_SWEEPS;
     me->grid_sweeps = kind == VPPGPU_ME_MULTIRES ? 4 : (kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : 8);
+    me->relax_blocks_per_sm = 4;
+    me->mrc_warps = 8;
     size_t npix = (size_t)width * height;
     size_t npad = (size_t)me->rstride * (height + 2 * vppgpu::PAD);
     me->plane_size = npad;
@@ -520,6 +526,132 @@ extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
         me->graph = nullptr;
     }
     me->graph_state = 0;
+    return VPPGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuning: the launch shapes and the relaxation policy that suit the
+// caller's content on this GPU, chosen by timing each candidate on one frame
+// pair.  Every candidate gives the same vectors (checked); only the time
+// differs.
+namespace {
+
+struct TuneCfg {
+    int relax, grid, bps, warps;
+};
+
+void apply_cfg(vppgpu_me* me, const TuneCfg& c)
+{
+    me->relax_sweeps = c.relax;
+    me->grid_sweeps = c.grid;
+    me->relax_blocks_per_sm = c.bps;
+    me->mrc_warps = c.warps;
+}
+
+}  // namespace
+
+extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src, const short* const* d_ref,
+                                        int npairs, int reps, int* chosen);
+
+extern "C" int vppgpu_me_autotune(vppgpu_me* me, const short* d_src, const short* d_ref, int reps, int* chosen)
+{
+    return vppgpu_me_autotune_pairs(me, &d_src, &d_ref, 1, reps, chosen);
+}
+
+extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src, const short* const* d_ref,
+                                        int npairs, int reps, int* chosen)
+{
+    if (!me || !d_src || !d_ref || npairs < 1 || reps < 1) return VPPGPU_ERR_INVALID_ARG;
+    for (int p = 0; p < npairs; p++)
+        if (!d_src[p] || !d_ref[p]) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    cudaStream_t st = me->ctx->stream;
+    std::vector<TuneCfg> cands;
+    const TuneCfg cur{me->relax_sweeps, me->grid_sweeps, me->relax_blocks_per_sm, me->mrc_warps};
+    cands.push_back(cur);
+    if (me->kind == VPPGPU_ME_MULTIRES_CROSS) {
+        for (int w : {2, 4, 8})
+            if (w != cur.warps) cands.push_back({cur.relax, cur.grid, cur.bps, w});
+    } else {
+        const int policies[][2] = {{4, 4}, {8, 8}, {14, 8}, {14, 4}, {14, 2}};
+        for (const auto& p : policies)
+            for (int bps : {2, 4, 8})
+                if (p[0] != cur.relax || p[1] != cur.grid || bps != cur.bps)
+                    cands.push_back({p[0], p[1], bps, cur.warps});
+    }
+    // time direct launches for every candidate (the captured graph is rebuilt afterwards)
+    if (me->graph) {
+        VPP_CUDA(cudaStreamSynchronize(st));
+        cudaGraphExecDestroy(me->graph);
+        me->graph = nullptr;
+    }
+    me->graph_state = -1;
+    std::vector<int> ref_mv((size_t)me->nmb * npairs), mv((size_t)me->nmb * npairs);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        me->graph_state = 0;
+        return VPPGPU_ERR_CUDA;
+    }
+    float best_ms = 0.f;
+    int best = 0;
+    for (size_t i = 0; i < cands.size() && !rc; i++) {
+        apply_cfg(me, cands[i]);
+        if ((rc = run(me, d_src[0], d_ref[0], nullptr, nullptr, me->d_out_mv, nullptr, nullptr, 1.05))) break;  // warm-up
+        if (cudaEventRecord(e0, st) != cudaSuccess) rc = VPPGPU_ERR_CUDA;
+        for (int r = 0; r < reps && !rc; r++)
+            for (int p = 0; p < npairs && !rc; p++) {
+                rc = run(me, d_src[p], d_ref[p], nullptr, nullptr, me->d_out_mv, nullptr, nullptr, 1.05);
+                if (!rc && r == reps - 1 &&  // the vectors of the last repetition, pair by pair
+                    cudaMemcpyAsync((i ? mv.data() : ref_mv.data()) + (size_t)p * me->nmb, me->d_out_mv,
+                                    sizeof(int) * (size_t)me->nmb, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+                    rc = VPPGPU_ERR_CUDA;
+            }
+        if (rc || cudaEventRecord(e1, st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+            if (!rc) rc = VPPGPU_ERR_CUDA;
+            break;
+        }
+        VPP_CUDA(cudaMemcpyAsync(me->h_ctrl, me->ctrl, sizeof(vppgpu::MeCtrl), cudaMemcpyDeviceToHost, st));
+        VPP_CUDA(cudaStreamSynchronize(st));
+        if ((rc = status_from_ctrl(*me->h_ctrl))) break;
+        if (i && mv != ref_mv) {  // a launch shape changed a result: never expected
+            rc = VPPGPU_ERR_CUDA;
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (i == 0 || ms < best_ms) {
+            best_ms = ms;
+            best = (int)i;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    apply_cfg(me, rc ? cur : cands[best]);
+    me->graph_state = 0;
+    if (chosen) *chosen = rc ? 0 : best;
+    return rc;
+}
+
+extern "C" int vppgpu_me_autotune_host(vppgpu_me* me, const short* src, const short* ref, int reps, int* chosen)
+{
+    if (!me || !src || !ref) return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    const size_t plane = sizeof(short) * (size_t)me->W * me->H;
+    VPP_CUDA(cudaMemcpyAsync(me->d_src16, src, plane, cudaMemcpyHostToDevice, me->ctx->stream));
+    VPP_CUDA(cudaMemcpyAsync(me->d_ref16, ref, plane, cudaMemcpyHostToDevice, me->ctx->stream));
+    return vppgpu_me_autotune(me, me->d_src16, me->d_ref16, reps, chosen);
+}
+
+extern "C" int vppgpu_me_get_tuning(vppgpu_me* me, int* tuning4)
+{
+    if (!me || !tuning4) return VPPGPU_ERR_INVALID_ARG;
+    tuning4[0] = me->relax_sweeps;
+    tuning4[1] = me->grid_sweeps;
+    tuning4[2] = me->relax_blocks_per_sm;
+    tuning4[3] = me->mrc_warps;
     return VPPGPU_OK;
 }
 

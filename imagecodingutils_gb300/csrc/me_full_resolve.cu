@@ -1064,7 +1064,8 @@ int resolve_launch(vppgpu_ctx* ctx, const FullArgs& args)
     VPP_CHECK_LAUNCH(ctx);
     {
         // many warps, few MBs each: a sweep's latency is its busiest warp's evaluations
-        const int want = (args.nmb + 7) / 8, cap = ctx->sm_count * 4, blocks = want < cap ? want : cap;
+        const int want = (args.nmb + 7) / 8, cap = ctx->sm_count * args.relax_blocks_per_sm;
+        const int blocks = want < cap ? want : cap;
         // the first sweeps over every MB, the rest (if any) over the dirty sets by one block
         const int grid_sweeps = args.relax_sweeps < args.grid_sweeps ? args.relax_sweeps : args.grid_sweeps;
         const bool tail = args.relax_sweeps > grid_sweeps;

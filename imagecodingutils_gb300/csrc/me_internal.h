@@ -90,6 +90,7 @@ struct FullArgs {
     int sweep_limit;
     int relax_sweeps;          // relaxation sweeps before the wavefront (0..RELAX_SWEEPS)
     int grid_sweeps;           // ... of which over every MB (the rest visit the dirty sets)
+    int relax_blocks_per_sm;   // grid of a sweep over every MB
     long long spin_limit;
     // MultiresCrossVer2 only: the search's level planes (device mrc::MrcArgs)
     // and one sub-pel lattice per macroblock for searches at a prediction
@@ -106,9 +107,10 @@ constexpr int WAVE_WARPS = 5;   // most warps (bands of 32 rows) of one wavefron
 // MultiresCross (me_mrc.cu): level planes in one scratch buffer.
 constexpr int ST_OUT_OF_BOUNDS = 4;  // a read the reference would make outside its buffer
 size_t mrc_scratch_bytes(int W, int H);
+// warps: macroblocks (warps) per CTA of the search kernel, 2, 4 or 8.
 int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const short* d_src16, const short* d_ref16,
                unsigned char* scratch, const unsigned char* incl, int* out_mv, int* out_dist, long long* out_avg,
-               MeCtrl* ctrl);
+               MeCtrl* ctrl, int warps = 8);
 
 // Device address of the status word (ST_* bits) of a handle's current
 // estimate, and the C ABI status those bits stand for.

@@ -114,9 +114,9 @@ __global__ void __launch_bounds__(256) k_mrc_level2(const unsigned char* __restr
 
 __global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
 {
-    __shared__ Lattice lattice[8];
+    extern __shared__ Lattice lattice[];  // one per warp
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int k = blockIdx.x * 8 + wib;
+    const int k = blockIdx.x * (blockDim.x >> 5) + wib;
     if (k >= a.cols * a.rows_all) return;
     bool bad = false;
     const int mbr = k / a.cols, mbc = k - mbr * a.cols;
@@ -289,7 +289,7 @@ int levels_launch(vppgpu_ctx* ctx, const MrcArgs& a, const short* d_src16, const
 
 int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const short* d_src16, const short* d_ref16,
                unsigned char* scratch, const unsigned char* incl, int* out_mv, int* out_dist, long long* out_avg,
-               MeCtrl* ctrl)
+               MeCtrl* ctrl, int warps)
 {
     MrcArgs a = mrc_args(W, H, motion_range, mode, scratch);
     a.incl = incl;
@@ -299,8 +299,8 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
     a.ctrl = ctrl;
     int rc = levels_launch(ctx, a, d_src16, d_ref16);
     if (rc) return rc;
-    const int warps = a.cols * a.rows_all;
-    k_mrc_search<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(a);
+    const int mbs = a.cols * a.rows_all, wpb = (warps == 2 || warps == 4) ? warps : 8;
+    k_mrc_search<<<(mbs + wpb - 1) / wpb, 32 * wpb, wpb * sizeof(Lattice), ctx->stream>>>(a);
     VPP_CHECK_LAUNCH(ctx);
     k_mrc_average<<<1, 1, 0, ctx->stream>>>(out_avg, ctrl);
     VPP_CHECK_LAUNCH(ctx);

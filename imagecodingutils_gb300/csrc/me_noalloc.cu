@@ -183,6 +183,7 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     a.dirty = reinterpret_cast<unsigned*>(a.changed + vppgpu::RELAX_SWEEPS + 2);
     a.relax_sweeps = 8;
     a.grid_sweeps = 8;
+    a.relax_blocks_per_sm = 4;
     a.mrc = nullptr;
     a.lattice = nullptr;
     a.search_cache = nullptr;

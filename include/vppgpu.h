@@ -123,6 +123,22 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps);
  * macroblocks whose predictions have not settled.  Results do not depend on it. */
 int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps);
 
+/* Autotuning, no vpp counterpart: times the estimator's tunable launch shapes
+ * and relaxation policy on one device frame pair (reps estimates each; every
+ * candidate must and is checked to give the same vectors) and keeps the
+ * fastest; *chosen (nullable) is its index, 0 = the configuration before the
+ * call.  Tunables: MultiresCross -- macroblocks per search CTA (2, 4, 8);
+ * the others -- relaxation sweeps / of which over every MB, and the CTAs per
+ * SM of such a sweep.  vppgpu_me_get_tuning returns {relaxation sweeps, grid
+ * sweeps, sweep CTAs per SM, search macroblocks per CTA}. */
+int vppgpu_me_autotune(vppgpu_me* me, const short* d_src, const short* d_ref, int reps, int* chosen);
+/* Same over several device frame pairs (each candidate timed over all). */
+int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src, const short* const* d_ref, int npairs,
+                             int reps, int* chosen);
+/* Same with host planes (copied once). */
+int vppgpu_me_autotune_host(vppgpu_me* me, const short* src, const short* ref, int reps, int* chosen);
+int vppgpu_me_get_tuning(vppgpu_me* me, int* tuning4);
+
 /* Counters of the last estimate's prediction-dependent stage: {sweeps,
  * converged-by-relaxation, relaxation evaluations, of which distortion
  * computations, MBs the wavefront evaluated in full, status bits, included
