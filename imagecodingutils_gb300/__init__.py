@@ -232,6 +232,50 @@ class MotionEstimatorH264ImplMultiresCrossVer2(MotionEstimatorH264ImplMultiresCr
     KIND = _lib.ME_MULTIRES_CROSS_V2
 
 
+class MotionCompensatorH264ImplStd:
+    """GPU MotionCompensatorH264ImplStd (src/CodecUtils/MotionCompensatorH264ImplStd.cpp):
+    Create(ref, w, h) takes the contiguous 4:2:0 int16 frame (Y, U, V) and
+    Compensate(vectors) replaces its macroblocks in place by the blocks the
+    quarter-pel vectors point at, as the reference does."""
+
+    def __init__(self, range_: int = 32, ctx: Context | None = None):
+        self._range = int(range_)
+        self._ctx = ctx or get_context()
+        self._h = None
+        self._ref = None
+
+    def Create(self, ref, imgWidth: int, imgHeight: int, macroBlkWidth: int = 16, macroBlkHeight: int = 16) -> int:
+        self._destroy()
+        if macroBlkWidth != 16 or macroBlkHeight != 16:
+            return 0
+        h = C.c_void_p()
+        if load().vppgpu_mc_create(self._ctx.handle, int(imgWidth), int(imgHeight), self._range, C.byref(h)) != _lib.OK:
+            return 0
+        self._h = h
+        self._ref = ref
+        self._w, self._hgt = int(imgWidth), int(imgHeight)
+        return 1
+
+    def Compensate(self, vectors) -> None:
+        if not self._h:
+            raise VppGpuError(_lib.ERR_NOT_READY, "Compensate before Create")
+        if not (isinstance(self._ref, np.ndarray) and self._ref.dtype == np.int16 and self._ref.flags.c_contiguous):
+            raise ValueError("the reference frame must be a contiguous int16 array (Y, U, V)")
+        mv = np.ascontiguousarray(vectors, np.int16)
+        check(load().vppgpu_mc_compensate(self._h, _ptr(self._ref), _ptr(mv)), "vppgpu_mc_compensate")
+
+    def _destroy(self):
+        if self._h:
+            load().vppgpu_mc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self._destroy()
+        except Exception:
+            pass
+
+
 # ---------------------------------------------------------------------------
 # 4x4 transforms
 # ---------------------------------------------------------------------------

@@ -61,6 +61,12 @@ SIGNATURES = {
                               C.POINTER(C.c_double)]),
     "vppgpu_me_timing_stages": (_I, [_P, C.POINTER(_I), _P]),
     "vppgpu_me_residual_device": (_I, [_P, _P, _P]),
+    "vppgpu_mc_create": (_I, [_P, _I, _I, _I, C.POINTER(_P)]),
+    "vppgpu_mc_destroy": (_I, [_P]),
+    "vppgpu_mc_compensate": (_I, [_P, _P, _P]),
+    "vppgpu_mc_compensate_device": (_I, [_P, _P, _P, _P]),
+    "vppgpu_add_clip255_device": (_I, [_P, _P, _P, C.c_longlong]),
+    "vppgpu_sub_device": (_I, [_P, _P, _P, C.c_longlong]),
     "vppgpu_server_create": (_I, [_P, _I, C.c_ulonglong, C.POINTER(_P)]),
     "vppgpu_server_prepare": (_I, [_P, _I, _I, _I]),
     "vppgpu_server_submit": (_I, [_P, _P, C.POINTER(C.c_ulonglong)]),

@@ -191,6 +191,29 @@ int vppgpu_me_batch_destroy(vppgpu_me_batch* b);
 int vppgpu_me_batch_run(vppgpu_me_batch* b, const vppgpu_me_job* jobs, int n, int* status_out, long* avg_out);
 int vppgpu_me_batch_launch_count(vppgpu_me_batch* b, unsigned long long* count);
 
+/* ---- motion compensation ------------------------------------------------ */
+/* MotionCompensatorH264ImplStd(range) + Create(ref, width, height, 16, 16)
+ * (src/CodecUtils/MotionCompensatorH264ImplStd.cpp:76-258).  The frame is
+ * contiguous 4:2:0 int16: Y width*height, then U and V (width/2)*(height/2). */
+typedef struct vppgpu_mc vppgpu_mc;
+int vppgpu_mc_create(vppgpu_ctx* ctx, int width, int height, int range, vppgpu_mc** out);
+int vppgpu_mc_destroy(vppgpu_mc* mc);
+/* Compensate(pMotionList) (…ImplStd.cpp:323-473): every macroblock of the
+ * frame replaced by the block its quarter-pel vector points at (luma
+ * QuarterRead, chroma EighthRead at the same vector in eighth-pel units; a
+ * zero vector keeps the block), read from the frame as it was before the
+ * call.  Host version in place like the reference; the device version writes
+ * d_out_yuv, which may be d_ref_yuv.  Vectors: 2 shorts per macroblock of the
+ * full macroblock rows, within the range (the reference's extended border). */
+int vppgpu_mc_compensate(vppgpu_mc* mc, short* yuv, const short* mv);
+int vppgpu_mc_compensate_device(vppgpu_mc* mc, const short* d_ref_yuv, const short* d_mv, short* d_out_yuv);
+/* OverlayMem2Dv2::Add16x16WithClip255 / Add8x8WithClip255 and Sub16x16 /
+ * Sub8x8 (OverlayMem2Dv2.cpp:1195-1426) over n samples of whole planes:
+ * a = clip255(a + b) (prediction + residual -> reconstruction), a -= b
+ * (input - prediction -> residual).  16-byte aligned device pointers. */
+int vppgpu_add_clip255_device(vppgpu_ctx* ctx, short* d_a, const short* d_b, long long n);
+int vppgpu_sub_device(vppgpu_ctx* ctx, short* d_a, const short* d_b, long long n);
+
 /* Serving, no vpp counterpart: a continuous-batching request loop for
  * sequence jobs.  A request is nframes host luma planes (W x H, back to back;
  * kept valid until the request completes); for every frame pair the server

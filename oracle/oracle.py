@@ -53,6 +53,9 @@ class Oracle:
         L.vo_me_multires_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.vo_me_multires_cross_v2.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_me_multires.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
+        L.vo_mc_compensate.argtypes = [_P, _I, _I, _I, _P]
+        L.vo_add_clip255.argtypes = [_P, _P, C.c_longlong]
+        L.vo_sub.argtypes = [_P, _P, C.c_longlong]
         L.vo_quarter_read16.argtypes = [_P, _I, _I, _I, _I, _I, _I, _P]
         L.vo_half.argtypes = [_P, _I, _I, _P]
         L.vo_fwd4x4.argtypes = [_P, _I, _I, _I, _I, _I]
@@ -126,6 +129,29 @@ class Oracle:
         if rc:
             raise ValueError(f"{fn.__name__} rc={rc}")
         return (mv, dist, avg.value, ties) if with_ties else (mv, dist, avg.value)
+
+    def mc_compensate(self, y, u, v, mv, range_):
+        """MotionCompensatorH264ImplStd::Compensate: the compensated (y, u, v) planes."""
+        h, w = y.shape
+        yuv = np.concatenate([np.ravel(y), np.ravel(u), np.ravel(v)]).astype(np.int16)
+        mvs = np.ascontiguousarray(mv, dtype=np.int16)
+        rc = self.lib.vo_mc_compensate(_ptr(yuv), w, h, range_, _ptr(mvs))
+        if rc:
+            raise ValueError(f"vo_mc_compensate rc={rc}")
+        n, c = w * h, (w // 2) * (h // 2)
+        return yuv[:n].reshape(h, w), yuv[n:n + c].reshape(h // 2, w // 2), yuv[n + c:].reshape(h // 2, w // 2)
+
+    def add_clip255(self, a, b):
+        out = np.array(a, dtype=np.int16, copy=True, order="C")
+        bb = np.ascontiguousarray(b, dtype=np.int16)
+        self.lib.vo_add_clip255(_ptr(out), _ptr(bb), out.size)
+        return out
+
+    def sub(self, a, b):
+        out = np.array(a, dtype=np.int16, copy=True, order="C")
+        bb = np.ascontiguousarray(b, dtype=np.int16)
+        self.lib.vo_sub(_ptr(out), _ptr(bb), out.size)
+        return out
 
     def me_full_intpel(self, src, ref, motion_range, metric=1):
         h, w = src.shape
@@ -206,6 +232,7 @@ class Reference:
         L.ref_inv_transform.argtypes = [_I, _P, _I, _I, _I, _P]
         L.ref_quantise_value.argtypes = [C.c_short, _I, _I, _I]
         L.ref_rgb_to_yuv.argtypes = [_I, _P, _I, _I, _I, _I, _P, _P, _P]
+        L.ref_mc_compensate.argtypes = [_I, _I, _I, _P, _P]
 
     @staticmethod
     def available(path: str = REF_SO) -> bool:
@@ -225,6 +252,16 @@ class Reference:
         if rc:
             raise ValueError(f"ref_me_estimate rc={rc}")
         return mv, avg.value
+
+    def mc_compensate(self, y, u, v, mv, range_):
+        h, w = y.shape
+        yuv = np.concatenate([np.ravel(y), np.ravel(u), np.ravel(v)]).astype(np.int16)
+        mvs = np.ascontiguousarray(mv, dtype=np.int16)
+        rc = self.lib.ref_mc_compensate(w, h, range_, _ptr(yuv), _ptr(mvs))
+        if rc:
+            raise ValueError(f"ref_mc_compensate rc={rc}")
+        n, c = w * h, (w // 2) * (h // 2)
+        return yuv[:n].reshape(h, w), yuv[n:n + c].reshape(h // 2, w // 2), yuv[n + c:].reshape(h // 2, w // 2)
 
     def fwd(self, impl, data, mode, qp, intra):
         d = np.array(data, dtype=np.int16, copy=True, order="C")

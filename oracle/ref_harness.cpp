@@ -19,6 +19,7 @@
 #include "MotionEstimatorH264ImplMultiresCross.h"
 #include "MotionEstimatorH264ImplMultiresCrossVer2.h"
 #include "VectorStructList.h"
+#include "MotionCompensatorH264ImplStd.h"
 #include "FastForward4x4ITImpl1.h"
 #include "FastForward4x4ITImpl2.h"
 #include "FastInverse4x4ITImpl1.h"
@@ -118,6 +119,26 @@ int ref_me_estimate(int kind, const short* src, const short* ref, int w, int h, 
     if (avg_out) *avg_out = avg;
     delete me;
     delete[] flags;
+    return 0;
+}
+
+/* MotionCompensatorH264ImplStd(range) + Create(yuv, w, h, 16, 16) +
+ * Compensate(list of the N_MB vectors): yuv (contiguous 4:2:0) is compensated
+ * in place.  Heights are multiples of 16 (the reference reads vectors past its
+ * list for a partial bottom row). */
+int ref_mc_compensate(int w, int h, int range, short* yuv, const short* mv)
+{
+    if (h % 16) return -1;
+    MotionCompensatorH264ImplStd mc(range);
+    if (!mc.Create(yuv, w, h, 16, 16)) return -2;
+    const int nmb = (w / 16) * (h / 16);
+    VectorStructList list(VectorStructList::SIMPLE2D);
+    list.SetLength(nmb);
+    for (int i = 0; i < nmb; i++) {
+        list.SetSimpleElement(i, 0, mv[2 * i]);
+        list.SetSimpleElement(i, 1, mv[2 * i + 1]);
+    }
+    mc.Compensate(&list);
     return 0;
 }
 

@@ -96,6 +96,15 @@ int vo_me_multires(const short* src, const short* ref, int w, int h, int motion_
                    const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist, long* avg_dist,
                    int* tie_out);
 
+/* MotionCompensatorH264ImplStd::Compensate(pMotionList)
+ * (src/CodecUtils/MotionCompensatorH264ImplStd.cpp:323-473): yuv is the
+ * contiguous 4:2:0 reference (Y w*h, U, V (w/2)*(h/2)), compensated in place
+ * by the quarter-pel vectors (2 shorts per macroblock, full macroblock rows). */
+int vo_mc_compensate(short* yuv, int w, int h, int range, const short* mv);
+/* Add16x16WithClip255 / Add8x8WithClip255 and Sub16x16 / Sub8x8 over n samples. */
+void vo_add_clip255(short* a, const short* b, long long n);
+void vo_sub(short* a, const short* b, long long n);
+
 /* OverlayMem2Dv2::QuarterRead (src/ImageUtils/OverlayMem2Dv2.cpp:704-1052) of
  * a 16x16 block whose full-pel origin is (x, y) in a frame extended by edge
  * replication, at quarter offsets (qx, qy) in -3..3. */

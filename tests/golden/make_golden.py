@@ -16,6 +16,9 @@ inputs and stores inputs and outputs:
                   avgDistortion, modes 0/1/2, with and without
                   pDistortionIncluded (pan and integer-shift content)
 * me_mr.npz       MotionEstimatorH264ImplMultires, the same cases as me_mrc2
+* mc.npz          MotionCompensatorH264ImplStd::Compensate of 4:2:0 frames by
+                  seeded vectors over the whole range (zero, full-pel, negative
+                  fractions), QCIF / CIF / 64x48
 * transform.npz   FastForward4x4ITImpl1 / Impl2 / On16x16 levels and
                   FastInverse4x4ITImpl1 / On16x16 reconstructions over QP 0..51,
                   intra and inter, modes 0/1/2, a custom SetScale, and
@@ -23,7 +26,7 @@ inputs and stores inputs and outputs:
 * colour.npz      the three RGB24->YUV420 converters, flip and chroma offsets
 
 Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
-names: me_full me_mrc me_mrc2 me_mr transform colour, default all)
+names: me_full me_mrc me_mrc2 me_mr mc transform colour, default all)
 """
 from __future__ import annotations
 
@@ -131,6 +134,28 @@ def mrc2_fixtures(ref: oracle.Reference, kind: str = "multires_cross_v2") -> dic
     return out
 
 
+MC_CASES = [("qcif_r16", 176, 144, 16, 61), ("cif_r32", 352, 288, 32, 62), ("small_r8", 64, 48, 8, 63)]
+
+
+def mc_fixtures(ref: oracle.Reference) -> dict:
+    out = {}
+    for name, w, h, rg, seed in MC_CASES:
+        y = synth.pan_sequence(seed, w, h, 1)[0]
+        u = synth.pan_sequence(seed + 100, w // 2, h // 2, 1)[0]
+        v = synth.pan_sequence(seed + 200, w // 2, h // 2, 1)[0]
+        nmb = (w // 16) * (h // 16)
+        mv = ((synth.splitmix64(seed, 2 * nmb) % np.uint64(8 * rg + 1)).astype(np.int64) - 4 * rg).astype(np.int16)
+        mv = mv.reshape(nmb, 2)
+        mv[::7] = 0
+        mv[1::11] = (4, -8)
+        cy, cu, cv = ref.mc_compensate(y, u, v, mv, rg)
+        out[f"{name}_meta"] = np.array([w, h, rg], np.int32)
+        out[f"{name}_mv"] = mv
+        for k, a in (("y", y), ("u", u), ("v", v), ("cy", cy), ("cu", cu), ("cv", cv)):
+            out[f"{name}_{k}"] = a.astype(np.uint8)
+    return out
+
+
 def transform_fixtures(ref: oracle.Reference) -> dict:
     lap = synth.residual_blocks(11, 16 * 64)
     full = ((synth.splitmix64(12, 16 * 16) % np.uint64(65536)).astype(np.int64) - 32768).astype(np.int16)
@@ -180,7 +205,7 @@ def main() -> None:
     oracle.build(with_reference=True)
     ref = oracle.Reference()
     makers = {"me_full": me_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
-              "me_mr": lambda r: mrc2_fixtures(r, "multires"),
+              "me_mr": lambda r: mrc2_fixtures(r, "multires"), "mc": mc_fixtures,
               "transform": transform_fixtures, "colour": colour_fixtures}
     names = sys.argv[1:] or list(makers)
     for name in names:

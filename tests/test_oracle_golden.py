@@ -195,3 +195,39 @@ def test_me_multires_against_compiled_reference(orc, seed, w, h, mr, mode):
     mv_o, _, avg_o = orc.me_multires(fr[1], fr[0], mr, mode=mode, dist_incl=incl)
     np.testing.assert_array_equal(mv_o, mv_r)
     assert avg_o == avg_r
+
+
+MC_CASES = ["qcif_r16", "cif_r32", "small_r8"]
+
+
+@pytest.mark.parametrize("case", MC_CASES)
+def test_mc_compensate_matches_reference(orc, golden, case):
+    g = golden("mc.npz")
+    w, h, rg = (int(v) for v in g[f"{case}_meta"])
+    y, u, v = (g[f"{case}_{k}"].astype(np.int16) for k in ("y", "u", "v"))
+    cy, cu, cv = orc.mc_compensate(y, u, v, g[f"{case}_mv"], rg)
+    np.testing.assert_array_equal(cy, g[f"{case}_cy"])
+    np.testing.assert_array_equal(cu, g[f"{case}_cu"])
+    np.testing.assert_array_equal(cv, g[f"{case}_cv"])
+
+
+@ref_available
+def test_mc_compensate_against_compiled_reference(orc):
+    ref_lib = oracle_mod.Reference()
+    w, h, rg = 640, 352, 32
+    y = synth.pan_sequence(64, w, h, 1)[0]
+    u = synth.pan_sequence(65, w // 2, h // 2, 1)[0]
+    v = synth.pan_sequence(66, w // 2, h // 2, 1)[0]
+    nmb = (w // 16) * (h // 16)
+    mv = ((synth.splitmix64(67, 2 * nmb) % np.uint64(8 * rg + 1)).astype(np.int64) - 4 * rg).astype(np.int16)
+    mv = mv.reshape(nmb, 2)
+    for a, b in zip(orc.mc_compensate(y, u, v, mv, rg), ref_lib.mc_compensate(y, u, v, mv, rg)):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_add_clip_and_sub(orc):
+    rng = np.random.default_rng(7)
+    a = rng.integers(0, 256, 1000).astype(np.int16)
+    r = rng.integers(-300, 300, 1000).astype(np.int16)
+    np.testing.assert_array_equal(orc.add_clip255(a, r), np.clip(a.astype(np.int32) + r, 0, 255))
+    np.testing.assert_array_equal(orc.sub(a, r), (a.astype(np.int32) - r).astype(np.int16))
