@@ -489,6 +489,39 @@ def run_hbm_paths(torch, _lib, L, ctx, stream, dev, pk):
                      "frac": gbs / pk["hbm_gbs"] if pk.get("hbm_gbs") else None,
                      "algorithmic_bytes_per_launch": nrgb * W * H * 6},
         "workload": "FastFixedPointRGB24toYUV420Converter, 1920x1080 uniform BGR frames"}
+
+    # motion compensation: 4:2:0 frames (1088 rows: whole macroblock rows), seeded vectors in +-32 pels,
+    # 2 x frame bytes per compensation (reference read once, prediction written once)
+    nmc, MH = 16, 1088
+    fbytes = W * MH * 3  # int16 Y + U + V
+    frames_mc = torch.from_numpy(np.stack([np.concatenate([synth.pan_sequence(970 + f, W, MH, 1)[0].ravel(),
+                                                           synth.pan_sequence(990 + f, W // 2, MH // 2, 1)[0].ravel(),
+                                                           synth.pan_sequence(1010 + f, W // 2, MH // 2, 1)[0].ravel()])
+                                           for f in range(nmc)]).astype(np.int16)).to(dev)
+    preds = torch.empty_like(frames_mc)
+    nmb_mc = (W // 16) * (MH // 16)
+    mvs = torch.from_numpy(((synth.splitmix64(1030, 2 * nmb_mc * nmc) % np.uint64(257)).astype(np.int64) - 128)
+                           .astype(np.int16).reshape(nmc, nmb_mc, 2)).to(dev)
+    mc = C.c_void_p()
+    _lib.check(L.vppgpu_mc_create(ctx.handle, W, MH, 32, C.byref(mc)), "vppgpu_mc_create")
+    state = {"i": 0}
+
+    def comp():
+        i = state["i"] % nmc
+        state["i"] += 1
+        _lib.check(L.vppgpu_mc_compensate_device(mc, C.c_void_p(frames_mc[i].data_ptr()), C.c_void_p(mvs[i].data_ptr()),
+                                                 C.c_void_p(preds[i].data_ptr())), "vppgpu_mc_compensate_device")
+
+    ms = timed(comp, reps=48)
+    gbs = 2 * fbytes / (ms * 1e-3) / 1e9
+    out["motion_compensation"] = {
+        "value": 1.0 / (ms * 1e-3), "unit": "frames/s", "ms_per_frame": ms,
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": gbs / pk["hbm_gbs"] if pk.get("hbm_gbs") else None,
+                     "algorithmic_bytes_per_launch": 2 * fbytes},
+        "workload": "MotionCompensatorH264ImplStd, 1920x1088 4:2:0 frames, vectors uniform in +-32 pels, "
+                    "16-frame rotation (100 MB)"}
+    L.vppgpu_mc_destroy(mc)
     return out
 
 

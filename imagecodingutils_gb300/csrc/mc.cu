@@ -9,14 +9,13 @@
 // by OverlayMem2Dv2::EighthRead at the same vector in eighth-pel units
 // (bilinear, (z + 32) >> 6).  A zero vector leaves its block as it is.
 //
-// GB300 design: the frame is first copied to a stream-ordered temporary (the
-// reference's temporaries; it makes compensation in place possible), then
-// one thread per output sample computes its value from the temporary.  The
-// edge extension is a clamp of the sample coordinates, which gives the
-// extended border's values for every vector within the reference's range.
-// Luma half-pel samples are computed on the fly (6-tap, and j from the
-// unrounded vertical taps), the two samples of a quarter position averaged
-// as QuarterRead does.  Only full macroblock rows are compensated (the
+// GB300 design: for compensation in place the frame is first copied to a
+// stream-ordered temporary (the reference's temporaries), else read as it is;
+// the output is computed from it in one launch, one warp per macroblock
+// (luma window and the half-pel lattices its fraction reads in shared
+// memory, then both chroma blocks).  The edge extension is a clamp of the sample coordinates,
+// which gives the extended border's values for every vector within the
+// reference's range.  Only full macroblock rows are compensated (the
 // reference reads vectors past the end of its list for a partial bottom
 // row); rows below keep the reference samples.
 //
@@ -39,100 +38,183 @@ struct Plane {
         y = y < 0 ? 0 : (y >= h ? h - 1 : y);
         return __ldg(p + (size_t)y * w + x);
     }
-    __device__ __forceinline__ int tap_h(int x, int y) const  // unrounded horizontal 6-tap between x and x+1
-    {
-        return at(x - 2, y) - 5 * at(x - 1, y) + 20 * at(x, y) + 20 * at(x + 1, y) - 5 * at(x + 2, y) + at(x + 3, y);
-    }
-    __device__ __forceinline__ int tap_v(int x, int y) const
-    {
-        return at(x, y - 2) - 5 * at(x, y - 1) + 20 * at(x, y) + 20 * at(x, y + 1) - 5 * at(x, y + 2) + at(x, y + 3);
-    }
-    __device__ __forceinline__ int b(int x, int y) const { return clip255((tap_h(x, y) + 16) >> 5); }
-    __device__ __forceinline__ int hh(int x, int y) const { return clip255((tap_v(x, y) + 16) >> 5); }
-    __device__ __forceinline__ int j(int x, int y) const
-    {
-        const int s = tap_v(x - 2, y) - 5 * tap_v(x - 1, y) + 20 * tap_v(x, y) + 20 * tap_v(x + 1, y) -
-                      5 * tap_v(x + 2, y) + tap_v(x + 3, y);
-        return clip255((s + 512) >> 10);
-    }
 };
 
-// One sample of QuarterRead at full-pel (x, y) with fraction (fx, fy) in 0..3
-// (a negative offset already folded into (x, y)): the full-pel sample, one of
-// the half-pel samples b, h, j, or the rounded mean of two of them.
-__device__ int qpel_sample(const Plane& P, int x, int y, int fx, int fy)
+constexpr int kMcWarps = 4;  // macroblocks per CTA, one warp each
+
+struct McLattice {
+    short win[22][24];     // luma window, 2 samples of margin on each side of the 17x17 the block reads
+    int th[22][16];        // unrounded horizontal 6-tap between window columns x+2 and x+3 (j cases only)
+    short cwin[2][9][10];  // the 9x9 chroma windows (U, V)
+};
+
+// the six-tap (1, -5, 20, 20, -5, 1) over samples s apart
+template <int kS, typename T>
+__device__ __forceinline__ int tap6(const T* p)
 {
-    switch (fx | (fy << 2)) {
-    case 0: return P.at(x, y);
-    case 2: return P.b(x, y);
-    case 8: return P.hh(x, y);
-    case 10: return P.j(x, y);
-    case 1: return (P.at(x, y) + P.b(x, y) + 1) >> 1;
-    case 3: return (P.at(x + 1, y) + P.b(x, y) + 1) >> 1;
-    case 4: return (P.at(x, y) + P.hh(x, y) + 1) >> 1;
-    case 12: return (P.at(x, y + 1) + P.hh(x, y) + 1) >> 1;
-    case 6: return (P.j(x, y) + P.b(x, y) + 1) >> 1;
-    case 14: return (P.j(x, y) + P.b(x, y + 1) + 1) >> 1;
-    case 9: return (P.j(x, y) + P.hh(x, y) + 1) >> 1;
-    case 11: return (P.j(x, y) + P.hh(x + 1, y) + 1) >> 1;
-    case 5: return (P.b(x, y) + P.hh(x, y) + 1) >> 1;
-    case 7: return (P.b(x, y) + P.hh(x + 1, y) + 1) >> 1;
-    case 13: return (P.hh(x, y) + P.b(x, y + 1) + 1) >> 1;
-    default: return (P.hh(x + 1, y) + P.b(x, y + 1) + 1) >> 1;
+    return p[0] - 5 * p[kS] + 20 * p[2 * kS] + 20 * p[3 * kS] - 5 * p[4 * kS] + p[5 * kS];
+}
+
+// QuarterRead per quarter case cs = fx | fy << 2: one sample, or the
+// rounded average of two, from G (full-pel), b (horizontal half: 6-tap over a
+// window row), h (vertical half: 6-tap down a window column) and j (centre:
+// 6-tap down th).  Each entry: kind and offset of the first and the second
+// term (kind 4: none), offsets in window samples from the output sample's
+// row base &win[Y][X] (G(dx, dy) at (dy + 2) * 24 + dx + 2, b(dy) at
+// (dy + 2) * 24, h(dx) at dx + 2).
+enum : int { kTermG = 0, kTermB = 1, kTermH = 2, kTermJ = 3, kTermNone = 4 };
+__constant__ int4 c_quarter_terms[16] = {
+    {kTermG, 50, kTermNone, 0},  // 0: G
+    {kTermG, 50, kTermB, 48},    // 1: (G + b) / 2
+    {kTermB, 48, kTermNone, 0},  // 2: b
+    {kTermG, 51, kTermB, 48},    // 3: (G(x+1) + b) / 2
+    {kTermG, 50, kTermH, 2},     // 4: (G + h) / 2
+    {kTermB, 48, kTermH, 2},     // 5: (b + h) / 2
+    {kTermJ, 0, kTermB, 48},     // 6: (j + b) / 2
+    {kTermB, 48, kTermH, 3},     // 7: (b + h(x+1)) / 2
+    {kTermH, 2, kTermNone, 0},   // 8: h
+    {kTermJ, 0, kTermH, 2},      // 9: (j + h) / 2
+    {kTermJ, 0, kTermNone, 0},   // 10: j
+    {kTermJ, 0, kTermH, 3},      // 11: (j + h(x+1)) / 2
+    {kTermG, 74, kTermH, 2},     // 12: (G(y+1) + h) / 2
+    {kTermH, 2, kTermB, 72},     // 13: (h + b(y+1)) / 2
+    {kTermJ, 0, kTermB, 72},     // 14: (j + b(y+1)) / 2
+    {kTermH, 3, kTermB, 72},     // 15: (h(x+1) + b(y+1)) / 2
+};
+
+// The 256 luma samples of quarter case cs, lane (X = lane & 15,
+// Y = lane >> 4 + 2t): one compact loop per term kind (the kind is
+// warp-uniform), every shared access a constant offset from the lane's base.
+__device__ __forceinline__ void mc_luma_quarter(const McLattice& L, int cs, int lane, short* __restrict__ dst,
+                                                int stride)
+{
+    const int X = lane & 15, Y0 = lane >> 4;
+    const int4 tm = c_quarter_terms[cs];
+    const int nterm = tm.z == kTermNone ? 1 : 2;
+    int acc[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) acc[t] = 0;
+#pragma unroll 1
+    for (int e = 0; e < nterm; e++) {
+        const int kind = e ? tm.z : tm.x;
+        if (kind == kTermJ) {
+            const int* tb = &L.th[Y0][X];
+#pragma unroll
+            for (int t = 0; t < 8; t++) acc[t] += clip255((tap6<16>(tb + 32 * t) + 512) >> 10);
+            continue;
+        }
+        const short* w = &L.win[Y0][X] + (e ? tm.w : tm.y);
+        if (kind == kTermG) {
+#pragma unroll
+            for (int t = 0; t < 8; t++) acc[t] += w[48 * t];
+        } else if (kind == kTermB) {
+#pragma unroll
+            for (int t = 0; t < 8; t++) acc[t] += clip255((tap6<1>(w + 48 * t) + 16) >> 5);
+        } else {
+#pragma unroll
+            for (int t = 0; t < 8; t++) acc[t] += clip255((tap6<24>(w + 48 * t) + 16) >> 5);
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < 8; t++)
+        dst[(size_t)(Y0 + 2 * t) * stride + X] = (short)(nterm == 1 ? acc[t] : (acc[t] + 1) >> 1);
+}
+
+// EighthRead of the two 8x8 chroma blocks at the vector in eighth-pel units,
+// from 9x9 windows staged one column per lane (U lanes 0-8, V lanes 16-24).
+__device__ __forceinline__ void mc_chroma_blocks(McLattice& L, const Plane& U, const Plane& V, int mvx, int mvy,
+                                                 int bx, int by, int lane, short* __restrict__ ou,
+                                                 short* __restrict__ ov)
+{
+    const int ex = mvx % 8, ey = mvy % 8;
+    const int dx = mvx / 8 + (ex < 0 ? -1 : 0), dy = mvy / 8 + (ey < 0 ? -1 : 0);
+    const int fx = ex < 0 ? ex + 8 : ex, fy = ey < 0 ? ey + 8 : ey;
+    const int pl = lane >> 4, c = lane & 15;
+    if (c < 9) {
+        const Plane& P = pl ? V : U;
+        int x = bx + dx + c;
+        x = x < 0 ? 0 : (x >= P.w ? P.w - 1 : x);
+        int q[9];
+#pragma unroll
+        for (int r = 0; r < 9; r++) {
+            int y = by + dy + r;
+            y = y < 0 ? 0 : (y >= P.h ? P.h - 1 : y);
+            q[r] = __ldg(P.p + (size_t)y * P.w + x);
+        }
+#pragma unroll
+        for (int r = 0; r < 9; r++) L.cwin[pl][r][c] = (short)q[r];
+    }
+    __syncwarp();
+    const int w00 = (8 - fx) * (8 - fy), w10 = fx * (8 - fy), w01 = (8 - fx) * fy, w11 = fx * fy;
+    const int x = lane & 7, y0 = lane >> 3;
+#pragma unroll
+    for (int t = 0; t < 4; t++) {  // t: U rows 0-3, U rows 4-7, V rows 0-3, V rows 4-7
+        const int y = y0 + 4 * (t & 1);
+        const short* p = &L.cwin[t >> 1][y][x];
+        const int s = (w00 * p[0] + w10 * p[1] + w01 * p[10] + w11 * p[11] + 32) >> 6;
+        (t < 2 ? ou : ov)[(size_t)(by + y) * U.w + bx + x] = (short)s;
     }
 }
 
-__global__ void __launch_bounds__(256) k_mc_luma(Plane ref, const int* __restrict__ mv, int cols, int rows,
-                                                short* __restrict__ out)
+// One warp per macroblock: its 16x16 luma block and its two 8x8 chroma
+// blocks.  Luma stages the 22x22 reference window around the vector's
+// full-pel position (one column per lane, rows clamped only at the frame
+// edge), the j cases also the horizontal 6-taps, then computes the quarter
+// samples of its case from the term table.  Warp-synchronous: no block barrier.
+__global__ void __launch_bounds__(32 * kMcWarps, 12) k_mc_frame(Plane ry, Plane ru, Plane rv,
+                                                               const int* __restrict__ mv, int cols, int nmb,
+                                                               short* __restrict__ oy, short* __restrict__ ou,
+                                                               short* __restrict__ ov)
 {
-    const long long n = (long long)ref.w * ref.h;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int y = (int)(i / ref.w), x = (int)(i - (long long)y * ref.w);
-        int v = __ldg(ref.p + i);
-        if (y < 16 * rows) {
-            const int k = (y >> 4) * cols + (x >> 4);
-            const int m = __ldg(mv + k), mvx = vppgpu::mv_x(m), mvy = vppgpu::mv_y(m);
-            if (mvx | mvy) {
-                // C quotient and remainder, a negative remainder folded as QuarterRead does
-                const int qx = mvx % 4, qy = mvy % 4;
-                const int ox = x + mvx / 4 + (qx < 0 ? -1 : 0), oy = y + mvy / 4 + (qy < 0 ? -1 : 0);
-                v = qpel_sample(ref, ox, oy, qx < 0 ? qx + 4 : qx, qy < 0 ? qy + 4 : qy);
-            }
-        }
-        out[i] = (short)v;
+    __shared__ McLattice lat_s[kMcWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int k = blockIdx.x * kMcWarps + w;
+    if (k >= nmb) return;  // whole warps only
+    McLattice& L = lat_s[w];
+    const int n = (k % cols) * 16, m = (k / cols) * 16;
+    const int v = __ldg(mv + k), mvx = vppgpu::mv_x(v), mvy = vppgpu::mv_y(v);
+    mc_chroma_blocks(L, ru, rv, mvx, mvy, n >> 1, m >> 1, lane, ou, ov);
+    short* dst = oy + (size_t)m * ry.w + n;
+    if (!(mvx | mvy)) {  // a zero vector keeps the block
+        const short* src = ry.p + (size_t)m * ry.w + n;
+        int q[8];
+#pragma unroll
+        for (int t = 0; t < 8; t++) q[t] = __ldg(src + (size_t)(2 * t + (lane >> 4)) * ry.w + (lane & 15));
+#pragma unroll
+        for (int t = 0; t < 8; t++) dst[(size_t)(2 * t + (lane >> 4)) * ry.w + (lane & 15)] = (short)q[t];
+        return;
     }
-}
-
-// Both chroma planes: EighthRead at the vector in eighth-pel units.
-__global__ void __launch_bounds__(256) k_mc_chroma(Plane u, Plane v, const int* __restrict__ mv, int cols, int rows,
-                                                  short* __restrict__ out_u, short* __restrict__ out_v)
-{
-    const long long n = (long long)u.w * u.h;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 2 * n;
-         i += (long long)gridDim.x * blockDim.x) {
-        const bool second = i >= n;
-        const long long o = second ? i - n : i;
-        const Plane& P = second ? v : u;
-        const int y = (int)(o / P.w), x = (int)(o - (long long)y * P.w);
-        int s = __ldg(P.p + o);
-        if (y < 8 * rows) {
-            const int k = (y >> 3) * cols + (x >> 3);
-            const int m = __ldg(mv + k), mvx = vppgpu::mv_x(m), mvy = vppgpu::mv_y(m);
-            if (mvx | mvy) {
-                const int ex = mvx % 8, ey = mvy % 8;
-                const int cx = x + mvx / 8 + (ex < 0 ? -1 : 0), cy = y + mvy / 8 + (ey < 0 ? -1 : 0);
-                const int fx = ex < 0 ? ex + 8 : ex, fy = ey < 0 ? ey + 8 : ey;
-                if (fx | fy) {
-                    const int z = (8 - fx) * (8 - fy) * P.at(cx, cy) + fx * (8 - fy) * P.at(cx + 1, cy) +
-                                  (8 - fx) * fy * P.at(cx, cy + 1) + fx * fy * P.at(cx + 1, cy + 1);
-                    s = (z + 32) >> 6;
-                } else {
-                    s = P.at(cx, cy);
-                }
+    // C quotient and remainder, a negative remainder folded as QuarterRead does
+    const int qx = mvx % 4, qy = mvy % 4;
+    const int ox = n + mvx / 4 + (qx < 0 ? -1 : 0) - 2, oy0 = m + mvy / 4 + (qy < 0 ? -1 : 0) - 2;
+    const int cs = (qx < 0 ? qx + 4 : qx) | ((qy < 0 ? qy + 4 : qy) << 2);
+    if (lane < 22) {
+        int x = ox + lane;
+        x = x < 0 ? 0 : (x >= ry.w ? ry.w - 1 : x);
+        const bool inside = oy0 >= 0 && oy0 + 22 <= ry.h;
+#pragma unroll
+        for (int h0 = 0; h0 < 22; h0 += 11) {  // two halves of 11 rows in flight
+            int q[11];
+            if (inside) {
+                const short* p = ry.p + (size_t)(oy0 + h0) * ry.w + x;
+#pragma unroll
+                for (int r = 0; r < 11; r++) q[r] = __ldg(p + (size_t)r * ry.w);
+            } else {
+#pragma unroll
+                for (int r = 0; r < 11; r++) q[r] = ry.at(x, oy0 + h0 + r);
             }
+#pragma unroll
+            for (int r = 0; r < 11; r++) L.win[h0 + r][lane] = (short)q[r];
         }
-        (second ? out_v : out_u)[o] = (short)s;
     }
+    __syncwarp();
+    if (cs == 6 || cs == 9 || cs == 10 || cs == 11 || cs == 14) {  // the cases that read j
+        const int c = lane & 15, r0 = lane >> 4;
+#pragma unroll
+        for (int t = 0; t < 11; t++) L.th[r0 + 2 * t][c] = tap6<1>(&L.win[r0 + 2 * t][c]);
+        __syncwarp();
+    }
+    mc_luma_quarter(L, cs, lane, dst, ry.w);
 }
 
 // a = clip255(a + b) or a -= b, 8 samples per thread (16-byte accesses), the tail one by one.
@@ -227,16 +309,29 @@ int vppgpu_mc_compensate_device(vppgpu_mc* mc, const short* d_ref_yuv, const sho
     if (rc) return rc;
     const int W = mc->W, H = mc->H, cw = W / 2, ch = H / 2, cols = W / 16, rows = H / 16;
     const size_t ny = (size_t)W * H, nc = (size_t)cw * ch;
-    VPP_CUDA(cudaMemcpyAsync(mc->d_tmp, d_ref_yuv, (ny + 2 * nc) * sizeof(short), cudaMemcpyDeviceToDevice,
-                             ctx->stream));
-    k_mc_luma<<<grid_for(ctx, (long long)ny), 256, 0, ctx->stream>>>(Plane{mc->d_tmp, W, H}, (const int*)d_mv, cols,
-                                                                      rows, d_out_yuv);
-    VPP_CHECK_LAUNCH(ctx);
-    k_mc_chroma<<<grid_for(ctx, 2 * (long long)nc), 256, 0, ctx->stream>>>(
-        Plane{mc->d_tmp + ny, cw, ch}, Plane{mc->d_tmp + ny + nc, cw, ch}, (const int*)d_mv, cols, rows,
-        d_out_yuv + ny, d_out_yuv + ny + nc);
-    VPP_CHECK_LAUNCH(ctx);
-    ctx->launches += 2;
+    // read from the frame itself unless the output overlaps it (then from a copy, as the reference does)
+    const size_t frame = ny + 2 * nc;
+    const short* src = d_ref_yuv;
+    if (d_out_yuv < d_ref_yuv + frame && d_ref_yuv < d_out_yuv + frame) {
+        VPP_CUDA(cudaMemcpyAsync(mc->d_tmp, d_ref_yuv, frame * sizeof(short), cudaMemcpyDeviceToDevice, ctx->stream));
+        src = mc->d_tmp;
+    }
+    if (cols * rows > 0) {
+        k_mc_frame<<<(cols * rows + kMcWarps - 1) / kMcWarps, 32 * kMcWarps, 0, ctx->stream>>>(
+            Plane{src, W, H}, Plane{src + ny, cw, ch}, Plane{src + ny + nc, cw, ch}, (const int*)d_mv, cols,
+            cols * rows, d_out_yuv, d_out_yuv + ny, d_out_yuv + ny + nc);
+        VPP_CHECK_LAUNCH(ctx);
+        ctx->launches++;
+    }
+    if (16 * rows < H) {  // rows below the last whole macroblock row keep the reference samples
+        VPP_CUDA(cudaMemcpyAsync(d_out_yuv + (size_t)16 * rows * W, src + (size_t)16 * rows * W,
+                                 (size_t)(H - 16 * rows) * W * sizeof(short), cudaMemcpyDeviceToDevice, ctx->stream));
+        for (int p = 0; p < 2; p++) {
+            const size_t o = ny + p * nc + (size_t)8 * rows * cw;
+            VPP_CUDA(cudaMemcpyAsync(d_out_yuv + o, src + o, (size_t)(ch - 8 * rows) * cw * sizeof(short),
+                                     cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+    }
     return VPPGPU_OK;
 }
 
