@@ -490,6 +490,29 @@ def run_hbm_paths(torch, _lib, L, ctx, stream, dev, pk):
                      "algorithmic_bytes_per_launch": nrgb * W * H * 6},
         "workload": "FastFixedPointRGB24toYUV420Converter, 1920x1080 uniform BGR frames"}
 
+    # DC Hadamard 4x4 (Intra16x16 luma DC blocks of 1024 1080p frames, one per macroblock): forward + quant,
+    # then dequant + inverse, in place; 2 x (32 B read + 32 B written) per block
+    ndc = 1024 * 8160
+    dcb = torch.from_numpy(((synth.splitmix64(1040, ndc * 16) % np.uint64(8161)).astype(np.int64) - 4080)
+                           .astype(np.int16)).to(dev)
+
+    def dc():
+        _lib.check(L.vppgpu_fwd_dc_device(ctx.handle, C.c_void_p(dcb.data_ptr()), ndc, 4, 0, 28),
+                   "vppgpu_fwd_dc_device")
+        _lib.check(L.vppgpu_inv_dc_device(ctx.handle, C.c_void_p(dcb.data_ptr()), ndc, 4, 0, 28, None),
+                   "vppgpu_inv_dc_device")
+
+    ms = timed(dc)
+    gbs = ndc * 128 / (ms * 1e-3) / 1e9
+    out["dc_hadamard_4x4"] = {
+        "value": ndc / (ms * 1e-3), "unit": "blocks/s", "ms_per_launch_pair": ms, "blocks_per_launch": ndc,
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": gbs / pk["hbm_gbs"] if pk.get("hbm_gbs") else None,
+                     "algorithmic_bytes_per_launch_pair": ndc * 128},
+        "workload": "FastForwardDC4x4ITImpl1 + FastInverseDC4x4ITImpl1 (QP 28), the Intra16x16 DC blocks of "
+                    "1024 1920x1088 frames (267 MB, > L2)"}
+    del dcb
+
     # motion compensation: 4:2:0 frames (1088 rows: whole macroblock rows), seeded vectors in +-32 pels,
     # 2 x frame bytes per compensation (reference read once, prediction written once)
     nmc, MH = 16, 1088

@@ -30,7 +30,8 @@ __all__ = [
     "Context", "get_context", "MotionEstimatorH264ImplFull", "MotionEstimatorH264ImplMultires",
     "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorBatch",
     "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
-    "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1",
+    "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1", "FastForwardDC4x4ITImpl1",
+    "FastForwardDC2x2ITImpl1", "FastInverseDC4x4ITImpl1", "FastInverseDC2x2ITImpl1",
     "FastGpuRGB24toYUV420Converter", "VppGpuError", "load",
 ]
 
@@ -498,6 +499,114 @@ class FastInverse4x4ITImpl1(_InverseBase):
 
 class FastInverse4x4On16x16ITImpl1(_InverseBase):
     LAYOUT, UNIT = _lib.LAYOUT_MB16, 256
+
+
+class _DcForwardBase:
+    """The DC Hadamard forward transforms: Transform(ptr) on an int16 array of
+    whole size*size blocks, in place, or Transform(pIn, pCoeff)."""
+    SIZE = 4
+
+    def __init__(self, ctx: Context | None = None):
+        self._ctx = ctx or get_context()
+        self._mode = TransformAndQuant
+        self._q = 1
+
+    def SetMode(self, mode):
+        self._mode = int(mode)
+
+    def GetMode(self):
+        return self._mode
+
+    def SetParameter(self, paramID, paramVal):
+        if paramID == QUANT_ID:
+            self._q = int(paramVal)
+
+    def GetParameter(self, paramID):
+        return self._q
+
+    def SetScale(self, pScale):
+        pass
+
+    def GetScale(self):
+        return None
+
+    def Transform(self, ptr, pCoeff=None):
+        if pCoeff is not None:
+            np.copyto(pCoeff, ptr)
+            ptr = pCoeff
+        a = _as_units(ptr, self.SIZE * self.SIZE)
+        check(load().vppgpu_fwd_dc(self._ctx.handle, _ptr(a), a.size // (self.SIZE * self.SIZE), self.SIZE,
+                                   self._mode, self._q), "vppgpu_fwd_dc")
+        if a is not ptr:
+            np.copyto(ptr, a.reshape(ptr.shape))
+        return ptr
+
+
+class FastForwardDC4x4ITImpl1(_DcForwardBase):
+    """Intra16x16 luma DC (src/CodecUtils/FastForwardDC4x4ITImpl1.cpp)."""
+    SIZE = 4
+
+    def QuantiseValue(self, val, pos, qp):
+        self._q = int(qp)
+        return load().vppgpu_dc_quantise_value(int(val), int(qp))
+
+
+class FastForwardDC2x2ITImpl1(_DcForwardBase):
+    """Chroma DC (src/CodecUtils/FastForwardDC2x2ITImpl1.cpp)."""
+    SIZE = 2
+
+    def QuantiseValue(self, val, pos, qp):
+        return 0
+
+
+class _DcInverseBase:
+    SIZE = 4
+
+    def __init__(self, ctx: Context | None = None):
+        self._ctx = ctx or get_context()
+        self._mode = TransformAndQuant
+        self._q = 1
+        self._weight = np.full(self.SIZE * self.SIZE, 16, np.int32)
+
+    def SetMode(self, mode):
+        self._mode = int(mode)
+
+    def GetMode(self):
+        return self._mode
+
+    def SetParameter(self, paramID, paramVal):
+        if paramID == QUANT_ID:
+            self._q = int(paramVal)
+
+    def GetParameter(self, paramID):
+        return self._q
+
+    def SetScale(self, pScale):
+        self._weight = np.ascontiguousarray(pScale, np.int32).reshape(self.SIZE * self.SIZE).copy()
+
+    def GetScale(self):
+        return self._weight
+
+    def InverseTransform(self, ptr, pOut=None):
+        if pOut is not None:
+            np.copyto(pOut, ptr)
+            ptr = pOut
+        a = _as_units(ptr, self.SIZE * self.SIZE)
+        check(load().vppgpu_inv_dc(self._ctx.handle, _ptr(a), a.size // (self.SIZE * self.SIZE), self.SIZE,
+                                   self._mode, self._q, _ptr(self._weight)), "vppgpu_inv_dc")
+        if a is not ptr:
+            np.copyto(ptr, a.reshape(ptr.shape))
+        return ptr
+
+
+class FastInverseDC4x4ITImpl1(_DcInverseBase):
+    """Intra16x16 luma DC (src/CodecUtils/FastInverseDC4x4ITImpl1.cpp)."""
+    SIZE = 4
+
+
+class FastInverseDC2x2ITImpl1(_DcInverseBase):
+    """Chroma DC (src/CodecUtils/FastInverseDC2x2ITImpl1.cpp)."""
+    SIZE = 2
 
 
 def _as_units(a, unit):

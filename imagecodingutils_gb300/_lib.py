@@ -88,6 +88,11 @@ SIGNATURES = {
     "vppgpu_tq_roundtrip_plane_device": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
     "vppgpu_tq_roundtrip_planes_device": (_I, [_P, _P, _I, _I, _P]),
     "vppgpu_quantise_value": (_I, [C.c_short, _I, _I, _I]),
+    "vppgpu_fwd_dc": (_I, [_P, _P, _LL, _I, _I, _I]),
+    "vppgpu_fwd_dc_device": (_I, [_P, _P, _LL, _I, _I, _I]),
+    "vppgpu_inv_dc": (_I, [_P, _P, _LL, _I, _I, _I, _P]),
+    "vppgpu_inv_dc_device": (_I, [_P, _P, _LL, _I, _I, _I, _P]),
+    "vppgpu_dc_quantise_value": (_I, [C.c_short, _I]),
     "vppgpu_rgb24_to_yuv420": (_I, [_P, _I, _P, _I, _I, _I, _I, _P, _P, _P]),
     "vppgpu_rgb24_to_yuv420_device": (_I, [_P, _I, _P, _I, _I, _I, _I, _P, _P, _P]),
     "vppgpu_rgb24_to_yuv420_frames_device": (_I, [_P, _I, _P, _I, _I, _I, _I, _I, _P, _P, _P]),

@@ -8,6 +8,10 @@
 // every intermediate the reference stores to a `short` is truncated to 16
 // bits here at the same point.
 //
+// Also the DC Hadamard transforms of the Intra16x16 luma DC block (4x4) and
+// the chroma DC block (2x2), FastForward/InverseDC4x4ITImpl1 and
+// FastForward/InverseDC2x2ITImpl1.
+//
 // The work is HBM-bound (32 B read, 32 B written per block and pass), so the
 // kernels are one thread per 4x4 block with each row moved as one 8-byte
 // access; a warp covers 32 horizontally adjacent blocks, i.e. 256 contiguous
@@ -299,6 +303,207 @@ __global__ void __launch_bounds__(256) k_tq_roundtrip_single(vppgpu::TqJob j, in
         roundtrip_one(j, blk, cols_first, wt.w);
 }
 
+// ---- DC Hadamard transforms (Intra16x16 luma DC 4x4, chroma DC 2x2) --------
+// FastForwardDC4x4ITImpl1 / FastInverseDC4x4ITImpl1 and FastForwardDC2x2ITImpl1
+// / FastInverseDC2x2ITImpl1 (src/CodecUtils/FastForwardDC4x4ITImpl1.cpp:101-196,
+// FastInverseDC4x4ITImpl1.cpp:111-202, FastForwardDC2x2ITImpl1.cpp:100-164,
+// FastInverseDC2x2ITImpl1.cpp:110-157): one thread per block, the block moved
+// with 16-byte (4x4) or 8-byte (2x2) accesses when the array allows it.
+struct DcParams {
+    int mode, q, qe;
+    int na, f, sh;  // forward: NormAdjust[qp%6], 2 * (2^(15+qe) / 3), 16 + qe
+    int ls[16];     // inverse: NormAdjust[qp%6] * weight[pos]
+};
+
+DcParams make_dc(int size, int mode, int qp, const int* weight)
+{
+    static const int fwd_na[6] = {13107, 11916, 10082, 9362, 8192, 7282};
+    static const int inv_na[6] = {10, 11, 13, 14, 16, 18};
+    DcParams p;
+    p.mode = mode;
+    p.q = qp;
+    p.qe = qp / 6;
+    p.na = fwd_na[qp % 6];
+    p.f = 2 * ((1 << (15 + p.qe)) / 3);
+    p.sh = 16 + p.qe;
+    for (int i = 0; i < 16; i++) p.ls[i] = i < size * size ? inv_na[qp % 6] * (weight ? weight[i] : 16) : 0;
+    return p;
+}
+
+__device__ __forceinline__ int dc_quant(int x, const DcParams& p)
+{
+    return x < 0 ? s16(-(((-x) * p.na + p.f) >> p.sh)) : s16((x * p.na + p.f) >> p.sh);
+}
+
+__device__ __forceinline__ int shl(int x, int s) { return (int)((unsigned)x << s); }
+
+// inverse 4x4 post-scale: qp < 36 rounds at 2^(5-qe) and shifts right by 6-qe, else shifts left by qe-6
+__device__ __forceinline__ int dc4_scale(int x, int ls, const DcParams& p)
+{
+    const int v = x * ls;
+    return p.q < 36 ? s16((v + (1 << (5 - p.qe))) >> (6 - p.qe)) : s16(shl(v, p.qe - 6));
+}
+
+__device__ __forceinline__ void fwd_dc4(int* b, const DcParams& p)
+{
+    if (p.mode == 2) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) b[i] = dc_quant(b[i], p);
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < 16; r += 4) {  // rows, each stored as short
+        const int a = b[r] + b[r + 3], d = b[r] - b[r + 3], c = b[r + 1] + b[r + 2], e = b[r + 1] - b[r + 2];
+        b[r] = s16(a + c);
+        b[r + 2] = s16(a - c);
+        b[r + 1] = s16(e + d);
+        b[r + 3] = s16(d - e);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {  // columns, halved, then quantised (mode 0)
+        const int a = b[k] + b[k + 12], d = b[k] - b[k + 12], c = b[k + 4] + b[k + 8], e = b[k + 4] - b[k + 8];
+        const int y0 = (a + c) >> 1, y2 = (a - c) >> 1, y1 = (e + d) >> 1, y3 = (d - e) >> 1;
+        b[k] = p.mode == 0 ? dc_quant(y0, p) : s16(y0);
+        b[k + 4] = p.mode == 0 ? dc_quant(y1, p) : s16(y1);
+        b[k + 8] = p.mode == 0 ? dc_quant(y2, p) : s16(y2);
+        b[k + 12] = p.mode == 0 ? dc_quant(y3, p) : s16(y3);
+    }
+}
+
+__device__ __forceinline__ void inv_dc4(int* b, const DcParams& p)
+{
+    if (p.mode == 2) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) b[i] = dc4_scale(b[i], p.ls[i], p);
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {  // columns, each stored as short
+        const int s0 = b[k] + b[8 + k], s1 = b[k] - b[8 + k], s2 = b[4 + k] - b[12 + k], s3 = b[4 + k] + b[12 + k];
+        b[k] = s16(s0 + s3);
+        b[12 + k] = s16(s0 - s3);
+        b[4 + k] = s16(s1 + s2);
+        b[8 + k] = s16(s1 - s2);
+    }
+#pragma unroll
+    for (int r = 0; r < 16; r += 4) {  // rows, post-scaled (mode 0)
+        const int s0 = b[r] + b[2 + r], s1 = b[r] - b[2 + r], s2 = b[1 + r] - b[3 + r], s3 = b[1 + r] + b[3 + r];
+        if (p.mode == 0) {
+            const int y0 = dc4_scale(s0 + s3, p.ls[r], p), y1 = dc4_scale(s1 + s2, p.ls[r + 1], p);
+            const int y2 = dc4_scale(s1 - s2, p.ls[r + 2], p), y3 = dc4_scale(s0 - s3, p.ls[r + 3], p);
+            b[r] = y0;
+            b[r + 1] = y1;
+            b[r + 2] = y2;
+            b[r + 3] = y3;
+        } else {
+            b[r] = s16(s0 + s3);
+            b[r + 3] = s16(s0 - s3);
+            b[r + 1] = s16(s1 + s2);
+            b[r + 2] = s16(s1 - s2);
+        }
+    }
+}
+
+__device__ __forceinline__ void fwd_dc2(int* b, const DcParams& p)
+{
+    if (p.mode == 2) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) b[i] = dc_quant(b[i], p);
+        return;
+    }
+    const int s0 = b[0] + b[1], s2 = b[0] - b[1], s1 = b[2] + b[3], s3 = b[2] - b[3];
+    const int y0 = s0 + s1, y2 = s0 - s1, y1 = s2 + s3, y3 = s2 - s3;
+    b[0] = p.mode == 0 ? dc_quant(y0, p) : s16(y0);
+    b[1] = p.mode == 0 ? dc_quant(y1, p) : s16(y1);
+    b[2] = p.mode == 0 ? dc_quant(y2, p) : s16(y2);
+    b[3] = p.mode == 0 ? dc_quant(y3, p) : s16(y3);
+}
+
+// inverse 2x2 post-scale: (x * levelScale << qe) >> 5
+__device__ __forceinline__ void inv_dc2(int* b, const DcParams& p)
+{
+    if (p.mode == 2) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) b[i] = s16(shl(b[i] * p.ls[i], p.qe) >> 5);
+        return;
+    }
+    const int s0 = b[0] + b[1], s2 = b[0] - b[1], s1 = b[2] + b[3], s3 = b[2] - b[3];
+    if (p.mode == 0) {
+        const int x0 = (s0 + s1) * p.ls[0], x1 = (s2 + s3) * p.ls[1], x2 = (s0 - s1) * p.ls[2],
+                  x3 = (s2 - s3) * p.ls[3];
+        b[0] = s16(shl(x0, p.qe) >> 5);
+        b[1] = s16(shl(x1, p.qe) >> 5);
+        b[2] = s16(shl(x2, p.qe) >> 5);
+        b[3] = s16(shl(x3, p.qe) >> 5);
+    } else {
+        b[0] = s16(s0 + s1);
+        b[2] = s16(s0 - s1);
+        b[1] = s16(s2 + s3);
+        b[3] = s16(s2 - s3);
+    }
+}
+
+template <int kN>
+__device__ __forceinline__ void load_unit(const short* q, bool vec, int* b)
+{
+    auto lo = [](unsigned w) { return (int)(short)(w & 0xffff); };
+    auto hi = [](unsigned w) { return (int)(short)(w >> 16); };
+    if (vec) {
+        if constexpr (kN == 16) {
+#pragma unroll
+            for (int h = 0; h < 16; h += 8) {
+                const uint4 v = *reinterpret_cast<const uint4*>(q + h);
+                b[h] = lo(v.x), b[h + 1] = hi(v.x), b[h + 2] = lo(v.y), b[h + 3] = hi(v.y);
+                b[h + 4] = lo(v.z), b[h + 5] = hi(v.z), b[h + 6] = lo(v.w), b[h + 7] = hi(v.w);
+            }
+        } else {
+            const uint2 v = *reinterpret_cast<const uint2*>(q);
+            b[0] = lo(v.x), b[1] = hi(v.x), b[2] = lo(v.y), b[3] = hi(v.y);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kN; i++) b[i] = q[i];
+    }
+}
+
+template <int kN>
+__device__ __forceinline__ void store_unit(short* q, bool vec, const int* b)
+{
+    auto pk = [&](int i) { return (unsigned)(b[i] & 0xffff) | ((unsigned)b[i + 1] << 16); };
+    if (vec) {
+        if constexpr (kN == 16) {
+#pragma unroll
+            for (int h = 0; h < 16; h += 8)
+                *reinterpret_cast<uint4*>(q + h) = make_uint4(pk(h), pk(h + 2), pk(h + 4), pk(h + 6));
+        } else {
+            *reinterpret_cast<uint2*>(q) = make_uint2(pk(0), pk(2));
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kN; i++) q[i] = (short)b[i];
+    }
+}
+
+template <int kSize, bool kFwd>
+__global__ void __launch_bounds__(256) k_dc_units(short* __restrict__ data, long long nunits, bool vec, DcParams p)
+{
+    constexpr int kN = kSize * kSize;
+    for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < nunits;
+         u += (long long)gridDim.x * blockDim.x) {
+        short* q = data + u * kN;
+        int b[kN];
+        load_unit<kN>(q, vec, b);
+        if constexpr (kSize == 4) {
+            if constexpr (kFwd) fwd_dc4(b, p);
+            else inv_dc4(b, p);
+        } else {
+            if constexpr (kFwd) fwd_dc2(b, p);
+            else inv_dc2(b, p);
+        }
+        store_unit<kN>(q, vec, b);
+    }
+}
+
 int grid_for(vppgpu_ctx* ctx, long long nblocks)
 {
     long long want = (nblocks + 255) / 256;
@@ -456,6 +661,80 @@ int vppgpu_tq_roundtrip_planes_device(vppgpu_ctx* ctx, const vppgpu_tq_job* d_jo
     // x extent sized for the largest plane the descriptors may hold (8K luma)
     return vppgpu::launch_tq_jobs(ctx, reinterpret_cast<const vppgpu::TqJob*>(d_jobs), njobs,
                                   (long long)(ctx->sm_count) * 8 * 256, inv_order, weight16);
+}
+
+static int dc_device(vppgpu_ctx* ctx, short* d, long long nunits, int size, bool forward, int mode, int qp,
+                     const int* weight)
+{
+    if (!ctx || nunits < 0 || (nunits > 0 && !d) || (size != 2 && size != 4) || mode < 0 || mode > 2 || qp < 0 ||
+        qp > 51)
+        return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(ctx);
+    if (rc) return rc;
+    if (nunits == 0) return VPPGPU_OK;
+    const bool vec = ((uintptr_t)d & (size == 4 ? 15 : 7)) == 0;
+    const DcParams p = make_dc(size, mode, qp, forward ? nullptr : weight);
+    const int g = grid_for(ctx, nunits);
+    if (size == 4 && forward) k_dc_units<4, true><<<g, 256, 0, ctx->stream>>>(d, nunits, vec, p);
+    else if (size == 4) k_dc_units<4, false><<<g, 256, 0, ctx->stream>>>(d, nunits, vec, p);
+    else if (forward) k_dc_units<2, true><<<g, 256, 0, ctx->stream>>>(d, nunits, vec, p);
+    else k_dc_units<2, false><<<g, 256, 0, ctx->stream>>>(d, nunits, vec, p);
+    VPP_CHECK_LAUNCH(ctx);
+    return VPPGPU_OK;
+}
+
+static int dc_host(vppgpu_ctx* ctx, short* data, long long nunits, int size, bool forward, int mode, int qp,
+                   const int* weight)
+{
+    if (!ctx || nunits < 0 || (nunits > 0 && !data) || (size != 2 && size != 4) || mode < 0 || mode > 2 || qp < 0 ||
+        qp > 51)
+        return VPPGPU_ERR_INVALID_ARG;
+    int rc = vppgpu::bind(ctx);
+    if (rc) return rc;
+    const size_t bytes = (size_t)nunits * size * size * sizeof(short);
+    if (bytes == 0) return VPPGPU_OK;
+    short* d = nullptr;
+    VPP_CUDA(cudaMallocAsync((void**)&d, bytes, ctx->stream));
+    cudaError_t e = cudaMemcpyAsync(d, data, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        rc = dc_device(ctx, d, nunits, size, forward, mode, qp, weight);
+        if (rc == VPPGPU_OK) e = cudaMemcpyAsync(data, d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    }
+    cudaFreeAsync(d, ctx->stream);
+    cudaError_t e2 = cudaStreamSynchronize(ctx->stream);
+    if (rc) return rc;
+    if (e != cudaSuccess) return vppgpu::cuda_status(e);
+    if (e2 != cudaSuccess) return vppgpu::cuda_status(e2);
+    return VPPGPU_OK;
+}
+
+int vppgpu_fwd_dc_device(vppgpu_ctx* ctx, short* d_data, long long nunits, int size, int mode, int qp)
+{
+    return dc_device(ctx, d_data, nunits, size, true, mode, qp, nullptr);
+}
+
+int vppgpu_inv_dc_device(vppgpu_ctx* ctx, short* d_data, long long nunits, int size, int mode, int qp,
+                         const int* weight)
+{
+    return dc_device(ctx, d_data, nunits, size, false, mode, qp, weight);
+}
+
+int vppgpu_fwd_dc(vppgpu_ctx* ctx, short* data, long long nunits, int size, int mode, int qp)
+{
+    return dc_host(ctx, data, nunits, size, true, mode, qp, nullptr);
+}
+
+int vppgpu_inv_dc(vppgpu_ctx* ctx, short* data, long long nunits, int size, int mode, int qp, const int* weight)
+{
+    return dc_host(ctx, data, nunits, size, false, mode, qp, weight);
+}
+
+int vppgpu_dc_quantise_value(short val, int qp)
+{
+    if (qp < 0 || qp > 51) return 0;
+    const DcParams p = make_dc(4, 0, qp, nullptr);
+    const int x = (int)val;
+    return x < 0 ? (int)(short)(-(((-x) * p.na + p.f) >> p.sh)) : (int)(short)((x * p.na + p.f) >> p.sh);
 }
 
 int vppgpu_quantise_value(short val, int pos, int qp, int intra)

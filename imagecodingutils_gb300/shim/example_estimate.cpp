@@ -9,9 +9,12 @@
 // (constructor, Create, SetMode(0), Estimate, predictor side effect), then
 // runs the forward/inverse 4x4 transform classes
 // on the motion-compensated-free residual (source - reference) of the first
-// macroblock row.  out.bin receives: the vectors (N x 2 int16), avgDistortion
-// (int64), the predictor's copy of the vectors (N x 2 int32), then the
-// transformed residual levels and reconstruction (int16).
+// macroblock row, and the Intra16x16-style DC path (4x4 transform only, DC
+// gathered per macroblock, DC Hadamard + quantisation and inverse) on it.
+// out.bin receives: the vectors (N x 2 int16), avgDistortion (int64), the
+// predictor's copy of the vectors (N x 2 int32), the transformed residual
+// levels and reconstruction (int16), then the DC levels and the inverse DC
+// (int16, 16 per macroblock of the row).
 #include <stdio.h>
 #include <stdlib.h>
 #include <string>
@@ -79,11 +82,34 @@ int main(int argc, char** argv)
     GpuForward4x4IT fwd;
     fwd.SetParameter(IForwardTransform::INTRA_FLAG_ID, 0);
     fwd.SetParameter(IForwardTransform::QUANT_ID, 28);
+    std::vector<short> levels_src = blocks;
     fwd.TransformBlocks(blocks.data(), nblk);
     std::vector<short> levels = blocks;
     GpuInverse4x4IT inv;
     inv.SetParameter(IInverseTransform::QUANT_ID, 28);
     inv.InverseTransformBlocks(blocks.data(), nblk);
+
+    // Intra16x16-style DC path on the same residual: 4x4 transform only, the
+    // 16 DC coefficients of each macroblock gathered into a 4x4 block, then the
+    // DC Hadamard with quantisation and its inverse
+    std::vector<short> coeffs(16 * (size_t)nblk);
+    for (int b = 0; b < nblk; b++)
+        for (int i = 0; i < 16; i++) coeffs[16 * b + i] = levels_src[16 * b + i];
+    GpuForward4x4IT it_only;
+    it_only.SetMode(IForwardTransform::TransformOnly);
+    it_only.TransformBlocks(coeffs.data(), nblk);
+    const int nmbr = w / 16;
+    std::vector<short> dc(16 * (size_t)nmbr);
+    for (int m = 0; m < nmbr; m++)
+        for (int r = 0; r < 4; r++)
+            for (int c = 0; c < 4; c++) dc[16 * m + 4 * r + c] = coeffs[16 * (r * (w / 4) + 4 * m + c)];
+    GpuForwardDCIT fdc(4);
+    fdc.SetParameter(IForwardTransform::QUANT_ID, 28);
+    fdc.TransformBlocks(dc.data(), nmbr);
+    std::vector<short> dc_levels = dc;
+    GpuInverseDCIT idc(4);
+    idc.SetParameter(IInverseTransform::QUANT_ID, 28);
+    idc.InverseTransformBlocks(dc.data(), nmbr);
 
     FILE* o = fopen(argv[5], "wb");
     for (int k = 0; k < nmb; k++) {
@@ -95,6 +121,8 @@ int main(int argc, char** argv)
     fwrite(pred.mv.data(), 4, pred.mv.size(), o);
     fwrite(levels.data(), 2, levels.size(), o);
     fwrite(blocks.data(), 2, blocks.size(), o);
+    fwrite(dc_levels.data(), 2, dc_levels.size(), o);
+    fwrite(dc.data(), 2, dc.size(), o);
     fclose(o);
     delete me;
     delete[] incl;

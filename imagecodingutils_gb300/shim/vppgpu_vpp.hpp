@@ -388,6 +388,77 @@ protected:
 };
 
 // ---------------------------------------------------------------------------
+// DC Hadamard transforms: size 4 replaces FastForwardDC4x4ITImpl1 /
+// FastInverseDC4x4ITImpl1 (Intra16x16 luma DC), size 2 FastForwardDC2x2ITImpl1
+// / FastInverseDC2x2ITImpl1 (chroma DC).  TransformBlocks() takes many
+// blocks at once.
+// ---------------------------------------------------------------------------
+class GpuForwardDCIT : public IForwardTransform {
+public:
+    explicit GpuForwardDCIT(int size = 4) : _size(size), _mode(TransformAndQuant), _q(1) {}
+    virtual void Transform(void* ptr) { TransformBlocks(ptr, 1); }
+    virtual void Transform(void* pIn, void* pCoeff)
+    {
+        memcpy(pCoeff, pIn, sizeof(short) * _size * _size);
+        Transform(pCoeff);
+    }
+    void TransformBlocks(void* ptr, long long nunits)
+    {
+        vppgpu_fwd_dc(vppgpu_vpp::context(), (short*)ptr, nunits, _size, _mode, _q);
+    }
+    virtual void SetScale(void* pScale) { (void)pScale; }
+    virtual void* GetScale(void) { return NULL; }
+    virtual void SetMode(int mode) { _mode = mode; }
+    virtual int GetMode(void) { return _mode; }
+    virtual void SetParameter(int paramID, int paramVal)
+    {
+        if (paramID == QUANT_ID) _q = paramVal;
+    }
+    virtual int GetParameter(int paramID) { (void)paramID; return _q; }
+    virtual int QuantiseValue(short val, int pos, int qp)
+    {
+        (void)pos;
+        if (_size != 4) return 0;  // FastForwardDC2x2ITImpl1 has no quantiser of single values
+        _q = qp;
+        return vppgpu_dc_quantise_value(val, qp);
+    }
+
+protected:
+    int _size, _mode, _q;
+};
+
+class GpuInverseDCIT : public IInverseTransform {
+public:
+    explicit GpuInverseDCIT(int size = 4) : _size(size), _mode(TransformAndQuant), _q(1)
+    {
+        for (int i = 0; i < 16; i++) _weight[i] = 16;
+    }
+    virtual void InverseTransform(void* ptr) { InverseTransformBlocks(ptr, 1); }
+    virtual void InverseTransform(void* pCoeff, void* pOut)
+    {
+        memcpy(pOut, pCoeff, sizeof(short) * _size * _size);
+        InverseTransform(pOut);
+    }
+    void InverseTransformBlocks(void* ptr, long long nunits)
+    {
+        vppgpu_inv_dc(vppgpu_vpp::context(), (short*)ptr, nunits, _size, _mode, _q, _weight);
+    }
+    virtual void SetScale(void* pScale) { memcpy(_weight, pScale, sizeof(int) * _size * _size); }
+    virtual void* GetScale(void) { return (void*)_weight; }
+    virtual void SetMode(int mode) { _mode = mode; }
+    virtual int GetMode(void) { return _mode; }
+    virtual void SetParameter(int paramID, int paramVal)
+    {
+        if (paramID == QUANT_ID) _q = paramVal;
+    }
+    virtual int GetParameter(int paramID) { (void)paramID; return _q; }
+
+protected:
+    int _size, _mode, _q;
+    int _weight[16];
+};
+
+// ---------------------------------------------------------------------------
 // The GPU slot vpp reserves for colour conversion (an empty class in the
 // reference, include/ImageUtils/FastGpuRGB24toYUV420Converter.h).
 // ---------------------------------------------------------------------------

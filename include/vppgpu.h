@@ -334,6 +334,24 @@ typedef struct vppgpu_tq_job {
 int vppgpu_tq_roundtrip_planes_device(vppgpu_ctx* ctx, const vppgpu_tq_job* d_jobs, int njobs, int inv_order,
                                       const int* weight16);
 
+/* DC Hadamard transforms over nunits contiguous blocks in place, with
+ * SetMode(mode) and SetParameter(QUANT_ID, qp): size 4 = the Intra16x16 luma
+ * DC block, FastForwardDC4x4ITImpl1::Transform(void*)
+ * (src/CodecUtils/FastForwardDC4x4ITImpl1.cpp:101-196) and
+ * FastInverseDC4x4ITImpl1::InverseTransform(void*) (FastInverseDC4x4ITImpl1.cpp:111-202);
+ * size 2 = the chroma DC block, FastForwardDC2x2ITImpl1.cpp:100-164 and
+ * FastInverseDC2x2ITImpl1.cpp:110-157.  weight: NULL (flat 16) or the
+ * SetScale() array of size*size ints (FastInverseDC4x4ITImpl1.cpp:224-240). */
+int vppgpu_fwd_dc(vppgpu_ctx* ctx, short* data, long long nunits, int size, int mode, int qp);
+int vppgpu_fwd_dc_device(vppgpu_ctx* ctx, short* d_data, long long nunits, int size, int mode, int qp);
+int vppgpu_inv_dc(vppgpu_ctx* ctx, short* data, long long nunits, int size, int mode, int qp, const int* weight);
+int vppgpu_inv_dc_device(vppgpu_ctx* ctx, short* d_data, long long nunits, int size, int mode, int qp,
+                         const int* weight);
+
+/* FastForwardDC4x4ITImpl1::QuantiseValue (src/CodecUtils/FastForwardDC4x4ITImpl1.cpp:268-283),
+ * host-side scalar helper (FastForwardDC2x2ITImpl1::QuantiseValue returns 0). */
+int vppgpu_dc_quantise_value(short val, int qp);
+
 /* FastForward4x4ITImpl2::QuantiseValue (src/CodecUtils/FastForward4x4ITImpl2.cpp:640-683),
  * host-side scalar helper kept for API completeness. */
 int vppgpu_quantise_value(short val, int pos, int qp, int intra);

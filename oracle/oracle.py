@@ -61,6 +61,9 @@ class Oracle:
         L.vo_fwd4x4.argtypes = [_P, _I, _I, _I, _I, _I]
         L.vo_inv4x4.argtypes = [_P, _I, _I, _I, _I, _P]
         L.vo_quantise_value.argtypes = [C.c_short, _I, _I, _I]
+        L.vo_fwd_dc.argtypes = [_P, _I, _I, _I, _I]
+        L.vo_inv_dc.argtypes = [_P, _I, _I, _I, _I, _P]
+        L.vo_dc_quantise_value.argtypes = [C.c_short, _I]
         L.vo_rgb24_to_yuv420.argtypes = [_I, _P, _I, _I, _I, _I, _P, _P, _P]
         L.vo_bench_me_full.argtypes = [_P, _P, _I, _I, _I, _I, _I, _P]
 
@@ -195,6 +198,22 @@ class Oracle:
     def quantise_value(self, val, pos, qp, intra):
         return self.lib.vo_quantise_value(int(val), pos, qp, intra)
 
+    def fwd_dc(self, data, size, mode, qp):
+        """size 4: FastForwardDC4x4ITImpl1, size 2: FastForwardDC2x2ITImpl1, on
+        contiguous size*size blocks."""
+        d = np.array(data, dtype=np.int16, copy=True, order="C")
+        self.lib.vo_fwd_dc(_ptr(d), d.size // (size * size), size, mode, qp)
+        return d
+
+    def inv_dc(self, data, size, mode, qp, weight=None):
+        d = np.array(data, dtype=np.int16, copy=True, order="C")
+        wt = None if weight is None else np.ascontiguousarray(weight, dtype=np.int32)
+        self.lib.vo_inv_dc(_ptr(d), d.size // (size * size), size, mode, qp, _ptr(wt))
+        return d
+
+    def dc_quantise_value(self, val, qp):
+        return self.lib.vo_dc_quantise_value(int(val), qp)
+
     def rgb_to_yuv(self, kind, bgr, chr_off=0, flip=0):
         h, w, _ = bgr.shape
         bgr = np.ascontiguousarray(bgr, dtype=np.uint8)
@@ -231,6 +250,9 @@ class Reference:
         L.ref_fwd_transform.argtypes = [_I, _P, _I, _I, _I, _I]
         L.ref_inv_transform.argtypes = [_I, _P, _I, _I, _I, _P]
         L.ref_quantise_value.argtypes = [C.c_short, _I, _I, _I]
+        L.ref_fwd_dc.argtypes = [_P, _I, _I, _I, _I]
+        L.ref_inv_dc.argtypes = [_P, _I, _I, _I, _I, _P]
+        L.ref_dc_quantise_value.argtypes = [C.c_short, _I]
         L.ref_rgb_to_yuv.argtypes = [_I, _P, _I, _I, _I, _I, _P, _P, _P]
         L.ref_mc_compensate.argtypes = [_I, _I, _I, _P, _P]
 
@@ -278,6 +300,20 @@ class Reference:
 
     def quantise_value(self, val, pos, qp, intra):
         return self.lib.ref_quantise_value(int(val), pos, qp, intra)
+
+    def fwd_dc(self, data, size, mode, qp):
+        d = np.array(data, dtype=np.int16, copy=True, order="C")
+        self.lib.ref_fwd_dc(_ptr(d), d.size // (size * size), size, mode, qp)
+        return d
+
+    def inv_dc(self, data, size, mode, qp, weight=None):
+        d = np.array(data, dtype=np.int16, copy=True, order="C")
+        wt = None if weight is None else np.ascontiguousarray(weight, dtype=np.int32)
+        self.lib.ref_inv_dc(_ptr(d), d.size // (size * size), size, mode, qp, _ptr(wt))
+        return d
+
+    def dc_quantise_value(self, val, qp):
+        return self.lib.ref_dc_quantise_value(int(val), qp)
 
     def rgb_to_yuv(self, kind, bgr, chr_off=0, flip=0):
         h, w, _ = bgr.shape

@@ -25,6 +25,10 @@
 #include "FastInverse4x4ITImpl1.h"
 #include "FastForward4x4On16x16ITImpl1.h"
 #include "FastInverse4x4On16x16ITImpl1.h"
+#include "FastForwardDC4x4ITImpl1.h"
+#include "FastInverseDC4x4ITImpl1.h"
+#include "FastForwardDC2x2ITImpl1.h"
+#include "FastInverseDC2x2ITImpl1.h"
 #include "FastFixedPointRGB24toYUV420Converter.h"
 #include "RealRGB24toYUV420Converter.h"
 #include "RealRGB24toYUV420ConverterImpl2.h"
@@ -174,6 +178,41 @@ int ref_inv_transform(int impl, short* data, int nunits, int mode, int qp, const
     for (int u = 0; u < nunits; u++) t->InverseTransform(data + (size_t)u * unit);
     delete t;
     return 0;
+}
+
+/* size 4: FastForwardDC4x4ITImpl1, size 2: FastForwardDC2x2ITImpl1. */
+int ref_fwd_dc(short* data, int nunits, int size, int mode, int qp)
+{
+    IForwardTransform* t = NULL;
+    if (size == 4) t = new FastForwardDC4x4ITImpl1();
+    else if (size == 2) t = new FastForwardDC2x2ITImpl1();
+    else return -1;
+    t->SetMode(mode);
+    t->SetParameter(IForwardTransform::QUANT_ID, qp);
+    for (int u = 0; u < nunits; u++) t->Transform(data + (size_t)u * size * size);
+    delete t;
+    return 0;
+}
+
+/* size 4: FastInverseDC4x4ITImpl1, size 2: FastInverseDC2x2ITImpl1; weight: NULL or size*size ints. */
+int ref_inv_dc(short* data, int nunits, int size, int mode, int qp, const int* weight)
+{
+    IInverseTransform* t = NULL;
+    if (size == 4) t = new FastInverseDC4x4ITImpl1();
+    else if (size == 2) t = new FastInverseDC2x2ITImpl1();
+    else return -1;
+    if (weight) t->SetScale((void*)weight);
+    t->SetMode(mode);
+    t->SetParameter(IInverseTransform::QUANT_ID, qp);
+    for (int u = 0; u < nunits; u++) t->InverseTransform(data + (size_t)u * size * size);
+    delete t;
+    return 0;
+}
+
+int ref_dc_quantise_value(short val, int qp)
+{
+    FastForwardDC4x4ITImpl1 t;
+    return t.QuantiseValue(val, 0, qp);
 }
 
 int ref_quantise_value(short val, int pos, int qp, int intra)

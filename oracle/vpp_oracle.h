@@ -126,6 +126,12 @@ void vo_inv4x4(short* data, int nunits, int layout, int mode, int qp, const int*
 /* FastForward4x4ITImpl2::QuantiseValue (FastForward4x4ITImpl2.cpp:640-683). */
 int vo_quantise_value(short val, int pos, int qp, int intra);
 
+/* DC Hadamard transforms (oracle_dc.c): size 4 = FastForward/InverseDC4x4ITImpl1,
+ * size 2 = FastForward/InverseDC2x2ITImpl1; nunits contiguous size*size blocks. */
+void vo_fwd_dc(short* data, int nunits, int size, int mode, int qp);
+void vo_inv_dc(short* data, int nunits, int size, int mode, int qp, const int* weight);
+int vo_dc_quantise_value(short val, int qp);
+
 /* ------------------------------------------------------------------------ */
 /* RGB24 -> YUV420                                                           */
 /* ------------------------------------------------------------------------ */

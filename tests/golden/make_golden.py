@@ -188,6 +188,37 @@ def transform_fixtures(ref: oracle.Reference) -> dict:
     return out
 
 
+def dc_fixtures(ref: oracle.Reference) -> dict:
+    """DC Hadamard transforms: forward inputs span small DC values, typical
+    Intra16x16 DC magnitudes and the full int16 range (wrap-around of the
+    short stores); inverse inputs are the forward levels and values up to
+    +-2048 (no int overflow in the reference's products)."""
+    out = {}
+    for size in (4, 2):
+        n = size * size
+        r = lambda seed, m, lim: ((synth.splitmix64(seed, m) % np.uint64(2 * lim + 1)).astype(np.int64) - lim)
+        x = np.concatenate([r(31 + size, n * 24, 300), r(41 + size, n * 24, 4080),
+                            r(51 + size, n * 16, 32768).clip(-32768, 32767)]).astype(np.int16)
+        xi = r(61 + size, n * 48, 2048).astype(np.int16)
+        weight = (np.arange(n, dtype=np.int32) * 5 + 9)
+        out[f"s{size}_x"], out[f"s{size}_xi"], out[f"s{size}_weight"] = x, xi, weight
+        for qp in range(52):
+            lev = ref.fwd_dc(x, size, 0, qp)
+            out[f"s{size}_fwd_q{qp}"] = lev
+            out[f"s{size}_inv_q{qp}"] = ref.inv_dc(lev, size, 0, qp)
+        for qp in (0, 11, 23, 28, 35, 36, 51):
+            for mode in (1, 2):
+                out[f"s{size}_fwd_m{mode}_q{qp}"] = ref.fwd_dc(x, size, mode, qp)
+                out[f"s{size}_inv_m{mode}_q{qp}"] = ref.inv_dc(xi, size, mode, qp)
+            out[f"s{size}_invw_q{qp}"] = ref.inv_dc(xi, size, 0, qp, weight)
+    qv = []
+    for qp in (0, 7, 28, 40, 51):
+        for val in (-32768, -4080, -300, -1, 0, 1, 255, 1000, 32767):
+            qv.append((val, qp, ref.dc_quantise_value(val, qp)))
+    out["quantise_value"] = np.array(qv, np.int32)
+    return out
+
+
 def colour_fixtures(ref: oracle.Reference) -> dict:
     bgr = synth.rgb_frame(21, 64, 48)
     out = {"bgr": bgr}
@@ -206,7 +237,7 @@ def main() -> None:
     ref = oracle.Reference()
     makers = {"me_full": me_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "mc": mc_fixtures,
-              "transform": transform_fixtures, "colour": colour_fixtures}
+              "transform": transform_fixtures, "dc": dc_fixtures, "colour": colour_fixtures}
     names = sys.argv[1:] or list(makers)
     for name in names:
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **makers[name](ref))

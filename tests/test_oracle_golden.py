@@ -54,6 +54,39 @@ def test_transform_matches_reference(orc, golden):
         assert orc.quantise_value(int(val), int(pos), int(qp), int(intra)) == want
 
 
+@pytest.mark.parametrize("size", [4, 2])
+def test_dc_transforms_match_reference(orc, golden, size):
+    """FastForward/InverseDC4x4ITImpl1 (size 4) and DC2x2ITImpl1 (size 2)."""
+    g = golden("dc.npz")
+    x, xi, wt = g[f"s{size}_x"], g[f"s{size}_xi"], g[f"s{size}_weight"]
+    for qp in range(52):
+        np.testing.assert_array_equal(orc.fwd_dc(x, size, 0, qp), g[f"s{size}_fwd_q{qp}"], err_msg=f"qp{qp}")
+        np.testing.assert_array_equal(orc.inv_dc(g[f"s{size}_fwd_q{qp}"], size, 0, qp), g[f"s{size}_inv_q{qp}"])
+    for qp in (0, 11, 23, 28, 35, 36, 51):
+        for mode in (1, 2):
+            np.testing.assert_array_equal(orc.fwd_dc(x, size, mode, qp), g[f"s{size}_fwd_m{mode}_q{qp}"])
+            np.testing.assert_array_equal(orc.inv_dc(xi, size, mode, qp), g[f"s{size}_inv_m{mode}_q{qp}"])
+        np.testing.assert_array_equal(orc.inv_dc(xi, size, 0, qp, wt), g[f"s{size}_invw_q{qp}"])
+    if size == 4:
+        for val, qp, want in g["quantise_value"]:
+            assert orc.dc_quantise_value(int(val), int(qp)) == want
+
+
+def test_dc_transforms_against_compiled_reference(orc):
+    if not oracle_mod.Reference.available():
+        pytest.skip("oracle/_ref not built (the reference sources are absent here)")
+    ref = oracle_mod.Reference()
+    rng = np.random.default_rng(7)
+    for size in (4, 2):
+        n = size * size
+        x = rng.integers(-32768, 32768, n * 200).astype(np.int16)
+        xi = rng.integers(-512, 513, n * 200).astype(np.int16)
+        for qp in range(0, 52, 3):
+            for mode in (0, 1, 2):
+                np.testing.assert_array_equal(orc.fwd_dc(x, size, mode, qp), ref.fwd_dc(x, size, mode, qp))
+                np.testing.assert_array_equal(orc.inv_dc(xi, size, mode, qp), ref.inv_dc(xi, size, mode, qp))
+
+
 def test_colour_matches_reference(orc, golden):
     g = golden("colour.npz")
     for kind in (0, 1, 2):

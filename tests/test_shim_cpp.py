@@ -55,7 +55,8 @@ def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
     pred = np.frombuffer(raw[4 * nmb + 8:12 * nmb + 8], np.int32).reshape(nmb, 2)
     rest = np.frombuffer(raw[12 * nmb + 8:], np.int16)
     nblk = (w // 4) * 4
-    levels, recon = rest[:16 * nblk], rest[16 * nblk:]
+    levels, recon = rest[:16 * nblk], rest[16 * nblk:32 * nblk]
+    dc_lev, dc_rec = rest[32 * nblk:32 * nblk + w], rest[32 * nblk + w:]
     ones = np.ones(nmb, np.uint8)
     if kind == "full":
         mv_o, _, avg_o = orc.me_full(fr[1], fr[0], mr, dist_incl=ones)
@@ -74,3 +75,8 @@ def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
     lev_o = orc.fwd4x4(blocks, 0, 0, 28, 0)
     np.testing.assert_array_equal(levels.reshape(-1, 16), lev_o)
     np.testing.assert_array_equal(recon.reshape(-1, 16), orc.inv4x4(lev_o, 0, 0, 28))
+    coeffs = orc.fwd4x4(blocks, 0, 1, 1, 1).reshape(4, w // 16, 4, 16)   # (block row, MB, block col, coeff)
+    dc = coeffs[:, :, :, 0].transpose(1, 0, 2).reshape(-1, 16)
+    dc_lev_o = orc.fwd_dc(dc, 4, 0, 28)
+    np.testing.assert_array_equal(dc_lev.reshape(-1, 16), dc_lev_o)
+    np.testing.assert_array_equal(dc_rec.reshape(-1, 16), orc.inv_dc(dc_lev_o, 4, 0, 28))
