@@ -253,54 +253,143 @@ static_assert(sizeof(TqJob) == sizeof(vppgpu_tq_job), "TqJob must mirror vppgpu_
 
 namespace {
 
-__device__ __forceinline__ void roundtrip_one(const vppgpu::TqJob& j, long long blk, int cols_first,
-                                              const int* weight)
+// Per-plane constants of the fused round trip, computed once per thread:
+// the quantiser factors of the three position classes, its rounding and
+// shift, the dequantiser scales V[qp%6][class] and the post-scale.  The
+// SetScale() weights stay in the kernel's parameter space: the dequantised
+// coefficient is x * V[class] * weight[pos] (the same bits as x * (V * w)).
+struct RtConsts {
+    int mf0, mf1, mf2, f, sh;
+    int v0, v1, v2, df, right, left;
+    bool small_q;  // qp < 24: rounded right shift, else left shift
+};
+
+__device__ __forceinline__ RtConsts rt_consts(int qp, int intra)
 {
-    int bw = j.width >> 2;
-    int by = (int)(blk / bw), bx = (int)(blk - (long long)by * bw);
-    size_t off = (size_t)by * 4 * j.stride + (size_t)bx * 4;
+    RtConsts c;
+    const int qe = qp / 6, qm = qp % 6;
+    c.mf0 = c_fwd_mf[qm][0];
+    c.mf1 = c_fwd_mf[qm][1];
+    c.mf2 = c_fwd_mf[qm][2];
+    c.sh = 15 + qe;
+    c.f = intra ? (1 << (15 + qe)) / 3 : (1 << (15 + qe)) / 6;
+    c.v0 = c_inv_v[qm][0];
+    c.v1 = c_inv_v[qm][1];
+    c.v2 = c_inv_v[qm][2];
+    c.df = qe <= 3 ? (1 << (3 - qe)) : 0;
+    c.right = 4 - qe;
+    c.left = qe - 4;
+    c.small_q = qp < 24;
+    return c;
+}
+
+__device__ __forceinline__ int rt_quant(int x, int mf, const RtConsts& c)
+{
+    const int q = ((x < 0 ? -x : x) * mf + c.f) >> c.sh;
+    return s16(x < 0 ? -q : q);
+}
+
+// Forward transform + quantisation (mode 0) of fwd_block, then the
+// dequantisation + inverse of inv_block (mode 0, pass order kColsFirst),
+// with the constants in registers; the levels are stored in between.
+template <bool kColsFirst>
+__device__ __forceinline__ void roundtrip_block(const short* res, short* lev, short* rec, int stride,
+                                               const RtConsts& c, const int* weight)
+{
     int b[16];
-    load_rows(j.res + off, j.stride, b);
-    FwdParams fp;
-    int qe = j.qp / 6;
-    fp.qm = j.qp % 6;
-    fp.sh = 15 + qe;
-    fp.f = j.intra ? (1 << (15 + qe)) / 3 : (1 << (15 + qe)) / 6;
-    fwd_block(b, 0, fp);
-    store_rows(j.lev + off, j.stride, b);
-    InvParams ip;
+    load_rows(res, stride, b);
 #pragma unroll
-    for (int i = 0; i < 16; i++) ip.weight[i] = weight[i];
-    ip.qm = fp.qm;
-    ip.q = j.qp;
-    ip.f = qe <= 3 ? (1 << (3 - qe)) : 0;
-    ip.right = 4 - qe;
-    ip.left = qe - 4;
-    inv_block(b, 0, cols_first, ip);
-    store_rows(j.rec + off, j.stride, b);
+    for (int r = 0; r < 4; r++) {
+        int* q = b + 4 * r;
+        const int s0 = q[0] + q[3], s3 = q[0] - q[3], s1 = q[1] + q[2], s2 = q[1] - q[2];
+        q[0] = s16(s0 + s1);
+        q[2] = s16(s0 - s1);
+        q[1] = s16(s2 + (s3 << 1));
+        q[3] = s16(s3 - (s2 << 1));
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int s0 = b[k] + b[12 + k], s3 = b[k] - b[12 + k], s1 = b[4 + k] + b[8 + k], s2 = b[4 + k] - b[8 + k];
+        // classes: even row & even col 0, odd & odd 1, mixed 2
+        const int mf_even = (k & 1) ? c.mf2 : c.mf0, mf_odd = (k & 1) ? c.mf1 : c.mf2;
+        b[k] = rt_quant(s0 + s1, mf_even, c);
+        b[4 + k] = rt_quant(s2 + (s3 << 1), mf_odd, c);
+        b[8 + k] = rt_quant(s0 - s1, mf_even, c);
+        b[12 + k] = rt_quant(s3 - (s2 << 1), mf_odd, c);
+    }
+    store_rows(lev, stride, b);
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        const int cls = pos_class(i);
+        const int v = b[i] * (cls == 0 ? c.v0 : (cls == 1 ? c.v1 : c.v2)) * weight[i];
+        b[i] = c.small_q ? (v + c.df) >> c.right : v << c.left;
+    }
+    int y0, y1, y2, y3;
+    if constexpr (!kColsFirst) {
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            int* q = b + 4 * r;
+            inv_1d(q[0], q[1], q[2], q[3], y0, y1, y2, y3);
+            q[0] = s16(y0); q[1] = s16(y1); q[2] = s16(y2); q[3] = s16(y3);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            inv_1d(b[k], b[4 + k], b[8 + k], b[12 + k], y0, y1, y2, y3);
+            b[k] = s16((y0 + 32) >> 6); b[4 + k] = s16((y1 + 32) >> 6);
+            b[8 + k] = s16((y2 + 32) >> 6); b[12 + k] = s16((y3 + 32) >> 6);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            inv_1d(b[k], b[4 + k], b[8 + k], b[12 + k], y0, y1, y2, y3);
+            b[k] = s16(y0); b[4 + k] = s16(y1); b[8 + k] = s16(y2); b[12 + k] = s16(y3);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            int* q = b + 4 * r;
+            inv_1d(q[0], q[1], q[2], q[3], y0, y1, y2, y3);
+            q[0] = s16((y0 + 32) >> 6); q[1] = s16((y1 + 32) >> 6);
+            q[2] = s16((y2 + 32) >> 6); q[3] = s16((y3 + 32) >> 6);
+        }
+    }
+    store_rows(rec, stride, b);
+}
+
+// One plane: rows of 4x4 blocks strided over the CTAs that serve the plane,
+// the blocks of a row over the CTA's threads (8-byte row accesses, 256
+// contiguous bytes per warp and row).  No index division.
+template <bool kColsFirst>
+__device__ __forceinline__ void roundtrip_plane(const vppgpu::TqJob& j, const int* weight, int row0, int rstep)
+{
+    const RtConsts c = rt_consts(j.qp, j.intra);
+    const int bw = j.width >> 2, bh = j.height >> 2;
+    for (int by = row0; by < bh; by += rstep) {
+        const size_t row = (size_t)by * 4 * j.stride;
+        for (int bx = threadIdx.x; bx < bw; bx += blockDim.x) {
+            const size_t off = row + (size_t)bx * 4;
+            roundtrip_block<kColsFirst>(j.res + off, j.lev + off, j.rec + off, j.stride, c, weight);
+        }
+    }
 }
 
 struct Weights {
     int w[16];
 };
 
-// blockIdx.y selects the job; x covers its blocks with a grid-stride loop.
-__global__ void __launch_bounds__(256) k_tq_roundtrip(const vppgpu::TqJob* __restrict__ jobs, int cols_first,
-                                                      Weights wt)
+// blockIdx.y selects the plane; blockIdx.x strides over its rows of blocks.
+// Up to 256 CTAs per plane, so a CTA holds one or two rows of a 1080p or 4K
+// plane and the kernel's tail is one short CTA.
+template <bool kColsFirst>
+__global__ void __launch_bounds__(256, 6) k_tq_roundtrip(const vppgpu::TqJob* __restrict__ jobs, Weights wt)
 {
-    vppgpu::TqJob j = jobs[blockIdx.y];
-    long long nblk = (long long)(j.width >> 2) * (j.height >> 2);
-    for (long long blk = blockIdx.x * (long long)blockDim.x + threadIdx.x; blk < nblk;
-         blk += (long long)gridDim.x * blockDim.x)
-        roundtrip_one(j, blk, cols_first, wt.w);
+    const vppgpu::TqJob j = jobs[blockIdx.y];
+    roundtrip_plane<kColsFirst>(j, wt.w, blockIdx.x, gridDim.x);
 }
 
-__global__ void __launch_bounds__(256) k_tq_roundtrip_single(vppgpu::TqJob j, int cols_first, Weights wt)
+template <bool kColsFirst>
+__global__ void __launch_bounds__(256, 6) k_tq_roundtrip_single(vppgpu::TqJob j, Weights wt)
 {
-    long long nblk = (long long)(j.width >> 2) * (j.height >> 2);
-    for (long long blk = blockIdx.x * (long long)blockDim.x + threadIdx.x; blk < nblk;
-         blk += (long long)gridDim.x * blockDim.x)
-        roundtrip_one(j, blk, cols_first, wt.w);
+    roundtrip_plane<kColsFirst>(j, wt.w, blockIdx.x, gridDim.x);
 }
 
 // ---- DC Hadamard transforms (Intra16x16 luma DC 4x4, chroma DC 2x2) --------
@@ -523,15 +612,15 @@ int check_common(vppgpu_ctx* ctx, const void* p, long long nunits, int layout, i
 
 namespace vppgpu {
 
-int launch_tq_jobs(vppgpu_ctx* ctx, const TqJob* d_jobs, int njobs, long long max_blocks, int inv_order,
-                   const int* weight16)
+int launch_tq_jobs(vppgpu_ctx* ctx, const TqJob* d_jobs, int njobs, int inv_order, const int* weight16)
 {
     Weights wt;
     for (int i = 0; i < 16; i++) wt.w[i] = weight16 ? weight16[i] : 16;
-    long long want = (max_blocks + 255) / 256;
-    int gx = (int)(want < 4096 ? (want > 0 ? want : 1) : 4096);
-    dim3 grid(gx, njobs);
-    k_tq_roundtrip<<<grid, 256, 0, ctx->stream>>>(d_jobs, inv_order == VPPGPU_INV_COLS_FIRST, wt);
+    const dim3 grid(256, njobs);
+    if (inv_order == VPPGPU_INV_COLS_FIRST)
+        k_tq_roundtrip<true><<<grid, 256, 0, ctx->stream>>>(d_jobs, wt);
+    else
+        k_tq_roundtrip<false><<<grid, 256, 0, ctx->stream>>>(d_jobs, wt);
     VPP_CHECK_LAUNCH(ctx);
     return VPPGPU_OK;
 }
@@ -615,9 +704,11 @@ int vppgpu_tq_roundtrip_plane_device(vppgpu_ctx* ctx, const short* res, short* l
     vppgpu::TqJob j{res, lev, rec, width, height, stride, qp, intra != 0};
     Weights wt;
     for (int i = 0; i < 16; i++) wt.w[i] = weight16 ? weight16[i] : 16;
-    long long nblk = (long long)(width >> 2) * (height >> 2);
-    k_tq_roundtrip_single<<<grid_for(ctx, nblk), 256, 0, ctx->stream>>>(j, inv_order == VPPGPU_INV_COLS_FIRST,
-                                                                         wt);
+    const int rows = height >> 2, g = rows < 2 * 8 * ctx->sm_count ? rows : 2 * 8 * ctx->sm_count;
+    if (inv_order == VPPGPU_INV_COLS_FIRST)
+        k_tq_roundtrip_single<true><<<g, 256, 0, ctx->stream>>>(j, wt);
+    else
+        k_tq_roundtrip_single<false><<<g, 256, 0, ctx->stream>>>(j, wt);
     VPP_CHECK_LAUNCH(ctx);
     return VPPGPU_OK;
 }
@@ -658,9 +749,7 @@ int vppgpu_tq_roundtrip_planes_device(vppgpu_ctx* ctx, const vppgpu_tq_job* d_jo
         return VPPGPU_ERR_INVALID_ARG;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
-    // x extent sized for the largest plane the descriptors may hold (8K luma)
-    return vppgpu::launch_tq_jobs(ctx, reinterpret_cast<const vppgpu::TqJob*>(d_jobs), njobs,
-                                  (long long)(ctx->sm_count) * 8 * 256, inv_order, weight16);
+    return vppgpu::launch_tq_jobs(ctx, reinterpret_cast<const vppgpu::TqJob*>(d_jobs), njobs, inv_order, weight16);
 }
 
 static int dc_device(vppgpu_ctx* ctx, short* d, long long nunits, int size, bool forward, int mode, int qp,
