@@ -490,6 +490,30 @@ def run_hbm_paths(torch, _lib, L, ctx, stream, dev, pk):
                      "algorithmic_bytes_per_launch": nrgb * W * H * 6},
         "workload": "FastFixedPointRGB24toYUV420Converter, 1920x1080 uniform BGR frames"}
 
+    # YUV420 -> RGB24 (RealYUV420toRGB24ConverterImpl2): 32 1080p frames per launch, 6 B per pixel (Y int16
+    # + quarter-size U, V int16 in, packed B,G,R out)
+    nyr = 32
+    ygen = lambda seed, shape: torch.from_numpy(((synth.splitmix64(seed, int(np.prod(shape))) % np.uint64(256))
+                                                  .astype(np.int16)).reshape(shape)).to(dev)
+    yy, yu, yv = ygen(1050, (nyr, H, W)), ygen(1051, (nyr, H // 2, W // 2)), ygen(1052, (nyr, H // 2, W // 2))
+    rgb_out = torch.empty(nyr * H * W * 3, dtype=torch.uint8, device=dev)
+
+    def yuv2rgb():
+        _lib.check(L.vppgpu_yuv420_to_rgb24_frames_device(ctx.handle, _lib.YUV_REAL_IMPL2, C.c_void_p(yy.data_ptr()),
+                                                          C.c_void_p(yu.data_ptr()), C.c_void_p(yv.data_ptr()), nyr,
+                                                          W, H, 0, 0, 0, C.c_void_p(rgb_out.data_ptr())),
+                   "vppgpu_yuv420_to_rgb24_frames_device")
+
+    ms = timed(yuv2rgb)
+    gbs = nyr * W * H * 6 / (ms * 1e-3) / 1e9
+    out["yuv420_to_rgb24"] = {
+        "value": nyr / (ms * 1e-3), "unit": "frames/s", "ms_per_launch": ms, "frames_per_launch": nyr,
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": gbs / pk["hbm_gbs"] if pk.get("hbm_gbs") else None,
+                     "algorithmic_bytes_per_launch": nyr * W * H * 6},
+        "workload": "RealYUV420toRGB24ConverterImpl2, 1920x1080 frames of uniform 0..255 samples (398 MB)"}
+    del yy, yu, yv, rgb_out
+
     # DC Hadamard 4x4 (Intra16x16 luma DC blocks of 1024 1080p frames, one per macroblock): forward + quant,
     # then dequant + inverse, in place; 2 x (32 B read + 32 B written) per block
     ndc = 1024 * 8160

@@ -32,7 +32,9 @@ __all__ = [
     "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
     "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1", "FastForwardDC4x4ITImpl1",
     "FastForwardDC2x2ITImpl1", "FastInverseDC4x4ITImpl1", "FastInverseDC2x2ITImpl1",
-    "FastGpuRGB24toYUV420Converter", "VppGpuError", "load",
+    "FastGpuRGB24toYUV420Converter", "RealYUV420toRGB24Converter", "RealYUV420toRGB24ConverterImpl2",
+    "RealYUV420toRGB24ConverterImpl2Ver16", "RealYUV420toRGB24CCIR601Converter",
+    "RealYUV420toRGB24CCIR601ConverterVer16", "MotionCompensatorH264ImplStd", "VppGpuError", "load",
 ]
 
 
@@ -673,3 +675,80 @@ class FastGpuRGB24toYUV420Converter:
         check(load().vppgpu_rgb24_to_yuv420(self._ctx.handle, self._kind, _ptr(rgb), self._width, self._height,
                                             self._chrOff, int(self._flip), _ptr(pY), _ptr(pU), _ptr(pV)),
               "vppgpu_rgb24_to_yuv420")
+
+
+# ---------------------------------------------------------------------------
+# YUV420 -> RGB24 (display side)
+# ---------------------------------------------------------------------------
+class _YUV420toRGB24Base:
+    """YUV420toRGBConverter (include/ImageUtils/YUV420toRGBConverter.h) on the
+    GPU: Convert(pY, pU, pV, pRgb) fills pRgb (uint8, width*height*3 packed
+    B,G,R) from int16 planes.  KIND selects the reference class's arithmetic."""
+    KIND = _lib.YUV_REAL_IMPL2
+
+    def __init__(self, width=0, height=0, chrOff=0, ctx: Context | None = None):
+        self._width, self._height, self._chrOff = int(width), int(height), int(chrOff)
+        self._rotate, self._flip = 0, False
+        self._ctx = ctx or get_context()
+
+    def GetWidth(self):
+        return self._width
+
+    def GetHeight(self):
+        return self._height
+
+    def GetRotate(self):
+        return self._rotate
+
+    def GetChrominanceOffset(self):
+        return self._chrOff
+
+    def GetFlip(self):
+        return self._flip
+
+    def SetDimensions(self, width, height):
+        self._width, self._height = int(width), int(height)
+
+    def SetRotate(self, rotate):
+        self._rotate = int(rotate)
+
+    def SetChrominanceOffset(self, val):
+        self._chrOff = int(val)
+
+    def SetFlip(self, flip):
+        self._flip = bool(flip)
+
+    def Convert(self, pY, pU, pV, pRgb):
+        for p in (pY, pU, pV):
+            if not isinstance(p, np.ndarray) or p.dtype != np.int16 or not p.flags.c_contiguous:
+                raise TypeError("input planes must be contiguous int16 arrays")
+        if pRgb.dtype != np.uint8 or not pRgb.flags.c_contiguous or pRgb.size != self._width * self._height * 3:
+            raise TypeError("pRgb must be a contiguous uint8 array of width*height*3 bytes")
+        check(load().vppgpu_yuv420_to_rgb24(self._ctx.handle, self.KIND, _ptr(pY), _ptr(pU), _ptr(pV), self._width,
+                                            self._height, self._chrOff, self._rotate, int(self._flip), _ptr(pRgb)),
+              "vppgpu_yuv420_to_rgb24")
+
+
+class RealYUV420toRGB24Converter(_YUV420toRGB24Base):
+    """src/ImageUtils/RealYUV420toRGB24Converter.cpp (chrOff on the unrotated paths)."""
+    KIND = _lib.YUV_REAL
+
+
+class RealYUV420toRGB24ConverterImpl2(_YUV420toRGB24Base):
+    """src/ImageUtils/RealYUV420toRGB24ConverterImpl2.cpp."""
+    KIND = _lib.YUV_REAL_IMPL2
+
+
+class RealYUV420toRGB24ConverterImpl2Ver16(_YUV420toRGB24Base):
+    """src/ImageUtils/RealYUV420toRGB24ConverterImpl2Ver16.cpp (the Impl2 arithmetic)."""
+    KIND = _lib.YUV_REAL_IMPL2
+
+
+class RealYUV420toRGB24CCIR601Converter(_YUV420toRGB24Base):
+    """src/ImageUtils/RealYUV420toRGB24CCIR601Converter.cpp (no flip)."""
+    KIND = _lib.YUV_CCIR601
+
+
+class RealYUV420toRGB24CCIR601ConverterVer16(_YUV420toRGB24Base):
+    """src/ImageUtils/RealYUV420toRGB24CCIR601ConverterVer16.cpp (the CCIR601 arithmetic)."""
+    KIND = _lib.YUV_CCIR601

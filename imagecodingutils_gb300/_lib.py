@@ -30,6 +30,7 @@ ME_FULL, ME_MULTIRES, ME_MULTIRES_CROSS, ME_MULTIRES_CROSS_V2 = 0, 1, 2, 3
 LAYOUT_BLOCKS, LAYOUT_MB16 = 0, 1
 INV_ROWS_FIRST, INV_COLS_FIRST = 0, 1
 RGB_FIXED_POINT, RGB_REAL, RGB_REAL_IMPL2 = 0, 1, 2
+YUV_REAL, YUV_REAL_IMPL2, YUV_CCIR601 = 0, 1, 2
 
 # name -> (restype, argtypes); the symbol list is also the export check of the tests
 SIGNATURES = {
@@ -96,6 +97,9 @@ SIGNATURES = {
     "vppgpu_rgb24_to_yuv420": (_I, [_P, _I, _P, _I, _I, _I, _I, _P, _P, _P]),
     "vppgpu_rgb24_to_yuv420_device": (_I, [_P, _I, _P, _I, _I, _I, _I, _P, _P, _P]),
     "vppgpu_rgb24_to_yuv420_frames_device": (_I, [_P, _I, _P, _I, _I, _I, _I, _I, _P, _P, _P]),
+    "vppgpu_yuv420_to_rgb24": (_I, [_P, _I, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
+    "vppgpu_yuv420_to_rgb24_device": (_I, [_P, _I, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
+    "vppgpu_yuv420_to_rgb24_frames_device": (_I, [_P, _I, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
 }
 
 _lib = None

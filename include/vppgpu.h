@@ -379,6 +379,28 @@ int vppgpu_rgb24_to_yuv420_frames_device(vppgpu_ctx* ctx, int kind, const unsign
                                          int width, int height, int chr_off, int flip, short* d_y, short* d_u,
                                          short* d_v);
 
+/* ---- YUV420 -> RGB24 ----------------------------------------------------- */
+#define VPPGPU_YUV_REAL       0  /* RealYUV420toRGB24Converter                               */
+#define VPPGPU_YUV_REAL_IMPL2 1  /* RealYUV420toRGB24ConverterImpl2, ...Impl2Ver16           */
+#define VPPGPU_YUV_CCIR601    2  /* RealYUV420toRGB24CCIR601Converter, ...CCIR601ConverterVer16 */
+
+/* YUV420toRGBConverter::Convert(pY, pU, pV, pRgb) (include/ImageUtils/YUV420toRGBConverter.h:66;
+ * src/ImageUtils/RealYUV420toRGB24Converter.cpp:66-352, RealYUV420toRGB24ConverterImpl2.cpp:94-368,
+ * RealYUV420toRGB24CCIR601Converter.cpp:59-241), with SetChrominanceOffset(chr_off), SetRotate(rotate)
+ * and SetFlip(flip): planar shorts in (Y width*height, U and V (width/2)*(height/2)), packed B,G,R
+ * bytes out, width*height*3.  flip writes the rows bottom-up and takes precedence over rotate (the
+ * CCIR601 converters ignore it); rotate writes the transpose (pixel (x, y) at byte 3*(x*height + y)).
+ * chr_off is used by RealYUV420toRGB24Converter's unrotated paths only, as in the reference. */
+int vppgpu_yuv420_to_rgb24(vppgpu_ctx* ctx, int kind, const short* y, const short* u, const short* v, int width,
+                           int height, int chr_off, int rotate, int flip, unsigned char* rgb);
+int vppgpu_yuv420_to_rgb24_device(vppgpu_ctx* ctx, int kind, const short* d_y, const short* d_u, const short* d_v,
+                                  int width, int height, int chr_off, int rotate, int flip, unsigned char* d_rgb);
+
+/* nframes frames stored back to back (Y, U, V and RGB each contiguous per frame) in one launch. */
+int vppgpu_yuv420_to_rgb24_frames_device(vppgpu_ctx* ctx, int kind, const short* d_y, const short* d_u,
+                                         const short* d_v, int nframes, int width, int height, int chr_off,
+                                         int rotate, int flip, unsigned char* d_rgb);
+
 #ifdef __cplusplus
 }
 #endif

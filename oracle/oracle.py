@@ -64,6 +64,7 @@ class Oracle:
         L.vo_fwd_dc.argtypes = [_P, _I, _I, _I, _I]
         L.vo_inv_dc.argtypes = [_P, _I, _I, _I, _I, _P]
         L.vo_dc_quantise_value.argtypes = [C.c_short, _I]
+        L.vo_yuv420_to_rgb24.argtypes = [_I, _P, _P, _P, _I, _I, _I, _I, _I, _P]
         L.vo_rgb24_to_yuv420.argtypes = [_I, _P, _I, _I, _I, _I, _P, _P, _P]
         L.vo_bench_me_full.argtypes = [_P, _P, _I, _I, _I, _I, _I, _P]
 
@@ -214,6 +215,15 @@ class Oracle:
     def dc_quantise_value(self, val, qp):
         return self.lib.vo_dc_quantise_value(int(val), qp)
 
+    def yuv_to_rgb(self, kind, y, u, v, chr_off=-128, rotate=0, flip=0):
+        """kind 0 RealYUV420toRGB24Converter, 1 ...Impl2, 2 ...CCIR601; packed
+        B,G,R bytes (height, width, 3), or (width, height, 3) when rotated."""
+        h, w = y.shape
+        y, u, v = (np.ascontiguousarray(a, dtype=np.int16) for a in (y, u, v))
+        out = np.zeros((w, h, 3) if rotate and not (kind != 2 and flip) else (h, w, 3), np.uint8)
+        self.lib.vo_yuv420_to_rgb24(kind, _ptr(y), _ptr(u), _ptr(v), w, h, chr_off, rotate, flip, _ptr(out))
+        return out
+
     def rgb_to_yuv(self, kind, bgr, chr_off=0, flip=0):
         h, w, _ = bgr.shape
         bgr = np.ascontiguousarray(bgr, dtype=np.uint8)
@@ -253,6 +263,7 @@ class Reference:
         L.ref_fwd_dc.argtypes = [_P, _I, _I, _I, _I]
         L.ref_inv_dc.argtypes = [_P, _I, _I, _I, _I, _P]
         L.ref_dc_quantise_value.argtypes = [C.c_short, _I]
+        L.ref_yuv_to_rgb.argtypes = [_I, _P, _P, _P, _I, _I, _I, _I, _I, _P]
         L.ref_rgb_to_yuv.argtypes = [_I, _P, _I, _I, _I, _I, _P, _P, _P]
         L.ref_mc_compensate.argtypes = [_I, _I, _I, _P, _P]
 
@@ -314,6 +325,16 @@ class Reference:
 
     def dc_quantise_value(self, val, qp):
         return self.lib.ref_dc_quantise_value(int(val), qp)
+
+    def yuv_to_rgb(self, kind, y, u, v, chr_off=-128, rotate=0, flip=0):
+        """kind 0..2 as Oracle.yuv_to_rgb; 3 Impl2Ver16, 4 CCIR601Ver16."""
+        h, w = y.shape
+        y, u, v = (np.ascontiguousarray(a, dtype=np.int16) for a in (y, u, v))
+        out = np.zeros((w, h, 3) if rotate and not (kind not in (2, 4) and flip) else (h, w, 3), np.uint8)
+        rc = self.lib.ref_yuv_to_rgb(kind, _ptr(y), _ptr(u), _ptr(v), w, h, chr_off, rotate, flip, _ptr(out))
+        if rc:
+            raise ValueError(f"ref_yuv_to_rgb rc={rc}")
+        return out
 
     def rgb_to_yuv(self, kind, bgr, chr_off=0, flip=0):
         h, w, _ = bgr.shape

@@ -25,6 +25,11 @@
 #include "FastInverse4x4ITImpl1.h"
 #include "FastForward4x4On16x16ITImpl1.h"
 #include "FastInverse4x4On16x16ITImpl1.h"
+#include "RealYUV420toRGB24Converter.h"
+#include "RealYUV420toRGB24ConverterImpl2.h"
+#include "RealYUV420toRGB24ConverterImpl2Ver16.h"
+#include "RealYUV420toRGB24CCIR601Converter.h"
+#include "RealYUV420toRGB24CCIR601ConverterVer16.h"
 #include "FastForwardDC4x4ITImpl1.h"
 #include "FastInverseDC4x4ITImpl1.h"
 #include "FastForwardDC2x2ITImpl1.h"
@@ -206,6 +211,26 @@ int ref_inv_dc(short* data, int nunits, int size, int mode, int qp, const int* w
     t->SetParameter(IInverseTransform::QUANT_ID, qp);
     for (int u = 0; u < nunits; u++) t->InverseTransform(data + (size_t)u * size * size);
     delete t;
+    return 0;
+}
+
+/* kind: 0 RealYUV420toRGB24Converter, 1 ...Impl2, 2 ...CCIR601, 3 ...Impl2Ver16, 4 ...CCIR601Ver16. */
+int ref_yuv_to_rgb(int kind, short* y, short* u, short* v, int w, int h, int chr_off, int rotate, int flip,
+                   unsigned char* rgb)
+{
+    YUV420toRGBConverter* c = NULL;
+    if (kind == 0) c = new RealYUV420toRGB24Converter(w, h);
+    else if (kind == 1) c = new RealYUV420toRGB24ConverterImpl2(w, h);
+    else if (kind == 2) c = new RealYUV420toRGB24CCIR601Converter(w, h);
+    else if (kind == 3) c = new RealYUV420toRGB24ConverterImpl2Ver16(w, h);
+    else if (kind == 4) c = new RealYUV420toRGB24CCIR601ConverterVer16(w, h);
+    else return -1;
+    /* the two-argument constructors leave the chrominance offset unset */
+    c->SetChrominanceOffset(chr_off);
+    c->SetRotate(rotate);
+    c->SetFlip(flip != 0);
+    c->Convert(y, u, v, rgb);
+    delete c;
     return 0;
 }
 

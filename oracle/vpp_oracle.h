@@ -132,6 +132,12 @@ void vo_fwd_dc(short* data, int nunits, int size, int mode, int qp);
 void vo_inv_dc(short* data, int nunits, int size, int mode, int qp, const int* weight);
 int vo_dc_quantise_value(short val, int qp);
 
+/* YUV420 -> RGB24 (oracle_yuv2rgb.c): kind 0 RealYUV420toRGB24Converter,
+ * 1 RealYUV420toRGB24ConverterImpl2 (and Ver16), 2 RealYUV420toRGB24CCIR601Converter
+ * (and Ver16); rgb holds width*height*3 bytes. */
+void vo_yuv420_to_rgb24(int kind, const short* py, const short* pu, const short* pv, int w, int h, int chr_off,
+                        int rotate, int flip, unsigned char* rgb);
+
 /* ------------------------------------------------------------------------ */
 /* RGB24 -> YUV420                                                           */
 /* ------------------------------------------------------------------------ */

@@ -219,6 +219,29 @@ def dc_fixtures(ref: oracle.Reference) -> dict:
     return out
 
 
+def yuv2rgb_fixtures(ref: oracle.Reference) -> dict:
+    """YUV420 -> RGB24: the five Real converters (kinds 0-4 of ref_yuv_to_rgb)
+    on a 64x48 frame of 0..255 samples, every rotate / flip combination
+    (RealYUV420toRGB24Converter with chrOff -128: its byte casts stay in
+    range), and Impl2 / CCIR601 on samples outside 0..255."""
+    out = {}
+    w, h = 64, 48
+    r = lambda seed, shape, lo, hi: ((synth.splitmix64(seed, int(np.prod(shape))) % np.uint64(hi - lo + 1))
+                                     .astype(np.int64) + lo).astype(np.int16).reshape(shape)
+    planes = {"n": (r(71, (h, w), 0, 255), r(72, (h // 2, w // 2), 0, 255), r(73, (h // 2, w // 2), 0, 255)),
+              "wide": (r(74, (h, w), -300, 600), r(75, (h // 2, w // 2), -200, 500),
+                       r(76, (h // 2, w // 2), -200, 500))}
+    for name, (y, u, v) in planes.items():
+        out[f"{name}_y"], out[f"{name}_u"], out[f"{name}_v"] = y, u, v
+        for kind in (0, 1, 2, 3, 4):
+            if kind == 0 and name == "wide":
+                continue
+            for rot in (0, 1):
+                for flip in (0, 1):
+                    out[f"{name}_k{kind}_r{rot}_f{flip}"] = ref.yuv_to_rgb(kind, y, u, v, -128, rot, flip)
+    return out
+
+
 def colour_fixtures(ref: oracle.Reference) -> dict:
     bgr = synth.rgb_frame(21, 64, 48)
     out = {"bgr": bgr}
@@ -237,7 +260,8 @@ def main() -> None:
     ref = oracle.Reference()
     makers = {"me_full": me_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "mc": mc_fixtures,
-              "transform": transform_fixtures, "dc": dc_fixtures, "colour": colour_fixtures}
+              "transform": transform_fixtures, "dc": dc_fixtures, "yuv2rgb": yuv2rgb_fixtures,
+              "colour": colour_fixtures}
     names = sys.argv[1:] or list(makers)
     for name in names:
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **makers[name](ref))

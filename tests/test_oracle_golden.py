@@ -87,6 +87,21 @@ def test_dc_transforms_against_compiled_reference(orc):
                 np.testing.assert_array_equal(orc.inv_dc(xi, size, mode, qp), ref.inv_dc(xi, size, mode, qp))
 
 
+def test_yuv_to_rgb_matches_reference(orc, golden):
+    """Oracle kinds 0-2 against the five Real converters (Ver16 classes share
+    the Impl2 / CCIR601 arithmetic)."""
+    g = golden("yuv2rgb.npz")
+    for name in ("n", "wide"):
+        y, u, v = g[f"{name}_y"], g[f"{name}_u"], g[f"{name}_v"]
+        for kind, okind in ((0, 0), (1, 1), (2, 2), (3, 1), (4, 2)):
+            if kind == 0 and name == "wide":
+                continue
+            for rot in (0, 1):
+                for flip in (0, 1):
+                    np.testing.assert_array_equal(orc.yuv_to_rgb(okind, y, u, v, -128, rot, flip),
+                                                  g[f"{name}_k{kind}_r{rot}_f{flip}"], err_msg=f"{name} k{kind}")
+
+
 def test_colour_matches_reference(orc, golden):
     g = golden("colour.npz")
     for kind in (0, 1, 2):
