@@ -8,8 +8,9 @@
 // and keeps everything else.
 //
 // Build inside the vpp tree with -DVPPGPU_WITH_VPP: the classes then derive
-// from vpp's own IMotionEstimator, IForwardTransform, IInverseTransform and
-// RGBtoYUV420Converter and return vpp's VectorStructList.  Without that
+// from vpp's own IMotionEstimator, IForwardTransform, IInverseTransform,
+// RGBtoYUV420Converter and YUV420toRGBConverter and return vpp's
+// VectorStructList.  Without that
 // macro, minimal local declarations with the same method signatures are
 // used (for this repository's tests and for codecs that only need the
 // methods).
@@ -27,6 +28,7 @@
 #include "IMotionVectorPredictor.h"
 #include "RGBtoYUV420Converter.h"
 #include "VectorStructList.h"
+#include "YUV420toRGBConverter.h"
 #else
 // ---- local declarations mirroring the vpp interfaces (same signatures) ----
 class IMotionEstimator {
@@ -127,6 +129,31 @@ public:
 
 protected:
     int _width, _height, _chrOff;
+    bool _flip;
+};
+
+class YUV420toRGBConverter {
+public:
+    YUV420toRGBConverter(void) { _width = 0; _height = 0; _rotate = 0; _chrOff = 0; _flip = false; }
+    YUV420toRGBConverter(int width, int height) { _width = width; _height = height; _rotate = 0; _chrOff = 0; _flip = false; }
+    YUV420toRGBConverter(int width, int height, int chrOff)
+    {
+        _width = width; _height = height; _rotate = 0; _chrOff = chrOff; _flip = false;
+    }
+    virtual ~YUV420toRGBConverter(void) {}
+    virtual void Convert(void* pY, void* pU, void* pV, void* pRgb) = 0;
+    int GetWidth(void) { return _width; }
+    int GetHeight(void) { return _height; }
+    int GetRotate(void) { return _rotate; }
+    int GetChrominanceOffset(void) { return _chrOff; }
+    bool GetFlip(void) { return _flip; }
+    void SetDimensions(int width, int height) { _width = width; _height = height; }
+    void SetRotate(int rotate) { _rotate = rotate; }
+    void SetChrominanceOffset(int val) { _chrOff = val; }
+    void SetFlip(bool flip) { _flip = flip; }
+
+protected:
+    int _width, _height, _rotate, _chrOff;
     bool _flip;
 };
 #endif  // VPPGPU_WITH_VPP
@@ -476,6 +503,28 @@ public:
     {
         vppgpu_rgb24_to_yuv420(vppgpu_vpp::context(), _kind, (const unsigned char*)pRgb, _width, _height, _chrOff,
                                _flip ? 1 : 0, (short*)pY, (short*)pU, (short*)pV);
+    }
+
+protected:
+    int _kind;
+};
+
+// ---------------------------------------------------------------------------
+// YUV420toRGBConverter on the GPU with the arithmetic of one of vpp's Real
+// converters: VPPGPU_YUV_REAL (RealYUV420toRGB24Converter), VPPGPU_YUV_REAL_IMPL2
+// (RealYUV420toRGB24ConverterImpl2 / ...Impl2Ver16) or VPPGPU_YUV_CCIR601
+// (RealYUV420toRGB24CCIR601Converter / ...Ver16).  The constructor sets the
+// chrominance offset as the reference's two-argument constructors do not;
+// call SetChrominanceOffset() as with the reference.
+// ---------------------------------------------------------------------------
+class GpuYUV420toRGB24Converter : public YUV420toRGBConverter {
+public:
+    GpuYUV420toRGB24Converter(int width, int height, int kind = VPPGPU_YUV_REAL_IMPL2)
+        : YUV420toRGBConverter(width, height, 0), _kind(kind) {}
+    virtual void Convert(void* pY, void* pU, void* pV, void* pRgb)
+    {
+        vppgpu_yuv420_to_rgb24(vppgpu_vpp::context(), _kind, (const short*)pY, (const short*)pU, (const short*)pV,
+                               _width, _height, _chrOff, _rotate, _flip ? 1 : 0, (unsigned char*)pRgb);
     }
 
 protected:
