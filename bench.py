@@ -323,8 +323,9 @@ MULTIRES = {  # kind -> (class name, oracle method)
     "multires": ("MotionEstimatorH264ImplMultires", "me_multires"),
     "multires_cross": ("MotionEstimatorH264ImplMultiresCross", "me_multires_cross"),
     "multires_cross_v2": ("MotionEstimatorH264ImplMultiresCrossVer2", "me_multires_cross_v2"),
+    "cross": ("MotionEstimatorH264ImplCross", "me_cross"),
 }
-MULTIRES_CODE = {"multires": 1, "multires_cross": 2, "multires_cross_v2": 3}  # VPPGPU_ME_*
+MULTIRES_CODE = {"multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4}  # VPPGPU_ME_*
 
 
 TUNE_PAIRS = 8
@@ -344,9 +345,10 @@ def autotune(L, _lib, h, dev_frames, npairs):
 
 
 def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with_cpu, kind="multires_cross"):
-    """A multi-resolution estimator (mode 0 -> 2 at 1080p) on the same 1080p
-    sequence: device-resident MB/s over the frame rotation, and the oracle
-    port on all host threads as its CPU baseline."""
+    """Another estimator on the same 1080p sequence after SetMode(0) (the
+    multi-resolution ones pick mode 2 at 1080p, Cross searches to quarter
+    pel): device-resident MB/s over the frame rotation, and the oracle port
+    on all host threads as its CPU baseline."""
     cls, ofn = MULTIRES[kind]
     code = MULTIRES_CODE[kind]
     h = C.c_void_p()
@@ -761,6 +763,8 @@ def main():
                                   kind="multires_cross_v2")
         mr = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
                                 kind="multires")
+        cr = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
+                                kind="cross")
         pk, pk_kind = peaks()
         hbm_rows = run_hbm_paths(torch, _lib, L, ctx, stream, f"cuda:{local}", pk)
         line = {
@@ -785,7 +789,7 @@ def main():
             "hbm_peak_gbs": pk.get("hbm_gbs"), "peaks_source": pk_kind,
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
             "serving": serving,
-            "multires": mr, "multires_cross": mrc, "multires_cross_v2": mrc2, **hbm_rows,
+            "multires": mr, "multires_cross": mrc, "multires_cross_v2": mrc2, "cross": cr, **hbm_rows,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -28,7 +28,8 @@ from ._lib import VppGpuError, check, load
 
 __all__ = [
     "Context", "get_context", "MotionEstimatorH264ImplFull", "MotionEstimatorH264ImplMultires",
-    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorBatch",
+    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross",
+    "MotionEstimatorBatch",
     "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
     "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1", "FastForwardDC4x4ITImpl1",
     "FastForwardDC2x2ITImpl1", "FastInverseDC4x4ITImpl1", "FastInverseDC2x2ITImpl1",
@@ -91,6 +92,7 @@ def get_context() -> Context:
 # ---------------------------------------------------------------------------
 class _MotionEstimatorBase:
     KIND = _lib.ME_FULL
+    DEFAULT_MODE = 1
 
     def __init__(self, pSrc, pRef, imgWidth: int, imgHeight: int, motionRange: int = 64, pMVPred=None,
                  pDistortionIncluded=None, mb_slice=None, ctx: Context | None = None):
@@ -106,7 +108,7 @@ class _MotionEstimatorBase:
         self._slice = None if mb_slice is None else np.ascontiguousarray(mb_slice, np.int32)
         self._ctx = ctx or get_context()
         self._h_me = None
-        self._mode = 1
+        self._mode = self.DEFAULT_MODE
         self.last_mb_distortion = None
 
     # IMotionEstimator
@@ -199,6 +201,17 @@ class MotionEstimatorH264ImplFull(_MotionEstimatorBase):
     """GPU MotionEstimatorH264ImplFull (src/CodecUtils/MotionEstimatorH264ImplFull.cpp)."""
 
     KIND = _lib.ME_FULL
+
+
+class MotionEstimatorH264ImplCross(_MotionEstimatorBase):
+    """GPU MotionEstimatorH264ImplCross (src/CodecUtils/MotionEstimatorH264ImplCross.cpp):
+    cross search of halving steps with the 64-point path distortion and its
+    extrapolating early exit, the full-search sub-pel window, ties towards the
+    rounded prediction, the pred-vector check and GetBestVector (lambda 0.9,
+    norm 64).  SetMode(0) quarter pel (the default), 1 half, 2 full pel."""
+
+    KIND = _lib.ME_CROSS
+    DEFAULT_MODE = 0
 
 
 class MotionEstimatorH264ImplMultiresCross(_MotionEstimatorBase):

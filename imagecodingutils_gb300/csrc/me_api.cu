@@ -177,6 +177,7 @@ vppgpu::FullArgs full_args(vppgpu_me* me, double lambda)
     a.lattice = me->d_lattice;
     a.search_cache = me->d_search_cache;
     a.tie_runs = me->d_tie_runs;
+    a.mode = me->mode;
     a.spin_limit = 20000000LL;  // ~2 s of polling before a barrier gives up
     return a;
 }
@@ -191,6 +192,11 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
                                   d_mv, d_dist, d_avg, me->ctrl, me->mrc_warps);
     int rc = vppgpu::set_job(ctx, me->d_job, vppgpu::JobDesc{d_src16, d_ref16, d_incl, d_slice, d_mv, d_dist, d_avg});
     if (rc) return rc;
+    if (me->kind == VPPGPU_ME_CROSS) {
+        // GetBestVector's lambda 0.9 (MotionEstimatorH264ImplCross.cpp:621)
+        VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
+        return vppgpu::cross_launch(ctx, full_args(me, 0.9));
+    }
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS_V2 || me->kind == VPPGPU_ME_MULTIRES) {
         // GetBestVector's lambda: 0.9 (MultiresCrossVer2.cpp:1050), 1.1 (Multires.cpp:958)
         const bool v2 = me->kind == VPPGPU_ME_MULTIRES_CROSS_V2;
@@ -258,7 +264,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
     if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
     if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
-    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_MULTIRES_CROSS_V2) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_CROSS) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me* me = (vppgpu_me*)calloc(1, sizeof(vppgpu_me));
@@ -271,7 +277,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     me->rows = height / 16;
     me->nmb = me->cols * me->rows;
     me->motion_range = motion_range;
-    me->mode = 1;
+    me->mode = kind == VPPGPU_ME_CROSS ? 0 : 1;  // Cross defaults to quarter pel (…ImplCross.cpp:184)
     me->rstride = width + 2 * vppgpu::PAD;
     me->sweep_limit = vppgpu::RELAX_SWEEPS + 2 + (me->nmb + 31) / 32;  // sweep counters, then the dirty bitmap
     // Sweep policy by how the estimator's predictions settle on moving content
@@ -299,6 +305,36 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
         if (cudaMallocHost((void**)&me->h_ctrl, sizeof(vppgpu::MeCtrl)) != cudaSuccess) {
             me_free(me);
             return VPPGPU_ERR_OUT_OF_MEMORY;
+        }
+        *out = me;
+        return VPPGPU_OK;
+    }
+    if (kind == VPPGPU_ME_CROSS) {
+        // MotionEstimatorH264ImplCross(…, pMVPred, …) + Create(): the padded reference with its half-pel
+        // planes, per-MB prediction state and the cache of searches at other rounded predictions
+        if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
+            (rc = dalloc(&me->d_src8, npix)) || (rc = dalloc(&me->d_refp, npad)) ||
+            (rc = dalloc(&me->d_hpel, 3 * npad)) ||
+            (rc = dalloc(&me->d_search_cache, (size_t)me->nmb * vppgpu::V2_SEARCH_CACHE)) ||
+            (rc = dalloc(&me->tie_list, me->nmb)) ||
+            (rc = dalloc(&me->d_job, 1)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
+            (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
+            (rc = dalloc(&me->cache, (size_t)me->nmb * vppgpu::KCACHE)) || (rc = dalloc(&me->dict, vppgpu::NDICT)) ||
+            (rc = dalloc(&me->d_wave_rec, vppgpu::wave_rec_count(me->cols, me->rows))) ||
+            (rc = dalloc(&me->d_wave_choice, me->nmb)) || (rc = dalloc(&me->changed, (size_t)me->sweep_limit)) ||
+            (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
+            (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||
+            (rc = dalloc(&me->d_slice, me->nmb)) || (rc = dalloc(&me->ctrl, 1))) {
+            me_free(me);
+            return rc;
+        }
+        if (cudaMallocHost((void**)&me->h_ctrl, sizeof(vppgpu::MeCtrl)) != cudaSuccess) {
+            me_free(me);
+            return VPPGPU_ERR_OUT_OF_MEMORY;
+        }
+        if ((rc = vppgpu::full_prepare(ctx, me->nmb, &me->resolve_grid))) {
+            me_free(me);
+            return rc;
         }
         *out = me;
         return VPPGPU_OK;
@@ -371,8 +407,9 @@ int vppgpu_me_destroy(vppgpu_me* me)
 int vppgpu_me_set_mode(vppgpu_me* me, int mode)
 {
     if (!me) return VPPGPU_ERR_INVALID_ARG;
-    // SetMode(0) picks by picture area (MultiresCross.cpp:501-513)
-    if (mode == 0 && me->kind != VPPGPU_ME_FULL)
+    // SetMode(0) picks by picture area for the multi-resolution estimators (MultiresCross.cpp:501-513);
+    // Cross keeps the mode as given (MotionEstimatorH264ImplCross.h:99)
+    if (mode == 0 && me->kind != VPPGPU_ME_FULL && me->kind != VPPGPU_ME_CROSS)
         mode = (me->W * me->H > 40000) ? 2 : 1;
     me->mode = mode;
     return VPPGPU_OK;
@@ -761,7 +798,7 @@ int vppgpu_me_batch_create(vppgpu_ctx* ctx, int kind, int streams, vppgpu_me_bat
 {
     if (!ctx || !out || streams < 1) return VPPGPU_ERR_INVALID_ARG;
     *out = nullptr;
-    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_MULTIRES_CROSS_V2) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_CROSS) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me_batch* b = (vppgpu_me_batch*)calloc(1, sizeof(vppgpu_me_batch));

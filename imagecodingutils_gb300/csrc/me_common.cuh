@@ -151,9 +151,10 @@ static __device__ __noinline__ int best_of3(int bx, int by, int bd, int px, int 
     return pos;
 }
 
-// Same decision without FP64 in the common cases.  Two costs with the same
-// sqrt argument differ only in D/norm, and D/256 is exact; with |lambda| <
-// 2^20 every sum stays below 2^40, where costs 1/256 apart never round
+// Same decision without FP64 in the common cases (norm a power of two: 256,
+// or 64 for the Cross estimator).  Two costs with the same sqrt argument
+// differ only in D/norm, and D/norm is exact; with |lambda| <
+// 2^20 every sum stays below 2^40, where costs 1/norm apart never round
 // together, so their double order is the order of the integers D.  This
 // covers the most frequent near-tie, the prediction slot against a searched
 // vector equal to it.  Other pairs compare in float: each float cost is
@@ -161,12 +162,12 @@ static __device__ __noinline__ int best_of3(int bx, int by, int bd, int px, int 
 // relative, so when a pair differs by more than 2^-18 relative both orderings
 // agree with the exact one; closer pairs take the double path.
 __device__ __forceinline__ int best_of3_fast(int bx, int by, int bd, int px, int py, int pd, int zd, double lambda,
-                                             int xref, int yref)
+                                             int xref, int yref, int norm = 256)
 {
     const int m0 = (bx - xref) * (bx - xref) + (by - yref) * (by - yref);
     const int m1 = (px - xref) * (px - xref) + (py - yref) * (py - yref);
     const int m2 = xref * xref + yref * yref;
-    const float lf = (float)lambda, inv = 1.0f / 256.0f;
+    const float lf = (float)lambda, inv = 1.0f / (float)norm;
     const float c0 = (float)bd * inv + lf * sqrtf((float)m0);
     const float c1 = (float)pd * inv + lf * sqrtf((float)m1);
     const float c2 = (float)zd * inv + lf * sqrtf((float)m2);
@@ -180,7 +181,7 @@ __device__ __forceinline__ int best_of3_fast(int bx, int by, int bd, int px, int
     };
     int pos = less(pd, m1, c1, bd, m0, c0) ? 1 : 0;
     const bool z = pos == 0 ? less(zd, m2, c2, bd, m0, c0) : less(zd, m2, c2, pd, m1, c1);
-    if (slow) return best_of3(bx, by, bd, px, py, pd, zd, lambda, 256.0, xref, yref);
+    if (slow) return best_of3(bx, by, bd, px, py, pd, zd, lambda, (double)norm, xref, yref);
     return z ? 2 : pos;
 }
 

@@ -31,6 +31,7 @@
 //                      progress counters.  A step is a median, a key match
 //                      against the MB's records (prefetched with cp.async)
 //                      and, on a miss only, a full evaluation by the warp.
+#include "me_cross_search.cuh"
 #include "me_full_common.cuh"
 #include "me_mrc_search.cuh"
 
@@ -116,6 +117,31 @@ template <int kEst>
 __device__ __noinline__ void pred_search_at(const FullArgs& a, int k, int px, int py, int lane, int* mvx, int* mvy,
                                             int* minD, mrc::Lattice* lt)
 {
+    if constexpr (kEst == cross::EST_CROSS) {
+        // Cross: the search depends on the prediction only through its rounding
+        // (MotionEstimatorH264ImplCross.cpp:393-405), the cache key
+        const int key = pack_mv(round_pred(px), round_pred(py));
+        int4* sc = a.search_cache + (size_t)k * V2_SEARCH_CACHE;
+        const int4 e = lane < V2_SEARCH_CACHE ? __ldcg(sc + lane) : make_int4(0, 0, 0, -1);
+        const unsigned hit = __ballot_sync(0xffffffffu, e.w >= 0 && e.x == key);
+        if (hit) {
+            const int f = __ffs(hit) - 1;
+            const int v = __shfl_sync(0xffffffffu, e.y, f);
+            *mvx = mv_x(v);
+            *mvy = mv_y(v);
+            *minD = __shfl_sync(0xffffffffu, e.z, f);
+            return;
+        }
+        const cross::CrossResult r =
+            cross::cross_search(a, (k % a.cols) * 16, (k / a.cols) * 16, round_pred(px), round_pred(py), lane);
+        *mvx = r.mvx;
+        *mvy = r.mvy;
+        *minD = r.min_d;
+        const unsigned slot = 1 + ((unsigned)key * 2654435761u >> 30) % (V2_SEARCH_CACHE - 1);
+        if (lane == 0) __stcg(sc + slot, make_int4(key, pack_mv(r.mvx, r.mvy), r.min_d, 1));
+        __syncwarp();
+        return;
+    }
     int tv, td;
     if (mrc::tie_tree_result(kEst, static_cast<const mrc::V2TieRun*>(a.tie_runs) + (size_t)k * mrc::V2_TIE_RUNS, px,
                              py, &tv, &td)) {
@@ -164,6 +190,10 @@ template <>
 struct LatticeSlots<0> {
     __device__ static mrc::Lattice* get(int) { return nullptr; }
 };
+template <>
+struct LatticeSlots<cross::EST_CROSS> {
+    __device__ static mrc::Lattice* get(int) { return nullptr; }
+};
 
 // Full evaluation of MB k for raw prediction (px, py), one warp: the record
 // {prediction, distortion at it, final vector, final distortion}.  kEst 0:
@@ -172,14 +202,18 @@ struct LatticeSlots<0> {
 // (at prediction (0, 0)) holds for any prediction unless the search met a
 // tie; for such an MB the search at the prediction's level vectors
 // (…MultiresCrossVer2.cpp:627-642) comes from pred_search_at.  kEst 2:
-// MotionEstimatorH264ImplMultires, the same with its own search.
+// MotionEstimatorH264ImplMultires, the same with its own search.  kEst 3:
+// MotionEstimatorH264ImplCross, the same with its search at the rounded
+// prediction, the 64-point path distortion and norm 64.
 template <int kEst>
 __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, int lane, mrc::Lattice* lt = nullptr)
 {
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
     const PredGeom g = pred_geom(n, m, a.W, a.H, px, py);
     const int4 sp = a.spec4[k];  // loads of spec and planes are independent: one round trip
-    const int pd = plane_pred_distortion(a, n, m, g, lane);
+    int pd;
+    if constexpr (kEst == cross::EST_CROSS) pd = cross::path_pred_distortion(a, n, m, g, lane);
+    else pd = plane_pred_distortion(a, n, m, g, lane);
     int mvx = mv_x(sp.x), mvy = mv_y(sp.x), minD = sp.y;
     const int zd = sp.z;
     if constexpr (kEst == 0) {
@@ -188,7 +222,8 @@ __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, 
     } else {
         if (sp.w & FLAG_TIE) pred_search_at<kEst>(a, k, px, py, lane, &mvx, &mvy, &minD, lt);
     }
-    const int pos = best_of3_fast(mvx, mvy, minD, g.pcx, g.pcy, pd, zd, a.lambda, g.pcx, g.pcy);
+    const int pos = best_of3_fast(mvx, mvy, minD, g.pcx, g.pcy, pd, zd, a.lambda, g.pcx, g.pcy,
+                                  kEst == cross::EST_CROSS ? cross::PATH_NORM : 256);
     int4 rec;
     rec.x = pack_mv(px, py);
     rec.y = pd;
@@ -1038,6 +1073,8 @@ int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
     VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tail_smem));
     VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tail_smem));
     VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tail_smem));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<cross::EST_CROSS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  tail_smem));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1049,6 +1086,10 @@ int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 2)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, cross::EST_CROSS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, cross::EST_CROSS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 2)));
     return VPPGPU_OK;
 }
@@ -1113,7 +1154,13 @@ int resolve_launch(vppgpu_ctx* ctx, const FullArgs& args)
 int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid, int est)
 {
     (void)resolve_grid;
-    return est == 0 ? resolve_launch<0>(ctx, args) : (est == 1 ? resolve_launch<1>(ctx, args) : resolve_launch<2>(ctx, args));
+    switch (est) {
+    case 0: return resolve_launch<0>(ctx, args);
+    case 1: return resolve_launch<1>(ctx, args);
+    case 2: return resolve_launch<2>(ctx, args);
+    case cross::EST_CROSS: return resolve_launch<cross::EST_CROSS>(ctx, args);
+    default: return VPPGPU_ERR_INVALID_ARG;
+    }
 }
 
 int full_residual_launch(vppgpu_ctx* ctx, const FullArgs& args, const int* d_mv, short* d_res)

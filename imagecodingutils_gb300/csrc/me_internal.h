@@ -98,6 +98,7 @@ struct FullArgs {
     void* lattice;
     int4* search_cache;  // V2_SEARCH_CACHE per MB: {rounded prediction, vector, distortion, tie levels or -1}
     void* tie_runs;      // 8 tie-tree runs (mrc::V2TieRun, 32 bytes) per MB
+    int mode;            // Cross: 0 quarter, 1 half, 2 full pel
 };
 constexpr int V2_SEARCH_CACHE = 4;
 
@@ -126,6 +127,11 @@ constexpr int RELAX_SWEEPS = 14;
 size_t mrc_args_bytes();
 size_t mrc_lattice_bytes();
 size_t mrc_tie_runs_bytes();  // per macroblock
+// MotionEstimatorH264ImplCross (me_cross.cu): the planes, the search at
+// prediction (0, 0) into args.spec4 / final_mv (args.search_cache seeded for
+// the tie macroblocks), then the resolve with the Cross evaluation
+// (estimator 3).
+int cross_launch(vppgpu_ctx* ctx, const FullArgs& args);
 // est: 1 MultiresCrossVer2, 2 Multires (the same pipeline, their own search).
 int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, const FullArgs& args,
                 const short* d_src16, const short* d_ref16);

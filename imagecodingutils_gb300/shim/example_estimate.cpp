@@ -4,8 +4,8 @@
 //
 // pair.bin holds the source then the reference luma plane (int16).  The
 // program estimates with GpuMotionEstimatorH264ImplFull (or, by the optional
-// last argument, ...Multires, ...MultiresCross or ...MultiresCrossVer2:
-// "multires", "mrc", "mrc2") exactly as a codec would with the vpp class
+// last argument, ...Multires, ...MultiresCross, ...MultiresCrossVer2 or
+// ...Cross: "multires", "mrc", "mrc2", "cross") exactly as a codec would with the vpp class
 // (constructor, Create, SetMode(0), Estimate, predictor side effect), then
 // runs the forward/inverse 4x4 transform classes
 // on the motion-compensated-free residual (source - reference) of the first
@@ -34,7 +34,7 @@ public:
 int main(int argc, char** argv)
 {
     if (argc != 6 && argc != 7) {
-        fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin [full|multires|mrc|mrc2]\n", argv[0]);
+        fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin [full|multires|mrc|mrc2|cross]\n", argv[0]);
         return 2;
     }
     const std::string kind = argc == 7 ? argv[6] : "full";
@@ -56,6 +56,8 @@ int main(int argc, char** argv)
         me = new GpuMotionEstimatorH264ImplMultiresCross(src.data(), ref.data(), w, h, range, incl);
     else if (kind == "mrc2")
         me = new GpuMotionEstimatorH264ImplMultiresCrossVer2(src.data(), ref.data(), w, h, range, &pred, incl);
+    else if (kind == "cross")
+        me = new GpuMotionEstimatorH264ImplCross(src.data(), ref.data(), w, h, range, &pred, incl);
     else
         me = new GpuMotionEstimatorH264ImplFull(src.data(), ref.data(), w, h, range, &pred, incl);
     if (!me->Create()) {

@@ -332,6 +332,24 @@ public:
     }
 };
 
+// MotionEstimatorH264ImplCross: quarter pel by default (SetMode 0; 1 half, 2 full pel).
+class GpuMotionEstimatorH264ImplCross : public GpuMotionEstimatorH264Base {
+public:
+    GpuMotionEstimatorH264ImplCross(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int motionRange,
+                                    IMotionVectorPredictor* pMVPred)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_CROSS, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred, NULL)
+    {
+        _mode = 0;
+    }
+    GpuMotionEstimatorH264ImplCross(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int motionRange,
+                                    IMotionVectorPredictor* pMVPred, void* pDistortionIncluded)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_CROSS, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred,
+                                     pDistortionIncluded)
+    {
+        _mode = 0;
+    }
+};
+
 class GpuMotionEstimatorH264ImplMultires : public GpuMotionEstimatorH264Base {
 public:
     GpuMotionEstimatorH264ImplMultires(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,

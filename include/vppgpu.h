@@ -61,6 +61,7 @@ int vppgpu_ctx_launch_count(vppgpu_ctx* ctx, unsigned long long* count);
 #define VPPGPU_ME_MULTIRES          1  /* MotionEstimatorH264ImplMultires          */
 #define VPPGPU_ME_MULTIRES_CROSS    2  /* MotionEstimatorH264ImplMultiresCross     */
 #define VPPGPU_ME_MULTIRES_CROSS_V2 3  /* MotionEstimatorH264ImplMultiresCrossVer2 */
+#define VPPGPU_ME_CROSS             4  /* MotionEstimatorH264ImplCross             */
 
 typedef struct vppgpu_me vppgpu_me;
 

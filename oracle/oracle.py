@@ -52,6 +52,7 @@ class Oracle:
         L.vo_me_full_intpel.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P]
         L.vo_me_multires_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.vo_me_multires_cross_v2.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
+        L.vo_me_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_me_multires.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_mc_compensate.argtypes = [_P, _I, _I, _I, _P]
         L.vo_add_clip255.argtypes = [_P, _P, C.c_longlong]
@@ -116,6 +117,10 @@ class Oracle:
                              with_ties=False):
         return self._me_pred(self.lib.vo_me_multires_cross_v2, src, ref, motion_range, mode, dist_incl, slice_map,
                              with_ties)
+
+    def me_cross(self, src, ref, motion_range, mode=0, dist_incl=None, slice_map=None, with_ties=False):
+        """MotionEstimatorH264ImplCross (mode 0 quarter, 1 half, 2 full pel)."""
+        return self._me_pred(self.lib.vo_me_cross, src, ref, motion_range, mode, dist_incl, slice_map, with_ties)
 
     def _me_pred(self, fn, src, ref, motion_range, mode, dist_incl, slice_map, with_ties):
         h, w = src.shape
@@ -251,7 +256,7 @@ class Oracle:
 class Reference:
     """The reference's own C++ classes (only where oracle/_ref was built)."""
 
-    KIND = {"full": 0, "multires": 1, "multires_cross": 2, "multires_cross_v2": 3}
+    KIND = {"full": 0, "multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4}
 
     def __init__(self, path: str = REF_SO):
         self.lib = C.CDLL(path)

@@ -385,3 +385,189 @@ int vo_me_full_intpel(const short* src, const short* ref, int w, int h, int moti
     free(e);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* MotionEstimatorH264ImplCross                                              */
+/* ------------------------------------------------------------------------ */
+/* The first 64 points of MotionEstimatorH264ImplCross::MEH264IC_OptimalPath
+ * (MotionEstimatorH264ImplCross.cpp:89-98), {x, y} within the macroblock:
+ * the distortion of this estimator is the SSD over these points only
+ * (_pathLength = 64, MotionEstimatorH264ImplCross.cpp:226). */
+static const signed char CROSS_PATH[64][2] = {
+    {5, 10}, {13, 5}, {2, 1},   {13, 14}, {1, 14},  {9, 1},   {1, 6},   {15, 9},  {8, 13},  {14, 2},  {7, 4},
+    {10, 8}, {4, 15}, {0, 10},  {0, 3},   {5, 0},   {12, 11}, {4, 7},   {12, 0},  {10, 14}, {3, 12},  {10, 5},
+    {15, 13}, {4, 3}, {7, 8},   {14, 7},  {6, 13},  {11, 3},  {2, 9},   {9, 10},  {15, 1},  {7, 2},   {3, 5},
+    {8, 15}, {1, 12}, {8, 6},   {0, 1},   {12, 9},  {14, 15}, {15, 4},  {11, 12}, {6, 6},   {7, 11},  {0, 7},
+    {14, 11}, {7, 0}, {2, 15},  {12, 7},  {2, 3},   {4, 9},   {12, 2},  {9, 3},   {12, 13}, {3, 0},   {5, 14},
+    {5, 4},  {0, 13}, {8, 9},   {2, 11},  {11, 15}, {10, 1},  {2, 7},   {15, 6},  {9, 12}};
+
+/* OverlayMem2Dv2::Tsd16x16PartialPath over the 64 path points (OverlayMem2Dv2.cpp:2495-2517). */
+static int cross_path_sd(const short* a, int as, const short* b, int bs)
+{
+    int d = 0;
+    for (int p = 0; p < 64; p++) {
+        const int x = CROSS_PATH[p][0], y = CROSS_PATH[p][1];
+        const int e = a[(size_t)y * as + x] - b[(size_t)y * bs + x];
+        d += e * e;
+    }
+    return d;
+}
+
+/* OverlayMem2Dv2::Tsd16x16PartialPathLessThan with batch length 16
+ * (OverlayMem2Dv2.cpp:2449-2493): after each batch of 16 path points the
+ * final distortion is predicted as Dp * 4 / batches-done; the first
+ * prediction above `min` is returned (early exit), else the full 64-point SSD. */
+static int cross_path_lt(const short* a, int as, const short* b, int bs, int min)
+{
+    int dp = 0, expected = 0;
+    for (int batch = 0; batch < 4 && expected <= min; batch++) {
+        for (int p = 16 * batch; p < 16 * batch + 16; p++) {
+            const int x = CROSS_PATH[p][0], y = CROSS_PATH[p][1];
+            const int e = a[(size_t)y * as + x] - b[(size_t)y * bs + x];
+            dp += e * e;
+        }
+        expected = (dp * 4) / (batch + 1);
+    }
+    return expected;
+}
+
+/* The half-pel then quarter-pel passes of MotionEstimatorH264ImplCross::Estimate
+ * (MotionEstimatorH264ImplCross.cpp:492-560): the window of the full-search
+ * estimator (the same LoadHalfQuartPelWindow / LoadQuartPelWindow /
+ * QuarterRead), candidates compared with the path LessThan, strict
+ * improvement; mode 1 stops after the half-pel pass. */
+static void cross_subpel(const short* in, int ins, const short* e, int es, int ox, int oy, int mode, int* min_d,
+                         int* qmx, int* qmy)
+{
+    subpel_win w;
+    win_load(&w, e, es, ox, oy);
+    short blk[256];
+    int hmx = 0, hmy = 0, best = *min_d;
+    for (int k = 0; k < 8; k++) {
+        int qx = 2 * SUB_X[k], qy = 2 * SUB_Y[k];
+        for (int r = 0; r < 16; r++)
+            for (int c = 0; c < 16; c++) blk[r * 16 + c] = (short)win_even(&w, 4 * r + qy, 4 * c + qx);
+        int d = cross_path_lt(in, ins, blk, 16, best);
+        if (d < best) { best = d; hmx = qx; hmy = qy; }
+    }
+    int bx = hmx, by = hmy;
+    if (mode != 1) {
+        for (int k = 0; k < 8; k++) {
+            for (int r = 0; r < 16; r++)
+                for (int c = 0; c < 16; c++)
+                    blk[r * 16 + c] = (short)win_quarter(&w, 4 * r + hmy, 4 * c + hmx, SUB_Y[k], SUB_X[k]);
+            int d = cross_path_lt(in, ins, blk, 16, best);
+            if (d < best) { best = d; bx = hmx + SUB_X[k]; by = hmy + SUB_Y[k]; }
+        }
+    }
+    *min_d = best;
+    *qmx = bx;
+    *qmy = by;
+}
+
+/* Cross positions in test order (MEH264IC_CrossPos, MotionEstimatorH264ImplCross.cpp:83-87). */
+static const int CROSS_X[4] = {-1, 1, 0, 0};
+static const int CROSS_Y[4] = {0, 0, -1, 1};
+
+/* MotionEstimatorH264ImplCross::Estimate (MotionEstimatorH264ImplCross.cpp:354-649):
+ * a full-pel cross search with steps mRng/2, mRng/4, .., 1 (mRng = motion
+ * range in pels) around the running winner, the four cross points tested in
+ * order against the step's running best (ties to the point not farther from
+ * the rounded prediction), the sub-pel passes, then GetBestVector of (best,
+ * prediction, zero) with lambda 0.9 and norm 64.  mode 0 quarter, 1 half,
+ * 2 full pel.  A partial bottom macroblock row is not computed (its vectors
+ * are dropped by the reference). */
+int vo_me_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist, long* avg_dist,
+                int* tie_out)
+{
+    if (!src || !ref || !mv_out || w < MB || h < MB || (w % MB) != 0 || motion_range < 4) return -1;
+    int cols = w / MB, rows = h / MB, nmb = cols * rows;
+    int es = w + 2 * EXT_BORDER;
+    short* e = vo_ext_alloc(ref, w, h, EXT_BORDER);
+    vo_pred_state ps;
+    if (!e || vo_pred_init(&ps, cols, rows, slice) != 0) {
+        free(e);
+        vo_pred_free(&ps);
+        return -2;
+    }
+    const int mrng = motion_range / 4;
+    long total = 0;
+    int included = 0;
+    for (int k = 0; k < nmb; k++) {
+        int n = (k % cols) * MB, m = (k / cols) * MB;
+        const short* in = src + (size_t)m * w + n;
+        int px, py;
+        vo_pred_get(&ps, k, &px, &py);
+        const int pxq = px % 4, pyq = py % 4;
+        int px0 = px / 4, py0 = py / 4;
+        const int prx = round_pred(px), pry = round_pred(py);
+
+        const int eox = n + EXT_BORDER, eoy = m + EXT_BORDER;
+        const int zd = cross_path_sd(in, w, e + (size_t)eoy * es + eox, es);
+        int min_d = zd, mx = 0, my = 0, tie = 0;
+        int xl, xr, yu, yd;
+        full_range(n, m, w, h, motion_range, mrng, &xl, &xr, &yu, &yd);
+        for (int step = mrng / 2; step > 0; step /= 2) {
+            int rmx = 0, rmy = 0;
+            for (int c = 0; c < 4; c++) {
+                const int i = step * CROSS_Y[c], j = step * CROSS_X[c];
+                if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+                const short* cand = e + (size_t)(eoy + my + i) * es + eox + mx + j;
+                const int d = cross_path_lt(in, w, cand, es, min_d);
+                if (d > min_d) continue;
+                if (d == min_d) {
+                    tie = 1;
+                    const int cxo = mx + rmx - prx, cyo = my + rmy - pry, nxo = mx + j - prx, nyo = my + i - pry;
+                    if ((cyo * cyo + cxo * cxo) - (nyo * nyo + nxo * nxo) < 0) continue;
+                }
+                min_d = d;
+                rmx = j;
+                rmy = i;
+            }
+            mx += rmx;
+            my += rmy;
+        }
+        int mvx = 4 * mx, mvy = 4 * my;
+        if (mode != 2) {
+            int qmx, qmy;
+            cross_subpel(in, w, e, es, eox + mx, eoy + my, mode, &min_d, &qmx, &qmy);
+            mvx += qmx;
+            mvy += qmy;
+        }
+        /* prediction clamped to one macroblock outside the picture (MotionEstimatorH264ImplCross.cpp:574-583) */
+        if (px0 + n > w) px0 = MB;
+        if (px0 + n < -MB) px0 = -MB;
+        if (py0 + m > h) py0 = MB;
+        if (py0 + m < -MB) py0 = -MB;
+        px = 4 * px0 + pxq;
+        py = 4 * py0 + pyq;
+        const int pox = vo_clamp_origin(px0 + n + EXT_BORDER, es, MB);
+        const int poy = vo_clamp_origin(py0 + m + EXT_BORDER, h + 2 * EXT_BORDER, MB);
+        int pd;
+        if (pxq || pyq) {
+            short blk[256];
+            vo_qread16_ext(e, es, pox, poy, pxq, pyq, blk);
+            pd = cross_path_sd(in, w, blk, 16);
+        } else {
+            pd = cross_path_sd(in, w, e + (size_t)poy * es + pox, es);
+        }
+        int xs[5] = {mvx, px, 0, 0, 0}, ys[5] = {mvy, py, 0, 0, 0}, ds[5] = {min_d, pd, zd, zd, zd};
+        int pos = vo_best_vector5(xs, ys, ds, 0.9, 64.0, px, py);
+        mvx = xs[pos];
+        mvy = ys[pos];
+        if (dist_incl && dist_incl[k]) {
+            included++;
+            total += ds[pos];
+        }
+        if (mb_dist) mb_dist[k] = ds[pos];
+        if (tie_out) tie_out[k] = tie;
+        mv_out[2 * k] = (short)mvx;
+        mv_out[2 * k + 1] = (short)mvy;
+        vo_pred_set(&ps, k, mvx, mvy);
+    }
+    if (avg_dist) *avg_dist = included ? total / included : 0;
+    vo_pred_free(&ps);
+    free(e);
+    return 0;
+}

@@ -44,6 +44,15 @@ int vo_num_mbs(int w, int h);
  *               chosen by GetBestVector, Full.cpp:579-590).
  *   avg_dist  : the reference's avgDistortion out-param.
  * Returns 0 on success, negative on invalid arguments. */
+/* MotionEstimatorH264ImplCross::Estimate (oracle_me_full.c): cross search with
+ * the 64-point path distortion and its extrapolating LessThan, the full-search
+ * estimator's sub-pel window, GetBestVector lambda 0.9 / norm 64.  mode 0
+ * quarter, 1 half, 2 full pel.  tie_out (optional): 1 where the full-pel search
+ * met an exact tie. */
+int vo_me_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist, long* avg_dist,
+                int* tie_out);
+
 int vo_me_full(const short* src, const short* ref, int w, int h, int motion_range,
                const unsigned char* dist_incl, const int* slice,
                short* mv_out, int* mb_dist, long* avg_dist);

@@ -259,7 +259,8 @@ def main() -> None:
     oracle.build(with_reference=True)
     ref = oracle.Reference()
     makers = {"me_full": me_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
-              "me_mr": lambda r: mrc2_fixtures(r, "multires"), "mc": mc_fixtures,
+              "me_mr": lambda r: mrc2_fixtures(r, "multires"), "me_cross": lambda r: mrc2_fixtures(r, "cross"),
+              "mc": mc_fixtures,
               "transform": transform_fixtures, "dc": dc_fixtures, "yuv2rgb": yuv2rgb_fixtures,
               "colour": colour_fixtures}
     names = sys.argv[1:] or list(makers)

@@ -1,5 +1,6 @@
-"""GPU parity of the multi-resolution estimators with a predictor,
-MotionEstimatorH264ImplMultiresCrossVer2 and MotionEstimatorH264ImplMultires:
+"""GPU parity of the estimators with a predictor besides the full search,
+MotionEstimatorH264ImplMultiresCrossVer2, MotionEstimatorH264ImplMultires and
+MotionEstimatorH264ImplCross:
 vectors and avgDistortion bit-exact with the reference's golden fixtures (modes 0/1/2,
 with and without pDistortionIncluded, a partial bottom row, integer-shift
 content), and vectors, per-macroblock distortions and averages bit-exact with
@@ -18,7 +19,8 @@ pytestmark = pytest.mark.gpu
 CASES = ["qcif_r64", "cif_r128", "partial_r128", "small_r32", "shift_r128"]
 # estimator class, oracle method, golden fixture file
 KINDS = {"ver2": ("MotionEstimatorH264ImplMultiresCrossVer2", "me_multires_cross_v2", "me_mrc2.npz"),
-         "multires": ("MotionEstimatorH264ImplMultires", "me_multires", "me_mr.npz")}
+         "multires": ("MotionEstimatorH264ImplMultires", "me_multires", "me_mr.npz"),
+         "cross": ("MotionEstimatorH264ImplCross", "me_cross", "me_cross.npz")}
 
 
 @pytest.fixture(params=list(KINDS))
@@ -49,8 +51,8 @@ def test_against_golden(vpp, ctx, golden, case, mode, kind):
     mv, _, avg, me = estimate(vpp, ctx, src, ref, mr, mode, kind=kind)
     np.testing.assert_array_equal(mv, g[f"{case}_m{mode}_mv"])
     assert avg == 0
-    if mode == 0:
-        assert me.GetMode() == (2 if w * h > 40000 else 1)
+    if mode == 0:  # the multi-resolution estimators pick by area, Cross keeps quarter pel
+        assert me.GetMode() == (0 if kind == "cross" else (2 if w * h > 40000 else 1))
     mvi, _, avgi, _ = estimate(vpp, ctx, src, ref, mr, mode, g[f"{case}_incl"], kind=kind)
     np.testing.assert_array_equal(mvi, mv)
     assert avgi == int(g[f"{case}_m{mode}_avg"][0])

@@ -187,6 +187,39 @@ def test_me_multires_cross_v2_matches_reference(orc, golden, case, mode):
     assert avgi == int(g[f"{case}_m{mode}_avg"][0])
 
 
+@pytest.mark.parametrize("case", MRC2_CASES)
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_me_cross_matches_reference(orc, golden, case, mode):
+    """MotionEstimatorH264ImplCross (mode 0 quarter, 1 half, 2 full pel)."""
+    g = golden("me_cross.npz")
+    src = g[f"{case}_src"].astype(np.int16)
+    ref = g[f"{case}_ref"].astype(np.int16)
+    mr = int(g[f"{case}_meta"][2])
+    mv, _, avg = orc.me_cross(src, ref, mr, mode=mode)
+    np.testing.assert_array_equal(mv, g[f"{case}_m{mode}_mv"])
+    assert avg == 0
+    mvi, _, avgi = orc.me_cross(src, ref, mr, mode=mode, dist_incl=g[f"{case}_incl"])
+    np.testing.assert_array_equal(mvi, mv)
+    assert avgi == int(g[f"{case}_m{mode}_avg"][0])
+
+
+@ref_available
+def test_me_cross_flat_content_ties(orc):
+    """Periodic content: the cross search meets exact ties that the rounded
+    prediction decides."""
+    ref_lib = oracle_mod.Reference()
+    w, h = 128, 96
+    yy, xx = np.mgrid[0:h, 0:w]
+    a = ((xx // 8 + yy // 8) % 2 * 40 + 100).astype(np.int16)
+    b = np.roll(a, (3, 5), axis=(0, 1))
+    b[20:40, 30:60] = 128
+    for mode in (0, 1, 2):
+        mv_r, _ = ref_lib.me("cross", b, a, 128, mode=mode)
+        mv_o, _, _, ties = orc.me_cross(b, a, 128, mode=mode, with_ties=True)
+        assert ties.sum() > 0
+        np.testing.assert_array_equal(mv_o, mv_r)
+
+
 @ref_available
 @pytest.mark.parametrize("seed,w,h,mr,mode", [(51, 176, 144, 128, 0), (52, 352, 288, 128, 1), (53, 208, 120, 96, 2),
                                               (54, 96, 64, 64, 2), (55, 640, 360, 128, 0)])
