@@ -311,11 +311,12 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     }
     if (kind == VPPGPU_ME_CROSS) {
         // MotionEstimatorH264ImplCross(…, pMVPred, …) + Create(): the padded reference with its half-pel
-        // planes, per-MB prediction state and the cache of searches at other rounded predictions
+        // planes, per-MB prediction state, tie trees and the cache of searches at other rounded predictions
         if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
             (rc = dalloc(&me->d_src8, npix)) || (rc = dalloc(&me->d_refp, npad)) ||
             (rc = dalloc(&me->d_hpel, 3 * npad)) ||
             (rc = dalloc(&me->d_search_cache, (size_t)me->nmb * vppgpu::V2_SEARCH_CACHE)) ||
+            (rc = dalloc((unsigned char**)&me->d_tie_runs, vppgpu::mrc_tie_runs_bytes() * (size_t)me->nmb)) ||
             (rc = dalloc(&me->tie_list, me->nmb)) ||
             (rc = dalloc(&me->d_job, 1)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
             (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||

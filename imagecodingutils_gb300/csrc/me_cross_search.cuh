@@ -20,6 +20,7 @@
 #pragma once
 
 #include "me_full_common.cuh"
+#include "me_mrc_search.cuh"
 
 namespace vppgpu {
 namespace cross {
@@ -97,9 +98,12 @@ struct CrossResult {
     bool tie;
 };
 
-// The search of macroblock (n, m) at rounded prediction (prx, pry); mode 0
-// quarter, 1 half, 2 full pel.  One warp; the result is warp-uniform.
-static __device__ __noinline__ CrossResult cross_search(const FullArgs& a, int n, int m, int prx, int pry, int lane)
+// The search of macroblock (n, m); an exact tie of the full-pel cross is
+// decided by skip(cx, cy, nx, ny) (true keeps the current winner (cx, cy)
+// against the point (nx, ny)).  mode 0 quarter, 1 half, 2 full pel.  One
+// warp; the result is warp-uniform.
+template <typename Skip>
+__device__ __forceinline__ CrossResult cross_search_with(const FullArgs& a, int n, int m, Skip&& skip, int lane)
 {
     constexpr int CX[4] = {-1, 1, 0, 0}, CY[4] = {0, 0, -1, 1};  // MEH264IC_CrossPos
     const LaneMasks mk = lane_masks(lane);
@@ -129,8 +133,7 @@ static __device__ __noinline__ CrossResult cross_search(const FullArgs& a, int n
             if (d > min_d) continue;
             if (d == min_d) {
                 tie = true;
-                const int cx = mx + rmx - prx, cy = my + rmy - pry, nx = mx + j - prx, ny = my + i - pry;
-                if ((cy * cy + cx * cx) - (ny * ny + nx * nx) < 0) continue;
+                if (skip(mx + rmx, my + rmy, mx + j, my + i)) continue;
             }
             min_d = d;
             rmx = j;
@@ -183,6 +186,44 @@ static __device__ __noinline__ CrossResult cross_search(const FullArgs& a, int n
         mvy += qmy;
     }
     return CrossResult{mvx, mvy, min_d, zd, tie};
+}
+
+// The search at rounded prediction (prx, pry): a tie keeps the current
+// winner when it is nearer (MotionEstimatorH264ImplCross.cpp:446-456).
+static __device__ __noinline__ CrossResult cross_search(const FullArgs& a, int n, int m, int prx, int pry, int lane)
+{
+    return cross_search_with(
+        a, n, m,
+        [prx, pry](int cx, int cy, int nx, int ny) {
+            return (cx - prx) * (cx - prx) + (cy - pry) * (cy - pry) < (nx - prx) * (nx - prx) + (ny - pry) * (ny - pry);
+        },
+        lane);
+}
+
+// Tie tree run `run` of a tie macroblock (the tree of the Ver2 estimator,
+// mrc::V2TieRun, at level 0): its t-th tie (t < 3) takes the point by bit t
+// of run; the two vectors compared and the result are recorded.
+static __device__ __noinline__ void cross_search_run(const FullArgs& a, int n, int m, int run, mrc::V2TieRun* rec,
+                                                      int lane)
+{
+    int t = 0, geo[mrc::V2_TIE_BITS] = {0, 0, 0};
+    const CrossResult r = cross_search_with(
+        a, n, m,
+        [&](int cx, int cy, int nx, int ny) {
+            const bool take = t < mrc::V2_TIE_BITS ? ((run >> t) & 1) : true;
+            if (t < mrc::V2_TIE_BITS)
+                geo[t] = (cx & 0xff) | ((cy & 0xff) << 8) | ((nx & 0xff) << 16) | ((ny & 0xff) << 24);
+            t++;
+            return !take;
+        },
+        lane);
+    if (lane == 0) {
+        for (int e = 0; e < mrc::V2_TIE_BITS; e++) rec->geo[e] = geo[e];
+        rec->lvl = 0;  // every tie at full pel
+        rec->nev = t;
+        rec->mv = pack_mv(r.mvx, r.mvy);
+        rec->min_d = r.min_d;
+    }
 }
 
 // Tsd16x16PartialPath at the prediction (QuarterRead's sixteen cases).

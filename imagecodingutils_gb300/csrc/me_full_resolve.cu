@@ -118,8 +118,18 @@ __device__ __noinline__ void pred_search_at(const FullArgs& a, int k, int px, in
                                             int* minD, mrc::Lattice* lt)
 {
     if constexpr (kEst == cross::EST_CROSS) {
-        // Cross: the search depends on the prediction only through its rounding
-        // (MotionEstimatorH264ImplCross.cpp:393-405), the cache key
+        // Cross: the tie tree, else a search at the rounded prediction (the
+        // only way the prediction enters, MotionEstimatorH264ImplCross.cpp:393-405),
+        // cached by it
+        int tv, td;
+        if (mrc::tie_tree_result(cross::EST_CROSS, static_cast<const mrc::V2TieRun*>(a.tie_runs) +
+                                                       (size_t)k * mrc::V2_TIE_RUNS,
+                                 px, py, &tv, &td)) {
+            *mvx = mv_x(tv);
+            *mvy = mv_y(tv);
+            *minD = td;
+            return;
+        }
         const int key = pack_mv(round_pred(px), round_pred(py));
         int4* sc = a.search_cache + (size_t)k * V2_SEARCH_CACHE;
         const int4 e = lane < V2_SEARCH_CACHE ? __ldcg(sc + lane) : make_int4(0, 0, 0, -1);
