@@ -40,7 +40,17 @@ struct YuvParams {
     int lim_b[256], lim_r[256];
 };
 
-__device__ __forceinline__ int floordiv1000(int n) { return n >= 0 ? n / 1000 : -((999 - n) / 1000); }
+// floor(n / 1000) and whether 1000 divides n, for |n| < 2^27 (every term of
+// short inputs: |2033 u| + |581 v| + 500 < 9e7): one unsigned division of
+// the biased numerator by a constant.
+__device__ __forceinline__ int floordiv1000(int n, bool& exact)
+{
+    constexpr int kBias = 1 << 17;  // multiples of 1000 added: n + 1000 * kBias > 0
+    const unsigned b = (unsigned)(n + 1000 * kBias);
+    const unsigned q = b / 1000u;
+    exact = b - q * 1000u == 0u;
+    return (int)q - kBias;
+}
 
 // Where the exact term is an integer m, the double term c may lie just
 // below it: c = m - d.  Then (int)(lum + c) is K = lum + m when the double
@@ -80,17 +90,18 @@ __device__ __forceinline__ Terms block_terms(int su, int sv, const YuvParams& p)
     }
     const int nb = p.a0 * u + 500, ng = -394 * u - 581 * v + 500, nr = 1140 * v + 500;
     Terms t;
-    t.qb = floordiv1000(nb);
-    t.qg = floordiv1000(ng);
-    t.qr = floordiv1000(nr);
+    bool xb, xg, xr;
+    t.qb = floordiv1000(nb, xb);
+    t.qg = floordiv1000(ng, xg);
+    t.qr = floordiv1000(nr, xr);
     t.lb = t.lg = t.lr = 0;
-    if (nb % 1000 == 0)
+    if (xb)
         t.lb = (unsigned)(u + 128) < 256u ? p.lim_b[u + 128]
                                           : below_limit(__dadd_rn(__dmul_rn(p.U0, (double)u), 0.5), t.qb);
-    if (ng % 1000 == 0)
+    if (xg)
         t.lg = below_limit(__dadd_rn(__dadd_rn(__dmul_rn(-0.394, (double)u), __dmul_rn(-0.581, (double)v)), 0.5),
                            t.qg);
-    if (nr % 1000 == 0)
+    if (xr)
         t.lr = (unsigned)(v + 128) < 256u ? p.lim_r[v + 128]
                                           : below_limit(__dadd_rn(__dmul_rn(1.140, (double)v), 0.5), t.qr);
     return t;
@@ -104,13 +115,17 @@ __device__ __forceinline__ int luma(int s, const YuvParams& p)
 __device__ __forceinline__ int chan(int l, int q, int lim)
 {
     const int k = l + q;
-    return clip255(k - (k >= 1 && k <= lim ? 1 : 0));
+    return clip255(k - ((unsigned)(k - 1) < (unsigned)lim ? 1 : 0));  // 1 <= k <= lim
 }
 
-// b, g, r of one pixel packed in the low 24 bits
+// b, g, r of one pixel packed in the low 24 bits; kExact: some term of the
+// block needs below_limit's correction
+template <bool kExact = true>
 __device__ __forceinline__ unsigned pixel(int s, const Terms& t, const YuvParams& p)
 {
     const int l = luma(s, p);
+    if constexpr (!kExact)
+        return (unsigned)clip255(l + t.qb) | ((unsigned)clip255(l + t.qg) << 8) | ((unsigned)clip255(l + t.qr) << 16);
     return (unsigned)chan(l, t.qb, t.lb) | ((unsigned)chan(l, t.qg, t.lg) << 8) | ((unsigned)chan(l, t.qr, t.lr) << 16);
 }
 
@@ -139,13 +154,29 @@ __global__ void __launch_bounds__(256) k_yuv_rgb_x8(const short* __restrict__ Y,
         const short* su = reinterpret_cast<const short*>(&uu);
         const short* sv = reinterpret_cast<const short*>(&vv);
         unsigned ra[8], rb[8];
+        Terms tk[4];
+        int lims = 0;
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            const Terms t = block_terms(su[k], sv[k], p);
-            ra[2 * k] = pixel(sa[2 * k], t, p);
-            ra[2 * k + 1] = pixel(sa[2 * k + 1], t, p);
-            rb[2 * k] = pixel(sb[2 * k], t, p);
-            rb[2 * k + 1] = pixel(sb[2 * k + 1], t, p);
+            tk[k] = block_terms(su[k], sv[k], p);
+            lims |= tk[k].lb | tk[k].lg | tk[k].lr;
+        }
+        if (__any_sync(__activemask(), lims != 0)) {  // a block of the warp needs the correction
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                ra[2 * k] = pixel<true>(sa[2 * k], tk[k], p);
+                ra[2 * k + 1] = pixel<true>(sa[2 * k + 1], tk[k], p);
+                rb[2 * k] = pixel<true>(sb[2 * k], tk[k], p);
+                rb[2 * k + 1] = pixel<true>(sb[2 * k + 1], tk[k], p);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                ra[2 * k] = pixel<false>(sa[2 * k], tk[k], p);
+                ra[2 * k + 1] = pixel<false>(sa[2 * k + 1], tk[k], p);
+                rb[2 * k] = pixel<false>(sb[2 * k], tk[k], p);
+                rb[2 * k + 1] = pixel<false>(sb[2 * k + 1], tk[k], p);
+            }
         }
         // 8 pixels x 3 bytes = six little-endian words per row
         auto pack = [](const unsigned* q, unsigned* w) {
