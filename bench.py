@@ -49,9 +49,28 @@ def dist_env():
     return rank, world, local
 
 
+def shard_seed(rank: int) -> int:
+    """Each rank estimates its own seeded sequence: independent frames, no
+    exchange between ranks (weak scaling)."""
+    return 1234 + 97 * rank
+
+
 def frames_for(rank: int):
     from imagecodingutils_gb300 import synth
-    return synth.pan_sequence(1234 + 97 * rank, W, H, NFRAMES)
+    return synth.pan_sequence(shard_seed(rank), W, H, NFRAMES)
+
+
+def max_over_ranks(torch, dist, values, device):
+    """The slowest rank's timings (barrier-bracketed, max over ranks)."""
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def whole_job_rate(units_per_rank: float, world: int, ms: float) -> float:
+    """Units all ranks processed per second of the slowest rank."""
+    return units_per_rank * world / (ms * 1e-3)
 
 
 def algorithmic_px_ops(subpel: bool = True):
@@ -732,14 +751,9 @@ def main():
         step_host(0)
         check = check and bool(np.array_equal(h_mv.numpy(), mv_o))
 
-    times = torch.tensor([dev_ms, e2e_s * 1e3], dtype=torch.float64, device=f"cuda:{local}")
-    if dist is not None:
-        dist.all_reduce(times, op=dist.ReduceOp.MAX)
-    dev_ms, e2e_ms = float(times[0]), float(times[1])
-
-    mbs_total = NMB * args.steps * world
-    value = mbs_total / (dev_ms * 1e-3)
-    e2e_value = mbs_total / (e2e_ms * 1e-3)
+    dev_ms, e2e_ms = max_over_ranks(torch, dist, [dev_ms, e2e_s * 1e3], f"cuda:{local}")
+    value = whole_job_rate(NMB * args.steps, world, dev_ms)
+    e2e_value = whole_job_rate(NMB * args.steps, world, e2e_ms)
 
     if rank == 0:
         dp4a = C.c_double()
