@@ -634,7 +634,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="wall time of each CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
-    ap.add_argument("--batch-streams", type=int, default=8)
+    ap.add_argument("--batch-streams", type=int, default=16)
     ap.add_argument("--batch-reps", type=int, default=3)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes and sweep policy")
