@@ -357,8 +357,12 @@ MULTIRES = {  # kind -> (class name, oracle method)
     "multires_cross": ("MotionEstimatorH264ImplMultiresCross", "me_multires_cross"),
     "multires_cross_v2": ("MotionEstimatorH264ImplMultiresCrossVer2", "me_multires_cross_v2"),
     "cross": ("MotionEstimatorH264ImplCross", "me_cross"),
+    "h263_multires_cross": ("MotionEstimatorH263ImplMultiresCross", "me_h263_multires_cross"),
 }
-MULTIRES_CODE = {"multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4}  # VPPGPU_ME_*
+MULTIRES_CODE = {"multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4,
+                 "h263_multires_cross": 5}  # VPPGPU_ME_*
+# motion ranges are in quarter pels, the H.263 estimator's in half pels: the same +-32 pels
+MULTIRES_RANGE = {"h263_multires_cross": MOTION_RANGE // 2}
 
 
 TUNE_PAIRS = 8
@@ -384,8 +388,9 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
     on all host threads as its CPU baseline."""
     cls, ofn = MULTIRES[kind]
     code = MULTIRES_CODE[kind]
+    mr = MULTIRES_RANGE.get(kind, MOTION_RANGE)
     h = C.c_void_p()
-    _lib.check(L.vppgpu_me_create(ctx.handle, code, W, H, MOTION_RANGE, C.byref(h)), "vppgpu_me_create")
+    _lib.check(L.vppgpu_me_create(ctx.handle, code, W, H, mr, C.byref(h)), "vppgpu_me_create")
     _lib.check(L.vppgpu_me_set_mode(h, 0), "vppgpu_me_set_mode")
     mode = C.c_int()
     L.vppgpu_me_get_mode(h, C.byref(mode))
@@ -411,8 +416,8 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
     out = {"value": NMB / (ms * 1e-3), "unit": UNIT, "ms_per_frame": ms, "mode": mode.value, "autotune": tuning,
-           "workload": f"{cls} plain per-frame, {W}x{H}, motionRange {MOTION_RANGE}"}
-    if kind != "multires_cross":
+           "workload": f"{cls} plain per-frame, {W}x{H}, motionRange {mr}"}
+    if kind not in ("multires_cross", "h263_multires_cross"):
         # per-frame device time and how each frame's predictions were decided
         per, exact = [], 0
         for t in range(NFRAMES - 1):
@@ -434,13 +439,13 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
         from concurrent.futures import ThreadPoolExecutor
         from oracle.oracle import Oracle
         orc = Oracle()
-        mv_o = getattr(orc, ofn)(frames[1], frames[0], MOTION_RANGE, mode=mode.value)[0]
+        mv_o = getattr(orc, ofn)(frames[1], frames[0], mr, mode=mode.value)[0]
         out["parity_first_frame"] = bool(np.array_equal(d_mv.cpu().numpy(), mv_o))
         nth = os.cpu_count() or 1
         npairs, t0 = 0, time.perf_counter()
         with ThreadPoolExecutor(nth) as ex:  # ctypes calls release the GIL: one estimate per thread
             while time.perf_counter() - t0 < args.cpu_seconds:
-                list(ex.map(lambda i: getattr(orc, ofn)(frames[i + 1], frames[i], MOTION_RANGE, mode=mode.value),
+                list(ex.map(lambda i: getattr(orc, ofn)(frames[i + 1], frames[i], mr, mode=mode.value),
                             range(NFRAMES - 1)))
                 npairs += NFRAMES - 1
         dt = time.perf_counter() - t0
@@ -793,6 +798,8 @@ def main():
                                 kind="multires")
         cr = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
                                 kind="cross")
+        h263 = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
+                                  kind="h263_multires_cross")
         pk, pk_kind = peaks()
         hbm_rows = run_hbm_paths(torch, _lib, L, ctx, stream, f"cuda:{local}", pk)
         line = {
@@ -817,7 +824,8 @@ def main():
             "hbm_peak_gbs": pk.get("hbm_gbs"), "peaks_source": pk_kind,
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
             "serving": serving,
-            "multires": mr, "multires_cross": mrc, "multires_cross_v2": mrc2, "cross": cr, **hbm_rows,
+            "multires": mr, "multires_cross": mrc, "multires_cross_v2": mrc2, "cross": cr,
+            "h263_multires_cross": h263, **hbm_rows,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

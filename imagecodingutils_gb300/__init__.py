@@ -29,7 +29,7 @@ from ._lib import VppGpuError, check, load
 __all__ = [
     "Context", "get_context", "MotionEstimatorH264ImplFull", "MotionEstimatorH264ImplMultires",
     "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross",
-    "MotionEstimatorBatch",
+    "MotionEstimatorH263ImplMultiresCross", "MotionEstimatorBatch",
     "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
     "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1", "FastForwardDC4x4ITImpl1",
     "FastForwardDC2x2ITImpl1", "FastInverseDC4x4ITImpl1", "FastInverseDC2x2ITImpl1",
@@ -227,6 +227,16 @@ class MotionEstimatorH264ImplMultiresCross(_MotionEstimatorBase):
             check(load().vppgpu_me_get_mode(self._h_me, C.byref(m)), "vppgpu_me_get_mode")
             return m.value
         return self._mode
+
+
+class MotionEstimatorH263ImplMultiresCross(MotionEstimatorH264ImplMultiresCross):
+    """GPU MotionEstimatorH263ImplMultiresCross
+    (src/CodecUtils/MotionEstimatorH263ImplMultiresCross.cpp): the MultiresCross
+    levels with the H.263 half-pel stage (OverlayMem2Dv2::HalfRead corners, then
+    the points beside the winner); motionRange (at most 64) and the vectors in
+    half pels."""
+
+    KIND = _lib.ME_H263_MULTIRES_CROSS
 
 
 class MotionEstimatorH264ImplMultires(MotionEstimatorH264ImplMultiresCross):

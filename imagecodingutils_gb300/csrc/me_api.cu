@@ -187,9 +187,10 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
 {
     vppgpu_ctx* ctx = me->ctx;
     VPP_CUDA(cudaMemsetAsync(me->ctrl, 0, sizeof(vppgpu::MeCtrl), ctx->stream));
-    if (me->kind == VPPGPU_ME_MULTIRES_CROSS)
+    if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS)
         return vppgpu::mrc_launch(ctx, me->W, me->H, me->motion_range, me->mode, d_src16, d_ref16, me->d_mrc, d_incl,
-                                  d_mv, d_dist, d_avg, me->ctrl, me->mrc_warps);
+                                  d_mv, d_dist, d_avg, me->ctrl, me->mrc_warps,
+                                  me->kind == VPPGPU_ME_H263_MULTIRES_CROSS);
     int rc = vppgpu::set_job(ctx, me->d_job, vppgpu::JobDesc{d_src16, d_ref16, d_incl, d_slice, d_mv, d_dist, d_avg});
     if (rc) return rc;
     if (me->kind == VPPGPU_ME_CROSS) {
@@ -264,7 +265,9 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
     if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
     if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
-    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_CROSS) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_H263_MULTIRES_CROSS) return VPPGPU_ERR_UNSUPPORTED;
+    // MotionEstimatorH263ImplMultiresCross's range is in half pels: at most 64 (+-31 pels), as 128 quarter pels
+    if (kind == VPPGPU_ME_H263_MULTIRES_CROSS && motion_range > 64) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me* me = (vppgpu_me*)calloc(1, sizeof(vppgpu_me));
@@ -292,8 +295,8 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     size_t npix = (size_t)width * height;
     size_t npad = (size_t)me->rstride * (height + 2 * vppgpu::PAD);
     me->plane_size = npad;
-    if (kind == VPPGPU_ME_MULTIRES_CROSS) {
-        // MotionEstimatorH264ImplMultiresCross(…) + Create(): the level planes and outputs only
+    if (kind == VPPGPU_ME_MULTIRES_CROSS || kind == VPPGPU_ME_H263_MULTIRES_CROSS) {
+        // MotionEstimatorH264ImplMultiresCross / H263ImplMultiresCross (…) + Create(): the level planes and outputs
         if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
             (rc = dalloc(&me->d_mrc, vppgpu::mrc_scratch_bytes(width, height))) ||
             (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
@@ -553,7 +556,8 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
 {
     if (!me || sweeps < 0 || sweeps > vppgpu::RELAX_SWEEPS) return VPPGPU_ERR_INVALID_ARG;
-    if (me->kind == VPPGPU_ME_MULTIRES_CROSS) return VPPGPU_ERR_UNSUPPORTED;
+    if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS)
+        return VPPGPU_ERR_UNSUPPORTED;
     if (sweeps == me->relax_sweeps) return VPPGPU_OK;
     int rc = vppgpu::bind(me->ctx);
     if (rc) return rc;
@@ -608,7 +612,7 @@ extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src
     std::vector<TuneCfg> cands;
     const TuneCfg cur{me->relax_sweeps, me->grid_sweeps, me->relax_blocks_per_sm, me->mrc_warps};
     cands.push_back(cur);
-    if (me->kind == VPPGPU_ME_MULTIRES_CROSS) {
+    if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS) {
         for (int w : {2, 4, 8})
             if (w != cur.warps) cands.push_back({cur.relax, cur.grid, cur.bps, w});
     } else {
@@ -799,7 +803,7 @@ int vppgpu_me_batch_create(vppgpu_ctx* ctx, int kind, int streams, vppgpu_me_bat
 {
     if (!ctx || !out || streams < 1) return VPPGPU_ERR_INVALID_ARG;
     *out = nullptr;
-    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_CROSS) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_H263_MULTIRES_CROSS) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me_batch* b = (vppgpu_me_batch*)calloc(1, sizeof(vppgpu_me_batch));

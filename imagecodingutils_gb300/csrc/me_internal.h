@@ -111,7 +111,7 @@ size_t mrc_scratch_bytes(int W, int H);
 // warps: macroblocks (warps) per CTA of the search kernel, 2, 4 or 8.
 int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const short* d_src16, const short* d_ref16,
                unsigned char* scratch, const unsigned char* incl, int* out_mv, int* out_dist, long long* out_avg,
-               MeCtrl* ctrl, int warps = 8);
+               MeCtrl* ctrl, int warps = 8, bool h263 = false);
 
 // Device address of the status word (ST_* bits) of a handle's current
 // estimate, and the C ABI status those bits stand for.

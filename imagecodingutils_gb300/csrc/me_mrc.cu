@@ -112,6 +112,9 @@ __global__ void __launch_bounds__(256) k_mrc_level2(const unsigned char* __restr
     }
 }
 
+// kH263: MotionEstimatorH263ImplMultiresCross (…H263ImplMultiresCross.cpp:531-1010), whose motion
+// range (doubled into a.motion_range by the caller) and vectors are in half pels.
+template <bool kH263>
 __global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
 {
     extern __shared__ Lattice lattice[];  // one per warp
@@ -121,13 +124,13 @@ __global__ void __launch_bounds__(256) k_mrc_search(MrcArgs a)
     bool bad = false;
     const int mbr = k / a.cols, mbc = k - mbr * a.cols;
     const int vec_pos = k < a.nmb ? k : a.nmb;
-    const MbSearch r = search_mb_mrc(a, lattice[wib], mbr, mbc, lane, bad);
+    const MbSearch r = search_mb_mrc<kH263>(a, lattice[wib], mbr, mbc, lane, bad);
     int mvx = r.mvx, mvy = r.mvy;
 
-    // accept-or-zero heuristic (…MultiresCross.cpp:943-999)
+    // accept-or-zero heuristic (…MultiresCross.cpp:943-999; …H263ImplMultiresCross.cpp:960-999: (diff >> 2))
     int weight = 0;
     const int diff0 = r.zero_d - r.min_d, mag = mvx * mvx + mvy * mvy;
-    if (diff0 < mag) weight++;
+    if (kH263 ? (diff0 >> 2) < mag : diff0 < mag) weight++;
     if (r.zero_d < MRC_NOISE_FLOOR) weight++;
     if (diff0 * 10 < r.min_d) weight++;
     int chosen;
@@ -289,9 +292,9 @@ int levels_launch(vppgpu_ctx* ctx, const MrcArgs& a, const short* d_src16, const
 
 int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const short* d_src16, const short* d_ref16,
                unsigned char* scratch, const unsigned char* incl, int* out_mv, int* out_dist, long long* out_avg,
-               MeCtrl* ctrl, int warps)
+               MeCtrl* ctrl, int warps, bool h263)
 {
-    MrcArgs a = mrc_args(W, H, motion_range, mode, scratch);
+    MrcArgs a = mrc_args(W, H, h263 ? 2 * motion_range : motion_range, mode, scratch);
     a.incl = incl;
     a.out_mv = out_mv;
     a.out_dist = out_dist;
@@ -300,7 +303,10 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
     int rc = levels_launch(ctx, a, d_src16, d_ref16);
     if (rc) return rc;
     const int mbs = a.cols * a.rows_all, wpb = (warps == 2 || warps == 4) ? warps : 8;
-    k_mrc_search<<<(mbs + wpb - 1) / wpb, 32 * wpb, wpb * sizeof(Lattice), ctx->stream>>>(a);
+    if (h263)
+        k_mrc_search<true><<<(mbs + wpb - 1) / wpb, 32 * wpb, wpb * sizeof(Lattice), ctx->stream>>>(a);
+    else
+        k_mrc_search<false><<<(mbs + wpb - 1) / wpb, 32 * wpb, wpb * sizeof(Lattice), ctx->stream>>>(a);
     VPP_CHECK_LAUNCH(ctx);
     k_mrc_average<<<1, 1, 0, ctx->stream>>>(out_avg, ctrl);
     VPP_CHECK_LAUNCH(ctx);

@@ -258,7 +258,7 @@ __device__ __forceinline__ bool farther(int mx, int my, int rmx, int rmy, int j,
 // decides an exact tie at an integer level: true keeps the current best
 // (offset (rmx, rmy) from the centre (mx, my)), false takes the candidate at
 // offset (j, i).  It is called with the same arguments in every lane.
-template <bool kVer2, typename Skip>
+template <bool kVer2, typename Skip, bool kH263 = false>
 __device__ MbSearch search_mb_with(const MrcArgs& a, Lattice& LT, int mbr, int mbc, Skip&& skip, int lane, bool& bad)
 {
     const int m = 16 * mbr, n = 16 * mbc, p = 8 * mbr, q = 8 * mbc, kk = 4 * mbr, ll = 4 * mbc;
@@ -390,6 +390,61 @@ __device__ MbSearch search_mb_with(const MrcArgs& a, Lattice& LT, int mbr, int m
         }
     mx += rmx;
     my += rmy;
+    if constexpr (kH263) {
+        // MotionEstimatorH263ImplMultiresCross (…H263ImplMultiresCross.cpp:885-940): the best of the
+        // four diagonal half-pel corners, then the two points beside the winning corner (the full cross
+        // if no corner won), each an OverlayMem2Dv2::HalfRead block (bilinear, +2 >> 2 diagonal, +1 >> 1
+        // linear; the left neighbour for -1) of the level-0 reference, strict improvements; half pels.
+        // Every sample read lies within 17 of the picture, where the border-19 copy holds the same edge
+        // replication as the reference's border-17 one.
+        constexpr int CX4[4] = {-1, 1, -1, 1}, CY4[4] = {-1, -1, 1, 1};
+        constexpr int RX[4][2] = {{0, -1}, {0, 1}, {0, -1}, {0, 1}}, RY[4][2] = {{-1, 0}, {-1, 0}, {1, 0}, {1, 0}};
+        const Org o = origin(a.e0, 16, 16, 19, n + mx, m + my);
+        auto half_part = [&](int hx, int hy) {
+            int acc = 0;
+#pragma unroll
+            for (int i = 0; i < 2; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int r = o.y + r0 + 4 * i, c = o.x + c0 + 4 * j + (hx < 0 ? -1 : 0);
+                    int v;
+                    if (hx && hy)
+                        v = (rd(a.e0, r, c, bad) + rd(a.e0, r + hy, c, bad) + rd(a.e0, r, c + 1, bad) +
+                             rd(a.e0, r + hy, c + 1, bad) + 2) >> 2;
+                    else if (hx)
+                        v = (rd(a.e0, r, c, bad) + rd(a.e0, r, c + 1, bad) + 1) >> 1;
+                    else
+                        v = (rd(a.e0, r, c, bad) + rd(a.e0, r + hy, c, bad) + 1) >> 1;
+                    const int d = cur0[4 * i + j] - v;
+                    acc += d * d;
+                }
+            return acc;
+        };
+        int hmx = 0, hmy = 0, best_corner = 0;
+        for (int k = 0; k < 4; k++) {
+            const int d = partial_value(half_part(CX4[k], CY4[k]), min_d, lane);
+            if (d < min_d) {
+                best_corner = k;
+                min_d = d;
+                hmx = CX4[k];
+                hmy = CY4[k];
+            }
+        }
+        const bool won = hmx || hmy;
+        for (int k = 0; k < (won ? 2 : 4); k++) {
+            const int hx = won ? RX[best_corner][k] : CRX[k], hy = won ? RY[best_corner][k] : CRY[k];
+            const int d = partial_value(half_part(hx, hy), min_d, lane);
+            if (d < min_d) {
+                min_d = d;
+                hmx = hx;
+                hmy = hy;
+            }
+        }
+        out.min_d = min_d;
+        out.mvx = 2 * mx + hmx;
+        out.mvy = 2 * my + hmy;
+        return out;
+    }
     int mvx = mx * 4, mvy = my * 4;
 
     // half then quarter pel in the estimator's window (…MultiresCross.cpp:875-941), strict improvements
@@ -617,12 +672,14 @@ __device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int m
 
 // MultiresCross's tie rules: at level 2 the centre against the offset
 // (…MultiresCross.cpp:673-679), elsewhere distances from (0, 0) (…:741-746, 857).
+template <bool kH263 = false>
 __device__ __forceinline__ MbSearch search_mb_mrc(const MrcArgs& a, Lattice& LT, int mbr, int mbc, int lane,
                                                   bool& bad)
 {
-    return search_mb_with<false>(a, LT, mbr, mbc, [](int lvl, int mx, int my, int rmx, int rmy, int j, int i) {
+    auto skip = [](int lvl, int mx, int my, int rmx, int rmy, int j, int i) {
         return lvl == 2 ? (my * my + mx * mx) - (i * i + j * j) < 0 : farther(mx, my, rmx, rmy, j, i, 0, 0);
-    }, lane, bad);
+    };
+    return search_mb_with<false, decltype(skip)&, kH263>(a, LT, mbr, mbc, skip, lane, bad);
 }
 
 // The prediction's vector at a pyramid level (quarter-pel component p):

@@ -332,6 +332,23 @@ public:
     }
 };
 
+// MotionEstimatorH263ImplMultiresCross: motionRange (at most 64) and the vectors in half pels.
+class GpuMotionEstimatorH263ImplMultiresCross : public GpuMotionEstimatorH264Base {
+public:
+    GpuMotionEstimatorH263ImplMultiresCross(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                            int motionRange)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_H263_MULTIRES_CROSS, pSrc, pRef, imgWidth, imgHeight, motionRange,
+                                     NULL, NULL)
+    {
+    }
+    GpuMotionEstimatorH263ImplMultiresCross(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                            int motionRange, void* pDistortionIncluded)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_H263_MULTIRES_CROSS, pSrc, pRef, imgWidth, imgHeight, motionRange,
+                                     NULL, pDistortionIncluded)
+    {
+    }
+};
+
 // MotionEstimatorH264ImplCross: quarter pel by default (SetMode 0; 1 half, 2 full pel).
 class GpuMotionEstimatorH264ImplCross : public GpuMotionEstimatorH264Base {
 public:

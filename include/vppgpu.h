@@ -62,6 +62,8 @@ int vppgpu_ctx_launch_count(vppgpu_ctx* ctx, unsigned long long* count);
 #define VPPGPU_ME_MULTIRES_CROSS    2  /* MotionEstimatorH264ImplMultiresCross     */
 #define VPPGPU_ME_MULTIRES_CROSS_V2 3  /* MotionEstimatorH264ImplMultiresCrossVer2 */
 #define VPPGPU_ME_CROSS             4  /* MotionEstimatorH264ImplCross             */
+#define VPPGPU_ME_H263_MULTIRES_CROSS 5 /* MotionEstimatorH263ImplMultiresCross:
+                                            motion range (<= 64) and vectors in half pels */
 
 typedef struct vppgpu_me vppgpu_me;
 

@@ -51,6 +51,7 @@ class Oracle:
         L.vo_me_full_detail.argtypes = [_P, _P, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L)] + [_P] * 6
         L.vo_me_full_intpel.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P]
         L.vo_me_multires_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
+        L.vo_me_h263_multires_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.vo_me_multires_cross_v2.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_me_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_me_multires.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
@@ -95,7 +96,11 @@ class Oracle:
             raise ValueError(f"vo_me_full_detail rc={rc}")
         return mv, dist, avg.value, extra
 
-    def me_multires_cross(self, src, ref, motion_range, mode=1, dist_incl=None):
+    def me_h263_multires_cross(self, src, ref, motion_range, mode=1, dist_incl=None):
+        """MotionEstimatorH263ImplMultiresCross: motion range and vectors in half pels."""
+        return self.me_multires_cross(src, ref, motion_range, mode, dist_incl, _fn=self.lib.vo_me_h263_multires_cross)
+
+    def me_multires_cross(self, src, ref, motion_range, mode=1, dist_incl=None, _fn=None):
         h, w = src.shape
         src = np.ascontiguousarray(src, dtype=np.int16)
         ref = np.ascontiguousarray(ref, dtype=np.int16)
@@ -104,8 +109,8 @@ class Oracle:
         dist = np.zeros(nmb, np.int32)
         avg = _L(0)
         incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
-        rc = self.lib.vo_me_multires_cross(_ptr(src), _ptr(ref), w, h, motion_range, mode, _ptr(incl),
-                                           _ptr(mv), _ptr(dist), C.byref(avg))
+        rc = (_fn or self.lib.vo_me_multires_cross)(_ptr(src), _ptr(ref), w, h, motion_range, mode, _ptr(incl),
+                                                    _ptr(mv), _ptr(dist), C.byref(avg))
         if rc:
             raise ValueError(f"vo_me_multires_cross rc={rc}")
         return mv, dist, avg.value
@@ -256,7 +261,8 @@ class Oracle:
 class Reference:
     """The reference's own C++ classes (only where oracle/_ref was built)."""
 
-    KIND = {"full": 0, "multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4}
+    KIND = {"full": 0, "multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4,
+            "h263_multires_cross": 5}
 
     def __init__(self, path: str = REF_SO):
         self.lib = C.CDLL(path)

@@ -256,7 +256,28 @@ typedef struct {
     mr_buf in0, in1, in2, r1, r2, e0, e1, e2;
     mr_level L0, L1, L2;
     mr_window* win;
+    int h263; /* MotionEstimatorH263ImplMultiresCross: half-pel stage by HalfRead, its accept rule */
 } mr_ctx;
+
+/* OverlayMem2Dv2::HalfRead at half-pel offset (hx, hy) in -1..1 of the
+ * block at overlay o (OverlayMem2Dv2.cpp:452-530, the unrolled branch that is
+ * compiled): bilinear means with +2 >> 2 (diagonal) or +1 >> 1 rounding; the
+ * left neighbour for hx = -1, the right one for hx = 1. */
+static void mr_half_read(const mr_ov* o, int hx, int hy, short* blk)
+{
+    for (int r = 0; r < 16; r++)
+        for (int col = 0; col < 16; col++) {
+            const int c0 = hx < 0 ? col - 1 : col;
+            int v;
+            if (hx && hy)
+                v = (ov_px(o, r, c0) + ov_px(o, r + hy, c0) + ov_px(o, r, c0 + 1) + ov_px(o, r + hy, c0 + 1) + 2) / 4;
+            else if (hx)
+                v = (ov_px(o, r, c0) + ov_px(o, r, c0 + 1) + 1) / 2;
+            else
+                v = (ov_px(o, r, col) + ov_px(o, r + hy, col) + 1) / 2;
+            blk[r * 16 + col] = (short)v;
+        }
+}
 
 static void mr_ctx_free(mr_ctx* c)
 {
@@ -272,9 +293,22 @@ static void mr_ctx_free(mr_ctx* c)
 
 /* Level copies as Estimate builds them before its macroblock loop
  * (…MultiresCross.cpp:539-601; …MultiresCrossVer2.cpp:552-611). */
+static int mr_ctx_init_h(mr_ctx* c, const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                         int h263);
 static int mr_ctx_init(mr_ctx* c, const short* src, const short* ref, int w, int h, int motion_range, int mode)
 {
+    return mr_ctx_init_h(c, src, ref, w, h, motion_range, mode, 0);
+}
+
+/* h263: MotionEstimatorH263ImplMultiresCross::Create (…H263ImplMultiresCross.cpp:160-300): the motion
+ * range is in half pels (level 0 vecRange motionRange/2, level 1 motionRange/4: the H.264 estimator's
+ * ranges at twice the value) and the level-0 reference is extended by 16 + 1 samples. */
+static int mr_ctx_init_h(mr_ctx* c, const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                         int h263)
+{
     memset(c, 0, sizeof(*c));
+    c->h263 = h263;
+    if (h263) motion_range *= 2;
     c->w = w;
     c->h = h;
     c->cols = w / 16;
@@ -305,7 +339,7 @@ static int mr_ctx_init(mr_ctx* c, const short* src, const short* ref, int w, int
         vo_half(c->r1.mem, w1, h1, c->r2.mem);
         vo_half(c->in1.mem, w1, h1, c->in2.mem);
     }
-    if (mr_buf_ext(&c->e0, ref, w, h, 19) || mr_buf_ext(&c->e1, c->r1.mem, w1, h1, 9) ||
+    if (mr_buf_ext(&c->e0, ref, w, h, h263 ? 17 : 19) || mr_buf_ext(&c->e1, c->r1.mem, w1, h1, 9) ||
         (mode == 2 && mr_buf_ext(&c->e2, c->r2.mem, w2, h2, 5)))
         return -2;
     c->L0 = (mr_level){16, w, h, motion_range / 4};
@@ -339,8 +373,9 @@ typedef struct {
 static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result* out)
 {
     const int m = 16 * mbr, n = 16 * mbc, p = 8 * mbr, q = 8 * mbc, kk = 4 * mbr, ll = 4 * mbc;
+    const int b0 = c->h263 ? 17 : 19;
     mr_ov oin0 = {&c->in0, 16, 16, 0, 0, 0, 0}, oin1 = {&c->in1, 8, 8, 0, 0, 0, 0}, oin2 = {&c->in2, 4, 4, 0, 0, 0, 0};
-    mr_ov oe0 = {&c->e0, 16, 16, 0, 0, 19, 19}, oe1 = {&c->e1, 8, 8, 0, 0, 9, 9}, oe2 = {&c->e2, 4, 4, 0, 0, 5, 5};
+    mr_ov oe0 = {&c->e0, 16, 16, 0, 0, b0, b0}, oe1 = {&c->e1, 8, 8, 0, 0, 9, 9}, oe2 = {&c->e2, 4, 4, 0, 0, 5, 5};
     int mx = 0, my = 0, rmx = 0, rmy = 0, hmx = 0, hmy = 0, qmx, qmy, xl, xr, yu, yd, tie = 0;
     short blk[256];
     ov_origin(&oin0, n, m);
@@ -450,6 +485,35 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
         }
     mx += rmx;
     my += rmy;
+    if (c->h263) {
+        /* half pel (…H263ImplMultiresCross.cpp:885-940): the best of the four diagonal corners, then the
+         * two half-pel points beside the winning corner (or the full cross if no corner won), each an
+         * OverlayMem2Dv2::HalfRead block, strict improvements; vector in half pels */
+        static const int CORNER[4][2] = {{-1, -1}, {1, -1}, {-1, 1}, {1, 1}};
+        static const int REFINED[4][2][2] = {{{0, -1}, {-1, 0}}, {{0, -1}, {1, 0}}, {{0, 1}, {-1, 0}}, {{0, 1}, {1, 0}}};
+        static const int CROSS[4][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}};
+        ov_origin(&oe0, n + mx, m + my);
+        int best_corner = 0;
+        for (int k = 0; k < 4; k++) {
+            mr_half_read(&oe0, CORNER[k][0], CORNER[k][1], blk);
+            int d = blk_tsd16_partial_lt(&oin0, blk, min_d);
+            if (d < min_d) { best_corner = k; min_d = d; hmx = CORNER[k][0]; hmy = CORNER[k][1]; }
+        }
+        const int won = hmx || hmy;
+        for (int k = 0; k < (won ? 2 : 4); k++) {
+            const int hx = won ? REFINED[best_corner][k][0] : CROSS[k][0];
+            const int hy = won ? REFINED[best_corner][k][1] : CROSS[k][1];
+            mr_half_read(&oe0, hx, hy, blk);
+            int d = blk_tsd16_partial_lt(&oin0, blk, min_d);
+            if (d < min_d) { min_d = d; hmx = hx; hmy = hy; }
+        }
+        out->zero_d = zero_d;
+        out->min_d = min_d;
+        out->mvx = 2 * mx + hmx;
+        out->mvy = 2 * my + hmy;
+        out->tie = tie;
+        return;
+    }
     int mvx = mx << 2, mvy = my << 2;
 
     /* half then quarter pel (…MultiresCross.cpp:875-941), strict improvements */
@@ -477,13 +541,33 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
     out->tie = tie;
 }
 
+static int me_multires_cross_any(int h263, const short* src, const short* ref, int w, int h, int motion_range,
+                                 int mode, const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist);
+
 int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
                          const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist)
+{
+    return me_multires_cross_any(0, src, ref, w, h, motion_range, mode, dist_incl, mv_out, mb_dist, avg_dist);
+}
+
+/* MotionEstimatorH263ImplMultiresCross::Estimate
+ * (src/CodecUtils/MotionEstimatorH263ImplMultiresCross.cpp:531-1010): the
+ * H.264 estimator's levels and level-0 refinement at its doubled range, the
+ * HalfRead half-pel stage, vectors in half pels and the accept rule with
+ * (zero - min) >> 2 against |v|^2. */
+int vo_me_h263_multires_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                              const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist)
+{
+    return me_multires_cross_any(1, src, ref, w, h, motion_range, mode, dist_incl, mv_out, mb_dist, avg_dist);
+}
+
+static int me_multires_cross_any(int h263, const short* src, const short* ref, int w, int h, int motion_range,
+                                 int mode, const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist)
 {
     if (!src || !ref || !mv_out || w < 16 || h < 16 || (w % 16) != 0) return -1;
     g_mr_fault = 0;
     mr_ctx c;
-    int rc = mr_ctx_init(&c, src, ref, w, h, motion_range, mode);
+    int rc = mr_ctx_init_h(&c, src, ref, w, h, motion_range, mode, h263);
     if (rc == 0) {
         long total = 0;
         int included = 0;
@@ -495,7 +579,7 @@ int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int m
                 int mvx = r.mvx, mvy = r.mvy;
                 /* accept-or-zero heuristic (…MultiresCross.cpp:943-999) */
                 int weight = 0, diff0 = r.zero_d - r.min_d, mag = mvx * mvx + mvy * mvy;
-                if (diff0 < mag) weight++;
+                if (h263 ? (diff0 >> 2) < mag : diff0 < mag) weight++;
                 if (r.zero_d < MRC_NOISE_FLOOR) weight++;
                 if (diff0 * 10 < r.min_d) weight++;
                 int do_it = dist_incl ? (vec_pos < c.nmb ? dist_incl[vec_pos] != 0 : 0) : 1;

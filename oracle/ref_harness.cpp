@@ -19,6 +19,7 @@
 #include "MotionEstimatorH264ImplMultiresCross.h"
 #include "MotionEstimatorH264ImplMultiresCrossVer2.h"
 #include "MotionEstimatorH264ImplCross.h"
+#include "MotionEstimatorH263ImplMultiresCross.h"
 #include "VectorStructList.h"
 #include "MotionCompensatorH264ImplStd.h"
 #include "FastForward4x4ITImpl1.h"
@@ -116,6 +117,7 @@ int ref_me_estimate(int kind, const short* src, const short* ref, int w, int h, 
     case 2: me = new MotionEstimatorH264ImplMultiresCross(src, ref, w, h, motion_range, flags); break;
     case 3: me = new MotionEstimatorH264ImplMultiresCrossVer2(src, ref, w, h, motion_range, &pred, flags); break;
     case 4: me = new MotionEstimatorH264ImplCross(src, ref, w, h, motion_range, &pred, flags); break;
+    case 5: me = new MotionEstimatorH263ImplMultiresCross(src, ref, w, h, motion_range, flags); break;
     default: mallopt(M_PERTURB, 0); delete[] flags; return -1;
     }
     int created = me->Create();

@@ -85,6 +85,12 @@ int vo_me_full_intpel(const short* src, const short* ref, int w, int h, int moti
 int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
                          const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist);
 
+/* MotionEstimatorH263ImplMultiresCross::Estimate
+ * (src/CodecUtils/MotionEstimatorH263ImplMultiresCross.cpp:531-1010): motion
+ * range and vectors in half pels, HalfRead half-pel stage. */
+int vo_me_h263_multires_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                              const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist);
+
 /* MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*)
  * (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:537-1151): the
  * MultiresCross search with ties towards the rounded median prediction of

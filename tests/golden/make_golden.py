@@ -87,9 +87,14 @@ MRC_CASES = [  # (name, w, h, motion_range, seed)
 ]
 
 
-def mrc_fixtures(ref: oracle.Reference) -> dict:
+# MotionEstimatorH263ImplMultiresCross: motion ranges in half pels
+H263_CASES = [("qcif_r32", 176, 144, 32, 25), ("cif_r64", 352, 288, 64, 26), ("partial_r64", 352, 280, 64, 27),
+              ("small_r16", 64, 48, 16, 28)]
+
+
+def mrc_fixtures(ref: oracle.Reference, kind: str = "multires_cross", cases=None) -> dict:
     out = {}
-    for name, w, h, mr, seed in MRC_CASES:
+    for name, w, h, mr, seed in (MRC_CASES if cases is None else cases):
         fr = synth.pan_sequence(seed, w, h, 2)
         src, rf = fr[1], fr[0]
         nmb = (w // 16) * (h // 16)
@@ -97,8 +102,8 @@ def mrc_fixtures(ref: oracle.Reference) -> dict:
         out[f"{name}_ref"] = rf.astype(np.uint8)
         out[f"{name}_meta"] = np.array([w, h, mr], np.int32)
         for mode in (0, 1, 2):
-            mv, avg = ref.me("multires_cross", src, rf, mr, mode=mode)
-            mvi, avgi = ref.me("multires_cross", src, rf, mr, mode=mode, dist_incl=np.ones(nmb, np.uint8))
+            mv, avg = ref.me(kind, src, rf, mr, mode=mode)
+            mvi, avgi = ref.me(kind, src, rf, mr, mode=mode, dist_incl=np.ones(nmb, np.uint8))
             assert np.array_equal(mv, mvi)
             out[f"{name}_m{mode}_mv"] = mv
             out[f"{name}_m{mode}_avg"] = np.array([avg, avgi], np.int64)
@@ -260,6 +265,7 @@ def main() -> None:
     ref = oracle.Reference()
     makers = {"me_full": me_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "me_cross": lambda r: mrc2_fixtures(r, "cross"),
+              "me_h263mrc": lambda r: mrc_fixtures(r, "h263_multires_cross", H263_CASES),
               "mc": mc_fixtures,
               "transform": transform_fixtures, "dc": dc_fixtures, "yuv2rgb": yuv2rgb_fixtures,
               "colour": colour_fixtures}

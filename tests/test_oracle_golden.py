@@ -169,6 +169,26 @@ def test_me_multires_cross_matches_reference(orc, golden, case, mode):
     assert avgi == int(g[f"{case}_m{mode}_avg"][1])
 
 
+H263_CASES = ["qcif_r32", "cif_r64", "partial_r64", "small_r16"]
+
+
+@pytest.mark.parametrize("case", H263_CASES)
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_me_h263_multires_cross_matches_reference(orc, golden, case, mode):
+    """MotionEstimatorH263ImplMultiresCross (half-pel ranges and vectors)."""
+    g = golden("me_h263mrc.npz")
+    w, h, mr = (int(v) for v in g[f"{case}_meta"])
+    src = g[f"{case}_src"].astype(np.int16)
+    ref = g[f"{case}_ref"].astype(np.int16)
+    mv, _, avg = orc.me_h263_multires_cross(src, ref, mr, mode=mode)
+    np.testing.assert_array_equal(mv, g[f"{case}_m{mode}_mv"])
+    assert avg == int(g[f"{case}_m{mode}_avg"][0])
+    mvi, _, avgi = orc.me_h263_multires_cross(src, ref, mr, mode=mode,
+                                               dist_incl=np.ones((w // 16) * (h // 16), np.uint8))
+    np.testing.assert_array_equal(mvi, mv)
+    assert avgi == int(g[f"{case}_m{mode}_avg"][1])
+
+
 MRC2_CASES = ["qcif_r64", "cif_r128", "partial_r128", "small_r32", "shift_r128"]
 
 
