@@ -358,9 +358,10 @@ MULTIRES = {  # kind -> (class name, oracle method)
     "multires_cross_v2": ("MotionEstimatorH264ImplMultiresCrossVer2", "me_multires_cross_v2"),
     "cross": ("MotionEstimatorH264ImplCross", "me_cross"),
     "h263_multires_cross": ("MotionEstimatorH263ImplMultiresCross", "me_h263_multires_cross"),
+    "full_sad": ("MotionEstimatorH264ImplFullSad", "me_full_intpel"),
 }
 MULTIRES_CODE = {"multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4,
-                 "h263_multires_cross": 5}  # VPPGPU_ME_*
+                 "h263_multires_cross": 5, "full_sad": 6}  # VPPGPU_ME_*
 # motion ranges are in quarter pels, the H.263 estimator's in half pels: the same +-32 pels
 MULTIRES_RANGE = {"h263_multires_cross": MOTION_RANGE // 2}
 
@@ -417,7 +418,7 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
     ms = e0.elapsed_time(e1) / steps
     out = {"value": NMB / (ms * 1e-3), "unit": UNIT, "ms_per_frame": ms, "mode": mode.value, "autotune": tuning,
            "workload": f"{cls} plain per-frame, {W}x{H}, motionRange {mr}"}
-    if kind not in ("multires_cross", "h263_multires_cross"):
+    if kind not in ("multires_cross", "h263_multires_cross", "full_sad"):
         # per-frame device time and how each frame's predictions were decided
         per, exact = [], 0
         for t in range(NFRAMES - 1):
@@ -439,14 +440,18 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
         from concurrent.futures import ThreadPoolExecutor
         from oracle.oracle import Oracle
         orc = Oracle()
-        mv_o = getattr(orc, ofn)(frames[1], frames[0], mr, mode=mode.value)[0]
+        def port(i):
+            if kind == "full_sad":
+                return orc.me_full_intpel(frames[i + 1], frames[i], mr, metric=1)
+            return getattr(orc, ofn)(frames[i + 1], frames[i], mr, mode=mode.value)
+
+        mv_o = port(0)[0]
         out["parity_first_frame"] = bool(np.array_equal(d_mv.cpu().numpy(), mv_o))
         nth = os.cpu_count() or 1
         npairs, t0 = 0, time.perf_counter()
         with ThreadPoolExecutor(nth) as ex:  # ctypes calls release the GIL: one estimate per thread
             while time.perf_counter() - t0 < args.cpu_seconds:
-                list(ex.map(lambda i: getattr(orc, ofn)(frames[i + 1], frames[i], mr, mode=mode.value),
-                            range(NFRAMES - 1)))
+                list(ex.map(port, range(NFRAMES - 1)))
                 npairs += NFRAMES - 1
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": npairs * NMB / dt, "unit": UNIT, "cores": nth, "kind": "port",
@@ -800,6 +805,8 @@ def main():
                                 kind="cross")
         h263 = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
                                   kind="h263_multires_cross")
+        sad = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
+                                 kind="full_sad")
         pk, pk_kind = peaks()
         hbm_rows = run_hbm_paths(torch, _lib, L, ctx, stream, f"cuda:{local}", pk)
         line = {
@@ -825,7 +832,7 @@ def main():
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
             "serving": serving,
             "multires": mr, "multires_cross": mrc, "multires_cross_v2": mrc2, "cross": cr,
-            "h263_multires_cross": h263, **hbm_rows,
+            "h263_multires_cross": h263, "full_sad": sad, **hbm_rows,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

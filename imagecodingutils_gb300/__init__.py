@@ -28,7 +28,7 @@ from ._lib import VppGpuError, check, load
 
 __all__ = [
     "Context", "get_context", "MotionEstimatorH264ImplFull", "MotionEstimatorH264ImplMultires",
-    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross",
+    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross", "MotionEstimatorH264ImplFullSad",
     "MotionEstimatorH263ImplMultiresCross", "MotionEstimatorBatch",
     "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
     "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1", "FastForwardDC4x4ITImpl1",
@@ -212,6 +212,16 @@ class MotionEstimatorH264ImplCross(_MotionEstimatorBase):
 
     KIND = _lib.ME_CROSS
     DEFAULT_MODE = 0
+
+
+class MotionEstimatorH264ImplFullSad(_MotionEstimatorBase):
+    """GPU integer-pel stage of MotionEstimatorH264ImplFull with the
+    MEH264IF_ABS_DIFF distortion (src/CodecUtils/MotionEstimatorH264ImplFull.cpp:341-446,
+    OverlayMem2Dv2::Tad16x16 / Tad16x16LessThan): full search of the range by SAD,
+    ties towards the rounded median prediction, vectors the full-pel winners in
+    quarter pels, distortions their SAD, no sub-pel stage or GetBestVector."""
+
+    KIND = _lib.ME_FULL_SAD
 
 
 class MotionEstimatorH264ImplMultiresCross(_MotionEstimatorBase):

@@ -142,7 +142,7 @@ int dalloc(T** p, size_t count)
 
 vppgpu::FullArgs full_args(vppgpu_me* me, double lambda)
 {
-    vppgpu::FullArgs a;
+    vppgpu::FullArgs a{};
     a.W = me->W;
     a.H = me->H;
     a.cols = me->cols;
@@ -205,6 +205,12 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
         return vppgpu::mrc2_launch(ctx, v2 ? 1 : 2, me->mode, me->d_mrc, full_args(me, v2 ? 0.9 : 1.1), d_src16,
                                    d_ref16);
     }
+    if (me->kind == VPPGPU_ME_FULL_SAD) {
+        // the integer-pel stage only: no sub-pel, no prediction check, no GetBestVector
+        vppgpu::FullArgs a = full_args(me, 0.0);
+        a.intpel = 1;
+        return vppgpu::sad_launch(ctx, a, me->nmb);
+    }
     const vppgpu::FullArgs a = full_args(me, lambda);
     cudaEvent_t* ev = ring_slot(me);
     if (!ev && me->graph_state == 0) {
@@ -265,7 +271,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
     if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
     if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
-    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_H263_MULTIRES_CROSS) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_FULL_SAD) return VPPGPU_ERR_UNSUPPORTED;
     // MotionEstimatorH263ImplMultiresCross's range is in half pels: at most 64 (+-31 pels), as 128 quarter pels
     if (kind == VPPGPU_ME_H263_MULTIRES_CROSS && motion_range > 64) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
@@ -556,7 +562,8 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
 {
     if (!me || sweeps < 0 || sweeps > vppgpu::RELAX_SWEEPS) return VPPGPU_ERR_INVALID_ARG;
-    if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS)
+    if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS ||
+        me->kind == VPPGPU_ME_FULL_SAD)
         return VPPGPU_ERR_UNSUPPORTED;
     if (sweeps == me->relax_sweeps) return VPPGPU_OK;
     int rc = vppgpu::bind(me->ctx);
@@ -606,6 +613,10 @@ extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src
     if (!me || !d_src || !d_ref || npairs < 1 || reps < 1) return VPPGPU_ERR_INVALID_ARG;
     for (int p = 0; p < npairs; p++)
         if (!d_src[p] || !d_ref[p]) return VPPGPU_ERR_INVALID_ARG;
+    if (me->kind == VPPGPU_ME_FULL_SAD) {  // one configuration: nothing to tune
+        if (chosen) *chosen = 0;
+        return VPPGPU_OK;
+    }
     int rc = vppgpu::bind(me->ctx);
     if (rc) return rc;
     cudaStream_t st = me->ctx->stream;
@@ -803,7 +814,7 @@ int vppgpu_me_batch_create(vppgpu_ctx* ctx, int kind, int streams, vppgpu_me_bat
 {
     if (!ctx || !out || streams < 1) return VPPGPU_ERR_INVALID_ARG;
     *out = nullptr;
-    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_H263_MULTIRES_CROSS) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_FULL_SAD) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me_batch* b = (vppgpu_me_batch*)calloc(1, sizeof(vppgpu_me_batch));

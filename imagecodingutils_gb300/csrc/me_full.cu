@@ -147,9 +147,13 @@ __global__ void __launch_bounds__(256) k_full_halfpel(const unsigned char* __res
 }
 
 // ---------------------------------------------------------------------------
-// Table stage, one CTA per macroblock, every warp busy: the SSD of all
+// Table stage, one CTA per macroblock, every warp busy: the SSD (kSad: the
+// SAD, OverlayMem2Dv2::Tad16x16, OverlayMem2Dv2.cpp:2655-2730) of all
 // (2R+1)^2 full-pel candidates, its row minima, to the MB's global table.
-__global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
+// The SAD has no energy decomposition: each word pair is one byte-wise
+// absolute difference summed by a dp4a against ones.
+template <bool kSad>
+__global__ void __launch_bounds__(128, kSad ? 4 : 5) k_full_table(FullArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TableSmem& S = *reinterpret_cast<TableSmem*>(smem_raw);
@@ -172,7 +176,7 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
     __syncthreads();
 
     // 2. template energy
-    if (tid < 32) {
+    if (!kSad && tid < 32) {
         int acc = 0;
 #pragma unroll
         for (int t = 0; t < 8; t++) {
@@ -217,7 +221,7 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
 #pragma unroll
         for (int r = 0; r < 8; r++) {
             load_row(al[r], ii0 + r);
-            row_energy(al[r], ii0 + r);
+            if (!kSad) row_energy(al[r], ii0 + r);
         }
 #pragma unroll
         for (int r = 0; r < 8; r++)
@@ -234,7 +238,8 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
                 for (int q = 0; q < 4; q++) {
                     unsigned c = acc[r][q];
 #pragma unroll
-                    for (int w = 0; w < 4; w++) c = __dp4a(A[w], B[q + w], c);
+                    for (int w = 0; w < 4; w++)
+                        c = kSad ? __dp4a(__vabsdiffu4(A[w], B[q + w]), 0x01010101u, c) : __dp4a(A[w], B[q + w], c);
                     acc[r][q] = c;
                 }
             }
@@ -242,7 +247,7 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
         }
     }
     // energies of window rows 64..77 (below every row group's own rows): 14 rows x 16 slices
-    for (int task = tid; task < (WROWS - 64) * 16; task += 128) {
+    for (int task = kSad ? (WROWS - 64) * 16 : tid; task < (WROWS - 64) * 16; task += 128) {
         const int r = 64 + (task >> 4), c = task & 15, ts = c & 3, tq = c >> 2;
         const uint4* p = reinterpret_cast<const uint4*>(&S.win[r][16 * tq]);
         const uint4 x0 = p[0], x1 = p[1];
@@ -264,7 +269,7 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
 
     // 4. vertical 16-row sums of the horizontal energies (task: column jj, run ib), then
     //    SSD = A^2 + B^2 - 2 sum(ab) for every candidate
-    for (int task = tid; task < TAB * 4; task += 128) {
+    for (int task = kSad ? TAB * 4 : tid; task < TAB * 4; task += 128) {
         const int jj = task & (TAB - 1), ib = task >> 6;
         const int* col = S.h2t[jj];
         const int r0 = 16 * ib, r1 = min(r0 + 16, 2 * RMAX + 1);
@@ -279,7 +284,7 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
     }
     __syncthreads();
     {
-        const int a2 = S.a2;
+        const int a2 = kSad ? 0 : S.a2;
 #pragma unroll
         for (int r = 0; r < 8; r++) {
             int ii = ii0 + r;
@@ -287,7 +292,7 @@ __global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     int jj = 4 * (4 * qg + q) + s;
-                    S.tab[ii][jj] = a2 + S.tab[ii][jj] - 2 * (int)acc[r][q];
+                    S.tab[ii][jj] = kSad ? (int)acc[r][q] : a2 + S.tab[ii][jj] - 2 * (int)acc[r][q];
                 }
             }
         }
@@ -320,8 +325,8 @@ __global__ void __launch_bounds__(256, 4) k_full_refine(FullArgs a)
     full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
     scan_table(GlobalTab{gt}, xl, xr, yu, yd, 0, 0, lane, &mx, &my, &minD, &tie);
     const int zero_d = __ldcg(gt + RMAX * TAB + RMAX + 1);
-    int qmx, qmy;
-    subpel_refine_planes(a, n + mx, m + my, cur, lane, &minD, &qmx, &qmy);
+    int qmx = 0, qmy = 0;
+    if (!a.intpel) subpel_refine_planes(a, n + mx, m + my, cur, lane, &minD, &qmx, &qmy);
     if (lane == 0) {
         const int qmv = pack_mv(4 * mx + qmx, 4 * my + qmy);
         const int av = neighbour_mask(a.job->slice, k, a.cols, a.nmb / a.cols);
@@ -359,8 +364,8 @@ __global__ void __launch_bounds__(TIE_RUNS * 32) k_full_tietree(FullArgs a)
         scan_table_t<true>(SmemTab{S.tab}, xl, xr, yu, yd, 0, 0, p, lane, &rmx, &rmy, &rmin, &rt, &nev, ev);
         int rq = sp.x, rqmin = sp.y;
         if (rmx != mv_x(imv) || rmy != mv_y(imv)) {
-            int sx, sy;
-            subpel_refine_planes(a, n + rmx, m + rmy, load_cur8(a, n, m, lane), lane, &rmin, &sx, &sy);
+            int sx = 0, sy = 0;
+            if (!a.intpel) subpel_refine_planes(a, n + rmx, m + rmy, load_cur8(a, n, m, lane), lane, &rmin, &sx, &sy);
             rq = pack_mv(4 * rmx + sx, 4 * rmy + sy);
             rqmin = rmin;
         }
@@ -433,7 +438,7 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid
     int rc = full_planes_launch(ctx, args);
     if (rc) return rc;
     if (ev) VPP_CUDA(cudaEventRecord(ev[1], ctx->stream));
-    k_full_table<<<nmb, 128, sizeof(TableSmem), ctx->stream>>>(args);
+    k_full_table<false><<<nmb, 128, sizeof(TableSmem), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     if (ev) VPP_CUDA(cudaEventRecord(ev[2], ctx->stream));
     k_full_refine<<<(nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
@@ -447,9 +452,26 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid
     return VPPGPU_OK;
 }
 
+// The integer-pel SAD stage (FullArgs::intpel): planes, the SAD table, the
+// scan at prediction (0, 0) without sub-pel, tie trees, then the tie wavefront.
+int sad_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb)
+{
+    int rc = full_planes_launch(ctx, args);
+    if (rc) return rc;
+    k_full_table<true><<<nmb, 128, sizeof(TableSmem), ctx->stream>>>(args);
+    VPP_CHECK_LAUNCH(ctx);
+    k_full_refine<<<(nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
+    VPP_CHECK_LAUNCH(ctx);
+    k_full_tietree<<<ctx->sm_count, TIE_RUNS * 32, sizeof(TieSmem), ctx->stream>>>(args);
+    VPP_CHECK_LAUNCH(ctx);
+    return sad_resolve_launch(ctx, args);
+}
+
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid)
 {
-    VPP_CUDA(cudaFuncSetAttribute(k_full_table, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    VPP_CUDA(cudaFuncSetAttribute(k_full_table<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(TableSmem)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_table<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(TableSmem)));
     VPP_CUDA(cudaFuncSetAttribute(k_full_tietree, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(TieSmem)));

@@ -87,6 +87,12 @@ __device__ __noinline__ void tie_path(const FullArgs& a, int k, int px, int py, 
     scan_table(GlobalTab{tab}, xl, xr, yu, yd, prx, pry, lane, &mx, &my, &md, &tie);
     int imv = a.spec_imv[k];
     if (mx != mv_x(imv) || my != mv_y(imv)) {
+        if (a.intpel) {  // the integer-pel stage ends at the full-pel winner
+            *mvx = 4 * mx;
+            *mvy = 4 * my;
+            *minD = md;
+            return;
+        }
         int qmx, qmy;
         subpel_refine_planes(a, n + mx, m + my, load_cur8(a, n, m, lane), lane, &md, &qmx, &qmy);
         *mvx = 4 * mx + qmx;
@@ -1033,6 +1039,73 @@ __global__ void k_full_average(FullArgs a)
     if (a.job->out_avg) *a.job->out_avg = c ? t / c : 0;
 }
 
+// The integer-pel SAD stage's tail.  The prediction enters only the exact-tie
+// decisions of the scan (MotionEstimatorH264ImplFull.cpp:424-441), so every
+// macroblock without a tie already holds its final vector.  One CTA walks the
+// anti-diagonals t = c + 2r: the median prediction of (r, c) reads (r, c-1),
+// (r-1, c-1), (r-1, c) and (r-1, c+1), all on earlier diagonals, so a
+// diagonal's tie macroblocks settle together (warp each: tie tree walk, or a
+// rescan of the kept table), with a block barrier between diagonals.  Then the
+// outputs and the included-distortion average (Full.cpp:581-607).
+__global__ void __launch_bounds__(1024, 1) k_sad_resolve(FullArgs a)
+{
+    __shared__ long long s_tot;
+    __shared__ int s_cnt;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int cols = a.cols, rows = a.nmb / cols;
+    if (threadIdx.x == 0) {
+        s_tot = 0;
+        s_cnt = 0;
+    }
+    if (*((volatile int*)&a.ctrl->ntie) > 0) {
+        for (int t = 0; t <= cols - 1 + 2 * (rows - 1); t++) {
+            const int r_lo = max(0, (t - cols + 2) / 2), r_hi = min(rows - 1, t / 2);
+            for (int r = r_lo + wib; r <= r_hi; r += nw) {
+                const int k = r * cols + (t - 2 * r);
+                const int4 sp = __ldcg(a.spec4 + k);
+                if (!(sp.w & FLAG_TIE)) continue;
+                int px, py;
+                median_pred(a.final_mv, sp.w, k, cols, &px, &py);
+                int mvx = mv_x(sp.x), mvy = mv_y(sp.x), md = sp.y;
+                tie_path(a, k, px, py, sp.w, lane, &mvx, &mvy, &md);
+                if (lane == 0) {
+                    __stcg(a.final_mv + k, pack_mv(mvx, mvy));
+                    __stcg(a.final_dist + k, md);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    long long tot = 0;
+    int cnt = 0;
+    for (int k = threadIdx.x; k < a.nmb; k += blockDim.x) {
+        const int4 sp = __ldcg(a.spec4 + k);
+        const int fmv = (sp.w & FLAG_TIE) ? __ldcg(a.final_mv + k) : sp.x;
+        const int d = (sp.w & FLAG_TIE) ? __ldcg(a.final_dist + k) : sp.y;
+        a.job->out_mv[k] = fmv;
+        if (a.job->out_dist) a.job->out_dist[k] = d;
+        if (a.job->incl && a.job->incl[k]) {
+            tot += d;
+            cnt++;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    if (lane == 0 && cnt) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&s_tot), (unsigned long long)tot);
+        atomicAdd(&s_cnt, cnt);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // the host reads the sums, device callers the average
+        a.ctrl->total = s_tot;
+        a.ctrl->count = s_cnt;
+        if (a.job->out_avg) *a.job->out_avg = s_cnt ? s_tot / s_cnt : 0;
+    }
+}
+
 // Motion-compensated luma residual (MotionCompensatorH264ImplStd::Compensate,
 // MotionCompensatorH264ImplStd.cpp:413-431: QuarterRead of the reference at
 // the vector, a copy for full-pel vectors; then OverlayMem2Dv2::Sub16x16):
@@ -1171,6 +1244,13 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid,
     case cross::EST_CROSS: return resolve_launch<cross::EST_CROSS>(ctx, args);
     default: return VPPGPU_ERR_INVALID_ARG;
     }
+}
+
+int sad_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args)
+{
+    k_sad_resolve<<<1, 1024, 0, ctx->stream>>>(args);
+    VPP_CHECK_LAUNCH(ctx);
+    return VPPGPU_OK;
 }
 
 int full_residual_launch(vppgpu_ctx* ctx, const FullArgs& args, const int* d_mv, short* d_res)

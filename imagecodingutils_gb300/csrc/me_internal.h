@@ -99,6 +99,7 @@ struct FullArgs {
     int4* search_cache;  // V2_SEARCH_CACHE per MB: {rounded prediction, vector, distortion, tie levels or -1}
     void* tie_runs;      // 8 tie-tree runs (mrc::V2TieRun, 32 bytes) per MB
     int mode;            // Cross: 0 quarter, 1 half, 2 full pel
+    int intpel;          // 1: the integer-pel SAD stage (no sub-pel, no prediction check)
 };
 constexpr int V2_SEARCH_CACHE = 4;
 
@@ -157,5 +158,10 @@ int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid);
 // ev: nullptr, or 5 events recorded before the pack kernel, before the
 // table kernel, before the refine kernel, before the resolve and after it.
 int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid, cudaEvent_t* ev);
+// Integer-pel SAD full search: the MotionEstimatorH264ImplFull integer stage
+// (MotionEstimatorH264ImplFull.cpp:341-446) with the MEH264IF_ABS_DIFF distortion.
+int sad_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb);
+// Its prediction-dependent tail: the tie macroblocks in wavefront order, then the outputs.
+int sad_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args);
 
 }  // namespace vppgpu

@@ -151,7 +151,7 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     ctx.stream = (cudaStream_t)cuda_stream;
 
     unsigned char* base = s->scratch;
-    vppgpu::FullArgs a;
+    vppgpu::FullArgs a{};
     a.W = width;
     a.H = height;
     a.cols = cols;

@@ -5,7 +5,7 @@
 // pair.bin holds the source then the reference luma plane (int16).  The
 // program estimates with GpuMotionEstimatorH264ImplFull (or, by the optional
 // last argument, ...Multires, ...MultiresCross, ...MultiresCrossVer2 or
-// ...Cross: "multires", "mrc", "mrc2", "cross") exactly as a codec would with the vpp class
+// ...Cross: "multires", "mrc", "mrc2", "cross", "sad") exactly as a codec would with the vpp class
 // (constructor, Create, SetMode(0), Estimate, predictor side effect), then
 // runs the forward/inverse 4x4 transform classes
 // on the motion-compensated-free residual (source - reference) of the first
@@ -58,6 +58,8 @@ int main(int argc, char** argv)
         me = new GpuMotionEstimatorH264ImplMultiresCrossVer2(src.data(), ref.data(), w, h, range, &pred, incl);
     else if (kind == "cross")
         me = new GpuMotionEstimatorH264ImplCross(src.data(), ref.data(), w, h, range, &pred, incl);
+    else if (kind == "sad")
+        me = new GpuMotionEstimatorH264ImplFullSad(src.data(), ref.data(), w, h, range, &pred, incl);
     else
         me = new GpuMotionEstimatorH264ImplFull(src.data(), ref.data(), w, h, range, &pred, incl);
     if (!me->Create()) {

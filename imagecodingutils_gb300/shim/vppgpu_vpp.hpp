@@ -349,6 +349,24 @@ public:
     }
 };
 
+// The integer-pel stage of MotionEstimatorH264ImplFull with its MEH264IF_ABS_DIFF
+// distortion (MotionEstimatorH264ImplFull.cpp:341-446, OverlayMem2Dv2::Tad16x16 /
+// Tad16x16LessThan): full-pel winners in quarter pels, their SAD as distortion.
+class GpuMotionEstimatorH264ImplFullSad : public GpuMotionEstimatorH264Base {
+public:
+    GpuMotionEstimatorH264ImplFullSad(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                      int motionRange, IMotionVectorPredictor* pMVPred)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_FULL_SAD, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred, NULL)
+    {
+    }
+    GpuMotionEstimatorH264ImplFullSad(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                      int motionRange, IMotionVectorPredictor* pMVPred, void* pDistortionIncluded)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_FULL_SAD, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred,
+                                     pDistortionIncluded)
+    {
+    }
+};
+
 // MotionEstimatorH264ImplCross: quarter pel by default (SetMode 0; 1 half, 2 full pel).
 class GpuMotionEstimatorH264ImplCross : public GpuMotionEstimatorH264Base {
 public:

@@ -161,6 +161,21 @@ def shift_sequence(seed: int, w: int, h: int, nframes: int, max_global: int = 8,
     return frames
 
 
+def tile_sequence(seed: int, w: int, h: int, nframes: int, period: int = 4, max_global: int = 8) -> list[np.ndarray]:
+    """A random period x period tile repeated over the frame, each next frame
+    the previous one rolled by a seeded integer shift: every candidate a whole
+    number of periods from the match has the same distortion, so the scans
+    meet exact ties everywhere and the prediction decides them."""
+    tile = (splitmix64(seed, period * period, stream=23) % np.uint64(256)).astype(np.int16).reshape(period, period)
+    cur = np.tile(tile, ((h + period - 1) // period, (w + period - 1) // period))[:h, :w]
+    frames = [cur.copy()]
+    for t in range(1, nframes):
+        g = (splitmix64(seed + t, 2, stream=24) % np.uint64(2 * max_global + 1)).astype(np.int64) - max_global
+        cur = np.roll(cur, (int(g[0]), int(g[1])), axis=(0, 1))
+        frames.append(cur.copy())
+    return frames
+
+
 def residual_blocks(seed: int, n: int, scale: float = 6.0) -> np.ndarray:
     """n int16 values, Laplacian(0, scale) rounded half away from zero, clipped to +-255."""
     u = _unit(seed, n, 31) - 0.5

@@ -64,6 +64,14 @@ int vppgpu_ctx_launch_count(vppgpu_ctx* ctx, unsigned long long* count);
 #define VPPGPU_ME_CROSS             4  /* MotionEstimatorH264ImplCross             */
 #define VPPGPU_ME_H263_MULTIRES_CROSS 5 /* MotionEstimatorH263ImplMultiresCross:
                                             motion range (<= 64) and vectors in half pels */
+/* The integer-pel stage of MotionEstimatorH264ImplFull::Estimate
+ * (src/CodecUtils/MotionEstimatorH264ImplFull.cpp:341-446) with its
+ * MEH264IF_ABS_DIFF distortion: OverlayMem2Dv2::Tad16x16 for the zero vector and
+ * Tad16x16LessThan for the scan (src/ImageUtils/OverlayMem2Dv2.cpp:2655-2960).
+ * Vectors are the full-pel winners in quarter pels, distortions their SAD; no
+ * sub-pel stage, prediction check or GetBestVector.  The median prediction
+ * still decides exact ties, so the estimator keeps the predictor contract. */
+#define VPPGPU_ME_FULL_SAD          6
 
 typedef struct vppgpu_me vppgpu_me;
 

@@ -268,6 +268,7 @@ class Reference:
         self.lib = C.CDLL(path)
         L = self.lib
         L.ref_me_estimate.argtypes = [_I, _P, _P, _I, _I, _I, _I, _P, _P, _I, _P, C.POINTER(_L)]
+        L.ref_me_full_sad.argtypes = [_P, _P, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.ref_fwd_transform.argtypes = [_I, _P, _I, _I, _I, _I]
         L.ref_inv_transform.argtypes = [_I, _P, _I, _I, _I, _P]
         L.ref_quantise_value.argtypes = [C.c_short, _I, _I, _I]
@@ -296,6 +297,24 @@ class Reference:
         if rc:
             raise ValueError(f"ref_me_estimate rc={rc}")
         return mv, avg.value
+
+    def me_full_sad(self, src, ref, motion_range, dist_incl=None):
+        """The integer-pel SAD stage of MotionEstimatorH264ImplFull on the
+        reference's own overlays (ref_harness.cpp FullSadStage): vectors, SADs
+        and the included-distortion average."""
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = (w // 16) * (h // 16)
+        mv = np.zeros((nmb, 2), np.int16)
+        dist = np.zeros(nmb, np.int32)
+        avg = _L(0)
+        incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
+        rc = self.lib.ref_me_full_sad(_ptr(src), _ptr(ref), w, h, motion_range, _ptr(incl), _ptr(mv), _ptr(dist),
+                                      C.byref(avg))
+        if rc:
+            raise ValueError(f"ref_me_full_sad rc={rc}")
+        return mv, dist, avg.value
 
     def mc_compensate(self, y, u, v, mv, range_):
         h, w = y.shape

@@ -90,9 +90,86 @@ void copy_vectors(VectorStructList* l, int nmb, short* out) {
     }
 }
 
+/* The integer-pel stage of MotionEstimatorH264ImplFull::Estimate
+ * (MotionEstimatorH264ImplFull.cpp:341-446) with its MEH264IF_ABS_DIFF
+ * distortion.  The switch is #undef'd inside the .cpp, so the loop is stated
+ * here, on the reference's own members: the extended reference overlay filled
+ * as Estimate fills it, OverlayMem2Dv2::Tad16x16 / Tad16x16LessThan,
+ * GetMotionRange and the predictor.  The chosen full-pel vector (in quarter
+ * pels) goes to the predictor as Estimate's final vector does (:593-600). */
+class FullSadStage : public MotionEstimatorH264ImplFull {
+public:
+    using MotionEstimatorH264ImplFull::MotionEstimatorH264ImplFull;
+    void run(int nmb, const bool* incl, short* mv_out, int* dist_out, long* avg_out) {
+        _pExtRefOver->SetOrigin(0, 0);
+        _pExtRefOver->SetOverlayDim(_imgWidth, _imgHeight);
+        _pExtRefOver->Write(*_pRefOver);
+        _pExtRefOver->FillBoundaryProxy();
+        _pExtRefOver->SetOverlayDim(_macroBlkWidth, _macroBlkHeight);
+        int vecPos = 0, included = 0;
+        long total = 0;
+        for (int m = 0; m < _imgHeight; m += _macroBlkHeight)
+            for (int n = 0; n < _imgWidth; n += _macroBlkWidth) {
+                int predX, predY;
+                _pMVPred->Get16x16Prediction(NULL, vecPos, &predX, &predY);
+                const int prx = predX < 0 ? (predX - 2) / 4 : (predX + 2) / 4;
+                const int pry = predY < 0 ? (predY - 2) / 4 : (predY + 2) / 4;
+                _pInOver->SetOrigin(n, m);
+                _pExtRefOver->SetOrigin(n, m);
+                int minDiff = _pInOver->Tad16x16(*_pExtRefOver);
+                int mx = 0, my = 0, xl, xr, yu, yd;
+                GetMotionRange(n, m, 0, 0, &xl, &xr, &yu, &yd, _motionRange / 4);
+                for (int i = yu; i <= yd; i++)
+                    for (int j = xl; j <= xr; j++) {
+                        if (!(i || j)) continue;
+                        if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+                        _pExtRefOver->SetOrigin(n + j, m + i);
+                        const int d = _pInOver->Tad16x16LessThan(*_pExtRefOver, minDiff);
+                        if (d > minDiff) continue;
+                        if (d == minDiff) {
+                            const int cx = mx - prx, cy = my - pry, nx = j - prx, ny = i - pry;
+                            if ((cy * cy + cx * cx) - (ny * ny + nx * nx) < 0) continue;
+                        }
+                        minDiff = d;
+                        mx = j;
+                        my = i;
+                    }
+                if (vecPos < nmb) {
+                    mv_out[2 * vecPos] = (short)(4 * mx);
+                    mv_out[2 * vecPos + 1] = (short)(4 * my);
+                    if (dist_out) dist_out[vecPos] = minDiff;
+                    if (incl && incl[vecPos]) {
+                        included++;
+                        total += minDiff;
+                    }
+                    _pMVPred->Set16x16MotionVector(vecPos, 4 * mx, 4 * my);
+                    vecPos++;
+                }
+            }
+        if (avg_out) *avg_out = included ? total / included : 0;
+    }
+};
+
 }  // namespace
 
 extern "C" {
+
+/* FullSadStage over one frame pair: vectors (quarter pels), per-MB SAD and the
+ * included-distortion average (0 without flags, as Full.cpp:582-609). */
+int ref_me_full_sad(const short* src, const short* ref, int w, int h, int motion_range, const unsigned char* incl,
+                    short* mv_out, int* dist_out, long* avg_out)
+{
+    int nmb = (w / 16) * (h / 16);
+    MbGrid grid(w, h);
+    H264MotionVectorPredictorImpl1 pred(grid.flat);
+    bool* flags = make_flags(incl, nmb);
+    FullSadStage* me = new FullSadStage(src, ref, w, h, motion_range, &pred, flags);
+    if (!me->Create()) { delete me; delete[] flags; return -2; }
+    me->run(nmb, flags, mv_out, dist_out, avg_out);
+    delete me;
+    delete[] flags;
+    return 0;
+}
 
 /* kind: 0 Full, 1 Multires, 2 MultiresCross, 3 MultiresCrossVer2.
  * lambda: NULL, or a pointer passed to Estimate(long*, void*) (Ver2 only).

@@ -16,6 +16,10 @@ inputs and stores inputs and outputs:
                   avgDistortion, modes 0/1/2, with and without
                   pDistortionIncluded (pan and integer-shift content)
 * me_mr.npz       MotionEstimatorH264ImplMultires, the same cases as me_mrc2
+* me_full_sad.npz the integer-pel stage of MotionEstimatorH264ImplFull with
+                  its MEH264IF_ABS_DIFF distortion (SAD): the QCIF +-16 shifted
+                  sequence, pan and tiled (tie-heavy) pairs, vectors, SADs and
+                  averages
 * mc.npz          MotionCompensatorH264ImplStd::Compensate of 4:2:0 frames by
                   seeded vectors over the whole range (zero, full-pel, negative
                   fractions), QCIF / CIF / 64x48
@@ -26,7 +30,7 @@ inputs and stores inputs and outputs:
 * colour.npz      the three RGB24->YUV420 converters, flip and chroma offsets
 
 Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
-names: me_full me_mrc me_mrc2 me_mr mc transform colour, default all)
+names: me_full me_full_sad me_mrc me_mrc2 me_mr mc transform colour, default all)
 """
 from __future__ import annotations
 
@@ -76,6 +80,42 @@ def me_fixtures(ref: oracle.Reference) -> dict:
                 one[k] = 1
                 _, d[k] = ref.me("full", src, rf, mr, dist_incl=one)
             out[f"{name}_mbdist"] = d
+    return out
+
+
+SAD_CASES = [  # (name, w, h, motion_range, seed, generator)
+    ("config1", 176, 144, 64, 11, "shift"),   # QCIF +-16, the reference's own CPU case
+    ("cif_r128", 352, 288, 128, 12, "pan"),
+    ("partial_r64", 176, 152, 64, 13, "pan"),
+    ("tiles_r64", 176, 144, 64, 14, "tiles"),
+    ("tiles_r128", 352, 288, 128, 15, "tiles"),
+]
+
+
+def sad_fixtures(ref: oracle.Reference) -> dict:
+    """The integer-pel SAD stage of MotionEstimatorH264ImplFull (the harness's
+    FullSadStage on the reference's overlays): per case the first frame pairs of
+    the sequence (four frames of config1, two otherwise), vectors, SADs and the
+    all-included average; the average without flags is 0."""
+    out = {}
+    gens = {"shift": synth.shift_sequence, "pan": synth.pan_sequence, "tiles": synth.tile_sequence}
+    for name, w, h, mr, seed, gen in SAD_CASES:
+        nf = 4 if name == "config1" else 2
+        fr = gens[gen](seed, w, h, nf)
+        nmb = (w // 16) * (h // 16)
+        out[f"{name}_frames"] = np.stack(fr).astype(np.uint8)
+        out[f"{name}_meta"] = np.array([w, h, mr], np.int32)
+        mvs, ds, avgs = [], [], []
+        for t in range(nf - 1):
+            mv, d, avg = ref.me_full_sad(fr[t + 1], fr[t], mr, dist_incl=np.ones(nmb, np.uint8))
+            mv0, d0, avg0 = ref.me_full_sad(fr[t + 1], fr[t], mr)
+            assert np.array_equal(mv, mv0) and np.array_equal(d, d0) and avg0 == 0
+            mvs.append(mv)
+            ds.append(d)
+            avgs.append(avg)
+        out[f"{name}_mv"] = np.stack(mvs)
+        out[f"{name}_dist"] = np.stack(ds)
+        out[f"{name}_avg"] = np.array(avgs, np.int64)
     return out
 
 
@@ -263,7 +303,7 @@ def colour_fixtures(ref: oracle.Reference) -> dict:
 def main() -> None:
     oracle.build(with_reference=True)
     ref = oracle.Reference()
-    makers = {"me_full": me_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
+    makers = {"me_full": me_fixtures, "me_full_sad": sad_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "me_cross": lambda r: mrc2_fixtures(r, "cross"),
               "me_h263mrc": lambda r: mrc_fixtures(r, "h263_multires_cross", H263_CASES),
               "mc": mc_fixtures,

@@ -26,6 +26,34 @@ def test_me_full_matches_reference_vectors(orc, golden, case):
     assert avg2 == 0
 
 
+@pytest.mark.parametrize("case", ["config1", "cif_r128", "partial_r64", "tiles_r64", "tiles_r128"])
+def test_me_full_sad_matches_reference(orc, golden, case):
+    """The integer-pel SAD stage (vo_me_full_intpel, metric 1) against the
+    reference's own stage on its overlays (Tad16x16 / Tad16x16LessThan)."""
+    g = golden("me_full_sad.npz")
+    w, h, mr = (int(v) for v in g[f"{case}_meta"])
+    frames = g[f"{case}_frames"].astype(np.int16)
+    for t in range(len(frames) - 1):
+        mv, dist = orc.me_full_intpel(frames[t + 1], frames[t], mr, metric=1)
+        np.testing.assert_array_equal(mv, g[f"{case}_mv"][t])
+        np.testing.assert_array_equal(dist, g[f"{case}_dist"][t])
+        assert int(dist.sum()) // dist.size == int(g[f"{case}_avg"][t])
+
+
+def test_me_full_sad_matches_compiled_reference():
+    """Further seeded pairs against the compiled reference (where oracle/_ref exists)."""
+    if not oracle_mod.Reference.available():
+        pytest.skip("oracle/_ref not built here")
+    orc, ref = oracle_mod.Oracle(), oracle_mod.Reference()
+    for seed, w, h, mr, gen in [(41, 208, 120, 48, synth.pan_sequence), (42, 96, 64, 128, synth.tile_sequence),
+                                (43, 176, 144, 64, synth.shift_sequence)]:
+        fr = gen(seed, w, h, 2)
+        mv, dist = orc.me_full_intpel(fr[1], fr[0], mr, metric=1)
+        mv_r, dist_r, _ = ref.me_full_sad(fr[1], fr[0], mr)
+        np.testing.assert_array_equal(mv, mv_r)
+        np.testing.assert_array_equal(dist, dist_r)
+
+
 def test_me_full_matches_reference_per_mb_distortion(orc, golden):
     g = golden("me_full.npz")
     src = g["qcif_r64_src"].astype(np.int16)
