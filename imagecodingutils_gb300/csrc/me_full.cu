@@ -147,13 +147,22 @@ __global__ void __launch_bounds__(256) k_full_halfpel(const unsigned char* __res
 }
 
 // ---------------------------------------------------------------------------
+// c + sum over the four bytes of |a - b| (unsigned bytes): the PTX SIMD
+// video instruction with its accumulate form.
+__device__ __forceinline__ unsigned sad4_add(unsigned a, unsigned b, unsigned c)
+{
+    unsigned d;
+    asm("vabsdiff4.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
 // Table stage, one CTA per macroblock, every warp busy: the SSD (kSad: the
 // SAD, OverlayMem2Dv2::Tad16x16, OverlayMem2Dv2.cpp:2655-2730) of all
 // (2R+1)^2 full-pel candidates, its row minima, to the MB's global table.
-// The SAD has no energy decomposition: each word pair is one byte-wise
-// absolute difference summed by a dp4a against ones.
+// The SAD has no energy decomposition: each word pair is one vabsdiff4 with
+// accumulate.
 template <bool kSad>
-__global__ void __launch_bounds__(128, kSad ? 4 : 5) k_full_table(FullArgs a)
+__global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TableSmem& S = *reinterpret_cast<TableSmem*>(smem_raw);
@@ -239,7 +248,7 @@ __global__ void __launch_bounds__(128, kSad ? 4 : 5) k_full_table(FullArgs a)
                     unsigned c = acc[r][q];
 #pragma unroll
                     for (int w = 0; w < 4; w++)
-                        c = kSad ? __dp4a(__vabsdiffu4(A[w], B[q + w]), 0x01010101u, c) : __dp4a(A[w], B[q + w], c);
+                        c = kSad ? sad4_add(A[w], B[q + w], c) : __dp4a(A[w], B[q + w], c);
                     acc[r][q] = c;
                 }
             }

@@ -47,6 +47,29 @@ constexpr int kSetMax = 6;          // possible final vectors kept per neighbour
 
 __device__ __forceinline__ int4 empty_record() { return make_int4(kEmpty, 0, 0, 0); }
 
+// Walk a tie tree held one word per lane (t0: words 0..31, t1: 32..): the
+// outcome of the scan for rounded prediction (prx, pry).
+__device__ __forceinline__ void tree_pick(int t0, int t1, int prx, int pry, int* mvx, int* mvy, int* minD)
+{
+    constexpr int RW = sizeof(TieRun) / sizeof(int);
+    auto get = [&](int idx) {
+        const int v0 = __shfl_sync(0xffffffffu, t0, idx & 31), v1 = __shfl_sync(0xffffffffu, t1, idx & 31);
+        return idx < 32 ? v0 : v1;
+    };
+    int path = 0;
+    for (int e = 0; e < TIE_DEPTH; e++) {
+        if (e >= get(path * RW + TIE_DEPTH)) break;
+        const int g = get(path * RW + e);
+        const int cx = (int)(signed char)(g & 0xff) - prx, cy = (int)(signed char)((g >> 8) & 0xff) - pry;
+        const int nx = (int)(signed char)((g >> 16) & 0xff) - prx, ny = (int)(signed char)((g >> 24) & 0xff) - pry;
+        if ((cy * cy + cx * cx) - (ny * ny + nx * nx) >= 0) path |= 1 << e;
+    }
+    const int q = get(path * RW + TIE_DEPTH + 1);
+    *mvx = mv_x(q);
+    *mvy = mv_y(q);
+    *minD = get(path * RW + TIE_DEPTH + 2);
+}
+
 // Exact-tie macroblocks: the integer scan depends on the rounded prediction.
 // Walk the tie tree the search kernel kept (one load per lane), or, for the
 // rare macroblock with more ties than the tree holds, replay the scan from
@@ -59,26 +82,11 @@ __device__ __noinline__ void tie_path(const FullArgs& a, int k, int px, int py, 
     if (prx == 0 && pry == 0) return;  // the search kernel already decided ties with (0,0)
     const int* tab = a.tables + (size_t)k * TAB * TAB;
     if (!(flags & FLAG_DEEP)) {
-        constexpr int RW = sizeof(TieRun) / sizeof(int), TW = TIE_RUNS * RW;
+        constexpr int TW = TIE_RUNS * (int)(sizeof(TieRun) / sizeof(int));
         const int* tree = tab + TIE_ROW * TAB;
         const int t0 = __ldcg(tree + lane);
         const int t1 = lane < TW - 32 ? __ldcg(tree + 32 + lane) : 0;
-        auto get = [&](int idx) {
-            const int v0 = __shfl_sync(0xffffffffu, t0, idx & 31), v1 = __shfl_sync(0xffffffffu, t1, idx & 31);
-            return idx < 32 ? v0 : v1;
-        };
-        int path = 0;
-        for (int e = 0; e < TIE_DEPTH; e++) {
-            if (e >= get(path * RW + TIE_DEPTH)) break;
-            const int g = get(path * RW + e);
-            const int cx = (int)(signed char)(g & 0xff) - prx, cy = (int)(signed char)((g >> 8) & 0xff) - pry;
-            const int nx = (int)(signed char)((g >> 16) & 0xff) - prx, ny = (int)(signed char)((g >> 24) & 0xff) - pry;
-            if ((cy * cy + cx * cx) - (ny * ny + nx * nx) >= 0) path |= 1 << e;
-        }
-        const int q = get(path * RW + TIE_DEPTH + 1);
-        *mvx = mv_x(q);
-        *mvy = mv_y(q);
-        *minD = get(path * RW + TIE_DEPTH + 2);
+        tree_pick(t0, t1, prx, pry, mvx, mvy, minD);
         return;
     }
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
@@ -1047,29 +1055,77 @@ __global__ void k_full_average(FullArgs a)
 // diagonal's tie macroblocks settle together (warp each: tie tree walk, or a
 // rescan of the kept table), with a block barrier between diagonals.  Then the
 // outputs and the included-distortion average (Full.cpp:581-607).
+constexpr int kSadWaveWords = 64;   // one bit per diagonal: 2048 >= cols + 2 rows - 1 at 8192 x 8192
+constexpr int kSadSmemMbs = 16384;  // final vectors kept in shared memory up to this many macroblocks
+
+size_t sad_resolve_smem(int nmb)
+{
+    const size_t words = (size_t)(nmb + 31) / 32;
+    return 4 * (words + (nmb <= kSadSmemMbs ? (size_t)nmb : 0));
+}
+
 __global__ void __launch_bounds__(1024, 1) k_sad_resolve(FullArgs a)
 {
+    extern __shared__ unsigned s_dyn[];  // tie bit per macroblock, then (local) the final vectors
     __shared__ long long s_tot;
     __shared__ int s_cnt;
+    __shared__ unsigned s_wave[kSadWaveWords];  // diagonals holding a tie macroblock
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int cols = a.cols, rows = a.nmb / cols;
+    const int cols = a.cols, rows = a.nmb / cols, words = (a.nmb + 31) >> 5;
+    const int ntie = *((volatile int*)&a.ctrl->ntie);
+    const int waves = cols + 2 * (rows - 1);
+    const bool every = waves > 32 * kSadWaveWords;
+    const bool local = a.nmb <= kSadSmemMbs;
+    unsigned* s_tie = s_dyn;
+    int* s_fin = reinterpret_cast<int*>(s_dyn + words);
     if (threadIdx.x == 0) {
         s_tot = 0;
         s_cnt = 0;
     }
-    if (*((volatile int*)&a.ctrl->ntie) > 0) {
-        for (int t = 0; t <= cols - 1 + 2 * (rows - 1); t++) {
+    for (int i = threadIdx.x; i < kSadWaveWords; i += blockDim.x) s_wave[i] = 0u;
+    for (int i = threadIdx.x; i < words; i += blockDim.x) s_tie[i] = 0u;
+    if (local)
+        for (int k = threadIdx.x; k < a.nmb; k += blockDim.x) s_fin[k] = __ldcg(a.final_mv + k);
+    __syncthreads();
+    for (int i = threadIdx.x; i < ntie; i += blockDim.x) {
+        const int k = a.tie_list[i], r = k / cols, t = k - r * cols + 2 * r;
+        atomicOr(&s_tie[k >> 5], 1u << (k & 31));
+        if (!every) atomicOr(&s_wave[t >> 5], 1u << (t & 31));
+    }
+    __syncthreads();
+    if (ntie > 0) {
+        constexpr int TW = TIE_RUNS * (int)(sizeof(TieRun) / sizeof(int));
+        for (int t = 0; t < waves; t++) {
+            if (!every && !((s_wave[t >> 5] >> (t & 31)) & 1u)) continue;  // block-uniform: no tie on it
             const int r_lo = max(0, (t - cols + 2) / 2), r_hi = min(rows - 1, t / 2);
             for (int r = r_lo + wib; r <= r_hi; r += nw) {
                 const int k = r * cols + (t - 2 * r);
+                if (!((s_tie[k >> 5] >> (k & 31)) & 1u)) continue;
+                // the record and the tie tree do not depend on the prediction: one round trip for both
+                const int* tree = a.tables + (size_t)k * TAB * TAB + TIE_ROW * TAB;
                 const int4 sp = __ldcg(a.spec4 + k);
-                if (!(sp.w & FLAG_TIE)) continue;
+                const int t0 = __ldcg(tree + lane);
+                const int t1 = lane < TW - 32 ? __ldcg(tree + 32 + lane) : 0;
                 int px, py;
-                median_pred(a.final_mv, sp.w, k, cols, &px, &py);
+                if (local) {
+                    const int av = sp.w;
+                    const int A = (av & AV_A) ? s_fin[k - 1] : 0;
+                    const int B = (av & AV_B) ? s_fin[k - cols] : 0;
+                    const int C = (av & AV_C) ? s_fin[k - cols + 1] : 0;
+                    const int D = (!(av & AV_C) && (av & AV_D)) ? s_fin[k - cols - 1] : 0;
+                    median_from(av, A, B, C, D, &px, &py);
+                } else {
+                    median_pred(a.final_mv, sp.w, k, cols, &px, &py);
+                }
                 int mvx = mv_x(sp.x), mvy = mv_y(sp.x), md = sp.y;
-                tie_path(a, k, px, py, sp.w, lane, &mvx, &mvy, &md);
+                if (round_pred(px) != 0 || round_pred(py) != 0) {  // (0, 0): the scan already decided
+                    if (!(sp.w & FLAG_DEEP)) tree_pick(t0, t1, round_pred(px), round_pred(py), &mvx, &mvy, &md);
+                    else tie_path(a, k, px, py, sp.w, lane, &mvx, &mvy, &md);
+                }
                 if (lane == 0) {
-                    __stcg(a.final_mv + k, pack_mv(mvx, mvy));
+                    const int v = pack_mv(mvx, mvy);
+                    if (local) s_fin[k] = v;
+                    __stcg(a.final_mv + k, v);
                     __stcg(a.final_dist + k, md);
                 }
             }
@@ -1080,9 +1136,9 @@ __global__ void __launch_bounds__(1024, 1) k_sad_resolve(FullArgs a)
     long long tot = 0;
     int cnt = 0;
     for (int k = threadIdx.x; k < a.nmb; k += blockDim.x) {
-        const int4 sp = __ldcg(a.spec4 + k);
-        const int fmv = (sp.w & FLAG_TIE) ? __ldcg(a.final_mv + k) : sp.x;
-        const int d = (sp.w & FLAG_TIE) ? __ldcg(a.final_dist + k) : sp.y;
+        const bool tie = (s_tie[k >> 5] >> (k & 31)) & 1u;
+        const int fmv = local ? s_fin[k] : __ldcg(a.final_mv + k);
+        const int d = tie ? __ldcg(a.final_dist + k) : __ldcg(&a.spec4[k].y);
         a.job->out_mv[k] = fmv;
         if (a.job->out_dist) a.job->out_dist[k] = d;
         if (a.job->incl && a.job->incl[k]) {
@@ -1248,7 +1304,9 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid,
 
 int sad_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args)
 {
-    k_sad_resolve<<<1, 1024, 0, ctx->stream>>>(args);
+    const size_t smem = sad_resolve_smem(args.nmb);
+    VPP_CUDA(cudaFuncSetAttribute(k_sad_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_sad_resolve<<<1, 1024, smem, ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     return VPPGPU_OK;
 }
