@@ -74,3 +74,34 @@ def test_against_oracle(vpp, ctx, orc, seed, w, h, mr, gen):
     np.testing.assert_array_equal(mv, mv_o)
     np.testing.assert_array_equal(me.last_mb_distortion, d_o)
     assert avg == avg_o
+
+
+def test_batched_form(vpp, ctx, orc):
+    """The batched form (vppgpu_me_batch_*, several streams) of the SAD search
+    gives every job the vectors, SADs and average of estimating it alone."""
+    torch = pytest.importorskip("torch")
+    from imagecodingutils_gb300 import _lib
+    dev = torch.device("cuda", 0)
+    sizes = [(176, 144, 64), (352, 288, 128), (640, 368, 128), (208, 120, 48), (176, 144, 64)]
+    jobs, keep = [], []
+    for i, (w, h, mr) in enumerate(sizes):
+        fr = (synth.tile_sequence if i % 2 else synth.pan_sequence)(400 + i, w, h, 2)
+        nmb = (w // 16) * (h // 16)
+        src, ref = torch.from_numpy(fr[1]).to(dev), torch.from_numpy(fr[0]).to(dev)
+        incl = torch.from_numpy((synth.splitmix64(400 + i, nmb) % np.uint64(3) != 0).astype(np.uint8)).to(dev)
+        mv = torch.zeros((nmb, 2), dtype=torch.int16, device=dev)
+        dist = torch.zeros(nmb, dtype=torch.int32, device=dev)
+        keep.append((fr, incl, mv, dist, w, h, mr, src, ref))  # the device inputs stay alive
+        jobs.append((src.data_ptr(), ref.data_ptr(), w, h, mr, mv.data_ptr(), dist.data_ptr(), incl.data_ptr()))
+    batch = vpp.MotionEstimatorBatch(streams=3, kind=_lib.ME_FULL_SAD, ctx=ctx)
+    for _ in range(2):
+        st, avg = batch.run(jobs)
+        torch.cuda.synchronize()
+        assert st == [0] * len(jobs)
+        for (fr, incl, mv, dist, w, h, mr, _, _), a in zip(keep, avg):
+            mv_o, d_o = orc.me_full_intpel(fr[1], fr[0], mr, metric=1)
+            sel = incl.cpu().numpy().astype(bool)
+            np.testing.assert_array_equal(mv.cpu().numpy(), mv_o)
+            np.testing.assert_array_equal(dist.cpu().numpy(), d_o)
+            assert a == (int(d_o[sel].sum()) // int(sel.sum()) if sel.any() else 0)
+    batch.close()
