@@ -28,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -94,10 +95,9 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        self.path = os.path.join(tempfile.mkdtemp(prefix="vppgpu_clocks_"), f"clocks_rank{index}.csv")
 
     def __enter__(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -157,12 +157,14 @@ def profile_traffic():
 
 def cpu_baseline(frames, nthreads: int, nframes: int, seconds: float):
     """The oracle restatement of the reference on host threads, one estimator
-    per thread over independent frame pairs: passes over `nframes` pairs of
-    the rotation until `seconds` of wall time have been spent."""
+    per thread over independent frame pairs: passes over the rotation's pairs
+    (a whole number per thread, taken as threads free up) until `seconds` of
+    wall time have been spent."""
     from oracle.oracle import Oracle
     orc = Oracle()
-    srcs = [frames[i + 1] for i in range(nframes)]
-    refs = [frames[i] for i in range(nframes)]
+    nframes = nthreads * -(-nframes // nthreads)
+    srcs = [frames[1 + i % (NFRAMES - 1)] for i in range(nframes)]
+    refs = [frames[i % (NFRAMES - 1)] for i in range(nframes)]
     orc.bench_me_full(srcs[:1], refs[:1], MOTION_RANGE, 1)  # warm caches
     done, t0 = 0, time.perf_counter()
     while True:
@@ -617,9 +619,20 @@ def run_hbm_paths(torch, _lib, L, ctx, stream, dev, pk):
     return out
 
 
+def headline_config(world: int) -> dict:
+    """The headline workload, the same for both arms (the reference arm's host
+    threads are stated in its cpu_baseline)."""
+    return {"workload": f"MotionEstimatorH264ImplFull plain per-frame drop-in, {W}x{H}, motionRange {MOTION_RANGE}",
+            "frames": NFRAMES - 1, "l2": "inputs larger than L2 (32-frame rotation, 133 MB int16)",
+            "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args, rank, world):
-    """One step = one frame-pair estimate, as in the GPU arm; the K steps are
-    spread over all host threads (one estimator per thread)."""
+    """The reference algorithm on every host thread (one estimator per
+    thread, the reference has no internal threading): one step is one frame
+    pair per thread, so every thread is busy for the whole timed region; the
+    K steps' pairs (K x threads, in rotation order) are taken by the threads as
+    they free up."""
     if rank != 0:
         return 0
     from oracle import oracle
@@ -628,24 +641,42 @@ def run_reference(args, rank, world):
     nthreads = os.cpu_count() or 1
     orc = oracle.Oracle()
     pairs = lambda n: ([frames[1 + t % (NFRAMES - 1)] for t in range(n)], [frames[t % (NFRAMES - 1)] for t in range(n)])
-    s, r = pairs(args.warmup)
+    s, r = pairs(args.warmup * nthreads)
     orc.bench_me_full(s, r, MOTION_RANGE, nthreads)
-    s, r = pairs(args.steps)
+    npairs = args.steps * nthreads
+    s, r = pairs(npairs)
     t0 = time.perf_counter()
     orc.bench_me_full(s, r, MOTION_RANGE, nthreads)
     dt = time.perf_counter() - t0
-    value = args.steps * NMB / dt
+    value = npairs * NMB / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded pan sequence)",
-        "config": {"workload": f"MotionEstimatorH264ImplFull plain per-frame, {W}x{H}, motionRange {MOTION_RANGE}"},
+        "config": headline_config(world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": f"{args.steps} frame pairs over {nthreads} threads, {dt:.1f} s"},
+                         "sample": f"{npairs} 1080p frame pairs ({args.steps} steps x {nthreads} threads, "
+                                   f"one pair per thread per step), {dt:.1f} s"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+ONLY_ROWS = ["hbm", "batched", "serving", *MULTIRES]
+
+
+def run_only(args, torch, vpp, _lib, L, ctx, stream, dev, frames):
+    """One secondary row of the full run, alone (the profiles' commands)."""
+    if args.only == "hbm":
+        pk, pk_kind = peaks()
+        return {"peaks_source": pk_kind, **run_hbm_paths(torch, _lib, L, ctx, stream, dev, pk)}
+    if args.only in MULTIRES:
+        return run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, False, kind=args.only)
+    bases = sequence_bases(torch, dev)
+    if args.only == "batched":
+        return run_batched(args, torch, vpp, _lib, L, ctx, stream, dev, bases)
+    return run_serving(args, vpp, torch, ctx, bases)
 
 
 def main():
@@ -666,6 +697,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-budget", type=int, default=0, help="bytes of request buffers (0: half the free HBM)")
+    ap.add_argument("--only", choices=ONLY_ROWS, default=None,
+                    help="run one secondary row alone and print it as a JSON line (for profiling that row)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -694,6 +727,11 @@ def main():
     ctx.set_stream(stream.cuda_stream)
 
     frames = frames_for(rank)
+    if args.only:
+        print(json.dumps({"only": args.only, **run_only(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}",
+                                                        frames)}), flush=True)
+        ctx.close()
+        return 0
     dev = torch.from_numpy(np.stack(frames)).to(f"cuda:{local}")           # device-resident planes
     pinned = torch.from_numpy(np.stack(frames)).pin_memory()               # host planes for e2e
     d_mv = torch.empty((NMB, 2), dtype=torch.int16, device=f"cuda:{local}")
@@ -813,9 +851,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8/int32", "data": "synthetic (seeded 5x5-box noise, quarter-pel pan, sigma 2)",
-            "config": {"workload": f"MotionEstimatorH264ImplFull plain per-frame drop-in, {W}x{H}, motionRange {MOTION_RANGE}",
-                       "frames": NFRAMES - 1, "l2": "inputs larger than L2 (32-frame rotation, 133 MB int16)",
-                       "parallelism": f"replicas x{world}"},
+            "config": headline_config(world),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * W * H * 2,
                     "d2h_bytes_per_step": NMB * 4 + 32},
             "roofline": {"bound": "int-alu", "kernel": "k_full_table", "achieved": achieved, "peak": peak,

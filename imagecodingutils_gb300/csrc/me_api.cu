@@ -268,7 +268,9 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
 {
     if (!ctx || !out) return VPPGPU_ERR_INVALID_ARG;
     *out = nullptr;
-    if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
+    // ranges below 4 (less than one full pel) are refused: the reference runs a
+    // sub-pel-only search there, which nothing pins
+    if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 4) return VPPGPU_ERR_INVALID_ARG;
     if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
     if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
     if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_FULL_SAD) return VPPGPU_ERR_UNSUPPORTED;

@@ -983,11 +983,15 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
         o2 = o1;
         o1 = out;
     }
-    // copies still in flight after an abort land before the CTA leaves
+    // copies still in flight after an abort land before the CTA leaves; a
+    // drain that gives up (only after a timeout) is reported as one too
     for (int ci = consumed; ci < issued; ci++) {
         long long it = 0;
         while (!mbar_try_wait(mybars + (ci & 1), (unsigned)(ci >> 1) & 1u))
-            if (++it > a.spin_limit) break;
+            if (++it > a.spin_limit) {
+                atomicOr(&a.ctrl->status, ST_TIMEOUT);
+                break;
+            }
     }
     if (lane == 0 && misses) atomicAdd(&a.ctrl->wave_miss, misses);
     __syncthreads();
@@ -1230,6 +1234,10 @@ int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
                                   (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, cross::EST_CROSS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 2)));
+    // the SAD resolve's largest dynamic shared memory: the local final vectors
+    // end at kSadSmemMbs macroblocks (larger pictures keep only the tie bits)
+    VPP_CUDA(cudaFuncSetAttribute(k_sad_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sad_resolve_smem(kSadSmemMbs)));
     return VPPGPU_OK;
 }
 
@@ -1304,9 +1312,7 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid,
 
 int sad_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args)
 {
-    const size_t smem = sad_resolve_smem(args.nmb);
-    VPP_CUDA(cudaFuncSetAttribute(k_sad_resolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_sad_resolve<<<1, 1024, smem, ctx->stream>>>(args);
+    k_sad_resolve<<<1, 1024, sad_resolve_smem(args.nmb), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     return VPPGPU_OK;
 }

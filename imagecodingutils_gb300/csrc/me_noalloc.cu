@@ -17,14 +17,18 @@
 // every GPU that loads the library, for as long as the process runs.
 //
 // Sharing: all calls use the same array and it keeps the previous call's
-// contents.  The words that must start at zero (status, grid barrier,
-// per-sweep counters) are cleared by every call; everything else is written
-// before it is read.  Calls that overlap on the GPU (other host threads, or
-// other streams) race on the array and must be serialised by the caller.
+// contents.  The words that must start at zero -- the status, counters and
+// the dirty bitmap (MeCtrl and changed[0 .. sweep_limit)) -- are cleared by
+// every call; everything else is written before it is read.  Calls that
+// overlap on the GPU (other host threads, or other streams) race on the array
+// and must be serialised by the caller.
 //
 // Set-up: the first call on a device, made with that device current, looks
 // up the array's device address with cudaGetSymbolAddress and configures the
-// kernels.  Make that first call before any stream capture begins.
+// kernels.  With CUDA's lazy module loading (the default) that first call is
+// also when the driver reserves the array, so a caller with a fixed budget
+// makes it at start-up; make it before any stream capture begins.  Every call
+// is synchronous: it returns once the results are written.
 #include <mutex>
 
 #include "me_full_common.cuh"
@@ -130,7 +134,7 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
 {
     if (!d_src || !d_ref || !d_mv_out) return VPPGPU_ERR_INVALID_ARG;
     if (((uintptr_t)d_src | (uintptr_t)d_ref | (uintptr_t)d_mv_out) & 3) return VPPGPU_ERR_INVALID_ARG;
-    if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
+    if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 4) return VPPGPU_ERR_INVALID_ARG;
     const int cols = width / 16, nmb = cols * (height / 16);
     if (width > VPPGPU_NOALLOC_MAX_DIM || height > VPPGPU_NOALLOC_MAX_DIM || nmb > VPPGPU_NOALLOC_MAX_MBS ||
         motion_range > 128 || (size_t)width * height > kSrcBytes ||

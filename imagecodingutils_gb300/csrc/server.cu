@@ -256,7 +256,7 @@ int vppgpu_server_create(vppgpu_ctx* ctx, int slots, unsigned long long hbm_budg
 
 int vppgpu_server_prepare(vppgpu_server* s, int width, int height, int motion_range)
 {
-    if (!s || width < 16 || height < 16 || (width % 16) || motion_range < 0) return VPPGPU_ERR_INVALID_ARG;
+    if (!s || width < 16 || height < 16 || (width % 16) || motion_range < 4) return VPPGPU_ERR_INVALID_ARG;
     int rc = vppgpu::bind(s->parent);
     if (rc) return rc;
     for (auto& sl : s->slots) {

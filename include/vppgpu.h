@@ -80,7 +80,9 @@ typedef struct vppgpu_me vppgpu_me;
  * width x height luma frame and a quarter-pel motion range.  width must be a
  * multiple of 16; a partial bottom macroblock row (height % 16 != 0) is not
  * reported, as in the reference (Full.cpp:293, 594).  Supported ranges:
- * 4 <= motion_range <= 128 (search of at most +-31 pels). */
+ * 4 <= motion_range <= 128 (search of at most +-31 pels); ranges 0..3, for
+ * which the reference runs a sub-pel-only search, are refused with
+ * VPPGPU_ERR_INVALID_ARG. */
 int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motion_range,
                      vppgpu_me** out);
 int vppgpu_me_destroy(vppgpu_me* me);
@@ -275,7 +277,9 @@ int vppgpu_calibrate_dp4a(vppgpu_ctx* ctx, double* dp4a_per_second);
  * stream); the call returns when the results are written.  All calls share
  * the array, so calls that overlap on the GPU race and must be serialised.
  * The first call on a device (with that device current) looks up the array's
- * address; make it before any stream capture. */
+ * address; with lazy module loading it is also when the driver reserves the
+ * array, so make it at start-up, before any stream capture.  motion_range
+ * as for vppgpu_me_create (4..128). */
 #define VPPGPU_NOALLOC_MAX_MBS 396
 #define VPPGPU_NOALLOC_MAX_DIM 1024
 int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* d_ref, int width, int height,

@@ -18,6 +18,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libvppref.so")
+# Where the reference's sources lie: VPP_REFERENCE_TREE, else the build
+# container's checkout (absent on other hosts: the reference build and the
+# tests that need it are then skipped).
 REF_TREE = os.environ.get("VPP_REFERENCE_TREE", "/root/reference")
 
 _P = C.c_void_p

@@ -12,7 +12,8 @@
 typedef struct {
     const short* const* srcs;
     const short* const* refs;
-    int nframes, w, h, motion_range, tid, nthreads, rc;
+    int nframes, w, h, motion_range, rc;
+    int* next;  /* shared work counter: pairs are taken in order as threads free up */
     short* mv_out;
 } me_job;
 
@@ -20,7 +21,8 @@ static void* me_worker(void* arg)
 {
     me_job* j = (me_job*)arg;
     int nmb = vo_num_mbs(j->w, j->h);
-    for (int f = j->tid; f < j->nframes; f += j->nthreads) {
+    for (int f = __atomic_fetch_add(j->next, 1, __ATOMIC_RELAXED); f < j->nframes;
+         f = __atomic_fetch_add(j->next, 1, __ATOMIC_RELAXED)) {
         long avg;
         int rc = vo_me_full(j->srcs[f], j->refs[f], j->w, j->h, j->motion_range, NULL, NULL,
                             j->mv_out + (size_t)f * 2 * nmb, NULL, &avg);
@@ -36,8 +38,9 @@ int vo_bench_me_full(const short* const* srcs, const short* const* refs, int nfr
     if (nthreads > 256) nthreads = 256;
     pthread_t th[256];
     me_job jobs[256];
+    int next = 0;
     for (int t = 0; t < nthreads; t++) {
-        me_job jb = {srcs, refs, nframes, w, h, motion_range, t, nthreads, 0, mv_out};
+        me_job jb = {srcs, refs, nframes, w, h, motion_range, 0, &next, mv_out};
         jobs[t] = jb;
         if (pthread_create(&th[t], NULL, me_worker, &jobs[t]) != 0) {
             jobs[t].rc = -3;

@@ -34,6 +34,22 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def hd_golden():
+    """The 1080p fixtures (tests/golden/me_1080p.npz, made by the compiled
+    reference) and the benchmark-sequence frames they were made from,
+    regenerated here and checked against the stored SHA-256."""
+    import hashlib
+
+    from imagecodingutils_gb300 import synth
+    g = dict(np.load(os.path.join(GOLDEN, "me_1080p.npz")))
+    seed, w, h, mr, *pairs = (int(v) for v in g["meta"])
+    fr = synth.pan_sequence(seed, w, h, max(pairs) + 2)
+    digest = hashlib.sha256(b"".join(np.ascontiguousarray(f, np.int16).tobytes() for f in fr)).digest()
+    assert digest == g["frames_sha256"].tobytes(), "the synthetic generator no longer makes the fixtures' frames"
+    return {"g": g, "frames": fr, "w": w, "h": h, "motion_range": mr, "pairs": pairs}
+
+
+@pytest.fixture(scope="session")
 def vpp():
     import imagecodingutils_gb300 as vpp
     from imagecodingutils_gb300 import build

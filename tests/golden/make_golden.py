@@ -28,9 +28,15 @@ inputs and stores inputs and outputs:
                   intra and inter, modes 0/1/2, a custom SetScale, and
                   FastForward4x4ITImpl2::QuantiseValue
 * colour.npz      the three RGB24->YUV420 converters, flip and chroma offsets
+* me_1080p.npz    the headline size: Full, MultiresCross / Ver2 / Multires
+                  (modes 0, 1, 2), Cross and the integer-pel SAD stage on three
+                  frame pairs of the 1920x1080 benchmark sequence at
+                  motionRange 128 (frames regenerated by synth, pinned by their
+                  SHA-256)
 
 Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
-names: me_full me_full_sad me_mrc me_mrc2 me_mr mc transform colour, default all)
+names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mr me_cross me_h263mrc mc
+transform dc yuv2rgb colour, default all)
 """
 from __future__ import annotations
 
@@ -300,10 +306,51 @@ def colour_fixtures(ref: oracle.Reference) -> dict:
     return out
 
 
+HD_SEED, HD_W, HD_H, HD_RANGE = 1234, 1920, 1080, 128   # the benchmark's own 1080p sequence
+HD_PAIRS = (0, 5, 17)                                     # frame pairs (t+1 on t) of that sequence
+HD_ESTIMATORS = [("full", 1), ("multires_cross", 0), ("multires_cross", 1), ("multires_cross", 2),
+                 ("multires_cross_v2", 0), ("multires_cross_v2", 1), ("multires_cross_v2", 2),
+                 ("multires", 0), ("multires", 1), ("multires", 2), ("cross", 0)]
+
+
+def hd_frames():
+    """Frames 0..max(HD_PAIRS)+1 of the 1080p benchmark sequence and the
+    SHA-256 of their int16 bytes (the fixtures store the digest, not the
+    4 MB frames: synth regenerates them bit for bit)."""
+    import hashlib
+    fr = synth.pan_sequence(HD_SEED, HD_W, HD_H, max(HD_PAIRS) + 2)
+    digest = hashlib.sha256(b"".join(np.ascontiguousarray(f, np.int16).tobytes() for f in fr)).digest()
+    return fr, np.frombuffer(digest, np.uint8)
+
+
+def hd_fixtures(ref: oracle.Reference) -> dict:
+    """The headline size: every estimator on pairs HD_PAIRS of the 1080p
+    benchmark sequence at motionRange 128 -- vectors and avgDistortion with
+    all macroblocks included (SetMode as listed; MultiresCross counts every
+    macroblock anyway), and the integer-pel SAD stage's vectors, SADs and
+    average."""
+    fr, digest = hd_frames()
+    nmb = (HD_W // 16) * (HD_H // 16)
+    incl = np.ones(nmb, np.uint8)
+    out = {"meta": np.array([HD_SEED, HD_W, HD_H, HD_RANGE, *HD_PAIRS], np.int32), "frames_sha256": digest}
+    for t in HD_PAIRS:
+        src, rf = fr[t + 1], fr[t]
+        for kind, mode in HD_ESTIMATORS:
+            mv, avg = ref.me(kind, src, rf, HD_RANGE, mode=mode, dist_incl=incl)
+            out[f"p{t}_{kind}_m{mode}_mv"] = mv
+            out[f"p{t}_{kind}_m{mode}_avg"] = np.array([avg], np.int64)
+        mv, d, avg = ref.me_full_sad(src, rf, HD_RANGE, dist_incl=incl)
+        out[f"p{t}_full_sad_mv"] = mv
+        out[f"p{t}_full_sad_dist"] = d
+        out[f"p{t}_full_sad_avg"] = np.array([avg], np.int64)
+    return out
+
+
 def main() -> None:
     oracle.build(with_reference=True)
     ref = oracle.Reference()
-    makers = {"me_full": me_fixtures, "me_full_sad": sad_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
+    makers = {"me_1080p": hd_fixtures,
+              "me_full": me_fixtures, "me_full_sad": sad_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "me_cross": lambda r: mrc2_fixtures(r, "cross"),
               "me_h263mrc": lambda r: mrc_fixtures(r, "h263_multires_cross", H263_CASES),
               "mc": mc_fixtures,

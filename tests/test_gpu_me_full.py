@@ -175,3 +175,20 @@ def test_wavefront_after_few_relaxation_sweeps(vpp, ctx, orc, sweeps):
         np.testing.assert_array_equal(me.last_mb_distortion, dist_o)
         if sweeps == 0:
             assert me.last_sweeps() == 1000
+
+
+@pytest.mark.parametrize("mr", [0, 1, 2, 3])
+def test_sub_pel_only_ranges_are_refused(vpp, ctx, mr):
+    """motionRange 0..3 makes the reference search sub-pel positions only;
+    nothing pins that, so every estimator kind refuses it at creation."""
+    import ctypes as C
+
+    from imagecodingutils_gb300 import _lib
+    L = vpp.load()
+    for kind in range(_lib.ME_FULL, _lib.ME_FULL_SAD + 1):
+        h = C.c_void_p()
+        assert L.vppgpu_me_create(ctx.handle, kind, 176, 144, mr, C.byref(h)) == _lib.ERR_INVALID_ARG
+        assert not h.value
+    me = vpp.MotionEstimatorH264ImplFull(np.zeros((144, 176), np.int16), np.zeros((144, 176), np.int16), 176, 144,
+                                         mr, ctx=ctx)
+    assert me.Create() == 0

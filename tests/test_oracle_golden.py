@@ -360,3 +360,39 @@ def test_add_clip_and_sub(orc):
     r = rng.integers(-300, 300, 1000).astype(np.int16)
     np.testing.assert_array_equal(orc.add_clip255(a, r), np.clip(a.astype(np.int32) + r, 0, 255))
     np.testing.assert_array_equal(orc.sub(a, r), (a.astype(np.int32) - r).astype(np.int16))
+
+
+HD_PORT = {"full": "me_full", "multires_cross": "me_multires_cross", "multires_cross_v2": "me_multires_cross_v2",
+           "multires": "me_multires", "cross": "me_cross"}
+
+
+def test_port_matches_reference_at_1080p(orc, hd_golden):
+    """The headline size: the oracle port against the compiled reference's
+    1080p fixtures (the benchmark's own frame pairs, motionRange 128) for every
+    estimator and mode, and for the integer-pel SAD stage."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    g, fr, mr = hd_golden["g"], hd_golden["frames"], hd_golden["motion_range"]
+    nmb = (hd_golden["w"] // 16) * (hd_golden["h"] // 16)
+    incl = np.ones(nmb, np.uint8)
+    keys = sorted({k.rsplit("_", 1)[0] for k in g if k.startswith("p") and k.endswith("_mv")})
+
+    def run(key):  # key: p<pair>_<estimator>_m<mode>, or p<pair>_full_sad
+        pair, est = key[1:].split("_", 1)
+        src, ref = fr[int(pair) + 1], fr[int(pair)]
+        if est == "full_sad":
+            mv, dist = orc.me_full_intpel(src, ref, mr, metric=1)
+            return key, mv, int(dist.sum()) // nmb, dist
+        kind, mode = est.rsplit("_m", 1)
+        kw = {} if kind == "full" else {"mode": int(mode)}
+        mv, _, avg = getattr(orc, HD_PORT[kind])(src, ref, mr, dist_incl=incl, **kw)
+        return key, mv, avg, None
+
+    with ThreadPoolExecutor(8) as ex:  # ctypes releases the GIL: one estimate per thread
+        results = list(ex.map(run, keys))
+    assert len(results) == 3 * 12
+    for key, mv, avg, dist in results:
+        np.testing.assert_array_equal(mv, g[f"{key}_mv"], err_msg=key)
+        assert avg == int(g[f"{key}_avg"][0]), key
+        if dist is not None:
+            np.testing.assert_array_equal(dist, g[f"{key}_dist"], err_msg=key)

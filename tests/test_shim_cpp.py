@@ -8,10 +8,11 @@ import numpy as np
 import pytest
 
 from imagecodingutils_gb300 import synth
+from oracle.oracle import REF_TREE
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SHIM = os.path.join(ROOT, "imagecodingutils_gb300", "shim")
-REF_INC = "/root/reference/include"
+REF_INC = os.path.join(REF_TREE, "include")  # vpp's headers, only where the reference tree is present
 
 
 def gxx(args):
