@@ -148,8 +148,8 @@ def peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per k_full_table launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_full_table_1080p.json")
+    """DRAM bytes per k_full_search launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_full_search_1080p.json")
     if os.path.exists(path):
         return json.load(open(path)).get("dram_bytes_per_launch")
     return None
@@ -663,11 +663,38 @@ def run_reference(args, rank, world):
     return 0
 
 
-ONLY_ROWS = ["hbm", "batched", "serving", *MULTIRES]
+ONLY_ROWS = ["full", "hbm", "batched", "serving", *MULTIRES]
+# the library's per-stage events of the full-search estimator
+STAGES = ("planes_energy", "search", "subpel_tietree", "resolve")
+
+
+def run_full_only(args, torch, _lib, L, ctx, dev, frames):
+    """The headline estimator alone: device-resident estimates over the frame
+    rotation with the library's per-stage CUDA events (direct launches; for
+    profiling captures)."""
+    d = torch.from_numpy(np.stack(frames)).to(dev)
+    d_mv = torch.empty((NMB, 2), dtype=torch.int16, device=dev)
+    h = C.c_void_p()
+    _lib.check(L.vppgpu_me_create(ctx.handle, _lib.ME_FULL, W, H, MOTION_RANGE, C.byref(h)), "vppgpu_me_create")
+    _lib.check(L.vppgpu_me_set_timing(h, 1), "vppgpu_me_set_timing")
+    for t in range(args.warmup + args.steps):
+        i = t % (NFRAMES - 1)
+        _lib.check(L.vppgpu_me_estimate_device(h, C.c_void_p(d[i + 1].data_ptr()), C.c_void_p(d[i].data_ptr()),
+                                               None, None, C.c_void_p(d_mv.data_ptr()), None, None),
+                   "vppgpu_me_estimate_device")
+    torch.cuda.synchronize()
+    n = C.c_int()
+    stage = (C.c_double * 4)()
+    _lib.check(L.vppgpu_me_timing_stages(h, C.byref(n), stage), "vppgpu_me_timing_stages")
+    L.vppgpu_me_destroy(h)
+    return {"estimates": n.value, "kernel_ms_per_frame": {k: stage[i] / max(n.value, 1) for i, k in enumerate(STAGES)},
+            "workload": f"MotionEstimatorH264ImplFull, {W}x{H}, motionRange {MOTION_RANGE}, stage events"}
 
 
 def run_only(args, torch, vpp, _lib, L, ctx, stream, dev, frames):
     """One secondary row of the full run, alone (the profiles' commands)."""
+    if args.only == "full":
+        return run_full_only(args, torch, _lib, L, ctx, dev, frames)
     if args.only == "hbm":
         pk, pk_kind = peaks()
         return {"peaks_source": pk_kind, **run_hbm_paths(torch, _lib, L, ctx, stream, dev, pk)}
@@ -854,12 +881,12 @@ def main():
             "config": headline_config(world),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * W * H * 2,
                     "d2h_bytes_per_step": NMB * 4 + 32},
-            "roofline": {"bound": "int-alu", "kernel": "k_full_table", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "int-alu", "kernel": "k_full_search", "achieved": achieved, "peak": peak,
                          "unit": "Tpx/s", "frac": achieved / peak, "traffic": profile_traffic(),
                          "peak_source": "measured dp4a rate x 4 px (vppgpu_calibrate_dp4a, this run)",
                          "algorithmic_px_per_launch": px_ops},
             "kernel_ms_per_frame": {k: stage[i] / max(n.value, 1)
-                                    for i, k in enumerate(("pack_halfpel", "table", "refine_tietree", "resolve"))},
+                                    for i, k in enumerate(STAGES)},
             "latency_ms": {"p50": per_frame[len(per_frame) // 2],
                            "p99": per_frame[min(len(per_frame) - 1, int(0.99 * len(per_frame)))],
                            "max": per_frame[-1], "unit": "device ms per frame, plain per-frame form"},

@@ -30,6 +30,8 @@ struct vppgpu_me {
     int graph_state;  // 0 not tried, 1 captured, -1 unavailable (direct launches)
     int* spec;  // 5 * nmb: {vector, distortion, zero distortion, flags} per MB, then full-pel winners
     int* tables;
+    int* energy;  // block energies of the padded reference (full search by SSD)
+    vppgpu::SearchMaps* maps;  // the search kernel's tensor maps over this handle's buffers
     int* tie_list;
     int4* cache;
     int* dict;
@@ -117,6 +119,8 @@ void me_free(vppgpu_me* me)
     if (me->graph) cudaGraphExecDestroy(me->graph);
     cudaFree(me->spec);
     cudaFree(me->tables);
+    cudaFree(me->energy);
+    delete me->maps;
     cudaFree(me->tie_list);
     cudaFree(me->cache);
     cudaFree(me->dict);
@@ -160,6 +164,7 @@ vppgpu::FullArgs full_args(vppgpu_me* me, double lambda)
     a.cache = me->cache;
     a.dict = me->dict;
     a.tables = me->tables;
+    a.energy = me->energy;
     a.tie_list = me->tie_list;
     a.final_mv = me->state;
     a.final_dist = me->state + me->nmb;
@@ -209,7 +214,7 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
         // the integer-pel stage only: no sub-pel, no prediction check, no GetBestVector
         vppgpu::FullArgs a = full_args(me, 0.0);
         a.intpel = 1;
-        return vppgpu::sad_launch(ctx, a, me->nmb);
+        return vppgpu::sad_launch(ctx, a, *me->maps, me->nmb);
     }
     const vppgpu::FullArgs a = full_args(me, lambda);
     cudaEvent_t* ev = ring_slot(me);
@@ -222,7 +227,7 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
             int crc = VPPGPU_OK;
             if (cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream) != cudaSuccess)
                 crc = VPPGPU_ERR_CUDA;
-            if (!crc) crc = vppgpu::full_launch(ctx, a, me->nmb, me->resolve_grid, nullptr);
+            if (!crc) crc = vppgpu::full_launch(ctx, a, *me->maps, me->nmb, me->resolve_grid, nullptr);
             const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
             if (!crc && e == cudaSuccess && g && cudaGraphInstantiate(&me->graph, g, 0) == cudaSuccess) {
                 me->graph_state = 1;
@@ -239,7 +244,7 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
         return VPPGPU_OK;
     }
     VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
-    return vppgpu::full_launch(ctx, a, me->nmb, me->resolve_grid, ev);
+    return vppgpu::full_launch(ctx, a, *me->maps, me->nmb, me->resolve_grid, ev);
 }
 
 int status_from_ctrl(const vppgpu::MeCtrl& c) { return vppgpu::status_from_bits(c.status); }
@@ -388,7 +393,8 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) || (rc = dalloc(&me->d_src8, npix)) ||
         (rc = dalloc(&me->d_refp, npad)) || (rc = dalloc(&me->d_hpel, 3 * npad)) ||
         (rc = dalloc(&me->d_wave_rec, vppgpu::wave_rec_count(me->cols, me->rows))) || (rc = dalloc(&me->d_wave_choice, me->nmb)) || (rc = dalloc(&me->spec, 5 * (size_t)me->nmb)) ||
-        (rc = dalloc(&me->tables, (size_t)me->nmb * 64 * 64)) || (rc = dalloc(&me->d_job, 1)) || (rc = dalloc(&me->tie_list, me->nmb)) || (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
+        (rc = dalloc(&me->tables, (size_t)me->nmb * 64 * 64)) ||
+        (kind == VPPGPU_ME_FULL && (rc = dalloc(&me->energy, npad))) || (rc = dalloc(&me->d_job, 1)) || (rc = dalloc(&me->tie_list, me->nmb)) || (rc = dalloc(&me->state, 3 * (size_t)me->nmb)) ||
         (rc = dalloc(&me->cache, (size_t)me->nmb * vppgpu::KCACHE)) || (rc = dalloc(&me->dict, vppgpu::NDICT)) ||
         (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
         (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||
@@ -404,6 +410,17 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if ((rc = vppgpu::full_prepare(ctx, me->nmb, &me->resolve_grid))) {
         me_free(me);
         return rc;
+    }
+    if (kind == VPPGPU_ME_FULL || kind == VPPGPU_ME_FULL_SAD) {
+        me->maps = new (std::nothrow) vppgpu::SearchMaps();
+        if (!me->maps) {
+            me_free(me);
+            return VPPGPU_ERR_OUT_OF_MEMORY;
+        }
+        if ((rc = vppgpu::search_maps_encode(full_args(me, 0.0), me->maps))) {
+            me_free(me);
+            return rc;
+        }
     }
     *out = me;
     return VPPGPU_OK;

@@ -10,41 +10,35 @@
 // GB300 design
 //   k_full_pack     int16 -> u8 (with a 0..255 check) and an edge-replicated
 //                   padded reference, one pass over the planes.
-//   k_full_table    one CTA per macroblock, every warp busy.  The whole
-//                   (2R+1)^2 SSD table is computed as A2 + B2 - 2*sum(a*b):
-//                   sum(a*b) with dp4a, window rows byte-aligned once per
-//                   thread (funnel shifts) and held in a register ring, 4
-//                   dp4a per 16-pixel row product; B2 by separable sliding
-//                   sums in 16-wide runs; row minima; the table goes to
-//                   global memory.
-//   k_full_refine   one warp per macroblock, many per SM: the reference's
-//                   sequential raster scan over the table (ballots; rows whose
-//                   minimum cannot win are skipped) and the sub-pel stages.
-//                   None of this depends on the predictor except exact ties
-//                   in the scan, which are listed.
-//   k_full_tietree  for the listed MBs, the scan outcome of every tie
-//                   decision pattern (the tie tree), read by the
-//                   prediction-dependent stage.
 //   k_full_halfpel  b / h / j half-pel planes of the padded reference, used
-//                   by every distortion at a predicted vector.
+//                   by the sub-pel stages and every distortion at a predicted
+//                   vector.
+//   k_full_energy   16x16 block energies of the padded reference (the B^2 of
+//                   every candidate's SSD = A^2 + B^2 - 2 sum(ab)).
+//   k_full_search   persistent, warp-specialised: compute warps build each
+//                   macroblock's (2R+1)^2 SSD table in shared memory (cross
+//                   terms with dp4a, tiles staged by TMA tensor copies), a scan
+//                   warp replays the reference's sequential raster scan over
+//                   it (rows whose minimum or range cannot win are skipped).
+//                   Only the tables of macroblocks whose scan met an exact tie
+//                   leave the SM (for their tie tree).
+//   k_full_subpel   half-pel then quarter-pel refinement, a warp per MB.
+//   k_full_tietree  for the tie MBs, the scan outcome of every tie decision
+//                   pattern (the tie tree), read by the prediction-dependent
+//                   stage.
 //   resolve         (me_full_resolve.cu) the prediction-dependent tail:
 //                   median prediction, tie rescans, prediction distortion
 //                   and the Lagrangian pick, in the reference's raster order.
 #include <string.h>
+
+#include <cudaTypedefs.h>
+#include <mutex>
 
 #include "me_full_common.cuh"
 
 namespace vppgpu {
 namespace {
 using namespace full;
-
-struct TableSmem {
-    alignas(16) unsigned char win[WROWS][WSTRIDE];
-    alignas(16) unsigned char cur[256];
-    alignas(16) int tab[TAB][TAB];
-    int h2t[TAB][H2STRIDE];  // h2t[jj][r] = sum_x win(r, jj+x)^2
-    int a2;
-};
 
 struct TieSmem {
     alignas(16) int tab[TAB][TAB];
@@ -147,6 +141,57 @@ __global__ void __launch_bounds__(256) k_full_halfpel(const unsigned char* __res
 }
 
 // ---------------------------------------------------------------------------
+// Window energies: E(Y, X) = sum over the 16x16 block at padded position
+// (Y, X) of the squared reference samples, the B^2 term of every candidate's
+// SSD = A^2 + B^2 - 2 sum(ab).  One int per padded position (same row stride
+// as the byte planes), for Y <= PH - 16 and X <= PW - 16.  A CTA makes a
+// 64 x 64 tile: its 79 x 80 input bytes staged by words, horizontal 16-sums
+// of squares per row, then vertical 16-sums per column, 16 outputs per thread
+// (sliding sums) with coalesced stores.
+constexpr int EN_T = 64;
+
+__global__ void __launch_bounds__(256) k_full_energy(const unsigned char* __restrict__ refp, int rstride, int PH,
+                                                     int* __restrict__ energy)
+{
+    __shared__ __align__(16) unsigned char px[EN_T + 15][EN_T + 16];
+    __shared__ int hs[EN_T + 15][EN_T];
+    const int X0 = blockIdx.x * EN_T, Y0 = blockIdx.y * EN_T, PW = rstride, wq = PW / 4;
+    constexpr int RW = (EN_T + 16) / 4;  // words per staged row
+    for (int i = threadIdx.x; i < (EN_T + 15) * RW; i += 256) {
+        const int r = i / RW, c = i - r * RW;
+        const int y = min(Y0 + r, PH - 1), w = min(X0 / 4 + c, wq - 1);
+        reinterpret_cast<unsigned*>(&px[r][0])[c] = __ldg(reinterpret_cast<const unsigned*>(refp + (size_t)y * rstride) + w);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < (EN_T + 15) * (EN_T / 16); t += 256) {
+        const int r = t >> 2, c0 = 16 * (t & 3);
+        const unsigned char* p = &px[r][c0];
+        int acc = 0;
+#pragma unroll
+        for (int d = 0; d < 16; d++) acc += p[d] * p[d];
+        hs[r][c0] = acc;
+#pragma unroll
+        for (int c = 1; c < 16; c++) {
+            acc += p[c + 15] * p[c + 15] - p[c - 1] * p[c - 1];
+            hs[r][c0 + c] = acc;
+        }
+    }
+    __syncthreads();
+    {
+        const int c = threadIdx.x & (EN_T - 1), r0 = 16 * (threadIdx.x >> 6), X = X0 + c;
+        int acc = 0;
+#pragma unroll
+        for (int d = 0; d < 16; d++) acc += hs[r0 + d][c];
+#pragma unroll
+        for (int r = r0; r < r0 + 16; r++) {
+            if (r > r0) acc += hs[r + 15][c] - hs[r - 1][c];
+            const int Y = Y0 + r;
+            if (X <= PW - 16 && Y <= PH - 16) energy[(size_t)Y * rstride + X] = acc;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // c + sum over the four bytes of |a - b| (unsigned bytes): the PTX SIMD
 // video instruction with its accumulate form.
 __device__ __forceinline__ unsigned sad4_add(unsigned a, unsigned b, unsigned c)
@@ -156,193 +201,290 @@ __device__ __forceinline__ unsigned sad4_add(unsigned a, unsigned b, unsigned c)
     return d;
 }
 
-// Table stage, one CTA per macroblock, every warp busy: the SSD (kSad: the
-// SAD, OverlayMem2Dv2::Tad16x16, OverlayMem2Dv2.cpp:2655-2730) of all
-// (2R+1)^2 full-pel candidates, its row minima, to the MB's global table.
-// The SAD has no energy decomposition: each word pair is one vabsdiff4 with
-// accumulate.
-template <bool kSad>
-__global__ void __launch_bounds__(128, 5) k_full_table(FullArgs a)
+// ---------------------------------------------------------------------------
+// Search stage: one persistent CTA per slot (SEARCH_CTAS_PER_SM per SM),
+// macroblocks blockIdx.x, blockIdx.x + gridDim.x, ...; warp-specialised.
+//
+//   compute warps      the SSD (kSad: the SAD, OverlayMem2Dv2::Tad16x16,
+//                      OverlayMem2Dv2.cpp:2655-2730) of all (2R+1)^2 full-pel
+//                      candidates of a macroblock into a shared-memory table,
+//                      with its row minima; warp 0 also stages the next
+//                      macroblock's window and template (TMA tensor copies)
+//   scan warp (1)      the reference's sequential raster scan over each
+//                      table (prediction (0, 0) for ties, Full.cpp:394-446);
+//                      tables of macroblocks whose scan met an exact tie go to
+//                      global memory for their tie tree; then, in the buffer
+//                      it released, it stages the energies of the candidates
+//                      two macroblocks on (a TMA copy; the SSDs overwrite them
+//                      in place), so the compute warps never wait for a scan
+//                      unless it falls two tables behind.  The sub-pel stages
+//                      follow in k_full_subpel, whose global-memory round trips
+//                      would otherwise lengthen the scan warp's chain.
+//
+// Two window buffers and two table buffers; the hand-offs are shared-memory
+// barriers (mbarrier) whose waits are bounded: a wait that runs out sets
+// ST_TIMEOUT and every role leaves, after the copies it issued landed.
+constexpr int SEARCH_ROWS = 8;    // candidate rows per thread (the window-row ring's period)
+constexpr int SEARCH_UNROLL = 16; // template rows per unrolled loop body (a multiple of SEARCH_ROWS)
+constexpr int SEARCH_WARPS = 64 / (2 * SEARCH_ROWS);  // compute warps: 2 row groups of a warp each
+constexpr int SEARCH_THREADS = 32 * (SEARCH_WARPS + 1);
+constexpr int SEARCH_CTAS_PER_SM = 4;
+constexpr unsigned WIN_BYTES = WROWS * WSTRIDE + 256;     // window rows + template
+constexpr unsigned E_BYTES = (2 * RMAX + 1) * TAB * 4;    // candidate rows of energies
+// one window, 128-byte aligned, with room for a row 78 that the TMA box does
+// not fill (only the unused candidate row 63 reads it)
+constexpr int WIN_BUF = (WROWS * WSTRIDE + WSTRIDE + 127) / 128 * 128;
+static_assert(SEARCH_UNROLL % SEARCH_ROWS == 0 && 16 % SEARCH_UNROLL == 0, "unroll must cover ring periods");
+
+struct SearchSmem {
+    alignas(128) int tab[2][TAB][TAB];  // rows 0 .. 2R: SSDs (column 0: row minima)
+    alignas(128) unsigned char win[2][WIN_BUF];  // WROWS rows of WSTRIDE bytes
+    alignas(128) unsigned char cur[2][256];
+    unsigned long long wfull[2];   // window b staged
+    unsigned long long wfree[2];   // window b read by every compute thread
+    unsigned long long efull[2];   // SSD: energies staged in table b (the scan released it)
+    unsigned long long tfull[2];   // table b written by every compute thread
+    unsigned long long tempty[2];  // SAD: table b released by the scan warp
+    int abort;
+};
+
+// Bounded wait for the phase of parity `par`; false when the search is
+// abandoned (this wait ran out, or another role's did).
+__device__ __forceinline__ bool search_wait(unsigned long long* bar, unsigned par, const FullArgs& a,
+                                            volatile int* abort)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TableSmem& S = *reinterpret_cast<TableSmem*>(smem_raw);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int k = blockIdx.x;
-    const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
-
-    // 1. window (rows m-31.., cols n-32..) and input block
-    {
-        const unsigned char* wbase = a.refp + (size_t)(m - 31 + PAD) * a.rstride + (n - 32 + PAD);
-        for (int i = tid; i < WROWS * (WSTRIDE / 16); i += 128) {
-            int r = i / (WSTRIDE / 16), c = i - r * (WSTRIDE / 16);
-            *reinterpret_cast<uint4*>(&S.win[r][16 * c]) =
-                *reinterpret_cast<const uint4*>(wbase + (size_t)r * a.rstride + 16 * c);
-        }
-        if (tid < 16)
-            *reinterpret_cast<uint4*>(&S.cur[16 * tid]) =
-                *reinterpret_cast<const uint4*>(a.src8 + (size_t)(m + tid) * a.W + n);
-    }
-    __syncthreads();
-
-    // 2. template energy
-    if (!kSad && tid < 32) {
-        int acc = 0;
-#pragma unroll
-        for (int t = 0; t < 8; t++) {
-            const int v = S.cur[tid + 32 * t];
-            acc += v * v;
-        }
-        acc = warp_sum(acc);
-        if (tid == 0) S.a2 = acc;
-    }
-
-    // 3. cross terms with dp4a; each thread: 8 candidate rows x 4 word offsets, one byte shift s.
-    //    Each window row is byte-aligned once for the thread's shift (funnel shifts: word i
-    //    holds bytes 4i+s .. 4i+s+3 of the thread's 32-byte slice) and kept in a ring of 8
-    //    rows; then every 16-pixel row product is 4 dp4a against the template row.  The
-    //    horizontal 16-sample energies of the thread's 4 columns come from the same aligned
-    //    words (a self-dp4a per word and a sliding sum), for the window rows the thread owns
-    //    (its first 8; rows 64..77 after the loop); they fill the issue slots the dp4a pipe
-    //    leaves.
-    unsigned acc[8][4];
-    const int s = lane & 3, qg = (lane >> 2) & 3, ig = 2 * warp + (lane >> 4);
-    const int ii0 = 8 * ig;
-    {
-        unsigned al[8][7];
-        auto load_row = [&](unsigned* dst, int r) {
-            const uint4* p = reinterpret_cast<const uint4*>(&S.win[r][16 * qg]);
-            const uint4 x0 = p[0], x1 = p[1];
-            const unsigned w[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-#pragma unroll
-            for (int i = 0; i < 7; i++) dst[i] = __funnelshift_r(w[i], w[i + 1], 8 * s);
-        };
-        auto row_energy = [&](const unsigned* w, int r) {
-            unsigned sq[7];
-#pragma unroll
-            for (int i = 0; i < 7; i++) sq[i] = __dp4a(w[i], w[i], 0u);
-            unsigned e = sq[0] + sq[1] + sq[2] + sq[3];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                if (q) e += sq[q + 3] - sq[q - 1];
-                S.h2t[16 * qg + 4 * q + s][r] = (int)e;
-            }
-        };
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-            load_row(al[r], ii0 + r);
-            if (!kSad) row_energy(al[r], ii0 + r);
-        }
-#pragma unroll
-        for (int r = 0; r < 8; r++)
-#pragma unroll
-            for (int q = 0; q < 4; q++) acc[r][q] = 0u;
-#pragma unroll
-        for (int y = 0; y < 16; y++) {
-            const uint4 t = *reinterpret_cast<const uint4*>(&S.cur[16 * y]);
-            const unsigned A[4] = {t.x, t.y, t.z, t.w};
-#pragma unroll
-            for (int r = 0; r < 8; r++) {
-                const unsigned* B = al[(r + y) & 7];
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    unsigned c = acc[r][q];
-#pragma unroll
-                    for (int w = 0; w < 4; w++)
-                        c = kSad ? sad4_add(A[w], B[q + w], c) : __dp4a(A[w], B[q + w], c);
-                    acc[r][q] = c;
-                }
-            }
-            if (y < 15) load_row(al[y & 7], ii0 + y + 8);
+    long long it = 0;
+    while (!mbar_try_wait(bar, par)) {
+        if (*abort) return false;
+        if (++it > a.spin_limit) {
+            atomicOr(&a.ctrl->status, ST_TIMEOUT);
+            *abort = 1;
+            return false;
         }
     }
-    // energies of window rows 64..77 (below every row group's own rows): 14 rows x 16 slices
-    for (int task = kSad ? (WROWS - 64) * 16 : tid; task < (WROWS - 64) * 16; task += 128) {
-        const int r = 64 + (task >> 4), c = task & 15, ts = c & 3, tq = c >> 2;
-        const uint4* p = reinterpret_cast<const uint4*>(&S.win[r][16 * tq]);
-        const uint4 x0 = p[0], x1 = p[1];
-        const unsigned w[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
-        unsigned sq[7];
-#pragma unroll
-        for (int i = 0; i < 7; i++) {
-            const unsigned v = __funnelshift_r(w[i], w[i + 1], 8 * ts);
-            sq[i] = __dp4a(v, v, 0u);
-        }
-        unsigned e = sq[0] + sq[1] + sq[2] + sq[3];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            if (q) e += sq[q + 3] - sq[q - 1];
-            S.h2t[16 * tq + 4 * q + ts][r] = (int)e;
-        }
-    }
-    __syncthreads();
-
-    // 4. vertical 16-row sums of the horizontal energies (task: column jj, run ib), then
-    //    SSD = A^2 + B^2 - 2 sum(ab) for every candidate
-    for (int task = kSad ? TAB * 4 : tid; task < TAB * 4; task += 128) {
-        const int jj = task & (TAB - 1), ib = task >> 6;
-        const int* col = S.h2t[jj];
-        const int r0 = 16 * ib, r1 = min(r0 + 16, 2 * RMAX + 1);
-        int sum = 0;
-#pragma unroll
-        for (int y = 0; y < 16; y++) sum += col[r0 + y];
-        S.tab[r0][jj] = sum;
-        for (int ii = r0 + 1; ii < r1; ii++) {
-            sum += col[ii + 15] - col[ii - 1];
-            S.tab[ii][jj] = sum;
-        }
-    }
-    __syncthreads();
-    {
-        const int a2 = kSad ? 0 : S.a2;
-#pragma unroll
-        for (int r = 0; r < 8; r++) {
-            int ii = ii0 + r;
-            if (ii < 2 * RMAX + 1) {
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    int jj = 4 * (4 * qg + q) + s;
-                    S.tab[ii][jj] = kSad ? (int)acc[r][q] : a2 + S.tab[ii][jj] - 2 * (int)acc[r][q];
-                }
-            }
-        }
-    }
-    __syncthreads();
-
-    // 5. row minima, then the table (rows 0 .. 2R) to global memory
-    int xl, xr, yu, yd;
-    full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
-    table_row_minima(S.tab, xl, xr, yu, yd, warp, 4, lane);
-    __syncthreads();
-    int4* dst = reinterpret_cast<int4*>(a.tables + (size_t)k * TAB * TAB);
-    for (int i = tid; i < (2 * RMAX + 1) * TAB / 4; i += 128) __stcg(dst + i, reinterpret_cast<const int4*>(&S.tab[0][0])[i]);
+    return true;
 }
 
-// ---------------------------------------------------------------------------
-// Refine stage, one warp per macroblock: the reference's sequential scan
-// over the table (prediction (0,0) for ties), then the half/quarter-pel
-// stages around the winner.  MBs whose scan met an exact tie go to the tie
-// list for their tie tree.
-__global__ void __launch_bounds__(256, 4) k_full_refine(FullArgs a)
+// Wait (bounded, abort ignored) for the stagings [from, to) on a pair of
+// barriers: copies must land before the CTA leaves.
+__device__ __forceinline__ void search_drain(unsigned long long* bars, int from, int to, long long limit)
 {
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int k = blockIdx.x * 8 + wib;
+    for (int i = from; i < to; i++) {
+        long long w = 0;
+        while (!mbar_try_wait(&bars[i & 1], (unsigned)(i >> 1) & 1u) && ++w <= limit) {}
+    }
+}
+
+template <bool kSad>
+__global__ void __launch_bounds__(SEARCH_THREADS, SEARCH_CTAS_PER_SM)
+    k_full_search(FullArgs a, const __grid_constant__ SearchMaps maps)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SearchSmem& S = *reinterpret_cast<SearchSmem*>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nit = (a.nmb - 1 - (int)blockIdx.x) / (int)gridDim.x + 1;  // grid <= nmb: at least one
+    volatile int* abort = &S.abort;
+    if (tid == 0) {
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&S.wfull[b], 1);
+            mbar_init(&S.wfree[b], 32 * SEARCH_WARPS);
+            mbar_init(&S.efull[b], 1);
+            mbar_init(&S.tfull[b], 32 * SEARCH_WARPS);
+            mbar_init(&S.tempty[b], 32);
+        }
+        S.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto mb_of = [&](int it) { return (int)blockIdx.x + it * (int)gridDim.x; };
+
+    if (warp < SEARCH_WARPS) {
+        // ---------------- compute warps ----------------
+        // warp 0 stages the window + template of iteration `it` into buffer it & 1
+        auto stage_window = [&](int it) {
+            if (lane == 0) {
+                const int b = it & 1, k = mb_of(it);
+                const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
+                mbar_expect_tx(&S.wfull[b], WIN_BYTES);
+                tma_load_2d(S.win[b], &maps.win, n - 32 + PAD, m - 31 + PAD, &S.wfull[b]);
+                tma_load_2d(S.cur[b], &maps.cur, n, m, &S.wfull[b]);
+            }
+        };
+        int wissued = 0;  // warp 0: windows staged for iterations 0 .. wissued-1
+        if (warp == 0) {
+            stage_window(0);
+            wissued = 1;
+        }
+        const int s = lane & 3, qg = (lane >> 2) & 3, ig = 2 * warp + (lane >> 4);
+        const int ii0 = SEARCH_ROWS * ig;
+        int it = 0;
+        for (; it < nit; it++) {
+            const int b = it & 1;
+            const unsigned use = (unsigned)(it >> 1) & 1u;  // parity of this buffer's use
+            if (warp == 0 && it + 1 < nit) {
+                // window buffer b^1 was read in iteration it-1 (its first use: free from the start)
+                if (!search_wait(&S.wfree[b ^ 1], ((unsigned)((it + 1) >> 1) & 1u) ^ 1u, a, abort)) break;
+                stage_window(it + 1);
+                wissued = it + 2;
+            }
+            if (!search_wait(&S.wfull[b], use, a, abort)) break;
+
+            // cross terms with dp4a (kSad: vabsdiff4 with accumulate); each thread:
+            // SEARCH_ROWS candidate rows x 4 word offsets, one byte shift s.  Each window
+            // row is byte-aligned once for the thread's shift (funnel shifts: word i holds
+            // bytes 4i+s .. 4i+s+3 of the thread's 32-byte slice) and kept in a ring of
+            // SEARCH_ROWS rows; every 16-pixel row product is then 4 dp4a against the
+            // template row.
+            unsigned acc[SEARCH_ROWS][4];
+            {
+                unsigned al[SEARCH_ROWS][7];
+                auto load_row = [&](unsigned* dst, int r) {
+                    const uint4* p = reinterpret_cast<const uint4*>(&S.win[b][r * WSTRIDE + 16 * qg]);
+                    const uint4 x0 = p[0], x1 = p[1];
+                    const unsigned w[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+                    for (int i = 0; i < 7; i++) dst[i] = __funnelshift_r(w[i], w[i + 1], 8 * s);
+                };
+#pragma unroll
+                for (int r = 0; r < SEARCH_ROWS; r++) load_row(al[r], ii0 + r);
+#pragma unroll
+                for (int r = 0; r < SEARCH_ROWS; r++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) acc[r][q] = 0u;
+#pragma unroll 1
+                for (int yq = 0; yq < 16; yq += SEARCH_UNROLL) {
+#pragma unroll
+                    for (int yu = 0; yu < SEARCH_UNROLL; yu++) {
+                        const int y = yq + yu;
+                        const uint4 t = *reinterpret_cast<const uint4*>(&S.cur[b][16 * y]);
+                        const unsigned A[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+                        for (int r = 0; r < SEARCH_ROWS; r++) {
+                            const unsigned* B = al[(r + yu) % SEARCH_ROWS];
+#pragma unroll
+                            for (int q = 0; q < 4; q++) {
+                                unsigned c = acc[r][q];
+#pragma unroll
+                                for (int w = 0; w < 4; w++)
+                                    c = kSad ? sad4_add(A[w], B[q + w], c) : __dp4a(A[w], B[q + w], c);
+                                acc[r][q] = c;
+                            }
+                        }
+                        if (y < 15) load_row(al[yu % SEARCH_ROWS], ii0 + y + SEARCH_ROWS);
+                    }
+                }
+            }
+            // template energy
+            int a2 = 0;
+            if (!kSad) {
+#pragma unroll
+                for (int t = 0; t < 8; t++) {
+                    const int v = S.cur[b][lane + 32 * t];
+                    a2 += v * v;
+                }
+                a2 = warp_sum(a2);
+            }
+            mbar_arrive(&S.wfree[b]);  // this thread is done with window b and its template
+
+            // the table buffer: its energies staged (the scan warp stages them once it released
+            // the buffer), or, for the SAD, released
+            if (!search_wait(kSad ? &S.tempty[b] : &S.efull[b], kSad ? use ^ 1u : use, a, abort)) break;
+            const int k = mb_of(it);
+            const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
+            int xl, xr, yu, yd;
+            full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
+#pragma unroll
+            for (int r = 0; r < SEARCH_ROWS; r++) {
+                const int ii = ii0 + r;
+                int v[4], mn = 0x7fffffff;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int jj = 16 * qg + 4 * q + s;
+                    v[q] = kSad ? (int)acc[r][q] : a2 + (ii < 2 * RMAX + 1 ? S.tab[b][ii][jj] : 0) - 2 * (int)acc[r][q];
+                    const int j = jj - RMAX - 1;
+                    if (j >= xl && j <= xr) mn = min(mn, v[q]);
+                }
+#pragma unroll
+                for (int o = 1; o < 16; o <<= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+                if (ii < 2 * RMAX + 1) {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const int jj = 16 * qg + 4 * q + s;
+                        S.tab[b][ii][jj] = jj == 0 ? mn : v[q];  // column 0 (outside every range): the row minimum
+                    }
+                }
+            }
+            mbar_arrive(&S.tfull[b]);
+        }
+        if (warp == 0) search_drain(S.wfull, it, wissued, a.spin_limit);
+    } else {
+        // ---------------- scan warp ----------------
+        // energies of iteration `it`'s candidates into table buffer it & 1 (SSD)
+        auto stage_energy = [&](int it) {
+            if (lane == 0) {
+                const int b = it & 1, k = mb_of(it);
+                const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
+                mbar_expect_tx(&S.efull[b], E_BYTES);
+                tma_load_2d(&S.tab[b][0][0], &maps.energy, n - 32 + PAD, m - 31 + PAD, &S.efull[b]);
+            }
+        };
+        int eissued = 0;  // energies staged for iterations 0 .. eissued-1
+        if (!kSad) {      // both table buffers start free
+            eissued = min(nit, 2);
+            for (int i = 0; i < eissued; i++) stage_energy(i);
+        }
+        int it = 0;
+        for (; it < nit; it++) {
+            const int b = it & 1;
+            const int k = mb_of(it);
+            const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
+            if (!search_wait(&S.tfull[b], (unsigned)(it >> 1) & 1u, a, abort)) break;
+            int xl, xr, yu, yd, mx, my, minD, tie;
+            full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
+            scan_table(SmemTab{S.tab[b]}, xl, xr, yu, yd, 0, 0, lane, &mx, &my, &minD, &tie);
+            const int zero_d = S.tab[b][RMAX][RMAX + 1];
+            if (tie) {  // its tie tree (and deep rescans) read the table from global memory
+                int4* dst = reinterpret_cast<int4*>(a.tables + (size_t)k * TAB * TAB);
+                const int4* src = reinterpret_cast<const int4*>(&S.tab[b][0][0]);
+                for (int i = lane; i < (2 * RMAX + 1) * TAB / 4; i += 32) __stcg(dst + i, src[i]);
+            }
+            __syncwarp();
+            if (kSad) {
+                mbar_arrive(&S.tempty[b]);
+            } else if (it + 2 < nit) {
+                stage_energy(it + 2);  // the buffer is released: the table two iterations on
+                eissued = it + 3;
+            }
+            if (lane == 0) {  // the full-pel result; k_full_subpel refines it (SSD search)
+                const int qmv = pack_mv(4 * mx, 4 * my);
+                const int av = neighbour_mask(a.job->slice, k, a.cols, a.nmb / a.cols);
+                a.spec4[k] = make_int4(qmv, minD, zero_d, (tie ? FLAG_TIE : 0) | av);
+                a.spec_imv[k] = pack_mv(mx, my);
+                __stcg(a.final_mv + k, qmv);
+                if (tie) a.tie_list[atomicAdd(&a.ctrl->ntie, 1)] = k;
+            }
+        }
+        if (!kSad) search_drain(S.efull, it, eissued, a.spin_limit);
+    }
+}
+
+// Half-pel then quarter-pel refinement around each macroblock's full-pel
+// winner (Full.cpp:452-517), one warp per macroblock, many per SM: the
+// prediction-independent result the resolve starts from.
+__global__ void __launch_bounds__(256) k_full_subpel(FullArgs a)
+{
+    const int lane = threadIdx.x & 31, k = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (k >= a.nmb) return;
     const int n = (k % a.cols) * 16, m = (k / a.cols) * 16;
-    const int* gt = a.tables + (size_t)k * TAB * TAB;
-    const uint2 cur = load_cur8(a, n, m, lane);
-    int xl, xr, yu, yd, mx, my, minD, tie;
-    full_range(n, m, a.W, a.H, a.motion_range, xl, xr, yu, yd);
-    scan_table(GlobalTab{gt}, xl, xr, yu, yd, 0, 0, lane, &mx, &my, &minD, &tie);
-    const int zero_d = __ldcg(gt + RMAX * TAB + RMAX + 1);
-    int qmx = 0, qmy = 0;
-    if (!a.intpel) subpel_refine_planes(a, n + mx, m + my, cur, lane, &minD, &qmx, &qmy);
+    const int imv = __ldcg(a.spec_imv + k);
+    const int mx = mv_x(imv), my = mv_y(imv);
+    int minD = __ldcg(&a.spec4[k].y), qmx = 0, qmy = 0;
+    subpel_refine_planes(a, n + mx, m + my, load_cur8(a, n, m, lane), lane, &minD, &qmx, &qmy);
     if (lane == 0) {
         const int qmv = pack_mv(4 * mx + qmx, 4 * my + qmy);
-        const int av = neighbour_mask(a.job->slice, k, a.cols, a.nmb / a.cols);
-        a.spec4[k] = make_int4(qmv, minD, zero_d, (tie ? FLAG_TIE : 0) | av);
-        a.spec_imv[k] = pack_mv(mx, my);
+        a.spec4[k].x = qmv;
+        a.spec4[k].y = minD;
         __stcg(a.final_mv + k, qmv);
-        if (tie) a.tie_list[atomicAdd(&a.ctrl->ntie, 1)] = k;
     }
 }
 
@@ -417,8 +559,6 @@ int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v)
     return VPPGPU_OK;
 }
 
-size_t full_search_smem() { return sizeof(TableSmem); }
-
 int full_planes_launch(vppgpu_ctx* ctx, const FullArgs& args)
 {
     {
@@ -441,16 +581,79 @@ int full_planes_launch(vppgpu_ctx* ctx, const FullArgs& args)
     return VPPGPU_OK;
 }
 
-int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid, cudaEvent_t* ev)
+namespace {
+
+// The search's grid: SEARCH_CTAS_PER_SM persistent CTAs per SM, at most one per macroblock.
+int search_grid(const vppgpu_ctx* ctx, int nmb)
+{
+    const int g = ctx->sm_count * SEARCH_CTAS_PER_SM;
+    return nmb < g ? nmb : g;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode_tiled = nullptr;
+std::once_flag g_encode_once;
+
+// A 2-D tiled map over a row-major plane: width x height elements of
+// `elem` bytes, `pitch` bytes per row, boxes of box_w x box_h elements, no
+// swizzle (the box lands as box_h packed rows).
+int encode_2d(CUtensorMap* map, const void* base, CUtensorMapDataType type, int elem, int width, int height,
+              size_t pitch, int box_w, int box_h)
+{
+    std::call_once(g_encode_once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode_tiled = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    });
+    if (!g_encode_tiled) return VPPGPU_ERR_NO_DEVICE;
+    if (((uintptr_t)base & 15) || (pitch & 15) || ((size_t)box_w * elem) % 16) return VPPGPU_ERR_INVALID_ARG;
+    const cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)height};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch};
+    const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode_tiled(map, type, 2, const_cast<void*>(base), dims, strides, box, estr,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? VPPGPU_OK : VPPGPU_ERR_CUDA;
+}
+
+}  // namespace
+
+int search_maps_encode(const FullArgs& a, SearchMaps* maps)
+{
+    memset(maps, 0, sizeof(*maps));
+    const int PW = a.W + 2 * PAD, PH = a.H + 2 * PAD;
+    int rc = encode_2d(&maps->win, a.refp, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, PW, PH, (size_t)a.rstride, WSTRIDE, WROWS);
+    if (!rc) rc = encode_2d(&maps->cur, a.src8, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, a.W, a.H, (size_t)a.W, 16, 16);
+    if (!rc && a.energy)
+        rc = encode_2d(&maps->energy, a.energy, CU_TENSOR_MAP_DATA_TYPE_INT32, 4, PW, PH, (size_t)a.rstride * 4, TAB,
+                       2 * RMAX + 1);
+    return rc;
+}
+
+int full_energy_launch(vppgpu_ctx* ctx, const FullArgs& args)
+{
+    const int PW = args.W + 2 * PAD, PH = args.H + 2 * PAD;
+    dim3 grid((PW - 16) / EN_T + 1, (PH - 16) / EN_T + 1);
+    k_full_energy<<<grid, 256, 0, ctx->stream>>>(args.refp, args.rstride, PH, const_cast<int*>(args.energy));
+    VPP_CHECK_LAUNCH(ctx);
+    return VPPGPU_OK;
+}
+
+int full_launch(vppgpu_ctx* ctx, const FullArgs& args, const SearchMaps& maps, int nmb, int resolve_grid,
+                cudaEvent_t* ev)
 {
     if (ev) VPP_CUDA(cudaEventRecord(ev[0], ctx->stream));
     int rc = full_planes_launch(ctx, args);
     if (rc) return rc;
+    if ((rc = full_energy_launch(ctx, args))) return rc;
     if (ev) VPP_CUDA(cudaEventRecord(ev[1], ctx->stream));
-    k_full_table<false><<<nmb, 128, sizeof(TableSmem), ctx->stream>>>(args);
+    k_full_search<false><<<search_grid(ctx, nmb), SEARCH_THREADS, sizeof(SearchSmem), ctx->stream>>>(args, maps);
     VPP_CHECK_LAUNCH(ctx);
     if (ev) VPP_CUDA(cudaEventRecord(ev[2], ctx->stream));
-    k_full_refine<<<(nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
+    k_full_subpel<<<(nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
     k_full_tietree<<<ctx->sm_count, TIE_RUNS * 32, sizeof(TieSmem), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
@@ -461,15 +664,13 @@ int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid
     return VPPGPU_OK;
 }
 
-// The integer-pel SAD stage (FullArgs::intpel): planes, the SAD table, the
-// scan at prediction (0, 0) without sub-pel, tie trees, then the tie wavefront.
-int sad_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb)
+// The integer-pel SAD stage (FullArgs::intpel): planes, the SAD search (table,
+// scan at prediction (0, 0), no sub-pel), tie trees, then the tie wavefront.
+int sad_launch(vppgpu_ctx* ctx, const FullArgs& args, const SearchMaps& maps, int nmb)
 {
     int rc = full_planes_launch(ctx, args);
     if (rc) return rc;
-    k_full_table<true><<<nmb, 128, sizeof(TableSmem), ctx->stream>>>(args);
-    VPP_CHECK_LAUNCH(ctx);
-    k_full_refine<<<(nmb + 7) / 8, 256, 0, ctx->stream>>>(args);
+    k_full_search<true><<<search_grid(ctx, nmb), SEARCH_THREADS, sizeof(SearchSmem), ctx->stream>>>(args, maps);
     VPP_CHECK_LAUNCH(ctx);
     k_full_tietree<<<ctx->sm_count, TIE_RUNS * 32, sizeof(TieSmem), ctx->stream>>>(args);
     VPP_CHECK_LAUNCH(ctx);
@@ -478,10 +679,10 @@ int sad_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb)
 
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid)
 {
-    VPP_CUDA(cudaFuncSetAttribute(k_full_table<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sizeof(TableSmem)));
-    VPP_CUDA(cudaFuncSetAttribute(k_full_table<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sizeof(TableSmem)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_search<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(SearchSmem)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_search<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(SearchSmem)));
     VPP_CUDA(cudaFuncSetAttribute(k_full_tietree, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sizeof(TieSmem)));
     int cap = 0;

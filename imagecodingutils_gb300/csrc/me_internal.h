@@ -1,6 +1,8 @@
 // me_internal.h -- host/device argument blocks of the motion estimators.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (types only; the encoder is reached through the runtime's driver entry point)
+
 #include "vppgpu_internal.cuh"
 
 namespace vppgpu {
@@ -71,7 +73,9 @@ struct FullArgs {
     //  zero-vector distortion, flags (FLAG_TIE | neighbour availability)}
     int4* spec4;
     int* spec_imv;   // packed full-pel winner
-    int* tables;     // 64x64 SSD table per macroblock (row minima in column 0, tie tree in row 63)
+    int* tables;     // 64x64 SSD table per macroblock, kept for the tie macroblocks only (row
+                     // minima in column 0, tie tree in row 63)
+    const int* energy;  // 16x16 block energies of the padded reference (int, rstride per row)
     int* tie_list;   // macroblocks whose scan met an exact tie (MeCtrl::ntie of them)
     // resolve state
     int* final_mv;
@@ -144,7 +148,16 @@ int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v);
 // Motion-compensated luma residual of the last estimate's planes at vectors d_mv.
 int full_residual_launch(vppgpu_ctx* ctx, const FullArgs& args, const int* d_mv, short* d_res);
 
-size_t full_search_smem();
+// Block energies of the padded reference (args.energy) for the SSD search.
+int full_energy_launch(vppgpu_ctx* ctx, const FullArgs& args);
+// 2-D tensor maps the search kernel stages its tiles with (one TMA copy each
+// per macroblock): the padded reference (80 x 78 window box), the packed
+// input (16 x 16 template box) and the block energies (64 x 63 box).  They
+// describe buffers, not a frame: encode once per buffer set.
+struct SearchMaps {
+    CUtensorMap win, cur, energy;
+};
+int search_maps_encode(const FullArgs& args, SearchMaps* maps);
 // Byte-packed input (args.src8), padded reference and its half-pel planes
 // from the int16 planes of args.job.
 int full_planes_launch(vppgpu_ctx* ctx, const FullArgs& args);
@@ -156,11 +169,13 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid,
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap);
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid);
 // ev: nullptr, or 5 events recorded before the pack kernel, before the
-// table kernel, before the refine kernel, before the resolve and after it.
-int full_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb, int resolve_grid, cudaEvent_t* ev);
+// search kernel, after it (before the sub-pel stage and the tie trees),
+// before the resolve and after it.
+int full_launch(vppgpu_ctx* ctx, const FullArgs& args, const SearchMaps& maps, int nmb, int resolve_grid,
+                cudaEvent_t* ev);
 // Integer-pel SAD full search: the MotionEstimatorH264ImplFull integer stage
 // (MotionEstimatorH264ImplFull.cpp:341-446) with the MEH264IF_ABS_DIFF distortion.
-int sad_launch(vppgpu_ctx* ctx, const FullArgs& args, int nmb);
+int sad_launch(vppgpu_ctx* ctx, const FullArgs& args, const SearchMaps& maps, int nmb);
 // Its prediction-dependent tail: the tie macroblocks in wavefront order, then the outputs.
 int sad_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args);
 

@@ -6,14 +6,15 @@
 // code paths whose rules forbid allocator calls after initialisation.  For
 // them, vppgpu_me_full_estimate_noalloc runs the same kernels as
 // vppgpu_me_estimate_device, but every intermediate buffer (packed source,
-// padded reference, per-macroblock results, SSD tables, control words) lives
+// padded reference, block energies, per-macroblock results, SSD tables of
+// tie macroblocks, control words) lives
 // in one file-scope device array of fixed size, g_noalloc_scratch below.
 // The caller passes device inputs and outputs; the call makes no
 // cudaMalloc, cudaFree or other allocating call.
 //
 // Limits: at most VPPGPU_NOALLOC_MAX_MBS (396) stored macroblocks, e.g. CIF
 // 352x288, width and height at most VPPGPU_NOALLOC_MAX_DIM (1024); larger
-// frames are rejected with VPPGPU_ERR_UNSUPPORTED.  The array takes 10 MiB on
+// frames are rejected with VPPGPU_ERR_UNSUPPORTED.  The array takes 12 MiB on
 // every GPU that loads the library, for as long as the process runs.
 //
 // Sharing: all calls use the same array and it keeps the previous call's
@@ -52,6 +53,7 @@ constexpr size_t kChoiceBytes = 1600;                      // one int per macrob
 constexpr size_t kTieListBytes = 1600;                     // one int per macroblock
 constexpr size_t kJobBytes = 64;                           // vppgpu::JobDesc
 constexpr size_t kTableBytes = (size_t)VPPGPU_NOALLOC_MAX_MBS * 64 * 64 * 4;
+constexpr size_t kEnergyBytes = 4 * kRefBytes;               // one int per padded reference sample
 constexpr size_t kOffSrc = 0;
 constexpr size_t kOffRef = kOffSrc + kSrcBytes;
 constexpr size_t kOffSpec = kOffRef + kRefBytes;
@@ -66,6 +68,7 @@ constexpr size_t kOffChoice = kOffWaveRec + kWaveRecBytes;
 constexpr size_t kOffTieList = kOffChoice + kChoiceBytes;
 constexpr size_t kOffJob = kOffTieList + kTieListBytes;
 constexpr size_t kOffTables = kOffJob + kJobBytes;
+constexpr size_t kOffEnergy = kOffTables + kTableBytes;
 static_assert(sizeof(vppgpu::JobDesc) <= kJobBytes && kOffJob % 16 == 0, "job descriptor does not fit");
 static_assert(16 * vppgpu::KCACHE * VPPGPU_NOALLOC_MAX_MBS <= kCacheBytes && 4 * vppgpu::NDICT <= kDictBytes,
               "resolve caches do not fit");
@@ -73,10 +76,10 @@ static_assert(sizeof(vppgpu::WaveRec) * VPPGPU_NOALLOC_MAX_MBS <= kWaveRecBytes 
                   4 * VPPGPU_NOALLOC_MAX_MBS <= kChoiceBytes,
               "wavefront records do not fit");
 static_assert(kOffSpec % 16 == 0 && kOffCache % 16 == 0 && kOffHpel % 16 == 0 &&
-                  kOffWaveRec % 16 == 0 && kOffTables % 16 == 0,
+                  kOffWaveRec % 16 == 0 && kOffTables % 16 == 0 && kOffEnergy % 16 == 0,
               "vector records and planes need 16-byte alignment");
-constexpr size_t kScratchBytes = 10u << 20;
-static_assert(kOffTables + kTableBytes <= kScratchBytes, "scratch layout exceeds the array");
+constexpr size_t kScratchBytes = 12u << 20;
+static_assert(kOffEnergy + kEnergyBytes <= kScratchBytes, "scratch layout exceeds the array");
 static_assert(sizeof(vppgpu::MeCtrl) <= kCtrlBytes, "control block does not fit");
 static_assert(5 * 4 * VPPGPU_NOALLOC_MAX_MBS <= kSpecBytes && 3 * 4 * VPPGPU_NOALLOC_MAX_MBS <= kStateBytes &&
                   4 * (vppgpu::RELAX_SWEEPS + 2 + (VPPGPU_NOALLOC_MAX_MBS + 31) / 32) <= kChangedBytes,
@@ -173,6 +176,7 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     a.spec4 = reinterpret_cast<int4*>(spec);
     a.spec_imv = spec + 4 * nmb;
     a.tables = (int*)(base + kOffTables);
+    a.energy = (const int*)(base + kOffEnergy);
     a.cache = (int4*)(base + kOffCache);
     a.dict = (int*)(base + kOffDict);
     int* state = (int*)(base + kOffState);
@@ -202,7 +206,9 @@ extern "C" int vppgpu_me_full_estimate_noalloc(const short* d_src, const short* 
     rc = vppgpu::set_job(&ctx, (vppgpu::JobDesc*)(base + kOffJob),
                          vppgpu::JobDesc{d_src, d_ref, d_dist_included, d_mb_slice, (int*)d_mv_out, d_mb_dist_out, nullptr});
     if (rc) return rc;
-    rc = vppgpu::full_launch(&ctx, a, nmb, grid, nullptr);
+    vppgpu::SearchMaps maps;  // host-side descriptors of the array's planes, passed by value
+    if ((rc = vppgpu::search_maps_encode(a, &maps))) return rc;
+    rc = vppgpu::full_launch(&ctx, a, maps, nmb, grid, nullptr);
     if (rc) return rc;
 
     vppgpu::MeCtrl h = {};

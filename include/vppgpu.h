@@ -269,7 +269,7 @@ int vppgpu_calibrate_dp4a(vppgpu_ctx* ctx, double* dp4a_per_second);
  * running (real-time encoders with a fixed budget, plugins inside a host
  * that owns all allocations, code paths that forbid allocator calls after
  * start-up).  Same kernels and results as vppgpu_me_estimate_device, but all
- * intermediate buffers live in one 10 MiB static device array held by every
+ * intermediate buffers live in one 12 MiB static device array held by every
  * GPU that loads the library until the process exits.  Limits: at most
  * VPPGPU_NOALLOC_MAX_MBS stored macroblocks and width, height at most
  * VPPGPU_NOALLOC_MAX_DIM, else VPPGPU_ERR_UNSUPPORTED.  Inputs and outputs are
