@@ -224,11 +224,16 @@ __device__ __forceinline__ unsigned sad4_add(unsigned a, unsigned b, unsigned c)
 // Two window buffers and two table buffers; the hand-offs are shared-memory
 // barriers (mbarrier) whose waits are bounded: a wait that runs out sets
 // ST_TIMEOUT and every role leaves, after the copies it issued landed.
+// Launch shape, measured on 1080p frames: 8 candidate rows per thread with the
+// template rows in two passes of the ring's period (a loop body small enough
+// for the instruction cache; the full 16-step unroll stalled on instruction
+// fetch, 0.179 against 0.167 ms), at 3 CTAs per SM, where the loop needs no
+// spills (4 CTAs with a 96-register cap: the same time).
 constexpr int SEARCH_ROWS = 8;    // candidate rows per thread (the window-row ring's period)
-constexpr int SEARCH_UNROLL = 16; // template rows per unrolled loop body (a multiple of SEARCH_ROWS)
+constexpr int SEARCH_UNROLL = 8;  // template rows per unrolled loop body (a multiple of SEARCH_ROWS)
 constexpr int SEARCH_WARPS = 64 / (2 * SEARCH_ROWS);  // compute warps: 2 row groups of a warp each
 constexpr int SEARCH_THREADS = 32 * (SEARCH_WARPS + 1);
-constexpr int SEARCH_CTAS_PER_SM = 4;
+constexpr int SEARCH_CTAS_PER_SM = 3;
 constexpr unsigned WIN_BYTES = WROWS * WSTRIDE + 256;     // window rows + template
 constexpr unsigned E_BYTES = (2 * RMAX + 1) * TAB * 4;    // candidate rows of energies
 // one window, 128-byte aligned, with room for a row 78 that the TMA box does
