@@ -58,6 +58,7 @@ SIGNATURES = {
     "vppgpu_me_autotune_pairs": (_I, [_P, _P, _P, _I, _I, C.POINTER(_I)]),
     "vppgpu_me_last_sweeps": (_I, [_P, C.POINTER(_I)]),
     "vppgpu_me_last_stats": (_I, [_P, _P]),
+    "vppgpu_me_last_relax_changes": (_I, [_P, _P, _I]),
     "vppgpu_me_set_timing": (_I, [_P, _I]),
     "vppgpu_me_timing": (_I, [_P, C.POINTER(_I), C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_double)]),

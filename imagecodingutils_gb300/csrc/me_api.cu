@@ -750,6 +750,17 @@ extern "C" int vppgpu_me_last_stats(vppgpu_me* me, int* stats8)
     return VPPGPU_OK;
 }
 
+extern "C" int vppgpu_me_last_relax_changes(vppgpu_me* me, int* changes, int n)
+{
+    if (!me || !changes || n < 0 || n > vppgpu::RELAX_SWEEPS) return VPPGPU_ERR_INVALID_ARG;
+    if (!me->changed) return VPPGPU_ERR_UNSUPPORTED;  // estimators without a relaxation
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    VPP_CUDA(cudaStreamSynchronize(me->ctx->stream));
+    if (n) VPP_CUDA(cudaMemcpy(changes, me->changed + 1, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost));
+    return VPPGPU_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Batched estimation: many independent frame pairs, any mix of sizes, spread
 // over several streams so that one frame's latency-bound stages run beside

@@ -8,13 +8,12 @@
 // Lagrangian pick between best, predicted and zero vectors (:573-601).
 //
 // GB300 design
-//   k_full_pack     int16 -> u8 (with a 0..255 check) and an edge-replicated
-//                   padded reference, one pass over the planes.
-//   k_full_halfpel  b / h / j half-pel planes of the padded reference, used
-//                   by the sub-pel stages and every distortion at a predicted
-//                   vector.
-//   k_full_energy   16x16 block energies of the padded reference (the B^2 of
-//                   every candidate's SSD = A^2 + B^2 - 2 sum(ab)).
+//   k_full_planes   one pass over tiles of the padded reference: int16 ->
+//                   u8 (with a 0..255 check) and edge replication, the b / h /
+//                   j half-pel planes (sub-pel stages, every distortion at a
+//                   predicted vector) and the 16x16 block energies (the B^2 of
+//                   every candidate's SSD = A^2 + B^2 - 2 sum(ab)); the input's
+//                   byte packing rides along.
 //   k_full_search   persistent, warp-specialised: compute warps build each
 //                   macroblock's (2R+1)^2 SSD table in shared memory (cross
 //                   terms with dp4a, tiles staged by TMA tensor copies), a scan
@@ -46,147 +45,125 @@ struct TieSmem {
 };
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_full_pack(const JobDesc* __restrict__ job, int W, int H,
-                                                  unsigned char* __restrict__ src8, unsigned char* __restrict__ refp,
-                                                  int rstride, int* status)
-{
-    const short* __restrict__ src16 = job->src16;
-    const short* __restrict__ ref16 = job->ref16;
-    // padded reference: 4 bytes per thread; source: 4 samples per thread
-    const int PW = W + 2 * PAD, PH = H + 2 * PAD;
-    const long long nref = (long long)(PW / 4) * PH;  // PW is a multiple of 16
-    const long long nsrc = (long long)W * H / 4;
-    bool bad = false;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nref + nsrc;
-         i += (long long)gridDim.x * blockDim.x) {
-        if (i < nref) {
-            int row = (int)(i / (PW / 4)), cq = (int)(i - (long long)row * (PW / 4));
-            int y = min(max(row - PAD, 0), H - 1);
-            unsigned out = 0;
-#pragma unroll
-            for (int b = 0; b < 4; b++) {
-                int x = min(max(4 * cq + b - PAD, 0), W - 1);
-                int v = ref16[(size_t)y * W + x];
-                bad |= (v < 0) | (v > 255);
-                out |= (unsigned)(v & 0xff) << (8 * b);
-            }
-            *reinterpret_cast<unsigned*>(refp + (size_t)row * rstride + 4 * cq) = out;
-        } else {
-            long long j = i - nref;
-            const short2* s = reinterpret_cast<const short2*>(src16) + 2 * j;
-            short2 a = s[0], b = s[1];
-            int v0 = a.x, v1 = a.y, v2 = b.x, v3 = b.y;
-            bad |= (v0 < 0) | (v0 > 255) | (v1 < 0) | (v1 > 255) | (v2 < 0) | (v2 > 255) | (v3 < 0) | (v3 > 255);
-            unsigned out = (unsigned)(v0 & 0xff) | ((unsigned)(v1 & 0xff) << 8) | ((unsigned)(v2 & 0xff) << 16) |
-                           ((unsigned)(v3 & 0xff) << 24);
-            reinterpret_cast<unsigned*>(src8)[j] = out;
-        }
-    }
-    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(status, ST_PIXEL_RANGE);
-}
+// The frame's planes in one pass, a CTA per PL_TX x PL_TY tile of the padded
+// reference (PAD samples of edge replication each side, OverlayExtMem2Dv2's
+// extended boundary as a coordinate clamp):
+//   refp    the padded reference as bytes (0..255 checked)
+//   hpel    its H.264 half-pel planes, b (x half: 6-tap (1,-5,20,20,-5,1) on
+//           the row, (+16) >> 5), h (y half, on the column) and j (centre:
+//           the 6-tap over the unrounded vertical taps, (+512) >> 10), each
+//           clipped to 0..255 -- the samples QuarterRead combines
+//           (OverlayMem2Dv2.cpp:704-1052)
+//   energy  (SSD search only) E(Y, X) = sum of squares of the 16x16 block at
+//           (Y, X), for Y <= PH-16, X <= PW-16: the B^2 term of every
+//           candidate's SSD = A^2 + B^2 - 2 sum(ab)
+// plus a share of the input's byte packing (src8, 0..255 checked).  The tile
+// and its halo (2 before, 15 after in each direction) are staged once as
+// bytes; taps read clamped coordinates, which differs from a clamped padded
+// plane only within 3 samples of its border, never read (a prediction stays
+// within 17 samples of the picture).
+constexpr int PL_TX = 64, PL_TY = 32;
+constexpr int PL_SX = PL_TX + 20, PL_SY = PL_TY + 17;  // staged columns X0-2 .. X0+81, rows Y0-2 .. Y0+46
 
-// ---------------------------------------------------------------------------
-// Half-pel planes of the padded reference (the H.264 6-tap b, h and j
-// samples QuarterRead combines, OverlayMem2Dv2.cpp): b(x,y) between x and
-// x+1, h(x,y) between y and y+1, j from the unrounded vertical taps.  Four
-// samples per thread; tap coordinates are clamped to the padded buffer, which
-// only changes samples within three of its border, never read (a prediction
-// stays within 17 samples of the picture, the padding is 48).
 __device__ __forceinline__ unsigned char clip_tap(int v, int round, int shift)
 {
     return (unsigned char)clip255((v + round) >> shift);
 }
 
-__global__ void __launch_bounds__(256) k_full_halfpel(const unsigned char* __restrict__ refp, int rstride, int PW,
-                                                      int PH, unsigned char* __restrict__ hpel, size_t plane_size)
+__global__ void __launch_bounds__(256) k_full_planes(const JobDesc* __restrict__ job, int W, int H, int rstride,
+                                                     unsigned char* __restrict__ src8, unsigned char* __restrict__ refp,
+                                                     unsigned char* __restrict__ hpel, size_t plane_size,
+                                                     int* __restrict__ energy, int* status)
 {
-    const int qw = PW / 4;
-    const long long total = (long long)qw * PH;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int Y = (int)(i / qw), X = 4 * (int)(i - (long long)Y * qw);
-        // columns X-4 .. X+7 of rows Y-2 .. Y+3 as three words per row
-        int g[6][12];
+    __shared__ __align__(16) unsigned char px[PL_SY][PL_SX];
+    __shared__ short vt[PL_TY][PL_TX + 5];            // unrounded vertical taps, columns X0-2 .. X0+66
+    __shared__ int hs[PL_TY + 15][PL_TX];             // horizontal 16-sums of squares (energy)
+    const short* __restrict__ ref16 = job->ref16;
+    const int PW = rstride, PH = H + 2 * PAD;
+    const int X0 = blockIdx.x * PL_TX, Y0 = blockIdx.y * PL_TY, tid = threadIdx.x;
+    bool bad = false;
+    // 1. stage: padded (Y, X) -> frame (clamp(Y - PAD), clamp(X - PAD)), 2 samples per thread step
+    for (int i = tid; i < PL_SY * (PL_SX / 2); i += 256) {
+        const int r = i / (PL_SX / 2), c = 2 * (i - r * (PL_SX / 2));
+        const int y = min(max(Y0 - 2 + r - PAD, 0), H - 1);
+        const short* row = ref16 + (size_t)y * W;
+        const int v0 = row[min(max(X0 - 2 + c - PAD, 0), W - 1)];
+        const int v1 = row[min(max(X0 - 1 + c - PAD, 0), W - 1)];
+        bad |= (v0 < 0) | (v0 > 255) | (v1 < 0) | (v1 > 255);
+        px[r][c] = (unsigned char)v0;
+        px[r][c + 1] = (unsigned char)v1;
+    }
+    // the input's byte packing, a share per CTA (4 samples per thread step)
+    {
+        const long long nq = (long long)W * H / 4, nb = (long long)gridDim.x * gridDim.y;
+        const long long b = (long long)blockIdx.y * gridDim.x + blockIdx.x;
+        const short2* s2 = reinterpret_cast<const short2*>(job->src16);
+        for (long long j = b * 256 + tid; j < nq; j += nb * 256) {
+            const short2 p = s2[2 * j], q = s2[2 * j + 1];
+            const int v0 = p.x, v1 = p.y, v2 = q.x, v3 = q.y;
+            bad |= (v0 < 0) | (v0 > 255) | (v1 < 0) | (v1 > 255) | (v2 < 0) | (v2 > 255) | (v3 < 0) | (v3 > 255);
+            reinterpret_cast<unsigned*>(src8)[j] = (unsigned)(v0 & 0xff) | ((unsigned)(v1 & 0xff) << 8) |
+                                                   ((unsigned)(v2 & 0xff) << 16) | ((unsigned)(v3 & 0xff) << 24);
+        }
+    }
+    if (__any_sync(0xffffffffu, bad) && (tid & 31) == 0) atomicOr(status, ST_PIXEL_RANGE);
+    __syncthreads();
+    // 2. vertical taps at rows Y0 .. Y0+31, columns X0-2 .. X0+66 (staged rows r .. r+5, column c)
+    for (int i = tid; i < PL_TY * (PL_TX + 5); i += 256) {
+        const int r = i / (PL_TX + 5), c = i - r * (PL_TX + 5);
+        vt[r][c] = (short)tap6(px[r][c], px[r + 1][c], px[r + 2][c], px[r + 3][c], px[r + 4][c], px[r + 5][c]);
+    }
+    if (energy) {  // horizontal 16-sums of squares, rows Y0 .. Y0+46 (staged row r + 2), columns X0 ..
+        for (int t = tid; t < (PL_TY + 15) * (PL_TX / 16); t += 256) {
+            const int r = t >> 2, c0 = 16 * (t & 3);
+            const unsigned char* p = &px[r + 2][c0 + 2];
+            int acc = 0;
 #pragma unroll
-        for (int dy = 0; dy < 6; dy++) {
-            const int yy = min(max(Y - 2 + dy, 0), PH - 1);
-            const unsigned* row = reinterpret_cast<const unsigned*>(refp + (size_t)yy * rstride);
+            for (int d = 0; d < 16; d++) acc += p[d] * p[d];
+            hs[r][c0] = acc;
 #pragma unroll
-            for (int q = 0; q < 3; q++) {
-                const int wq = min(max(X / 4 - 1 + q, 0), qw - 1);
-                const unsigned w = __ldg(row + wq);
-#pragma unroll
-                for (int b = 0; b < 4; b++) g[dy][4 * q + b] = (w >> (8 * b)) & 0xff;
+            for (int c = 1; c < 16; c++) {
+                acc += p[c + 15] * p[c + 15] - p[c - 1] * p[c - 1];
+                hs[r][c0 + c] = acc;
             }
         }
-        // unrounded vertical taps at columns X-2 .. X+6 (g index 2 .. 10)
-        int v[9];
+    }
+    __syncthreads();
+    // 3. bytes and half-pel samples, 4 columns per thread task
+    for (int t = tid; t < PL_TY * (PL_TX / 4); t += 256) {
+        const int r = t >> 4, cq = 4 * (t & 15);
+        const int Y = Y0 + r, X = X0 + cq;
+        if (Y >= PH || X >= PW) continue;  // PW is a multiple of 16: a task is inside or outside whole
+        const unsigned char* row = &px[r + 2][cq + 2];  // sample (Y, X)
+        unsigned og = 0, ob = 0, oh = 0, oj = 0;
 #pragma unroll
-        for (int c = 0; c < 9; c++) v[c] = tap6(g[0][c + 2], g[1][c + 2], g[2][c + 2], g[3][c + 2], g[4][c + 2], g[5][c + 2]);
-        unsigned ob = 0, oh = 0, oj = 0;
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-            const int x = t + 4;  // g index of column X + t
-            const int bv = tap6(g[2][x - 2], g[2][x - 1], g[2][x], g[2][x + 1], g[2][x + 2], g[2][x + 3]);
-            ob |= (unsigned)clip_tap(bv, 16, 5) << (8 * t);
-            oh |= (unsigned)clip_tap(v[t + 2], 16, 5) << (8 * t);
-            const int jv = tap6(v[t], v[t + 1], v[t + 2], v[t + 3], v[t + 4], v[t + 5]);
-            oj |= (unsigned)clip_tap(jv, 512, 10) << (8 * t);
+        for (int u = 0; u < 4; u++) {
+            og |= (unsigned)row[u] << (8 * u);
+            const int bv = tap6(row[u - 2], row[u - 1], row[u], row[u + 1], row[u + 2], row[u + 3]);
+            ob |= (unsigned)clip_tap(bv, 16, 5) << (8 * u);
+            const short* v = &vt[r][cq + u];  // columns X+u-2 .. X+u+3
+            oh |= (unsigned)clip_tap(v[2], 16, 5) << (8 * u);
+            const int jv = tap6(v[0], v[1], v[2], v[3], v[4], v[5]);
+            oj |= (unsigned)clip_tap(jv, 512, 10) << (8 * u);
         }
         const size_t o = (size_t)Y * rstride + X;
+        *reinterpret_cast<unsigned*>(refp + o) = og;
         *reinterpret_cast<unsigned*>(hpel + o) = ob;
         *reinterpret_cast<unsigned*>(hpel + plane_size + o) = oh;
         *reinterpret_cast<unsigned*>(hpel + 2 * plane_size + o) = oj;
     }
-}
-
-// ---------------------------------------------------------------------------
-// Window energies: E(Y, X) = sum over the 16x16 block at padded position
-// (Y, X) of the squared reference samples, the B^2 term of every candidate's
-// SSD = A^2 + B^2 - 2 sum(ab).  One int per padded position (same row stride
-// as the byte planes), for Y <= PH - 16 and X <= PW - 16.  A CTA makes a
-// 64 x 64 tile: its 79 x 80 input bytes staged by words, horizontal 16-sums
-// of squares per row, then vertical 16-sums per column, 16 outputs per thread
-// (sliding sums) with coalesced stores.
-constexpr int EN_T = 64;
-
-__global__ void __launch_bounds__(256) k_full_energy(const unsigned char* __restrict__ refp, int rstride, int PH,
-                                                     int* __restrict__ energy)
-{
-    __shared__ __align__(16) unsigned char px[EN_T + 15][EN_T + 16];
-    __shared__ int hs[EN_T + 15][EN_T];
-    const int X0 = blockIdx.x * EN_T, Y0 = blockIdx.y * EN_T, PW = rstride, wq = PW / 4;
-    constexpr int RW = (EN_T + 16) / 4;  // words per staged row
-    for (int i = threadIdx.x; i < (EN_T + 15) * RW; i += 256) {
-        const int r = i / RW, c = i - r * RW;
-        const int y = min(Y0 + r, PH - 1), w = min(X0 / 4 + c, wq - 1);
-        reinterpret_cast<unsigned*>(&px[r][0])[c] = __ldg(reinterpret_cast<const unsigned*>(refp + (size_t)y * rstride) + w);
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < (EN_T + 15) * (EN_T / 16); t += 256) {
-        const int r = t >> 2, c0 = 16 * (t & 3);
-        const unsigned char* p = &px[r][c0];
-        int acc = 0;
+    if (energy) {  // vertical 16-sums: column c, 16 rows per task
+        for (int t = tid; t < PL_TX * (PL_TY / 16); t += 256) {
+            const int c = t & (PL_TX - 1), r0 = 16 * (t >> 6), X = X0 + c;
+            int acc = 0;
 #pragma unroll
-        for (int d = 0; d < 16; d++) acc += p[d] * p[d];
-        hs[r][c0] = acc;
+            for (int d = 0; d < 16; d++) acc += hs[r0 + d][c];
 #pragma unroll
-        for (int c = 1; c < 16; c++) {
-            acc += p[c + 15] * p[c + 15] - p[c - 1] * p[c - 1];
-            hs[r][c0 + c] = acc;
-        }
-    }
-    __syncthreads();
-    {
-        const int c = threadIdx.x & (EN_T - 1), r0 = 16 * (threadIdx.x >> 6), X = X0 + c;
-        int acc = 0;
-#pragma unroll
-        for (int d = 0; d < 16; d++) acc += hs[r0 + d][c];
-#pragma unroll
-        for (int r = r0; r < r0 + 16; r++) {
-            if (r > r0) acc += hs[r + 15][c] - hs[r - 1][c];
-            const int Y = Y0 + r;
-            if (X <= PW - 16 && Y <= PH - 16) energy[(size_t)Y * rstride + X] = acc;
+            for (int r = r0; r < r0 + 16; r++) {
+                if (r > r0) acc += hs[r + 15][c] - hs[r - 1][c];
+                const int Y = Y0 + r;
+                if (X <= PW - 16 && Y <= PH - 16) energy[(size_t)Y * rstride + X] = acc;
+            }
         }
     }
 }
@@ -566,23 +543,12 @@ int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v)
 
 int full_planes_launch(vppgpu_ctx* ctx, const FullArgs& args)
 {
-    {
-        long long work = (long long)((args.W + 2 * PAD) / 4) * (args.H + 2 * PAD) + (long long)args.W * args.H / 4;
-        int grid = (int)((work + 255) / 256);
-        if (grid > ctx->sm_count * 16) grid = ctx->sm_count * 16;
-        k_full_pack<<<grid, 256, 0, ctx->stream>>>(args.job, args.W, args.H, (unsigned char*)args.src8,
-                                                   (unsigned char*)args.refp, args.rstride, &args.ctrl->status);
-        VPP_CHECK_LAUNCH(ctx);
-    }
-    {
-        const int PW = args.W + 2 * PAD, PH = args.H + 2 * PAD;
-        long long work = (long long)(PW / 4) * PH;
-        int grid = (int)((work + 255) / 256);
-        if (grid > ctx->sm_count * 16) grid = ctx->sm_count * 16;
-        k_full_halfpel<<<grid, 256, 0, ctx->stream>>>(args.refp, args.rstride, PW, PH, (unsigned char*)args.hpel,
-                                                      args.plane_size);
-        VPP_CHECK_LAUNCH(ctx);
-    }
+    const int PW = args.W + 2 * PAD, PH = args.H + 2 * PAD;
+    dim3 grid((PW + PL_TX - 1) / PL_TX, (PH + PL_TY - 1) / PL_TY);
+    k_full_planes<<<grid, 256, 0, ctx->stream>>>(args.job, args.W, args.H, args.rstride, (unsigned char*)args.src8,
+                                                 (unsigned char*)args.refp, (unsigned char*)args.hpel, args.plane_size,
+                                                 const_cast<int*>(args.energy), &args.ctrl->status);
+    VPP_CHECK_LAUNCH(ctx);
     return VPPGPU_OK;
 }
 
@@ -638,22 +604,12 @@ int search_maps_encode(const FullArgs& a, SearchMaps* maps)
     return rc;
 }
 
-int full_energy_launch(vppgpu_ctx* ctx, const FullArgs& args)
-{
-    const int PW = args.W + 2 * PAD, PH = args.H + 2 * PAD;
-    dim3 grid((PW - 16) / EN_T + 1, (PH - 16) / EN_T + 1);
-    k_full_energy<<<grid, 256, 0, ctx->stream>>>(args.refp, args.rstride, PH, const_cast<int*>(args.energy));
-    VPP_CHECK_LAUNCH(ctx);
-    return VPPGPU_OK;
-}
-
 int full_launch(vppgpu_ctx* ctx, const FullArgs& args, const SearchMaps& maps, int nmb, int resolve_grid,
                 cudaEvent_t* ev)
 {
     if (ev) VPP_CUDA(cudaEventRecord(ev[0], ctx->stream));
-    int rc = full_planes_launch(ctx, args);
+    int rc = full_planes_launch(ctx, args);  // with the block energies (args.energy)
     if (rc) return rc;
-    if ((rc = full_energy_launch(ctx, args))) return rc;
     if (ev) VPP_CUDA(cudaEventRecord(ev[1], ctx->stream));
     k_full_search<false><<<search_grid(ctx, nmb), SEARCH_THREADS, sizeof(SearchSmem), ctx->stream>>>(args, maps);
     VPP_CHECK_LAUNCH(ctx);

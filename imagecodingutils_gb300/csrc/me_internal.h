@@ -148,8 +148,6 @@ int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v);
 // Motion-compensated luma residual of the last estimate's planes at vectors d_mv.
 int full_residual_launch(vppgpu_ctx* ctx, const FullArgs& args, const int* d_mv, short* d_res);
 
-// Block energies of the padded reference (args.energy) for the SSD search.
-int full_energy_launch(vppgpu_ctx* ctx, const FullArgs& args);
 // 2-D tensor maps the search kernel stages its tiles with (one TMA copy each
 // per macroblock): the padded reference (80 x 78 window box), the packed
 // input (16 x 16 template box) and the block energies (64 x 63 box).  They
@@ -159,7 +157,8 @@ struct SearchMaps {
 };
 int search_maps_encode(const FullArgs& args, SearchMaps* maps);
 // Byte-packed input (args.src8), padded reference and its half-pel planes
-// from the int16 planes of args.job.
+// from the int16 planes of args.job, and the block energies when args.energy
+// is set (the SSD full search), in one kernel.
 int full_planes_launch(vppgpu_ctx* ctx, const FullArgs& args);
 // Launch the prediction-dependent tail (sweep 0, relaxation, dictionary
 // precompute, exact wavefront) of an estimate whose search has run.

@@ -157,6 +157,11 @@ int vppgpu_me_get_tuning(vppgpu_me* me, int* tuning4);
  * computations, MBs the wavefront evaluated in full, status bits, included
  * MBs, 0}.  Synchronises the context stream.  No vpp counterpart. */
 int vppgpu_me_last_stats(vppgpu_me* me, int* stats8);
+/* Macroblocks whose final vector changed in each relaxation sweep 1 .. n of
+ * the last estimate (n <= 14; 0 for sweeps that did not run).  Synchronises
+ * the context stream.  No vpp counterpart: a diagnostic of the relaxation
+ * policy (vppgpu_me_set_relax_sweeps). */
+int vppgpu_me_last_relax_changes(vppgpu_me* me, int* changes, int n);
 
 /* Observability, no vpp counterpart.  While enabled, every estimate records
  * CUDA events around its three kernels on the context stream (no host
