@@ -35,7 +35,8 @@ __all__ = [
     "FastForwardDC2x2ITImpl1", "FastInverseDC4x4ITImpl1", "FastInverseDC2x2ITImpl1",
     "FastGpuRGB24toYUV420Converter", "RealYUV420toRGB24Converter", "RealYUV420toRGB24ConverterImpl2",
     "RealYUV420toRGB24ConverterImpl2Ver16", "RealYUV420toRGB24CCIR601Converter",
-    "RealYUV420toRGB24CCIR601ConverterVer16", "MotionCompensatorH264ImplStd", "VppGpuError", "load",
+    "RealYUV420toRGB24CCIR601ConverterVer16", "Fast6BitYUV420toRGB24Converter", "Real6BitYUV420toRGB24Converter",
+    "Fast6BitYUV420toRGB24ZoomConverter", "MotionCompensatorH264ImplStd", "VppGpuError", "load",
 ]
 
 
@@ -785,3 +786,47 @@ class RealYUV420toRGB24CCIR601Converter(_YUV420toRGB24Base):
 class RealYUV420toRGB24CCIR601ConverterVer16(_YUV420toRGB24Base):
     """src/ImageUtils/RealYUV420toRGB24CCIR601ConverterVer16.cpp (the CCIR601 arithmetic)."""
     KIND = _lib.YUV_CCIR601
+
+
+class Fast6BitYUV420toRGB24Converter(_YUV420toRGB24Base):
+    """src/ImageUtils/Fast6BitYUV420toRGB24Converter.cpp: 6-bit samples, integer
+    terms; rotate only (the flip and the chrominance offset are not used)."""
+    KIND = _lib.YUV_FAST_6BIT
+
+
+class Real6BitYUV420toRGB24Converter(_YUV420toRGB24Base):
+    """src/ImageUtils/Real6BitYUV420toRGB24Converter.cpp: 6-bit samples scaled by
+    4, the Real double terms; rotate only."""
+    KIND = _lib.YUV_REAL_6BIT
+
+
+class Fast6BitYUV420toRGB24ZoomConverter(_YUV420toRGB24Base):
+    """src/ImageUtils/Fast6BitYUV420toRGB24ZoomConverter.cpp: 6-bit planes of the
+    constructor's size to an output of SetOutputDimensions' size (even sizes whose
+    source positions stay inside the planes; rotation is not supported, as in the
+    reference)."""
+
+    def __init__(self, width=0, height=0, ctx: Context | None = None):
+        super().__init__(width, height, 0, ctx)
+        self._out_w, self._out_h = 1, 1
+
+    def GetOutputWidth(self):
+        return self._out_w
+
+    def GetOutputHeight(self):
+        return self._out_h
+
+    def SetOutputDimensions(self, width, height):
+        self._out_w, self._out_h = int(width), int(height)
+
+    def Convert(self, pY, pU, pV, pRgb):
+        if self._rotate:
+            return  # the reference's Convert does nothing when rotated
+        for p in (pY, pU, pV):
+            if not isinstance(p, np.ndarray) or p.dtype != np.int16 or not p.flags.c_contiguous:
+                raise TypeError("input planes must be contiguous int16 arrays")
+        if pRgb.dtype != np.uint8 or not pRgb.flags.c_contiguous or pRgb.size != self._out_w * self._out_h * 3:
+            raise TypeError("pRgb must be a contiguous uint8 array of out_width*out_height*3 bytes")
+        check(load().vppgpu_yuv420_to_rgb24_zoom(self._ctx.handle, _ptr(pY), _ptr(pU), _ptr(pV), self._width,
+                                                 self._height, self._out_w, self._out_h, _ptr(pRgb)),
+              "vppgpu_yuv420_to_rgb24_zoom")

@@ -31,7 +31,7 @@ ME_FULL_SAD = 6
 LAYOUT_BLOCKS, LAYOUT_MB16 = 0, 1
 INV_ROWS_FIRST, INV_COLS_FIRST = 0, 1
 RGB_FIXED_POINT, RGB_REAL, RGB_REAL_IMPL2 = 0, 1, 2
-YUV_REAL, YUV_REAL_IMPL2, YUV_CCIR601 = 0, 1, 2
+YUV_REAL, YUV_REAL_IMPL2, YUV_CCIR601, YUV_FAST_6BIT, YUV_REAL_6BIT = 0, 1, 2, 3, 4
 
 # name -> (restype, argtypes); the symbol list is also the export check of the tests
 SIGNATURES = {
@@ -102,6 +102,8 @@ SIGNATURES = {
     "vppgpu_yuv420_to_rgb24": (_I, [_P, _I, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "vppgpu_yuv420_to_rgb24_device": (_I, [_P, _I, _P, _P, _P, _I, _I, _I, _I, _I, _P]),
     "vppgpu_yuv420_to_rgb24_frames_device": (_I, [_P, _I, _P, _P, _P, _I, _I, _I, _I, _I, _I, _P]),
+    "vppgpu_yuv420_to_rgb24_zoom": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _P]),
+    "vppgpu_yuv420_to_rgb24_zoom_device": (_I, [_P, _P, _P, _P, _I, _I, _I, _I, _P]),
 }
 
 _lib = None

@@ -403,6 +403,8 @@ int vppgpu_rgb24_to_yuv420_frames_device(vppgpu_ctx* ctx, int kind, const unsign
 #define VPPGPU_YUV_REAL       0  /* RealYUV420toRGB24Converter                               */
 #define VPPGPU_YUV_REAL_IMPL2 1  /* RealYUV420toRGB24ConverterImpl2, ...Impl2Ver16           */
 #define VPPGPU_YUV_CCIR601    2  /* RealYUV420toRGB24CCIR601Converter, ...CCIR601ConverterVer16 */
+#define VPPGPU_YUV_FAST_6BIT  3  /* Fast6BitYUV420toRGB24Converter (6-bit samples; rotate only) */
+#define VPPGPU_YUV_REAL_6BIT  4  /* Real6BitYUV420toRGB24Converter (6-bit samples; rotate only) */
 
 /* YUV420toRGBConverter::Convert(pY, pU, pV, pRgb) (include/ImageUtils/YUV420toRGBConverter.h:66;
  * src/ImageUtils/RealYUV420toRGB24Converter.cpp:66-352, RealYUV420toRGB24ConverterImpl2.cpp:94-368,
@@ -410,7 +412,10 @@ int vppgpu_rgb24_to_yuv420_frames_device(vppgpu_ctx* ctx, int kind, const unsign
  * and SetFlip(flip): planar shorts in (Y width*height, U and V (width/2)*(height/2)), packed B,G,R
  * bytes out, width*height*3.  flip writes the rows bottom-up and takes precedence over rotate (the
  * CCIR601 converters ignore it); rotate writes the transpose (pixel (x, y) at byte 3*(x*height + y)).
- * chr_off is used by RealYUV420toRGB24Converter's unrotated paths only, as in the reference. */
+ * chr_off is used by RealYUV420toRGB24Converter's unrotated paths only, as in the reference.
+ * VPPGPU_YUV_FAST_6BIT / VPPGPU_YUV_REAL_6BIT (src/ImageUtils/Fast6BitYUV420toRGB24Converter.cpp:47-245,
+ * Real6BitYUV420toRGB24Converter.cpp:53-246) take 6-bit samples (0..63, scaled by 4 inside) and
+ * ignore chr_off and flip, as their Convert() does. */
 int vppgpu_yuv420_to_rgb24(vppgpu_ctx* ctx, int kind, const short* y, const short* u, const short* v, int width,
                            int height, int chr_off, int rotate, int flip, unsigned char* rgb);
 int vppgpu_yuv420_to_rgb24_device(vppgpu_ctx* ctx, int kind, const short* d_y, const short* d_u, const short* d_v,
@@ -420,6 +425,17 @@ int vppgpu_yuv420_to_rgb24_device(vppgpu_ctx* ctx, int kind, const short* d_y, c
 int vppgpu_yuv420_to_rgb24_frames_device(vppgpu_ctx* ctx, int kind, const short* d_y, const short* d_u,
                                          const short* d_v, int nframes, int width, int height, int chr_off,
                                          int rotate, int flip, unsigned char* d_rgb);
+
+/* Fast6BitYUV420toRGB24ZoomConverter (include/ImageUtils/Fast6BitYUV420toRGB24ZoomConverter.h:33-60,
+ * src/ImageUtils/Fast6BitYUV420toRGB24ZoomConverter.cpp:48-230) with SetOutputDimensions(out_width,
+ * out_height): 6-bit planar shorts of width x height in, out_width x out_height packed B,G,R out,
+ * each output sample a 16-weight smoothing at its nearest source position.  Output sizes must be
+ * even, and every source position (int)(scale * i + 0.5) inside the planes: the reference reads
+ * outside its buffers otherwise (e.g. at a 2x zoom), refused with VPPGPU_ERR_UNSUPPORTED. */
+int vppgpu_yuv420_to_rgb24_zoom(vppgpu_ctx* ctx, const short* y, const short* u, const short* v, int width,
+                                int height, int out_width, int out_height, unsigned char* rgb);
+int vppgpu_yuv420_to_rgb24_zoom_device(vppgpu_ctx* ctx, const short* d_y, const short* d_u, const short* d_v,
+                                       int width, int height, int out_width, int out_height, unsigned char* d_rgb);
 
 #ifdef __cplusplus
 }

@@ -70,6 +70,8 @@ class Oracle:
         L.vo_inv_dc.argtypes = [_P, _I, _I, _I, _I, _P]
         L.vo_dc_quantise_value.argtypes = [C.c_short, _I]
         L.vo_yuv420_to_rgb24.argtypes = [_I, _P, _P, _P, _I, _I, _I, _I, _I, _P]
+        L.vo_yuv420_to_rgb24_6bit.argtypes = [_I, _P, _P, _P, _I, _I, _I, _P]
+        L.vo_yuv420_to_rgb24_zoom.argtypes = [_P, _P, _P, _I, _I, _I, _I, _P]
         L.vo_rgb24_to_yuv420.argtypes = [_I, _P, _I, _I, _I, _I, _P, _P, _P]
         L.vo_bench_me_full.argtypes = [_P, _P, _I, _I, _I, _I, _I, _P]
 
@@ -237,6 +239,24 @@ class Oracle:
         self.lib.vo_yuv420_to_rgb24(kind, _ptr(y), _ptr(u), _ptr(v), w, h, chr_off, rotate, flip, _ptr(out))
         return out
 
+    def yuv_to_rgb_6bit(self, kind, y, u, v, rotate=0):
+        """kind 3 Fast6BitYUV420toRGB24Converter, 4 Real6BitYUV420toRGB24Converter
+        (no flip or chrominance offset): (height, width, 3), or transposed."""
+        h, w = y.shape
+        y, u, v = (np.ascontiguousarray(a, dtype=np.int16) for a in (y, u, v))
+        out = np.zeros((w, h, 3) if rotate else (h, w, 3), np.uint8)
+        self.lib.vo_yuv420_to_rgb24_6bit(kind, _ptr(y), _ptr(u), _ptr(v), w, h, rotate, _ptr(out))
+        return out
+
+    def yuv_to_rgb_zoom(self, y, u, v, out_w, out_h):
+        """Fast6BitYUV420toRGB24ZoomConverter to out_h x out_w x 3."""
+        h, w = y.shape
+        y, u, v = (np.ascontiguousarray(a, dtype=np.int16) for a in (y, u, v))
+        out = np.zeros((out_h, out_w, 3), np.uint8)
+        if self.lib.vo_yuv420_to_rgb24_zoom(_ptr(y), _ptr(u), _ptr(v), w, h, out_w, out_h, _ptr(out)):
+            raise ValueError("output size outside the zoom converter's range")
+        return out
+
     def rgb_to_yuv(self, kind, bgr, chr_off=0, flip=0):
         h, w, _ = bgr.shape
         bgr = np.ascontiguousarray(bgr, dtype=np.uint8)
@@ -279,6 +299,7 @@ class Reference:
         L.ref_inv_dc.argtypes = [_P, _I, _I, _I, _I, _P]
         L.ref_dc_quantise_value.argtypes = [C.c_short, _I]
         L.ref_yuv_to_rgb.argtypes = [_I, _P, _P, _P, _I, _I, _I, _I, _I, _P]
+        L.ref_yuv_to_rgb_zoom.argtypes = [_P, _P, _P, _I, _I, _I, _I, _P]
         L.ref_rgb_to_yuv.argtypes = [_I, _P, _I, _I, _I, _I, _P, _P, _P]
         L.ref_mc_compensate.argtypes = [_I, _I, _I, _P, _P]
 
@@ -367,6 +388,24 @@ class Reference:
         rc = self.lib.ref_yuv_to_rgb(kind, _ptr(y), _ptr(u), _ptr(v), w, h, chr_off, rotate, flip, _ptr(out))
         if rc:
             raise ValueError(f"ref_yuv_to_rgb rc={rc}")
+        return out
+
+    def yuv_to_rgb_6bit(self, kind, y, u, v, rotate=0):
+        """kind 3 Fast6BitYUV420toRGB24Converter, 4 Real6BitYUV420toRGB24Converter."""
+        h, w = y.shape
+        y, u, v = (np.ascontiguousarray(a, dtype=np.int16) for a in (y, u, v))
+        out = np.zeros((w, h, 3) if rotate else (h, w, 3), np.uint8)
+        rc = self.lib.ref_yuv_to_rgb(kind + 2, _ptr(y), _ptr(u), _ptr(v), w, h, 0, rotate, 0, _ptr(out))
+        if rc:
+            raise ValueError(f"ref_yuv_to_rgb rc={rc}")
+        return out
+
+    def yuv_to_rgb_zoom(self, y, u, v, out_w, out_h):
+        """Fast6BitYUV420toRGB24ZoomConverter to out_h x out_w x 3."""
+        h, w = y.shape
+        y, u, v = (np.ascontiguousarray(a, dtype=np.int16) for a in (y, u, v))
+        out = np.zeros((out_h, out_w, 3), np.uint8)
+        self.lib.ref_yuv_to_rgb_zoom(_ptr(y), _ptr(u), _ptr(v), w, h, out_w, out_h, _ptr(out))
         return out
 
     def rgb_to_yuv(self, kind, bgr, chr_off=0, flip=0):

@@ -32,6 +32,9 @@
 #include "RealYUV420toRGB24ConverterImpl2Ver16.h"
 #include "RealYUV420toRGB24CCIR601Converter.h"
 #include "RealYUV420toRGB24CCIR601ConverterVer16.h"
+#include "Fast6BitYUV420toRGB24Converter.h"
+#include "Real6BitYUV420toRGB24Converter.h"
+#include "Fast6BitYUV420toRGB24ZoomConverter.h"
 #include "FastForwardDC4x4ITImpl1.h"
 #include "FastInverseDC4x4ITImpl1.h"
 #include "FastForwardDC2x2ITImpl1.h"
@@ -305,6 +308,8 @@ int ref_yuv_to_rgb(int kind, short* y, short* u, short* v, int w, int h, int chr
     else if (kind == 2) c = new RealYUV420toRGB24CCIR601Converter(w, h);
     else if (kind == 3) c = new RealYUV420toRGB24ConverterImpl2Ver16(w, h);
     else if (kind == 4) c = new RealYUV420toRGB24CCIR601ConverterVer16(w, h);
+    else if (kind == 5) c = new Fast6BitYUV420toRGB24Converter(w, h);
+    else if (kind == 6) c = new Real6BitYUV420toRGB24Converter(w, h);
     else return -1;
     /* the two-argument constructors leave the chrominance offset unset */
     c->SetChrominanceOffset(chr_off);
@@ -312,6 +317,15 @@ int ref_yuv_to_rgb(int kind, short* y, short* u, short* v, int w, int h, int chr
     c->SetFlip(flip != 0);
     c->Convert(y, u, v, rgb);
     delete c;
+    return 0;
+}
+
+/* Fast6BitYUV420toRGB24ZoomConverter to an ow x oh output (no rotation). */
+int ref_yuv_to_rgb_zoom(short* y, short* u, short* v, int w, int h, int ow, int oh, unsigned char* rgb)
+{
+    Fast6BitYUV420toRGB24ZoomConverter c(w, h);
+    c.SetOutputDimensions(ow, oh);
+    c.Convert(y, u, v, rgb);
     return 0;
 }
 

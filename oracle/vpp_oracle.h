@@ -152,6 +152,12 @@ int vo_dc_quantise_value(short val, int qp);
  * (and Ver16); rgb holds width*height*3 bytes. */
 void vo_yuv420_to_rgb24(int kind, const short* py, const short* pu, const short* pv, int w, int h, int chr_off,
                         int rotate, int flip, unsigned char* rgb);
+/* kind 3 Fast6BitYUV420toRGB24Converter, 4 Real6BitYUV420toRGB24Converter */
+void vo_yuv420_to_rgb24_6bit(int kind, const short* py, const short* pu, const short* pv, int w, int h, int rotate,
+                             unsigned char* rgb);
+/* Fast6BitYUV420toRGB24ZoomConverter to an ow x oh output; -1 for sizes it cannot hold */
+int vo_yuv420_to_rgb24_zoom(const short* py, const short* pu, const short* pv, int w, int h, int ow, int oh,
+                            unsigned char* rgb);
 
 /* ------------------------------------------------------------------------ */
 /* RGB24 -> YUV420                                                           */

@@ -28,6 +28,9 @@ inputs and stores inputs and outputs:
                   intra and inter, modes 0/1/2, a custom SetScale, and
                   FastForward4x4ITImpl2::QuantiseValue
 * colour.npz      the three RGB24->YUV420 converters, flip and chroma offsets
+* yuv2rgb.npz     the five Real YUV420->RGB24 converters, every rotate / flip,
+                  the two 6-bit converters (6-bit, wider and +-32767 samples,
+                  both layouts) and the 6-bit zoom converter at several sizes
 * me_1080p.npz    the headline size: Full, MultiresCross / Ver2 / Multires
                   (modes 0, 1, 2), Cross and the integer-pel SAD stage on three
                   frame pairs of the 1920x1080 benchmark sequence at
@@ -290,7 +293,26 @@ def yuv2rgb_fixtures(ref: oracle.Reference) -> dict:
             for rot in (0, 1):
                 for flip in (0, 1):
                     out[f"{name}_k{kind}_r{rot}_f{flip}"] = ref.yuv_to_rgb(kind, y, u, v, -128, rot, flip)
+    # the 6-bit converters: 6-bit samples (their domain), samples past it, and
+    # samples past +-16000 (Real6Bit's per-pixel double path)
+    six = {"six": (r(77, (h, w), 0, 63), r(78, (h // 2, w // 2), 0, 63), r(79, (h // 2, w // 2), 0, 63)),
+           "sixwide": (r(80, (h, w), -300, 600), r(81, (h // 2, w // 2), -200, 500), r(82, (h // 2, w // 2), -200, 500)),
+           "sixhuge": (r(83, (h, w), -32768, 32767), r(84, (h // 2, w // 2), -32768, 32767),
+                       r(85, (h // 2, w // 2), -32768, 32767))}
+    for name, (y, u, v) in six.items():
+        out[f"{name}_y"], out[f"{name}_u"], out[f"{name}_v"] = y, u, v
+        for kind in (3, 4):
+            for rot in (0, 1):
+                out[f"{name}_k{kind}_r{rot}"] = ref.yuv_to_rgb_6bit(kind, y, u, v, rot)
+    # Fast6BitYUV420toRGB24ZoomConverter at output sizes whose source positions stay inside the planes
+    y, u, v = six["six"]
+    out["zoom_sizes"] = np.array(ZOOM_SIZES, np.int32)
+    for ow, oh in ZOOM_SIZES:
+        out[f"zoom_{ow}x{oh}"] = ref.yuv_to_rgb_zoom(y, u, v, ow, oh)
     return out
+
+
+ZOOM_SIZES = [(64, 48), (96, 72), (32, 24), (100, 50), (48, 36), (66, 94)]
 
 
 def colour_fixtures(ref: oracle.Reference) -> dict:

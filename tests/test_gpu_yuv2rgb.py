@@ -105,6 +105,71 @@ def test_yuv_to_rgb_argument_checks(vpp, ctx):
     a = np.zeros(64, np.int16)
     o = np.zeros(64 * 3, np.uint8)
     p = C.c_void_p(a.ctypes.data)
-    assert L.vppgpu_yuv420_to_rgb24(ctx.handle, 3, p, p, p, 8, 8, 0, 0, 0, C.c_void_p(o.ctypes.data)) != 0
+    assert L.vppgpu_yuv420_to_rgb24(ctx.handle, 5, p, p, p, 8, 8, 0, 0, 0, C.c_void_p(o.ctypes.data)) != 0  # no kind 5
     assert L.vppgpu_yuv420_to_rgb24(ctx.handle, 1, p, p, p, 7, 8, 0, 0, 0, C.c_void_p(o.ctypes.data)) != 0
     assert L.vppgpu_yuv420_to_rgb24(ctx.handle, 1, None, p, p, 8, 8, 0, 0, 0, C.c_void_p(o.ctypes.data)) != 0
+
+
+SIX = [("Fast6BitYUV420toRGB24Converter", 3), ("Real6BitYUV420toRGB24Converter", 4)]
+
+
+@pytest.mark.parametrize("cls,kind", SIX)
+def test_six_bit_against_golden(vpp, ctx, golden, cls, kind):
+    """The 6-bit converters: 6-bit samples, wider ones, and samples past
+    +-16000 (Real6Bit's double path), rows and transpose; flip is ignored."""
+    g = golden("yuv2rgb.npz")
+    for name in ("six", "sixwide", "sixhuge"):
+        y, u, v = g[f"{name}_y"], g[f"{name}_u"], g[f"{name}_v"]
+        h, w = y.shape
+        c = getattr(vpp, cls)(w, h, ctx=ctx)
+        for rot in (0, 1):
+            c.SetRotate(rot)
+            c.SetFlip(1)
+            want = g[f"{name}_k{kind}_r{rot}"]
+            out = np.zeros(w * h * 3, np.uint8)
+            c.Convert(y, u, v, out)
+            np.testing.assert_array_equal(out.reshape(want.shape), want, err_msg=f"{name} r{rot}")
+
+
+@pytest.mark.parametrize("cls,kind", SIX)
+def test_six_bit_1080p_against_oracle(vpp, ctx, orc, cls, kind):
+    from imagecodingutils_gb300 import synth
+    w, h = 1920, 1080
+    r = lambda seed, shape: ((synth.splitmix64(seed, int(np.prod(shape))) % np.uint64(64)).astype(np.int16)
+                             .reshape(shape))
+    y, u, v = r(90 + kind, (h, w)), r(91 + kind, (h // 2, w // 2)), r(92 + kind, (h // 2, w // 2))
+    c = getattr(vpp, cls)(w, h, ctx=ctx)
+    for rot in (0, 1):
+        c.SetRotate(rot)
+        out = np.zeros(w * h * 3, np.uint8)
+        c.Convert(y, u, v, out)
+        want = orc.yuv_to_rgb_6bit(kind, y, u, v, rot)
+        np.testing.assert_array_equal(out.reshape(want.shape), want)
+
+
+def test_zoom_against_golden_and_oracle(vpp, ctx, golden, orc):
+    from imagecodingutils_gb300 import _lib, synth
+    g = golden("yuv2rgb.npz")
+    ZOOM_SIZES = [tuple(int(x) for x in p) for p in g["zoom_sizes"]]
+    y, u, v = g["six_y"], g["six_u"], g["six_v"]
+    h, w = y.shape
+    c = vpp.Fast6BitYUV420toRGB24ZoomConverter(w, h, ctx=ctx)
+    for ow, oh in ZOOM_SIZES:
+        c.SetOutputDimensions(ow, oh)
+        out = np.zeros(ow * oh * 3, np.uint8)
+        c.Convert(y, u, v, out)
+        np.testing.assert_array_equal(out.reshape(oh, ow, 3), g[f"zoom_{ow}x{oh}"], err_msg=f"{ow}x{oh}")
+    c.SetOutputDimensions(2 * w, 2 * h)  # past the planes in the reference: refused
+    with pytest.raises(vpp.VppGpuError) as e:
+        c.Convert(y, u, v, np.zeros(4 * w * h * 3, np.uint8))
+    assert e.value.status == _lib.ERR_UNSUPPORTED
+    # a larger frame against the oracle: 1920x1080 to 1440x810 (3/4)
+    W, H = 1920, 1080
+    r = lambda seed, shape: ((synth.splitmix64(seed, int(np.prod(shape))) % np.uint64(64)).astype(np.int16)
+                             .reshape(shape))
+    y, u, v = r(95, (H, W)), r(96, (H // 2, W // 2)), r(97, (H // 2, W // 2))
+    c = vpp.Fast6BitYUV420toRGB24ZoomConverter(W, H, ctx=ctx)
+    c.SetOutputDimensions(1440, 810)
+    out = np.zeros(1440 * 810 * 3, np.uint8)
+    c.Convert(y, u, v, out)
+    np.testing.assert_array_equal(out.reshape(810, 1440, 3), orc.yuv_to_rgb_zoom(y, u, v, 1440, 810))

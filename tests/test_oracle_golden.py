@@ -130,6 +130,25 @@ def test_yuv_to_rgb_matches_reference(orc, golden):
                                                   g[f"{name}_k{kind}_r{rot}_f{flip}"], err_msg=f"{name} k{kind}")
 
 
+def test_six_bit_yuv_to_rgb_matches_reference(orc, golden):
+    """Fast6BitYUV420toRGB24Converter (kind 3) and Real6BitYUV420toRGB24Converter
+    (kind 4) on 6-bit samples, samples past that range and samples past +-16000,
+    both layouts; Fast6BitYUV420toRGB24ZoomConverter at several output sizes."""
+    g = golden("yuv2rgb.npz")
+    ZOOM_SIZES = [tuple(int(x) for x in p) for p in g["zoom_sizes"]]
+    for name in ("six", "sixwide", "sixhuge"):
+        y, u, v = g[f"{name}_y"], g[f"{name}_u"], g[f"{name}_v"]
+        for kind in (3, 4):
+            for rot in (0, 1):
+                np.testing.assert_array_equal(orc.yuv_to_rgb_6bit(kind, y, u, v, rot), g[f"{name}_k{kind}_r{rot}"],
+                                              err_msg=f"{name} k{kind} r{rot}")
+    y, u, v = g["six_y"], g["six_u"], g["six_v"]
+    for ow, oh in ZOOM_SIZES:
+        np.testing.assert_array_equal(orc.yuv_to_rgb_zoom(y, u, v, ow, oh), g[f"zoom_{ow}x{oh}"], err_msg=f"{ow}x{oh}")
+    with pytest.raises(ValueError):  # a 2x zoom: the reference reads past its planes
+        orc.yuv_to_rgb_zoom(y, u, v, 2 * y.shape[1], 2 * y.shape[0])
+
+
 def test_colour_matches_reference(orc, golden):
     g = golden("colour.npz")
     for kind in (0, 1, 2):
