@@ -676,6 +676,7 @@ def run_full_only(args, torch, _lib, L, ctx, dev, frames):
     d_mv = torch.empty((NMB, 2), dtype=torch.int16, device=dev)
     h = C.c_void_p()
     _lib.check(L.vppgpu_me_create(ctx.handle, _lib.ME_FULL, W, H, MOTION_RANGE, C.byref(h)), "vppgpu_me_create")
+    tuning = None if args.no_autotune else autotune(L, _lib, h, d, TUNE_PAIRS)
     _lib.check(L.vppgpu_me_set_timing(h, 1), "vppgpu_me_set_timing")
     for t in range(args.warmup + args.steps):
         i = t % (NFRAMES - 1)
@@ -687,7 +688,8 @@ def run_full_only(args, torch, _lib, L, ctx, dev, frames):
     stage = (C.c_double * 4)()
     _lib.check(L.vppgpu_me_timing_stages(h, C.byref(n), stage), "vppgpu_me_timing_stages")
     L.vppgpu_me_destroy(h)
-    return {"estimates": n.value, "kernel_ms_per_frame": {k: stage[i] / max(n.value, 1) for i, k in enumerate(STAGES)},
+    return {"estimates": n.value, "autotune": tuning,
+            "kernel_ms_per_frame": {k: stage[i] / max(n.value, 1) for i, k in enumerate(STAGES)},
             "workload": f"MotionEstimatorH264ImplFull, {W}x{H}, motionRange {MOTION_RANGE}, stage events"}
 
 
