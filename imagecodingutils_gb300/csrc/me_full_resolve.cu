@@ -828,7 +828,9 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
         if (nchunks > 1) issue(1);
     }
     int issued = min(2, nchunks), consumed = 0;  // chunks of this warp
-    int o1 = 0, o2 = 0, o3 = 0;  // this lane's outputs of steps t-1, t-2, t-3
+    // o1: this lane's output of step t-1 (its left neighbour at step t); s1, s2, s3: lane l-1's outputs of
+    // steps t-1, t-2, t-3 (above-right, above, above-left at step t), received one shuffle per step
+    int o1 = 0, s1 = 0, s2 = 0, s3 = 0;
     int pb = 0, pc = 0;          // lane 0: row above at columns c-1 and c (previous step's B and C)
     int misses = 0;
     bool stop = false;
@@ -841,7 +843,8 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
                     stop = true;
                     break;
                 }
-            if (__any_sync(0xffffffffu, stop)) {
+            // a wait that ran out here, or lane 0's wait on the row above in the last chunk
+            if (__any_sync(0xffffffffu, stop || *((volatile int*)&abort_flag))) {
                 if (lane == 0) {
                     abort_flag = 1;
                     atomicOr(&a.ctrl->status, ST_TIMEOUT);
@@ -857,17 +860,19 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
         }
         const int c = t - 2 * lane;
         const bool active = row_ok && c >= 0 && c < cols;
-        int B = __shfl_up_sync(0xffffffffu, o2, 1);
-        int C = __shfl_up_sync(0xffffffffu, o1, 1);
-        int D = __shfl_up_sync(0xffffffffu, o3, 1);
-        if (lane == 0 && active) {
-            if (w > 0) {
-                // warp w-1's lane 31 stores the row above: only column c+1 is new
+        const WaveRec& rec = mybuf[((ci & 1) * kChunk + ti) * 32 + lane];
+        int B = s2, C = s1, D = s3;
+        if (w > 0) {
+            if (lane == 0 && active) {
+                // warp w-1's lane 31 stores the row above: only column c+1 is new.  A wait that runs
+                // out leaves this step's neighbours as they are (indices do not depend on them) and
+                // ends the warp at the next chunk boundary.
                 if (c == 0) {
                     long long it = 0;
                     while ((pc = above[0]) == kEmpty)
                         if (++it > a.spin_limit || *((volatile int*)&abort_flag)) {
                             stop = true;
+                            abort_flag = 1;
                             break;
                         }
                     pb = 0;
@@ -878,6 +883,7 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
                     while ((nc = above[c + 1]) == kEmpty)
                         if (++it > a.spin_limit || *((volatile int*)&abort_flag)) {
                             stop = true;
+                            abort_flag = 1;
                             break;
                         }
                 }
@@ -886,43 +892,29 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
                 C = nc;
                 pb = pc;
                 pc = nc;
-            } else if (band0 > 0) {
-                B = __ldcg(above_g + c);
-                C = c + 1 < cols ? __ldcg(above_g + c + 1) : 0;
-                D = c >= 1 ? __ldcg(above_g + c - 1) : 0;
             }
+        } else if (band0 > 0 && lane == 0 && active) {
+            B = __ldcg(above_g + c);
+            C = c + 1 < cols ? __ldcg(above_g + c + 1) : 0;
+            D = c >= 1 ? __ldcg(above_g + c - 1) : 0;
         }
-        if (w > 0 && __any_sync(0xffffffffu, stop)) {
-            if (lane == 0) {
-                abort_flag = 1;
-                atomicOr(&a.ctrl->status, ST_TIMEOUT);
-            }
-            break;
-        }
-        int out = 0, key = 0;
-        bool hit = false;
-        if (active) {
-            const WaveRec& rec = mybuf[((ci & 1) * kChunk + ti) * 32 + lane];
-            key = median_packed(rec.av, o1, B, C, D);
-            unsigned e;
-            const bool inr = wave_encode(key, &e);
-            int h1, h2;
-            wave_buckets(e, &h1, &h2);
-            const uint4 b1 = reinterpret_cast<const uint4*>(rec.slot)[h1];
-            const uint4 b2 = reinterpret_cast<const uint4*>(rec.slot)[h2];
-            int code = -1;
-            const unsigned m = 0xff3fffffu;
-            if ((b1.x & m) == e) code = (int)((b1.x >> 22) & 3u);
-            if ((b1.y & m) == e) code = (int)((b1.y >> 22) & 3u);
-            if ((b1.z & m) == e) code = (int)((b1.z >> 22) & 3u);
-            if ((b1.w & m) == e) code = (int)((b1.w >> 22) & 3u);
-            if ((b2.x & m) == e) code = (int)((b2.x >> 22) & 3u);
-            if ((b2.y & m) == e) code = (int)((b2.y >> 22) & 3u);
-            if ((b2.z & m) == e) code = (int)((b2.z >> 22) & 3u);
-            if ((b2.w & m) == e) code = (int)((b2.w >> 22) & 3u);
-            hit = inr && code >= 0;
-            out = code == 0 ? rec.spec : (code == 1 ? key : 0);
-        }
+        // the record lookup, straight-line in every lane (an inactive lane's record slot holds data of
+        // some step, its result is not stored)
+        const int key = median_packed(rec.av, o1, B, C, D);
+        unsigned e;
+        const bool inr = wave_encode(key, &e);
+        int h1, h2;
+        wave_buckets(e, &h1, &h2);
+        const uint4 b1 = reinterpret_cast<const uint4*>(rec.slot)[h1];
+        const uint4 b2 = reinterpret_cast<const uint4*>(rec.slot)[h2];
+        // a table holds each prediction once: the matching entry's code + 1, else 0
+        const unsigned m = 0xff3fffffu;
+        auto code1 = [&](unsigned v) { return (v & m) == e ? ((v >> 22) & 3u) + 1u : 0u; };
+        const unsigned k1 = max(max(code1(b1.x), code1(b1.y)), max(code1(b1.z), code1(b1.w)));
+        const unsigned k2 = max(max(code1(b2.x), code1(b2.y)), max(code1(b2.z), code1(b2.w)));
+        const unsigned k = max(k1, k2);
+        const bool hit = inr && k != 0u;
+        int out = k == 1u ? rec.spec : (k == 2u ? key : 0);
         unsigned miss = __ballot_sync(0xffffffffu, active && !hit);
         if (miss) {
             misses += __popc(miss);
@@ -931,11 +923,11 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
                 miss &= miss - 1;
                 const int fkey = __shfl_sync(0xffffffffu, key, f);
                 const int fk = (32 * band + f) * cols + (t - 2 * f);
-                const int4 rec = evaluate<kEst>(a, fk, mv_x(fkey), mv_y(fkey), lane);
+                const int4 rv = evaluate<kEst>(a, fk, mv_x(fkey), mv_y(fkey), lane);
                 if (lane == f) {
-                    out = rec.z;
-                    a.final_mv[fk] = rec.z;
-                    a.final_dist[fk] = rec.w;
+                    out = rv.z;
+                    a.final_mv[fk] = rv.z;
+                    a.final_dist[fk] = rv.w;
                 }
             } while (miss);
         }
@@ -946,9 +938,10 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
                 a.final_mv[r * cols + c] = out;  // the next launch's first band reads this row
             }
         }
-        o3 = o2;
-        o2 = o1;
         o1 = out;
+        s3 = s2;
+        s2 = s1;
+        s1 = __shfl_up_sync(0xffffffffu, out, 1);
     }
     // copies still in flight after an abort land before the CTA leaves; a
     // drain that gives up (only after a timeout) is reported as one too
