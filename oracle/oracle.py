@@ -58,6 +58,8 @@ class Oracle:
         L.vo_me_multires_cross_v2.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_me_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_me_multires.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
+        L.vo_me_multires_cross_v2_lambda.argtypes = [_P, _P, _I, _I, _I, _I, C.c_double, _P, _P, _P, _P,
+                                                     C.POINTER(_L)]
         L.vo_mc_compensate.argtypes = [_P, _I, _I, _I, _P]
         L.vo_add_clip255.argtypes = [_P, _P, C.c_longlong]
         L.vo_sub.argtypes = [_P, _P, C.c_longlong]
@@ -127,6 +129,23 @@ class Oracle:
                              with_ties=False):
         return self._me_pred(self.lib.vo_me_multires_cross_v2, src, ref, motion_range, mode, dist_incl, slice_map,
                              with_ties)
+
+    def me_multires_cross_v2_lambda(self, src, ref, motion_range, lam, mode=1, dist_incl=None, slice_map=None):
+        """Ver2's Estimate(long*, void* lambda): GetBestVector at every level."""
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = self.lib.vo_num_mbs(w, h)
+        mv = np.zeros((nmb, 2), np.int16)
+        dist = np.zeros(nmb, np.int32)
+        avg = _L(0)
+        incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
+        sl = None if slice_map is None else np.ascontiguousarray(slice_map, dtype=np.int32)
+        rc = self.lib.vo_me_multires_cross_v2_lambda(_ptr(src), _ptr(ref), w, h, motion_range, mode, float(lam),
+                                                     _ptr(incl), _ptr(sl), _ptr(mv), _ptr(dist), C.byref(avg))
+        if rc:
+            raise ValueError(f"vo_me_multires_cross_v2_lambda rc={rc}")
+        return mv, dist, avg.value
 
     def me_cross(self, src, ref, motion_range, mode=0, dist_incl=None, slice_map=None, with_ties=False):
         """MotionEstimatorH264ImplCross (mode 0 quarter, 1 half, 2 full pel)."""

@@ -6,6 +6,8 @@
  *     (src/CodecUtils/MotionEstimatorH264ImplMultiresCross.cpp:525-1019)
  *   MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*)
  *     (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:537-1151)
+ *   MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*, void* lambda)
+ *     (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:1162-1742)
  *   MotionEstimatorH264ImplMultires::Estimate
  *     (src/CodecUtils/MotionEstimatorH264ImplMultires.cpp:557-1024)
  *
@@ -25,6 +27,7 @@
  * buffer when its allocation is fresh zeroed memory; the unscaled edge
  * samples are reproduced as they are.
  */
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
 #include "oracle_internal.h"
@@ -541,6 +544,218 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
     out->tie = tie;
 }
 
+/* The candidate lists of the Lagrangian overload: Fifo(5) of doubles
+ * (include/GeneralUtils/Fifo.h), the newest item at 0.  AddFirstIn on an
+ * empty list fills every slot with the item; GetLength is always 5. */
+typedef struct {
+    int x[5], y[5], d[5];
+} mr_fifo;
+
+static void fifo_reset(mr_fifo* f, int x, int y, int d)
+{
+    for (int i = 0; i < 5; i++) {
+        f->x[i] = x;
+        f->y[i] = y;
+        f->d[i] = d;
+    }
+}
+
+static void fifo_push(mr_fifo* f, int x, int y, int d)
+{
+    for (int i = 4; i > 0; i--) {
+        f->x[i] = f->x[i - 1];
+        f->y[i] = f->y[i - 1];
+        f->d[i] = f->d[i - 1];
+    }
+    f->x[0] = x;
+    f->y[0] = y;
+    f->d[0] = d;
+}
+
+/* GetBestVector (include/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.h:168-197):
+ * cost D/norm + lambda*|v - ref| over the five slots; slot 0 is costed at the
+ * current vector (*mx, *my) with lambda * 2^(level+2) / 16, the others with the
+ * raw lambda; strict improvement.  Returns the slot and sets (*mx, *my). */
+static int fifo_best(const mr_fifo* f, double lambda, double norm, int level, int xref, int yref, int* mx, int* my)
+{
+    const double lcl = (lambda * (double)(1 << (level + 2))) / 16.0;
+    int pos = 0;
+    const double mag = (double)((*mx - xref) * (*mx - xref) + (*my - yref) * (*my - yref));
+    double cost = ((double)f->d[0] / norm) + (lcl * sqrt(mag));
+    for (int i = 1; i < 5; i++) {
+        const double m = (double)((f->x[i] - xref) * (f->x[i] - xref) + (f->y[i] - yref) * (f->y[i] - yref));
+        const double c = ((double)f->d[i] / norm) + (lambda * sqrt(m));
+        if (c < cost) {
+            *mx = f->x[i];
+            *my = f->y[i];
+            cost = c;
+            pos = i;
+        }
+    }
+    return pos;
+}
+
+/* The search of MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*, void* lambda)
+ * (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:1237-1676): the
+ * Ver2 search whose every level ends with GetBestVector over the last five
+ * improvements of that level (level 2: norm 16, level 1: 64, level 0: 256,
+ * sub-pel: 256 at level weight 2), each towards the prediction's vector of the
+ * level.  Unlike Estimate(long*), the cross mode's level 1 adds its last
+ * refinement once only (…:1434-1499).  pl = {level-2 x, y, level-1 x, y,
+ * level-0 rounded x, y}; (pcx, pcy) the clamped quarter-pel prediction. */
+static void mr_search_mb_lambda(mr_ctx* c, int mbr, int mbc, const int* pl, int pcx, int pcy, double lambda,
+                                mr_result* out)
+{
+    const int m = 16 * mbr, n = 16 * mbc, p = 8 * mbr, q = 8 * mbc, kk = 4 * mbr, ll = 4 * mbc;
+    mr_ov oin0 = {&c->in0, 16, 16, 0, 0, 0, 0}, oin1 = {&c->in1, 8, 8, 0, 0, 0, 0}, oin2 = {&c->in2, 4, 4, 0, 0, 0, 0};
+    mr_ov oe0 = {&c->e0, 16, 16, 0, 0, 19, 19}, oe1 = {&c->e1, 8, 8, 0, 0, 9, 9}, oe2 = {&c->e2, 4, 4, 0, 0, 5, 5};
+    int mx = 0, my = 0, rmx = 0, rmy = 0, hmx = 0, hmy = 0, qmx, qmy, xl, xr, yu, yd;
+    mr_fifo f;
+    short blk[256];
+    ov_origin(&oin0, n, m);
+    ov_origin(&oe0, n, m);
+    const int zero_d = ov_tsd(&oin0, &oe0, 16);
+
+    if (c->mode == 2) { /* level 2 cross search (…:1287-1370) */
+        ov_origin(&oin2, ll, kk);
+        ov_origin(&oe2, ll, kk);
+        int min2 = ov_tsd(&oin2, &oe2, 4);
+        fifo_reset(&f, 0, 0, min2);
+        mr_range(&c->L2, ll, kk, 0, 0, c->l2_range - 1, &xl, &xr, &yu, &yd);
+        for (int s = c->l2_range / 2; s > 0; s /= 2) {
+            rmx = rmy = 0;
+            for (int k = 0; k < 4; k++) {
+                int i = s * CRY[k], j = s * CRX[k];
+                if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+                ov_origin(&oe2, j + ll + mx, i + kk + my);
+                int d = ov_tsd4_lt(&oin2, &oe2, min2);
+                if (d > min2) continue;
+                if (d == min2 && mr_farther(mx, my, rmx, rmy, j, i, pl[0], pl[1])) continue;
+                min2 = d;
+                rmx = j;
+                rmy = i;
+                fifo_push(&f, j + mx, i + my, d);
+            }
+            mx += rmx;
+            my += rmy;
+        }
+        fifo_best(&f, lambda, 16.0, 2, pl[0], pl[1], &mx, &my);
+        mx <<= 1;
+        my <<= 1;
+    }
+
+    /* level 1 (…:1374-1502) */
+    ov_origin(&oin1, q, p);
+    ov_origin(&oe1, mx + q, my + p);
+    int min1 = ov_tsd(&oin1, &oe1, 8);
+    fifo_reset(&f, mx, my, min1);
+    rmx = rmy = 0;
+    if (c->mode == 2) {
+        mr_range(&c->L1, q, p, mx, my, c->lcl_l1_range, &xl, &xr, &yu, &yd);
+        for (int i = yu; i <= yd; i++)
+            for (int j = xl; j <= xr; j++) {
+                if (!(i || j)) continue;
+                ov_origin(&oe1, j + mx + q, i + my + p);
+                int d = ov_tsd_partial_lt(&oin1, &oe1, 8, min1);
+                if (d > min1) continue;
+                if (d == min1 && mr_farther(mx, my, rmx, rmy, j, i, pl[2], pl[3])) continue;
+                min1 = d;
+                rmx = j;
+                rmy = i;
+                fifo_push(&f, j + mx, i + my, d);
+            }
+        mx += rmx;
+        my += rmy;
+    } else {
+        for (int s = c->l1_range / 2; s > 0; s /= 2) {
+            mr_range(&c->L1, q, p, mx, my, c->lcl_l1_range - 1, &xl, &xr, &yu, &yd);
+            rmx = rmy = 0;
+            for (int k = 0; k < 4; k++) {
+                int i = s * CRY[k], j = s * CRX[k];
+                if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+                ov_origin(&oe1, j + mx + q, i + my + p);
+                int d = ov_tsd_partial_lt(&oin1, &oe1, 8, min1);
+                if (d > min1) continue;
+                if (d == min1 && mr_farther(mx, my, rmx, rmy, j, i, pl[2], pl[3])) continue;
+                min1 = d;
+                rmx = j;
+                rmy = i;
+                fifo_push(&f, j + mx, i + my, d);
+            }
+            mx += rmx;
+            my += rmy;
+        }
+    }
+    fifo_best(&f, lambda, 64.0, 1, pl[2], pl[3], &mx, &my);
+    mx <<= 1;
+    my <<= 1;
+
+    /* level 0 +-2 refinement (…:1503-1574) */
+    int min_d = zero_d;
+    if (mx || my) {
+        ov_origin(&oe0, n + mx, m + my);
+        min_d = ov_tsd(&oin0, &oe0, 16);
+    }
+    fifo_reset(&f, mx, my, min_d);
+    rmx = rmy = 0;
+    mr_range(&c->L0, n, m, mx, my, 2, &xl, &xr, &yu, &yd);
+    for (int i = yu; i <= yd; i++)
+        for (int j = xl; j <= xr; j++) {
+            if (!(i || j)) continue;
+            ov_origin(&oe0, n + mx + j, m + my + i);
+            int d = ov_tsd_partial_lt(&oin0, &oe0, 16, min_d);
+            if (d > min_d) continue;
+            if (d == min_d && mr_farther(mx, my, rmx, rmy, j, i, pl[4], pl[5])) continue;
+            min_d = d;
+            rmx = j;
+            rmy = i;
+            fifo_push(&f, j + mx, i + my, d);
+        }
+    mx += rmx;
+    my += rmy;
+    min_d = f.d[fifo_best(&f, lambda, 256.0, 0, pl[4], pl[5], &mx, &my)];
+
+    /* half then quarter pel in Ver2's window (…:1575-1662), strict improvements */
+    int mvx = mx << 2, mvy = my << 2;
+    fifo_reset(&f, mvx, mvy, min_d);
+    ov_origin(&oe0, n + mx, m + my);
+    mr_load_half_window(c->win, &oe0, 1);
+    for (int k = 0; k < 8; k++) {
+        int qx = 2 * SUBX[k], qy = 2 * SUBY[k];
+        mr_window_read(c->win, qx, qy, blk);
+        int d = blk_tsd16_partial_lt(&oin0, blk, min_d);
+        if (d < min_d) {
+            min_d = d;
+            hmx = qx;
+            hmy = qy;
+            fifo_push(&f, qx + mvx, qy + mvy, d);
+        }
+    }
+    qmx = hmx;
+    qmy = hmy;
+    mr_load_quarter_window(c->win, hmx, hmy);
+    for (int k = 0; k < 8; k++) {
+        int qx = hmx + SUBX[k], qy = hmy + SUBY[k];
+        mr_window_read(c->win, qx, qy, blk);
+        int d = blk_tsd16_partial_lt(&oin0, blk, min_d);
+        if (d < min_d) {
+            min_d = d;
+            qmx = qx;
+            qmy = qy;
+            fifo_push(&f, qx + mvx, qy + mvy, d);
+        }
+    }
+    mvx += qmx;
+    mvy += qmy;
+    /* towards the clamped quarter-pel prediction (…:1664-1677) */
+    min_d = f.d[fifo_best(&f, lambda, 256.0, 2, pcx, pcy, &mvx, &mvy)];
+    out->zero_d = zero_d;
+    out->min_d = min_d;
+    out->mvx = mvx;
+    out->mvy = mvy;
+    out->tie = 0;
+}
+
 static int me_multires_cross_any(int h263, const short* src, const short* ref, int w, int h, int motion_range,
                                  int mode, const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist);
 
@@ -732,7 +947,7 @@ static void mr_search_mb_multires(mr_ctx* c, int mbr, int mbc, const int* pl, mr
  * 4 level 0; the search then depends on the prediction). */
 static int me_multires_pred(int multires, const short* src, const short* ref, int w, int h, int motion_range,
                             int mode, const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist,
-                            long* avg_dist, int* tie_out)
+                            long* avg_dist, int* tie_out, const double* lambda)
 {
     if (!src || !ref || !mv_out || w < 16 || h < 16 || (w % 16) != 0) return -1;
     g_mr_fault = 0;
@@ -756,7 +971,16 @@ static int me_multires_pred(int multires, const short* src, const short* ref, in
             int px0 = px / 4, py0 = py / 4;
             const int px0r = px < 0 ? (px - 2) / 4 : (px + 2) / 4, py0r = py < 0 ? (py - 2) / 4 : (py + 2) / 4;
             mr_result r;
-            if (multires) {
+            if (lambda) {
+                /* the clamped prediction of the last two GetBestVector calls (…:1664-1675) */
+                int cx0 = px0, cy0 = py0;
+                if (cx0 + n > w) cx0 = 16;
+                if (cx0 + n < -16) cx0 = -16;
+                if (cy0 + m > h) cy0 = 16;
+                if (cy0 + m < -16) cy0 = -16;
+                const int pl[6] = {px0r / 2 / 2, py0r / 2 / 2, px0r / 2, py0r / 2, px0r, py0r};
+                mr_search_mb_lambda(&c, mbr, mbc, pl, 4 * cx0 + pxq, 4 * cy0 + pyq, *lambda, &r);
+            } else if (multires) {
                 /* Multires rounds to every level (…Multires.cpp:646-655) */
                 const int pl[6] = {px < 0 ? (px - 8) / 16 : (px + 8) / 16, py < 0 ? (py - 8) / 16 : (py + 8) / 16,
                                    px < 0 ? (px - 4) / 8 : (px + 4) / 8,   py < 0 ? (py - 4) / 8 : (py + 4) / 8,
@@ -788,7 +1012,7 @@ static int me_multires_pred(int multires, const short* src, const short* ref, in
             /* Fifo after pushing zero, pred, best (…:1047-1050) */
             int xs[5] = {r.mvx, px, 0, 0, 0}, ys[5] = {r.mvy, py, 0, 0, 0};
             int ds[5] = {r.min_d, pd, r.zero_d, r.zero_d, r.zero_d};
-            const int pos = vo_best_vector5(xs, ys, ds, multires ? 1.1 : 0.9, 256.0, px, py);
+            const int pos = vo_best_vector5(xs, ys, ds, lambda ? *lambda : (multires ? 1.1 : 0.9), 256.0, px, py);
             if (dist_incl && dist_incl[k]) {
                 included++;
                 total += ds[pos];
@@ -811,7 +1035,20 @@ int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, in
                             long* avg_dist, int* tie_out)
 {
     return me_multires_pred(0, src, ref, w, h, motion_range, mode, dist_incl, slice, mv_out, mb_dist, avg_dist,
-                            tie_out);
+                            tie_out, NULL);
+}
+
+/* MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*, void* lambda)
+ * (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:1162-1742): the
+ * search above with GetBestVector at every level, then the pred-vector check
+ * and the final GetBestVector (…:1704-1710) with the given lambda.  Full
+ * macroblock rows only, as for Estimate(long*). */
+int vo_me_multires_cross_v2_lambda(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                                   double lambda, const unsigned char* dist_incl, const int* slice, short* mv_out,
+                                   int* mb_dist, long* avg_dist)
+{
+    return me_multires_pred(0, src, ref, w, h, motion_range, mode, dist_incl, slice, mv_out, mb_dist, avg_dist, NULL,
+                            &lambda);
 }
 
 /* MotionEstimatorH264ImplMultires::Estimate (src/CodecUtils/MotionEstimatorH264ImplMultires.cpp:557-1024):
@@ -823,5 +1060,5 @@ int vo_me_multires(const short* src, const short* ref, int w, int h, int motion_
                    int* tie_out)
 {
     return me_multires_pred(1, src, ref, w, h, motion_range, mode, dist_incl, slice, mv_out, mb_dist, avg_dist,
-                            tie_out);
+                            tie_out, NULL);
 }

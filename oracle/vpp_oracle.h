@@ -102,6 +102,15 @@ int vo_me_multires_cross_v2(const short* src, const short* ref, int w, int h, in
                             const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist,
                             long* avg_dist, int* tie_out);
 
+/* MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*, void* lambda)
+ * (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:1162-1742):
+ * GetBestVector (MultiresCrossVer2.h:168-197) over the last five improvements
+ * of every search level, then the pred-vector check and the final choice with
+ * the given lambda.  Other arguments as above. */
+int vo_me_multires_cross_v2_lambda(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                                   double lambda, const unsigned char* dist_incl, const int* slice, short* mv_out,
+                                   int* mb_dist, long* avg_dist);
+
 /* MotionEstimatorH264ImplMultires::Estimate
  * (src/CodecUtils/MotionEstimatorH264ImplMultires.cpp:557-1024): full searches
  * at levels 2 and 1, +-2 at level 0, sub-pel in the MultiresCross-style

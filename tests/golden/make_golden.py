@@ -15,6 +15,9 @@ inputs and stores inputs and outputs:
 * me_mrc2.npz     MotionEstimatorH264ImplMultiresCrossVer2 vectors and
                   avgDistortion, modes 0/1/2, with and without
                   pDistortionIncluded (pan and integer-shift content)
+* me_mrc2_lambda.npz  Ver2's Estimate(long*, void* lambda): the me_mrc2 cases
+                  at lambdas 0, 0.9, 2.5 and 20 (modes 0/1/2), and the 1080p
+                  benchmark pair 0 at lambdas 0.9 and 4 (modes 1/2)
 * me_mr.npz       MotionEstimatorH264ImplMultires, the same cases as me_mrc2
 * me_full_sad.npz the integer-pel stage of MotionEstimatorH264ImplFull with
                   its MEH264IF_ABS_DIFF distortion (SAD): the QCIF +-16 shifted
@@ -38,7 +41,7 @@ inputs and stores inputs and outputs:
                   SHA-256)
 
 Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
-names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mr me_cross me_h263mrc mc
+names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc mc
 transform dc yuv2rgb colour, default all)
 """
 from __future__ import annotations
@@ -185,6 +188,38 @@ def mrc2_fixtures(ref: oracle.Reference, kind: str = "multires_cross_v2") -> dic
             assert np.array_equal(mv, mvi) and avg == 0
             out[f"{name}_m{mode}_mv"] = mv
             out[f"{name}_m{mode}_avg"] = np.array([avgi], np.int64)
+    return out
+
+
+LAMBDAS = (0.0, 0.9, 2.5, 20.0)
+
+
+def mrc2_lambda_fixtures(ref: oracle.Reference) -> dict:
+    """Ver2's Estimate(long*, void* lambda) on the me_mrc2 cases at LAMBDAS
+    (modes 0/1/2, with the me_mrc2 inclusion map; the frames are stored in
+    me_mrc2.npz only), and on pair 0 of the 1080p
+    benchmark sequence at motionRange 128, modes 1 and 2, lambdas 0.9 and 4."""
+    out = {"lambdas": np.array(LAMBDAS, np.float64)}
+    for name, w, h, mr, seed, gen in MRC2_CASES:
+        fr = (synth.shift_sequence if gen == "shift" else synth.pan_sequence)(seed, w, h, 2)
+        src, rf = fr[1], fr[0]
+        nmb = (w // 16) * (h // 16)
+        incl = (np.arange(nmb) % 3 != 0).astype(np.uint8)
+        # the frames, meta and inclusion map are those of me_mrc2.npz
+        for mode in (0, 1, 2):
+            for li, lam in enumerate(LAMBDAS):
+                mv, avg = ref.me("multires_cross_v2", src, rf, mr, mode=mode, dist_incl=incl, lam=lam)
+                out[f"{name}_m{mode}_l{li}_mv"] = mv
+                out[f"{name}_m{mode}_l{li}_avg"] = np.array([avg], np.int64)
+    fr, digest = hd_frames()
+    out["hd_meta"] = np.array([HD_SEED, HD_W, HD_H, HD_RANGE, 0], np.int32)
+    out["hd_frames_sha256"] = digest
+    incl = np.ones((HD_W // 16) * (HD_H // 16), np.uint8)
+    for mode in (1, 2):
+        for lam in (0.9, 4.0):
+            mv, avg = ref.me("multires_cross_v2", fr[1], fr[0], HD_RANGE, mode=mode, dist_incl=incl, lam=lam)
+            out[f"hd_m{mode}_lam{lam:g}_mv"] = mv
+            out[f"hd_m{mode}_lam{lam:g}_avg"] = np.array([avg], np.int64)
     return out
 
 
@@ -373,6 +408,7 @@ def main() -> None:
     ref = oracle.Reference()
     makers = {"me_1080p": hd_fixtures,
               "me_full": me_fixtures, "me_full_sad": sad_fixtures, "me_mrc": mrc_fixtures, "me_mrc2": mrc2_fixtures,
+              "me_mrc2_lambda": mrc2_lambda_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "me_cross": lambda r: mrc2_fixtures(r, "cross"),
               "me_h263mrc": lambda r: mrc_fixtures(r, "h263_multires_cross", H263_CASES),
               "mc": mc_fixtures,

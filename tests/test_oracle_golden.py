@@ -256,6 +256,55 @@ def test_me_multires_cross_v2_matches_reference(orc, golden, case, mode):
 
 @pytest.mark.parametrize("case", MRC2_CASES)
 @pytest.mark.parametrize("mode", [0, 1, 2])
+def test_me_multires_cross_v2_lambda_matches_reference(orc, golden, case, mode):
+    """Ver2's Estimate(long*, void* lambda) at lambdas 0, 0.9, 2.5 and 20:
+    GetBestVector at every level, then the final choice with that lambda."""
+    g, gl = golden("me_mrc2.npz"), golden("me_mrc2_lambda.npz")
+    mr = int(g[f"{case}_meta"][2])
+    src = g[f"{case}_src"].astype(np.int16)
+    ref = g[f"{case}_ref"].astype(np.int16)
+    plain = orc.me_multires_cross_v2(src, ref, mr, mode=mode)[0]
+    differs = 0
+    for li, lam in enumerate(gl["lambdas"]):
+        mv, _, avg = orc.me_multires_cross_v2_lambda(src, ref, mr, float(lam), mode=mode, dist_incl=g[f"{case}_incl"])
+        np.testing.assert_array_equal(mv, gl[f"{case}_m{mode}_l{li}_mv"], err_msg=f"lambda {lam}")
+        assert avg == int(gl[f"{case}_m{mode}_l{li}_avg"][0])
+        differs += int((mv != plain).any(axis=1).sum())
+    if case != "small_r32":
+        assert differs > 0  # the overload is not Estimate(long*) under another name
+
+
+def test_me_multires_cross_v2_lambda_1080p_matches_reference(orc, hd_golden, golden):
+    """The lambda overload on pair 0 of the 1080p benchmark sequence."""
+    gl = golden("me_mrc2_lambda.npz")
+    fr, mr = hd_golden["frames"], hd_golden["motion_range"]
+    assert gl["hd_frames_sha256"].tobytes() == hd_golden["g"]["frames_sha256"].tobytes()
+    incl = np.ones((hd_golden["w"] // 16) * (hd_golden["h"] // 16), np.uint8)
+    for mode in (1, 2):
+        for lam in (0.9, 4.0):
+            mv, _, avg = orc.me_multires_cross_v2_lambda(fr[1], fr[0], mr, lam, mode=mode, dist_incl=incl)
+            np.testing.assert_array_equal(mv, gl[f"hd_m{mode}_lam{lam:g}_mv"], err_msg=f"mode {mode} lambda {lam}")
+            assert avg == int(gl[f"hd_m{mode}_lam{lam:g}_avg"][0])
+
+
+@ref_available
+@pytest.mark.parametrize("seed,w,h,mr,mode,lam", [(56, 176, 144, 128, 0, 1.5), (57, 352, 288, 64, 1, 0.25),
+                                                  (58, 208, 120, 96, 2, 7.0), (59, 96, 64, 64, 2, -0.5),
+                                                  (60, 640, 360, 128, 1, 3.0)])
+def test_me_multires_cross_v2_lambda_against_compiled_reference(orc, seed, w, h, mr, mode, lam):
+    """Other sizes, ranges and lambdas (a negative one too), with a random
+    inclusion map."""
+    ref_lib = oracle_mod.Reference()
+    fr = synth.pan_sequence(seed, w, h, 2)
+    incl = (synth.splitmix64(seed, (w // 16) * (h // 16)) & np.uint64(1)).astype(np.uint8)
+    mv_r, avg_r = ref_lib.me("multires_cross_v2", fr[1], fr[0], mr, mode=mode, dist_incl=incl, lam=lam)
+    mv_o, _, avg_o = orc.me_multires_cross_v2_lambda(fr[1], fr[0], mr, lam, mode=mode, dist_incl=incl)
+    np.testing.assert_array_equal(mv_o, mv_r)
+    assert avg_o == avg_r
+
+
+@pytest.mark.parametrize("case", MRC2_CASES)
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_me_cross_matches_reference(orc, golden, case, mode):
     """MotionEstimatorH264ImplCross (mode 0 quarter, 1 half, 2 full pel)."""
     g = golden("me_cross.npz")
