@@ -140,11 +140,16 @@ class _MotionEstimatorBase:
     def num_mbs(self) -> int:
         return (self._w // 16) * (self._h // 16)
 
-    def Estimate(self, *args, want_mb_distortion: bool = True):
+    def Estimate(self, *args, param: float | None = None, want_mb_distortion: bool = True):
         """Estimate() -> (vectors[N_MB, 2] int16 quarter-pel, avgDistortion).
 
         Estimate(pSrc, pRef) ignores its arguments and uses the constructor
-        planes, exactly like the reference (MotionEstimatorH264ImplFull.h:109-110)."""
+        planes, exactly like the reference (MotionEstimatorH264ImplFull.h:109-110).
+        Estimate(param) or Estimate(param=lambda) is Estimate(long*, void* param)
+        (IMotionEstimator.h:94): MultiresCrossVer2's Lagrangian overload, the
+        plain estimate for the other estimators, which ignore the parameter."""
+        if len(args) == 1:
+            param = args[0]
         if not self._h_me:
             raise VppGpuError(_lib.ERR_NOT_READY, "Estimate before Create")
         src = np.ascontiguousarray(self._src, np.int16)
@@ -155,8 +160,13 @@ class _MotionEstimatorBase:
         mv = np.empty((n, 2), np.int16)
         dist = np.empty(n, np.int32) if want_mb_distortion else None
         avg = C.c_long(0)
-        check(load().vppgpu_me_estimate(self._h_me, _ptr(src), _ptr(ref), _ptr(self._incl), _ptr(self._slice),
-                                        _ptr(mv), _ptr(dist), C.byref(avg)), "vppgpu_me_estimate")
+        if param is None:
+            check(load().vppgpu_me_estimate(self._h_me, _ptr(src), _ptr(ref), _ptr(self._incl), _ptr(self._slice),
+                                            _ptr(mv), _ptr(dist), C.byref(avg)), "vppgpu_me_estimate")
+        else:
+            check(load().vppgpu_me_estimate_lambda(self._h_me, _ptr(src), _ptr(ref), _ptr(self._incl),
+                                                   _ptr(self._slice), float(param), _ptr(mv), _ptr(dist),
+                                                   C.byref(avg)), "vppgpu_me_estimate_lambda")
         self.last_mb_distortion = dist
         if self._pred is not None:  # side effect of the reference on its predictor
             for k in range(n):
@@ -187,9 +197,12 @@ class _MotionEstimatorBase:
         return s.value
 
     def _destroy(self):
-        if self._h_me:
+        # a handle outlived by its context (finalizers at interpreter exit run
+        # in any order) is left to the process exit: destroying it would
+        # touch the freed context
+        if self._h_me and self._ctx.handle:
             load().vppgpu_me_destroy(self._h_me)
-            self._h_me = None
+        self._h_me = None
 
     def __del__(self):
         try:
@@ -263,8 +276,10 @@ class MotionEstimatorH264ImplMultiresCrossVer2(MotionEstimatorH264ImplMultiresCr
     """GPU MotionEstimatorH264ImplMultiresCrossVer2
     (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp): the
     MultiresCross search with ties towards the median prediction, the
-    pred-vector check and GetBestVector (lambda 0.9); Estimate(long*) only
-    (its lambda overload is not built)."""
+    pred-vector check and GetBestVector (lambda 0.9).  Estimate(param=lambda)
+    is the Lagrangian overload (…MultiresCrossVer2.cpp:1162-1742):
+    GetBestVector over the last five improvements of every search level,
+    then the final choice with that lambda."""
 
     KIND = _lib.ME_MULTIRES_CROSS_V2
 
@@ -302,9 +317,9 @@ class MotionCompensatorH264ImplStd:
         check(load().vppgpu_mc_compensate(self._h, _ptr(self._ref), _ptr(mv)), "vppgpu_mc_compensate")
 
     def _destroy(self):
-        if self._h:
+        if self._h and self._ctx.handle:  # as for the estimators
             load().vppgpu_mc_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:
@@ -352,9 +367,9 @@ class MotionEstimatorBatch:
         return c.value
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and self._ctx.handle:  # as for the estimators
             load().vppgpu_me_batch_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -416,9 +431,9 @@ class Server:
         return {"reserved_peak_bytes": b.value, "running_peak": r.value}
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and self._ctx.handle:  # as for the estimators
             load().vppgpu_server_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:

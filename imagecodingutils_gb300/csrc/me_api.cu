@@ -187,8 +187,10 @@ vppgpu::FullArgs full_args(vppgpu_me* me, double lambda)
     return a;
 }
 
+// lambda: the full-search estimator's GetBestVector lambda (1.05), or with
+// v2_lambda the lambda of Ver2's Lagrangian overload.
 int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigned char* d_incl, const int* d_slice,
-        int* d_mv, int* d_dist, long long* d_avg, double lambda)
+        int* d_mv, int* d_dist, long long* d_avg, double lambda, bool v2_lambda = false)
 {
     vppgpu_ctx* ctx = me->ctx;
     VPP_CUDA(cudaMemsetAsync(me->ctrl, 0, sizeof(vppgpu::MeCtrl), ctx->stream));
@@ -207,6 +209,8 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
         // GetBestVector's lambda: 0.9 (MultiresCrossVer2.cpp:1050), 1.1 (Multires.cpp:958)
         const bool v2 = me->kind == VPPGPU_ME_MULTIRES_CROSS_V2;
         VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
+        if (v2 && v2_lambda)  // Estimate(long*, void* lambda) (MultiresCrossVer2.cpp:1162-1742)
+            return vppgpu::mrc2_launch(ctx, 4, me->mode, me->d_mrc, full_args(me, lambda), d_src16, d_ref16);
         return vppgpu::mrc2_launch(ctx, v2 ? 1 : 2, me->mode, me->d_mrc, full_args(me, v2 ? 0.9 : 1.1), d_src16,
                                    d_ref16);
     }
@@ -470,7 +474,8 @@ int vppgpu_me_estimate_device(vppgpu_me* me, const short* d_src, const short* d_
 }
 
 static int estimate_host(vppgpu_me* me, const short* src, const short* ref, const unsigned char* incl,
-                         const int* slice, short* mv_out, int* mb_dist_out, long* avg, double lambda)
+                         const int* slice, short* mv_out, int* mb_dist_out, long* avg, double lambda,
+                         bool v2_lambda = false)
 {
     if (!me || !src || !ref || !mv_out) return VPPGPU_ERR_INVALID_ARG;
     int rc = vppgpu::bind(me->ctx);
@@ -482,7 +487,7 @@ static int estimate_host(vppgpu_me* me, const short* src, const short* ref, cons
     if (incl) VPP_CUDA(cudaMemcpyAsync(me->d_incl, incl, (size_t)me->nmb, cudaMemcpyHostToDevice, st));
     if (slice) VPP_CUDA(cudaMemcpyAsync(me->d_slice, slice, sizeof(int) * me->nmb, cudaMemcpyHostToDevice, st));
     rc = run(me, me->d_src16, me->d_ref16, incl ? me->d_incl : nullptr, slice ? me->d_slice : nullptr,
-             me->d_out_mv, mb_dist_out ? me->d_out_dist : nullptr, nullptr, lambda);
+             me->d_out_mv, mb_dist_out ? me->d_out_dist : nullptr, nullptr, lambda, v2_lambda);
     if (rc) return rc;
     VPP_CUDA(cudaMemcpyAsync(mv_out, me->d_out_mv, sizeof(int) * me->nmb, cudaMemcpyDeviceToHost, st));
     if (mb_dist_out)
@@ -504,12 +509,12 @@ int vppgpu_me_estimate(vppgpu_me* me, const short* src, const short* ref, const 
 int vppgpu_me_estimate_lambda(vppgpu_me* me, const short* src, const short* ref, const unsigned char* incl,
                               const int* slice, double lambda, short* mv_out, int* mb_dist_out, long* avg)
 {
-    // The full-search and MultiresCross estimators have no lambda overload:
-    // IMotionEstimator's default Estimate(long*, void*) ignores the parameter
-    // (IMotionEstimator.h:94).  Ver2's overload (per-level GetBestVector,
-    // MultiresCrossVer2.cpp:1162-1722) is not built.
-    (void)lambda;
-    if (me && me->kind == VPPGPU_ME_MULTIRES_CROSS_V2) return VPPGPU_ERR_UNSUPPORTED;
+    // Ver2's overload: GetBestVector at every search level and at the end
+    // with this lambda (MultiresCrossVer2.cpp:1162-1742).  The other
+    // estimators have none: IMotionEstimator's default Estimate(long*, void*)
+    // ignores the parameter (IMotionEstimator.h:94).
+    if (me && me->kind == VPPGPU_ME_MULTIRES_CROSS_V2)
+        return estimate_host(me, src, ref, incl, slice, mv_out, mb_dist_out, avg, lambda, true);
     return estimate_host(me, src, ref, incl, slice, mv_out, mb_dist_out, avg, 1.05);
 }
 

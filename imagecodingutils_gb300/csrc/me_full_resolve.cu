@@ -167,7 +167,10 @@ __device__ __noinline__ void pred_search_at(const FullArgs& a, int k, int px, in
         return;
     }
     int tv, td;
-    if (mrc::tie_tree_result(kEst, static_cast<const mrc::V2TieRun*>(a.tie_runs) + (size_t)k * mrc::V2_TIE_RUNS, px,
+    // the Lagrangian overload's search depends on the whole prediction: no tie tree, kept searches by
+    // their exact prediction
+    if (kEst != mrc::EST_V2_LAMBDA &&
+        mrc::tie_tree_result(kEst, static_cast<const mrc::V2TieRun*>(a.tie_runs) + (size_t)k * mrc::V2_TIE_RUNS, px,
                              py, &tv, &td)) {
         *mvx = mv_x(tv);
         *mvy = mv_y(tv);
@@ -176,8 +179,10 @@ __device__ __noinline__ void pred_search_at(const FullArgs& a, int k, int px, in
     }
     int4* sc = a.search_cache + (size_t)k * V2_SEARCH_CACHE;
     const int4 e = lane < V2_SEARCH_CACHE ? __ldcg(sc + lane) : make_int4(0, 0, 0, -1);
-    const unsigned hit =
-        __ballot_sync(0xffffffffu, e.w >= 0 && mrc::search_reusable(kEst, e.w, mv_x(e.x), mv_y(e.x), px, py));
+    const unsigned hit = __ballot_sync(0xffffffffu, e.w >= 0 && (kEst == mrc::EST_V2_LAMBDA
+                                                                     ? e.x == pack_mv(px, py)
+                                                                     : mrc::search_reusable(kEst, e.w, mv_x(e.x),
+                                                                                            mv_y(e.x), px, py)));
     if (hit) {
         const int f = __ffs(hit) - 1;
         const int v = __shfl_sync(0xffffffffu, e.y, f);
@@ -228,7 +233,10 @@ struct LatticeSlots<cross::EST_CROSS> {
 // (…MultiresCrossVer2.cpp:627-642) comes from pred_search_at.  kEst 2:
 // MotionEstimatorH264ImplMultires, the same with its own search.  kEst 3:
 // MotionEstimatorH264ImplCross, the same with its search at the rounded
-// prediction, the 64-point path distortion and norm 64.
+// prediction, the 64-point path distortion and norm 64.  kEst 4: Ver2's
+// Lagrangian overload (…MultiresCrossVer2.cpp:1162-1742), every MB searched at
+// its prediction (mrc::search_lambda), the final choice with the caller's
+// lambda.
 template <int kEst>
 __device__ __noinline__ int4 evaluate(const FullArgs& a, int k, int px, int py, int lane, mrc::Lattice* lt = nullptr)
 {
@@ -923,7 +931,22 @@ __global__ void __launch_bounds__(kWaveMaxWarps * 32, 1) k_full_wave(FullArgs a,
                 miss &= miss - 1;
                 const int fkey = __shfl_sync(0xffffffffu, key, f);
                 const int fk = (32 * band + f) * cols + (t - 2 * f);
-                const int4 rv = evaluate<kEst>(a, fk, mv_x(fkey), mv_y(fkey), lane);
+                int4 rv;
+                if constexpr (kEst == mrc::EST_V2_LAMBDA) {
+                    // a full search per miss: first the MB's records of this estimate (their final
+                    // vectors are searched ones, which the wavefront table leaves out)
+                    const int4 cr = __ldcg(a.cache + (size_t)fk * KCACHE + lane);
+                    const unsigned ch = __ballot_sync(0xffffffffu, cr.x == fkey);
+                    if (ch) {
+                        const int src = __ffs(ch) - 1;
+                        rv = make_int4(fkey, 0, __shfl_sync(0xffffffffu, cr.z, src),
+                                       __shfl_sync(0xffffffffu, cr.w, src));
+                    } else {
+                        rv = evaluate<kEst>(a, fk, mv_x(fkey), mv_y(fkey), lane);
+                    }
+                } else {
+                    rv = evaluate<kEst>(a, fk, mv_x(fkey), mv_y(fkey), lane);
+                }
                 if (lane == f) {
                     out = rv.z;
                     a.final_mv[fk] = rv.z;
@@ -1176,6 +1199,8 @@ int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
     VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, tail_smem));
     VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, tail_smem));
     VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, tail_smem));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<mrc::EST_V2_LAMBDA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  tail_smem));
     VPP_CUDA(cudaFuncSetAttribute(k_full_relax_tail<cross::EST_CROSS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   tail_smem));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1189,6 +1214,10 @@ int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap)
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 2)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, mrc::EST_V2_LAMBDA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
+    VPP_CUDA(cudaFuncSetAttribute(k_full_wave<2, mrc::EST_V2_LAMBDA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(kWaveMaxWarps, kWaveMaxCols, 2)));
     VPP_CUDA(cudaFuncSetAttribute(k_full_wave<4, cross::EST_CROSS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)wave_smem_bytes(3, kWaveMaxCols, 4)));
@@ -1266,6 +1295,7 @@ int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid,
     case 1: return resolve_launch<1>(ctx, args);
     case 2: return resolve_launch<2>(ctx, args);
     case cross::EST_CROSS: return resolve_launch<cross::EST_CROSS>(ctx, args);
+    case mrc::EST_V2_LAMBDA: return resolve_launch<mrc::EST_V2_LAMBDA>(ctx, args);
     default: return VPPGPU_ERR_INVALID_ARG;
     }
 }

@@ -137,7 +137,8 @@ size_t mrc_tie_runs_bytes();  // per macroblock
 // the tie macroblocks), then the resolve with the Cross evaluation
 // (estimator 3).
 int cross_launch(vppgpu_ctx* ctx, const FullArgs& args);
-// est: 1 MultiresCrossVer2, 2 Multires (the same pipeline, their own search).
+// est: 1 MultiresCrossVer2, 2 Multires (the same pipeline, their own search),
+// 4 Ver2's Lagrangian overload (args.lambda is its lambda).
 int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, const FullArgs& args,
                 const short* d_src16, const short* d_ref16);
 
@@ -163,7 +164,8 @@ int full_planes_launch(vppgpu_ctx* ctx, const FullArgs& args);
 // Launch the prediction-dependent tail (sweep 0, relaxation, dictionary
 // precompute, exact wavefront) of an estimate whose search has run.
 // est: 0 MotionEstimatorH264ImplFull, 1 MotionEstimatorH264ImplMultiresCrossVer2,
-// 2 MotionEstimatorH264ImplMultires.
+// 2 MotionEstimatorH264ImplMultires, 3 MotionEstimatorH264ImplCross, 4 Ver2's
+// Lagrangian overload.
 int full_resolve_launch(vppgpu_ctx* ctx, const FullArgs& args, int resolve_grid, int est);
 int full_resolve_prepare(vppgpu_ctx* ctx, int* resolve_cap);
 int full_prepare(vppgpu_ctx* ctx, int nmb, int* resolve_grid);

@@ -240,6 +240,7 @@ MrcArgs mrc_args(int W, int H, int motion_range, int mode, unsigned char* scratc
     a.rows_all = (H + 15) / 16;
     a.mode = mode;
     a.motion_range = motion_range;
+    a.lambda = 0.0;
     unsigned char* p = scratch;
     unsigned char* in0 = p;
     p += (size_t)W * H;
@@ -322,6 +323,7 @@ int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, cons
 {
     MrcArgs m = mrc_args(args.W, args.H, args.motion_range, mode, scratch);
     m.ctrl = args.ctrl;
+    m.lambda = args.lambda;
     k_set_mrc<<<1, 1, 0, ctx->stream>>>((MrcArgs*)args.mrc, m);  // for the searches at a prediction
     VPP_CHECK_LAUNCH(ctx);
     int rc = full_planes_launch(ctx, args);
@@ -331,6 +333,9 @@ int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, cons
         k_pred_search<EST_MULTIRES><<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(m, args);
         VPP_CHECK_LAUNCH(ctx);
         k_pred_tietree<EST_MULTIRES><<<ctx->sm_count * 2, V2_TIE_RUNS * 32, 0, ctx->stream>>>(m, args);
+    } else if (est == EST_V2_LAMBDA) {
+        // every MB depends on its prediction: the search at (0, 0) seeds the resolve, no tie trees
+        k_pred_search<EST_V2_LAMBDA><<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(m, args);
     } else {
         k_pred_search<EST_VER2><<<(args.nmb + 7) / 8, 256, 0, ctx->stream>>>(m, args);
         VPP_CHECK_LAUNCH(ctx);

@@ -32,6 +32,7 @@ struct Buf {
 
 struct MrcArgs {
     int W, H, cols, nmb, rows_all, mode, motion_range;
+    double lambda;  // MultiresCrossVer2's Lagrangian overload: its lambda
     Buf in0, in1, in2, e0, e1, e2;
     const unsigned char* incl;
     int* out_mv;
@@ -670,6 +671,262 @@ __device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int m
     return out;
 }
 
+// ---------------------------------------------------------------------------
+// MultiresCrossVer2::Estimate(long*, void* lambda): every search level keeps
+// its improvements in a five-slot list (Fifo(5) of include/GeneralUtils/Fifo.h,
+// newest in slot 0; the first item after a reset fills every slot) and ends
+// with GetBestVector over it.  Lane i < 5 of the searching warp holds slot i.
+struct Fifo5 {
+    int x, y, d;
+    __device__ __forceinline__ void reset(int vx, int vy, int vd)
+    {
+        x = vx;
+        y = vy;
+        d = vd;
+    }
+    __device__ __forceinline__ void push(int vx, int vy, int vd, int lane)
+    {
+        x = __shfl_up_sync(0xffffffffu, x, 1);
+        y = __shfl_up_sync(0xffffffffu, y, 1);
+        d = __shfl_up_sync(0xffffffffu, d, 1);
+        if (lane == 0) {
+            x = vx;
+            y = vy;
+            d = vd;
+        }
+    }
+};
+
+// GetBestVector (include/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.h:168-197):
+// cost D/norm + lambda*sqrt(|v - ref|^2) in IEEE double, one rounding per
+// operation as the reference's expression; slot 0 is costed at the current
+// vector (mx, my) with lambda * 2^(level+2) / 16, slots 1..4 with the raw
+// lambda; the slots in order, strict improvement.  Lanes 0..4 cost their slot
+// at once.  Sets (mx, my) and returns the winning slot's distortion.
+__device__ __forceinline__ int fifo_best(const Fifo5& f, double lambda, double norm, int level, int xr, int yr,
+                                         int& mx, int& my, int lane)
+{
+    const double l = lane == 0 ? __ddiv_rn(__dmul_rn(lambda, (double)(1 << (level + 2))), 16.0) : lambda;
+    const int vx = lane == 0 ? mx : f.x, vy = lane == 0 ? my : f.y;
+    const double m2 = (double)((vx - xr) * (vx - xr) + (vy - yr) * (vy - yr));
+    const double c = __dadd_rn(__ddiv_rn((double)f.d, norm), __dmul_rn(l, __dsqrt_rn(m2)));
+    double best = __shfl_sync(0xffffffffu, c, 0);
+    int bi = 0;
+#pragma unroll
+    for (int i = 1; i < 5; i++) {
+        const double ci = __shfl_sync(0xffffffffu, c, i);
+        if (ci < best) {
+            best = ci;
+            bi = i;
+        }
+    }
+    const int nx = __shfl_sync(0xffffffffu, f.x, bi), ny = __shfl_sync(0xffffffffu, f.y, bi);
+    if (bi) {
+        mx = nx;
+        my = ny;
+    }
+    return __shfl_sync(0xffffffffu, f.d, bi);
+}
+
+constexpr int TIE_ALL = TIE_L2 | TIE_L1 | TIE_L0;
+
+// The search of the Lagrangian overload (…MultiresCrossVer2.cpp:1237-1676),
+// one warp: the Ver2 search with GetBestVector towards the prediction's
+// vector of each level (pl[2l], pl[2l+1]: level l's x, y, level 0 rounded;
+// norms 16, 64, 256 at levels 2, 1, 0), at the end of the sub-pel stages towards the clamped
+// quarter-pel prediction (pcx, pcy).  Unlike Estimate(long*), the cross mode
+// adds its last level-1 refinement once only (…:1434-1499), and level 0
+// continues from the list's choice.  Every result depends on the prediction:
+// tie = TIE_ALL.
+__device__ MbSearch search_lambda(const MrcArgs& a, Lattice& LT, int mbr, int mbc, const int* pl, int pcx, int pcy,
+                                  int lane, bool& bad)
+{
+    const int m = 16 * mbr, n = 16 * mbc, p = 8 * mbr, q = 8 * mbc, kk = 4 * mbr, ll = 4 * mbc;
+    const int w1 = a.W / 2, h1 = a.H / 2, w2 = w1 / 2, h2 = h1 / 2;
+    const int l1_range = a.motion_range / 8, l2_range = l1_range / 2;
+    const int lcl_l1_range = a.mode == 2 ? 2 : l1_range;
+    const Level L0{16, a.W, a.H, a.motion_range / 4}, L1{8, w1, h1, l1_range}, L2{4, w2, h2, l2_range};
+    constexpr int CRX[4] = {-1, 1, 0, 0}, CRY[4] = {0, 0, -1, 1};
+    constexpr int SX[8] = {-1, 0, 1, -1, 1, -1, 0, 1}, SY[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+    const double lam = a.lambda;
+    MbSearch out;
+    out.tie = TIE_ALL;
+    Fifo5 f;
+
+    const Org oin0 = origin(a.in0, 16, 16, 0, n, m);
+    out.zero_d = full_ssd(a.in0, oin0, a.e0, origin(a.e0, 16, 16, 19, n, m), 16, lane, bad);
+    int mx = 0, my = 0, rmx = 0, rmy = 0, xl, xr, yu, yd;
+
+    if (a.mode == 2) {  // level 2 cross search (…:1287-1370)
+        const Org oin2 = origin(a.in2, 4, 4, 0, ll, kk);
+        int min2 = full_ssd(a.in2, oin2, a.e2, origin(a.e2, 4, 4, 5, ll, kk), 4, lane, bad);
+        f.reset(0, 0, min2);
+        mr_range(L2, ll, kk, 0, 0, l2_range - 1, xl, xr, yu, yd);
+        for (int s = l2_range / 2; s > 0; s /= 2) {
+            rmx = rmy = 0;
+            for (int c = 0; c < 4; c++) {
+                const int i = s * CRY[c], j = s * CRX[c];
+                if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+                // Tsd4x4LessThan stops early only on a sum already above min: a full SSD decides the same
+                const int d = full_ssd(a.in2, oin2, a.e2, origin(a.e2, 4, 4, 5, j + ll + mx, i + kk + my), 4, lane, bad);
+                if (d > min2) continue;
+                if (d == min2 && farther(mx, my, rmx, rmy, j, i, pl[4], pl[5])) continue;
+                min2 = d;
+                rmx = j;
+                rmy = i;
+                f.push(j + mx, i + my, d, lane);
+            }
+            mx += rmx;
+            my += rmy;
+        }
+        fifo_best(f, lam, 16.0, 2, pl[4], pl[5], mx, my, lane);
+        mx <<= 1;
+        my <<= 1;
+    }
+
+    // level 1 (…:1374-1502): input samples of this lane's phase share, kept
+    const Org oin1 = origin(a.in1, 8, 8, 0, q, p);
+    int r1, c1;
+    phase_coords<8>(lane, r1, c1);
+    int cur1[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) cur1[j] = rd(a.in1, oin1.y + r1, oin1.x + c1 + 4 * j, bad);
+    auto part8 = [&](Org o) {
+        int acc = 0;
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int d = cur1[j] - rd(a.e1, o.y + r1, o.x + c1 + 4 * j, bad);
+            acc += d * d;
+        }
+        return acc;
+    };
+    int min1 = full_ssd(a.in1, oin1, a.e1, origin(a.e1, 8, 8, 9, mx + q, my + p), 8, lane, bad);
+    f.reset(mx, my, min1);
+    rmx = rmy = 0;
+    auto consider1 = [&](int i, int j) {
+        const int d = partial_value(part8(origin(a.e1, 8, 8, 9, j + mx + q, i + my + p)), min1, lane);
+        if (d > min1) return;
+        if (d == min1 && farther(mx, my, rmx, rmy, j, i, pl[2], pl[3])) return;
+        min1 = d;
+        rmx = j;
+        rmy = i;
+        f.push(j + mx, i + my, d, lane);
+    };
+    if (a.mode == 2) {
+        mr_range(L1, q, p, mx, my, lcl_l1_range, xl, xr, yu, yd);
+        for (int i = yu; i <= yd; i++)
+            for (int j = xl; j <= xr; j++)
+                if (i || j) consider1(i, j);
+        mx += rmx;
+        my += rmy;
+    } else {
+        for (int s = l1_range / 2; s > 0; s /= 2) {
+            mr_range(L1, q, p, mx, my, lcl_l1_range - 1, xl, xr, yu, yd);
+            rmx = rmy = 0;
+            for (int c = 0; c < 4; c++) {
+                const int i = s * CRY[c], j = s * CRX[c];
+                if (i + my < yu || i + my > yd || j + mx < xl || j + mx > xr) continue;
+                consider1(i, j);
+            }
+            mx += rmx;
+            my += rmy;
+        }
+    }
+    fifo_best(f, lam, 64.0, 1, pl[2], pl[3], mx, my, lane);
+    mx <<= 1;
+    my <<= 1;
+
+    // level 0 +-2 refinement (…:1503-1574)
+    int r0, c0;
+    phase_coords<16>(lane, r0, c0);
+    int cur0[8];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) cur0[4 * i + j] = rd(a.in0, oin0.y + r0 + 4 * i, oin0.x + c0 + 4 * j, bad);
+    auto part16 = [&](Org o) {
+        int acc = 0;
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int d = cur0[4 * i + j] - rd(a.e0, o.y + r0 + 4 * i, o.x + c0 + 4 * j, bad);
+                acc += d * d;
+            }
+        return acc;
+    };
+    int min_d = out.zero_d;
+    if (mx || my) min_d = full_ssd(a.in0, oin0, a.e0, origin(a.e0, 16, 16, 19, n + mx, m + my), 16, lane, bad);
+    f.reset(mx, my, min_d);
+    rmx = rmy = 0;
+    mr_range(L0, n, m, mx, my, 2, xl, xr, yu, yd);
+    for (int i = yu; i <= yd; i++)
+        for (int j = xl; j <= xr; j++) {
+            if (!(i || j)) continue;
+            const int d = partial_value(part16(origin(a.e0, 16, 16, 19, n + mx + j, m + my + i)), min_d, lane);
+            if (d > min_d) continue;
+            if (d == min_d && farther(mx, my, rmx, rmy, j, i, pl[0], pl[1])) continue;
+            min_d = d;
+            rmx = j;
+            rmy = i;
+            f.push(j + mx, i + my, d, lane);
+        }
+    mx += rmx;
+    my += rmy;
+    min_d = fifo_best(f, lam, 256.0, 0, pl[0], pl[1], mx, my, lane);
+
+    // half then quarter pel in Ver2's window (…:1575-1662), strict improvements
+    int mvx = mx * 4, mvy = my * 4;
+    f.reset(mvx, mvy, min_d);
+    build_lattice<true>(LT, a.e0, origin(a.e0, 16, 16, 19, n + mx, m + my), lane, bad);
+    int hmx = 0, hmy = 0;
+    for (int c = 0; c < 8; c++) {
+        const int qx = 2 * SX[c], qy = 2 * SY[c];
+        int acc = 0;
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int d = cur0[4 * i + j] - lat(LT, 12 + qy + 4 * (r0 + 4 * i), 12 + qx + 4 * (c0 + 4 * j));
+                acc += d * d;
+            }
+        const int d = partial_value(acc, min_d, lane);
+        if (d < min_d) {
+            min_d = d;
+            hmx = qx;
+            hmy = qy;
+            f.push(qx + mvx, qy + mvy, d, lane);
+        }
+    }
+    int qmx = hmx, qmy = hmy;
+    for (int c = 0; c < 8; c++) {
+        int acc = 0;
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int d = cur0[4 * i + j] -
+                              quarter(LT, 12 + hmy + 4 * (r0 + 4 * i), 12 + hmx + 4 * (c0 + 4 * j), SY[c], SX[c]);
+                acc += d * d;
+            }
+        const int d = partial_value(acc, min_d, lane);
+        if (d < min_d) {
+            min_d = d;
+            qmx = hmx + SX[c];
+            qmy = hmy + SY[c];
+            f.push(qmx + mvx, qmy + mvy, d, lane);
+        }
+    }
+    __syncwarp();  // the lattice is reused by this warp's next search
+    mvx += qmx;
+    mvy += qmy;
+    // towards the clamped quarter-pel prediction (…:1664-1677)
+    out.min_d = fifo_best(f, lam, 256.0, 2, pcx, pcy, mvx, mvy, lane);
+    out.mvx = mvx;
+    out.mvy = mvy;
+    return out;
+}
+
 // MultiresCross's tie rules: at level 2 the centre against the offset
 // (…MultiresCross.cpp:673-679), elsewhere distances from (0, 0) (…:741-746, 857).
 template <bool kH263 = false>
@@ -685,7 +942,7 @@ __device__ __forceinline__ MbSearch search_mb_mrc(const MrcArgs& a, Lattice& LT,
 // The prediction's vector at a pyramid level (quarter-pel component p):
 // Ver2 rounds to level 0 and halves (…MultiresCrossVer2.cpp:627-642),
 // Multires rounds to every level (…Multires.cpp:646-655).
-constexpr int EST_VER2 = 1, EST_MULTIRES = 2;
+constexpr int EST_VER2 = 1, EST_MULTIRES = 2, EST_V2_LAMBDA = 4;
 __device__ __forceinline__ int level_pred(int est, int p, int lvl)
 {
     if (est == EST_MULTIRES) {
@@ -707,6 +964,16 @@ __device__ __forceinline__ MbSearch search_pred(const MrcArgs& a, Lattice& LT, i
     for (int l = 0; l < 3; l++) {
         pl[2 * l] = level_pred(kEst, px, l);
         pl[2 * l + 1] = level_pred(kEst, py, l);
+    }
+    if constexpr (kEst == EST_V2_LAMBDA) {
+        // the prediction clamped to one macroblock outside the picture (…MultiresCrossVer2.cpp:1664-1675)
+        const int n = 16 * mbc, m = 16 * mbr;
+        int px0 = px / 4, py0 = py / 4;
+        if (px0 + n > a.W) px0 = 16;
+        if (px0 + n < -16) px0 = -16;
+        if (py0 + m > a.H) py0 = 16;
+        if (py0 + m < -16) py0 = -16;
+        return search_lambda(a, LT, mbr, mbc, pl, 4 * px0 + px % 4, 4 * py0 + py % 4, lane, bad);
     }
     auto skip = [&pl](int lvl, int mx, int my, int rmx, int rmy, int j, int i) {
         return farther(mx, my, rmx, rmy, j, i, pl[2 * lvl], pl[2 * lvl + 1]);

@@ -116,8 +116,11 @@ int vppgpu_me_estimate_device(vppgpu_me* me, const short* d_src, const short* d_
                               const unsigned char* d_dist_included, const int* d_mb_slice,
                               short* d_mv_out, int* d_mb_dist_out, long long* d_avg_out);
 
-/* IMotionEstimator::Estimate(long*, void* param) with a Lagrange multiplier
- * (MotionEstimatorH264ImplMultiresCrossVer2.cpp:1162-). */
+/* IMotionEstimator::Estimate(long*, void* param) with a Lagrange multiplier:
+ * for VPPGPU_ME_MULTIRES_CROSS_V2 the Lagrangian overload
+ * (MotionEstimatorH264ImplMultiresCrossVer2.cpp:1162-1742: GetBestVector at
+ * every search level and at the end with this lambda); every other kind
+ * ignores the parameter (IMotionEstimator.h:94) and runs Estimate(long*). */
 int vppgpu_me_estimate_lambda(vppgpu_me* me, const short* src, const short* ref,
                               const unsigned char* dist_included, const int* mb_slice,
                               double lambda, short* mv_out, int* mb_dist_out,

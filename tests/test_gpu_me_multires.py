@@ -133,18 +133,3 @@ def test_pixel_range_rejected(vpp, ctx, kind):
     assert me.Create() == 1
     with pytest.raises(vpp.VppGpuError):
         me.Estimate()
-
-
-def test_lambda_overload_not_built(vpp, ctx):
-    fr = synth.pan_sequence(81, 64, 48, 2)
-    L = vpp.load()
-    from imagecodingutils_gb300 import _lib
-    h = C.c_void_p()
-    _lib.check(L.vppgpu_me_create(ctx.handle, _lib.ME_MULTIRES_CROSS_V2, 64, 48, 64, C.byref(h)), "create")
-    mv = np.zeros((12, 2), np.int16)
-    avg = C.c_long()
-    src, ref = np.ascontiguousarray(fr[1]), np.ascontiguousarray(fr[0])
-    rc = L.vppgpu_me_estimate_lambda(h, src.ctypes.data_as(C.c_void_p), ref.ctypes.data_as(C.c_void_p), None, None,
-                                     C.c_double(0.5), mv.ctypes.data_as(C.c_void_p), None, C.byref(avg))
-    assert rc == _lib.ERR_UNSUPPORTED
-    L.vppgpu_me_destroy(h)
