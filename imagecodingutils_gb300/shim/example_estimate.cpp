@@ -5,8 +5,10 @@
 // pair.bin holds the source then the reference luma plane (int16).  The
 // program estimates with GpuMotionEstimatorH264ImplFull (or, by the optional
 // last argument, ...Multires, ...MultiresCross, ...MultiresCrossVer2 or
-// ...Cross: "multires", "mrc", "mrc2", "cross", "sad") exactly as a codec would with the vpp class
-// (constructor, Create, SetMode(0), Estimate, predictor side effect), then
+// ...Cross: "multires", "mrc", "mrc2", "cross", "sad"; "mrc2lam" is Ver2's
+// Lagrangian Estimate(long*, void*) with lambda 2.5) exactly as a codec would
+// with the vpp class (constructor, Create, SetMode(0), Estimate, predictor
+// side effect), then
 // runs the forward/inverse 4x4 transform classes
 // on the motion-compensated-free residual (source - reference) of the first
 // macroblock row, and the Intra16x16-style DC path (4x4 transform only, DC
@@ -34,7 +36,7 @@ public:
 int main(int argc, char** argv)
 {
     if (argc != 6 && argc != 7) {
-        fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin [full|multires|mrc|mrc2|cross]\n", argv[0]);
+        fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin [full|multires|mrc|mrc2|mrc2lam|cross|sad]\n", argv[0]);
         return 2;
     }
     const std::string kind = argc == 7 ? argv[6] : "full";
@@ -54,7 +56,7 @@ int main(int argc, char** argv)
         me = new GpuMotionEstimatorH264ImplMultires(src.data(), ref.data(), w, h, range, &pred, incl);
     else if (kind == "mrc")
         me = new GpuMotionEstimatorH264ImplMultiresCross(src.data(), ref.data(), w, h, range, incl);
-    else if (kind == "mrc2")
+    else if (kind == "mrc2" || kind == "mrc2lam")
         me = new GpuMotionEstimatorH264ImplMultiresCrossVer2(src.data(), ref.data(), w, h, range, &pred, incl);
     else if (kind == "cross")
         me = new GpuMotionEstimatorH264ImplCross(src.data(), ref.data(), w, h, range, &pred, incl);
@@ -68,7 +70,9 @@ int main(int argc, char** argv)
     }
     me->SetMode(0);
     long avg = 0;
-    VectorStructList* vl = (VectorStructList*)me->Estimate(&avg);
+    double lambda = 2.5;
+    VectorStructList* vl =
+        (VectorStructList*)(kind == "mrc2lam" ? me->Estimate(&avg, (void*)&lambda) : me->Estimate(&avg));
     if (!vl) {
         fprintf(stderr, "Estimate failed\n");
         return 5;

@@ -34,7 +34,7 @@ def test_shim_compiles_against_vpp_interfaces():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["full", "multires", "mrc", "mrc2", "cross", "sad"])
+@pytest.mark.parametrize("kind", ["full", "multires", "mrc", "mrc2", "mrc2lam", "cross", "sad"])
 def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
     from imagecodingutils_gb300 import build
     exe = tmp_path / "example_estimate"
@@ -67,6 +67,8 @@ def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
         mv_o, _, avg_o = orc.me_multires_cross(fr[1], fr[0], mr, mode=0, dist_incl=ones)
     elif kind == "cross":
         mv_o, _, avg_o = orc.me_cross(fr[1], fr[0], mr, mode=0, dist_incl=ones)
+    elif kind == "mrc2lam":
+        mv_o, _, avg_o = orc.me_multires_cross_v2_lambda(fr[1], fr[0], mr, 2.5, mode=0, dist_incl=ones)
     elif kind == "sad":
         mv_o, d_o = orc.me_full_intpel(fr[1], fr[0], mr, metric=1)
         avg_o = int(d_o.sum()) // nmb
