@@ -338,9 +338,11 @@ TransformAndQuant, TransformOnly, QuantOnly = 0, 1, 2
 
 class MotionEstimatorBatch:
     """Many independent frame pairs of mixed sizes in one call
-    (vppgpu_me_batch_*; no vpp counterpart).  Jobs are dicts or tuples of
-    device pointers: (src, ref, width, height, motion_range, mv_out[,
-    mb_dist_out[, dist_included]]); run() returns (statuses, avgDistortions)."""
+    (vppgpu_me_batch_*; no vpp counterpart).  Jobs are tuples of device
+    pointers: (src, ref, width, height, motion_range, mv_out[, mb_dist_out[,
+    dist_included[, residual_out, levels_out, recon_out, qp]]]); the last four
+    add the coding stage (residual at the vectors, T+Q at qp and its inverse).
+    run() returns (statuses, avgDistortions)."""
 
     def __init__(self, streams: int = 4, kind: int = _lib.ME_FULL, ctx: Context | None = None):
         self._ctx = ctx or get_context()
@@ -355,10 +357,13 @@ class MotionEstimatorBatch:
             src, ref, w, hgt, mr, mv = j[:6]
             dist = j[6] if len(j) > 6 else None
             incl = j[7] if len(j) > 7 else None
-            arr[i] = _lib.MeJob(src, ref, w, hgt, mr, incl, mv, dist)
+            res, lev, rec, qp = j[8:12] if len(j) > 8 else (None, None, None, 0)
+            arr[i] = _lib.MeJob(src, ref, w, hgt, mr, incl, mv, dist, res, lev, rec, qp)
         st = (C.c_int * max(n, 1))()
         avg = (C.c_long * max(n, 1))()
-        load().vppgpu_me_batch_run(self.handle, arr, n, st, avg)
+        rc = load().vppgpu_me_batch_run(self.handle, arr, n, st, avg)
+        if rc != _lib.OK and not any(list(st)[:n]):  # refused as a whole (arguments, CUDA), not a job's status
+            raise VppGpuError(rc, "vppgpu_me_batch_run")
         return list(st)[:n], list(avg)[:n]
 
     def launch_count(self) -> int:

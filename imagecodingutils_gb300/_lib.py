@@ -147,7 +147,8 @@ class MeJob(C.Structure):
     """vppgpu_me_job (include/vppgpu.h)."""
     _fields_ = [("src", C.c_void_p), ("ref", C.c_void_p), ("width", C.c_int), ("height", C.c_int),
                 ("motion_range", C.c_int), ("dist_included", C.c_void_p), ("mv_out", C.c_void_p),
-                ("mb_dist_out", C.c_void_p)]
+                ("mb_dist_out", C.c_void_p), ("residual_out", C.c_void_p), ("levels_out", C.c_void_p),
+                ("recon_out", C.c_void_p), ("qp", C.c_int)]
 
 
 class SeqRequest(C.Structure):

@@ -888,6 +888,8 @@ int vppgpu_me_batch_run(vppgpu_me_batch* b, const vppgpu_me_job* jobs, int n, in
     for (int j = 0; j < n; j++) {
         const vppgpu_me_job& J = jobs[j];
         if (!J.src || !J.ref || !J.mv_out || J.width < 16 || J.height < 16 || J.width % 16) return VPPGPU_ERR_INVALID_ARG;
+        if (J.levels_out && (!J.residual_out || !J.recon_out || J.qp < 0 || J.qp > 51 || b->kind != VPPGPU_ME_FULL))
+            return VPPGPU_ERR_INVALID_ARG;
     }
     if (n > b->cap) {
         if (b->h_ctrl) cudaFreeHost(b->h_ctrl);
@@ -933,6 +935,15 @@ int vppgpu_me_batch_run(vppgpu_me_batch* b, const vppgpu_me_job* jobs, int n, in
             return rc;
         VPP_CUDA(cudaMemcpyAsync(b->h_ctrl + j, me->ctrl, sizeof(vppgpu::MeCtrl), cudaMemcpyDeviceToHost,
                                  sl.ctx->stream));
+        if (J.levels_out) {
+            // the coding stage on the same stream: residual at the vectors, then T+Q and its inverse over the
+            // full macroblock rows (rows below them carry no residual)
+            if ((rc = vppgpu_me_residual_device(me, J.mv_out, J.residual_out))) return rc;
+            if ((rc = vppgpu_tq_roundtrip_plane_device(sl.ctx, J.residual_out, J.levels_out, J.recon_out, J.width,
+                                                       16 * (J.height / 16), J.width, J.qp, 0,
+                                                       VPPGPU_INV_ROWS_FIRST, nullptr)))
+                return rc;
+        }
     }
     for (int s = 0; s < b->nslots; s++) {
         VPP_CUDA(cudaEventRecord(b->done[s], b->slot[s].ctx->stream));

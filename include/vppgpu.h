@@ -206,6 +206,17 @@ typedef struct {
     const unsigned char* dist_included;  /* device, one flag per MB, or NULL */
     short* mv_out;                       /* device, 2 shorts per MB */
     int* mb_dist_out;                    /* device, one int per MB, or NULL */
+    /* Optional coding stage of the job (levels_out NULL: none): the
+     * motion-compensated luma residual at the estimated vectors
+     * (vppgpu_me_residual_device) into residual_out, then its 4x4 forward
+     * transform + quantisation at `qp` (inter rounding) and the dequantised
+     * inverse (vppgpu_tq_roundtrip_plane_device, rows first) over the full
+     * macroblock rows into levels_out / recon_out.  Device, W x H shorts each;
+     * Full estimator batches only. */
+    short* residual_out;
+    short* levels_out;
+    short* recon_out;
+    int qp;
 } vppgpu_me_job;
 int vppgpu_me_batch_create(vppgpu_ctx* ctx, int kind, int streams, vppgpu_me_batch** out);
 int vppgpu_me_batch_destroy(vppgpu_me_batch* b);

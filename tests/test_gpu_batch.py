@@ -63,3 +63,57 @@ def test_batch_reports_per_job_status(vpp, ctx):
     assert st[0] == 0
     assert st[1] == -4  # VPPGPU_ERR_PIXEL_RANGE
     batch.close()
+
+
+def test_batch_coding_stage_matches_oracle(vpp, ctx, orc):
+    """Jobs with the coding stage (residual at the vectors, T+Q at QP 28 inter
+    and its inverse): vectors, residual, levels and reconstruction of every job
+    equal the oracle's chain (Full estimate, QuarterRead residual, 4x4 round
+    trip), on several streams, with a partial bottom row and a job without the
+    stage in the same batch."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    sizes = [(176, 144, 128, 28), (352, 288, 128, 28), (208, 120, 96, 17), (176, 152, 128, 40)]
+    jobs, keep = [], []
+    for i, (w, h, mr, qp) in enumerate(sizes):
+        fr = synth.pan_sequence(320 + i, w, h, 2)
+        src, ref = torch.from_numpy(fr[1]).to(dev), torch.from_numpy(fr[0]).to(dev)
+        nmb = (w // 16) * (h // 16)
+        mv = torch.zeros((nmb, 2), dtype=torch.int16, device=dev)
+        bufs = [torch.full((h, w), 9, dtype=torch.int16, device=dev) for _ in range(3)]
+        keep.append((fr, src, ref, mv, bufs, w, h, mr, qp))
+        jobs.append((src.data_ptr(), ref.data_ptr(), w, h, mr, mv.data_ptr(), None, None,
+                     *[b.data_ptr() for b in bufs], qp))
+    fr = synth.pan_sequence(330, 176, 144, 2)
+    plain_src, plain_ref = torch.from_numpy(fr[1]).to(dev), torch.from_numpy(fr[0]).to(dev)
+    plain_mv = torch.zeros((99, 2), dtype=torch.int16, device=dev)
+    jobs.append((plain_src.data_ptr(), plain_ref.data_ptr(), 176, 144, 128, plain_mv.data_ptr()))
+    batch = vpp.MotionEstimatorBatch(streams=3, ctx=ctx)
+    st, _ = batch.run(jobs)
+    torch.cuda.synchronize()
+    assert st == [0] * len(jobs)
+    np.testing.assert_array_equal(plain_mv.cpu().numpy(), orc.me_full(fr[1], fr[0], 128)[0])
+    for fr, src, ref, mv, (res, lev, rec), w, h, mr, qp in keep:
+        mv_o, _, _ = orc.me_full(fr[1], fr[0], mr)
+        np.testing.assert_array_equal(mv.cpu().numpy(), mv_o)
+        cols, rows = w // 16, h // 16
+        hh = 16 * rows
+        res_o = np.zeros((hh, w), np.int32)
+        for k in range(cols * rows):
+            n, m = (k % cols) * 16, (k // cols) * 16
+            vx, vy = int(mv_o[k, 0]), int(mv_o[k, 1])
+            qx, qy = int(np.fmod(vx, 4)), int(np.fmod(vy, 4))
+            pred = orc.quarter_read16(fr[0], n + (vx - qx) // 4, m + (vy - qy) // 4, qx, qy)
+            res_o[m:m + 16, n:n + 16] = fr[1][m:m + 16, n:n + 16].astype(np.int32) - pred
+        np.testing.assert_array_equal(res.cpu().numpy()[:hh], res_o)
+        blocks = res_o.astype(np.int16).reshape(hh // 4, 4, w // 4, 4).transpose(0, 2, 1, 3).reshape(-1, 16)
+        lev_o = orc.fwd4x4(blocks, 0, 0, qp, 0)
+        rec_o = orc.inv4x4(lev_o, 0, 0, qp)
+        back = lambda b: b.reshape(hh // 4, w // 4, 4, 4).transpose(0, 2, 1, 3).reshape(hh, w)
+        np.testing.assert_array_equal(lev.cpu().numpy()[:hh], back(lev_o))
+        np.testing.assert_array_equal(rec.cpu().numpy()[:hh], back(rec_o))
+    bad = list(jobs[0])
+    bad[11] = 52  # QP out of range
+    with pytest.raises(vpp.VppGpuError):
+        batch.run([tuple(bad)])
+    batch.close()
