@@ -28,7 +28,7 @@ from ._lib import VppGpuError, check, load
 
 __all__ = [
     "Context", "get_context", "MotionEstimatorH264ImplFull", "MotionEstimatorH264ImplMultires",
-    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross", "MotionEstimatorH264ImplFullSad",
+    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross", "MotionEstimatorH264ImplFullSad", "MotionEstimatorH264ImplUMHS",
     "MotionEstimatorH263ImplMultiresCross", "MotionEstimatorBatch",
     "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
     "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1", "FastForwardDC4x4ITImpl1",
@@ -236,6 +236,45 @@ class MotionEstimatorH264ImplFullSad(_MotionEstimatorBase):
     quarter pels, distortions their SAD, no sub-pel stage or GetBestVector."""
 
     KIND = _lib.ME_FULL_SAD
+
+
+class MotionEstimatorH264ImplUMHS(_MotionEstimatorBase):
+    """GPU MotionEstimatorH264ImplUMHS (src/CodecUtils/MotionEstimatorH264ImplUMHS.cpp):
+    the unsymmetrical-cross multi-hexagon-grid search from the median prediction,
+    as built by the reference's eight-argument constructor
+    (pSrc, pRef, w, h, motionRange, pMVPred, pDistortionIncluded, pPrevFrmMBlk).
+    pPrevFrmMBlk is given as (prev_mv[N_MB, 2] quarter-pel, prev_intra[N_MB] or
+    None), the _mvX[0] / _mvY[0] / _intraFlag fields of the previous frame's
+    macroblocks; it is re-read on every Estimate(), as the reference reads the
+    caller's array.  The predictor side effect carries the distortion:
+    Set16x16MotionVector(k, x, y, d).  SetMode(0) quarter pel (the default),
+    1 half, 2 full pel."""
+
+    KIND = _lib.ME_UMHS
+    DEFAULT_MODE = 0
+
+    def __init__(self, pSrc, pRef, imgWidth: int, imgHeight: int, motionRange: int = 64, pMVPred=None,
+                 pDistortionIncluded=None, pPrevFrmMBlk=None, mb_slice=None, ctx: Context | None = None):
+        super().__init__(pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred, pDistortionIncluded, mb_slice, ctx)
+        self._prev = pPrevFrmMBlk
+
+    def Estimate(self, *args, param: float | None = None, want_mb_distortion: bool = True):
+        if not self._h_me:
+            raise VppGpuError(_lib.ERR_NOT_READY, "Estimate before Create")
+        pmv, pin = (None, None) if self._prev is None else self._prev
+        pmv = None if pmv is None else np.ascontiguousarray(pmv, np.int16)
+        pin = None if pin is None else np.ascontiguousarray(pin, np.uint8)
+        check(load().vppgpu_me_set_prev_frame(self._h_me, _ptr(pmv), _ptr(pin)), "vppgpu_me_set_prev_frame")
+        pred, self._pred = self._pred, None
+        try:
+            mv, avg = super().Estimate(*args, param=param, want_mb_distortion=True)
+        finally:
+            self._pred = pred
+        if self._pred is not None:  # the reference hands the predictor each vector with its distortion
+            d = self.last_mb_distortion
+            for k in range(self.num_mbs()):
+                self._pred.Set16x16MotionVector(k, int(mv[k, 0]), int(mv[k, 1]), int(d[k]))
+        return mv, avg
 
 
 class MotionEstimatorH264ImplMultiresCross(_MotionEstimatorBase):

@@ -28,6 +28,7 @@ ERR_NO_DEVICE = -8
 
 ME_FULL, ME_MULTIRES, ME_MULTIRES_CROSS, ME_MULTIRES_CROSS_V2, ME_CROSS, ME_H263_MULTIRES_CROSS = 0, 1, 2, 3, 4, 5
 ME_FULL_SAD = 6
+ME_UMHS = 7
 LAYOUT_BLOCKS, LAYOUT_MB16 = 0, 1
 INV_ROWS_FIRST, INV_COLS_FIRST = 0, 1
 RGB_FIXED_POINT, RGB_REAL, RGB_REAL_IMPL2 = 0, 1, 2
@@ -50,6 +51,7 @@ SIGNATURES = {
     "vppgpu_me_estimate": (_I, [_P, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_long)]),
     "vppgpu_me_estimate_device": (_I, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "vppgpu_me_estimate_lambda": (_I, [_P, _P, _P, _P, _P, C.c_double, _P, _P, C.POINTER(C.c_long)]),
+    "vppgpu_me_set_prev_frame": (_I, [_P, _P, _P]),
     "vppgpu_me_last_status": (_I, [_P]),
     "vppgpu_me_set_relax_sweeps": (_I, [_P, _I]),
     "vppgpu_me_autotune": (_I, [_P, _P, _P, _I, C.POINTER(_I)]),

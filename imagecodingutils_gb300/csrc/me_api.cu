@@ -53,6 +53,11 @@ struct vppgpu_me {
     void* d_lattice;   // MultiresCrossVer2: one sub-pel lattice per MB
     int4* d_search_cache;  // MultiresCrossVer2: searches of tie MBs at other predictions
     void* d_tie_runs;      // MultiresCrossVer2: tie trees
+    unsigned long long* d_ustate;  // UMHS: sweep states, then the dataflow pass's states (2 * nmb)
+    int4* d_urec;                  // UMHS: records (UMHS_RECORDS per MB)
+    int* d_uprev;                  // UMHS: previous frame's full-pel starting points
+    int* d_uorder;                 // UMHS: dataflow ticket -> macroblock
+    int wave_grid;                 // UMHS: CTAs of the dataflow pass
     vppgpu::MeCtrl* h_ctrl;  // pinned
     int last_status;
     // per-kernel timing (vppgpu_me_set_timing)
@@ -115,6 +120,10 @@ void me_free(vppgpu_me* me)
     cudaFree(me->d_lattice);
     cudaFree(me->d_search_cache);
     cudaFree(me->d_tie_runs);
+    cudaFree(me->d_ustate);
+    cudaFree(me->d_urec);
+    cudaFree(me->d_uprev);
+    cudaFree(me->d_uorder);
     cudaFree(me->d_job);
     if (me->graph) cudaGraphExecDestroy(me->graph);
     cudaFree(me->spec);
@@ -187,6 +196,19 @@ vppgpu::FullArgs full_args(vppgpu_me* me, double lambda)
     return a;
 }
 
+vppgpu::UmhsArgs umhs_args(vppgpu_me* me)
+{
+    vppgpu::UmhsArgs u{};
+    u.f = full_args(me, 1.05);
+    u.state = me->d_ustate;
+    u.wave = me->d_ustate + me->nmb;
+    u.rec = me->d_urec;
+    u.prev = me->d_uprev;
+    u.order = me->d_uorder;
+    u.sweeps = me->relax_sweeps < 1 ? 1 : me->relax_sweeps;
+    return u;
+}
+
 // lambda: the full-search estimator's GetBestVector lambda (1.05), or with
 // v2_lambda the lambda of Ver2's Lagrangian overload.
 int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigned char* d_incl, const int* d_slice,
@@ -213,6 +235,10 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
             return vppgpu::mrc2_launch(ctx, 4, me->mode, me->d_mrc, full_args(me, lambda), d_src16, d_ref16);
         return vppgpu::mrc2_launch(ctx, v2 ? 1 : 2, me->mode, me->d_mrc, full_args(me, v2 ? 0.9 : 1.1), d_src16,
                                    d_ref16);
+    }
+    if (me->kind == VPPGPU_ME_UMHS) {
+        VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
+        return vppgpu::umhs_launch(ctx, umhs_args(me), me->wave_grid);
     }
     if (me->kind == VPPGPU_ME_FULL_SAD) {
         // the integer-pel stage only: no sub-pel, no prediction check, no GetBestVector
@@ -282,7 +308,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 4) return VPPGPU_ERR_INVALID_ARG;
     if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
     if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
-    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_FULL_SAD) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_UMHS) return VPPGPU_ERR_UNSUPPORTED;
     // MotionEstimatorH263ImplMultiresCross's range is in half pels: at most 64 (+-31 pels), as 128 quarter pels
     if (kind == VPPGPU_ME_H263_MULTIRES_CROSS && motion_range > 64) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
@@ -297,7 +323,8 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     me->rows = height / 16;
     me->nmb = me->cols * me->rows;
     me->motion_range = motion_range;
-    me->mode = kind == VPPGPU_ME_CROSS ? 0 : 1;  // Cross defaults to quarter pel (…ImplCross.cpp:184)
+    // Cross and UMHS default to quarter pel (…ImplCross.cpp:184, …ImplUMHS.cpp:259)
+    me->mode = (kind == VPPGPU_ME_CROSS || kind == VPPGPU_ME_UMHS) ? 0 : 1;
     me->rstride = width + 2 * vppgpu::PAD;
     me->sweep_limit = vppgpu::RELAX_SWEEPS + 2 + (me->nmb + 31) / 32;  // sweep counters, then the dirty bitmap
     // Sweep policy by how the estimator's predictions settle on moving content
@@ -305,7 +332,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     // within 8 sweeps over every MB, a few more over the dirty sets; Multires
     // keeps settling with more sweeps, cheaply over the dirty sets; Ver2
     // rarely settles, so its wavefront starts early.
-    me->relax_sweeps = kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : vppgpu::RELAX_SWEEPS;
+    me->relax_sweeps = kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : (kind == VPPGPU_ME_UMHS ? 6 : vppgpu::RELAX_SWEEPS);
     me->grid_sweeps = kind == VPPGPU_ME_MULTIRES ? 4 : (kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : 8);
     me->relax_blocks_per_sm = 4;
     me->mrc_warps = 8;
@@ -357,6 +384,45 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
             me_free(me);
             return rc;
         }
+        *out = me;
+        return VPPGPU_OK;
+    }
+    if (kind == VPPGPU_ME_UMHS) {
+        // MotionEstimatorH264ImplUMHS(…, pMVPred, pDistortionIncluded, pPrevFrmMBlk) + Create(): the padded
+        // reference with its half-pel planes, sweep and dataflow states, records, the previous frame's
+        // starting points (zero until vppgpu_me_set_prev_frame) and the dataflow order
+        if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
+            (rc = dalloc(&me->d_src8, npix)) || (rc = dalloc(&me->d_refp, npad)) ||
+            (rc = dalloc(&me->d_hpel, 3 * npad)) || (rc = dalloc(&me->d_job, 1)) ||
+            (rc = dalloc(&me->d_ustate, 2 * (size_t)me->nmb)) ||
+            (rc = dalloc(&me->d_urec, (size_t)me->nmb * vppgpu::UMHS_RECORDS)) ||
+            (rc = dalloc(&me->d_uprev, me->nmb)) || (rc = dalloc(&me->d_uorder, me->nmb)) ||
+            (rc = dalloc(&me->changed, (size_t)me->sweep_limit)) ||
+            (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
+            (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||
+            (rc = dalloc(&me->d_slice, me->nmb)) || (rc = dalloc(&me->ctrl, 1))) {
+            me_free(me);
+            return rc;
+        }
+        if (cudaMallocHost((void**)&me->h_ctrl, sizeof(vppgpu::MeCtrl)) != cudaSuccess) {
+            me_free(me);
+            return VPPGPU_ERR_OUT_OF_MEMORY;
+        }
+        // anti-diagonals c + 2r, rows ascending: every neighbour a prediction reads has a lower ticket
+        std::vector<int> order;
+        order.reserve(me->nmb);
+        for (int d = 0; d <= (me->cols - 1) + 2 * (me->rows - 1); d++)
+            for (int r = 0; r < me->rows; r++) {
+                const int c = d - 2 * r;
+                if (c >= 0 && c < me->cols) order.push_back(r * me->cols + c);
+            }
+        if (cudaMemcpy(me->d_uorder, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemset(me->d_uprev, 0, sizeof(int) * (size_t)me->nmb) != cudaSuccess) {
+            me_free(me);
+            return VPPGPU_ERR_CUDA;
+        }
+        const int g = (me->nmb + 3) / 4;
+        me->wave_grid = g < 4 * ctx->sm_count ? g : 4 * ctx->sm_count;
         *out = me;
         return VPPGPU_OK;
     }
@@ -441,8 +507,8 @@ int vppgpu_me_set_mode(vppgpu_me* me, int mode)
 {
     if (!me) return VPPGPU_ERR_INVALID_ARG;
     // SetMode(0) picks by picture area for the multi-resolution estimators (MultiresCross.cpp:501-513);
-    // Cross keeps the mode as given (MotionEstimatorH264ImplCross.h:99)
-    if (mode == 0 && me->kind != VPPGPU_ME_FULL && me->kind != VPPGPU_ME_CROSS)
+    // Cross and UMHS keep the mode as given (MotionEstimatorH264ImplCross.h:99, …ImplUMHS.h:107)
+    if (mode == 0 && me->kind != VPPGPU_ME_FULL && me->kind != VPPGPU_ME_CROSS && me->kind != VPPGPU_ME_UMHS)
         mode = (me->W * me->H > 40000) ? 2 : 1;
     me->mode = mode;
     return VPPGPU_OK;
@@ -504,6 +570,30 @@ int vppgpu_me_estimate(vppgpu_me* me, const short* src, const short* ref, const 
                        const int* slice, short* mv_out, int* mb_dist_out, long* avg)
 {
     return estimate_host(me, src, ref, incl, slice, mv_out, mb_dist_out, avg, 1.05);
+}
+
+int vppgpu_me_set_prev_frame(vppgpu_me* me, const short* prev_mv, const unsigned char* prev_intra)
+{
+    if (!me) return VPPGPU_ERR_INVALID_ARG;
+    if (me->kind != VPPGPU_ME_UMHS) return VPPGPU_ERR_UNSUPPORTED;
+    int rc = vppgpu::bind(me->ctx);
+    if (rc) return rc;
+    // the starting point of MotionEstimatorH264ImplUMHS.cpp:551-571: the
+    // vector in full pels (C division), none for intra macroblocks; a block
+    // origin outside [-16, W] x [-16, H] would make the reference read
+    // outside its buffers should it win
+    std::vector<int> start((size_t)me->nmb, 0);
+    for (int k = 0; prev_mv && k < me->nmb; k++) {
+        if (prev_intra && prev_intra[k]) continue;
+        const int x = prev_mv[2 * k] / 4, y = prev_mv[2 * k + 1] / 4;
+        const int ox = (k % me->cols) * 16 + x, oy = (k / me->cols) * 16 + y;
+        if (ox < -16 || ox > me->W || oy < -16 || oy > me->H) return VPPGPU_ERR_INVALID_ARG;
+        start[k] = (int)((unsigned)(x & 0xffff) | ((unsigned)y << 16));
+    }
+    VPP_CUDA(cudaMemcpyAsync(me->d_uprev, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice,
+                             me->ctx->stream));
+    VPP_CUDA(cudaStreamSynchronize(me->ctx->stream));
+    return VPPGPU_OK;
 }
 
 int vppgpu_me_estimate_lambda(vppgpu_me* me, const short* src, const short* ref, const unsigned char* incl,
@@ -650,6 +740,9 @@ extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS) {
         for (int w : {2, 4, 8})
             if (w != cur.warps) cands.push_back({cur.relax, cur.grid, cur.bps, w});
+    } else if (me->kind == VPPGPU_ME_UMHS) {  // only the sweeps before the dataflow pass matter
+        for (int r : {1, 2, 4, 6, 8, 12})
+            if (r != cur.relax) cands.push_back({r, cur.grid, cur.bps, cur.warps});
     } else {
         const int policies[][2] = {{4, 4}, {8, 8}, {14, 8}, {14, 4}, {14, 2}};
         for (const auto& p : policies)

@@ -240,9 +240,10 @@ __device__ __forceinline__ const unsigned char* even_block(const FullArgs& a, in
 // eight half-pel neighbours in MEH264IF_SubPos order, then eight quarter-pel
 // neighbours of the half-pel winner, each the rounded mean of the two
 // lattice samples LoadQuartPelWindow pairs (Full.cpp:1207-1220); strict
-// improvement.  cur: this lane's 8 input samples.
+// improvement.  cur: this lane's 8 input samples.  quarter false: the
+// half-pel pass only (a half-pel SetMode).
 __device__ __forceinline__ void subpel_refine_planes(const FullArgs& a, int x0, int y0, uint2 cur, int lane, int* min_d,
-                                                     int* qmx, int* qmy)
+                                                     int* qmx, int* qmy, bool quarter = true)
 {
     constexpr int SX[8] = {-1, 0, 1, -1, 1, -1, 0, 1};
     constexpr int SY[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
@@ -261,6 +262,12 @@ __device__ __forceinline__ void subpel_refine_planes(const FullArgs& a, int x0, 
             hmx = 2 * SX[k];
             hmy = 2 * SY[k];
         }
+    }
+    if (!quarter) {
+        *min_d = best;
+        *qmx = hmx;
+        *qmy = hmy;
+        return;
     }
 #pragma unroll
     for (int k = 0; k < 8; k++) {

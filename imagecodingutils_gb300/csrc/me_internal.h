@@ -142,6 +142,27 @@ int cross_launch(vppgpu_ctx* ctx, const FullArgs& args);
 int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, const FullArgs& args,
                 const short* d_src16, const short* d_ref16);
 
+// MotionEstimatorH264ImplUMHS (me_umhs.cu).  Its search starts at the
+// prediction, so every macroblock's result is a function of its prediction
+// (vector and distortion): relaxation sweeps evaluate every macroblock at the
+// prediction of the current neighbour states and keep the evaluations as
+// records; unless a sweep changes nothing (the fixed point, which is the
+// sequential result), a dataflow pass over the wavefront order settles the
+// exact raster result, looking predictions up in the records first.
+constexpr int UMHS_RECORDS = 4;  // records per macroblock
+struct UmhsArgs {
+    FullArgs f;                 // planes, geometry, job, control, change counters
+    unsigned long long* state;  // per MB: sweep state, packed vector | distortion << 32
+    unsigned long long* wave;   // per MB: the dataflow pass's state, all ones until written
+    int4* rec;                  // UMHS_RECORDS per MB: {prediction, outcome word, vector, distortion}
+    const int* prev;            // per MB: the previous frame's full-pel starting point (packed; 0: none)
+    const int* order;           // dataflow ticket -> macroblock (anti-diagonals c + 2r, rows ascending)
+    int sweeps;                 // relaxation sweeps before the dataflow pass (>= 1)
+};
+// The planes, `sweeps` relaxation sweeps, the dataflow pass (wave_grid CTAs of
+// 4 warps) and the outputs.
+int umhs_launch(vppgpu_ctx* ctx, const UmhsArgs& args, int wave_grid);
+
 // Write this estimate's pointers to the device descriptor (a one-thread
 // kernel with the descriptor as its parameter: stream-ordered, no host copy).
 int set_job(vppgpu_ctx* ctx, JobDesc* d_job, const JobDesc& v);

@@ -72,6 +72,15 @@ int vppgpu_ctx_launch_count(vppgpu_ctx* ctx, unsigned long long* count);
  * sub-pel stage, prediction check or GetBestVector.  The median prediction
  * still decides exact ties, so the estimator keeps the predictor contract. */
 #define VPPGPU_ME_FULL_SAD          6
+/* MotionEstimatorH264ImplUMHS (src/CodecUtils/MotionEstimatorH264ImplUMHS.cpp:446-945):
+ * the unsymmetrical-cross multi-hexagon-grid search from the median prediction,
+ * built as by its eight-argument constructor (…ImplUMHS.cpp:231-254; the others
+ * leave the previous-frame macroblocks unset while Estimate reads them).  Its
+ * predictor also predicts a distortion (MacroBlockH264.cpp:818-915), so the
+ * caller's predictor side effect is Set16x16MotionVector(k, x, y, mb_dist_out[k])
+ * (H264MotionVectorPredictorImpl1.h:112-121).  Modes 0 quarter (default), 1 half,
+ * 2 full pel, kept as given. */
+#define VPPGPU_ME_UMHS              7
 
 typedef struct vppgpu_me vppgpu_me;
 
@@ -125,6 +134,17 @@ int vppgpu_me_estimate_lambda(vppgpu_me* me, const short* src, const short* ref,
                               const unsigned char* dist_included, const int* mb_slice,
                               double lambda, short* mv_out, int* mb_dist_out,
                               long* avg_distortion);
+
+/* The previous frame's macroblocks of MotionEstimatorH264ImplUMHS's
+ * pPrevFrmMBlk argument (…ImplUMHS.cpp:231-254, read at :551-571): per macroblock
+ * its 16x16 vector (MacroBlockH264::_mvX[0], _mvY[0], quarter pels; 2 shorts) and
+ * intra flag (MacroBlockH264::_intraFlag; NULL: all inter).  prev_mv NULL: all
+ * zero.  Kept for every later estimate of the handle until set again.  A vector
+ * whose block origin (full pels, C division) leaves [-16, width] x [-16, height],
+ * which an earlier estimate never produces and for which the reference would
+ * read outside its buffers, is refused with VPPGPU_ERR_INVALID_ARG.  Other kinds:
+ * VPPGPU_ERR_UNSUPPORTED.  Synchronous. */
+int vppgpu_me_set_prev_frame(vppgpu_me* me, const short* prev_mv, const unsigned char* prev_intra);
 
 /* Status of the last device-side estimate (pixel-range or timeout flags);
  * synchronises the context stream. */

@@ -60,6 +60,7 @@ class Oracle:
         L.vo_me_multires.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_me_multires_cross_v2_lambda.argtypes = [_P, _P, _I, _I, _I, _I, C.c_double, _P, _P, _P, _P,
                                                      C.POINTER(_L)]
+        L.vo_me_umhs.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, C.POINTER(_L)]
         L.vo_mc_compensate.argtypes = [_P, _I, _I, _I, _P]
         L.vo_add_clip255.argtypes = [_P, _P, C.c_longlong]
         L.vo_sub.argtypes = [_P, _P, C.c_longlong]
@@ -150,6 +151,26 @@ class Oracle:
     def me_cross(self, src, ref, motion_range, mode=0, dist_incl=None, slice_map=None, with_ties=False):
         """MotionEstimatorH264ImplCross (mode 0 quarter, 1 half, 2 full pel)."""
         return self._me_pred(self.lib.vo_me_cross, src, ref, motion_range, mode, dist_incl, slice_map, with_ties)
+
+    def me_umhs(self, src, ref, motion_range, mode=0, dist_incl=None, slice_map=None, prev_mv=None,
+                prev_intra=None):
+        """MotionEstimatorH264ImplUMHS: vectors, the distortion stored with each, the average."""
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = self.lib.vo_num_mbs(w, h)
+        mv = np.zeros((nmb, 2), np.int16)
+        dist = np.zeros(nmb, np.int32)
+        avg = _L(0)
+        incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
+        sl = None if slice_map is None else np.ascontiguousarray(slice_map, dtype=np.int32)
+        pmv = None if prev_mv is None else np.ascontiguousarray(prev_mv, dtype=np.int16)
+        pin = None if prev_intra is None else np.ascontiguousarray(prev_intra, dtype=np.uint8)
+        rc = self.lib.vo_me_umhs(_ptr(src), _ptr(ref), w, h, motion_range, mode, _ptr(incl), _ptr(sl), _ptr(pmv),
+                                 _ptr(pin), _ptr(mv), _ptr(dist), C.byref(avg))
+        if rc:
+            raise ValueError(f"vo_me_umhs rc={rc}")
+        return mv, dist, avg.value
 
     def _me_pred(self, fn, src, ref, motion_range, mode, dist_incl, slice_map, with_ties):
         h, w = src.shape
@@ -311,6 +332,7 @@ class Reference:
         L = self.lib
         L.ref_me_estimate.argtypes = [_I, _P, _P, _I, _I, _I, _I, _P, _P, _I, _P, C.POINTER(_L)]
         L.ref_me_full_sad.argtypes = [_P, _P, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
+        L.ref_me_umhs.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P, C.POINTER(_L)]
         L.ref_fwd_transform.argtypes = [_I, _P, _I, _I, _I, _I]
         L.ref_inv_transform.argtypes = [_I, _P, _I, _I, _I, _P]
         L.ref_quantise_value.argtypes = [C.c_short, _I, _I, _I]
@@ -357,6 +379,25 @@ class Reference:
                                       C.byref(avg))
         if rc:
             raise ValueError(f"ref_me_full_sad rc={rc}")
+        return mv, dist, avg.value
+
+    def me_umhs(self, src, ref, motion_range, mode=0, dist_incl=None, prev_mv=None, prev_intra=None):
+        """MotionEstimatorH264ImplUMHS (eight-argument constructor): vectors, the
+        distortion stored with each for the predictor, the average."""
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = (w // 16) * (h // 16)
+        mv = np.zeros((nmb, 2), np.int16)
+        dist = np.zeros(nmb, np.int32)
+        avg = _L(0)
+        incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
+        pmv = None if prev_mv is None else np.ascontiguousarray(prev_mv, dtype=np.int16)
+        pin = None if prev_intra is None else np.ascontiguousarray(prev_intra, dtype=np.uint8)
+        rc = self.lib.ref_me_umhs(_ptr(src), _ptr(ref), w, h, motion_range, mode, _ptr(incl), _ptr(pmv), _ptr(pin),
+                                  _ptr(mv), _ptr(dist), C.byref(avg))
+        if rc:
+            raise ValueError(f"ref_me_umhs rc={rc}")
         return mv, dist, avg.value
 
     def mc_compensate(self, y, u, v, mv, range_):

@@ -193,8 +193,9 @@ static const int SUB_Y[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
 
 /* Half-pel pass then quarter-pel pass around the full-pel winner at ext
  * origin (ox, oy) (Full.cpp:452-517).  *min_d enters as the full-pel minimum
- * and leaves as the refined one; returns the quarter-pel refinement. */
-static void subpel_refine(const short* in, int ins, const short* e, int es, int ox, int oy,
+ * and leaves as the refined one; returns the quarter-pel refinement.
+ * quarter == 0: the half-pel pass only (a half-pel SetMode). */
+static void subpel_refine(const short* in, int ins, const short* e, int es, int ox, int oy, int quarter,
                           int* min_d, int* qmx, int* qmy)
 {
     subpel_win w;
@@ -210,7 +211,7 @@ static void subpel_refine(const short* in, int ins, const short* e, int es, int 
         if (d < best) { best = d; hmx = qx; hmy = qy; }
     }
     int bx = hmx, by = hmy;
-    for (int k = 0; k < 8; k++) {
+    for (int k = 0; quarter && k < 8; k++) {
         for (int r = 0; r < 16; r++)
             for (int c = 0; c < 16; c++)
                 blk[r * 16 + c] = (short)win_quarter(&w, 4 * r + hmy, 4 * c + hmx, SUB_Y[k], SUB_X[k]);
@@ -301,7 +302,7 @@ int vo_me_full_detail(const short* src, const short* ref, int w, int h, int moti
         int ox = vo_clamp_origin(n + mx + EXT_BORDER, es, MB);
         int oy = vo_clamp_origin(m + my + EXT_BORDER, h + 2 * EXT_BORDER, MB);
         int qmx, qmy;
-        subpel_refine(in, w, e, es, ox, oy, &min_d, &qmx, &qmy);
+        subpel_refine(in, w, e, es, ox, oy, 1, &min_d, &qmx, &qmy);
         int mvx = 4 * mx + qmx, mvy = 4 * my + qmy;
         if (sub_mv) { sub_mv[2 * k] = mvx; sub_mv[2 * k + 1] = mvy; }
         if (min_dv) min_dv[k] = min_d;
@@ -568,6 +569,287 @@ int vo_me_cross(const short* src, const short* ref, int w, int h, int motion_ran
     }
     if (avg_dist) *avg_dist = included ? total / included : 0;
     vo_pred_free(&ps);
+    free(e);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* MotionEstimatorH264ImplUMHS                                               */
+/* ------------------------------------------------------------------------ */
+/* Pattern tables of MotionEstimatorH264ImplUMHS.cpp:82-122, {x, y} offsets in
+ * the order the reference tests them. */
+static const signed char UMHS_5X5[24][2] = {
+    {-1, 0}, {1, 0}, {0, -1}, {0, 1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}, {0, -2}, {-2, 0}, {2, 0}, {0, 2},
+    {-1, -2}, {1, -2}, {-2, -1}, {2, -1}, {-2, 1}, {2, 1}, {-1, 2}, {1, 2}, {-2, -2}, {2, -2}, {-2, 2}, {2, 2}};
+static const signed char UMHS_CROSS[4][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}};
+static const signed char UMHS_HEX[16][2] = {{-4, 0}, {4, 0},  {-4, 1}, {4, 1},  {-4, -1}, {4, -1}, {-4, 2}, {4, 2},
+                                            {-4, -2}, {4, -2}, {-2, 3}, {2, 3}, {-2, -3}, {2, -3}, {0, 4},  {0, -4}};
+static const signed char UMHS_EXTHEX[6][2] = {{-2, 0}, {-1, -2}, {1, -2}, {2, 0}, {1, 2}, {-1, 2}};
+
+/* MEH264IUMHS_COST (MotionEstimatorH264ImplUMHS.cpp:179): D/256 plus 1.05 x the
+ * Euclidean distance to the reference vector, in double, truncated to int. */
+static int umhs_cost(int d, int x, int y, int xr, int yr)
+{
+    const double mag = sqrt((double)((x - xr) * (x - xr) + (y - yr) * (y - yr)));
+    return (int)(((double)d / 256.0) + (1.05 * mag));
+}
+
+/* MacroBlockH264::GetMbMotionMedianPred with the distortion output
+ * (MacroBlockH264.cpp:818-915): the median vector of A, B, C (D for a missing
+ * C; B and C take A when both are missing), and the smaller of the
+ * distortions attached to each median component: among the neighbours whose
+ * component equals the median, A first, then B and C if smaller.  The y
+ * component compares C's x component with the median (MacroBlockH264.cpp:898),
+ * kept as it is. */
+static void umhs_pred_get(const vo_pred_state* st, const int* dist, int k, int* px, int* py, int* pd)
+{
+    int r = k / st->cols, c = k % st->cols;
+    int a = nb_avail(st, k, r, c - 1);
+    int b = nb_avail(st, k, r - 1, c);
+    int cc = nb_avail(st, k, r - 1, c + 1);
+    int ax = 0, ay = 0, ad = 0, bx = 0, by = 0, bd = 0, cx = 0, cy = 0, cd = 0;
+    if (a >= 0) { ax = st->mvx[a]; ay = st->mvy[a]; ad = dist[a]; }
+    if (b >= 0) { bx = st->mvx[b]; by = st->mvy[b]; bd = dist[b]; }
+    if (cc >= 0) { cx = st->mvx[cc]; cy = st->mvy[cc]; cd = dist[cc]; }
+    else {
+        int d = nb_avail(st, k, r - 1, c - 1);
+        if (d >= 0) { cx = st->mvx[d]; cy = st->mvy[d]; cd = dist[d]; }
+    }
+    if (b < 0 && cc < 0) { bx = cx = ax; by = cy = ay; bd = cd = ad; }
+    const int x = vo_median3(ax, bx, cx), y = vo_median3(ay, by, cy);
+    int xd = ad;
+    if (x == bx && bd < xd) xd = bd;
+    if (x == cx && cd < xd) xd = cd;
+    int yd = ad;
+    if (y == by && bd < yd) yd = bd;
+    if (y == cx && cd < yd) yd = cd;
+    *px = x;
+    *py = y;
+    *pd = yd < xd ? yd : xd;
+}
+
+/* State of one macroblock's UMHS search: the running best (its distortion
+ * and cost), the pattern centre and the refinement offset from it. */
+typedef struct {
+    const short* in;
+    int ins;
+    const short* e;
+    int es, w, h, n, m;
+    int xl, xr, yu, yd;
+    int px0, py0;  /* full-pel prediction after truncation: the cost reference */
+    int mx, my, rmx, rmy, min_d, min_cost;
+} umhs_search;
+
+static int umhs_sd(const umhs_search* s, int x, int y)
+{
+    const int ox = vo_clamp_origin(s->n + x + EXT_BORDER, s->es, MB);
+    const int oy = vo_clamp_origin(s->m + y + EXT_BORDER, s->h + 2 * EXT_BORDER, MB);
+    return vo_tsd16(s->in, s->ins, s->e + (size_t)oy * s->es + ox, s->es);
+}
+
+/* One candidate offset (j, i) from the centre, as every pattern loop of
+ * MotionEstimatorH264ImplUMHS::Estimate tests it: inside the range, D not
+ * above the running minimum (Tsd16x16LessThan decides as the full SSD), then
+ * a strictly lower cost. */
+static void umhs_probe(umhs_search* s, int j, int i)
+{
+    if (i + s->my < s->yu || i + s->my > s->yd || j + s->mx < s->xl || j + s->mx > s->xr) return;
+    const int ox = vo_clamp_origin(s->n + s->mx + j + EXT_BORDER, s->es, MB);
+    const int oy = vo_clamp_origin(s->m + s->my + i + EXT_BORDER, s->h + 2 * EXT_BORDER, MB);
+    const int d = vo_tsd16_lt(s->in, s->ins, s->e + (size_t)oy * s->es + ox, s->es, s->min_d);
+    if (d > s->min_d) return;
+    const int cost = umhs_cost(d, s->mx + j, s->my + i, s->px0, s->py0);
+    if (cost < s->min_cost) {
+        s->min_d = d;
+        s->min_cost = cost;
+        s->rmx = j;
+        s->rmy = i;
+    }
+}
+
+/* MotionEstimatorH264ImplUMHS::Estimate (MotionEstimatorH264ImplUMHS.cpp:446-945).
+ * Per macroblock in raster order: the median prediction with its distortion,
+ * truncated to one macroblock outside the picture; starting points at the
+ * prediction, zero and the previous frame's co-located vector; early exits on
+ * absolute and prediction-relative thresholds; the unsymmetrical cross, 5x5,
+ * multi-hexagon, extended hexagon and diamond patterns; the half / quarter
+ * passes of the full-search window; the prediction check at quarter-pel
+ * costs.  The chosen vector and its distortion feed later predictions. */
+int vo_me_umhs(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+               const unsigned char* dist_incl, const int* slice, const short* prev_mv,
+               const unsigned char* prev_intra, short* mv_out, int* mb_dist, long* avg_dist)
+{
+    if (!src || !ref || !mv_out || w < MB || h < MB || (w % MB) != 0 || motion_range < 4) return -1;
+    int cols = w / MB, rows = h / MB, nmb = cols * rows;
+    int es = w + 2 * EXT_BORDER;
+    short* e = vo_ext_alloc(ref, w, h, EXT_BORDER);
+    int* dist = (int*)calloc((size_t)nmb, sizeof(int));
+    vo_pred_state ps;
+    if (!e || !dist || vo_pred_init(&ps, cols, rows, slice) != 0) {
+        free(e);
+        free(dist);
+        vo_pred_free(&ps);
+        return -2;
+    }
+    /* A previous-frame vector is a starting point whose block the reference
+     * reads through its clamped extended-reference overlay; should it win,
+     * the sub-pel window around it is read unclamped.  Vectors whose block
+     * origin leaves [-16, w] x [-16, h] (what a previous estimate never gives)
+     * would make it read outside its buffers: refused. */
+    for (int k = 0; prev_mv && k < nmb; k++) {
+        const int x = (k % cols) * MB + prev_mv[2 * k] / 4, y = (k / cols) * MB + prev_mv[2 * k + 1] / 4;
+        if (!(prev_intra && prev_intra[k]) && (x < -MB || x > w || y < -MB || y > h)) {
+            free(e);
+            free(dist);
+            vo_pred_free(&ps);
+            return -3;
+        }
+    }
+    const int mrng = motion_range / 4;
+    long total = 0;
+    int included = 0;
+    for (int k = 0; k < nmb; k++) {
+        umhs_search s;
+        s.n = (k % cols) * MB;
+        s.m = (k / cols) * MB;
+        s.in = src + (size_t)s.m * w + s.n;
+        s.ins = w;
+        s.e = e;
+        s.es = es;
+        s.w = w;
+        s.h = h;
+        int px, py, pred_d;
+        umhs_pred_get(&ps, dist, k, &px, &py, &pred_d);
+        const int pxq = px % 4, pyq = py % 4;
+        int px0 = px / 4, py0 = py / 4;
+        const int opx0 = px0, opy0 = py0;
+        if (px0 + s.n > w) px0 = MB;
+        if (px0 + s.n < -MB) px0 = -MB;
+        if (py0 + s.m > h) py0 = MB;
+        if (py0 + s.m < -MB) py0 = -MB;
+        const int truncated = opx0 != px0 || opy0 != py0;
+        s.px0 = px0;
+        s.py0 = py0;
+        full_range(s.n, s.m, w, h, motion_range, mrng, &s.xl, &s.xr, &s.yu, &s.yd);
+
+        /* starting points (:489-571) */
+        int pred_vd = umhs_sd(&s, px0, py0);
+        s.min_d = pred_vd;
+        s.mx = px0;
+        s.my = py0;
+        s.min_cost = pred_vd / 256;
+        if (px0 || py0) {
+            const int zd = umhs_sd(&s, 0, 0);
+            const int zc = umhs_cost(zd, 0, 0, px0, py0);
+            if (zc < s.min_cost) { s.min_d = zd; s.min_cost = zc; s.mx = 0; s.my = 0; }
+        }
+        if (!(prev_intra && prev_intra[k])) {
+            const int pvx0 = prev_mv ? prev_mv[2 * k] / 4 : 0, pvy0 = prev_mv ? prev_mv[2 * k + 1] / 4 : 0;
+            if ((pvx0 || pvy0) && pvx0 != px0 && pvy0 != py0) {
+                const int vd = umhs_sd(&s, pvx0, pvy0);
+                const int vc = umhs_cost(vd, pvx0, pvy0, px0, py0);
+                if (vc < s.min_cost) { s.min_d = vd; s.min_cost = vc; s.mx = pvx0; s.my = pvy0; }
+            }
+        }
+        int prior;
+        if (s.min_d < 1000) goto diamond;
+        if (s.min_d < 4000 || (s.min_d == pred_vd && s.min_d < pred_d * 12 / 10 && s.min_d > pred_d * 8 / 10))
+            goto hexagon;
+
+        /* unsymmetrical cross, vertical reach below half the range (:573-623) */
+        s.rmx = s.rmy = 0;
+        prior = s.min_d;
+        for (int wgt = 1; wgt < 16; wgt += 2)
+            for (int x = 0; x < 4; x++) {
+                const int i = wgt * UMHS_CROSS[x][1], j = wgt * UMHS_CROSS[x][0];
+                if (i < mrng / 2 && i > -mrng / 2) umhs_probe(&s, j, i);
+            }
+        s.mx += s.rmx;
+        s.my += s.rmy;
+        if (s.min_d < 1000) goto diamond;
+        if (s.min_d < 2000 ||
+            (s.min_d < prior * 9 / 10 && (s.rmx || s.rmy) && abs(s.rmx) <= 3 && abs(s.rmy) <= 3))
+            goto hexagon;
+
+        /* 5x5 without the points the cross already tested (:625-656) */
+        {
+            const int crx = s.rmx, cry = s.rmy;
+            s.rmx = s.rmy = 0;
+            for (int x = 0; x < 24; x++) {
+                const int j = UMHS_5X5[x][0], i = UMHS_5X5[x][1];
+                const int tested = (crx || cry) && ((cry == 0 && (j == 2 || j == -2)) || (crx == 0 && (i == 2 || i == -2)));
+                if (!tested) umhs_probe(&s, j, i);
+            }
+        }
+        /* the centre stays at the cross winner on this exit (:658-662) */
+        if (s.min_d < 1000) goto diamond;
+
+        /* multi-hexagon from the cross winner; the 5x5 offset stays a candidate (:664-702) */
+        prior = s.min_d;
+        for (int wgt = 1; wgt < 4; wgt++) {
+            for (int x = 0; x < 16; x++) umhs_probe(&s, wgt * UMHS_HEX[x][0], wgt * UMHS_HEX[x][1]);
+            if ((s.rmx || s.rmy) && (s.min_d < 2000 || s.min_d < prior / 5)) break;
+        }
+        s.mx += s.rmx;
+        s.my += s.rmy;
+
+    hexagon: /* extended hexagon until the centre wins (:705-736) */
+        do {
+            s.rmx = s.rmy = 0;
+            for (int x = 0; x < 6; x++) umhs_probe(&s, UMHS_EXTHEX[x][0], UMHS_EXTHEX[x][1]);
+            s.mx += s.rmx;
+            s.my += s.rmy;
+        } while (s.rmx || s.rmy);
+
+    diamond: /* small diamond until the centre wins (:739-769) */
+        do {
+            s.rmx = s.rmy = 0;
+            for (int x = 0; x < 4; x++) umhs_probe(&s, UMHS_CROSS[x][0], UMHS_CROSS[x][1]);
+            s.mx += s.rmx;
+            s.my += s.rmy;
+        } while (s.rmx || s.rmy);
+
+        /* half / quarter passes (:790-867) */
+        int min_d = s.min_d;
+        int mvx = 4 * s.mx, mvy = 4 * s.my;
+        if (mode != 2) {
+            const int ox = vo_clamp_origin(s.n + s.mx + EXT_BORDER, es, MB);
+            const int oy = vo_clamp_origin(s.m + s.my + EXT_BORDER, h + 2 * EXT_BORDER, MB);
+            int qmx, qmy;
+            subpel_refine(s.in, w, e, es, ox, oy, mode != 1, &min_d, &qmx, &qmy);
+            mvx += qmx;
+            mvy += qmy;
+        }
+
+        /* the prediction at quarter pel against the winner (:869-908) */
+        const int rpx = 4 * px0 + pxq, rpy = 4 * py0 + pyq;
+        if (pxq || pyq) {
+            short blk[256];
+            const int pox = vo_clamp_origin(px0 + s.n + EXT_BORDER, es, MB);
+            const int poy = vo_clamp_origin(py0 + s.m + EXT_BORDER, h + 2 * EXT_BORDER, MB);
+            vo_qread16_ext(e, es, pox, poy, pxq, pyq, blk);
+            pred_vd = vo_tsd16(s.in, w, blk, 16);
+        } else if (truncated) {
+            pred_vd = umhs_sd(&s, px0, py0);
+        }
+        if (umhs_cost(pred_vd, rpx, rpy, px, py) <= umhs_cost(min_d, mvx, mvy, px, py)) {
+            min_d = pred_vd;
+            mvx = rpx;
+            mvy = rpy;
+        }
+        if (dist_incl && dist_incl[k]) {
+            included++;
+            total += min_d;
+        }
+        if (mb_dist) mb_dist[k] = min_d;
+        mv_out[2 * k] = (short)mvx;
+        mv_out[2 * k + 1] = (short)mvy;
+        vo_pred_set(&ps, k, mvx, mvy);
+        dist[k] = min_d;
+    }
+    if (avg_dist) *avg_dist = included ? total / included : 0;
+    vo_pred_free(&ps);
+    free(dist);
     free(e);
     return 0;
 }

@@ -19,6 +19,7 @@
 #include "MotionEstimatorH264ImplMultiresCross.h"
 #include "MotionEstimatorH264ImplMultiresCrossVer2.h"
 #include "MotionEstimatorH264ImplCross.h"
+#include "MotionEstimatorH264ImplUMHS.h"
 #include "MotionEstimatorH263ImplMultiresCross.h"
 #include "VectorStructList.h"
 #include "MotionCompensatorH264ImplStd.h"
@@ -212,6 +213,41 @@ int ref_me_estimate(int kind, const short* src, const short* ref, int w, int h, 
     if (avg_out) *avg_out = avg;
     delete me;
     delete[] flags;
+    return 0;
+}
+
+/* MotionEstimatorH264ImplUMHS through its eight-argument constructor (the
+ * others leave the previous-frame macroblocks unset, which Estimate reads).
+ * prev_mv / prev_intra (nullable: zero vectors, inter) fill the previous
+ * frame's macroblock array; entries past N_MB, read by a partial bottom row
+ * whose results are dropped, are intra.  dist_out: the distortion the
+ * estimator hands the predictor with each vector (MacroBlockH264::_distortion[0]). */
+int ref_me_umhs(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                const unsigned char* incl, const short* prev_mv, const unsigned char* prev_intra, short* mv_out,
+                int* dist_out, long* avg_out)
+{
+    int nmb = (w / 16) * (h / 16);
+    MbGrid grid(w, h);
+    H264MotionVectorPredictorImpl1 pred(grid.flat);
+    MacroBlockH264* prev = new MacroBlockH264[nmb + w / 16];
+    for (int i = 0; i < nmb + w / 16; i++) {
+        prev[i]._intraFlag = i < nmb ? (prev_intra ? (prev_intra[i] != 0) : 0) : 1;
+        prev[i]._mvX[MacroBlockH264::_16x16] = (i < nmb && prev_mv) ? prev_mv[2 * i] : 0;
+        prev[i]._mvY[MacroBlockH264::_16x16] = (i < nmb && prev_mv) ? prev_mv[2 * i + 1] : 0;
+    }
+    bool* flags = make_flags(incl, nmb);
+    MotionEstimatorH264ImplUMHS* me = new MotionEstimatorH264ImplUMHS(src, ref, w, h, motion_range, &pred, flags, prev);
+    if (!me->Create()) { delete me; delete[] flags; delete[] prev; return -2; }
+    me->SetMode(mode);
+    long avg = 0;
+    void* res = me->Estimate(&avg);
+    copy_vectors((VectorStructList*)res, nmb, mv_out);
+    if (dist_out)
+        for (int i = 0; i < nmb; i++) dist_out[i] = grid.flat[i]._distortion[0];
+    if (avg_out) *avg_out = avg;
+    delete me;
+    delete[] flags;
+    delete[] prev;
     return 0;
 }
 

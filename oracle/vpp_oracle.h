@@ -53,6 +53,21 @@ int vo_me_cross(const short* src, const short* ref, int w, int h, int motion_ran
                 const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist, long* avg_dist,
                 int* tie_out);
 
+/* MotionEstimatorH264ImplUMHS::Estimate (src/CodecUtils/MotionEstimatorH264ImplUMHS.cpp:446-945):
+ * unsymmetrical-cross multi-hexagon-grid search started at the median
+ * prediction, whose distortion (the five-argument predictor,
+ * MacroBlockH264.cpp:818-915) enters an early exit; the previous frame's
+ * co-located vector is a starting point.  mode 0 quarter, 1 half, 2 full pel.
+ *   prev_mv    : NULL (all zero) or 2*N_MB shorts, the previous frame's
+ *                macroblock vectors (MacroBlockH264::_mvX[0], _mvY[0]);
+ *   prev_intra : NULL (all inter) or N_MB flags (MacroBlockH264::_intraFlag).
+ * mb_dist receives the distortion the predictor stores with each vector.
+ * Returns -3 for a previous-frame vector whose block origin leaves
+ * [-16, w] x [-16, h]: the reference would read outside its buffers. */
+int vo_me_umhs(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+               const unsigned char* dist_incl, const int* slice, const short* prev_mv,
+               const unsigned char* prev_intra, short* mv_out, int* mb_dist, long* avg_dist);
+
 int vo_me_full(const short* src, const short* ref, int w, int h, int motion_range,
                const unsigned char* dist_incl, const int* slice,
                short* mv_out, int* mb_dist, long* avg_dist);

@@ -34,6 +34,12 @@ inputs and stores inputs and outputs:
 * yuv2rgb.npz     the five Real YUV420->RGB24 converters, every rotate / flip,
                   the two 6-bit converters (6-bit, wider and +-32767 samples,
                   both layouts) and the 6-bit zoom converter at several sizes
+* me_umhs.npz     MotionEstimatorH264ImplUMHS (eight-argument constructor):
+                  pan, integer-shift and part-noise pairs at QCIF / CIF and
+                  motion ranges 64 / 128, modes 0/1/2, seeded previous-frame
+                  vectors and intra flags, vectors, the distortion stored with
+                  each and avgDistortion; and pair 0 of the 1080p benchmark
+                  sequence (mode 0, zero previous vectors)
 * me_1080p.npz    the headline size: Full, MultiresCross / Ver2 / Multires
                   (modes 0, 1, 2), Cross and the integer-pel SAD stage on three
                   frame pairs of the 1920x1080 benchmark sequence at
@@ -41,7 +47,7 @@ inputs and stores inputs and outputs:
                   SHA-256)
 
 Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
-names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc mc
+names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc me_umhs mc
 transform dc yuv2rgb colour, default all)
 """
 from __future__ import annotations
@@ -220,6 +226,82 @@ def mrc2_lambda_fixtures(ref: oracle.Reference) -> dict:
             mv, avg = ref.me("multires_cross_v2", fr[1], fr[0], HD_RANGE, mode=mode, dist_incl=incl, lam=lam)
             out[f"hd_m{mode}_lam{lam:g}_mv"] = mv
             out[f"hd_m{mode}_lam{lam:g}_avg"] = np.array([avg], np.int64)
+    return out
+
+
+UMHS_CASES = [  # (name, w, h, motion_range, seed, generator)
+    ("qcif_r64", 176, 144, 64, 71, "pan"),
+    ("cif_r128", 352, 288, 128, 72, "pan"),
+    ("shift_r128", 176, 144, 128, 73, "shift"),
+    ("noisy_r128", 352, 288, 128, 74, "noisy"),
+    ("small_r32", 64, 48, 32, 75, "noisy"),
+]
+
+
+def prev_frame_vectors(seed: int, w: int, h: int, motion_range: int):
+    """Seeded previous-frame macroblock vectors (quarter pels) whose blocks stay
+    within [-16, w] x [-16, h] (as an earlier estimate's do), and intra flags."""
+    rng = np.random.default_rng(seed)
+    cols, rows = w // 16, h // 16
+    nmb = cols * rows
+    mv = rng.integers(-motion_range, motion_range, size=(nmb, 2)).astype(np.int64)
+    full = np.where(mv < 0, -((-mv) // 4), mv // 4)
+    x = (np.arange(nmb) % cols) * 16 + full[:, 0]
+    y = (np.arange(nmb) // cols) * 16 + full[:, 1]
+    mv[:, 0] = np.where((x < -16) | (x > w), 0, mv[:, 0])
+    mv[:, 1] = np.where((y < -16) | (y > h), 0, mv[:, 1])
+    intra = (rng.random(nmb) < 0.2).astype(np.uint8)
+    return mv.astype(np.int16), intra
+
+
+def umhs_frames(seed: int, w: int, h: int, gen: str):
+    """A frame pair: the pan or shift sequence, or ("noisy") a pan pair whose
+    second frame has 40 % of its macroblocks replaced by uniform noise (large
+    distortions take every stage of the search)."""
+    if gen == "shift":
+        return synth.shift_sequence(seed, w, h, 2)
+    fr = synth.pan_sequence(seed, w, h, 2)
+    if gen == "noisy":
+        rng = np.random.default_rng(seed)
+        mask = np.kron(rng.random((h // 16, w // 16)) < 0.4, np.ones((16, 16), bool))
+        noise = rng.integers(0, 256, size=mask.shape).astype(np.int16)
+        cur = fr[1].copy()
+        cur[:mask.shape[0], :mask.shape[1]][mask] = noise[mask]
+        fr = [fr[0], cur]
+    return fr
+
+
+def umhs_fixtures(ref: oracle.Reference) -> dict:
+    out = {}
+    for name, w, h, mr, seed, gen in UMHS_CASES:
+        fr = umhs_frames(seed, w, h, gen)
+        src, rf = fr[1], fr[0]
+        nmb = (w // 16) * (h // 16)
+        incl = (np.arange(nmb) % 4 != 1).astype(np.uint8)
+        pmv, pin = prev_frame_vectors(seed + 1000, w, h, mr)
+        out[f"{name}_src"] = src.astype(np.uint8)
+        out[f"{name}_ref"] = rf.astype(np.uint8)
+        out[f"{name}_meta"] = np.array([w, h, mr], np.int32)
+        out[f"{name}_incl"] = incl
+        out[f"{name}_prev_mv"] = pmv
+        out[f"{name}_prev_intra"] = pin
+        for mode in (0, 1, 2):
+            mv, d, avg = ref.me_umhs(src, rf, mr, mode=mode, dist_incl=incl, prev_mv=pmv, prev_intra=pin)
+            out[f"{name}_m{mode}_mv"] = mv
+            out[f"{name}_m{mode}_dist"] = d
+            out[f"{name}_m{mode}_avg"] = np.array([avg], np.int64)
+        # without previous vectors or inclusion flags
+        mv, d, avg = ref.me_umhs(src, rf, mr, mode=0)
+        out[f"{name}_noprev_mv"] = mv
+        out[f"{name}_noprev_dist"] = d
+    fr, digest = hd_frames()
+    incl = np.ones((HD_W // 16) * (HD_H // 16), np.uint8)
+    out["hd_meta"] = np.array([HD_SEED, HD_W, HD_H, HD_RANGE, 0], np.int32)
+    out["hd_frames_sha256"] = digest
+    mv, d, avg = ref.me_umhs(fr[1], fr[0], HD_RANGE, mode=0, dist_incl=incl)
+    out["hd_mv"] = mv
+    out["hd_dist"] = d
+    out["hd_avg"] = np.array([avg], np.int64)
     return out
 
 
@@ -411,6 +493,7 @@ def main() -> None:
               "me_mrc2_lambda": mrc2_lambda_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "me_cross": lambda r: mrc2_fixtures(r, "cross"),
               "me_h263mrc": lambda r: mrc_fixtures(r, "h263_multires_cross", H263_CASES),
+              "me_umhs": umhs_fixtures,
               "mc": mc_fixtures,
               "transform": transform_fixtures, "dc": dc_fixtures, "yuv2rgb": yuv2rgb_fixtures,
               "colour": colour_fixtures}

@@ -464,3 +464,67 @@ def test_port_matches_reference_at_1080p(orc, hd_golden):
         assert avg == int(g[f"{key}_avg"][0]), key
         if dist is not None:
             np.testing.assert_array_equal(dist, g[f"{key}_dist"], err_msg=key)
+
+
+UMHS_CASES = ["qcif_r64", "cif_r128", "shift_r128", "noisy_r128", "small_r32"]
+
+
+@pytest.mark.parametrize("case", UMHS_CASES)
+def test_me_umhs_matches_reference(orc, golden, case):
+    """MotionEstimatorH264ImplUMHS: vectors, the distortion stored with each
+    vector for the predictor, and the average, modes 0/1/2 with previous-frame
+    vectors and intra flags, and once without either."""
+    g = golden("me_umhs.npz")
+    w, h, mr = (int(v) for v in g[f"{case}_meta"])
+    src, ref = g[f"{case}_src"].astype(np.int16), g[f"{case}_ref"].astype(np.int16)
+    for mode in (0, 1, 2):
+        mv, dist, avg = orc.me_umhs(src, ref, mr, mode=mode, dist_incl=g[f"{case}_incl"],
+                                    prev_mv=g[f"{case}_prev_mv"], prev_intra=g[f"{case}_prev_intra"])
+        np.testing.assert_array_equal(mv, g[f"{case}_m{mode}_mv"], err_msg=f"mode {mode}")
+        np.testing.assert_array_equal(dist, g[f"{case}_m{mode}_dist"], err_msg=f"mode {mode}")
+        assert avg == int(g[f"{case}_m{mode}_avg"][0])
+    mv, dist, avg = orc.me_umhs(src, ref, mr)
+    np.testing.assert_array_equal(mv, g[f"{case}_noprev_mv"])
+    np.testing.assert_array_equal(dist, g[f"{case}_noprev_dist"])
+    assert avg == 0
+
+
+def test_me_umhs_1080p_matches_reference(orc, golden, hd_golden):
+    g = golden("me_umhs.npz")
+    assert g["hd_frames_sha256"].tobytes() == hd_golden["g"]["frames_sha256"].tobytes()
+    fr, mr = hd_golden["frames"], hd_golden["motion_range"]
+    incl = np.ones((hd_golden["w"] // 16) * (hd_golden["h"] // 16), np.uint8)
+    mv, dist, avg = orc.me_umhs(fr[1], fr[0], mr, mode=0, dist_incl=incl)
+    np.testing.assert_array_equal(mv, g["hd_mv"])
+    np.testing.assert_array_equal(dist, g["hd_dist"])
+    assert avg == int(g["hd_avg"][0])
+
+
+def test_me_umhs_refuses_prev_vectors_outside_the_frame(orc):
+    """A previous-frame vector whose block leaves [-16, w] x [-16, h] would make
+    the reference read outside its buffers should it win: refused."""
+    fr = synth.pan_sequence(3, 64, 48, 2)
+    pmv = np.zeros((12, 2), np.int16)
+    pmv[0] = (-4 * 17, 0)
+    with pytest.raises(ValueError, match="rc=-3"):
+        orc.me_umhs(fr[1], fr[0], 128, prev_mv=pmv)
+    pin = np.zeros(12, np.uint8)
+    pin[0] = 1  # an intra macroblock's vector is not read
+    orc.me_umhs(fr[1], fr[0], 128, prev_mv=pmv, prev_intra=pin)
+
+
+@ref_available
+@pytest.mark.parametrize("seed,w,h,mr,mode,gen", [(81, 176, 144, 128, 0, "noisy"), (82, 208, 120, 96, 1, "pan"),
+                                                 (83, 96, 64, 256, 0, "shift"), (84, 640, 368, 128, 0, "noisy"),
+                                                 (85, 352, 288, 16, 2, "noisy")])
+def test_me_umhs_against_compiled_reference(orc, seed, w, h, mr, mode, gen):
+    from tests.golden.make_golden import prev_frame_vectors, umhs_frames
+    ref_lib = oracle_mod.Reference()
+    fr = umhs_frames(seed, w, h, gen)
+    pmv, pin = prev_frame_vectors(seed, w, h, mr)
+    incl = (synth.splitmix64(seed, (w // 16) * (h // 16)) & np.uint64(1)).astype(np.uint8)
+    r = ref_lib.me_umhs(fr[1], fr[0], mr, mode=mode, dist_incl=incl, prev_mv=pmv, prev_intra=pin)
+    o = orc.me_umhs(fr[1], fr[0], mr, mode=mode, dist_incl=incl, prev_mv=pmv, prev_intra=pin)
+    np.testing.assert_array_equal(o[0], r[0])
+    np.testing.assert_array_equal(o[1], r[1])
+    assert o[2] == r[2]
