@@ -206,6 +206,7 @@ vppgpu::UmhsArgs umhs_args(vppgpu_me* me)
     u.prev = me->d_uprev;
     u.order = me->d_uorder;
     u.sweeps = me->relax_sweeps < 1 ? 1 : me->relax_sweeps;
+    u.diag_limit = 256;
     return u;
 }
 
@@ -327,12 +328,14 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     me->mode = (kind == VPPGPU_ME_CROSS || kind == VPPGPU_ME_UMHS) ? 0 : 1;
     me->rstride = width + 2 * vppgpu::PAD;
     me->sweep_limit = vppgpu::RELAX_SWEEPS + 2 + (me->nmb + 31) / 32;  // sweep counters, then the dirty bitmap
+    if (kind == VPPGPU_ME_UMHS && me->sweep_limit < vppgpu::UMHS_SWEEPS + 2)  // its counters only, up to 24 sweeps
+        me->sweep_limit = vppgpu::UMHS_SWEEPS + 2;
     // Sweep policy by how the estimator's predictions settle on moving content
     // (measured over 1080p pans): the full-search estimator mostly settles
     // within 8 sweeps over every MB, a few more over the dirty sets; Multires
     // keeps settling with more sweeps, cheaply over the dirty sets; Ver2
     // rarely settles, so its wavefront starts early.
-    me->relax_sweeps = kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : (kind == VPPGPU_ME_UMHS ? 6 : vppgpu::RELAX_SWEEPS);
+    me->relax_sweeps = kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : (kind == VPPGPU_ME_UMHS ? 20 : vppgpu::RELAX_SWEEPS);
     me->grid_sweeps = kind == VPPGPU_ME_MULTIRES ? 4 : (kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : 8);
     me->relax_blocks_per_sm = 4;
     me->mrc_warps = 8;
@@ -417,12 +420,19 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
                 if (c >= 0 && c < me->cols) order.push_back(r * me->cols + c);
             }
         if (cudaMemcpy(me->d_uorder, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemset(me->d_uprev, 0, sizeof(int) * (size_t)me->nmb) != cudaSuccess) {
+            cudaMemset(me->d_uprev, 0, sizeof(int) * (size_t)me->nmb) != cudaSuccess ||
+            cudaMemset(me->d_ustate, 0, sizeof(unsigned long long) * (size_t)me->nmb) != cudaSuccess) {
             me_free(me);
             return VPPGPU_ERR_CUDA;
         }
+        // one CTA of 4 warps per SM: a wavefront holds at most min(rows, cols / 2)
+        // macroblocks at a time, and warps holding later tickets only wait
         const int g = (me->nmb + 3) / 4;
-        me->wave_grid = g < 4 * ctx->sm_count ? g : 4 * ctx->sm_count;
+        me->wave_grid = g < ctx->sm_count ? g : ctx->sm_count;
+        if ((rc = vppgpu::umhs_prepare())) {
+            me_free(me);
+            return rc;
+        }
         *out = me;
         return VPPGPU_OK;
     }
@@ -675,7 +685,8 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 
 extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
 {
-    if (!me || sweeps < 0 || sweeps > vppgpu::RELAX_SWEEPS) return VPPGPU_ERR_INVALID_ARG;
+    if (!me || sweeps < 0 || sweeps > (me->kind == VPPGPU_ME_UMHS ? vppgpu::UMHS_SWEEPS : vppgpu::RELAX_SWEEPS))
+        return VPPGPU_ERR_INVALID_ARG;
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS ||
         me->kind == VPPGPU_ME_FULL_SAD)
         return VPPGPU_ERR_UNSUPPORTED;
@@ -741,7 +752,7 @@ extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src
         for (int w : {2, 4, 8})
             if (w != cur.warps) cands.push_back({cur.relax, cur.grid, cur.bps, w});
     } else if (me->kind == VPPGPU_ME_UMHS) {  // only the sweeps before the dataflow pass matter
-        for (int r : {1, 2, 4, 6, 8, 12})
+        for (int r : {4, 8, 12, 16, 20, 24})
             if (r != cur.relax) cands.push_back({r, cur.grid, cur.bps, cur.warps});
     } else {
         const int policies[][2] = {{4, 4}, {8, 8}, {14, 8}, {14, 4}, {14, 2}};

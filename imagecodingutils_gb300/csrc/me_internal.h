@@ -149,7 +149,8 @@ int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, cons
 // records; unless a sweep changes nothing (the fixed point, which is the
 // sequential result), a dataflow pass over the wavefront order settles the
 // exact raster result, looking predictions up in the records first.
-constexpr int UMHS_RECORDS = 4;  // records per macroblock
+constexpr int UMHS_RECORDS = 8;  // records per macroblock
+constexpr int UMHS_SWEEPS = 24;  // most relaxation sweeps
 struct UmhsArgs {
     FullArgs f;                 // planes, geometry, job, control, change counters
     unsigned long long* state;  // per MB: sweep state, packed vector | distortion << 32
@@ -158,10 +159,13 @@ struct UmhsArgs {
     const int* prev;            // per MB: the previous frame's full-pel starting point (packed; 0: none)
     const int* order;           // dataflow ticket -> macroblock (anti-diagonals c + 2r, rows ascending)
     int sweeps;                 // relaxation sweeps before the dataflow pass (>= 1)
+    int diag_limit;             // last-sweep changes up to which the one-CTA diagonal pass decides
 };
 // The planes, `sweeps` relaxation sweeps, the dataflow pass (wave_grid CTAs of
 // 4 warps) and the outputs.
 int umhs_launch(vppgpu_ctx* ctx, const UmhsArgs& args, int wave_grid);
+// Once per device: the diagonal pass's shared-memory limit.
+int umhs_prepare();
 
 // Write this estimate's pointers to the device descriptor (a one-thread
 // kernel with the descriptor as its parameter: stream-ordered, no host copy).

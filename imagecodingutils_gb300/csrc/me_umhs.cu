@@ -41,15 +41,18 @@ __device__ __forceinline__ unsigned long long state_word(int mv, int d)
 __device__ __forceinline__ int state_mv(unsigned long long s) { return (int)(unsigned)(s & 0xffffffffull); }
 __device__ __forceinline__ int state_d(unsigned long long s) { return (int)(unsigned)(s >> 32); }
 
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p)
+// A published state is one 64-bit word holding all a reader needs (vector and
+// distortion), so the dataflow pass publishes and polls with relaxed
+// device-scope accesses: no other data is ordered by them.
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p)
 {
     unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v)
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v)
 {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 // MEH264IUMHS_COST (MotionEstimatorH264ImplUMHS.cpp:179): (int)(D/256.0 +
@@ -80,15 +83,54 @@ __device__ __forceinline__ int sd_part(const FullArgs& a, int x0, int y0, uint2 
     return ssd8(cur, load8(p));
 }
 
-// Pattern tables of MotionEstimatorH264ImplUMHS.cpp:82-122 ({x, y} offsets in
-// the reference's test order).
-__constant__ signed char kSq5[24][2] = {{-1, 0},  {1, 0},  {0, -1}, {0, 1},  {-1, -1}, {1, -1}, {-1, 1}, {1, 1},
-                                        {0, -2},  {-2, 0}, {2, 0},  {0, 2},  {-1, -2}, {1, -2}, {-2, -1}, {2, -1},
-                                        {-2, 1},  {2, 1},  {-1, 2}, {1, 2},  {-2, -2}, {2, -2}, {-2, 2}, {2, 2}};
-__constant__ signed char kCross[4][2] = {{-1, 0}, {1, 0}, {0, -1}, {0, 1}};
-__constant__ signed char kHex[16][2] = {{-4, 0},  {4, 0},  {-4, 1}, {4, 1},  {-4, -1}, {4, -1}, {-4, 2}, {4, 2},
-                                        {-4, -2}, {4, -2}, {-2, 3}, {2, 3}, {-2, -3}, {2, -3}, {0, 4},  {0, -4}};
-__constant__ signed char kExtHex[6][2] = {{-2, 0}, {-1, -2}, {1, -2}, {2, 0}, {1, 2}, {-1, 2}};
+// The search window of one macroblock in shared memory: rows m-31 .. m+46,
+// columns n-32 .. n+47 of the padded reference (every candidate of a +-31
+// range; 16-byte aligned rows, filled with 16-byte loads), and the
+// macroblock's own 16x16 samples.
+constexpr int kWinRows = 78, kWinStride = 80;
+constexpr int kWinBytes = kWinRows * kWinStride;
+// per-warp slot: the window, 16 bytes the last row's five-word reads may
+// touch, and the 256-byte template
+constexpr int kWinSlot = kWinBytes + 16 + 256;
+
+__device__ __forceinline__ void window_fill(const FullArgs& a, int n, int m, unsigned char* win, int lane)
+{
+    const unsigned char* src = a.refp + (size_t)(m - 31 + PAD) * a.rstride + (n - 32 + PAD);
+    constexpr int kVecs = kWinBytes / 16;  // 5 per row
+    for (int v = lane; v < kVecs; v += 32) {
+        const int r = v / 5, c = v - 5 * r;
+        *reinterpret_cast<uint4*>(win + r * kWinStride + 16 * c) =
+            __ldg(reinterpret_cast<const uint4*>(src + (size_t)r * a.rstride + 16 * c));
+    }
+    if (lane < 16)
+        *reinterpret_cast<uint4*>(win + kWinBytes + 16 + 16 * lane) =
+            __ldg(reinterpret_cast<const uint4*>(a.src8 + (size_t)(m + lane) * a.W + n));
+    __syncwarp();
+}
+
+// SSD of the whole 16x16 block at offset (x, y) from the macroblock, by one
+// lane: per row five window words, funnel-shifted to the block's 16 bytes,
+// against the template row (a broadcast read), |a-b| per byte and dp4a.
+__device__ __forceinline__ int lane_ssd(const unsigned char* win, int x, int y)
+{
+    const unsigned char* p = win + (31 + y) * kWinStride + 32 + x;
+    const uint4* t = reinterpret_cast<const uint4*>(win + kWinBytes + 16);
+    const unsigned* w = reinterpret_cast<const unsigned*>(reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)3);
+    const unsigned sh = (unsigned)(reinterpret_cast<uintptr_t>(p) & 3) * 8;
+    unsigned acc = 0;
+#pragma unroll 2
+    for (int r = 0; r < 16; r++) {
+        const unsigned* q = w + r * (kWinStride / 4);
+        const unsigned w0 = q[0], w1 = q[1], w2 = q[2], w3 = q[3], w4 = q[4];
+        const uint4 tr = t[r];
+        const unsigned d0 = __vabsdiffu4(__funnelshift_r(w0, w1, sh), tr.x);
+        const unsigned d1 = __vabsdiffu4(__funnelshift_r(w1, w2, sh), tr.y);
+        const unsigned d2 = __vabsdiffu4(__funnelshift_r(w2, w3, sh), tr.z);
+        const unsigned d3 = __vabsdiffu4(__funnelshift_r(w3, w4, sh), tr.w);
+        acc = __dp4a(d0, d0, __dp4a(d1, d1, __dp4a(d2, d2, __dp4a(d3, d3, acc))));
+    }
+    return (int)acc;
+}
 
 // One macroblock's search state; every lane of the warp holds the same copy.
 struct Search {
@@ -96,45 +138,73 @@ struct Search {
     int mx, my, rmx, rmy, min_d, min_cost;
 };
 
-// Candidates c = 0..K-1 at offsets off(c) = (j, i, tested) from the centre,
-// in the reference's order: a candidate in range with D <= the running
-// minimum and a strictly lower cost becomes the best offset (each pattern
-// loop of UMHS.cpp:590-767).  The K distortions are summed together (lane c
-// keeps candidate c's sum and its cost), then a ballot walk applies the
-// acceptances in order: a candidate the walk passes was rejected by the state
-// the reference had when it reached it, since the state only changes on an
-// acceptance.
-template <int K, typename Off>
-__device__ __forceinline__ void probe(const FullArgs& a, Search& s, uint2 cur, int lane, Off off)
+// Search patterns of MotionEstimatorH264ImplUMHS.cpp:82-122, as the steps of
+// the search's state machine.
+enum Pattern { P_CROSS, P_SQ5, P_HEX, P_EXTHEX, P_DIAMOND, P_DONE };
+
+// Offset (j, i) of candidate c of a pattern, in the reference's test order,
+// and whether the pattern tests it at all.  The tables are packed four bits
+// per coordinate (value + 4).
+__device__ __forceinline__ bool pattern_offset(int kind, int c, int w, int crx, int cry, int mrng, int& j, int& i)
 {
-    static_assert(K <= 32, "one candidate per lane");
-    int myd = 0, myj = 0, myi = 0;
-    bool myv = false;
-#pragma unroll
-    for (int c = 0; c < K; c++) {
-        int j, i;
-        bool v = off(c, j, i);
-        v = v && i + s.my >= s.yu && i + s.my <= s.yd && j + s.mx >= s.xl && j + s.mx <= s.xr;
-        const int part = v ? sd_part(a, s.n + s.mx + j, s.m + s.my + i, cur, lane) : 0;
-        const int sum = warp_sum(part);
-        if (lane == c) {
-            myd = sum;
-            myj = j;
-            myi = i;
-            myv = v;
-        }
+    auto nib = [](unsigned long long t, int e) { return (int)((t >> (4 * e)) & 15ull) - 4; };
+    switch (kind) {
+    case P_CROSS: {  // MEH264IUMHS_CrossPos at scales 1, 3, .., 15, vertical reach below half the range
+        const int s = 2 * (c >> 2) + 1, dir = c & 3;
+        j = dir == 0 ? -s : (dir == 1 ? s : 0);
+        i = dir == 2 ? -s : (dir == 3 ? s : 0);
+        return c < 32 && i < mrng / 2 && i > -mrng / 2;
     }
-    const int dx = s.mx + myj - s.px0, dy = s.my + myi - s.py0;
-    const int mycost = myv ? umhs_cost(myd, dx * dx + dy * dy) : 0;
+    case P_SQ5: {  // MEH264IUMHS_5x5Pos without the points the cross tested (:632-633)
+        if (c >= 24) return false;
+        j = c < 16 ? nib(0x6253462453534453ull, c) : nib(0x62625362ull, c - 16);
+        i = c < 16 ? nib(0x3322644255335344ull, c) : nib(0x66226655ull, c - 16);
+        return !((crx || cry) && ((cry == 0 && (j == 2 || j == -2)) || (crx == 0 && (i == 2 || i == -2))));
+    }
+    case P_HEX:  // MEH264IUMHS_HexPos at scale w
+        if (c >= 16) return false;
+        j = w * nib(0x4462628080808080ull, c);
+        i = w * nib(0x0811772266335544ull, c);
+        return true;
+    case P_EXTHEX:  // MEH264IUMHS_ExtHexPos
+        if (c >= 6) return false;
+        j = nib(0x356532ull, c);
+        i = nib(0x664224ull, c);
+        return true;
+    default:  // P_DIAMOND: MEH264IUMHS_CrossPos at scale 1
+        j = c == 0 ? -1 : (c == 1 ? 1 : 0);
+        i = c == 2 ? -1 : (c == 3 ? 1 : 0);
+        return c < 4;
+    }
+}
+
+// One pattern step: lane c takes candidate c (in range, D <= the running
+// minimum and a strictly lower cost make it the best offset: each pattern
+// loop of UMHS.cpp:590-767), computes its SSD and cost, then a ballot walk
+// applies the acceptances in the reference's order -- a candidate the walk
+// passes was rejected by the state the reference had when it reached it,
+// since the state only changes on an acceptance.
+__device__ __forceinline__ void probe(Search& s, int kind, int w, int crx, int cry, int mrng, const unsigned char* win,
+                                      int lane)
+{
+    int j = 0, i = 0;
+    bool v = pattern_offset(kind, lane, w, crx, cry, mrng, j, i);
+    v = v && i + s.my >= s.yu && i + s.my <= s.yd && j + s.mx >= s.xl && j + s.mx <= s.xr;
+    int d = 0, cost = 0;
+    if (v) {
+        d = lane_ssd(win, s.mx + j, s.my + i);
+        const int dx = s.mx + j - s.px0, dy = s.my + i - s.py0;
+        cost = umhs_cost(d, dx * dx + dy * dy);
+    }
     int last = -1;
     while (true) {
-        const unsigned m = __ballot_sync(0xffffffffu, myv && lane > last && myd <= s.min_d && mycost < s.min_cost);
+        const unsigned m = __ballot_sync(0xffffffffu, v && lane > last && d <= s.min_d && cost < s.min_cost);
         if (!m) break;
         const int f = __ffs(m) - 1;
-        s.min_d = __shfl_sync(0xffffffffu, myd, f);
-        s.min_cost = __shfl_sync(0xffffffffu, mycost, f);
-        s.rmx = __shfl_sync(0xffffffffu, myj, f);
-        s.rmy = __shfl_sync(0xffffffffu, myi, f);
+        s.min_d = __shfl_sync(0xffffffffu, d, f);
+        s.min_cost = __shfl_sync(0xffffffffu, cost, f);
+        s.rmx = __shfl_sync(0xffffffffu, j, f);
+        s.rmy = __shfl_sync(0xffffffffu, i, f);
         last = f;
     }
 }
@@ -143,8 +213,10 @@ __device__ __forceinline__ void probe(const FullArgs& a, Search& s, uint2 cur, i
 // (px, py) with distortion pd, one warp.  Returns the record {prediction,
 // outcome word, vector, distortion}; the outcome word says whether the
 // prediction's distortion decided the first early exit (UMHS.cpp:573-579)
-// and how: (start minimum << 1) | taken, else kNoPdTest.
-__device__ __noinline__ int4 umhs_evaluate(const UmhsArgs& u, int k, int px, int py, int pd, int lane, int* bad)
+// and how: (start minimum << 1) | taken, else kNoPdTest.  The reference's
+// gotos between its pattern stages are a state machine over one probe.
+__device__ __noinline__ int4 umhs_evaluate(const UmhsArgs& u, int k, int px, int py, int pd, int lane, int* bad,
+                                           unsigned char* win)
 {
     const FullArgs& a = u.f;
     Search s;
@@ -170,6 +242,7 @@ __device__ __noinline__ int4 umhs_evaluate(const UmhsArgs& u, int k, int px, int
     const int p0 = sd_part(a, s.n + px0, s.m + py0, cur, lane);
     const int p1 = use_zero ? sd_part(a, s.n, s.m, cur, lane) : 0;
     const int p2 = use_prev ? sd_part(a, s.n + pvx, s.m + pvy, cur, lane) : 0;
+    window_fill(a, s.n, s.m, win, lane);  // the patterns read their candidates from here
     const int pred_vd = warp_sum(p0);
     s.min_d = pred_vd;
     s.mx = px0;
@@ -196,95 +269,75 @@ __device__ __noinline__ int4 umhs_evaluate(const UmhsArgs& u, int k, int px, int
     }
     int outcome = kNoPdTest;
     const int d0 = s.min_d;
-    // 0: diamond, 1: extended hexagon, 2: the full descent
-    int entry;
+    int st;  // first early exit (:573-579)
     if (d0 < 1000) {
-        entry = 0;
+        st = P_DIAMOND;
     } else if (d0 < 4000) {
-        entry = 1;
+        st = P_EXTHEX;
     } else {
         bool taken = false;
         if (d0 == pred_vd) {
             taken = d0 < pd * 12 / 10 && d0 > pd * 8 / 10;
             outcome = (d0 << 1) | (taken ? 1 : 0);
         }
-        entry = taken ? 1 : 2;
+        st = taken ? P_EXTHEX : P_CROSS;
     }
-    if (entry == 2) {
-        // unsymmetrical cross, 8 scales x 4 points, vertical reach below half the range (:581-616)
-        s.rmx = s.rmy = 0;
-        int prior = s.min_d;
-        probe<32>(a, s, cur, lane, [&](int c, int& j, int& i) {
-            const int w = 2 * (c >> 2) + 1;
-            j = w * kCross[c & 3][0];
-            i = w * kCross[c & 3][1];
-            return i < mrng / 2 && i > -mrng / 2;
-        });
-        s.mx += s.rmx;
-        s.my += s.rmy;
-        if (s.min_d < 1000) {
-            entry = 0;
-        } else if (s.min_d < 2000 ||
-                   (s.min_d < prior * 9 / 10 && (s.rmx || s.rmy) && abs(s.rmx) <= 3 && abs(s.rmy) <= 3)) {
-            entry = 1;
-        } else {
-            // 5x5 without the points the cross tested (:625-656)
-            const int crx = s.rmx, cry = s.rmy;
+    // each step lowers the integer cost or moves to the next stage: a bound far above any search
+    constexpr int kMaxSteps = 1 << 14;
+    int w = 1, prior = 0, crx = 0, cry = 0, steps = 0;
+    while (st != P_DONE && steps++ < kMaxSteps) {
+        if (st == P_CROSS) {  // unsymmetrical cross (:581-616)
             s.rmx = s.rmy = 0;
-            probe<24>(a, s, cur, lane, [&](int c, int& j, int& i) {
-                j = kSq5[c][0];
-                i = kSq5[c][1];
-                return !((crx || cry) && ((cry == 0 && (j == 2 || j == -2)) || (crx == 0 && (i == 2 || i == -2))));
-            });
-            if (s.min_d < 1000) {
-                entry = 0;  // the centre stays at the cross winner (:658-662)
-            } else {
-                // three hexagon scales around the cross winner, the 5x5 offset still a candidate (:664-702)
-                prior = s.min_d;
-                for (int w = 1; w < 4; w++) {
-                    probe<16>(a, s, cur, lane, [&](int c, int& j, int& i) {
-                        j = w * kHex[c][0];
-                        i = w * kHex[c][1];
-                        return true;
-                    });
-                    if ((s.rmx || s.rmy) && (s.min_d < 2000 || s.min_d < prior / 5)) break;
-                }
+            prior = s.min_d;
+        } else if (st == P_SQ5) {  // 5x5 around the cross winner (:625-656)
+            crx = s.rmx;
+            cry = s.rmy;
+            s.rmx = s.rmy = 0;
+        } else if (st == P_HEX) {  // hexagon scales 1..3 around the cross winner, the 5x5 offset kept (:664-702)
+            if (w == 1) prior = s.min_d;
+        } else {  // extended hexagon (:705-736) and diamond (:739-769) until the centre wins
+            s.rmx = s.rmy = 0;
+        }
+        probe(s, st, w, crx, cry, mrng, win, lane);
+        switch (st) {
+        case P_CROSS:
+            s.mx += s.rmx;
+            s.my += s.rmy;
+            if (s.min_d < 1000) st = P_DIAMOND;
+            else if (s.min_d < 2000 ||
+                     (s.min_d < prior * 9 / 10 && (s.rmx || s.rmy) && abs(s.rmx) <= 3 && abs(s.rmy) <= 3))
+                st = P_EXTHEX;
+            else st = P_SQ5;
+            break;
+        case P_SQ5:  // on this exit the centre stays at the cross winner (:658-662)
+            if (s.min_d < 1000) st = P_DIAMOND;
+            else {
+                st = P_HEX;
+                w = 1;
+            }
+            break;
+        case P_HEX:
+            if (((s.rmx || s.rmy) && (s.min_d < 2000 || s.min_d < prior / 5)) || w == 3) {
                 s.mx += s.rmx;
                 s.my += s.rmy;
-                entry = 1;
+                st = P_EXTHEX;
+            } else {
+                w++;
             }
+            break;
+        case P_EXTHEX:
+            s.mx += s.rmx;
+            s.my += s.rmy;
+            if (!(s.rmx || s.rmy)) st = P_DIAMOND;
+            break;
+        default:
+            s.mx += s.rmx;
+            s.my += s.rmy;
+            if (!(s.rmx || s.rmy)) st = P_DONE;
+            break;
         }
     }
-    // each step of the descents lowers the integer cost: at most a few hundred steps
-    constexpr int kMaxSteps = 1 << 14;
-    if (entry == 1) {  // extended hexagon until the centre wins (:705-736)
-        int it = 0;
-        do {
-            s.rmx = s.rmy = 0;
-            probe<6>(a, s, cur, lane, [&](int c, int& j, int& i) {
-                j = kExtHex[c][0];
-                i = kExtHex[c][1];
-                return true;
-            });
-            s.mx += s.rmx;
-            s.my += s.rmy;
-        } while ((s.rmx || s.rmy) && ++it < kMaxSteps);
-        if (it >= kMaxSteps) *bad = 1;
-    }
-    {  // diamond until the centre wins (:739-769)
-        int it = 0;
-        do {
-            s.rmx = s.rmy = 0;
-            probe<4>(a, s, cur, lane, [&](int c, int& j, int& i) {
-                j = kCross[c][0];
-                i = kCross[c][1];
-                return true;
-            });
-            s.mx += s.rmx;
-            s.my += s.rmy;
-        } while ((s.rmx || s.rmy) && ++it < kMaxSteps);
-        if (it >= kMaxSteps) *bad = 1;
-    }
+    if (st != P_DONE) *bad = 1;
     // half / quarter passes of the full-search window (:790-867)
     int min_d = s.min_d;
     int mvx = 4 * s.mx, mvy = 4 * s.my;
@@ -357,10 +410,13 @@ __device__ __forceinline__ bool record_lookup(int4 e, int px, int py, int pd, in
 __device__ __forceinline__ int4 empty_record() { return make_int4(0, 0, 0, -1); }
 
 // One relaxation sweep: every macroblock (a warp each, grid-stride) at the
-// prediction of its neighbours' current states (all zero in sweep 0).
-// Skipped once an earlier sweep changed nothing.
-__global__ void __launch_bounds__(256) k_umhs_sweep(UmhsArgs u, int sweep)
+// prediction of its neighbours' current states.  Sweep 0 starts from the
+// handle's previous estimate's final states (zero after creation): the fixed
+// point does not depend on where the relaxation starts, and consecutive frames
+// start close to it.  Skipped once an earlier sweep changed nothing.
+__global__ void __launch_bounds__(128) k_umhs_sweep(UmhsArgs u, int sweep)
 {
+    __shared__ __align__(16) unsigned char wins[4][kWinSlot];
     const FullArgs& a = u.f;
     if (sweep > 0 && __ldcg(a.changed + sweep - 1) == 0) {
         return;  // the fixed point: this sweep's counter stays 0, so the next sweeps return too
@@ -372,7 +428,7 @@ __global__ void __launch_bounds__(256) k_umhs_sweep(UmhsArgs u, int sweep)
     for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < a.nmb; k += (gridDim.x * blockDim.x) >> 5) {
         const int av = neighbour_mask(slice, k, a.cols, rows);
         unsigned long long v = 0;
-        if (sweep > 0) {
+        {
             int nb = -1;
             if (lane == 0 && (av & AV_A)) nb = k - 1;
             if (lane == 1 && (av & AV_B)) nb = k - a.cols;
@@ -387,7 +443,7 @@ __global__ void __launch_bounds__(256) k_umhs_sweep(UmhsArgs u, int sweep)
         int mv, d;
         if (!record_lookup(e, px, py, pd, &mv, &d)) {
             int bad = 0;
-            const int4 r = umhs_evaluate(u, k, px, py, pd, lane, &bad);
+            const int4 r = umhs_evaluate(u, k, px, py, pd, lane, &bad, wins[threadIdx.x >> 5]);
             if (bad && lane == 0) atomicOr(&a.ctrl->status, ST_OUT_OF_BOUNDS);
             mv = r.z;
             d = r.w;
@@ -419,6 +475,97 @@ __device__ __forceinline__ bool relaxed(const UmhsArgs& u)
     return false;
 }
 
+// Which exact pass decides a frame the relaxation left unsettled: the one-CTA
+// diagonal pass when the last sweep changed few macroblocks (few record
+// misses to come: cheap steps matter), else the dataflow pass over all SMs
+// (many misses: parallel searches matter).
+__device__ __forceinline__ bool diagonal_pass(const UmhsArgs& u)
+{
+    return *((volatile const int*)u.f.changed + u.sweeps - 1) <= u.diag_limit;
+}
+
+// The exact raster result in one CTA: lane l of warp w owns row 32w + l and
+// at step t takes column t - 2r, so a step is an anti-diagonal c + 2r = t,
+// whose predictions read only earlier steps: the row's own previous result
+// (a register) and the row above's last three (a four-slot ring per row in
+// shared memory; the slot the row above writes in step t is none of the
+// three read).  One block barrier per step, no waits.  A record gives the
+// result for the prediction; the lanes that find none are searched by their
+// warp, one after another.
+__global__ void __launch_bounds__(512) k_umhs_diag(UmhsArgs u)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const FullArgs& a = u.f;
+    if (relaxed(u) || !diagonal_pass(u)) return;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int cols = a.cols, rows = a.nmb / cols;
+    unsigned char* win = smem + (size_t)wid * kWinSlot;
+    unsigned long long* ring = reinterpret_cast<unsigned long long*>(smem + (size_t)nw * kWinSlot);
+    const int r = wid * 32 + lane;
+    const bool row_ok = r < rows;
+    const int* slice = a.job->slice;
+    unsigned long long left = 0;
+    int4 nxt[UMHS_RECORDS];
+#pragma unroll
+    for (int e = 0; e < UMHS_RECORDS; e++) nxt[e] = empty_record();
+    if (row_ok && r == 0)
+#pragma unroll
+        for (int e = 0; e < UMHS_RECORDS; e++) nxt[e] = __ldcg(u.rec + e);
+    int misses = 0;
+    const int steps = cols + 2 * (rows - 1);
+    for (int t = 0; t < steps; t++) {
+        const int c = t - 2 * r;
+        const bool act = row_ok && c >= 0 && c < cols;
+        int4 cur[UMHS_RECORDS];
+#pragma unroll
+        for (int e = 0; e < UMHS_RECORDS; e++) cur[e] = nxt[e];
+        if (row_ok && c + 1 >= 0 && c + 1 < cols)  // next step's records, loaded during this one
+#pragma unroll
+            for (int e = 0; e < UMHS_RECORDS; e++) nxt[e] = __ldcg(u.rec + ((size_t)r * cols + c + 1) * UMHS_RECORDS + e);
+        const int k = r * cols + c;
+        int px = 0, py = 0, pd = 0, mv = 0, d = 0;
+        bool hit = false;
+        if (act) {
+            const int av = neighbour_mask(slice, k, cols, rows);
+            const unsigned long long* above = ring + (size_t)(r - 1) * 4;
+            const unsigned long long B = (av & AV_B) ? above[c & 3] : 0;
+            const unsigned long long C =
+                (av & AV_C) ? above[(c + 1) & 3] : ((av & AV_D) ? above[(c - 1) & 3] : 0);
+            median_with_distortion(av, left, B, C, &px, &py, &pd);
+#pragma unroll
+            for (int e = 0; e < UMHS_RECORDS; e++)
+                if (!hit && cur[e].w >= 0 && cur[e].x == pack_mv(px, py) && record_holds(cur[e].y, pd)) {
+                    hit = true;
+                    mv = cur[e].z;
+                    d = cur[e].w;
+                }
+        }
+        unsigned miss = __ballot_sync(0xffffffffu, act && !hit);
+        while (miss) {
+            const int f = __ffs(miss) - 1;
+            miss &= miss - 1;
+            int bad = 0;
+            const int4 rr = umhs_evaluate(u, __shfl_sync(0xffffffffu, k, f), __shfl_sync(0xffffffffu, px, f),
+                                          __shfl_sync(0xffffffffu, py, f), __shfl_sync(0xffffffffu, pd, f), lane,
+                                          &bad, win);
+            if (bad && lane == 0) atomicOr(&a.ctrl->status, ST_OUT_OF_BOUNDS);
+            if (lane == f) {
+                mv = rr.z;
+                d = rr.w;
+            }
+            misses++;
+        }
+        if (act) {
+            const unsigned long long st = state_word(mv, d);
+            left = st;
+            ring[(size_t)r * 4 + (c & 3)] = st;
+            __stcg(u.wave + k, st);
+        }
+        __syncthreads();
+    }
+    if (lane == 0 && misses) atomicAdd(&a.ctrl->wave_miss, misses);
+}
+
 // The exact raster result by dataflow over the anti-diagonal order.  A warp
 // takes the next ticket, prefetches the macroblock's records, waits for its
 // neighbours' published states (lanes 0..2, bounded, giving up at once when
@@ -426,8 +573,9 @@ __device__ __forceinline__ bool relaxed(const UmhsArgs& u)
 // searches, and publishes its state with release semantics.
 __global__ void __launch_bounds__(128) k_umhs_wave(UmhsArgs u)
 {
+    __shared__ __align__(16) unsigned char wins[4][kWinSlot];
     const FullArgs& a = u.f;
-    if (relaxed(u)) return;
+    if (relaxed(u) || diagonal_pass(u)) return;
     const int lane = threadIdx.x & 31;
     const int rows = a.nmb / a.cols;
     const int* slice = a.job->slice;
@@ -448,12 +596,13 @@ __global__ void __launch_bounds__(128) k_umhs_wave(UmhsArgs u)
         unsigned long long v = 0;
         if (nb >= 0) {
             long long it = 0;
-            while ((v = ld_acquire_u64(u.wave + nb)) == kPending) {
+            while ((v = ld_relaxed_u64(u.wave + nb)) == kPending) {
                 if ((++it & 63) == 0 && ((*status & ST_TIMEOUT) || it > a.spin_limit)) {
                     atomicOr(&a.ctrl->status, ST_TIMEOUT);
                     v = 0;
                     break;
                 }
+                __nanosleep(32);
             }
         }
         int px, py, pd;
@@ -462,20 +611,21 @@ __global__ void __launch_bounds__(128) k_umhs_wave(UmhsArgs u)
         int mv, d;
         if (!record_lookup(e, px, py, pd, &mv, &d)) {
             int bad = 0;
-            const int4 r = umhs_evaluate(u, k, px, py, pd, lane, &bad);
+            const int4 r = umhs_evaluate(u, k, px, py, pd, lane, &bad, wins[threadIdx.x >> 5]);
             if (bad && lane == 0) atomicOr(&a.ctrl->status, ST_OUT_OF_BOUNDS);
             mv = r.z;
             d = r.w;
             misses++;
         }
-        if (lane == 0) st_release_u64(u.wave + k, state_word(mv, d));
+        if (lane == 0) st_relaxed_u64(u.wave + k, state_word(mv, d));
         __syncwarp();
     }
     if (lane == 0 && misses) atomicAdd(&a.ctrl->wave_miss, misses);
 }
 
-// Outputs: the relaxed state or the dataflow pass's, vectors, distortions and
-// the included sums (UMHS.cpp:910-935).
+// Outputs: the relaxed state or the exact pass's, vectors, distortions and
+// the included sums (UMHS.cpp:910-935); the final states stay as the next
+// estimate's starting point.
 __global__ void __launch_bounds__(256) k_umhs_outputs(UmhsArgs u)
 {
     const FullArgs& a = u.f;
@@ -485,6 +635,7 @@ __global__ void __launch_bounds__(256) k_umhs_outputs(UmhsArgs u)
     int cnt = 0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.nmb; k += gridDim.x * blockDim.x) {
         const unsigned long long s = rel ? __ldcg(u.state + k) : __ldcg(u.wave + k);
+        if (!rel) __stcg(u.state + k, s);
         const int d = state_d(s);
         a.job->out_mv[k] = state_mv(s);
         if (a.job->out_dist) a.job->out_dist[k] = d;
@@ -523,16 +674,29 @@ __global__ void k_umhs_average(UmhsArgs u)
 
 }  // namespace
 
+size_t umhs_diag_smem(int rows) { return (size_t)((rows + 31) / 32) * kWinSlot + (size_t)rows * 4 * 8; }
+
+int umhs_prepare()
+{
+    // the largest frame: 8192 / 16 = 512 macroblock rows, 16 warps
+    VPP_CUDA(cudaFuncSetAttribute(k_umhs_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)umhs_diag_smem(512)));
+    return VPPGPU_OK;
+}
+
 int umhs_launch(vppgpu_ctx* ctx, const UmhsArgs& u, int wave_grid)
 {
     int rc = full_planes_launch(ctx, u.f);
     if (rc) return rc;
-    const int sweep_grid = (u.f.nmb + 7) / 8;
+    const int sweep_grid = (u.f.nmb + 3) / 4;
     for (int s = 0; s < u.sweeps; s++) {
-        k_umhs_sweep<<<sweep_grid, 256, 0, ctx->stream>>>(u, s);
+        k_umhs_sweep<<<sweep_grid, 128, 0, ctx->stream>>>(u, s);
         VPP_CHECK_LAUNCH(ctx);
     }
     VPP_CUDA(cudaMemsetAsync(u.wave, 0xff, sizeof(unsigned long long) * (size_t)u.f.nmb, ctx->stream));
+    const int rows = u.f.nmb / u.f.cols, nw = (rows + 31) / 32;
+    k_umhs_diag<<<1, nw * 32, umhs_diag_smem(rows), ctx->stream>>>(u);
+    VPP_CHECK_LAUNCH(ctx);
     k_umhs_wave<<<wave_grid, 128, 0, ctx->stream>>>(u);
     VPP_CHECK_LAUNCH(ctx);
     k_umhs_outputs<<<(u.f.nmb + 255) / 256, 256, 0, ctx->stream>>>(u);

@@ -154,7 +154,7 @@ int vppgpu_me_last_status(vppgpu_me* me);
 int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps);
 
 /* Estimators with a predictor, no vpp counterpart: at most this many
- * relaxation sweeps (0..14; defaults 14 Full and Multires, 4 Ver2; fewer when
+ * relaxation sweeps (0..14, UMHS 0..24; defaults 14 Full and Multires, 4 Ver2, 20 UMHS; fewer when
  * the changes stop falling fast) run before the exact wavefront decides the
  * macroblocks whose predictions have not settled.  Results do not depend on it. */
 int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps);

@@ -114,6 +114,16 @@ def test_1080p_sequence(vpp, ctx, orc):
         np.testing.assert_array_equal(mv, mv_o, err_msg=f"pair {t}")
         np.testing.assert_array_equal(me.last_mb_distortion, dist_o, err_msg=f"pair {t}")
         prev = (mv.copy(), None)
+    # the relaxation starts from the previous estimate's states: unrelated
+    # content before must not change a result
+    noisy = umhs_frames(5, w, h, "noisy")
+    cur[...] = noisy[1]
+    ref[...] = noisy[0]
+    me._prev = None
+    mv, _ = me.Estimate()
+    mv_o, dist_o, _ = orc.me_umhs(noisy[1], noisy[0], mr)
+    np.testing.assert_array_equal(mv, mv_o)
+    np.testing.assert_array_equal(me.last_mb_distortion, dist_o)
 
 
 def test_predictor_side_effect_carries_distortion(vpp, ctx):
