@@ -61,6 +61,7 @@ class Oracle:
         L.vo_me_multires_cross_v2_lambda.argtypes = [_P, _P, _I, _I, _I, _I, C.c_double, _P, _P, _P, _P,
                                                      C.POINTER(_L)]
         L.vo_me_umhs.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, C.POINTER(_L)]
+        L.vo_me_fhs.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), C.POINTER(_I)]
         L.vo_mc_compensate.argtypes = [_P, _I, _I, _I, _P]
         L.vo_add_clip255.argtypes = [_P, _P, C.c_longlong]
         L.vo_sub.argtypes = [_P, _P, C.c_longlong]
@@ -171,6 +172,25 @@ class Oracle:
         if rc:
             raise ValueError(f"vo_me_umhs rc={rc}")
         return mv, dist, avg.value
+
+    def me_fhs(self, src, ref, motion_range, mode=0, dist_incl=None, slice_map=None, with_stale=False):
+        """MotionEstimatorH264ImplFHS: vectors, the distortion stored with each, the
+        average (and the number of stale sub-pel cache reads replaced)."""
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = self.lib.vo_num_mbs(w, h)
+        mv = np.zeros((nmb, 2), np.int16)
+        dist = np.zeros(nmb, np.int32)
+        avg = _L(0)
+        stale = _I(0)
+        incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
+        sl = None if slice_map is None else np.ascontiguousarray(slice_map, dtype=np.int32)
+        rc = self.lib.vo_me_fhs(_ptr(src), _ptr(ref), w, h, motion_range, mode, _ptr(incl), _ptr(sl), _ptr(mv),
+                                _ptr(dist), C.byref(avg), C.byref(stale))
+        if rc:
+            raise ValueError(f"vo_me_fhs rc={rc}")
+        return (mv, dist, avg.value, stale.value) if with_stale else (mv, dist, avg.value)
 
     def _me_pred(self, fn, src, ref, motion_range, mode, dist_incl, slice_map, with_ties):
         h, w = src.shape
@@ -333,6 +353,7 @@ class Reference:
         L.ref_me_estimate.argtypes = [_I, _P, _P, _I, _I, _I, _I, _P, _P, _I, _P, C.POINTER(_L)]
         L.ref_me_full_sad.argtypes = [_P, _P, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.ref_me_umhs.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P, C.POINTER(_L)]
+        L.ref_me_fhs.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.ref_fwd_transform.argtypes = [_I, _P, _I, _I, _I, _I]
         L.ref_inv_transform.argtypes = [_I, _P, _I, _I, _I, _P]
         L.ref_quantise_value.argtypes = [C.c_short, _I, _I, _I]
@@ -398,6 +419,22 @@ class Reference:
                                   _ptr(mv), _ptr(dist), C.byref(avg))
         if rc:
             raise ValueError(f"ref_me_umhs rc={rc}")
+        return mv, dist, avg.value
+
+    def me_fhs(self, src, ref, motion_range, mode=0, dist_incl=None):
+        """MotionEstimatorH264ImplFHS: vectors, the distortion stored with each, the average."""
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        nmb = (w // 16) * (h // 16)
+        mv = np.zeros((nmb, 2), np.int16)
+        dist = np.zeros(nmb, np.int32)
+        avg = _L(0)
+        incl = None if dist_incl is None else np.ascontiguousarray(dist_incl, dtype=np.uint8)
+        rc = self.lib.ref_me_fhs(_ptr(src), _ptr(ref), w, h, motion_range, mode, _ptr(incl), _ptr(mv), _ptr(dist),
+                                 C.byref(avg))
+        if rc:
+            raise ValueError(f"ref_me_fhs rc={rc}")
         return mv, dist, avg.value
 
     def mc_compensate(self, y, u, v, mv, range_):

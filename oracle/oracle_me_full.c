@@ -853,3 +853,293 @@ int vo_me_umhs(const short* src, const short* ref, int w, int h, int motion_rang
     free(e);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* MotionEstimatorH264ImplFHS                                                */
+/* ------------------------------------------------------------------------ */
+/* Points 64..79 of the path MotionEstimatorH264ImplFHS::Td16x16OptimalPathLessThan
+ * reads (MotionEstimatorH264ImplFHS.cpp:1685-1785, {x, y}); points 0..63 are
+ * CROSS_PATH. */
+static const signed char FHS_PATH_TAIL[16][2] = {{5, 2},  {5, 12}, {1, 4},  {11, 5}, {13, 8},  {9, 7},
+                                                 {13, 3}, {5, 8},  {10, 11}, {6, 15}, {13, 10}, {8, 4},
+                                                 {3, 10}, {13, 1}, {1, 8},  {14, 0}};
+static void fhs_path_point(int p, int* x, int* y)
+{
+    if (p < 64) {
+        *x = CROSS_PATH[p][0];
+        *y = CROSS_PATH[p][1];
+    } else {
+        *x = FHS_PATH_TAIL[p - 64][0];
+        *y = FHS_PATH_TAIL[p - 64][1];
+    }
+}
+
+/* Td16x16OptimalPathLessThan (MotionEstimatorH264ImplFHS.cpp:1685-1790): squared
+ * differences along the first 80 path points; after 32, 40, 48, 56, 64 and 72 of
+ * them the whole block's distortion is extrapolated as D * 256 / N and returned
+ * once it exceeds min; after 80 the extrapolation is returned. */
+static int fhs_path_lt(const short* a, int as, const short* b, int bs, int min)
+{
+    int d = 0;
+    for (int p = 0; p < 80; p++) {
+        int x, y;
+        fhs_path_point(p, &x, &y);
+        const int e = a[(size_t)y * as + x] - b[(size_t)y * bs + x];
+        d += e * e;
+        const int n = p + 1;
+        if (n >= 32 && n < 80 && (n % 8) == 0) {
+            const int v = d * 256 / n;
+            if (v > min) return v;
+        }
+    }
+    return d * 256 / 80;
+}
+
+/* MEH264IFHS_COST (MotionEstimatorH264ImplFHS.cpp:222): (D + 269 * (int)sqrt(s)) >> 8,
+ * all integer but the square root, truncated. */
+static int fhs_cost(int d, int x, int y, int xr, int yr)
+{
+    const int s = (x - xr) * (x - xr) + (y - yr) * (y - yr);
+    return (d + 269 * (int)sqrt((double)s)) >> 8;
+}
+
+/* One macroblock's FHS state: the running best and the pattern centre. */
+typedef struct {
+    const short* in;
+    const short* e;
+    int es, w, h, n, m;
+    int xl, xr, yu, yd, px0, py0;
+    int mx, my, rmx, rmy, min_d, min_cost;
+} fhs_search;
+
+static const short* fhs_block(const fhs_search* s, int x, int y)
+{
+    const int ox = vo_clamp_origin(s->n + x + EXT_BORDER, s->es, MB);
+    const int oy = vo_clamp_origin(s->m + y + EXT_BORDER, s->h + 2 * EXT_BORDER, MB);
+    return s->e + (size_t)oy * s->es + ox;
+}
+
+/* A pattern candidate (UMHS-style loop body of FHS.cpp:690-738, :758-780, :792-818):
+ * in range, its path distortion not above the running minimum, a strictly lower cost. */
+static void fhs_probe(fhs_search* s, int j, int i)
+{
+    if (i + s->my < s->yu || i + s->my > s->yd || j + s->mx < s->xl || j + s->mx > s->xr) return;
+    const int d = fhs_path_lt(s->in, s->w, fhs_block(s, s->mx + j, s->my + i), s->es, s->min_d);
+    if (d > s->min_d) return;
+    const int cost = fhs_cost(d, s->mx + j, s->my + i, s->px0, s->py0);
+    if (cost < s->min_cost) {
+        s->min_d = d;
+        s->min_cost = cost;
+        s->rmx = j;
+        s->rmy = i;
+    }
+}
+
+/* SSD of the block at quarter-pel offset (qx, qy) from the full-pel origin
+ * (ox, oy) of the extended reference: the H.264 samples the reference's
+ * half-pel cache and QuarterRead hold there. */
+static int fhs_sub_sd(const fhs_search* s, int ox, int oy, int qx, int qy)
+{
+    short blk[256];
+    vo_qread16_ext(s->e, s->es, ox, oy, qx, qy, blk);
+    return vo_tsd16(s->in, s->w, blk, 16);
+}
+
+/* HalfPelEstimate (MotionEstimatorH264ImplFHS.cpp:1109-1200): the two "h"
+ * offsets, then the two "b", then the four "j", strict improvement, leaving
+ * after a stage whose minimum is below 1000.  Returns the minimum and the
+ * half-pel offset; *h_exit says it left after the "h" stage. */
+static int fhs_half(const fhs_search* s, int ox, int oy, int min, int* hx, int* hy, int* h_exit)
+{
+    static const int HX[8] = {0, 0, -1, 1, -1, 1, -1, 1}, HY[8] = {-1, 1, 0, 0, -1, -1, 1, 1};
+    int lcl = min;
+    *hx = *hy = 0;
+    *h_exit = 0;
+    for (int k = 0; k < 8; k++) {
+        const int d = fhs_sub_sd(s, ox, oy, 2 * HX[k], 2 * HY[k]);
+        if (d < lcl) {
+            lcl = d;
+            *hx = HX[k];
+            *hy = HY[k];
+        }
+        if ((k == 1 || k == 3) && lcl < 1000) {
+            *h_exit = k == 1;
+            break;
+        }
+    }
+    return lcl;
+}
+
+/* QuarterPelEstimate (MotionEstimatorH264ImplFHS.cpp:1213-1480): the half-pel
+ * stage, then the eight quarter offsets around its winner, strict improvement,
+ * leaving at a minimum below 1000.  The returned offset is the last quarter-pel
+ * improvement only: a half-pel winner without one returns (0, 0) with the
+ * half-pel distortion, as the reference does.
+ *
+ * When the half-pel stage leaves after its "h" stage without an improvement
+ * (the full-pel minimum was already below 1000), the reference's quarter pass
+ * reads "b" and "j" samples its cache holds from earlier macroblocks.  That
+ * history is not reproduced: the samples of this macroblock are used, and
+ * *stale counts the occurrence so that pinned cases can assert there is none. */
+static int fhs_quarter(const fhs_search* s, int ox, int oy, int min, int* qx, int* qy, int* stale)
+{
+    int hx, hy, h_exit;
+    const int half = fhs_half(s, ox, oy, min, &hx, &hy, &h_exit);
+    int lcl = min;
+    *qx = *qy = 0;
+    if (half < min) {
+        lcl = half;
+        if (half < 1000) return lcl;
+    }
+    if (h_exit) (*stale)++;
+    for (int k = 0; k < 8; k++) {
+        const int qox = 2 * hx + SUB_X[k], qoy = 2 * hy + SUB_Y[k];
+        const int d = fhs_sub_sd(s, ox, oy, qox, qoy);
+        if (d < lcl) {
+            lcl = d;
+            *qx = qox;
+            *qy = qoy;
+            if (d < 1000) break;
+        }
+    }
+    return lcl;
+}
+
+/* MotionEstimatorH264ImplFHS::Estimate (MotionEstimatorH264ImplFHS.cpp:497-900).
+ * Per macroblock in raster order: the median prediction with its distortion,
+ * truncated to one macroblock outside the picture (its quarter-pel part then
+ * dropped); the prediction's full SSD at quarter pel and the zero vector's path
+ * distortion as starting points, each ending the search below 1000; the
+ * four-scale hexagon, one extended-hexagon and one diamond pass on path
+ * distortions with integer costs; the half / quarter stages; the prediction
+ * check, whose costs compare quarter-pel vectors with the full-pel prediction
+ * as the reference does.  The previous-frame starting point is disabled in the
+ * reference (:627-673). */
+int vo_me_fhs(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+              const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist, long* avg_dist,
+              int* stale_out)
+{
+    if (!src || !ref || !mv_out || w < MB || h < MB || (w % MB) != 0 || motion_range < 4) return -1;
+    int cols = w / MB, rows = h / MB, nmb = cols * rows;
+    int es = w + 2 * EXT_BORDER;
+    short* e = vo_ext_alloc(ref, w, h, EXT_BORDER);
+    int* dist = (int*)calloc((size_t)nmb, sizeof(int));
+    vo_pred_state ps;
+    if (!e || !dist || vo_pred_init(&ps, cols, rows, slice) != 0) {
+        free(e);
+        free(dist);
+        vo_pred_free(&ps);
+        return -2;
+    }
+    long total = 0;
+    int included = 0, stale = 0;
+    for (int k = 0; k < nmb; k++) {
+        fhs_search s;
+        s.n = (k % cols) * MB;
+        s.m = (k / cols) * MB;
+        s.in = src + (size_t)s.m * w + s.n;
+        s.e = e;
+        s.es = es;
+        s.w = w;
+        s.h = h;
+        int px, py, pred_d;
+        umhs_pred_get(&ps, dist, k, &px, &py, &pred_d);
+        int pxq = px % 4, pyq = py % 4;
+        int px0 = px / 4, py0 = py / 4;
+        const int opx0 = px0, opy0 = py0;
+        if (px0 + s.n > w) px0 = MB;
+        if (px0 + s.n < -MB) px0 = -MB;
+        if (py0 + s.m > h) py0 = MB;
+        if (py0 + s.m < -MB) py0 = -MB;
+        if (opx0 != px0 || opy0 != py0) pxq = pyq = 0;  /* (:549-550) */
+        const int rpx = 4 * px0 + pxq, rpy = 4 * py0 + pyq;
+        s.px0 = px0;
+        s.py0 = py0;
+        full_range(s.n, s.m, w, h, motion_range, motion_range / 4, &s.xl, &s.xr, &s.yu, &s.yd);
+        int mvx, mvy;
+
+        /* the prediction at quarter pel (:555-597) */
+        const int pox = vo_clamp_origin(px0 + s.n + EXT_BORDER, es, MB);
+        const int poy = vo_clamp_origin(py0 + s.m + EXT_BORDER, h + 2 * EXT_BORDER, MB);
+        const int pred_vd = fhs_sub_sd(&s, pox, poy, pxq, pyq);
+        s.min_d = pred_vd;
+        s.mx = px0;
+        s.my = py0;
+        s.min_cost = pred_vd / 256;
+        if (pred_vd < 1000) {
+            mvx = rpx;
+            mvy = rpy;
+            goto done;
+        }
+        /* zero (:599-625) */
+        if (rpx || rpy) {
+            const int zd = fhs_path_lt(s.in, w, fhs_block(&s, 0, 0), es, s.min_d);
+            if (zd < s.min_d) {
+                const int zc = fhs_cost(zd, 0, 0, px0, py0);
+                if (zc < s.min_cost) { s.min_d = zd; s.min_cost = zc; s.mx = 0; s.my = 0; }
+                if (zd < 1000) {
+                    mvx = 0;
+                    mvy = 0;
+                    goto done;
+                }
+            }
+        }
+        if (s.min_d < 1000) goto diamond;
+        if (s.min_d < 4000 || (s.min_d == pred_vd && s.min_d < pred_d * 12 / 10 && s.min_d > pred_d * 8 / 10))
+            goto hexagon;
+        /* four hexagon scales (:684-748) */
+        s.rmx = s.rmy = 0;
+        for (int wgt = 1; wgt <= 4; wgt++)
+            for (int x = 0; x < 16; x++) fhs_probe(&s, wgt * UMHS_HEX[x][0], wgt * UMHS_HEX[x][1]);  /* MEH264IFHS_HexPos, the UMHS table */
+        s.mx += s.rmx;
+        s.my += s.rmy;
+    hexagon: /* one extended-hexagon pass (:751-784) */
+        s.rmx = s.rmy = 0;
+        for (int x = 0; x < 6; x++) fhs_probe(&s, UMHS_EXTHEX[x][0], UMHS_EXTHEX[x][1]);
+        s.mx += s.rmx;
+        s.my += s.rmy;
+    diamond: /* one diamond pass (:786-820) */
+        s.rmx = s.rmy = 0;
+        for (int x = 0; x < 4; x++) fhs_probe(&s, UMHS_CROSS[x][0], UMHS_CROSS[x][1]);
+        s.mx += s.rmx;
+        s.my += s.rmy;
+        /* half / quarter stages (:822-856) */
+        mvx = 4 * s.mx;
+        mvy = 4 * s.my;
+        {
+            const int ox = vo_clamp_origin(s.n + s.mx + EXT_BORDER, es, MB);
+            const int oy = vo_clamp_origin(s.m + s.my + EXT_BORDER, h + 2 * EXT_BORDER, MB);
+            if (mode == 0) {
+                int qx, qy;
+                const int nm = fhs_quarter(&s, ox, oy, s.min_d, &qx, &qy, &stale);
+                if (nm < s.min_d) { s.min_d = nm; mvx += qx; mvy += qy; }
+            } else if (mode == 1) {
+                int hx, hy, h_exit;
+                const int nm = fhs_half(&s, ox, oy, s.min_d, &hx, &hy, &h_exit);
+                if (nm < s.min_d) { s.min_d = nm; mvx += 2 * hx; mvy += 2 * hy; }
+            }
+        }
+        /* the prediction check (:858-867) */
+        if (fhs_cost(pred_vd, rpx, rpy, px0, py0) <= fhs_cost(s.min_d, mvx, mvy, px0, py0)) {
+            s.min_d = pred_vd;
+            mvx = rpx;
+            mvy = rpy;
+        }
+    done: /* (:869-890) */
+        if (dist_incl && dist_incl[k]) {
+            included++;
+            total += s.min_d;
+        }
+        if (mb_dist) mb_dist[k] = s.min_d;
+        mv_out[2 * k] = (short)mvx;
+        mv_out[2 * k + 1] = (short)mvy;
+        vo_pred_set(&ps, k, mvx, mvy);
+        dist[k] = s.min_d;
+    }
+    if (avg_dist) *avg_dist = included ? total / included : 0;
+    if (stale_out) *stale_out = stale;
+    vo_pred_free(&ps);
+    free(dist);
+    free(e);
+    return 0;
+}

@@ -20,6 +20,7 @@
 #include "MotionEstimatorH264ImplMultiresCrossVer2.h"
 #include "MotionEstimatorH264ImplCross.h"
 #include "MotionEstimatorH264ImplUMHS.h"
+#include "MotionEstimatorH264ImplFHS.h"
 #include "MotionEstimatorH263ImplMultiresCross.h"
 #include "VectorStructList.h"
 #include "MotionCompensatorH264ImplStd.h"
@@ -248,6 +249,34 @@ int ref_me_umhs(const short* src, const short* ref, int w, int h, int motion_ran
     delete me;
     delete[] flags;
     delete[] prev;
+    return 0;
+}
+
+/* MotionEstimatorH264ImplFHS through its seven-argument constructor: vectors,
+ * the distortion handed to the predictor with each, the average.  Its
+ * quarter-pel cache is allocated zero-filled (glibc M_PERTURB), so reads it
+ * makes before any macroblock filled a sample are reproducible. */
+int ref_me_fhs(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+               const unsigned char* incl, short* mv_out, int* dist_out, long* avg_out)
+{
+    int nmb = (w / 16) * (h / 16);
+    MbGrid grid(w, h);
+    H264MotionVectorPredictorImpl1 pred(grid.flat);
+    bool* flags = make_flags(incl, nmb);
+    mallopt(M_PERTURB, 0xff);
+    MotionEstimatorH264ImplFHS* me = new MotionEstimatorH264ImplFHS(src, ref, w, h, motion_range, &pred, flags);
+    int created = me->Create();
+    mallopt(M_PERTURB, 0);
+    if (!created) { delete me; delete[] flags; return -2; }
+    me->SetMode(mode);
+    long avg = 0;
+    void* res = me->Estimate(&avg);
+    copy_vectors((VectorStructList*)res, nmb, mv_out);
+    if (dist_out)
+        for (int i = 0; i < nmb; i++) dist_out[i] = grid.flat[i]._distortion[0];
+    if (avg_out) *avg_out = avg;
+    delete me;
+    delete[] flags;
     return 0;
 }
 

@@ -68,6 +68,17 @@ int vo_me_umhs(const short* src, const short* ref, int w, int h, int motion_rang
                const unsigned char* dist_incl, const int* slice, const short* prev_mv,
                const unsigned char* prev_intra, short* mv_out, int* mb_dist, long* avg_dist);
 
+/* MotionEstimatorH264ImplFHS::Estimate (src/CodecUtils/MotionEstimatorH264ImplFHS.cpp:497-900):
+ * hexagon search started at the median prediction on 80-point extrapolated path
+ * distortions with integer costs, its own half / quarter stages and the
+ * prediction check.  mode 0 quarter, 1 half, 2 full pel.  stale_out (optional):
+ * how many macroblocks met the reference's stale sub-pel cache reads, which the
+ * oracle replaces by this macroblock's samples (see oracle_me_full.c).
+ * mb_dist receives the distortion the predictor stores with each vector. */
+int vo_me_fhs(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+              const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist, long* avg_dist,
+              int* stale_out);
+
 int vo_me_full(const short* src, const short* ref, int w, int h, int motion_range,
                const unsigned char* dist_incl, const int* slice,
                short* mv_out, int* mb_dist, long* avg_dist);

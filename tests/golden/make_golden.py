@@ -40,6 +40,10 @@ inputs and stores inputs and outputs:
                   vectors and intra flags, vectors, the distortion stored with
                   each and avgDistortion; and pair 0 of the 1080p benchmark
                   sequence (mode 0, zero previous vectors)
+* me_fhs.npz      MotionEstimatorH264ImplFHS: the me_umhs cases (frames stored
+                  in me_umhs.npz) at modes 0/1/2 with pDistortionIncluded,
+                  vectors, the distortion stored with each and avgDistortion,
+                  and pair 0 of the 1080p benchmark sequence (mode 0)
 * me_1080p.npz    the headline size: Full, MultiresCross / Ver2 / Multires
                   (modes 0, 1, 2), Cross and the integer-pel SAD stage on three
                   frame pairs of the 1920x1080 benchmark sequence at
@@ -47,7 +51,7 @@ inputs and stores inputs and outputs:
                   SHA-256)
 
 Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
-names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc me_umhs mc
+names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc me_umhs me_fhs mc
 transform dc yuv2rgb colour, default all)
 """
 from __future__ import annotations
@@ -305,6 +309,28 @@ def umhs_fixtures(ref: oracle.Reference) -> dict:
     return out
 
 
+def fhs_fixtures(ref: oracle.Reference) -> dict:
+    out = {}
+    for name, w, h, mr, seed, gen in UMHS_CASES:
+        fr = umhs_frames(seed, w, h, gen)
+        src, rf = fr[1], fr[0]
+        nmb = (w // 16) * (h // 16)
+        incl = (np.arange(nmb) % 4 != 1).astype(np.uint8)
+        for mode in (0, 1, 2):
+            mv, d, avg = ref.me_fhs(src, rf, mr, mode=mode, dist_incl=incl)
+            out[f"{name}_m{mode}_mv"] = mv
+            out[f"{name}_m{mode}_dist"] = d
+            out[f"{name}_m{mode}_avg"] = np.array([avg], np.int64)
+    fr, digest = hd_frames()
+    incl = np.ones((HD_W // 16) * (HD_H // 16), np.uint8)
+    out["hd_frames_sha256"] = digest
+    mv, d, avg = ref.me_fhs(fr[1], fr[0], HD_RANGE, mode=0, dist_incl=incl)
+    out["hd_mv"] = mv
+    out["hd_dist"] = d
+    out["hd_avg"] = np.array([avg], np.int64)
+    return out
+
+
 MC_CASES = [("qcif_r16", 176, 144, 16, 61), ("cif_r32", 352, 288, 32, 62), ("small_r8", 64, 48, 8, 63)]
 
 
@@ -493,7 +519,7 @@ def main() -> None:
               "me_mrc2_lambda": mrc2_lambda_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "me_cross": lambda r: mrc2_fixtures(r, "cross"),
               "me_h263mrc": lambda r: mrc_fixtures(r, "h263_multires_cross", H263_CASES),
-              "me_umhs": umhs_fixtures,
+              "me_umhs": umhs_fixtures, "me_fhs": fhs_fixtures,
               "mc": mc_fixtures,
               "transform": transform_fixtures, "dc": dc_fixtures, "yuv2rgb": yuv2rgb_fixtures,
               "colour": colour_fixtures}

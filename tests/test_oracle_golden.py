@@ -528,3 +528,45 @@ def test_me_umhs_against_compiled_reference(orc, seed, w, h, mr, mode, gen):
     np.testing.assert_array_equal(o[0], r[0])
     np.testing.assert_array_equal(o[1], r[1])
     assert o[2] == r[2]
+
+
+@pytest.mark.parametrize("case", UMHS_CASES)
+def test_me_fhs_matches_reference(orc, golden, case):
+    """MotionEstimatorH264ImplFHS on the me_umhs frames: vectors, stored
+    distortions and the average, modes 0/1/2."""
+    g, gu = golden("me_fhs.npz"), golden("me_umhs.npz")
+    w, h, mr = (int(v) for v in gu[f"{case}_meta"])
+    src, ref = gu[f"{case}_src"].astype(np.int16), gu[f"{case}_ref"].astype(np.int16)
+    for mode in (0, 1, 2):
+        mv, dist, avg = orc.me_fhs(src, ref, mr, mode=mode, dist_incl=gu[f"{case}_incl"])
+        np.testing.assert_array_equal(mv, g[f"{case}_m{mode}_mv"], err_msg=f"mode {mode}")
+        np.testing.assert_array_equal(dist, g[f"{case}_m{mode}_dist"], err_msg=f"mode {mode}")
+        assert avg == int(g[f"{case}_m{mode}_avg"][0])
+
+
+def test_me_fhs_1080p_matches_reference(orc, golden, hd_golden):
+    g = golden("me_fhs.npz")
+    assert g["hd_frames_sha256"].tobytes() == hd_golden["g"]["frames_sha256"].tobytes()
+    fr, mr = hd_golden["frames"], hd_golden["motion_range"]
+    incl = np.ones((hd_golden["w"] // 16) * (hd_golden["h"] // 16), np.uint8)
+    mv, dist, avg, stale = orc.me_fhs(fr[1], fr[0], mr, mode=0, dist_incl=incl, with_stale=True)
+    assert stale == 0
+    np.testing.assert_array_equal(mv, g["hd_mv"])
+    np.testing.assert_array_equal(dist, g["hd_dist"])
+    assert avg == int(g["hd_avg"][0])
+
+
+@ref_available
+@pytest.mark.parametrize("seed,w,h,mr,mode,gen", [(86, 176, 144, 128, 0, "noisy"), (87, 208, 120, 96, 1, "pan"),
+                                                 (88, 96, 64, 256, 0, "shift"), (89, 640, 368, 128, 0, "noisy"),
+                                                 (90, 352, 288, 16, 2, "shift")])
+def test_me_fhs_against_compiled_reference(orc, seed, w, h, mr, mode, gen):
+    from tests.golden.make_golden import umhs_frames
+    ref_lib = oracle_mod.Reference()
+    fr = umhs_frames(seed, w, h, gen)
+    incl = (synth.splitmix64(seed, (w // 16) * (h // 16)) & np.uint64(1)).astype(np.uint8)
+    r = ref_lib.me_fhs(fr[1], fr[0], mr, mode=mode, dist_incl=incl)
+    o = orc.me_fhs(fr[1], fr[0], mr, mode=mode, dist_incl=incl)
+    np.testing.assert_array_equal(o[0], r[0])
+    np.testing.assert_array_equal(o[1], r[1])
+    assert o[2] == r[2]
