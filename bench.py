@@ -411,9 +411,10 @@ MULTIRES = {  # kind -> (class name, oracle method)
     "h263_multires_cross": ("MotionEstimatorH263ImplMultiresCross", "me_h263_multires_cross"),
     "full_sad": ("MotionEstimatorH264ImplFullSad", "me_full_intpel"),
     "umhs": ("MotionEstimatorH264ImplUMHS", "me_umhs"),
+    "fhs": ("MotionEstimatorH264ImplFHS", "me_fhs"),
 }
 MULTIRES_CODE = {"multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4,
-                 "h263_multires_cross": 5, "full_sad": 6, "umhs": 7}  # VPPGPU_ME_*
+                 "h263_multires_cross": 5, "full_sad": 6, "umhs": 7, "fhs": 8}  # VPPGPU_ME_*
 # motion ranges are in quarter pels, the H.263 estimator's in half pels: the same +-32 pels
 MULTIRES_RANGE = {"h263_multires_cross": MOTION_RANGE // 2}
 
@@ -926,6 +927,8 @@ def main():
                                  kind="full_sad")
         umhs = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
                                   kind="umhs")
+        fhs = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames, not args.no_cpu,
+                                 kind="fhs")
         pk, pk_kind = peaks()
         hbm_rows = run_hbm_paths(torch, _lib, L, ctx, stream, f"cuda:{local}", pk)
         line = {
@@ -949,7 +952,7 @@ def main():
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
             "serving": serving,
             "multires": mr, "multires_cross": mrc, "multires_cross_v2": mrc2, "cross": cr,
-            "h263_multires_cross": h263, "full_sad": sad, "umhs": umhs, **hbm_rows,
+            "h263_multires_cross": h263, "full_sad": sad, "umhs": umhs, "fhs": fhs, **hbm_rows,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

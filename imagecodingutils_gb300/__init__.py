@@ -28,7 +28,7 @@ from ._lib import VppGpuError, check, load
 
 __all__ = [
     "Context", "get_context", "MotionEstimatorH264ImplFull", "MotionEstimatorH264ImplMultires",
-    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross", "MotionEstimatorH264ImplFullSad", "MotionEstimatorH264ImplUMHS",
+    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross", "MotionEstimatorH264ImplFullSad", "MotionEstimatorH264ImplUMHS", "MotionEstimatorH264ImplFHS",
     "MotionEstimatorH263ImplMultiresCross", "MotionEstimatorBatch",
     "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
     "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1", "FastForwardDC4x4ITImpl1",
@@ -265,6 +265,37 @@ class MotionEstimatorH264ImplUMHS(_MotionEstimatorBase):
         pmv = None if pmv is None else np.ascontiguousarray(pmv, np.int16)
         pin = None if pin is None else np.ascontiguousarray(pin, np.uint8)
         check(load().vppgpu_me_set_prev_frame(self._h_me, _ptr(pmv), _ptr(pin)), "vppgpu_me_set_prev_frame")
+        pred, self._pred = self._pred, None
+        try:
+            mv, avg = super().Estimate(*args, param=param, want_mb_distortion=True)
+        finally:
+            self._pred = pred
+        if self._pred is not None:  # the reference hands the predictor each vector with its distortion
+            d = self.last_mb_distortion
+            for k in range(self.num_mbs()):
+                self._pred.Set16x16MotionVector(k, int(mv[k, 0]), int(mv[k, 1]), int(d[k]))
+        return mv, avg
+
+
+class MotionEstimatorH264ImplFHS(_MotionEstimatorBase):
+    """GPU MotionEstimatorH264ImplFHS (src/CodecUtils/MotionEstimatorH264ImplFHS.cpp):
+    the four-scale hexagon search from the median prediction on 80-point
+    extrapolated path distortions with integer costs, its half / quarter-pel
+    stages and the prediction check.  Constructor as the reference's
+    (pSrc, pRef, w, h, motionRange, pMVPred[, pDistortionIncluded[, pPrevFrmMBlk]]);
+    the previous-frame macroblocks are accepted and not read, as in the
+    reference.  The predictor side effect carries the distortion:
+    Set16x16MotionVector(k, x, y, d).  SetMode(0) quarter pel (the default),
+    1 half, 2 full pel."""
+
+    KIND = _lib.ME_FHS
+    DEFAULT_MODE = 0
+
+    def __init__(self, pSrc, pRef, imgWidth: int, imgHeight: int, motionRange: int = 64, pMVPred=None,
+                 pDistortionIncluded=None, pPrevFrmMBlk=None, mb_slice=None, ctx: Context | None = None):
+        super().__init__(pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred, pDistortionIncluded, mb_slice, ctx)
+
+    def Estimate(self, *args, param: float | None = None, want_mb_distortion: bool = True):
         pred, self._pred = self._pred, None
         try:
             mv, avg = super().Estimate(*args, param=param, want_mb_distortion=True)

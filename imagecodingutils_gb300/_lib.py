@@ -29,6 +29,7 @@ ERR_NO_DEVICE = -8
 ME_FULL, ME_MULTIRES, ME_MULTIRES_CROSS, ME_MULTIRES_CROSS_V2, ME_CROSS, ME_H263_MULTIRES_CROSS = 0, 1, 2, 3, 4, 5
 ME_FULL_SAD = 6
 ME_UMHS = 7
+ME_FHS = 8
 LAYOUT_BLOCKS, LAYOUT_MB16 = 0, 1
 INV_ROWS_FIRST, INV_COLS_FIRST = 0, 1
 RGB_FIXED_POINT, RGB_REAL, RGB_REAL_IMPL2 = 0, 1, 2

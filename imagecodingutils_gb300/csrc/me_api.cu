@@ -71,6 +71,10 @@ struct vppgpu_me {
 namespace {
 constexpr int kRing = 256;
 
+// The estimators whose search starts at the prediction (UMHS, FHS): one
+// pipeline (me_umhs.cu), its own relaxation policy.
+bool searches_from_prediction(int kind) { return kind == VPPGPU_ME_UMHS || kind == VPPGPU_ME_FHS; }
+
 void ring_fold(vppgpu_me* me)
 {
     for (int i = 0; i < me->ring_used; i++) {
@@ -206,7 +210,8 @@ vppgpu::UmhsArgs umhs_args(vppgpu_me* me)
     u.prev = me->d_uprev;
     u.order = me->d_uorder;
     u.sweeps = me->relax_sweeps < 1 ? 1 : me->relax_sweeps;
-    u.diag_limit = 256;
+    u.diag_limit = 1024;
+    u.fhs = me->kind == VPPGPU_ME_FHS;
     return u;
 }
 
@@ -237,7 +242,7 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
         return vppgpu::mrc2_launch(ctx, v2 ? 1 : 2, me->mode, me->d_mrc, full_args(me, v2 ? 0.9 : 1.1), d_src16,
                                    d_ref16);
     }
-    if (me->kind == VPPGPU_ME_UMHS) {
+    if (searches_from_prediction(me->kind)) {
         VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
         return vppgpu::umhs_launch(ctx, umhs_args(me), me->wave_grid);
     }
@@ -309,7 +314,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 4) return VPPGPU_ERR_INVALID_ARG;
     if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
     if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
-    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_UMHS) return VPPGPU_ERR_UNSUPPORTED;
+    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_FHS) return VPPGPU_ERR_UNSUPPORTED;
     // MotionEstimatorH263ImplMultiresCross's range is in half pels: at most 64 (+-31 pels), as 128 quarter pels
     if (kind == VPPGPU_ME_H263_MULTIRES_CROSS && motion_range > 64) return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
@@ -325,17 +330,17 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     me->nmb = me->cols * me->rows;
     me->motion_range = motion_range;
     // Cross and UMHS default to quarter pel (…ImplCross.cpp:184, …ImplUMHS.cpp:259)
-    me->mode = (kind == VPPGPU_ME_CROSS || kind == VPPGPU_ME_UMHS) ? 0 : 1;
+    me->mode = (kind == VPPGPU_ME_CROSS || searches_from_prediction(kind)) ? 0 : 1;
     me->rstride = width + 2 * vppgpu::PAD;
     me->sweep_limit = vppgpu::RELAX_SWEEPS + 2 + (me->nmb + 31) / 32;  // sweep counters, then the dirty bitmap
-    if (kind == VPPGPU_ME_UMHS && me->sweep_limit < vppgpu::UMHS_SWEEPS + 2)  // its counters only, up to 24 sweeps
-        me->sweep_limit = vppgpu::UMHS_SWEEPS + 2;
+    if (searches_from_prediction(kind) && me->sweep_limit < 2 * vppgpu::UMHS_EVALS)  // change and search counts
+        me->sweep_limit = 2 * vppgpu::UMHS_EVALS;
     // Sweep policy by how the estimator's predictions settle on moving content
     // (measured over 1080p pans): the full-search estimator mostly settles
     // within 8 sweeps over every MB, a few more over the dirty sets; Multires
     // keeps settling with more sweeps, cheaply over the dirty sets; Ver2
     // rarely settles, so its wavefront starts early.
-    me->relax_sweeps = kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : (kind == VPPGPU_ME_UMHS ? 20 : vppgpu::RELAX_SWEEPS);
+    me->relax_sweeps = kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : (searches_from_prediction(kind) ? 20 : vppgpu::RELAX_SWEEPS);
     me->grid_sweeps = kind == VPPGPU_ME_MULTIRES ? 4 : (kind == VPPGPU_ME_MULTIRES_CROSS_V2 ? 4 : 8);
     me->relax_blocks_per_sm = 4;
     me->mrc_warps = 8;
@@ -390,7 +395,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
         *out = me;
         return VPPGPU_OK;
     }
-    if (kind == VPPGPU_ME_UMHS) {
+    if (searches_from_prediction(kind)) {
         // MotionEstimatorH264ImplUMHS(…, pMVPred, pDistortionIncluded, pPrevFrmMBlk) + Create(): the padded
         // reference with its half-pel planes, sweep and dataflow states, records, the previous frame's
         // starting points (zero until vppgpu_me_set_prev_frame) and the dataflow order
@@ -518,7 +523,7 @@ int vppgpu_me_set_mode(vppgpu_me* me, int mode)
     if (!me) return VPPGPU_ERR_INVALID_ARG;
     // SetMode(0) picks by picture area for the multi-resolution estimators (MultiresCross.cpp:501-513);
     // Cross and UMHS keep the mode as given (MotionEstimatorH264ImplCross.h:99, …ImplUMHS.h:107)
-    if (mode == 0 && me->kind != VPPGPU_ME_FULL && me->kind != VPPGPU_ME_CROSS && me->kind != VPPGPU_ME_UMHS)
+    if (mode == 0 && me->kind != VPPGPU_ME_FULL && me->kind != VPPGPU_ME_CROSS && !searches_from_prediction(me->kind))
         mode = (me->W * me->H > 40000) ? 2 : 1;
     me->mode = mode;
     return VPPGPU_OK;
@@ -685,7 +690,7 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 
 extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
 {
-    if (!me || sweeps < 0 || sweeps > (me->kind == VPPGPU_ME_UMHS ? vppgpu::UMHS_SWEEPS : vppgpu::RELAX_SWEEPS))
+    if (!me || sweeps < 0 || sweeps > (searches_from_prediction(me->kind) ? vppgpu::UMHS_SWEEPS : vppgpu::RELAX_SWEEPS))
         return VPPGPU_ERR_INVALID_ARG;
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS ||
         me->kind == VPPGPU_ME_FULL_SAD)
@@ -751,7 +756,7 @@ extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS) {
         for (int w : {2, 4, 8})
             if (w != cur.warps) cands.push_back({cur.relax, cur.grid, cur.bps, w});
-    } else if (me->kind == VPPGPU_ME_UMHS) {  // only the sweeps before the dataflow pass matter
+    } else if (searches_from_prediction(me->kind)) {  // only the sweeps before the dataflow pass matter
         for (int r : {4, 8, 12, 16, 20, 24})
             if (r != cur.relax) cands.push_back({r, cur.grid, cur.bps, cur.warps});
     } else {
@@ -854,7 +859,7 @@ extern "C" int vppgpu_me_last_stats(vppgpu_me* me, int* stats8)
     VPP_CUDA(cudaMemcpyAsync(me->h_ctrl, me->ctrl, sizeof(vppgpu::MeCtrl), cudaMemcpyDeviceToHost, me->ctx->stream));
     VPP_CUDA(cudaStreamSynchronize(me->ctx->stream));
     const vppgpu::MeCtrl& c = *me->h_ctrl;
-    int v[8] = {c.sweeps, c.converged, c.relax_evals, c.relax_miss, c.wave_miss, c.status, c.count, 0};
+    int v[8] = {c.sweeps, c.converged, c.relax_evals, c.relax_miss, c.wave_miss, c.status, c.count, c.ntie};
     for (int i = 0; i < 8; i++) stats8[i] = v[i];
     return VPPGPU_OK;
 }

@@ -151,6 +151,7 @@ int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, cons
 // exact raster result, looking predictions up in the records first.
 constexpr int UMHS_RECORDS = 8;  // records per macroblock
 constexpr int UMHS_SWEEPS = 24;  // most relaxation sweeps
+constexpr int UMHS_EVALS = UMHS_SWEEPS + 2;  // FullArgs::changed index of the per-sweep search counts
 struct UmhsArgs {
     FullArgs f;                 // planes, geometry, job, control, change counters
     unsigned long long* state;  // per MB: sweep state, packed vector | distortion << 32
@@ -159,7 +160,8 @@ struct UmhsArgs {
     const int* prev;            // per MB: the previous frame's full-pel starting point (packed; 0: none)
     const int* order;           // dataflow ticket -> macroblock (anti-diagonals c + 2r, rows ascending)
     int sweeps;                 // relaxation sweeps before the dataflow pass (>= 1)
-    int diag_limit;             // last-sweep changes up to which the one-CTA diagonal pass decides
+    int diag_limit;             // last-sweep searches up to which the one-CTA diagonal pass starts
+    int fhs;                    // 1: MotionEstimatorH264ImplFHS's search, 0: UMHS's
 };
 // The planes, `sweeps` relaxation sweeps, the dataflow pass (wave_grid CTAs of
 // 4 warps) and the outputs.

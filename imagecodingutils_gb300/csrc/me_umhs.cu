@@ -1,5 +1,8 @@
 // me_umhs.cu -- MotionEstimatorH264ImplUMHS::Estimate
-// (src/CodecUtils/MotionEstimatorH264ImplUMHS.cpp:446-945) on the GPU.
+// (src/CodecUtils/MotionEstimatorH264ImplUMHS.cpp:446-945) and
+// MotionEstimatorH264ImplFHS::Estimate (src/CodecUtils/MotionEstimatorH264ImplFHS.cpp:497-900)
+// on the GPU.  Both search from the median prediction and share everything
+// but the search itself (the kernels are templates on it).
 //
 // The estimator searches from the median prediction: starting points at the
 // prediction, zero and the previous frame's co-located vector; early exits on
@@ -360,6 +363,281 @@ __device__ __noinline__ int4 umhs_evaluate(const UmhsArgs& u, int k, int px, int
     return make_int4(pack_mv(px, py), outcome, pack_mv(mvx, mvy), min_d);
 }
 
+// ---------------------------------------------------------------------------
+// MotionEstimatorH264ImplFHS (src/CodecUtils/MotionEstimatorH264ImplFHS.cpp:497-900)
+// ---------------------------------------------------------------------------
+
+// Exact floor(sqrt(s)): what (int)std::sqrt(int) gives for the integers met here.
+__device__ __forceinline__ int isqrt_floor(int s)
+{
+    int r = (int)__fsqrt_rn((float)s);
+    while (r * r > s) r--;
+    while ((r + 1) * (r + 1) <= s) r++;
+    return r;
+}
+
+// MEH264IFHS_COST (MotionEstimatorH264ImplFHS.cpp:222): (D + 269 * (int)sqrt(s)) >> 8.
+__device__ __forceinline__ int fhs_cost(int d, int s) { return (d + 269 * isqrt_floor(s)) >> 8; }
+
+// Td16x16OptimalPathLessThan (MotionEstimatorH264ImplFHS.cpp:1685-1790) by one
+// lane for the block at offset (x, y): squared differences along the first 80
+// path points, the whole block's distortion extrapolated as D * 256 / N after
+// 32, 40, .., 72 points (returned at once above the running minimum) and after
+// 80 (returned).  The reference accepts a candidate iff no extrapolation
+// exceeds the minimum and the last does not either: *worst is the largest
+// extrapolation, *last the value returned when none exceeds.
+__device__ __forceinline__ void lane_path(const unsigned char* win, int x, int y, int* worst, int* last)
+{
+    constexpr signed char P[80][2] = {
+        {5, 10},  {13, 5},  {2, 1},   {13, 14}, {1, 14},  {9, 1},   {1, 6},   {15, 9},  {8, 13},  {14, 2},
+        {7, 4},   {10, 8},  {4, 15},  {0, 10},  {0, 3},   {5, 0},   {12, 11}, {4, 7},   {12, 0},  {10, 14},
+        {3, 12},  {10, 5},  {15, 13}, {4, 3},   {7, 8},   {14, 7},  {6, 13},  {11, 3},  {2, 9},   {9, 10},
+        {15, 1},  {7, 2},   {3, 5},   {8, 15},  {1, 12},  {8, 6},   {0, 1},   {12, 9},  {14, 15}, {15, 4},
+        {11, 12}, {6, 6},   {7, 11},  {0, 7},   {14, 11}, {7, 0},   {2, 15},  {12, 7},  {2, 3},   {4, 9},
+        {12, 2},  {9, 3},   {12, 13}, {3, 0},   {5, 14},  {5, 4},   {0, 13},  {8, 9},   {2, 11},  {11, 15},
+        {10, 1},  {2, 7},   {15, 6},  {9, 12},  {5, 2},   {5, 12},  {1, 4},   {11, 5},  {13, 8},  {9, 7},
+        {13, 3},  {5, 8},   {10, 11}, {6, 15},  {13, 10}, {8, 4},   {3, 10},  {13, 1},  {1, 8},   {14, 0}};
+    const unsigned char* b = win + (31 + y) * kWinStride + 32 + x;
+    const unsigned char* t = win + kWinBytes + 16;
+    int d = 0, w = 0;
+#pragma unroll
+    for (int p = 0; p < 80; p++) {
+        const int e = (int)b[P[p][1] * kWinStride + P[p][0]] - (int)t[P[p][1] * 16 + P[p][0]];
+        d += e * e;
+        if (p + 1 >= 32 && p + 1 < 80 && ((p + 1) & 7) == 0) w = max(w, d * 256 / (p + 1));
+    }
+    *last = d * 256 / 80;
+    *worst = max(w, *last);
+}
+
+// One FHS pattern pass (the loops of FHS.cpp:688-818): lane c takes candidate
+// c, in range, its path distortion accepted at the running minimum and a
+// strictly lower integer cost; the acceptances are applied in order by a
+// ballot walk as in probe().
+__device__ __forceinline__ void fhs_probe(Search& s, int kind, int w, const unsigned char* win, int lane)
+{
+    int j = 0, i = 0;
+    bool v = pattern_offset(kind, lane, w, 0, 0, 1 << 20, j, i);
+    v = v && i + s.my >= s.yu && i + s.my <= s.yd && j + s.mx >= s.xl && j + s.mx <= s.xr;
+    int worst = 0, d = 0, cost = 0;
+    if (v) {
+        lane_path(win, s.mx + j, s.my + i, &worst, &d);
+        const int dx = s.mx + j - s.px0, dy = s.my + i - s.py0;
+        cost = fhs_cost(d, dx * dx + dy * dy);
+    }
+    int last = -1;
+    while (true) {
+        const unsigned m = __ballot_sync(0xffffffffu, v && lane > last && worst <= s.min_d && cost < s.min_cost);
+        if (!m) break;
+        const int f = __ffs(m) - 1;
+        s.min_d = __shfl_sync(0xffffffffu, d, f);
+        s.min_cost = __shfl_sync(0xffffffffu, cost, f);
+        s.rmx = __shfl_sync(0xffffffffu, j, f);
+        s.rmy = __shfl_sync(0xffffffffu, i, f);
+        last = f;
+    }
+}
+
+// SSD of the block at quarter-pel offset (qx, qy) from full-pel origin
+// (x0, y0), one warp: the H.264 samples of the half-pel planes (the values
+// FHS's half-pel cache and QuarterRead hold).
+__device__ __forceinline__ int fhs_sub_sd(const FullArgs& a, int x0, int y0, int qx, int qy, uint2 cur, int lane)
+{
+    const int fx = qx & 3, fy = qy & 3;
+    return warp_sum(ssd8(cur, qpel_block8(a, x0 + (qx >> 2), y0 + (qy >> 2), fx, fy, lane)));
+}
+
+// HalfPelEstimate (FHS.cpp:1109-1200): the two "h" offsets, the two "b", the
+// four "j", strict improvement, leaving after a stage whose minimum is below
+// 1000.  *h_exit: it left after the "h" stage.
+__device__ __forceinline__ int fhs_half(const FullArgs& a, int x0, int y0, int min, uint2 cur, int lane, int* hx,
+                                        int* hy, bool* h_exit)
+{
+    constexpr int HX[8] = {0, 0, -1, 1, -1, 1, -1, 1}, HY[8] = {-1, 1, 0, 0, -1, -1, 1, 1};
+    int part[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        part[k] = ssd8(cur, load8(even_block(a, x0, y0, 2 * HY[k], 2 * HX[k], lane)));
+    int lcl = min;
+    *hx = *hy = 0;
+    *h_exit = false;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int d = warp_sum(part[k]);
+        if (d < lcl) {
+            lcl = d;
+            *hx = HX[k];
+            *hy = HY[k];
+        }
+        if ((k == 1 || k == 3) && lcl < 1000) {
+            *h_exit = k == 1;
+            break;
+        }
+    }
+    return lcl;
+}
+
+// QuarterPelEstimate (FHS.cpp:1213-1480): the half-pel stage, then the eight
+// quarter offsets around its winner in MEH264IFHS_SubPos order, strict
+// improvement, leaving at a minimum below 1000.  The offset returned is the
+// last quarter-pel improvement only (a half-pel winner without one comes back
+// as (0, 0) with its distortion), as the reference does.  Where the half-pel
+// stage left after "h" with nothing better, the reference's quarter pass reads
+// "b" / "j" cache samples of earlier macroblocks; this macroblock's samples
+// are used instead, and the event is counted (MeCtrl::ntie).
+__device__ __forceinline__ int fhs_quarter(const FullArgs& a, int x0, int y0, int min, uint2 cur, int lane, int* qx,
+                                           int* qy)
+{
+    constexpr int SX[8] = {-1, 0, 1, -1, 1, -1, 0, 1}, SY[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+    int hx, hy;
+    bool h_exit;
+    const int half = fhs_half(a, x0, y0, min, cur, lane, &hx, &hy, &h_exit);
+    int lcl = min;
+    *qx = *qy = 0;
+    if (half < min) {
+        lcl = half;
+        if (half < 1000) return lcl;
+    }
+    if (h_exit && lane == 0) atomicAdd(&a.ctrl->ntie, 1);
+    for (int k = 0; k < 8; k++) {
+        const int ox = 2 * hx + SX[k], oy = 2 * hy + SY[k];
+        const int d = fhs_sub_sd(a, x0, y0, ox, oy, cur, lane);
+        if (d < lcl) {
+            lcl = d;
+            *qx = ox;
+            *qy = oy;
+            if (d < 1000) break;
+        }
+    }
+    return lcl;
+}
+
+// MotionEstimatorH264ImplFHS::Estimate for macroblock k at prediction (px, py)
+// with distortion pd, one warp; the record as umhs_evaluate returns it.
+__device__ __noinline__ int4 fhs_evaluate(const UmhsArgs& u, int k, int px, int py, int pd, int lane, int* bad,
+                                          unsigned char* win)
+{
+    const FullArgs& a = u.f;
+    Search s;
+    s.n = (k % a.cols) * 16;
+    s.m = (k / a.cols) * 16;
+    const uint2 cur = load_cur8(a, s.n, s.m, lane);
+    // the prediction truncated to one macroblock outside the picture, its
+    // quarter-pel part dropped then (:540-560)
+    int pxq = px % 4, pyq = py % 4, px0 = px / 4, py0 = py / 4;
+    const int opx0 = px0, opy0 = py0;
+    if (px0 + s.n > a.W) px0 = 16;
+    if (px0 + s.n < -16) px0 = -16;
+    if (py0 + s.m > a.H) py0 = 16;
+    if (py0 + s.m < -16) py0 = -16;
+    if (opx0 != px0 || opy0 != py0) pxq = pyq = 0;
+    const int rpx = 4 * px0 + pxq, rpy = 4 * py0 + pyq;
+    s.px0 = px0;
+    s.py0 = py0;
+    full_range(s.n, s.m, a.W, a.H, a.motion_range, s.xl, s.xr, s.yu, s.yd);
+    // the prediction's full SSD at quarter pel (:562-597)
+    const int pq = ssd8(cur, qpel_block8(a, s.n + px0 + (pxq < 0 ? -1 : 0), s.m + py0 + (pyq < 0 ? -1 : 0), pxq & 3,
+                                         pyq & 3, lane));
+    window_fill(a, s.n, s.m, win, lane);
+    const int pred_vd = warp_sum(pq);
+    s.min_d = pred_vd;
+    s.mx = px0;
+    s.my = py0;
+    s.min_cost = pred_vd >> 8;
+    if (pred_vd < 1000) return make_int4(pack_mv(px, py), kNoPdTest, pack_mv(rpx, rpy), pred_vd);
+    // zero (:599-625)
+    if (rpx || rpy) {
+        int worst = 0, zd = 0;
+        if (lane == 0) lane_path(win, 0, 0, &worst, &zd);
+        worst = __shfl_sync(0xffffffffu, worst, 0);
+        zd = __shfl_sync(0xffffffffu, zd, 0);
+        if (worst <= s.min_d && zd < s.min_d) {
+            const int zc = fhs_cost(zd, px0 * px0 + py0 * py0);
+            if (zc < s.min_cost) {
+                s.min_d = zd;
+                s.min_cost = zc;
+                s.mx = s.my = 0;
+            }
+            if (zd < 1000) return make_int4(pack_mv(px, py), kNoPdTest, 0, s.min_d);
+        }
+    }
+    // first early exit (:681-683)
+    int outcome = kNoPdTest;
+    const int d0 = s.min_d;
+    int st;
+    if (d0 < 1000) {
+        st = P_DIAMOND;
+    } else if (d0 < 4000) {
+        st = P_EXTHEX;
+    } else {
+        bool taken = false;
+        if (d0 == pred_vd) {
+            taken = d0 < pd * 12 / 10 && d0 > pd * 8 / 10;
+            outcome = (d0 << 1) | (taken ? 1 : 0);
+        }
+        st = taken ? P_EXTHEX : P_HEX;
+    }
+    if (st == P_HEX) {  // four hexagon scales, no early exit (:684-748)
+        s.rmx = s.rmy = 0;
+        for (int w = 1; w <= 4; w++) fhs_probe(s, P_HEX, w, win, lane);
+        s.mx += s.rmx;
+        s.my += s.rmy;
+        st = P_EXTHEX;
+    }
+    if (st == P_EXTHEX) {  // one extended-hexagon pass (:751-784)
+        s.rmx = s.rmy = 0;
+        fhs_probe(s, P_EXTHEX, 1, win, lane);
+        s.mx += s.rmx;
+        s.my += s.rmy;
+    }
+    {  // one diamond pass (:786-820)
+        s.rmx = s.rmy = 0;
+        fhs_probe(s, P_DIAMOND, 1, win, lane);
+        s.mx += s.rmx;
+        s.my += s.rmy;
+    }
+    // half / quarter stages (:822-856)
+    int mvx = 4 * s.mx, mvy = 4 * s.my;
+    if (a.mode == 0) {
+        int qx, qy;
+        const int nm = fhs_quarter(a, s.n + s.mx, s.m + s.my, s.min_d, cur, lane, &qx, &qy);
+        if (nm < s.min_d) {
+            s.min_d = nm;
+            mvx += qx;
+            mvy += qy;
+        }
+    } else if (a.mode == 1) {
+        int hx, hy;
+        bool h_exit;
+        const int nm = fhs_half(a, s.n + s.mx, s.m + s.my, s.min_d, cur, lane, &hx, &hy, &h_exit);
+        if (nm < s.min_d) {
+            s.min_d = nm;
+            mvx += 2 * hx;
+            mvy += 2 * hy;
+        }
+    }
+    // the prediction check; the costs compare quarter-pel vectors with the
+    // full-pel prediction, as the reference does (:858-867)
+    const int cp = fhs_cost(pred_vd, (rpx - px0) * (rpx - px0) + (rpy - py0) * (rpy - py0));
+    const int cw = fhs_cost(s.min_d, (mvx - px0) * (mvx - px0) + (mvy - py0) * (mvy - py0));
+    if (cp <= cw) {
+        s.min_d = pred_vd;
+        mvx = rpx;
+        mvy = rpy;
+    }
+    (void)bad;
+    return make_int4(pack_mv(px, py), outcome, pack_mv(mvx, mvy), s.min_d);
+}
+
+// The estimator's evaluation: UMHS or FHS.
+template <bool kFhs>
+__device__ __forceinline__ int4 evaluate(const UmhsArgs& u, int k, int px, int py, int pd, int lane, int* bad,
+                                         unsigned char* win)
+{
+    if constexpr (kFhs) return fhs_evaluate(u, k, px, py, pd, lane, bad, win);
+    else return umhs_evaluate(u, k, px, py, pd, lane, bad, win);
+}
+
 // Whether a record made at the prediction's vector holds for distortion pd.
 __device__ __forceinline__ bool record_holds(int outcome, int pd)
 {
@@ -414,6 +692,7 @@ __device__ __forceinline__ int4 empty_record() { return make_int4(0, 0, 0, -1); 
 // handle's previous estimate's final states (zero after creation): the fixed
 // point does not depend on where the relaxation starts, and consecutive frames
 // start close to it.  Skipped once an earlier sweep changed nothing.
+template <bool kFhs>
 __global__ void __launch_bounds__(128) k_umhs_sweep(UmhsArgs u, int sweep)
 {
     __shared__ __align__(16) unsigned char wins[4][kWinSlot];
@@ -443,7 +722,7 @@ __global__ void __launch_bounds__(128) k_umhs_sweep(UmhsArgs u, int sweep)
         int mv, d;
         if (!record_lookup(e, px, py, pd, &mv, &d)) {
             int bad = 0;
-            const int4 r = umhs_evaluate(u, k, px, py, pd, lane, &bad, wins[threadIdx.x >> 5]);
+            const int4 r = evaluate<kFhs>(u, k, px, py, pd, lane, &bad, wins[threadIdx.x >> 5]);
             if (bad && lane == 0) atomicOr(&a.ctrl->status, ST_OUT_OF_BOUNDS);
             mv = r.z;
             d = r.w;
@@ -463,7 +742,10 @@ __global__ void __launch_bounds__(128) k_umhs_sweep(UmhsArgs u, int sweep)
     }
     if (lane == 0) {
         if (changed) atomicAdd(a.changed + sweep, changed);
-        if (evals) atomicAdd(&a.ctrl->relax_miss, evals);
+        if (evals) {
+            atomicAdd(&a.ctrl->relax_miss, evals);
+            atomicAdd(a.changed + UMHS_EVALS + sweep, evals);
+        }
     }
 }
 
@@ -476,13 +758,15 @@ __device__ __forceinline__ bool relaxed(const UmhsArgs& u)
 }
 
 // Which exact pass decides a frame the relaxation left unsettled: the one-CTA
-// diagonal pass when the last sweep changed few macroblocks (few record
+// diagonal pass when the last sweep had to search few macroblocks (few record
 // misses to come: cheap steps matter), else the dataflow pass over all SMs
-// (many misses: parallel searches matter).
+// (many misses: parallel searches matter).  The diagonal pass hands the rest
+// of the frame to the dataflow pass when its misses exceed a budget.
 __device__ __forceinline__ bool diagonal_pass(const UmhsArgs& u)
 {
-    return *((volatile const int*)u.f.changed + u.sweeps - 1) <= u.diag_limit;
+    return *((volatile const int*)u.f.changed + UMHS_EVALS + u.sweeps - 1) <= u.diag_limit;
 }
+constexpr int kDiagMissBudget = 48;
 
 // The exact raster result in one CTA: lane l of warp w owns row 32w + l and
 // at step t takes column t - 2r, so a step is an anti-diagonal c + 2r = t,
@@ -492,6 +776,7 @@ __device__ __forceinline__ bool diagonal_pass(const UmhsArgs& u)
 // three read).  One block barrier per step, no waits.  A record gives the
 // result for the prediction; the lanes that find none are searched by their
 // warp, one after another.
+template <bool kFhs>
 __global__ void __launch_bounds__(512) k_umhs_diag(UmhsArgs u)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -501,10 +786,13 @@ __global__ void __launch_bounds__(512) k_umhs_diag(UmhsArgs u)
     const int cols = a.cols, rows = a.nmb / cols;
     unsigned char* win = smem + (size_t)wid * kWinSlot;
     unsigned long long* ring = reinterpret_cast<unsigned long long*>(smem + (size_t)nw * kWinSlot);
+    __shared__ int s_misses;
     const int r = wid * 32 + lane;
     const bool row_ok = r < rows;
     const int* slice = a.job->slice;
     unsigned long long left = 0;
+    if (threadIdx.x == 0) s_misses = 0;
+    __syncthreads();
     int4 nxt[UMHS_RECORDS];
 #pragma unroll
     for (int e = 0; e < UMHS_RECORDS; e++) nxt[e] = empty_record();
@@ -545,7 +833,7 @@ __global__ void __launch_bounds__(512) k_umhs_diag(UmhsArgs u)
             const int f = __ffs(miss) - 1;
             miss &= miss - 1;
             int bad = 0;
-            const int4 rr = umhs_evaluate(u, __shfl_sync(0xffffffffu, k, f), __shfl_sync(0xffffffffu, px, f),
+            const int4 rr = evaluate<kFhs>(u, __shfl_sync(0xffffffffu, k, f), __shfl_sync(0xffffffffu, px, f),
                                           __shfl_sync(0xffffffffu, py, f), __shfl_sync(0xffffffffu, pd, f), lane,
                                           &bad, win);
             if (bad && lane == 0) atomicOr(&a.ctrl->status, ST_OUT_OF_BOUNDS);
@@ -561,9 +849,15 @@ __global__ void __launch_bounds__(512) k_umhs_diag(UmhsArgs u)
             ring[(size_t)r * 4 + (c & 3)] = st;
             __stcg(u.wave + k, st);
         }
+        if (lane == 0 && misses) atomicAdd(&s_misses, misses);
+        if (lane == 0 && misses) atomicAdd(&a.ctrl->wave_miss, misses);
+        misses = 0;
         __syncthreads();
+        // every macroblock of diagonals 0..t is published: past the budget the
+        // dataflow pass takes the rest
+        if (s_misses > kDiagMissBudget) return;
     }
-    if (lane == 0 && misses) atomicAdd(&a.ctrl->wave_miss, misses);
+    if (threadIdx.x == 0) a.ctrl->converged = 2;  // the diagonal pass decided the whole frame
 }
 
 // The exact raster result by dataflow over the anti-diagonal order.  A warp
@@ -571,11 +865,12 @@ __global__ void __launch_bounds__(512) k_umhs_diag(UmhsArgs u)
 // neighbours' published states (lanes 0..2, bounded, giving up at once when
 // another warp gave up), then takes the record for its prediction or
 // searches, and publishes its state with release semantics.
+template <bool kFhs>
 __global__ void __launch_bounds__(128) k_umhs_wave(UmhsArgs u)
 {
     __shared__ __align__(16) unsigned char wins[4][kWinSlot];
     const FullArgs& a = u.f;
-    if (relaxed(u) || diagonal_pass(u)) return;
+    if (relaxed(u) || *((volatile int*)&a.ctrl->converged) == 2) return;
     const int lane = threadIdx.x & 31;
     const int rows = a.nmb / a.cols;
     const int* slice = a.job->slice;
@@ -587,6 +882,7 @@ __global__ void __launch_bounds__(128) k_umhs_wave(UmhsArgs u)
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= a.nmb) break;
         const int k = __ldg(u.order + t);
+        if (__ldcg(u.wave + k) != kPending) continue;  // decided by the diagonal pass before it handed over
         const int av = neighbour_mask(slice, k, a.cols, rows);
         const int4 e = lane < UMHS_RECORDS ? __ldcg(u.rec + (size_t)k * UMHS_RECORDS + lane) : empty_record();
         int nb = -1;
@@ -611,7 +907,7 @@ __global__ void __launch_bounds__(128) k_umhs_wave(UmhsArgs u)
         int mv, d;
         if (!record_lookup(e, px, py, pd, &mv, &d)) {
             int bad = 0;
-            const int4 r = umhs_evaluate(u, k, px, py, pd, lane, &bad, wins[threadIdx.x >> 5]);
+            const int4 r = evaluate<kFhs>(u, k, px, py, pd, lane, &bad, wins[threadIdx.x >> 5]);
             if (bad && lane == 0) atomicOr(&a.ctrl->status, ST_OUT_OF_BOUNDS);
             mv = r.z;
             d = r.w;
@@ -679,7 +975,9 @@ size_t umhs_diag_smem(int rows) { return (size_t)((rows + 31) / 32) * kWinSlot +
 int umhs_prepare()
 {
     // the largest frame: 8192 / 16 = 512 macroblock rows, 16 warps
-    VPP_CUDA(cudaFuncSetAttribute(k_umhs_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    VPP_CUDA(cudaFuncSetAttribute(k_umhs_diag<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)umhs_diag_smem(512)));
+    VPP_CUDA(cudaFuncSetAttribute(k_umhs_diag<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)umhs_diag_smem(512)));
     return VPPGPU_OK;
 }
@@ -690,14 +988,17 @@ int umhs_launch(vppgpu_ctx* ctx, const UmhsArgs& u, int wave_grid)
     if (rc) return rc;
     const int sweep_grid = (u.f.nmb + 3) / 4;
     for (int s = 0; s < u.sweeps; s++) {
-        k_umhs_sweep<<<sweep_grid, 128, 0, ctx->stream>>>(u, s);
+        if (u.fhs) k_umhs_sweep<true><<<sweep_grid, 128, 0, ctx->stream>>>(u, s);
+        else k_umhs_sweep<false><<<sweep_grid, 128, 0, ctx->stream>>>(u, s);
         VPP_CHECK_LAUNCH(ctx);
     }
     VPP_CUDA(cudaMemsetAsync(u.wave, 0xff, sizeof(unsigned long long) * (size_t)u.f.nmb, ctx->stream));
     const int rows = u.f.nmb / u.f.cols, nw = (rows + 31) / 32;
-    k_umhs_diag<<<1, nw * 32, umhs_diag_smem(rows), ctx->stream>>>(u);
+    if (u.fhs) k_umhs_diag<true><<<1, nw * 32, umhs_diag_smem(rows), ctx->stream>>>(u);
+    else k_umhs_diag<false><<<1, nw * 32, umhs_diag_smem(rows), ctx->stream>>>(u);
     VPP_CHECK_LAUNCH(ctx);
-    k_umhs_wave<<<wave_grid, 128, 0, ctx->stream>>>(u);
+    if (u.fhs) k_umhs_wave<true><<<wave_grid, 128, 0, ctx->stream>>>(u);
+    else k_umhs_wave<false><<<wave_grid, 128, 0, ctx->stream>>>(u);
     VPP_CHECK_LAUNCH(ctx);
     k_umhs_outputs<<<(u.f.nmb + 255) / 256, 256, 0, ctx->stream>>>(u);
     VPP_CHECK_LAUNCH(ctx);

@@ -81,6 +81,18 @@ int vppgpu_ctx_launch_count(vppgpu_ctx* ctx, unsigned long long* count);
  * (H264MotionVectorPredictorImpl1.h:112-121).  Modes 0 quarter (default), 1 half,
  * 2 full pel, kept as given. */
 #define VPPGPU_ME_UMHS              7
+/* MotionEstimatorH264ImplFHS (src/CodecUtils/MotionEstimatorH264ImplFHS.cpp:497-900):
+ * the four-scale hexagon search from the median prediction on 80-point
+ * extrapolated path distortions (Td16x16OptimalPathLessThan, :1685-1790) with
+ * integer costs, its own half / quarter-pel stages (:1109-1480) and the
+ * prediction check.  The same predictor contract as VPPGPU_ME_UMHS (a predicted
+ * distortion; Set16x16MotionVector with mb_dist_out); no previous-frame input
+ * (the reference's use of it is disabled, :627-673).  Modes 0 quarter (default),
+ * 1 half, 2 full pel.  Where the reference's quarter-pel pass would read sub-pel
+ * samples its cache holds from earlier macroblocks (the half-pel stage left
+ * early without an improvement), this macroblock's samples are used; such
+ * macroblocks are counted in vppgpu_me_last_stats()[7]. */
+#define VPPGPU_ME_FHS               8
 
 typedef struct vppgpu_me vppgpu_me;
 
@@ -177,8 +189,11 @@ int vppgpu_me_get_tuning(vppgpu_me* me, int* tuning4);
 
 /* Counters of the last estimate's prediction-dependent stage: {sweeps,
  * converged-by-relaxation, relaxation evaluations, of which distortion
- * computations, MBs the wavefront evaluated in full, status bits, included
- * MBs, 0}.  Synchronises the context stream.  No vpp counterpart. */
+ * computations (UMHS / FHS: searches in the relaxation), MBs the wavefront
+ * evaluated in full, status bits, included MBs, a kind-specific count (Full:
+ * macroblocks whose scan met a tie; FHS: quarter-pel passes over samples the
+ * reference would take from earlier macroblocks)}.  Synchronises the context
+ * stream.  No vpp counterpart. */
 int vppgpu_me_last_stats(vppgpu_me* me, int* stats8);
 /* Macroblocks whose final vector changed in each relaxation sweep 1 .. n of
  * the last estimate (n <= 14; 0 for sweeps that did not run).  Synchronises
