@@ -5,8 +5,10 @@
 // pair.bin holds the source then the reference luma plane (int16).  The
 // program estimates with GpuMotionEstimatorH264ImplFull (or, by the optional
 // last argument, ...Multires, ...MultiresCross, ...MultiresCrossVer2 or
-// ...Cross: "multires", "mrc", "mrc2", "cross", "sad"; "mrc2lam" is Ver2's
-// Lagrangian Estimate(long*, void*) with lambda 2.5) exactly as a codec would
+// ...Cross, ...UMHS, ...FHS: "multires", "mrc", "mrc2", "cross", "sad", "umhs",
+// "fhs"; "mrc2lam" is Ver2's Lagrangian Estimate(long*, void*) with lambda 2.5;
+// UMHS gets the previous frame's vectors from a first estimate of the same
+// pair, as a codec chains frames) exactly as a codec would
 // with the vpp class (constructor, Create, SetMode(0), Estimate, predictor
 // side effect), then
 // runs the forward/inverse 4x4 transform classes
@@ -30,13 +32,20 @@ public:
     virtual int Create(void) { return 1; }
     virtual int Get16x16Prediction(void*, int, int* x, int* y) { *x = *y = 0; return 1; }
     virtual void Set16x16MotionVector(int blk, int x, int y) { mv[2 * blk] = x; mv[2 * blk + 1] = y; }
+    virtual void Set16x16MotionVector(int blk, int x, int y, int d)
+    {
+        Set16x16MotionVector(blk, x, y);
+        if ((size_t)blk < dist.size()) dist[blk] = d;
+    }
     std::vector<int> mv;
+    std::vector<int> dist;
 };
 
 int main(int argc, char** argv)
 {
     if (argc != 6 && argc != 7) {
-        fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin [full|multires|mrc|mrc2|mrc2lam|cross|sad]\n", argv[0]);
+        fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin "
+                        "[full|multires|mrc|mrc2|mrc2lam|cross|sad|umhs|fhs]\n", argv[0]);
         return 2;
     }
     const std::string kind = argc == 7 ? argv[6] : "full";
@@ -51,6 +60,8 @@ int main(int argc, char** argv)
     for (int i = 0; i < nmb; i++) incl[i] = true;
 
     RecordingPredictor pred(nmb);
+    pred.dist.assign(nmb, -1);
+    std::vector<short> prev_mv;
     IMotionEstimator* me;
     if (kind == "multires")
         me = new GpuMotionEstimatorH264ImplMultires(src.data(), ref.data(), w, h, range, &pred, incl);
@@ -62,6 +73,23 @@ int main(int argc, char** argv)
         me = new GpuMotionEstimatorH264ImplCross(src.data(), ref.data(), w, h, range, &pred, incl);
     else if (kind == "sad")
         me = new GpuMotionEstimatorH264ImplFullSad(src.data(), ref.data(), w, h, range, &pred, incl);
+    else if (kind == "umhs") {
+        // a first estimate without a previous frame gives the vectors the second one starts from
+        GpuMotionEstimatorH264ImplUMHS first(src.data(), ref.data(), w, h, range, NULL);
+        long a0 = 0;
+        VectorStructList* v0 = first.Create() ? (VectorStructList*)first.Estimate(&a0) : NULL;
+        if (!v0) return 6;
+        prev_mv.resize(2 * (size_t)nmb);
+        for (int k = 0; k < nmb; k++) {
+            prev_mv[2 * k] = (short)v0->GetSimpleElement(k, 0);
+            prev_mv[2 * k + 1] = (short)v0->GetSimpleElement(k, 1);
+        }
+        GpuMotionEstimatorH264ImplUMHS* u = new GpuMotionEstimatorH264ImplUMHS(src.data(), ref.data(), w, h, range,
+                                                                               &pred, incl);
+        u->SetPrevFrame(prev_mv.data(), NULL);
+        me = u;
+    } else if (kind == "fhs")
+        me = new GpuMotionEstimatorH264ImplFHS(src.data(), ref.data(), w, h, range, &pred, incl);
     else
         me = new GpuMotionEstimatorH264ImplFull(src.data(), ref.data(), w, h, range, &pred, incl);
     if (!me->Create()) {
@@ -131,6 +159,8 @@ int main(int argc, char** argv)
     fwrite(blocks.data(), 2, blocks.size(), o);
     fwrite(dc_levels.data(), 2, dc_levels.size(), o);
     fwrite(dc.data(), 2, dc.size(), o);
+    fwrite(pred.dist.data(), 4, pred.dist.size(), o);
+    fwrite(prev_mv.data(), 2, prev_mv.size(), o);
     fclose(o);
     delete me;
     delete[] incl;

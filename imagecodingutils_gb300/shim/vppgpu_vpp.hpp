@@ -26,6 +26,7 @@
 #include "IInverseTransform.h"
 #include "IMotionEstimator.h"
 #include "IMotionVectorPredictor.h"
+#include "MacroBlockH264.h"
 #include "RGBtoYUV420Converter.h"
 #include "VectorStructList.h"
 #include "YUV420toRGBConverter.h"
@@ -49,7 +50,16 @@ public:
     virtual ~IMotionVectorPredictor() {}
     virtual int Create(void) = 0;
     virtual int Get16x16Prediction(void* pList, int blk, int* predX, int* predY) = 0;
+    virtual int Get16x16Prediction(void* pList, int blk, int* predX, int* predY, int* distortion)
+    {
+        (void)pList; (void)blk; (void)predX; (void)predY; (void)distortion;
+        return 0;
+    }
     virtual void Set16x16MotionVector(int blk, int mvX, int mvY) = 0;
+    virtual void Set16x16MotionVector(int blk, int mvX, int mvY, int distortion)
+    {
+        (void)blk; (void)mvX; (void)mvY; (void)distortion;
+    }
 };
 
 // The SIMPLE2D layout of vpp's VectorStructList: one {short x, short y} per block.
@@ -190,7 +200,7 @@ public:
                                int motionRange, IMotionVectorPredictor* pMVPred, void* pDistortionIncluded)
         : _kind(kind), _pSrc(pSrc), _pRef(pRef), _w(imgWidth), _h(imgHeight), _range(motionRange),
           _pMVPred(pMVPred), _pIncl((bool*)pDistortionIncluded), _mode(1), _me(NULL), _list(NULL),
-          _incl(NULL), _last(VPPGPU_OK)
+          _incl(NULL), _dist(NULL), _predDist(false), _last(VPPGPU_OK)
     {
     }
     virtual ~GpuMotionEstimatorH264Base() { Destroy(); }
@@ -209,6 +219,7 @@ public:
         _list = new VectorStructList(VectorStructList::SIMPLE2D);
         _list->SetLength(n);
         _incl = new unsigned char[n > 0 ? n : 1];
+        _dist = new int[n > 0 ? n : 1];
         return 1;
     }
     virtual void Reset(void) {}
@@ -247,14 +258,19 @@ protected:
         }
         short* mv = (short*)_list->GetListPtr();
         long a = 0;
+        int* dist = _predDist ? _dist : NULL;
         _last = with_lambda ? vppgpu_me_estimate_lambda(_me, (const short*)_pSrc, (const short*)_pRef, incl, NULL,
-                                                        lambda, mv, NULL, &a)
+                                                        lambda, mv, dist, &a)
                             : vppgpu_me_estimate(_me, (const short*)_pSrc, (const short*)_pRef, incl, NULL, mv,
-                                                 NULL, &a);
+                                                 dist, &a);
         if (avg) *avg = _last == VPPGPU_OK ? a : 0;
         if (_last != VPPGPU_OK) return NULL;
-        if (_pMVPred)
-            for (int k = 0; k < n; k++) _pMVPred->Set16x16MotionVector(k, mv[2 * k], mv[2 * k + 1]);
+        if (_pMVPred) {
+            if (_predDist)  // estimators whose predictor also predicts a distortion
+                for (int k = 0; k < n; k++) _pMVPred->Set16x16MotionVector(k, mv[2 * k], mv[2 * k + 1], dist[k]);
+            else
+                for (int k = 0; k < n; k++) _pMVPred->Set16x16MotionVector(k, mv[2 * k], mv[2 * k + 1]);
+        }
         return (void*)_list;
     }
     void Destroy(void)
@@ -265,6 +281,8 @@ protected:
         _list = NULL;
         delete[] _incl;
         _incl = NULL;
+        delete[] _dist;
+        _dist = NULL;
     }
 
     int _kind;
@@ -277,6 +295,8 @@ protected:
     vppgpu_me* _me;
     VectorStructList* _list;
     unsigned char* _incl;
+    int* _dist;      // per-macroblock distortions handed to the predictor
+    bool _predDist;  // Set16x16MotionVector(k, x, y, distortion) instead of (k, x, y)
     int _last;
 };
 
@@ -393,6 +413,123 @@ public:
                                      pDistortionIncluded)
     {
     }
+};
+
+// The estimators that search from the prediction and predict a distortion
+// too: MotionEstimatorH264ImplUMHS (…ImplUMHS.cpp:187-254) and
+// MotionEstimatorH264ImplFHS (…ImplFHS.cpp:230-297), quarter pel by default,
+// SetMode kept as given.  Each vector goes to the predictor with its
+// distortion (H264MotionVectorPredictorImpl1.h:112-121).  UMHS reads the
+// previous frame's macroblocks (vectors and intra flags) on every Estimate():
+// from the MacroBlockH264 array of its eight-argument constructor when built
+// against vpp, or from the arrays given to SetPrevFrame().
+class GpuMotionEstimatorH264ImplUMHS : public GpuMotionEstimatorH264Base {
+public:
+    GpuMotionEstimatorH264ImplUMHS(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int motionRange,
+                                   IMotionVectorPredictor* pMVPred, void* pDistortionIncluded = NULL)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_UMHS, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred,
+                                     pDistortionIncluded),
+          _prevMv(NULL), _prevIntra(NULL)
+#ifdef VPPGPU_WITH_VPP
+          , _pPrevFrmMBlk(NULL)
+#endif
+    {
+        _mode = 0;
+        _predDist = true;
+    }
+#ifdef VPPGPU_WITH_VPP
+    GpuMotionEstimatorH264ImplUMHS(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int motionRange,
+                                   IMotionVectorPredictor* pMVPred, void* pDistortionIncluded,
+                                   MacroBlockH264* pPrevFrmMBlk)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_UMHS, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred,
+                                     pDistortionIncluded),
+          _prevMv(NULL), _prevIntra(NULL), _pPrevFrmMBlk(pPrevFrmMBlk)
+    {
+        _mode = 0;
+        _predDist = true;
+    }
+#endif
+    virtual ~GpuMotionEstimatorH264ImplUMHS() { FreePrev(); }
+    // The previous frame's 16x16 vectors (2 shorts per macroblock, quarter pels)
+    // and intra flags (NULL: all inter); read on every Estimate(), not copied.
+    void SetPrevFrame(const short* prevMv, const unsigned char* prevIntra)
+    {
+        _prevMv = prevMv;
+        _prevIntra = prevIntra;
+    }
+    virtual void* Estimate(long* avgDistortion)
+    {
+        if (!_me) return NULL;
+        const short* mv = _prevMv;
+        const unsigned char* intra = _prevIntra;
+#ifdef VPPGPU_WITH_VPP
+        int n = _list->GetLength();
+        if (_pPrevFrmMBlk) {  // MacroBlockH264::_mvX[_16x16], _mvY[_16x16], _intraFlag
+            if (!_mvBuf) _mvBuf = new short[2 * (size_t)n];
+            if (!_intraBuf) _intraBuf = new unsigned char[n];
+            for (int k = 0; k < n; k++) {
+                _mvBuf[2 * k] = (short)_pPrevFrmMBlk[k]._mvX[MacroBlockH264::_16x16];
+                _mvBuf[2 * k + 1] = (short)_pPrevFrmMBlk[k]._mvY[MacroBlockH264::_16x16];
+                _intraBuf[k] = _pPrevFrmMBlk[k]._intraFlag ? 1 : 0;
+            }
+            mv = _mvBuf;
+            intra = _intraBuf;
+        }
+#endif
+        _last = vppgpu_me_set_prev_frame(_me, mv, intra);
+        if (_last != VPPGPU_OK) {
+            if (avgDistortion) *avgDistortion = 0;
+            return NULL;
+        }
+        return GpuMotionEstimatorH264Base::Estimate(avgDistortion);
+    }
+    virtual void* Estimate(const void* pSrc, const void* pRef, long* avgDistortion)
+    {
+        (void)pSrc;
+        (void)pRef;
+        return Estimate(avgDistortion);
+    }
+
+private:
+    void FreePrev(void)
+    {
+#ifdef VPPGPU_WITH_VPP
+        delete[] _mvBuf;
+        delete[] _intraBuf;
+        _mvBuf = NULL;
+        _intraBuf = NULL;
+#endif
+    }
+    const short* _prevMv;
+    const unsigned char* _prevIntra;
+#ifdef VPPGPU_WITH_VPP
+    MacroBlockH264* _pPrevFrmMBlk;
+    short* _mvBuf = NULL;
+    unsigned char* _intraBuf = NULL;
+#endif
+};
+
+class GpuMotionEstimatorH264ImplFHS : public GpuMotionEstimatorH264Base {
+public:
+    GpuMotionEstimatorH264ImplFHS(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int motionRange,
+                                  IMotionVectorPredictor* pMVPred, void* pDistortionIncluded = NULL)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_FHS, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred,
+                                     pDistortionIncluded)
+    {
+        _mode = 0;
+        _predDist = true;
+    }
+#ifdef VPPGPU_WITH_VPP
+    // the previous-frame macroblocks are accepted and not read, as in the reference (…ImplFHS.cpp:627-673)
+    GpuMotionEstimatorH264ImplFHS(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int motionRange,
+                                  IMotionVectorPredictor* pMVPred, void* pDistortionIncluded, MacroBlockH264*)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_FHS, pSrc, pRef, imgWidth, imgHeight, motionRange, pMVPred,
+                                     pDistortionIncluded)
+    {
+        _mode = 0;
+        _predDist = true;
+    }
+#endif
 };
 
 // ---------------------------------------------------------------------------

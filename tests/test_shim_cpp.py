@@ -34,7 +34,7 @@ def test_shim_compiles_against_vpp_interfaces():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["full", "multires", "mrc", "mrc2", "mrc2lam", "cross", "sad"])
+@pytest.mark.parametrize("kind", ["full", "multires", "mrc", "mrc2", "mrc2lam", "cross", "sad", "umhs", "fhs"])
 def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
     from imagecodingutils_gb300 import build
     exe = tmp_path / "example_estimate"
@@ -57,7 +57,10 @@ def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
     rest = np.frombuffer(raw[12 * nmb + 8:], np.int16)
     nblk = (w // 4) * 4
     levels, recon = rest[:16 * nblk], rest[16 * nblk:32 * nblk]
-    dc_lev, dc_rec = rest[32 * nblk:32 * nblk + w], rest[32 * nblk + w:]
+    dc_lev, dc_rec = rest[32 * nblk:32 * nblk + w], rest[32 * nblk + w:32 * nblk + 2 * w]
+    tail = raw[12 * nmb + 8 + 2 * (32 * nblk + 2 * w):]
+    pdist = np.frombuffer(tail[:4 * nmb], np.int32)
+    prev_mv = np.frombuffer(tail[4 * nmb:], np.int16).reshape(-1, 2)
     ones = np.ones(nmb, np.uint8)
     if kind == "full":
         mv_o, _, avg_o = orc.me_full(fr[1], fr[0], mr, dist_incl=ones)
@@ -72,6 +75,14 @@ def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
     elif kind == "sad":
         mv_o, d_o = orc.me_full_intpel(fr[1], fr[0], mr, metric=1)
         avg_o = int(d_o.sum()) // nmb
+    elif kind == "umhs":
+        mv0, _, _ = orc.me_umhs(fr[1], fr[0], mr)
+        np.testing.assert_array_equal(prev_mv, mv0)
+        mv_o, d_o, avg_o = orc.me_umhs(fr[1], fr[0], mr, dist_incl=ones, prev_mv=mv0)
+        np.testing.assert_array_equal(pdist, d_o)  # the predictor receives each vector with its distortion
+    elif kind == "fhs":
+        mv_o, d_o, avg_o = orc.me_fhs(fr[1], fr[0], mr, dist_incl=ones)
+        np.testing.assert_array_equal(pdist, d_o)
     else:
         mv_o, _, avg_o = orc.me_multires_cross_v2(fr[1], fr[0], mr, mode=0, dist_incl=ones)
     np.testing.assert_array_equal(mv, mv_o)
