@@ -21,6 +21,8 @@
 #include "MotionEstimatorH264ImplCross.h"
 #include "MotionEstimatorH264ImplUMHS.h"
 #include "MotionEstimatorH264ImplFHS.h"
+#include "MotionEstimatorImpl1.h"
+#include "SimpleMotionVectorList.h"
 #include "MotionEstimatorH263ImplMultiresCross.h"
 #include "VectorStructList.h"
 #include "MotionCompensatorH264ImplStd.h"
@@ -277,6 +279,26 @@ int ref_me_fhs(const short* src, const short* ref, int w, int h, int motion_rang
     if (avg_out) *avg_out = avg;
     delete me;
     delete[] flags;
+    return 0;
+}
+
+/* MotionEstimatorImpl1 (pSrc, pRef, w, h, macroBlkWidth, macroBlkHeight,
+ * motionRange): its SimpleMotionVectorList of (char x, char y) half-pel
+ * vectors, read as signed chars, and avgDistortion. */
+int ref_me_impl1(const short* src, const short* ref, int w, int h, int bw, int bh, int range, short* mv_out,
+                 long* avg_out)
+{
+    MotionEstimatorImpl1 me(src, ref, w, h, bw, bh, range);
+    if (!me.Create()) return -2;
+    long avg = 0;
+    SimpleMotionVectorList* l = (SimpleMotionVectorList*)me.Estimate(&avg);
+    const signed char* p = (const signed char*)l->GetDataPtr();
+    const int step = l->GetPatternSize(), n = l->GetLength();
+    for (int i = 0; i < n; i++) {
+        mv_out[2 * i] = p[(size_t)i * step];
+        mv_out[2 * i + 1] = p[(size_t)i * step + 1];
+    }
+    if (avg_out) *avg_out = avg;
     return 0;
 }
 

@@ -79,6 +79,15 @@ int vo_me_fhs(const short* src, const short* ref, int w, int h, int motion_range
               const unsigned char* dist_incl, const int* slice, short* mv_out, int* mb_dist, long* avg_dist,
               int* stale_out);
 
+/* MotionEstimatorImpl1::Estimate (src/CodecUtils/MotionEstimatorImpl1.cpp:275-395): full
+ * search of [-range, range-1]^2 full pels (range in pels, 1..63) for bw x bh blocks
+ * (even bw <= 16, bh <= 16, dividing w and h), HalfRead half-pel refinement,
+ * the weighted zero-vector choice; vectors in half pels (chars in the
+ * reference's SimpleMotionVectorList), per-block chosen distortion, the average
+ * over every block. */
+int vo_me_impl1(const short* src, const short* ref, int w, int h, int bw, int bh, int range, short* mv_out,
+                int* mb_dist, long* avg_dist);
+
 int vo_me_full(const short* src, const short* ref, int w, int h, int motion_range,
                const unsigned char* dist_incl, const int* slice,
                short* mv_out, int* mb_dist, long* avg_dist);

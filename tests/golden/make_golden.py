@@ -44,6 +44,10 @@ inputs and stores inputs and outputs:
                   in me_umhs.npz) at modes 0/1/2 with pDistortionIncluded,
                   vectors, the distortion stored with each and avgDistortion,
                   and pair 0 of the 1080p benchmark sequence (mode 0)
+* me_impl1.npz    MotionEstimatorImpl1 (the H.263-style full search with half-pel
+                  refinement and the weighted zero-vector choice): pan, shift and
+                  part-noise pairs, 16x16 and 8x8 blocks, ranges 7..32 pels;
+                  half-pel vectors and avgDistortion
 * me_1080p.npz    the headline size: Full, MultiresCross / Ver2 / Multires
                   (modes 0, 1, 2), Cross and the integer-pel SAD stage on three
                   frame pairs of the 1920x1080 benchmark sequence at
@@ -51,7 +55,7 @@ inputs and stores inputs and outputs:
                   SHA-256)
 
 Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
-names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc me_umhs me_fhs mc
+names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc me_umhs me_fhs me_impl1 mc
 transform dc yuv2rgb colour, default all)
 """
 from __future__ import annotations
@@ -331,6 +335,29 @@ def fhs_fixtures(ref: oracle.Reference) -> dict:
     return out
 
 
+IMPL1_CASES = [  # (name, w, h, block w, block h, range in pels, seed, generator)
+    ("qcif16_r16", 176, 144, 16, 16, 16, 111, "pan"),
+    ("qcif8_r16", 176, 144, 8, 8, 16, 112, "noisy"),
+    ("cif16_r15", 352, 288, 16, 16, 15, 113, "shift"),
+    ("small16_r7", 64, 48, 16, 16, 7, 114, "noisy"),
+    ("small8_r31", 96, 64, 8, 8, 31, 115, "pan"),
+    ("qcif16_r32", 176, 144, 16, 16, 32, 116, "shift"),
+]
+
+
+def impl1_fixtures(ref: oracle.Reference) -> dict:
+    out = {}
+    for name, w, h, bw, bh, rng, seed, gen in IMPL1_CASES:
+        fr = umhs_frames(seed, w, h, gen)
+        mv, avg = ref.me_impl1(fr[1], fr[0], rng, bw, bh)
+        out[f"{name}_src"] = fr[1].astype(np.uint8)
+        out[f"{name}_ref"] = fr[0].astype(np.uint8)
+        out[f"{name}_meta"] = np.array([w, h, bw, bh, rng], np.int32)
+        out[f"{name}_mv"] = mv
+        out[f"{name}_avg"] = np.array([avg], np.int64)
+    return out
+
+
 MC_CASES = [("qcif_r16", 176, 144, 16, 61), ("cif_r32", 352, 288, 32, 62), ("small_r8", 64, 48, 8, 63)]
 
 
@@ -519,7 +546,7 @@ def main() -> None:
               "me_mrc2_lambda": mrc2_lambda_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "me_cross": lambda r: mrc2_fixtures(r, "cross"),
               "me_h263mrc": lambda r: mrc_fixtures(r, "h263_multires_cross", H263_CASES),
-              "me_umhs": umhs_fixtures, "me_fhs": fhs_fixtures,
+              "me_umhs": umhs_fixtures, "me_fhs": fhs_fixtures, "me_impl1": impl1_fixtures,
               "mc": mc_fixtures,
               "transform": transform_fixtures, "dc": dc_fixtures, "yuv2rgb": yuv2rgb_fixtures,
               "colour": colour_fixtures}

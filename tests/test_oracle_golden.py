@@ -570,3 +570,29 @@ def test_me_fhs_against_compiled_reference(orc, seed, w, h, mr, mode, gen):
     np.testing.assert_array_equal(o[0], r[0])
     np.testing.assert_array_equal(o[1], r[1])
     assert o[2] == r[2]
+
+
+IMPL1_CASES = ["qcif16_r16", "qcif8_r16", "cif16_r15", "small16_r7", "small8_r31", "qcif16_r32"]
+
+
+@pytest.mark.parametrize("case", IMPL1_CASES)
+def test_me_impl1_matches_reference(orc, golden, case):
+    """MotionEstimatorImpl1: half-pel vectors and avgDistortion."""
+    g = golden("me_impl1.npz")
+    w, h, bw, bh, rng = (int(v) for v in g[f"{case}_meta"])
+    mv, dist, avg = orc.me_impl1(g[f"{case}_src"].astype(np.int16), g[f"{case}_ref"].astype(np.int16), rng, bw, bh)
+    np.testing.assert_array_equal(mv, g[f"{case}_mv"])
+    assert avg == int(g[f"{case}_avg"][0])
+    assert int(dist.sum()) // dist.size == avg
+
+
+@ref_available
+@pytest.mark.parametrize("seed,w,h,bw,bh,rng,gen", [(121, 176, 144, 16, 16, 12, "noisy"), (122, 208, 120, 8, 8, 20, "pan"),
+                                                   (123, 128, 96, 16, 16, 24, "shift")])
+def test_me_impl1_against_compiled_reference(orc, seed, w, h, bw, bh, rng, gen):
+    from tests.golden.make_golden import umhs_frames
+    fr = umhs_frames(seed, w, h, gen)
+    mv_r, avg_r = oracle_mod.Reference().me_impl1(fr[1], fr[0], rng, bw, bh)
+    mv, _, avg = orc.me_impl1(fr[1], fr[0], rng, bw, bh)
+    np.testing.assert_array_equal(mv, mv_r)
+    assert avg == avg_r
