@@ -28,7 +28,7 @@ from ._lib import VppGpuError, check, load
 
 __all__ = [
     "Context", "get_context", "MotionEstimatorH264ImplFull", "MotionEstimatorH264ImplMultires",
-    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross", "MotionEstimatorH264ImplFullSad", "MotionEstimatorH264ImplUMHS", "MotionEstimatorH264ImplFHS",
+    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross", "MotionEstimatorH264ImplFullSad", "MotionEstimatorH264ImplUMHS", "MotionEstimatorH264ImplFHS", "MotionEstimatorImpl1",
     "MotionEstimatorH263ImplMultiresCross", "MotionEstimatorBatch",
     "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
     "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1", "FastForwardDC4x4ITImpl1",
@@ -306,6 +306,37 @@ class MotionEstimatorH264ImplFHS(_MotionEstimatorBase):
             for k in range(self.num_mbs()):
                 self._pred.Set16x16MotionVector(k, int(mv[k, 0]), int(mv[k, 1]), int(d[k]))
         return mv, avg
+
+
+class MotionEstimatorImpl1(_MotionEstimatorBase):
+    """GPU MotionEstimatorImpl1 (src/CodecUtils/MotionEstimatorImpl1.cpp): constructor
+    (pSrc, pRef, imgWidth, imgHeight, macroBlkWidth, macroBlkHeight, motionRange) as the
+    reference's, blocks 16x16 or 8x8, motionRange in full pels (1..32).  Estimate()
+    returns the half-pel vectors (the reference's SimpleMotionVectorList of chars)
+    and avgDistortion over every block; no predictor."""
+
+    KIND = _lib.ME_IMPL1
+    DEFAULT_MODE = 0
+
+    def __init__(self, pSrc, pRef, imgWidth: int, imgHeight: int, macroBlkWidth: int = 16,
+                 macroBlkHeight: int = 16, motionRange: int = 16, ctx: Context | None = None):
+        super().__init__(pSrc, pRef, imgWidth, imgHeight, motionRange, None, None, None, ctx)
+        self._bw = int(macroBlkWidth)
+        self._bh = int(macroBlkHeight)
+
+    def Create(self) -> int:
+        self._destroy()
+        h = C.c_void_p()
+        rc = load().vppgpu_me_create_blocks(self._ctx.handle, self.KIND, self._w, self._h, self._bw, self._bh,
+                                            self._range, C.byref(h))
+        if rc != _lib.OK:
+            return 0
+        self._h_me = h
+        load().vppgpu_me_set_mode(self._h_me, self._mode)
+        return 1
+
+    def num_mbs(self) -> int:
+        return (self._w // self._bw) * (self._h // self._bh)
 
 
 class MotionEstimatorH264ImplMultiresCross(_MotionEstimatorBase):

@@ -30,6 +30,7 @@ ME_FULL, ME_MULTIRES, ME_MULTIRES_CROSS, ME_MULTIRES_CROSS_V2, ME_CROSS, ME_H263
 ME_FULL_SAD = 6
 ME_UMHS = 7
 ME_FHS = 8
+ME_IMPL1 = 9
 LAYOUT_BLOCKS, LAYOUT_MB16 = 0, 1
 INV_ROWS_FIRST, INV_COLS_FIRST = 0, 1
 RGB_FIXED_POINT, RGB_REAL, RGB_REAL_IMPL2 = 0, 1, 2
@@ -45,6 +46,7 @@ SIGNATURES = {
     "vppgpu_ctx_synchronize": (_I, [_P]),
     "vppgpu_ctx_launch_count": (_I, [_P, C.POINTER(C.c_ulonglong)]),
     "vppgpu_me_create": (_I, [_P, _I, _I, _I, _I, C.POINTER(_P)]),
+    "vppgpu_me_create_blocks": (_I, [_P, _I, _I, _I, _I, _I, _I, C.POINTER(_P)]),
     "vppgpu_me_destroy": (_I, [_P]),
     "vppgpu_me_set_mode": (_I, [_P, _I]),
     "vppgpu_me_get_mode": (_I, [_P, C.POINTER(_I)]),

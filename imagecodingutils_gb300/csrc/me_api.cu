@@ -58,6 +58,7 @@ struct vppgpu_me {
     int* d_uprev;                  // UMHS: previous frame's full-pel starting points
     int* d_uorder;                 // UMHS: dataflow ticket -> macroblock
     int wave_grid;                 // UMHS: CTAs of the dataflow pass
+    int bw, bh;                    // block size (16 x 16 but for MotionEstimatorImpl1)
     vppgpu::MeCtrl* h_ctrl;  // pinned
     int last_status;
     // per-kernel timing (vppgpu_me_set_timing)
@@ -246,6 +247,7 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
         VPP_CUDA(cudaMemsetAsync(me->changed, 0, sizeof(int) * (size_t)me->sweep_limit, ctx->stream));
         return vppgpu::umhs_launch(ctx, umhs_args(me), me->wave_grid);
     }
+    if (me->kind == VPPGPU_ME_IMPL1) return vppgpu::impl1_launch(ctx, full_args(me, 0.0), me->bw, me->bh, me->motion_range);
     if (me->kind == VPPGPU_ME_FULL_SAD) {
         // the integer-pel stage only: no sub-pel, no prediction check, no GetBestVector
         vppgpu::FullArgs a = full_args(me, 0.0);
@@ -305,10 +307,62 @@ const int* me_status_word(vppgpu_me* me) { return &me->ctrl->status; }
 
 extern "C" {
 
+int vppgpu_me_create_blocks(vppgpu_ctx* ctx, int kind, int width, int height, int block_w, int block_h,
+                            int motion_range, vppgpu_me** out)
+{
+    if (!ctx || !out) return VPPGPU_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (kind == VPPGPU_ME_IMPL1) {
+        // MotionEstimatorImpl1(pSrc, pRef, w, h, macroBlkWidth, macroBlkHeight, motionRange): range in full
+        // pels; 16x16 or 8x8 blocks tiling the picture (the reference reads past its input otherwise)
+        if (width < 16 || height < block_h || (width % 16) != 0 || motion_range < 1) return VPPGPU_ERR_INVALID_ARG;
+        if (!((block_w == 16 && block_h == 16) || (block_w == 8 && block_h == 8)) || (height % block_h) != 0)
+            return VPPGPU_ERR_UNSUPPORTED;
+        if (width > 8192 || height > 8192 || motion_range > 32) return VPPGPU_ERR_UNSUPPORTED;
+        int rc = vppgpu::bind(ctx);
+        if (rc) return rc;
+        vppgpu_me* me = (vppgpu_me*)calloc(1, sizeof(vppgpu_me));
+        if (!me) return VPPGPU_ERR_OUT_OF_MEMORY;
+        me->ctx = ctx;
+        me->kind = kind;
+        me->W = width;
+        me->H = height;
+        me->bw = block_w;
+        me->bh = block_h;
+        me->cols = width / block_w;
+        me->rows = height / block_h;
+        me->nmb = me->cols * me->rows;
+        me->motion_range = motion_range;
+        me->rstride = width + 2 * vppgpu::PAD;
+        me->sweep_limit = 1;
+        const size_t npix = (size_t)width * height;
+        me->plane_size = (size_t)me->rstride * (height + 2 * vppgpu::PAD);
+        if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
+            (rc = dalloc(&me->d_src8, npix)) || (rc = dalloc(&me->d_refp, me->plane_size)) ||
+            (rc = dalloc(&me->d_hpel, 3 * me->plane_size)) || (rc = dalloc(&me->d_job, 1)) ||
+            (rc = dalloc(&me->changed, 1)) || (rc = dalloc(&me->d_out_mv, me->nmb)) ||
+            (rc = dalloc(&me->d_out_dist, me->nmb)) || (rc = dalloc(&me->d_out_avg, 1)) ||
+            (rc = dalloc(&me->d_incl, me->nmb)) || (rc = dalloc(&me->d_slice, me->nmb)) ||
+            (rc = dalloc(&me->ctrl, 1))) {
+            me_free(me);
+            return rc;
+        }
+        if (cudaMallocHost((void**)&me->h_ctrl, sizeof(vppgpu::MeCtrl)) != cudaSuccess) {
+            me_free(me);
+            return VPPGPU_ERR_OUT_OF_MEMORY;
+        }
+        *out = me;
+        return VPPGPU_OK;
+    }
+    if (block_w != 16 || block_h != 16) return VPPGPU_ERR_UNSUPPORTED;
+    return vppgpu_me_create(ctx, kind, width, height, motion_range, out);
+}
+
 int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motion_range, vppgpu_me** out)
 {
     if (!ctx || !out) return VPPGPU_ERR_INVALID_ARG;
     *out = nullptr;
+    if (kind == VPPGPU_ME_IMPL1) return vppgpu_me_create_blocks(ctx, kind, width, height, 16, 16, motion_range, out);
     // ranges below 4 (less than one full pel) are refused: the reference runs a
     // sub-pel-only search there, which nothing pins
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 4) return VPPGPU_ERR_INVALID_ARG;
@@ -328,6 +382,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     me->cols = width / 16;
     me->rows = height / 16;
     me->nmb = me->cols * me->rows;
+    me->bw = me->bh = 16;
     me->motion_range = motion_range;
     // Cross and UMHS default to quarter pel (…ImplCross.cpp:184, …ImplUMHS.cpp:259)
     me->mode = (kind == VPPGPU_ME_CROSS || searches_from_prediction(kind)) ? 0 : 1;
@@ -523,7 +578,8 @@ int vppgpu_me_set_mode(vppgpu_me* me, int mode)
     if (!me) return VPPGPU_ERR_INVALID_ARG;
     // SetMode(0) picks by picture area for the multi-resolution estimators (MultiresCross.cpp:501-513);
     // Cross and UMHS keep the mode as given (MotionEstimatorH264ImplCross.h:99, …ImplUMHS.h:107)
-    if (mode == 0 && me->kind != VPPGPU_ME_FULL && me->kind != VPPGPU_ME_CROSS && !searches_from_prediction(me->kind))
+    if (mode == 0 && me->kind != VPPGPU_ME_FULL && me->kind != VPPGPU_ME_CROSS && !searches_from_prediction(me->kind) &&
+        me->kind != VPPGPU_ME_IMPL1)
         mode = (me->W * me->H > 40000) ? 2 : 1;
     me->mode = mode;
     return VPPGPU_OK;
@@ -693,7 +749,7 @@ extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
     if (!me || sweeps < 0 || sweeps > (searches_from_prediction(me->kind) ? vppgpu::UMHS_SWEEPS : vppgpu::RELAX_SWEEPS))
         return VPPGPU_ERR_INVALID_ARG;
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS ||
-        me->kind == VPPGPU_ME_FULL_SAD)
+        me->kind == VPPGPU_ME_FULL_SAD || me->kind == VPPGPU_ME_IMPL1)
         return VPPGPU_ERR_UNSUPPORTED;
     if (sweeps == me->relax_sweeps) return VPPGPU_OK;
     int rc = vppgpu::bind(me->ctx);
@@ -743,7 +799,7 @@ extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src
     if (!me || !d_src || !d_ref || npairs < 1 || reps < 1) return VPPGPU_ERR_INVALID_ARG;
     for (int p = 0; p < npairs; p++)
         if (!d_src[p] || !d_ref[p]) return VPPGPU_ERR_INVALID_ARG;
-    if (me->kind == VPPGPU_ME_FULL_SAD) {  // one configuration: nothing to tune
+    if (me->kind == VPPGPU_ME_FULL_SAD || me->kind == VPPGPU_ME_IMPL1) {  // one configuration: nothing to tune
         if (chosen) *chosen = 0;
         return VPPGPU_OK;
     }

@@ -166,6 +166,9 @@ struct UmhsArgs {
 // The planes, `sweeps` relaxation sweeps, the dataflow pass (wave_grid CTAs of
 // 4 warps) and the outputs.
 int umhs_launch(vppgpu_ctx* ctx, const UmhsArgs& args, int wave_grid);
+// MotionEstimatorImpl1 (me_impl1.cu): the planes, then a warp per bw x bh block
+// (16x16 or 8x8) searching [-range, range-1]^2 full pels (range <= 32).
+int impl1_launch(vppgpu_ctx* ctx, const FullArgs& args, int bw, int bh, int range);
 // Once per device: the diagonal pass's shared-memory limit.
 int umhs_prepare();
 

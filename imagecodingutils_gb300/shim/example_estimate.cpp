@@ -6,7 +6,8 @@
 // program estimates with GpuMotionEstimatorH264ImplFull (or, by the optional
 // last argument, ...Multires, ...MultiresCross, ...MultiresCrossVer2 or
 // ...Cross, ...UMHS, ...FHS: "multires", "mrc", "mrc2", "cross", "sad", "umhs",
-// "fhs"; "mrc2lam" is Ver2's Lagrangian Estimate(long*, void*) with lambda 2.5;
+// "fhs"; "impl1" is MotionEstimatorImpl1 with 16x16 blocks and a +-16 pel range,
+// its half-pel char vectors widened to the output's shorts; "mrc2lam" is Ver2's Lagrangian Estimate(long*, void*) with lambda 2.5;
 // UMHS gets the previous frame's vectors from a first estimate of the same
 // pair, as a codec chains frames) exactly as a codec would
 // with the vpp class (constructor, Create, SetMode(0), Estimate, predictor
@@ -45,7 +46,7 @@ int main(int argc, char** argv)
 {
     if (argc != 6 && argc != 7) {
         fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin "
-                        "[full|multires|mrc|mrc2|mrc2lam|cross|sad|umhs|fhs]\n", argv[0]);
+                        "[full|multires|mrc|mrc2|mrc2lam|cross|sad|umhs|fhs|impl1]\n", argv[0]);
         return 2;
     }
     const std::string kind = argc == 7 ? argv[6] : "full";
@@ -61,6 +62,24 @@ int main(int argc, char** argv)
 
     RecordingPredictor pred(nmb);
     pred.dist.assign(nmb, -1);
+    if (kind == "impl1") {  // no predictor: the vectors, the average, then the rest of the output zero
+        GpuMotionEstimatorImpl1 me1(src.data(), ref.data(), w, h, 16, 16, 16);
+        if (!me1.Create()) return 4;
+        long a1 = 0;
+        SimpleMotionVectorList* l = (SimpleMotionVectorList*)me1.Estimate(&a1);
+        if (!l) return 5;
+        FILE* o1 = fopen(argv[5], "wb");
+        const signed char* p = (const signed char*)l->GetDataPtr();
+        for (int k = 0; k < l->GetLength(); k++) {
+            short v[2] = {(short)p[(size_t)k * l->GetPatternSize()], (short)p[(size_t)k * l->GetPatternSize() + 1]};
+            fwrite(v, 2, 2, o1);
+        }
+        long long a = a1;
+        fwrite(&a, 8, 1, o1);
+        fclose(o1);
+        delete[] incl;
+        return 0;
+    }
     std::vector<short> prev_mv;
     IMotionEstimator* me;
     if (kind == "multires")

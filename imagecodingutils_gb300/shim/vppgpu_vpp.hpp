@@ -28,6 +28,7 @@
 #include "IMotionVectorPredictor.h"
 #include "MacroBlockH264.h"
 #include "RGBtoYUV420Converter.h"
+#include "SimpleMotionVectorList.h"
 #include "VectorStructList.h"
 #include "YUV420toRGBConverter.h"
 #else
@@ -60,6 +61,27 @@ public:
     {
         (void)blk; (void)mvX; (void)mvY; (void)distortion;
     }
+};
+
+// vpp's SimpleMotionVectorList (VectorList(SIMPLE, 2, sizeof(char))): one
+// {char x, char y} pattern per block.
+class SimpleMotionVectorList {
+public:
+    SimpleMotionVectorList() : _length(0), _pData(NULL) {}
+    virtual ~SimpleMotionVectorList() { delete[] _pData; }
+    virtual int SetLength(int length) {
+        delete[] _pData;
+        _pData = new char[2 * (size_t)(length > 0 ? length : 1)];
+        _length = length;
+        return 1;
+    }
+    int GetPatternSize(void) { return 2; }
+    int GetLength(void) { return _length; }
+    void* GetDataPtr(void) { return _pData; }
+
+private:
+    int _length;
+    char* _pData;
 };
 
 // The SIMPLE2D layout of vpp's VectorStructList: one {short x, short y} per block.
@@ -530,6 +552,80 @@ public:
         _predDist = true;
     }
 #endif
+};
+
+// MotionEstimatorImpl1 (pSrc, pRef, w, h, macroBlkWidth, macroBlkHeight, motionRange)
+// (src/CodecUtils/MotionEstimatorImpl1.cpp:111-395): blocks 16x16 or 8x8, the range
+// in full pels; Estimate() returns a SimpleMotionVectorList of half-pel
+// (char x, char y) vectors, as the reference does.  No predictor.
+class GpuMotionEstimatorImpl1 : public IMotionEstimator {
+public:
+    GpuMotionEstimatorImpl1(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int macroBlkWidth,
+                            int macroBlkHeight, int motionRange)
+        : _pSrc(pSrc), _pRef(pRef), _w(imgWidth), _h(imgHeight), _bw(macroBlkWidth), _bh(macroBlkHeight),
+          _range(motionRange), _mode(0), _me(NULL), _list(NULL), _mv(NULL), _last(VPPGPU_OK)
+    {
+    }
+    virtual ~GpuMotionEstimatorImpl1() { Destroy(); }
+    virtual int Create(void)
+    {
+        Destroy();
+        vppgpu_ctx* ctx = vppgpu_vpp::context();
+        if (!ctx || vppgpu_me_create_blocks(ctx, VPPGPU_ME_IMPL1, _w, _h, _bw, _bh, _range, &_me) != VPPGPU_OK) {
+            _me = NULL;
+            return 0;
+        }
+        int n = 0;
+        vppgpu_me_num_mbs(_me, &n);
+        _list = new SimpleMotionVectorList();
+        _list->SetLength(n);
+        _mv = new short[2 * (size_t)(n > 0 ? n : 1)];
+        return 1;
+    }
+    virtual void Reset(void) {}
+    virtual int Ready(void) { return _me ? 1 : 0; }
+    virtual void SetMode(int mode) { _mode = mode; }
+    virtual int GetMode(void) { return _mode; }
+    virtual void* Estimate(const void* pSrc, const void* pRef, long* avgDistortion)
+    {
+        (void)pSrc;
+        (void)pRef;
+        return Estimate(avgDistortion);
+    }
+    virtual void* Estimate(long* avgDistortion)
+    {
+        if (!_me) return NULL;
+        long a = 0;
+        _last = vppgpu_me_estimate(_me, (const short*)_pSrc, (const short*)_pRef, NULL, NULL, _mv, NULL, &a);
+        if (avgDistortion) *avgDistortion = _last == VPPGPU_OK ? a : 0;
+        if (_last != VPPGPU_OK) return NULL;
+        char* p = (char*)_list->GetDataPtr();
+        const int step = _list->GetPatternSize();
+        for (int k = 0; k < _list->GetLength(); k++) {  // the half-pel vectors fit in chars (|v| <= 65)
+            p[(size_t)k * step] = (char)_mv[2 * k];
+            p[(size_t)k * step + 1] = (char)_mv[2 * k + 1];
+        }
+        return (void*)_list;
+    }
+    int LastStatus(void) const { return _last; }
+
+private:
+    void Destroy(void)
+    {
+        if (_me) vppgpu_me_destroy(_me);
+        _me = NULL;
+        delete _list;
+        _list = NULL;
+        delete[] _mv;
+        _mv = NULL;
+    }
+    const void* _pSrc;
+    const void* _pRef;
+    int _w, _h, _bw, _bh, _range, _mode;
+    vppgpu_me* _me;
+    SimpleMotionVectorList* _list;
+    short* _mv;
+    int _last;
 };
 
 // ---------------------------------------------------------------------------

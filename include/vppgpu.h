@@ -93,6 +93,16 @@ int vppgpu_ctx_launch_count(vppgpu_ctx* ctx, unsigned long long* count);
  * early without an improvement), this macroblock's samples are used; such
  * macroblocks are counted in vppgpu_me_last_stats()[7]. */
 #define VPPGPU_ME_FHS               8
+/* MotionEstimatorImpl1 (src/CodecUtils/MotionEstimatorImpl1.cpp:275-395): the
+ * H.263-style full search of [-motion_range, motion_range-1]^2 FULL pels by SSD,
+ * the OverlayMem2Dv2::HalfRead half-pel refinement and the weighted choice
+ * between the winner and the zero vector; no predictor.  Vectors in HALF pels
+ * (the reference stores them as chars in a SimpleMotionVectorList), one per
+ * block of the size given to vppgpu_me_create_blocks (16x16 through
+ * vppgpu_me_create); avg_distortion over every block.  1 <= motion_range <= 32;
+ * heights must be a multiple of the block height (the reference reads past
+ * its input for a partial row). */
+#define VPPGPU_ME_IMPL1             9
 
 typedef struct vppgpu_me vppgpu_me;
 
@@ -106,6 +116,11 @@ typedef struct vppgpu_me vppgpu_me;
  * VPPGPU_ERR_INVALID_ARG. */
 int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motion_range,
                      vppgpu_me** out);
+/* The same for estimators whose constructor takes a block size: MotionEstimatorImpl1's
+ * (pSrc, pRef, w, h, macroBlkWidth, macroBlkHeight, motionRange) (MotionEstimatorImpl1.cpp:111-135),
+ * blocks 16x16 or 8x8.  Every other kind accepts 16x16 only. */
+int vppgpu_me_create_blocks(vppgpu_ctx* ctx, int kind, int width, int height, int block_w, int block_h,
+                            int motion_range, vppgpu_me** out);
 int vppgpu_me_destroy(vppgpu_me* me);
 /* IMotionEstimator::SetMode / GetMode (include/CodecUtils/IMotionEstimator.h:80-81). */
 int vppgpu_me_set_mode(vppgpu_me* me, int mode);
