@@ -61,6 +61,7 @@ class Oracle:
         L.vo_me_multires_cross_v2_lambda.argtypes = [_P, _P, _I, _I, _I, _I, C.c_double, _P, _P, _P, _P,
                                                      C.POINTER(_L)]
         L.vo_me_umhs.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, C.POINTER(_L)]
+        L.vo_me_impl2.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, C.POINTER(_L)]
         L.vo_me_impl1.argtypes = [_P, _P, _I, _I, _I, _I, _I, _P, _P, C.POINTER(_L)]
         L.vo_me_fhs.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), C.POINTER(_I)]
         L.vo_mc_compensate.argtypes = [_P, _I, _I, _I, _P]
@@ -192,6 +193,20 @@ class Oracle:
         if rc:
             raise ValueError(f"vo_me_fhs rc={rc}")
         return (mv, dist, avg.value, stale.value) if with_stale else (mv, dist, avg.value)
+
+    def me_impl2(self, src, ref, range_, mode=1):
+        """MotionEstimatorImpl2: half-pel vectors, per-block distortion, the average."""
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        n = (w // 16) * (h // 16)
+        mv = np.zeros((n, 2), np.int16)
+        dist = np.zeros(n, np.int32)
+        avg = _L(0)
+        rc = self.lib.vo_me_impl2(_ptr(src), _ptr(ref), w, h, range_, mode, _ptr(mv), _ptr(dist), C.byref(avg))
+        if rc:
+            raise ValueError(f"vo_me_impl2 rc={rc}")
+        return mv, dist, avg.value
 
     def me_impl1(self, src, ref, range_, bw=16, bh=16):
         """MotionEstimatorImpl1: half-pel vectors, per-block distortion, the average."""
@@ -368,6 +383,7 @@ class Reference:
         L.ref_me_estimate.argtypes = [_I, _P, _P, _I, _I, _I, _I, _P, _P, _I, _P, C.POINTER(_L)]
         L.ref_me_full_sad.argtypes = [_P, _P, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.ref_me_umhs.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P, C.POINTER(_L)]
+        L.ref_me_impl2.argtypes = [_P, _P, _I, _I, _I, _I, _P, C.POINTER(_L)]
         L.ref_me_impl1.argtypes = [_P, _P, _I, _I, _I, _I, _I, _P, C.POINTER(_L)]
         L.ref_me_fhs.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.ref_fwd_transform.argtypes = [_I, _P, _I, _I, _I, _I]
@@ -436,6 +452,19 @@ class Reference:
         if rc:
             raise ValueError(f"ref_me_umhs rc={rc}")
         return mv, dist, avg.value
+
+    def me_impl2(self, src, ref, range_, mode=1):
+        """MotionEstimatorImpl2 after SetMode(mode): half-pel vectors and avgDistortion."""
+        h, w = src.shape
+        src = np.ascontiguousarray(src, dtype=np.int16)
+        ref = np.ascontiguousarray(ref, dtype=np.int16)
+        n = (w // 16) * (h // 16)
+        mv = np.zeros((n, 2), np.int16)
+        avg = _L(0)
+        rc = self.lib.ref_me_impl2(_ptr(src), _ptr(ref), w, h, range_, mode, _ptr(mv), C.byref(avg))
+        if rc:
+            raise ValueError(f"ref_me_impl2 rc={rc}")
+        return mv, avg.value
 
     def me_impl1(self, src, ref, range_, bw=16, bh=16):
         """MotionEstimatorImpl1: half-pel vectors and avgDistortion."""

@@ -22,6 +22,7 @@
 #include "MotionEstimatorH264ImplUMHS.h"
 #include "MotionEstimatorH264ImplFHS.h"
 #include "MotionEstimatorImpl1.h"
+#include "MotionEstimatorImpl2.h"
 #include "SimpleMotionVectorList.h"
 #include "MotionEstimatorH263ImplMultiresCross.h"
 #include "VectorStructList.h"
@@ -290,6 +291,24 @@ int ref_me_impl1(const short* src, const short* ref, int w, int h, int bw, int b
 {
     MotionEstimatorImpl1 me(src, ref, w, h, bw, bh, range);
     if (!me.Create()) return -2;
+    long avg = 0;
+    SimpleMotionVectorList* l = (SimpleMotionVectorList*)me.Estimate(&avg);
+    const signed char* p = (const signed char*)l->GetDataPtr();
+    const int step = l->GetPatternSize(), n = l->GetLength();
+    for (int i = 0; i < n; i++) {
+        mv_out[2 * i] = p[(size_t)i * step];
+        mv_out[2 * i + 1] = p[(size_t)i * step + 1];
+    }
+    if (avg_out) *avg_out = avg;
+    return 0;
+}
+
+/* MotionEstimatorImpl2 (pSrc, pRef, w, h, 16, 16, motionRange) after SetMode(mode). */
+int ref_me_impl2(const short* src, const short* ref, int w, int h, int range, int mode, short* mv_out, long* avg_out)
+{
+    MotionEstimatorImpl2 me(src, ref, w, h, 16, 16, range);
+    if (!me.Create()) return -2;
+    me.SetMode(mode);
     long avg = 0;
     SimpleMotionVectorList* l = (SimpleMotionVectorList*)me.Estimate(&avg);
     const signed char* p = (const signed char*)l->GetDataPtr();

@@ -88,6 +88,14 @@ int vo_me_fhs(const short* src, const short* ref, int w, int h, int motion_range
 int vo_me_impl1(const short* src, const short* ref, int w, int h, int bw, int bh, int range, short* mv_out,
                 int* mb_dist, long* avg_dist);
 
+/* MotionEstimatorImpl2::Estimate (src/CodecUtils/MotionEstimatorImpl2.cpp:505-826): 16x16
+ * blocks, range in full pels (4..63); mode 2 (SetMode(0) above 40000 pixels) a full
+ * SAD search at level 2 then +-2 at level 1, else a full search at level 1;
+ * +-2 at level 0, ties towards the origin; HalfRead half pel; the weighted
+ * zero-vector choice; half-pel char vectors, per-block distortion, the average. */
+int vo_me_impl2(const short* src, const short* ref, int w, int h, int range, int mode, short* mv_out, int* mb_dist,
+                long* avg_dist);
+
 int vo_me_full(const short* src, const short* ref, int w, int h, int motion_range,
                const unsigned char* dist_incl, const int* slice,
                short* mv_out, int* mb_dist, long* avg_dist);

@@ -48,6 +48,9 @@ inputs and stores inputs and outputs:
                   refinement and the weighted zero-vector choice): pan, shift and
                   part-noise pairs, 16x16 and 8x8 blocks, ranges 7..32 pels;
                   half-pel vectors and avgDistortion
+* me_impl2.npz    MotionEstimatorImpl2 (the SAD pyramid): pan, shift and part-noise
+                  pairs, ranges 8..32 pels, modes 1 and 2; half-pel vectors and
+                  avgDistortion
 * me_1080p.npz    the headline size: Full, MultiresCross / Ver2 / Multires
                   (modes 0, 1, 2), Cross and the integer-pel SAD stage on three
                   frame pairs of the 1920x1080 benchmark sequence at
@@ -55,7 +58,7 @@ inputs and stores inputs and outputs:
                   SHA-256)
 
 Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
-names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc me_umhs me_fhs me_impl1 mc
+names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc me_umhs me_fhs me_impl1 me_impl2 mc
 transform dc yuv2rgb colour, default all)
 """
 from __future__ import annotations
@@ -358,6 +361,29 @@ def impl1_fixtures(ref: oracle.Reference) -> dict:
     return out
 
 
+IMPL2_CASES = [  # (name, w, h, range in pels, mode, seed, generator)
+    ("qcif_r16_m1", 176, 144, 16, 1, 141, "pan"),
+    ("qcif_r16_m2", 176, 144, 16, 2, 142, "noisy"),
+    ("cif_r15_m2", 352, 288, 15, 2, 143, "shift"),
+    ("small_r8_m1", 64, 48, 8, 1, 144, "noisy"),
+    ("cif_r32_m2", 352, 288, 32, 2, 145, "pan"),
+    ("wide_r20_m1", 208, 112, 20, 1, 146, "shift"),
+]
+
+
+def impl2_fixtures(ref: oracle.Reference) -> dict:
+    out = {}
+    for name, w, h, rng, mode, seed, gen in IMPL2_CASES:
+        fr = umhs_frames(seed, w, h, gen)
+        mv, avg = ref.me_impl2(fr[1], fr[0], rng, mode)
+        out[f"{name}_src"] = fr[1].astype(np.uint8)
+        out[f"{name}_ref"] = fr[0].astype(np.uint8)
+        out[f"{name}_meta"] = np.array([w, h, rng, mode], np.int32)
+        out[f"{name}_mv"] = mv
+        out[f"{name}_avg"] = np.array([avg], np.int64)
+    return out
+
+
 MC_CASES = [("qcif_r16", 176, 144, 16, 61), ("cif_r32", 352, 288, 32, 62), ("small_r8", 64, 48, 8, 63)]
 
 
@@ -546,7 +572,7 @@ def main() -> None:
               "me_mrc2_lambda": mrc2_lambda_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "me_cross": lambda r: mrc2_fixtures(r, "cross"),
               "me_h263mrc": lambda r: mrc_fixtures(r, "h263_multires_cross", H263_CASES),
-              "me_umhs": umhs_fixtures, "me_fhs": fhs_fixtures, "me_impl1": impl1_fixtures,
+              "me_umhs": umhs_fixtures, "me_fhs": fhs_fixtures, "me_impl1": impl1_fixtures, "me_impl2": impl2_fixtures,
               "mc": mc_fixtures,
               "transform": transform_fixtures, "dc": dc_fixtures, "yuv2rgb": yuv2rgb_fixtures,
               "colour": colour_fixtures}

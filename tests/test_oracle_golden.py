@@ -596,3 +596,28 @@ def test_me_impl1_against_compiled_reference(orc, seed, w, h, bw, bh, rng, gen):
     mv, _, avg = orc.me_impl1(fr[1], fr[0], rng, bw, bh)
     np.testing.assert_array_equal(mv, mv_r)
     assert avg == avg_r
+
+
+IMPL2_CASES = ["qcif_r16_m1", "qcif_r16_m2", "cif_r15_m2", "small_r8_m1", "cif_r32_m2", "wide_r20_m1"]
+
+
+@pytest.mark.parametrize("case", IMPL2_CASES)
+def test_me_impl2_matches_reference(orc, golden, case):
+    """MotionEstimatorImpl2: half-pel vectors and avgDistortion."""
+    g = golden("me_impl2.npz")
+    w, h, rng, mode = (int(v) for v in g[f"{case}_meta"])
+    mv, dist, avg = orc.me_impl2(g[f"{case}_src"].astype(np.int16), g[f"{case}_ref"].astype(np.int16), rng, mode)
+    np.testing.assert_array_equal(mv, g[f"{case}_mv"])
+    assert avg == int(g[f"{case}_avg"][0])
+
+
+@ref_available
+@pytest.mark.parametrize("seed,w,h,rng,mode,gen", [(151, 176, 144, 12, 1, "noisy"), (152, 352, 288, 24, 0, "pan"),
+                                                  (153, 128, 96, 6, 2, "shift")])
+def test_me_impl2_against_compiled_reference(orc, seed, w, h, rng, mode, gen):
+    from tests.golden.make_golden import umhs_frames
+    fr = umhs_frames(seed, w, h, gen)
+    mv_r, avg_r = oracle_mod.Reference().me_impl2(fr[1], fr[0], rng, mode)
+    mv, _, avg = orc.me_impl2(fr[1], fr[0], rng, mode)
+    np.testing.assert_array_equal(mv, mv_r)
+    assert avg == avg_r
