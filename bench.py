@@ -413,11 +413,12 @@ MULTIRES = {  # kind -> (class name, oracle method)
     "umhs": ("MotionEstimatorH264ImplUMHS", "me_umhs"),
     "fhs": ("MotionEstimatorH264ImplFHS", "me_fhs"),
     "impl1": ("MotionEstimatorImpl1", "me_impl1"),
+    "impl2": ("MotionEstimatorImpl2", "me_impl2"),
 }
 MULTIRES_CODE = {"multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4,
-                 "h263_multires_cross": 5, "full_sad": 6, "umhs": 7, "fhs": 8, "impl1": 9}  # VPPGPU_ME_*
+                 "h263_multires_cross": 5, "full_sad": 6, "umhs": 7, "fhs": 8, "impl1": 9, "impl2": 10}  # VPPGPU_ME_*
 # motion ranges are in quarter pels, the H.263 estimator's in half pels: the same +-32 pels
-MULTIRES_RANGE = {"h263_multires_cross": MOTION_RANGE // 2, "impl1": 16}  # Impl1's range is in full pels (+-16)
+MULTIRES_RANGE = {"h263_multires_cross": MOTION_RANGE // 2, "impl1": 16, "impl2": 16}  # Impl1/2: full pels
 
 
 TUNE_PAIRS = 8
@@ -445,7 +446,7 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
     code = MULTIRES_CODE[kind]
     mr = MULTIRES_RANGE.get(kind, MOTION_RANGE)
     hk = H
-    if kind == "impl1":  # blocks must tile the picture: the 1072 full macroblock rows, the same 8040 blocks
+    if kind in ("impl1", "impl2"):  # blocks must tile the picture: the 1072 full macroblock rows, 8040 blocks
         hk = (H // 16) * 16
         frames = [np.ascontiguousarray(f[:hk]) for f in frames]
     h = C.c_void_p()
@@ -476,8 +477,8 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
     ms = e0.elapsed_time(e1) / steps
     out = {"value": NMB / (ms * 1e-3), "unit": UNIT, "ms_per_frame": ms, "mode": mode.value, "autotune": tuning,
            "workload": f"{cls} plain per-frame, {W}x{hk}, motionRange {mr}"
-                       + (" full pels, 16x16 blocks" if kind == "impl1" else "")}
-    if kind not in ("multires_cross", "h263_multires_cross", "full_sad", "impl1"):
+                       + (" full pels, 16x16 blocks" if kind in ("impl1", "impl2") else "")}
+    if kind not in ("multires_cross", "h263_multires_cross", "full_sad", "impl1", "impl2"):
         # per-frame device time and how each frame's predictions were decided
         per, exact = [], 0
         for t in range(NFRAMES - 1):
@@ -504,6 +505,8 @@ def run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, dev, frames, with
                 return orc.me_full_intpel(frames[i + 1], frames[i], mr, metric=1)
             if kind == "impl1":
                 return orc.me_impl1(frames[i + 1], frames[i], mr)
+            if kind == "impl2":
+                return orc.me_impl2(frames[i + 1], frames[i], mr, mode=mode.value)
             return getattr(orc, ofn)(frames[i + 1], frames[i], mr, mode=mode.value)
 
         mv_o = port(0)[0]
@@ -939,6 +942,8 @@ def main():
                                  kind="fhs")
         impl1 = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames,
                                    not args.no_cpu, kind="impl1")
+        impl2 = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames,
+                                   not args.no_cpu, kind="impl2")
         pk, pk_kind = peaks()
         hbm_rows = run_hbm_paths(torch, _lib, L, ctx, stream, f"cuda:{local}", pk)
         line = {
@@ -962,7 +967,7 @@ def main():
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
             "serving": serving,
             "multires": mr, "multires_cross": mrc, "multires_cross_v2": mrc2, "cross": cr,
-            "h263_multires_cross": h263, "full_sad": sad, "umhs": umhs, "fhs": fhs, "impl1": impl1, **hbm_rows,
+            "h263_multires_cross": h263, "full_sad": sad, "umhs": umhs, "fhs": fhs, "impl1": impl1, "impl2": impl2, **hbm_rows,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

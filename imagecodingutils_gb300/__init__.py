@@ -28,7 +28,7 @@ from ._lib import VppGpuError, check, load
 
 __all__ = [
     "Context", "get_context", "MotionEstimatorH264ImplFull", "MotionEstimatorH264ImplMultires",
-    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross", "MotionEstimatorH264ImplFullSad", "MotionEstimatorH264ImplUMHS", "MotionEstimatorH264ImplFHS", "MotionEstimatorImpl1",
+    "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross", "MotionEstimatorH264ImplFullSad", "MotionEstimatorH264ImplUMHS", "MotionEstimatorH264ImplFHS", "MotionEstimatorImpl1", "MotionEstimatorImpl2",
     "MotionEstimatorH263ImplMultiresCross", "MotionEstimatorBatch",
     "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
     "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1", "FastForwardDC4x4ITImpl1",
@@ -337,6 +337,22 @@ class MotionEstimatorImpl1(_MotionEstimatorBase):
 
     def num_mbs(self) -> int:
         return (self._w // self._bw) * (self._h // self._bh)
+
+
+class MotionEstimatorImpl2(MotionEstimatorImpl1):
+    """GPU MotionEstimatorImpl2 (src/CodecUtils/MotionEstimatorImpl2.cpp): the SAD
+    pyramid, 16x16 blocks, motionRange in full pels (4..32); SetMode(1) (the
+    default) two levels, 2 three, 0 picks by area.  Half-pel vectors and
+    avgDistortion over every block; no predictor."""
+
+    KIND = _lib.ME_IMPL2
+    DEFAULT_MODE = 1
+
+    def GetMode(self) -> int:
+        m = C.c_int(self._mode)
+        if self._h_me:
+            load().vppgpu_me_get_mode(self._h_me, C.byref(m))
+        return m.value
 
 
 class MotionEstimatorH264ImplMultiresCross(_MotionEstimatorBase):

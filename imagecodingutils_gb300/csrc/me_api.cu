@@ -248,6 +248,8 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
         return vppgpu::umhs_launch(ctx, umhs_args(me), me->wave_grid);
     }
     if (me->kind == VPPGPU_ME_IMPL1) return vppgpu::impl1_launch(ctx, full_args(me, 0.0), me->bw, me->bh, me->motion_range);
+    if (me->kind == VPPGPU_ME_IMPL2)
+        return vppgpu::impl2_launch(ctx, full_args(me, 0.0), me->d_mrc, me->motion_range, me->mode);
     if (me->kind == VPPGPU_ME_FULL_SAD) {
         // the integer-pel stage only: no sub-pel, no prediction check, no GetBestVector
         vppgpu::FullArgs a = full_args(me, 0.0);
@@ -312,13 +314,17 @@ int vppgpu_me_create_blocks(vppgpu_ctx* ctx, int kind, int width, int height, in
 {
     if (!ctx || !out) return VPPGPU_ERR_INVALID_ARG;
     *out = nullptr;
-    if (kind == VPPGPU_ME_IMPL1) {
-        // MotionEstimatorImpl1(pSrc, pRef, w, h, macroBlkWidth, macroBlkHeight, motionRange): range in full
-        // pels; 16x16 or 8x8 blocks tiling the picture (the reference reads past its input otherwise)
+    if (kind == VPPGPU_ME_IMPL1 || kind == VPPGPU_ME_IMPL2) {
+        // MotionEstimatorImpl1 / Impl2 (pSrc, pRef, w, h, macroBlkWidth, macroBlkHeight, motionRange): range in
+        // full pels; blocks tiling the picture (the reference reads past its input otherwise): 16x16 or 8x8
+        // for Impl1, 16x16 for Impl2 (its distortions are hard-wired to 16x16 / 8x8 / 4x4 levels)
         if (width < 16 || height < block_h || (width % 16) != 0 || motion_range < 1) return VPPGPU_ERR_INVALID_ARG;
-        if (!((block_w == 16 && block_h == 16) || (block_w == 8 && block_h == 8)) || (height % block_h) != 0)
-            return VPPGPU_ERR_UNSUPPORTED;
+        const bool blocks_ok = kind == VPPGPU_ME_IMPL1
+                                   ? ((block_w == 16 && block_h == 16) || (block_w == 8 && block_h == 8))
+                                   : (block_w == 16 && block_h == 16);
+        if (!blocks_ok || (height % block_h) != 0) return VPPGPU_ERR_UNSUPPORTED;
         if (width > 8192 || height > 8192 || motion_range > 32) return VPPGPU_ERR_UNSUPPORTED;
+        if (kind == VPPGPU_ME_IMPL2 && motion_range < 4) return VPPGPU_ERR_UNSUPPORTED;
         int rc = vppgpu::bind(ctx);
         if (rc) return rc;
         vppgpu_me* me = (vppgpu_me*)calloc(1, sizeof(vppgpu_me));
@@ -333,6 +339,7 @@ int vppgpu_me_create_blocks(vppgpu_ctx* ctx, int kind, int width, int height, in
         me->rows = height / block_h;
         me->nmb = me->cols * me->rows;
         me->motion_range = motion_range;
+        me->mode = 1;  // Impl2's default, MotionEstimatorImpl2.cpp:120
         me->rstride = width + 2 * vppgpu::PAD;
         me->sweep_limit = 1;
         const size_t npix = (size_t)width * height;
@@ -343,7 +350,8 @@ int vppgpu_me_create_blocks(vppgpu_ctx* ctx, int kind, int width, int height, in
             (rc = dalloc(&me->changed, 1)) || (rc = dalloc(&me->d_out_mv, me->nmb)) ||
             (rc = dalloc(&me->d_out_dist, me->nmb)) || (rc = dalloc(&me->d_out_avg, 1)) ||
             (rc = dalloc(&me->d_incl, me->nmb)) || (rc = dalloc(&me->d_slice, me->nmb)) ||
-            (rc = dalloc(&me->ctrl, 1))) {
+            (rc = dalloc(&me->ctrl, 1)) ||
+            (kind == VPPGPU_ME_IMPL2 && (rc = dalloc(&me->d_mrc, vppgpu::impl2_scratch_bytes(width, height))))) {
             me_free(me);
             return rc;
         }
@@ -362,7 +370,8 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
 {
     if (!ctx || !out) return VPPGPU_ERR_INVALID_ARG;
     *out = nullptr;
-    if (kind == VPPGPU_ME_IMPL1) return vppgpu_me_create_blocks(ctx, kind, width, height, 16, 16, motion_range, out);
+    if (kind == VPPGPU_ME_IMPL1 || kind == VPPGPU_ME_IMPL2)
+        return vppgpu_me_create_blocks(ctx, kind, width, height, 16, 16, motion_range, out);
     // ranges below 4 (less than one full pel) are refused: the reference runs a
     // sub-pel-only search there, which nothing pins
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 4) return VPPGPU_ERR_INVALID_ARG;
@@ -749,7 +758,7 @@ extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
     if (!me || sweeps < 0 || sweeps > (searches_from_prediction(me->kind) ? vppgpu::UMHS_SWEEPS : vppgpu::RELAX_SWEEPS))
         return VPPGPU_ERR_INVALID_ARG;
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS ||
-        me->kind == VPPGPU_ME_FULL_SAD || me->kind == VPPGPU_ME_IMPL1)
+        me->kind == VPPGPU_ME_FULL_SAD || me->kind == VPPGPU_ME_IMPL1 || me->kind == VPPGPU_ME_IMPL2)
         return VPPGPU_ERR_UNSUPPORTED;
     if (sweeps == me->relax_sweeps) return VPPGPU_OK;
     int rc = vppgpu::bind(me->ctx);
@@ -799,7 +808,8 @@ extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src
     if (!me || !d_src || !d_ref || npairs < 1 || reps < 1) return VPPGPU_ERR_INVALID_ARG;
     for (int p = 0; p < npairs; p++)
         if (!d_src[p] || !d_ref[p]) return VPPGPU_ERR_INVALID_ARG;
-    if (me->kind == VPPGPU_ME_FULL_SAD || me->kind == VPPGPU_ME_IMPL1) {  // one configuration: nothing to tune
+    if (me->kind == VPPGPU_ME_FULL_SAD || me->kind == VPPGPU_ME_IMPL1 ||
+        me->kind == VPPGPU_ME_IMPL2) {  // one configuration: nothing to tune
         if (chosen) *chosen = 0;
         return VPPGPU_OK;
     }

@@ -169,6 +169,11 @@ int umhs_launch(vppgpu_ctx* ctx, const UmhsArgs& args, int wave_grid);
 // MotionEstimatorImpl1 (me_impl1.cu): the planes, then a warp per bw x bh block
 // (16x16 or 8x8) searching [-range, range-1]^2 full pels (range <= 32).
 int impl1_launch(vppgpu_ctx* ctx, const FullArgs& args, int bw, int bh, int range);
+// MotionEstimatorImpl2 (me_impl.cu): the planes, the level-1 / level-2 planes in
+// `scratch` (impl2_scratch_bytes), then a warp per 16x16 block; mode 1 two
+// levels, 2 three; range in full pels (4..32).
+size_t impl2_scratch_bytes(int W, int H);
+int impl2_launch(vppgpu_ctx* ctx, const FullArgs& args, unsigned char* scratch, int range, int mode);
 // Once per device: the diagonal pass's shared-memory limit.
 int umhs_prepare();
 

@@ -6,7 +6,7 @@
 // program estimates with GpuMotionEstimatorH264ImplFull (or, by the optional
 // last argument, ...Multires, ...MultiresCross, ...MultiresCrossVer2 or
 // ...Cross, ...UMHS, ...FHS: "multires", "mrc", "mrc2", "cross", "sad", "umhs",
-// "fhs"; "impl1" is MotionEstimatorImpl1 with 16x16 blocks and a +-16 pel range,
+// "fhs"; "impl1" / "impl2" are MotionEstimatorImpl1 / Impl2 with 16x16 blocks, a +-16 pel range and SetMode(0),
 // its half-pel char vectors widened to the output's shorts; "mrc2lam" is Ver2's Lagrangian Estimate(long*, void*) with lambda 2.5;
 // UMHS gets the previous frame's vectors from a first estimate of the same
 // pair, as a codec chains frames) exactly as a codec would
@@ -46,7 +46,7 @@ int main(int argc, char** argv)
 {
     if (argc != 6 && argc != 7) {
         fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin "
-                        "[full|multires|mrc|mrc2|mrc2lam|cross|sad|umhs|fhs|impl1]\n", argv[0]);
+                        "[full|multires|mrc|mrc2|mrc2lam|cross|sad|umhs|fhs|impl1|impl2]\n", argv[0]);
         return 2;
     }
     const std::string kind = argc == 7 ? argv[6] : "full";
@@ -62,11 +62,14 @@ int main(int argc, char** argv)
 
     RecordingPredictor pred(nmb);
     pred.dist.assign(nmb, -1);
-    if (kind == "impl1") {  // no predictor: the vectors, the average, then the rest of the output zero
-        GpuMotionEstimatorImpl1 me1(src.data(), ref.data(), w, h, 16, 16, 16);
-        if (!me1.Create()) return 4;
+    if (kind == "impl1" || kind == "impl2") {  // no predictor: the vectors and the average only
+        GpuMotionEstimatorImpl1* me1 = kind == "impl1"
+                                           ? new GpuMotionEstimatorImpl1(src.data(), ref.data(), w, h, 16, 16, 16)
+                                           : new GpuMotionEstimatorImpl2(src.data(), ref.data(), w, h, 16, 16, 16);
+        if (!me1->Create()) return 4;
+        me1->SetMode(0);
         long a1 = 0;
-        SimpleMotionVectorList* l = (SimpleMotionVectorList*)me1.Estimate(&a1);
+        SimpleMotionVectorList* l = (SimpleMotionVectorList*)me1->Estimate(&a1);
         if (!l) return 5;
         FILE* o1 = fopen(argv[5], "wb");
         const signed char* p = (const signed char*)l->GetDataPtr();
@@ -77,6 +80,7 @@ int main(int argc, char** argv)
         long long a = a1;
         fwrite(&a, 8, 1, o1);
         fclose(o1);
+        delete me1;
         delete[] incl;
         return 0;
     }

@@ -562,8 +562,8 @@ class GpuMotionEstimatorImpl1 : public IMotionEstimator {
 public:
     GpuMotionEstimatorImpl1(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int macroBlkWidth,
                             int macroBlkHeight, int motionRange)
-        : _pSrc(pSrc), _pRef(pRef), _w(imgWidth), _h(imgHeight), _bw(macroBlkWidth), _bh(macroBlkHeight),
-          _range(motionRange), _mode(0), _me(NULL), _list(NULL), _mv(NULL), _last(VPPGPU_OK)
+        : _kind(VPPGPU_ME_IMPL1), _pSrc(pSrc), _pRef(pRef), _w(imgWidth), _h(imgHeight), _bw(macroBlkWidth),
+          _bh(macroBlkHeight), _range(motionRange), _mode(0), _me(NULL), _list(NULL), _mv(NULL), _last(VPPGPU_OK)
     {
     }
     virtual ~GpuMotionEstimatorImpl1() { Destroy(); }
@@ -571,10 +571,12 @@ public:
     {
         Destroy();
         vppgpu_ctx* ctx = vppgpu_vpp::context();
-        if (!ctx || vppgpu_me_create_blocks(ctx, VPPGPU_ME_IMPL1, _w, _h, _bw, _bh, _range, &_me) != VPPGPU_OK) {
+        if (!ctx || vppgpu_me_create_blocks(ctx, _kind, _w, _h, _bw, _bh, _range, &_me) != VPPGPU_OK) {
             _me = NULL;
             return 0;
         }
+        vppgpu_me_set_mode(_me, _mode);
+        vppgpu_me_get_mode(_me, &_mode);
         int n = 0;
         vppgpu_me_num_mbs(_me, &n);
         _list = new SimpleMotionVectorList();
@@ -584,7 +586,14 @@ public:
     }
     virtual void Reset(void) {}
     virtual int Ready(void) { return _me ? 1 : 0; }
-    virtual void SetMode(int mode) { _mode = mode; }
+    virtual void SetMode(int mode)
+    {
+        _mode = mode;
+        if (_me) {  // Impl2 picks its levels by area for mode 0, as the reference does
+            vppgpu_me_set_mode(_me, mode);
+            vppgpu_me_get_mode(_me, &_mode);
+        }
+    }
     virtual int GetMode(void) { return _mode; }
     virtual void* Estimate(const void* pSrc, const void* pRef, long* avgDistortion)
     {
@@ -609,6 +618,14 @@ public:
     }
     int LastStatus(void) const { return _last; }
 
+protected:
+    GpuMotionEstimatorImpl1(int kind, int mode, const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                            int macroBlkWidth, int macroBlkHeight, int motionRange)
+        : _kind(kind), _pSrc(pSrc), _pRef(pRef), _w(imgWidth), _h(imgHeight), _bw(macroBlkWidth),
+          _bh(macroBlkHeight), _range(motionRange), _mode(mode), _me(NULL), _list(NULL), _mv(NULL), _last(VPPGPU_OK)
+    {
+    }
+
 private:
     void Destroy(void)
     {
@@ -619,6 +636,7 @@ private:
         delete[] _mv;
         _mv = NULL;
     }
+    int _kind;
     const void* _pSrc;
     const void* _pRef;
     int _w, _h, _bw, _bh, _range, _mode;
@@ -626,6 +644,19 @@ private:
     SimpleMotionVectorList* _list;
     short* _mv;
     int _last;
+};
+
+// MotionEstimatorImpl2 (src/CodecUtils/MotionEstimatorImpl2.cpp:111-826): the SAD
+// pyramid, 16x16 blocks, the range in full pels; SetMode(1) (the default) two
+// levels, 2 three, 0 by area; the same SimpleMotionVectorList output.
+class GpuMotionEstimatorImpl2 : public GpuMotionEstimatorImpl1 {
+public:
+    GpuMotionEstimatorImpl2(const void* pSrc, const void* pRef, int imgWidth, int imgHeight, int macroBlkWidth,
+                            int macroBlkHeight, int motionRange)
+        : GpuMotionEstimatorImpl1(VPPGPU_ME_IMPL2, 1, pSrc, pRef, imgWidth, imgHeight, macroBlkWidth, macroBlkHeight,
+                                  motionRange)
+    {
+    }
 };
 
 // ---------------------------------------------------------------------------

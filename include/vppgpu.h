@@ -103,6 +103,13 @@ int vppgpu_ctx_launch_count(vppgpu_ctx* ctx, unsigned long long* count);
  * heights must be a multiple of the block height (the reference reads past
  * its input for a partial row). */
 #define VPPGPU_ME_IMPL1             9
+/* MotionEstimatorImpl2 (src/CodecUtils/MotionEstimatorImpl2.cpp:505-826): a SAD
+ * pyramid for 16x16 blocks, motion_range in FULL pels (4..32): SetMode(2) (or 0
+ * above 40000 pixels) a full search at level 2 then +-2 at level 1, SetMode(1)
+ * (the default) a full search at level 1; +-2 at level 0, ties towards the
+ * origin; HalfRead half pel; the weighted zero-vector choice.  Vectors in HALF
+ * pels, as for VPPGPU_ME_IMPL1. */
+#define VPPGPU_ME_IMPL2             10
 
 typedef struct vppgpu_me vppgpu_me;
 
@@ -118,7 +125,8 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
                      vppgpu_me** out);
 /* The same for estimators whose constructor takes a block size: MotionEstimatorImpl1's
  * (pSrc, pRef, w, h, macroBlkWidth, macroBlkHeight, motionRange) (MotionEstimatorImpl1.cpp:111-135),
- * blocks 16x16 or 8x8.  Every other kind accepts 16x16 only. */
+ * blocks 16x16 or 8x8, and MotionEstimatorImpl2's (MotionEstimatorImpl2.cpp:111-181), 16x16.  Every
+ * other kind accepts 16x16 only. */
 int vppgpu_me_create_blocks(vppgpu_ctx* ctx, int kind, int width, int height, int block_w, int block_h,
                             int motion_range, vppgpu_me** out);
 int vppgpu_me_destroy(vppgpu_me* me);

@@ -55,3 +55,35 @@ def test_limits(vpp, ctx):
     assert L.vppgpu_me_create_blocks(ctx.handle, 0, 64, 48, 8, 8, 64, C.byref(h)) == -6    # other kinds: 16x16
     mv, _, _ = estimate(vpp, ctx, fr[1], fr[0], 16, 16, 8)
     assert mv.shape == (12, 2)
+
+
+IMPL2_CASES = ["qcif_r16_m1", "qcif_r16_m2", "cif_r15_m2", "small_r8_m1", "cif_r32_m2", "wide_r20_m1"]
+
+
+@pytest.mark.parametrize("case", IMPL2_CASES)
+def test_impl2_against_golden(vpp, ctx, golden, case):
+    """MotionEstimatorImpl2 (the SAD pyramid) against the reference's fixtures."""
+    g = golden("me_impl2.npz")
+    w, h, rng, mode = (int(v) for v in g[f"{case}_meta"])
+    me = vpp.MotionEstimatorImpl2(g[f"{case}_src"].astype(np.int16), g[f"{case}_ref"].astype(np.int16), w, h, 16, 16,
+                                  rng, ctx=ctx)
+    assert me.Create() == 1
+    me.SetMode(mode)
+    mv, avg = me.Estimate()
+    np.testing.assert_array_equal(mv, g[f"{case}_mv"])
+    assert avg == int(g[f"{case}_avg"][0])
+
+
+@pytest.mark.parametrize("seed,w,h,rng,mode,gen", [(161, 176, 144, 12, 1, "noisy"), (162, 352, 288, 24, 0, "pan"),
+                                                  (163, 128, 96, 6, 2, "shift"), (164, 1920, 1088, 16, 0, "pan"),
+                                                  (165, 640, 368, 32, 1, "noisy")])
+def test_impl2_against_oracle(vpp, ctx, orc, seed, w, h, rng, mode, gen):
+    fr = umhs_frames(seed, w, h, gen)
+    mv_o, dist_o, avg_o = orc.me_impl2(fr[1], fr[0], rng, mode)
+    me = vpp.MotionEstimatorImpl2(fr[1], fr[0], w, h, 16, 16, rng, ctx=ctx)
+    assert me.Create() == 1
+    me.SetMode(mode)
+    mv, avg = me.Estimate()
+    np.testing.assert_array_equal(mv, mv_o)
+    np.testing.assert_array_equal(me.last_mb_distortion, dist_o)
+    assert avg == avg_o

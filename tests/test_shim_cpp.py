@@ -34,7 +34,8 @@ def test_shim_compiles_against_vpp_interfaces():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["full", "multires", "mrc", "mrc2", "mrc2lam", "cross", "sad", "umhs", "fhs", "impl1"])
+@pytest.mark.parametrize("kind", ["full", "multires", "mrc", "mrc2", "mrc2lam", "cross", "sad", "umhs", "fhs", "impl1",
+                                  "impl2"])
 def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
     from imagecodingutils_gb300 import build
     exe = tmp_path / "example_estimate"
@@ -51,9 +52,10 @@ def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
     assert r.returncode == 0, r.stderr
     nmb = (w // 16) * (h // 16)
     raw = out.read_bytes()
-    if kind == "impl1":  # MotionEstimatorImpl1: the SimpleMotionVectorList's char vectors and the average
+    if kind in ("impl1", "impl2"):  # the SimpleMotionVectorList's char vectors and the average
         mv = np.frombuffer(raw[:4 * nmb], np.int16).reshape(nmb, 2)
-        mv_o, _, avg_o = orc.me_impl1(fr[1], fr[0], 16)
+        # SetMode(0) at 176x144 (area below 40000) is Impl2's two-level mode 1
+        mv_o, _, avg_o = orc.me_impl1(fr[1], fr[0], 16) if kind == "impl1" else orc.me_impl2(fr[1], fr[0], 16, 1)
         np.testing.assert_array_equal(mv, mv_o)
         assert np.frombuffer(raw[4 * nmb:4 * nmb + 8], np.int64)[0] == avg_o
         return
