@@ -55,6 +55,7 @@ class Oracle:
         L.vo_me_full_intpel.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P]
         L.vo_me_multires_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.vo_me_h263_multires_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
+        L.vo_me_h263_multires_cross_ver2.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, C.POINTER(_L)]
         L.vo_me_multires_cross_v2.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_me_cross.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
         L.vo_me_multires.argtypes = [_P, _P, _I, _I, _I, _I, _P, _P, _P, _P, C.POINTER(_L), _P]
@@ -110,6 +111,11 @@ class Oracle:
     def me_h263_multires_cross(self, src, ref, motion_range, mode=1, dist_incl=None):
         """MotionEstimatorH263ImplMultiresCross: motion range and vectors in half pels."""
         return self.me_multires_cross(src, ref, motion_range, mode, dist_incl, _fn=self.lib.vo_me_h263_multires_cross)
+
+    def me_h263_multires_cross_ver2(self, src, ref, motion_range, mode=1, dist_incl=None):
+        """MotionEstimatorH263ImplMultiresCrossVer2 with the H.263 median predictor: half pels."""
+        return self.me_multires_cross(src, ref, motion_range, mode, dist_incl,
+                                      _fn=self.lib.vo_me_h263_multires_cross_ver2)
 
     def me_multires_cross(self, src, ref, motion_range, mode=1, dist_incl=None, _fn=None):
         h, w = src.shape
@@ -375,7 +381,7 @@ class Reference:
     """The reference's own C++ classes (only where oracle/_ref was built)."""
 
     KIND = {"full": 0, "multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4,
-            "h263_multires_cross": 5}
+            "h263_multires_cross": 5, "h263_multires_cross_v2": 6}
 
     def __init__(self, path: str = REF_SO):
         self.lib = C.CDLL(path)

@@ -260,6 +260,7 @@ typedef struct {
     mr_level L0, L1, L2;
     mr_window* win;
     int h263; /* MotionEstimatorH263ImplMultiresCross: half-pel stage by HalfRead, its accept rule */
+    int tie_plus_y; /* MotionEstimatorH263ImplMultiresCrossVer2: the candidate's y distance adds the prediction */
 } mr_ctx;
 
 /* OverlayMem2Dv2::HalfRead at half-pel offset (hx, hy) in -1..1 of the
@@ -363,6 +364,16 @@ static inline int mr_farther(int mx, int my, int rmx, int rmy, int j, int i, int
     return (cy * cy + cx * cx) - (ny * ny + nx * nx) < 0;
 }
 
+/* MotionEstimatorH263ImplMultiresCrossVer2's tie rule (…H263ImplMultiresCrossVer2.cpp:714-721, 787-794,
+ * 844-851, 912-919): the candidate's y distance is taken as my + i + predY, with the prediction's y added
+ * where the current best's subtracts it. */
+static inline int mr_farther_v2(const mr_ctx* c, int mx, int my, int rmx, int rmy, int j, int i, int px, int py)
+{
+    if (!c->tie_plus_y) return mr_farther(mx, my, rmx, rmy, j, i, px, py);
+    const int cx = mx + rmx - px, cy = my + rmy - py, nx = mx + j - px, ny = my + i + py;
+    return (cy * cy + cx * cx) - (ny * ny + nx * nx) < 0;
+}
+
 /* Result of the search of one macroblock. */
 typedef struct {
     int zero_d, min_d, mvx, mvy;
@@ -402,7 +413,7 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
                 if (d == min2) {
                     tie |= 1;
                     /* MultiresCross compares the centre with the offset (…:673-679) */
-                    if (pred ? mr_farther(mx, my, rmx, rmy, j, i, pred[0], pred[1])
+                    if (pred ? mr_farther_v2(c, mx, my, rmx, rmy, j, i, pred[0], pred[1])
                              : (my * my + mx * mx) - (i * i + j * j) < 0)
                         continue;
                 }
@@ -433,7 +444,7 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
                 if (d > min1) continue;
                 if (d == min1) {
                     tie |= 2;
-                    if (mr_farther(mx, my, rmx, rmy, j, i, p1x, p1y)) continue;
+                    if (mr_farther_v2(c, mx, my, rmx, rmy, j, i, p1x, p1y)) continue;
                 }
                 min1 = d;
                 rmx = j;
@@ -451,7 +462,7 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
                 if (d > min1) continue;
                 if (d == min1) {
                     tie |= 2;
-                    if (mr_farther(mx, my, rmx, rmy, j, i, p1x, p1y)) continue;
+                    if (mr_farther_v2(c, mx, my, rmx, rmy, j, i, p1x, p1y)) continue;
                 }
                 min1 = d;
                 rmx = j;
@@ -480,7 +491,7 @@ static void mr_search_mb(mr_ctx* c, int mbr, int mbc, const int* pred, mr_result
             if (d > min_d) continue;
             if (d == min_d) {
                 tie |= 4;
-                if (mr_farther(mx, my, rmx, rmy, j, i, p0x, p0y)) continue;
+                if (mr_farther_v2(c, mx, my, rmx, rmy, j, i, p0x, p0y)) continue;
             }
             min_d = d;
             rmx = j;
@@ -804,6 +815,126 @@ static int me_multires_cross_any(int h263, const short* src, const short* ref, i
                 } else {
                     mvx = mvy = 0;
                     chosen = r.zero_d;
+                }
+                if (do_it) {
+                    included++;
+                    total += chosen;
+                }
+                if (vec_pos < c.nmb) {
+                    mv_out[2 * vec_pos] = (short)mvx;
+                    mv_out[2 * vec_pos + 1] = (short)mvy;
+                    if (mb_dist) mb_dist[vec_pos] = chosen;
+                }
+            }
+        if (avg_dist) *avg_dist = included ? total / included : 0;
+        if (g_mr_fault) rc = -3;
+    }
+    mr_ctx_free(&c);
+    return rc;
+}
+
+/* H263MotionVectorPredictorImpl1::Get16x16Prediction (src/CodecUtils/H263MotionVectorPredictorImpl1.cpp:72-128)
+ * over the vectors written so far: in the top row the left neighbour (0 at the left edge), else the
+ * componentwise median of left, above and above-right, each 0 beyond the left or right edge. */
+static void h263_pred(const short* mv, int cols, int blk, int* px, int* py)
+{
+    const int mby = blk / cols, mbx = blk % cols;
+    int a[2] = {0, 0}, b[2], c[2] = {0, 0};
+    if (mbx > 0) {
+        a[0] = mv[2 * (mby * cols + mbx - 1)];
+        a[1] = mv[2 * (mby * cols + mbx - 1) + 1];
+    }
+    if (mby < 1) {
+        *px = a[0];
+        *py = a[1];
+        return;
+    }
+    b[0] = mv[2 * ((mby - 1) * cols + mbx)];
+    b[1] = mv[2 * ((mby - 1) * cols + mbx) + 1];
+    if (mbx + 1 < cols) {
+        c[0] = mv[2 * ((mby - 1) * cols + mbx + 1)];
+        c[1] = mv[2 * ((mby - 1) * cols + mbx + 1) + 1];
+    }
+    int out[2];
+    for (int k = 0; k < 2; k++) {
+        int lo = b[k] < c[k] ? b[k] : c[k], hi = b[k] < c[k] ? c[k] : b[k];
+        if (a[k] < lo) lo = a[k];
+        if (a[k] > hi) hi = a[k];
+        out[k] = a[k] + b[k] + c[k] - lo - hi;
+    }
+    *px = out[0];
+    *py = out[1];
+}
+
+/* MotionEstimatorH263ImplMultiresCrossVer2::Estimate
+ * (src/CodecUtils/MotionEstimatorH263ImplMultiresCrossVer2.cpp:537-1151): the H.263 MultiresCross
+ * search with ties decided towards the prediction of each level (half-pel prediction rounded away
+ * from zero to full pels, then halved per level, :622-639) by the rule of mr_farther_v2; then the
+ * distortion at the prediction clamped to one macroblock outside the picture (HalfRead for its half
+ * components, :1012-1050) competes with the zero vector's, and the accept rule of MultiresCross picks
+ * the searched vector or the better of the two (:1052-1142).  The prediction of a partial bottom row
+ * is that of index N_MB (vecPos stops there); its results only enter the average. */
+int vo_me_h263_multires_cross_ver2(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                                   const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist)
+{
+    if (!src || !ref || !mv_out || w < 16 || h < 16 || (w % 16) != 0) return -1;
+    g_mr_fault = 0;
+    mr_ctx c;
+    int rc = mr_ctx_init_h(&c, src, ref, w, h, motion_range, mode, 1);
+    c.tie_plus_y = 1;
+    if (rc == 0) {
+        long total = 0;
+        int included = 0;
+        short blk[256];
+        for (int mbr = 0; mbr < c.rows_all; mbr++)
+            for (int mbc = 0; mbc < c.cols; mbc++) {
+                const int vec_pos = mbr * c.cols + mbc < c.nmb ? mbr * c.cols + mbc : c.nmb;
+                const int n = 16 * mbc, m = 16 * mbr;
+                int px, py;
+                h263_pred(mv_out, c.cols, vec_pos, &px, &py);
+                const int pxh = px % 2, pyh = py % 2;
+                int px0 = px / 2, py0 = py / 2;
+                const int px0r = px < 0 ? (px - 1) / 2 : (px + 1) / 2, py0r = py < 0 ? (py - 1) / 2 : (py + 1) / 2;
+                const int pl[6] = {px0r / 2 / 2, py0r / 2 / 2, px0r / 2, py0r / 2, px0r, py0r};
+                mr_result r;
+                mr_search_mb(&c, mbr, mbc, pl, &r);
+                int mvx = r.mvx, mvy = r.mvy;
+                if (px0 + n > w) px0 = 16;
+                if (px0 + n < -16) px0 = -16;
+                if (py0 + m > h) py0 = 16;
+                if (py0 + m < -16) py0 = -16;
+                const int pvx = 2 * px0 + pxh, pvy = 2 * py0 + pyh;
+                mr_ov oin0 = {&c.in0, 16, 16, 0, 0, 0, 0}, oe0 = {&c.e0, 16, 16, 0, 0, 17, 17};
+                ov_origin(&oin0, n, m);
+                ov_origin(&oe0, px0 + n, py0 + m);
+                int pred_d;
+                if (pxh || pyh) {
+                    mr_half_read(&oe0, pxh, pyh, blk);
+                    pred_d = 0;
+                    for (int i = 0; i < 256; i++) {
+                        const int d = ov_px(&oin0, i / 16, i % 16) - blk[i];
+                        pred_d += d * d;
+                    }
+                } else {
+                    pred_d = ov_tsd(&oin0, &oe0, 16);
+                }
+                int zx = pvx, zy = pvy, zd = pred_d;
+                if (r.zero_d < zd) {
+                    zd = r.zero_d;
+                    zx = zy = 0;
+                }
+                int weight = 0, diff0 = zd - r.min_d, mag = mvx * mvx + mvy * mvy;
+                if ((diff0 >> 2) < mag) weight++;
+                if (zd < MRC_NOISE_FLOOR) weight++;
+                if (diff0 * 10 < r.min_d) weight++;
+                int do_it = dist_incl ? (vec_pos < c.nmb ? dist_incl[vec_pos] != 0 : 0) : 1;
+                int chosen;
+                if (r.min_d < zd && weight < 2) {
+                    chosen = r.min_d;
+                } else {
+                    mvx = zx;
+                    mvy = zy;
+                    chosen = zd;
                 }
                 if (do_it) {
                     included++;

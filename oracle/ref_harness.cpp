@@ -25,6 +25,8 @@
 #include "MotionEstimatorImpl2.h"
 #include "SimpleMotionVectorList.h"
 #include "MotionEstimatorH263ImplMultiresCross.h"
+#include "MotionEstimatorH263ImplMultiresCrossVer2.h"
+#include "H263MotionVectorPredictorImpl1.h"
 #include "VectorStructList.h"
 #include "MotionCompensatorH264ImplStd.h"
 #include "FastForward4x4ITImpl1.h"
@@ -179,7 +181,8 @@ int ref_me_full_sad(const short* src, const short* ref, int w, int h, int motion
     return 0;
 }
 
-/* kind: 0 Full, 1 Multires, 2 MultiresCross, 3 MultiresCrossVer2.
+/* kind: 0 Full, 1 Multires, 2 MultiresCross, 3 MultiresCrossVer2, 4 Cross, 5 H263MultiresCross,
+ * 6 H263MultiresCrossVer2 (with an H263MotionVectorPredictorImpl1).
  * lambda: NULL, or a pointer passed to Estimate(long*, void*) (Ver2 only).
  * Returns 0 on success. */
 int ref_me_estimate(int kind, const short* src, const short* ref, int w, int h, int motion_range,
@@ -189,6 +192,7 @@ int ref_me_estimate(int kind, const short* src, const short* ref, int w, int h, 
     int nmb = (w / 16) * (h / 16);
     MbGrid grid(w, h);
     H264MotionVectorPredictorImpl1 pred(grid.flat);
+    H263MotionVectorPredictorImpl1 pred263(w, h);
     bool* flags = make_flags(incl, nmb);
     IMotionEstimator* me = NULL;
     /* The multi-resolution estimators read window samples they never write
@@ -203,6 +207,7 @@ int ref_me_estimate(int kind, const short* src, const short* ref, int w, int h, 
     case 3: me = new MotionEstimatorH264ImplMultiresCrossVer2(src, ref, w, h, motion_range, &pred, flags); break;
     case 4: me = new MotionEstimatorH264ImplCross(src, ref, w, h, motion_range, &pred, flags); break;
     case 5: me = new MotionEstimatorH263ImplMultiresCross(src, ref, w, h, motion_range, flags); break;
+    case 6: me = new MotionEstimatorH263ImplMultiresCrossVer2(src, ref, w, h, motion_range, &pred263, flags); break;
     default: mallopt(M_PERTURB, 0); delete[] flags; return -1;
     }
     int created = me->Create();

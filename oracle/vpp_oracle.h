@@ -133,6 +133,10 @@ int vo_me_multires_cross(const short* src, const short* ref, int w, int h, int m
  * range and vectors in half pels, HalfRead half-pel stage. */
 int vo_me_h263_multires_cross(const short* src, const short* ref, int w, int h, int motion_range, int mode,
                               const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist);
+/* MotionEstimatorH263ImplMultiresCrossVer2 with H263MotionVectorPredictorImpl1: half-pel vectors,
+ * the chosen distortion per macroblock, avgDistortion (all macroblocks when dist_incl is NULL). */
+int vo_me_h263_multires_cross_ver2(const short* src, const short* ref, int w, int h, int motion_range, int mode,
+                                   const unsigned char* dist_incl, short* mv_out, int* mb_dist, long* avg_dist);
 
 /* MotionEstimatorH264ImplMultiresCrossVer2::Estimate(long*)
  * (src/CodecUtils/MotionEstimatorH264ImplMultiresCrossVer2.cpp:537-1151): the

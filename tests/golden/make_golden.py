@@ -58,7 +58,7 @@ inputs and stores inputs and outputs:
                   SHA-256)
 
 Usage: python tests/golden/make_golden.py [name ...]   (needs the reference tree;
-names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc me_umhs me_fhs me_impl1 me_impl2 mc
+names: me_1080p me_full me_full_sad me_mrc me_mrc2 me_mrc2_lambda me_mr me_cross me_h263mrc me_h263mrc2 me_umhs me_fhs me_impl1 me_impl2 mc
 transform dc yuv2rgb colour, default all)
 """
 from __future__ import annotations
@@ -313,6 +313,45 @@ def umhs_fixtures(ref: oracle.Reference) -> dict:
     out["hd_mv"] = mv
     out["hd_dist"] = d
     out["hd_avg"] = np.array([avg], np.int64)
+    return out
+
+
+H263V2_CASES = [  # (name, w, h, half-pel motion range, seed, generator)
+    ("qcif_r32", 176, 144, 32, 61, "pan"),
+    ("cif_r64", 352, 288, 64, 62, "noisy"),
+    ("partial_r64", 352, 280, 64, 63, "shift"),
+    ("small_r16", 64, 48, 16, 64, "noisy"),
+    ("wide_r48", 208, 120, 48, 65, "pan"),
+]
+
+
+def h263v2_fixtures(ref: oracle.Reference) -> dict:
+    """MotionEstimatorH263ImplMultiresCrossVer2 with H263MotionVectorPredictorImpl1:
+    vectors and avgDistortion at modes 0/1/2, without and with a seeded
+    pDistortionIncluded, and the 1080p benchmark pair at the largest range."""
+    out = {}
+    for name, w, h, mr, seed, gen in H263V2_CASES:
+        fr = umhs_frames(seed, w, h, gen)
+        src, rf = fr[1], fr[0]
+        nmb = (w // 16) * (h // 16)
+        incl = (synth.splitmix64(seed, nmb) % np.uint64(3) != 0).astype(np.uint8)
+        out[f"{name}_src"] = src.astype(np.uint8)
+        out[f"{name}_ref"] = rf.astype(np.uint8)
+        out[f"{name}_meta"] = np.array([w, h, mr], np.int32)
+        out[f"{name}_incl"] = incl
+        for mode in (0, 1, 2):
+            mv, avg = ref.me("h263_multires_cross_v2", src, rf, mr, mode=mode)
+            mvi, avgi = ref.me("h263_multires_cross_v2", src, rf, mr, mode=mode, dist_incl=incl)
+            assert np.array_equal(mv, mvi)
+            out[f"{name}_m{mode}_mv"] = mv
+            out[f"{name}_m{mode}_avg"] = np.array([avg, avgi], np.int64)
+    fr, digest = hd_frames()
+    out["hd_meta"] = np.array([HD_SEED, HD_W, HD_H, 64], np.int32)
+    out["hd_frames_sha256"] = digest
+    for mode in (0, 1):
+        mv, avg = ref.me("h263_multires_cross_v2", fr[1], fr[0], 64, mode=mode)
+        out[f"hd_m{mode}_mv"] = mv
+        out[f"hd_m{mode}_avg"] = np.array([avg], np.int64)
     return out
 
 
@@ -572,6 +611,7 @@ def main() -> None:
               "me_mrc2_lambda": mrc2_lambda_fixtures,
               "me_mr": lambda r: mrc2_fixtures(r, "multires"), "me_cross": lambda r: mrc2_fixtures(r, "cross"),
               "me_h263mrc": lambda r: mrc_fixtures(r, "h263_multires_cross", H263_CASES),
+              "me_h263mrc2": h263v2_fixtures,
               "me_umhs": umhs_fixtures, "me_fhs": fhs_fixtures, "me_impl1": impl1_fixtures, "me_impl2": impl2_fixtures,
               "mc": mc_fixtures,
               "transform": transform_fixtures, "dc": dc_fixtures, "yuv2rgb": yuv2rgb_fixtures,

@@ -236,6 +236,52 @@ def test_me_h263_multires_cross_matches_reference(orc, golden, case, mode):
     assert avgi == int(g[f"{case}_m{mode}_avg"][1])
 
 
+H263V2_CASES = ["qcif_r32", "cif_r64", "partial_r64", "small_r16", "wide_r48"]
+
+
+@pytest.mark.parametrize("case", H263V2_CASES)
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_me_h263_multires_cross_ver2_matches_reference(orc, golden, case, mode):
+    """MotionEstimatorH263ImplMultiresCrossVer2 (H.263 median predictor over the
+    vectors written so far, the y-sum quirk of its tie rule, the clamped
+    half-pel prediction against the zero vector)."""
+    g = golden("me_h263mrc2.npz")
+    w, h, mr = (int(v) for v in g[f"{case}_meta"])
+    src = g[f"{case}_src"].astype(np.int16)
+    ref = g[f"{case}_ref"].astype(np.int16)
+    mv, _, avg = orc.me_h263_multires_cross_ver2(src, ref, mr, mode=mode)
+    np.testing.assert_array_equal(mv, g[f"{case}_m{mode}_mv"])
+    assert avg == int(g[f"{case}_m{mode}_avg"][0])
+    mvi, _, avgi = orc.me_h263_multires_cross_ver2(src, ref, mr, mode=mode, dist_incl=g[f"{case}_incl"])
+    np.testing.assert_array_equal(mvi, mv)
+    assert avgi == int(g[f"{case}_m{mode}_avg"][1])
+
+
+def test_me_h263_multires_cross_ver2_1080p_matches_reference(orc, golden, hd_golden):
+    g = golden("me_h263mrc2.npz")
+    assert g["hd_frames_sha256"].tobytes() == hd_golden["g"]["frames_sha256"].tobytes()
+    fr = hd_golden["frames"]
+    for mode in (0, 1):
+        mv, _, avg = orc.me_h263_multires_cross_ver2(fr[1], fr[0], int(g["hd_meta"][3]), mode=mode)
+        np.testing.assert_array_equal(mv, g[f"hd_m{mode}_mv"])
+        assert avg == int(g[f"hd_m{mode}_avg"][0])
+
+
+@ref_available
+@pytest.mark.parametrize("seed,w,h,mr,mode,gen", [(71, 176, 144, 64, 2, "noisy"), (72, 640, 360, 64, 0, "pan"),
+                                                 (73, 96, 64, 16, 1, "noisy"), (74, 320, 176, 40, 2, "shift")])
+def test_me_h263_multires_cross_ver2_against_compiled_reference(orc, seed, w, h, mr, mode, gen):
+    from tests.golden.make_golden import umhs_frames
+    fr = umhs_frames(seed, w, h, gen)
+    r = oracle_mod.Reference()
+    incl = (synth.splitmix64(seed, (w // 16) * (h // 16)) & np.uint64(1)).astype(np.uint8)
+    for dist_incl in (None, incl):
+        mv, _, avg = orc.me_h263_multires_cross_ver2(fr[1], fr[0], mr, mode=mode, dist_incl=dist_incl)
+        mv_r, avg_r = r.me("h263_multires_cross_v2", fr[1], fr[0], mr, mode=mode, dist_incl=dist_incl)
+        np.testing.assert_array_equal(mv, mv_r)
+        assert avg == avg_r
+
+
 MRC2_CASES = ["qcif_r64", "cif_r128", "partial_r128", "small_r32", "shift_r128"]
 
 
