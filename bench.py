@@ -409,6 +409,7 @@ MULTIRES = {  # kind -> (class name, oracle method)
     "multires_cross_v2": ("MotionEstimatorH264ImplMultiresCrossVer2", "me_multires_cross_v2"),
     "cross": ("MotionEstimatorH264ImplCross", "me_cross"),
     "h263_multires_cross": ("MotionEstimatorH263ImplMultiresCross", "me_h263_multires_cross"),
+    "h263_multires_cross_v2": ("MotionEstimatorH263ImplMultiresCrossVer2", "me_h263_multires_cross_ver2"),
     "full_sad": ("MotionEstimatorH264ImplFullSad", "me_full_intpel"),
     "umhs": ("MotionEstimatorH264ImplUMHS", "me_umhs"),
     "fhs": ("MotionEstimatorH264ImplFHS", "me_fhs"),
@@ -416,9 +417,11 @@ MULTIRES = {  # kind -> (class name, oracle method)
     "impl2": ("MotionEstimatorImpl2", "me_impl2"),
 }
 MULTIRES_CODE = {"multires": 1, "multires_cross": 2, "multires_cross_v2": 3, "cross": 4,
-                 "h263_multires_cross": 5, "full_sad": 6, "umhs": 7, "fhs": 8, "impl1": 9, "impl2": 10}  # VPPGPU_ME_*
+                 "h263_multires_cross": 5, "full_sad": 6, "umhs": 7, "fhs": 8, "impl1": 9, "impl2": 10,
+                 "h263_multires_cross_v2": 11}  # VPPGPU_ME_*
 # motion ranges are in quarter pels, the H.263 estimator's in half pels: the same +-32 pels
-MULTIRES_RANGE = {"h263_multires_cross": MOTION_RANGE // 2, "impl1": 16, "impl2": 16}  # Impl1/2: full pels
+MULTIRES_RANGE = {"h263_multires_cross": MOTION_RANGE // 2, "h263_multires_cross_v2": MOTION_RANGE // 2, "impl1": 16,
+                  "impl2": 16}  # Impl1/2: full pels
 
 
 TUNE_PAIRS = 8
@@ -944,6 +947,8 @@ def main():
                                    not args.no_cpu, kind="impl1")
         impl2 = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames,
                                    not args.no_cpu, kind="impl2")
+        h263v2 = run_multires_cross(args, torch, vpp, _lib, L, ctx, stream, f"cuda:{local}", frames,
+                                    not args.no_cpu, kind="h263_multires_cross_v2")
         pk, pk_kind = peaks()
         hbm_rows = run_hbm_paths(torch, _lib, L, ctx, stream, f"cuda:{local}", pk)
         line = {
@@ -967,7 +972,8 @@ def main():
             "gpu_launches": launches, "cpu_baseline": cpu, "parity_first_frame": check, "batched": batched,
             "serving": serving,
             "multires": mr, "multires_cross": mrc, "multires_cross_v2": mrc2, "cross": cr,
-            "h263_multires_cross": h263, "full_sad": sad, "umhs": umhs, "fhs": fhs, "impl1": impl1, "impl2": impl2, **hbm_rows,
+            "h263_multires_cross": h263, "full_sad": sad, "umhs": umhs, "fhs": fhs, "impl1": impl1, "impl2": impl2,
+            "h263_multires_cross_v2": h263v2, **hbm_rows,
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -29,7 +29,8 @@ from ._lib import VppGpuError, check, load
 __all__ = [
     "Context", "get_context", "MotionEstimatorH264ImplFull", "MotionEstimatorH264ImplMultires",
     "MotionEstimatorH264ImplMultiresCross", "MotionEstimatorH264ImplMultiresCrossVer2", "MotionEstimatorH264ImplCross", "MotionEstimatorH264ImplFullSad", "MotionEstimatorH264ImplUMHS", "MotionEstimatorH264ImplFHS", "MotionEstimatorImpl1", "MotionEstimatorImpl2",
-    "MotionEstimatorH263ImplMultiresCross", "MotionEstimatorBatch",
+    "MotionEstimatorH263ImplMultiresCross",
+    "MotionEstimatorH263ImplMultiresCrossVer2", "MotionEstimatorBatch",
     "Server", "FastForward4x4ITImpl1", "FastForward4x4ITImpl2",
     "FastForward4x4On16x16ITImpl1", "FastInverse4x4ITImpl1", "FastInverse4x4On16x16ITImpl1", "FastForwardDC4x4ITImpl1",
     "FastForwardDC2x2ITImpl1", "FastInverseDC4x4ITImpl1", "FastInverseDC2x2ITImpl1",
@@ -168,9 +169,10 @@ class _MotionEstimatorBase:
                                                    _ptr(self._slice), float(param), _ptr(mv), _ptr(dist),
                                                    C.byref(avg)), "vppgpu_me_estimate_lambda")
         self.last_mb_distortion = dist
-        if self._pred is not None:  # side effect of the reference on its predictor
+        setter = getattr(self._pred, "Set16x16MotionVector", None)
+        if setter is not None:  # side effect of the reference on its predictor
             for k in range(n):
-                self._pred.Set16x16MotionVector(k, int(mv[k, 0]), int(mv[k, 1]))
+                setter(k, int(mv[k, 0]), int(mv[k, 1]))
         return mv, avg.value
 
     def Autotune(self, reps: int = 2) -> dict:
@@ -378,6 +380,20 @@ class MotionEstimatorH263ImplMultiresCross(MotionEstimatorH264ImplMultiresCross)
     half pels."""
 
     KIND = _lib.ME_H263_MULTIRES_CROSS
+
+
+class MotionEstimatorH263ImplMultiresCrossVer2(MotionEstimatorH264ImplMultiresCross):
+    """GPU MotionEstimatorH263ImplMultiresCrossVer2
+    (src/CodecUtils/MotionEstimatorH263ImplMultiresCrossVer2.cpp) with the
+    H.263 median prediction of H263MotionVectorPredictorImpl1: the H.263
+    MultiresCross search with ties towards the prediction, then the better of
+    the clamped prediction and the zero vector against the searched vector;
+    motionRange (at most 64) and vectors in half pels.  The prediction comes
+    from the vectors the estimate writes, so pMVPred (an
+    H263MotionVectorPredictorImpl1 in the reference) is not consulted; an
+    object with Set16x16MotionVector still receives every vector."""
+
+    KIND = _lib.ME_H263_MULTIRES_CROSS_V2
 
 
 class MotionEstimatorH264ImplMultires(MotionEstimatorH264ImplMultiresCross):

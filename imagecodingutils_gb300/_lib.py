@@ -32,6 +32,7 @@ ME_UMHS = 7
 ME_FHS = 8
 ME_IMPL1 = 9
 ME_IMPL2 = 10
+ME_H263_MULTIRES_CROSS_V2 = 11
 LAYOUT_BLOCKS, LAYOUT_MB16 = 0, 1
 INV_ROWS_FIRST, INV_COLS_FIRST = 0, 1
 RGB_FIXED_POINT, RGB_REAL, RGB_REAL_IMPL2 = 0, 1, 2

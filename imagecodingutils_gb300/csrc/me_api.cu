@@ -223,6 +223,13 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
 {
     vppgpu_ctx* ctx = me->ctx;
     VPP_CUDA(cudaMemsetAsync(me->ctrl, 0, sizeof(vppgpu::MeCtrl), ctx->stream));
+    if (me->kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2) {
+        const vppgpu::H263V2Job j{me->W,      me->H,         me->motion_range, me->mode,           me->relax_sweeps,
+                                  me->wave_grid, d_src16,    d_ref16,          me->d_mrc,          d_incl,
+                                  d_mv,       d_dist,        d_avg,            me->ctrl,           (int4*)me->spec,
+                                  me->state,  me->state + me->nmb, me->d_urec, me->changed,        me->d_uorder};
+        return vppgpu::h263v2_launch(ctx, j);
+    }
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS)
         return vppgpu::mrc_launch(ctx, me->W, me->H, me->motion_range, me->mode, d_src16, d_ref16, me->d_mrc, d_incl,
                                   d_mv, d_dist, d_avg, me->ctrl, me->mrc_warps,
@@ -288,6 +295,25 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
 }
 
 int status_from_ctrl(const vppgpu::MeCtrl& c) { return vppgpu::status_from_bits(c.status); }
+
+// The dataflow passes' ticket order: anti-diagonals c + 2r, rows ascending, so that every neighbour a
+// prediction reads has a lower ticket; and their grid, one CTA of 4 warps per SM (a wavefront holds at
+// most min(rows, cols / 2) macroblocks at a time, and warps holding later tickets only wait).
+int upload_diagonal_order(vppgpu_me* me)
+{
+    std::vector<int> order;
+    order.reserve(me->nmb);
+    for (int d = 0; d <= (me->cols - 1) + 2 * (me->rows - 1); d++)
+        for (int r = 0; r < me->rows; r++) {
+            const int c = d - 2 * r;
+            if (c >= 0 && c < me->cols) order.push_back(r * me->cols + c);
+        }
+    if (cudaMemcpy(me->d_uorder, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return VPPGPU_ERR_CUDA;
+    const int g = (me->nmb + 3) / 4;
+    me->wave_grid = g < me->ctx->sm_count ? g : me->ctx->sm_count;
+    return VPPGPU_OK;
+}
 
 bool aligned(const void* p, size_t a) { return ((uintptr_t)p & (a - 1)) == 0; }
 
@@ -377,9 +403,11 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     if (width < 16 || height < 16 || (width % 16) != 0 || motion_range < 4) return VPPGPU_ERR_INVALID_ARG;
     if (width > 8192 || height > 8192) return VPPGPU_ERR_UNSUPPORTED;
     if (motion_range > 128) return VPPGPU_ERR_UNSUPPORTED;
-    if (kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_FHS) return VPPGPU_ERR_UNSUPPORTED;
-    // MotionEstimatorH263ImplMultiresCross's range is in half pels: at most 64 (+-31 pels), as 128 quarter pels
-    if (kind == VPPGPU_ME_H263_MULTIRES_CROSS && motion_range > 64) return VPPGPU_ERR_UNSUPPORTED;
+    if ((kind < VPPGPU_ME_FULL || kind > VPPGPU_ME_FHS) && kind != VPPGPU_ME_H263_MULTIRES_CROSS_V2)
+        return VPPGPU_ERR_UNSUPPORTED;
+    // the H.263 MultiresCross estimators' range is in half pels: at most 64 (+-31 pels), as 128 quarter pels
+    if ((kind == VPPGPU_ME_H263_MULTIRES_CROSS || kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2) && motion_range > 64)
+        return VPPGPU_ERR_UNSUPPORTED;
     int rc = vppgpu::bind(ctx);
     if (rc) return rc;
     vppgpu_me* me = (vppgpu_me*)calloc(1, sizeof(vppgpu_me));
@@ -459,6 +487,33 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
         *out = me;
         return VPPGPU_OK;
     }
+    if (kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2) {
+        // MotionEstimatorH263ImplMultiresCrossVer2(…, pMVPred, pDistortionIncluded) + Create(): the level
+        // planes, the searches at prediction (0, 0), relaxation and dataflow vectors, records, the
+        // dataflow order
+        me->relax_sweeps = 8;
+        if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
+            (rc = dalloc(&me->d_mrc, vppgpu::mrc_scratch_bytes(width, height))) ||
+            (rc = dalloc(&me->spec, 4 * (size_t)me->nmb)) || (rc = dalloc(&me->state, 2 * (size_t)me->nmb)) ||
+            (rc = dalloc(&me->d_urec, (size_t)me->nmb * vppgpu::H263V2_RECORDS)) ||
+            (rc = dalloc(&me->d_uorder, me->nmb)) || (rc = dalloc(&me->changed, (size_t)me->sweep_limit)) ||
+            (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
+            (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||
+            (rc = dalloc(&me->d_slice, me->nmb)) || (rc = dalloc(&me->ctrl, 1))) {
+            me_free(me);
+            return rc;
+        }
+        if (cudaMallocHost((void**)&me->h_ctrl, sizeof(vppgpu::MeCtrl)) != cudaSuccess) {
+            me_free(me);
+            return VPPGPU_ERR_OUT_OF_MEMORY;
+        }
+        if ((rc = upload_diagonal_order(me))) {
+            me_free(me);
+            return rc;
+        }
+        *out = me;
+        return VPPGPU_OK;
+    }
     if (searches_from_prediction(kind)) {
         // MotionEstimatorH264ImplUMHS(…, pMVPred, pDistortionIncluded, pPrevFrmMBlk) + Create(): the padded
         // reference with its half-pel planes, sweep and dataflow states, records, the previous frame's
@@ -480,24 +535,13 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
             me_free(me);
             return VPPGPU_ERR_OUT_OF_MEMORY;
         }
-        // anti-diagonals c + 2r, rows ascending: every neighbour a prediction reads has a lower ticket
-        std::vector<int> order;
-        order.reserve(me->nmb);
-        for (int d = 0; d <= (me->cols - 1) + 2 * (me->rows - 1); d++)
-            for (int r = 0; r < me->rows; r++) {
-                const int c = d - 2 * r;
-                if (c >= 0 && c < me->cols) order.push_back(r * me->cols + c);
-            }
-        if (cudaMemcpy(me->d_uorder, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemset(me->d_uprev, 0, sizeof(int) * (size_t)me->nmb) != cudaSuccess ||
-            cudaMemset(me->d_ustate, 0, sizeof(unsigned long long) * (size_t)me->nmb) != cudaSuccess) {
+        if ((rc = upload_diagonal_order(me)) ||
+            (cudaMemset(me->d_uprev, 0, sizeof(int) * (size_t)me->nmb) != cudaSuccess && (rc = VPPGPU_ERR_CUDA)) ||
+            (cudaMemset(me->d_ustate, 0, sizeof(unsigned long long) * (size_t)me->nmb) != cudaSuccess &&
+             (rc = VPPGPU_ERR_CUDA))) {
             me_free(me);
-            return VPPGPU_ERR_CUDA;
+            return rc;
         }
-        // one CTA of 4 warps per SM: a wavefront holds at most min(rows, cols / 2)
-        // macroblocks at a time, and warps holding later tickets only wait
-        const int g = (me->nmb + 3) / 4;
-        me->wave_grid = g < ctx->sm_count ? g : ctx->sm_count;
         if ((rc = vppgpu::umhs_prepare())) {
             me_free(me);
             return rc;
@@ -822,6 +866,9 @@ extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS) {
         for (int w : {2, 4, 8})
             if (w != cur.warps) cands.push_back({cur.relax, cur.grid, cur.bps, w});
+    } else if (me->kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2) {  // the sweeps before the dataflow pass
+        for (int r : {0, 2, 4, 8, 14})
+            if (r != cur.relax) cands.push_back({r, cur.grid, cur.bps, cur.warps});
     } else if (searches_from_prediction(me->kind)) {  // only the sweeps before the dataflow pass matter
         for (int r : {4, 8, 12, 16, 20, 24})
             if (r != cur.relax) cands.push_back({r, cur.grid, cur.bps, cur.warps});

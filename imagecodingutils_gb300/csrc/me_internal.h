@@ -118,6 +118,29 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
                unsigned char* scratch, const unsigned char* incl, int* out_mv, int* out_dist, long long* out_avg,
                MeCtrl* ctrl, int warps = 8, bool h263 = false);
 
+// MotionEstimatorH263ImplMultiresCrossVer2 (me_mrc.cu): the level planes in `scratch`
+// (mrc_scratch_bytes), per-MB search results (s0), relaxation and dataflow vectors, records
+// (H263V2_RECORDS per MB), per-sweep change counts, the dataflow order; motion_range in half pels.
+constexpr int H263V2_RECORDS = 4;
+struct H263V2Job {
+    int W, H, motion_range, mode, sweeps, wave_grid;
+    const short* src16;
+    const short* ref16;
+    unsigned char* scratch;
+    const unsigned char* incl;
+    int* out_mv;
+    int* out_dist;
+    long long* out_avg;
+    MeCtrl* ctrl;
+    int4* s0;
+    int* state;
+    int* wave;
+    int4* rec;
+    int* changed;
+    const int* order;
+};
+int h263v2_launch(vppgpu_ctx* ctx, const H263V2Job& j);
+
 // Device address of the status word (ST_* bits) of a handle's current
 // estimate, and the C ABI status those bits stand for.
 const int* me_status_word(vppgpu_me* me);

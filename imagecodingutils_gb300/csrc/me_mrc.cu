@@ -217,6 +217,327 @@ __global__ void __launch_bounds__(V2_TIE_RUNS * 32) k_pred_tietree(MrcArgs m, Fu
 
 __global__ void k_set_mrc(MrcArgs* dst, MrcArgs v) { *dst = v; }
 
+// ---------------------------------------------------------------------------
+// MotionEstimatorH263ImplMultiresCrossVer2 (…H263ImplMultiresCrossVer2.cpp:537-1151).  Its search is
+// the H.263 MultiresCross search with ties decided towards the prediction of each level, and what
+// follows the search (the distortion at the clamped prediction against the zero vector's, the
+// accept rule) is a function of the prediction, which H263MotionVectorPredictorImpl1 takes from the
+// vectors written so far: a DAG in raster order, as for the H.264 predictor estimators.  Every
+// macroblock is searched at prediction (0, 0); a search whose ties never involved a level where the
+// prediction differs from zero holds for every prediction.  Relaxation sweeps then evaluate every
+// macroblock at the prediction its neighbours' current vectors give (results kept as records keyed
+// by the prediction) until a sweep changes nothing, which is the unique fixed point of the DAG and
+// so the sequential result; otherwise a dataflow pass over the anti-diagonal order decides the
+// frame exactly.
+constexpr int kV2Rec = H263V2_RECORDS;   // records per macroblock: {prediction, vector, distortion, 0}
+constexpr int kV2Empty = 0x7f7f7f7f;     // no half-pel vector packs to this (memset byte 0x7f)
+
+struct V263 {
+    MrcArgs m;
+    int4* s0;           // per MB: searched vector at prediction (0, 0), its distortion, zero-vector distortion, ties
+    int* state;         // per MB: relaxation's current vector (packed half pels)
+    int* wave;          // per MB: the dataflow pass's vector, kV2Empty until published
+    int4* rec;          // kV2Rec per MB
+    int* changed;       // vectors changed per sweep
+    const int* order;   // dataflow ticket -> macroblock
+    int sweeps;
+    long long spin_limit;
+};
+
+__device__ __forceinline__ int ld_relaxed_b32(const int* p)
+{
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_b32(int* p, int v)
+{
+    asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// H263MotionVectorPredictorImpl1::Get16x16Prediction (…H263MotionVectorPredictorImpl1.cpp:72-128) from
+// the left (a), above (b) and above-right (c) vectors, each 0 beyond the picture's side: the left one
+// in the top row, else the componentwise median.
+__device__ __forceinline__ int h263_median(bool top, int a, int b, int c)
+{
+    if (top) return a;
+    return pack_mv(median3(mv_x(a), mv_x(b), mv_x(c)), median3(mv_y(a), mv_y(b), mv_y(c)));
+}
+
+// The prediction's vector at each level (…H263ImplMultiresCrossVer2.cpp:624-639): half pels rounded
+// away from zero to full pels, halved per level by truncation; pl[2l], pl[2l+1] for level l.
+__device__ __forceinline__ void h263_levels(int px, int py, int* pl)
+{
+    const int x0 = px < 0 ? (px - 1) / 2 : (px + 1) / 2, y0 = py < 0 ? (py - 1) / 2 : (py + 1) / 2;
+    pl[0] = x0;
+    pl[1] = y0;
+    pl[2] = x0 / 2;
+    pl[3] = y0 / 2;
+    pl[4] = x0 / 2 / 2;
+    pl[5] = y0 / 2 / 2;
+}
+
+// The search with the estimator's tie rule (…:714-721, 787-794, 844-851, 912-919): the current best
+// is kept when the candidate is farther from the level's prediction, the candidate's y distance being
+// taken as my + i + predY (the prediction added where the current best's subtracts it).
+__device__ __forceinline__ MbSearch h263v2_search(const MrcArgs& a, Lattice& lt, int mbr, int mbc, const int* pl,
+                                                  int lane, bool& bad)
+{
+    auto skip = [pl](int lvl, int mx, int my, int rmx, int rmy, int j, int i) {
+        const int px = pl[2 * lvl], py = pl[2 * lvl + 1];
+        const int cx = mx + rmx - px, cy = my + rmy - py, nx = mx + j - px, ny = my + i + py;
+        return (cy * cy + cx * cx) - (ny * ny + nx * nx) < 0;
+    };
+    return search_mb_with<false, decltype(skip)&, true>(a, lt, mbr, mbc, skip, lane, bad);
+}
+
+// Distortion at the prediction (…:1012-1050): its full-pel part clamped to one macroblock outside the
+// picture, OverlayMem2Dv2::HalfRead for its half-pel part, against the input block; one warp, eight
+// samples per lane.  *pv: the clamped half-pel vector.
+__device__ int h263v2_pred_d(const MrcArgs& a, int mbr, int mbc, int px, int py, int lane, bool& bad, int* pv)
+{
+    const int n = 16 * mbc, m = 16 * mbr;
+    const int hx = px % 2, hy = py % 2;
+    int x0 = px / 2, y0 = py / 2;
+    if (x0 + n > a.W) x0 = 16;
+    if (x0 + n < -16) x0 = -16;
+    if (y0 + m > a.H) y0 = 16;
+    if (y0 + m < -16) y0 = -16;
+    *pv = pack_mv(2 * x0 + hx, 2 * y0 + hy);
+    const Org oi = origin(a.in0, 16, 16, 0, n, m), oe = origin(a.e0, 16, 16, 19, x0 + n, y0 + m);
+    const int r = oe.y + (lane >> 1), ri = oi.y + (lane >> 1), cb = (lane & 1) * 8;
+    int acc = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const int c = oe.x + cb + j + (hx < 0 ? -1 : 0);
+        int v;
+        if (hx && hy)
+            v = (rd(a.e0, r, c, bad) + rd(a.e0, r + hy, c, bad) + rd(a.e0, r, c + 1, bad) + rd(a.e0, r + hy, c + 1, bad) +
+                 2) >> 2;
+        else if (hx)
+            v = (rd(a.e0, r, c, bad) + rd(a.e0, r, c + 1, bad) + 1) >> 1;
+        else if (hy)
+            v = (rd(a.e0, r, c, bad) + rd(a.e0, r + hy, c, bad) + 1) >> 1;
+        else
+            v = rd(a.e0, r, c, bad);
+        const int d = rd(a.in0, ri, oi.x + cb + j, bad) - v;
+        acc += d * d;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    return acc;
+}
+
+// The choice (…:1052-1142): the better of the clamped prediction and the zero vector (the zero vector on
+// a strictly smaller distortion) against the searched vector by MultiresCross's accept rule with
+// (zero - min) >> 2.  Returns {vector, distortion}.
+__device__ __forceinline__ int2 h263v2_choose(const MbSearch& s, int pv, int pred_d)
+{
+    int zv = pv, zd = pred_d;
+    if (s.zero_d < zd) {
+        zd = s.zero_d;
+        zv = 0;
+    }
+    const int diff0 = zd - s.min_d, mag = s.mvx * s.mvx + s.mvy * s.mvy;
+    int weight = 0;
+    if ((diff0 >> 2) < mag) weight++;
+    if (zd < MRC_NOISE_FLOOR) weight++;
+    if (diff0 * 10 < s.min_d) weight++;
+    if (s.min_d < zd && weight < 2) return make_int2(pack_mv(s.mvx, s.mvy), s.min_d);
+    return make_int2(zv, zd);
+}
+
+__device__ __forceinline__ unsigned rec_slot(int p) { return ((unsigned)p * 2654435761u) >> 30; }
+
+// Vector and distortion of macroblock k (row mbr, column mbc) at prediction p: its record, else the
+// search at (0, 0) where that search's ties do not involve the prediction, else a search at p; then the
+// choice, recorded.  One warp.  ghost: a macroblock of a partial bottom row (no record, no search at
+// (0, 0)).
+__device__ int2 h263v2_eval(const V263& v, Lattice& lt, int k, int mbr, int mbc, int p, bool ghost, int lane,
+                            bool& bad)
+{
+    if (!ghost) {
+        const int4 e = lane < kV2Rec ? __ldcg(v.rec + (size_t)k * kV2Rec + lane) : make_int4(kV2Empty, 0, 0, 0);
+        const unsigned hit = __ballot_sync(0xffffffffu, e.x == p);
+        if (hit) {
+            const int f = __ffs(hit) - 1;
+            return make_int2(__shfl_sync(0xffffffffu, e.y, f), __shfl_sync(0xffffffffu, e.z, f));
+        }
+    }
+    const int px = mv_x(p), py = mv_y(p);
+    int pl[6];
+    h263_levels(px, py, pl);
+    MbSearch s;
+    bool reuse = !ghost;
+    if (!ghost) {
+        const int4 s0 = __ldcg(v.s0 + k);
+        s.mvx = mv_x(s0.x);
+        s.mvy = mv_y(s0.x);
+        s.min_d = s0.y;
+        s.zero_d = s0.z;
+        s.tie = s0.w;
+        for (int l = 0; l < 3; l++)
+            if ((s.tie & (TIE_L0 >> l)) && (pl[2 * l] || pl[2 * l + 1])) reuse = false;
+    }
+    if (!reuse) s = h263v2_search(v.m, lt, mbr, mbc, pl, lane, bad);
+    int pv;
+    const int pd = h263v2_pred_d(v.m, mbr, mbc, px, py, lane, bad, &pv);
+    const int2 r = h263v2_choose(s, pv, pd);
+    if (!ghost && lane == 0) v.rec[(size_t)k * kV2Rec + rec_slot(p)] = make_int4(p, r.x, r.y, 0);
+    return r;
+}
+
+// Prediction of macroblock k from the vector words s, read by ld (left, above, above-right).
+template <typename Ld>
+__device__ __forceinline__ int h263v2_pred(int k, int cols, Ld&& ld)
+{
+    const int r = k / cols, c = k - r * cols;
+    const int a = c > 0 ? ld(k - 1) : 0;
+    if (r == 0) return a;
+    return h263_median(false, a, ld(k - cols), c + 1 < cols ? ld(k - cols + 1) : 0);
+}
+
+// The search at prediction (0, 0) of every macroblock and its choice there: the first state.
+__global__ void __launch_bounds__(256) k_v263_search(V263 v)
+{
+    __shared__ Lattice lt;  // never touched by the H.263 search (no sub-pel lattice)
+    const int lane = threadIdx.x & 31, k = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (k >= v.m.nmb) return;
+    bool bad = false;
+    const int pl[6] = {0, 0, 0, 0, 0, 0};
+    const int mbr = k / v.m.cols, mbc = k - mbr * v.m.cols;
+    const MbSearch s = h263v2_search(v.m, lt, mbr, mbc, pl, lane, bad);
+    const int2 r = h263v2_choose(s, 0, s.zero_d);  // at (0, 0) the prediction's distortion is the zero vector's
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        if (bad) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
+        v.s0[k] = make_int4(pack_mv(s.mvx, s.mvy), s.min_d, s.zero_d, s.tie);
+        v.state[k] = r.x;
+        v.rec[(size_t)k * kV2Rec + rec_slot(0)] = make_int4(0, r.x, r.y, 0);
+    }
+}
+
+// One relaxation sweep: every macroblock at the prediction of the current vectors (updated in place);
+// a sweep after one that changed nothing returns at once.
+__global__ void __launch_bounds__(256) k_v263_sweep(V263 v, int sweep)
+{
+    __shared__ Lattice lt;
+    if (sweep > 0 && __ldcg(v.changed + sweep - 1) == 0) return;
+    const int lane = threadIdx.x & 31;
+    int changed = 0;
+    bool bad = false;
+    for (int k = blockIdx.x * 8 + (threadIdx.x >> 5); k < v.m.nmb; k += gridDim.x * 8) {
+        const int p = h263v2_pred(k, v.m.cols, [&](int i) { return __ldcg(v.state + i); });
+        const int mbr = k / v.m.cols;
+        const int2 r = h263v2_eval(v, lt, k, mbr, k - mbr * v.m.cols, p, false, lane, bad);
+        if (lane == 0 && r.x != __ldcg(v.state + k)) {
+            __stcg(v.state + k, r.x);
+            changed++;
+        }
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        if (bad) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
+        if (changed) atomicAdd(v.changed + sweep, changed);
+    }
+}
+
+__device__ __forceinline__ bool v263_relaxed(const V263& v)
+{
+    return v.sweeps > 0 && __ldcg(v.changed + v.sweeps - 1) == 0;
+}
+
+// The exact result by dataflow over the anti-diagonal order (c + 2r; every neighbour a prediction reads
+// has a lower ticket, and a ticket is only taken by a running warp, so every wait ends).  A warp takes
+// the next ticket, waits for the neighbours' published vectors (lanes 0..2, bounded, giving up at once
+// when another warp gave up), evaluates (a record from the sweeps when the prediction was met there)
+// and publishes its vector.
+__global__ void __launch_bounds__(128) k_v263_wave(V263 v)
+{
+    __shared__ Lattice lt;
+    if (v263_relaxed(v)) return;
+    const int lane = threadIdx.x & 31, cols = v.m.cols, nmb = v.m.nmb;
+    volatile int* status = &v.m.ctrl->status;
+    bool bad = false;
+    while (true) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&v.m.ctrl->ticket, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= nmb) break;
+        const int k = __ldg(v.order + t), r = k / cols, c = k - r * cols;
+        int nb = -1;
+        if (lane == 0 && c > 0) nb = k - 1;
+        if (lane == 1 && r > 0) nb = k - cols;
+        if (lane == 2 && r > 0 && c + 1 < cols) nb = k - cols + 1;
+        int w = 0;
+        if (nb >= 0) {
+            long long it = 0;
+            while ((w = ld_relaxed_b32(v.wave + nb)) == kV2Empty) {
+                if ((++it & 63) == 0 && ((*status & ST_TIMEOUT) || it > v.spin_limit)) {
+                    atomicOr(&v.m.ctrl->status, ST_TIMEOUT);
+                    w = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        const int a = __shfl_sync(0xffffffffu, w, 0), b = __shfl_sync(0xffffffffu, w, 1),
+                  cc = __shfl_sync(0xffffffffu, w, 2);
+        const int p = h263_median(r == 0, a, b, cc);
+        const int2 res = h263v2_eval(v, lt, k, r, c, p, false, lane, bad);
+        if (lane == 0) st_relaxed_b32(v.wave + k, res.x);
+        __syncwarp();
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
+}
+
+// Outputs: every macroblock's vector and distortion at its final prediction (a record), the
+// macroblocks of a partial bottom row evaluated at the prediction of list position N_MB (vecPos stops
+// there, …:1137-1143) for the average only, and the included sums (all macroblocks when
+// pDistortionIncluded is NULL, …:1095-1101).
+__global__ void __launch_bounds__(256) k_v263_outputs(V263 v)
+{
+    __shared__ Lattice lt;
+    if (*((volatile int*)&v.m.ctrl->status) & ST_TIMEOUT) return;
+    const int* fin = v263_relaxed(v) ? v.state : v.wave;
+    const int lane = threadIdx.x & 31, cols = v.m.cols, nmb = v.m.nmb;
+    const int k = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (k >= cols * v.m.rows_all) return;
+    const bool ghost = k >= nmb;
+    if (ghost && v.m.incl) return;  // pDistortionIncluded[N_MB] is past its end: not included
+    bool bad = false;
+    int p;
+    if (ghost) {
+        const int top = nmb - cols;  // H263MotionVectorPredictorImpl1 at blk = N_MB: row N_MB / cols, column 0
+        p = top < 0 ? 0 : h263_median(false, 0, __ldcg(fin + top), cols > 1 ? __ldcg(fin + top + 1) : 0);
+    } else {
+        p = h263v2_pred(k, cols, [&](int i) { return __ldcg(fin + i); });
+    }
+    const int mbr = k / cols;
+    const int2 r = h263v2_eval(v, lt, k, mbr, k - mbr * cols, p, ghost, lane, bad);
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        if (bad) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
+        if (!ghost) {
+            v.m.out_mv[k] = r.x;
+            if (v.m.out_dist) v.m.out_dist[k] = r.y;
+        }
+        if (ghost || !v.m.incl || v.m.incl[k]) {
+            atomicAdd(reinterpret_cast<unsigned long long*>(&v.m.ctrl->total), (unsigned long long)(long long)r.y);
+            atomicAdd(&v.m.ctrl->count, 1);
+        }
+        if (k == 0) {  // sweeps to the fixed point, or 1000 + the sweeps run when the dataflow pass decided
+            int used = 1000 + v.sweeps;
+            for (int s = 0; s < v.sweeps; s++)
+                if (__ldcg(v.changed + s) == 0) {
+                    used = s + 1;
+                    break;
+                }
+            v.m.ctrl->sweeps = used;
+        }
+    }
+}
+
 }  // namespace
 
 size_t mrc_scratch_bytes(int W, int H)
@@ -343,6 +664,45 @@ int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, cons
     }
     VPP_CHECK_LAUNCH(ctx);
     return full_resolve_launch(ctx, args, 0, est);
+}
+
+int h263v2_launch(vppgpu_ctx* ctx, const H263V2Job& j)
+{
+    MrcArgs m = mrc_args(j.W, j.H, 2 * j.motion_range, j.mode, j.scratch);
+    m.incl = j.incl;
+    m.out_mv = j.out_mv;
+    m.out_dist = j.out_dist;
+    m.out_avg = j.out_avg;
+    m.ctrl = j.ctrl;
+    int rc = levels_launch(ctx, m, j.src16, j.ref16);
+    if (rc) return rc;
+    V263 v;
+    v.m = m;
+    v.s0 = j.s0;
+    v.state = j.state;
+    v.wave = j.wave;
+    v.rec = j.rec;
+    v.changed = j.changed;
+    v.order = j.order;
+    v.sweeps = j.sweeps;
+    v.spin_limit = 20000000LL;  // ~2 s of polling before a wait gives up
+    VPP_CUDA(cudaMemsetAsync(j.rec, 0x7f, sizeof(int4) * kV2Rec * (size_t)m.nmb, ctx->stream));
+    VPP_CUDA(cudaMemsetAsync(j.wave, 0x7f, sizeof(int) * (size_t)m.nmb, ctx->stream));
+    VPP_CUDA(cudaMemsetAsync(j.changed, 0, sizeof(int) * (size_t)(j.sweeps > 0 ? j.sweeps : 1), ctx->stream));
+    const int blocks = (m.nmb + 7) / 8;
+    k_v263_search<<<blocks, 256, 0, ctx->stream>>>(v);
+    VPP_CHECK_LAUNCH(ctx);
+    for (int s = 0; s < j.sweeps; s++) {
+        k_v263_sweep<<<blocks, 256, 0, ctx->stream>>>(v, s);
+        VPP_CHECK_LAUNCH(ctx);
+    }
+    k_v263_wave<<<j.wave_grid, 128, 0, ctx->stream>>>(v);
+    VPP_CHECK_LAUNCH(ctx);
+    k_v263_outputs<<<(m.cols * m.rows_all + 7) / 8, 256, 0, ctx->stream>>>(v);
+    VPP_CHECK_LAUNCH(ctx);
+    k_mrc_average<<<1, 1, 0, ctx->stream>>>(j.out_avg, j.ctrl);
+    VPP_CHECK_LAUNCH(ctx);
+    return VPPGPU_OK;
 }
 
 }  // namespace vppgpu

@@ -110,6 +110,18 @@ int vppgpu_ctx_launch_count(vppgpu_ctx* ctx, unsigned long long* count);
  * origin; HalfRead half pel; the weighted zero-vector choice.  Vectors in HALF
  * pels, as for VPPGPU_ME_IMPL1. */
 #define VPPGPU_ME_IMPL2             10
+/* MotionEstimatorH263ImplMultiresCrossVer2
+ * (src/CodecUtils/MotionEstimatorH263ImplMultiresCrossVer2.cpp:537-1151) with
+ * H263MotionVectorPredictorImpl1 (src/CodecUtils/H263MotionVectorPredictorImpl1.cpp:72-128):
+ * the H.263 MultiresCross search with ties decided towards the prediction of
+ * each level, then the better of the prediction (clamped, HalfRead for its
+ * half-pel part) and the zero vector against the searched vector.  Motion
+ * range (<= 64) and vectors in half pels; avg_distortion over every macroblock
+ * when incl is NULL (the partial bottom row's too).  The prediction is the
+ * H.263 median of the vectors this estimate writes (left; above; above-right,
+ * zero beyond the right edge; the left one in the top row): there is no
+ * predictor object to pass and slice maps are ignored. */
+#define VPPGPU_ME_H263_MULTIRES_CROSS_V2 11
 
 typedef struct vppgpu_me vppgpu_me;
 
