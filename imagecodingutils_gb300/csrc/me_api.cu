@@ -224,10 +224,11 @@ int run(vppgpu_me* me, const short* d_src16, const short* d_ref16, const unsigne
     vppgpu_ctx* ctx = me->ctx;
     VPP_CUDA(cudaMemsetAsync(me->ctrl, 0, sizeof(vppgpu::MeCtrl), ctx->stream));
     if (me->kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2) {
-        const vppgpu::H263V2Job j{me->W,      me->H,         me->motion_range, me->mode,           me->relax_sweeps,
-                                  me->wave_grid, d_src16,    d_ref16,          me->d_mrc,          d_incl,
-                                  d_mv,       d_dist,        d_avg,            me->ctrl,           (int4*)me->spec,
-                                  me->state,  me->state + me->nmb, me->d_urec, me->changed,        me->d_uorder};
+        const vppgpu::H263V2Job j{me->W,      me->H,      me->motion_range, me->mode,      me->relax_sweeps,
+                                  d_src16,    d_ref16,    me->d_mrc,        d_incl,        d_mv,
+                                  d_dist,     d_avg,      me->ctrl,         (int4*)me->spec, me->state,
+                                  me->state + me->nmb,    me->d_urec,       me->changed,   me->d_wave_choice,
+                                  me->tie_list, me->d_tie_runs, 2 * ctx->sm_count};
         return vppgpu::h263v2_launch(ctx, j);
     }
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS)
@@ -489,14 +490,17 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
     }
     if (kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2) {
         // MotionEstimatorH263ImplMultiresCrossVer2(…, pMVPred, pDistortionIncluded) + Create(): the level
-        // planes, the searches at prediction (0, 0), relaxation and dataflow vectors, records, the
-        // dataflow order
-        me->relax_sweeps = 8;
+        // planes, the searches at prediction (0, 0) and tie trees, relaxation and exact-pass vectors,
+        // records, the sweeps' work lists
+        const size_t nall = (size_t)me->cols * ((height + 15) / 16);  // a partial bottom row searched too
+        me->relax_sweeps = vppgpu::UMHS_SWEEPS;
+        if (me->sweep_limit < 32 + vppgpu::UMHS_SWEEPS) me->sweep_limit = 32 + vppgpu::UMHS_SWEEPS;
         if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
             (rc = dalloc(&me->d_mrc, vppgpu::mrc_scratch_bytes(width, height))) ||
-            (rc = dalloc(&me->spec, 4 * (size_t)me->nmb)) || (rc = dalloc(&me->state, 2 * (size_t)me->nmb)) ||
+            (rc = dalloc(&me->spec, 4 * nall)) || (rc = dalloc(&me->state, 2 * (size_t)me->nmb)) ||
             (rc = dalloc(&me->d_urec, (size_t)me->nmb * vppgpu::H263V2_RECORDS)) ||
-            (rc = dalloc(&me->d_uorder, me->nmb)) || (rc = dalloc(&me->changed, (size_t)me->sweep_limit)) ||
+            (rc = dalloc(&me->changed, (size_t)me->sweep_limit)) || (rc = dalloc(&me->tie_list, nall)) || (rc = dalloc(&me->d_wave_choice, 3 * (size_t)me->nmb)) ||
+            (rc = dalloc((unsigned char**)&me->d_tie_runs, vppgpu::mrc_tie_runs_bytes() * nall)) ||
             (rc = dalloc(&me->d_out_mv, me->nmb)) || (rc = dalloc(&me->d_out_dist, me->nmb)) ||
             (rc = dalloc(&me->d_out_avg, 1)) || (rc = dalloc(&me->d_incl, me->nmb)) ||
             (rc = dalloc(&me->d_slice, me->nmb)) || (rc = dalloc(&me->ctrl, 1))) {
@@ -507,7 +511,7 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
             me_free(me);
             return VPPGPU_ERR_OUT_OF_MEMORY;
         }
-        if ((rc = upload_diagonal_order(me))) {
+        if ((rc = vppgpu::h263v2_prepare())) {
             me_free(me);
             return rc;
         }
@@ -799,7 +803,10 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 
 extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
 {
-    if (!me || sweeps < 0 || sweeps > (searches_from_prediction(me->kind) ? vppgpu::UMHS_SWEEPS : vppgpu::RELAX_SWEEPS))
+    if (!me || sweeps < 0 ||
+        sweeps > ((searches_from_prediction(me->kind) || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2)
+                      ? vppgpu::UMHS_SWEEPS
+                      : vppgpu::RELAX_SWEEPS))
         return VPPGPU_ERR_INVALID_ARG;
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS ||
         me->kind == VPPGPU_ME_FULL_SAD || me->kind == VPPGPU_ME_IMPL1 || me->kind == VPPGPU_ME_IMPL2)
@@ -866,8 +873,8 @@ extern "C" int vppgpu_me_autotune_pairs(vppgpu_me* me, const short* const* d_src
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS) {
         for (int w : {2, 4, 8})
             if (w != cur.warps) cands.push_back({cur.relax, cur.grid, cur.bps, w});
-    } else if (me->kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2) {  // the sweeps before the dataflow pass
-        for (int r : {0, 2, 4, 8, 14})
+    } else if (me->kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2) {  // the sweeps before the exact pass
+        for (int r : {4, 8, 14, 20, 24})
             if (r != cur.relax) cands.push_back({r, cur.grid, cur.bps, cur.warps});
     } else if (searches_from_prediction(me->kind)) {  // only the sweeps before the dataflow pass matter
         for (int r : {4, 8, 12, 16, 20, 24})

@@ -20,6 +20,7 @@ struct MeCtrl {
     int wave_miss;   // MBs the wavefront had to evaluate in full
     int ntie;        // entries of FullArgs::tie_list
     int ticket;      // MultiresCrossVer2 dataflow pass: next macroblock
+    int tie_mbs;     // H263 MultiresCrossVer2: entries of its tie list
 };
 
 constexpr int KCACHE = 32;  // records per macroblock
@@ -119,11 +120,12 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
                MeCtrl* ctrl, int warps = 8, bool h263 = false);
 
 // MotionEstimatorH263ImplMultiresCrossVer2 (me_mrc.cu): the level planes in `scratch`
-// (mrc_scratch_bytes), per-MB search results (s0), relaxation and dataflow vectors, records
-// (H263V2_RECORDS per MB), per-sweep change counts, the dataflow order; motion_range in half pels.
+// (mrc_scratch_bytes), per-MB search results (s0; tie_list and tie_runs too: every macroblock of
+// (H + 15) / 16 rows), relaxation and exact-pass vectors, records (H263V2_RECORDS per MB), per-sweep
+// change counts and work lists; motion_range in half pels.
 constexpr int H263V2_RECORDS = 4;
 struct H263V2Job {
-    int W, H, motion_range, mode, sweeps, wave_grid;
+    int W, H, motion_range, mode, sweeps;
     const short* src16;
     const short* ref16;
     unsigned char* scratch;
@@ -136,10 +138,14 @@ struct H263V2Job {
     int* state;
     int* wave;
     int4* rec;
-    int* changed;
-    const int* order;
+    int* changed;    // at least 32 + UMHS_SWEEPS entries
+    int* lists;      // 3 * N_MB: the sweeps' work lists and queue marks
+    int* tie_list;   // macroblocks whose search at (0, 0) met a tie
+    void* tie_runs;  // their tie trees (mrc_tie_runs_bytes() per MB)
+    int tree_grid;   // CTAs of the tie-tree kernel
 };
 int h263v2_launch(vppgpu_ctx* ctx, const H263V2Job& j);
+int h263v2_prepare();  // once per process before the first launch (shared-memory limit)
 
 // Device address of the status word (ST_* bits) of a handle's current
 // estimate, and the C ABI status those bits stand for.

@@ -224,11 +224,11 @@ __global__ void k_set_mrc(MrcArgs* dst, MrcArgs v) { *dst = v; }
 // accept rule) is a function of the prediction, which H263MotionVectorPredictorImpl1 takes from the
 // vectors written so far: a DAG in raster order, as for the H.264 predictor estimators.  Every
 // macroblock is searched at prediction (0, 0); a search whose ties never involved a level where the
-// prediction differs from zero holds for every prediction.  Relaxation sweeps then evaluate every
-// macroblock at the prediction its neighbours' current vectors give (results kept as records keyed
-// by the prediction) until a sweep changes nothing, which is the unique fixed point of the DAG and
-// so the sequential result; otherwise a dataflow pass over the anti-diagonal order decides the
-// frame exactly.
+// prediction differs from zero holds for every prediction, and for the others a tie tree answers for
+// any prediction.  Relaxation sweeps then evaluate the macroblocks at the prediction their
+// neighbours' current vectors give (results kept as records keyed by the prediction) until a sweep
+// changes nothing, which is the unique fixed point of the DAG and so the sequential result;
+// otherwise a one-CTA pass over the anti-diagonals decides the frame exactly.
 constexpr int kV2Rec = H263V2_RECORDS;   // records per macroblock: {prediction, vector, distortion, 0}
 constexpr int kV2Empty = 0x7f7f7f7f;     // no half-pel vector packs to this (memset byte 0x7f)
 
@@ -236,24 +236,14 @@ struct V263 {
     MrcArgs m;
     int4* s0;           // per MB: searched vector at prediction (0, 0), its distortion, zero-vector distortion, ties
     int* state;         // per MB: relaxation's current vector (packed half pels)
-    int* wave;          // per MB: the dataflow pass's vector, kV2Empty until published
+    int* wave;          // per MB: the exact pass's vector
     int4* rec;          // kV2Rec per MB
-    int* changed;       // vectors changed per sweep
-    const int* order;   // dataflow ticket -> macroblock
+    int* changed;       // vectors changed per sweep, then (from kListLen) each sweep's work-list length
+    int* lists;         // two work lists of nmb macroblocks (sweeps alternate), then nmb queue marks
+    int* tie_list;      // macroblocks whose search at (0, 0) met a tie
+    V2TieRun* runs;     // V2_TIE_RUNS per macroblock: the tie trees of those
     int sweeps;
-    long long spin_limit;
 };
-
-__device__ __forceinline__ int ld_relaxed_b32(const int* p)
-{
-    int v;
-    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_relaxed_b32(int* p, int v)
-{
-    asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 // H263MotionVectorPredictorImpl1::Get16x16Prediction (…H263MotionVectorPredictorImpl1.cpp:72-128) from
 // the left (a), above (b) and above-right (c) vectors, each 0 beyond the picture's side: the left one
@@ -347,15 +337,112 @@ __device__ __forceinline__ int2 h263v2_choose(const MbSearch& s, int pv, int pre
     return make_int2(zv, zd);
 }
 
+// Tie tree of a macroblock (V2TieRun, as the H.264 Ver2 trees): run `run` of eight decides its t-th tie
+// (t < 3) by bit t of run (1 takes the candidate) and records the tie's level and the two vectors
+// compared, current (cx, cy) and candidate (nx, ny) in level units.
+__device__ void h263v2_run(const MrcArgs& a, Lattice& lt, int mbr, int mbc, int run, V2TieRun* rec, int lane,
+                           bool& bad)
+{
+    int t = 0, lvls = 0, geo[V2_TIE_BITS] = {0, 0, 0};
+    bool wide = false;
+    auto skip = [&](int lvl, int mx, int my, int rmx, int rmy, int j, int i) {
+        const int cx = mx + rmx, cy = my + rmy, nx = mx + j, ny = my + i;
+        const bool take = t < V2_TIE_BITS ? ((run >> t) & 1) : true;
+        if (t < V2_TIE_BITS) {
+            wide |= (unsigned)(cx + 128) > 255u || (unsigned)(cy + 128) > 255u || (unsigned)(nx + 128) > 255u ||
+                    (unsigned)(ny + 128) > 255u;
+            geo[t] = (cx & 0xff) | ((cy & 0xff) << 8) | ((nx & 0xff) << 16) | ((ny & 0xff) << 24);
+            lvls |= lvl << (2 * t);
+        }
+        t++;
+        return !take;
+    };
+    const MbSearch r = search_mb_with<false, decltype(skip)&, true>(a, lt, mbr, mbc, skip, lane, bad);
+    if (lane == 0) {
+        for (int e = 0; e < V2_TIE_BITS; e++) rec->geo[e] = geo[e];
+        rec->lvl = lvls;
+        rec->nev = wide ? 1000 : t;
+        rec->mv = pack_mv(r.mvx, r.mvy);
+        rec->min_d = r.min_d;
+    }
+}
+
+// The searched vector and distortion for level predictions pl from a tie tree (the estimator's
+// y-sum rule at every recorded tie); false when the tree is too deep.  Lane i < 8 loads run i, so the
+// walk costs one round trip.  One warp.
+__device__ __forceinline__ bool h263v2_tree(const V2TieRun* runs, const int* pl, int lane, int* mv, int* min_d)
+{
+    static_assert(kV2Rec == 4, "rec_slot picks one of 4");
+    static_assert(sizeof(V2TieRun) == 32, "two 16-byte words per run");
+    int4 a = make_int4(0, 0, 0, 0), b = make_int4(0, 0, 0, 0);  // {geo0, geo1, geo2, lvl}, {nev, mv, min_d, -}
+    if (lane < V2_TIE_RUNS) {
+        const int4* w = reinterpret_cast<const int4*>(runs + lane);
+        a = __ldcg(w);
+        b = __ldcg(w + 1);
+    }
+    int run = 0;
+    for (int t = 0; t < V2_TIE_BITS; t++) {
+        if (t >= __shfl_sync(0xffffffffu, b.x, run)) break;
+        const int g = __shfl_sync(0xffffffffu, t == 0 ? a.x : (t == 1 ? a.y : a.z), run);
+        const int lvl = (__shfl_sync(0xffffffffu, a.w, run) >> (2 * t)) & 3;
+        const int cx = (signed char)(g & 0xff), cy = (signed char)((g >> 8) & 0xff);
+        const int nx = (signed char)((g >> 16) & 0xff), ny = (signed char)(g >> 24);
+        const int px = pl[2 * lvl], py = pl[2 * lvl + 1];
+        const bool skip = (cy - py) * (cy - py) + (cx - px) * (cx - px) < (ny + py) * (ny + py) + (nx - px) * (nx - px);
+        run |= (skip ? 0 : 1) << t;
+    }
+    if (__shfl_sync(0xffffffffu, b.x, run) > V2_TIE_BITS) return false;
+    *mv = __shfl_sync(0xffffffffu, b.y, run);
+    *min_d = __shfl_sync(0xffffffffu, b.z, run);
+    return true;
+}
+
 __device__ __forceinline__ unsigned rec_slot(int p) { return ((unsigned)p * 2654435761u) >> 30; }
 
-// Vector and distortion of macroblock k (row mbr, column mbc) at prediction p: its record, else the
-// search at (0, 0) where that search's ties do not involve the prediction, else a search at p; then the
-// choice, recorded.  One warp.  ghost: a macroblock of a partial bottom row (no record, no search at
-// (0, 0)).
-__device__ int2 h263v2_eval(const V263& v, Lattice& lt, int k, int mbr, int mbc, int p, bool ghost, int lane,
-                            bool& bad)
+// Vector and distortion of macroblock k (row mbr, column mbc) at prediction p given its search at
+// (0, 0), s0: that search where its ties do not involve the prediction, else the tie tree's answer,
+// else a search at p; then the choice, recorded.  One warp.  ghost: a macroblock of a partial bottom
+// row (not recorded).
+__device__ int2 h263v2_compute(const V263& v, Lattice& lt, int k, int mbr, int mbc, int p, int4 s0, bool ghost,
+                               int lane, bool& bad, int& misses, int& searches)
 {
+    const int px = mv_x(p), py = mv_y(p);
+    int pl[6];
+    h263_levels(px, py, pl);
+    MbSearch s;
+    s.mvx = mv_x(s0.x);
+    s.mvy = mv_y(s0.x);
+    s.min_d = s0.y;
+    s.zero_d = s0.z;
+    s.tie = s0.w;
+    bool reuse = true;
+    for (int l = 0; l < 3; l++)
+        if ((s.tie & (TIE_L0 >> l)) && (pl[2 * l] || pl[2 * l + 1])) reuse = false;
+    if (!reuse) {
+        int tmv, td;
+        if (h263v2_tree(v.runs + (size_t)k * V2_TIE_RUNS, pl, lane, &tmv, &td)) {
+            s.mvx = mv_x(tmv);
+            s.mvy = mv_y(tmv);
+            s.min_d = td;
+        } else {
+            s = h263v2_search(v.m, lt, mbr, mbc, pl, lane, bad);
+            searches++;
+        }
+    }
+    misses++;
+    int pv;
+    const int pd = h263v2_pred_d(v.m, mbr, mbc, px, py, lane, bad, &pv);
+    const int2 r = h263v2_choose(s, pv, pd);
+    if (!ghost && lane == 0) v.rec[(size_t)k * kV2Rec + rec_slot(p)] = make_int4(p, r.x, r.y, 0);
+    return r;
+}
+
+// The same from the macroblock's record when it holds prediction p (its records and its search at
+// (0, 0) are loaded together).
+__device__ int2 h263v2_eval(const V263& v, Lattice& lt, int k, int mbr, int mbc, int p, bool ghost, int lane,
+                            bool& bad, int& misses, int& searches)
+{
+    const int4 s0 = __ldcg(v.s0 + k);
     if (!ghost) {
         const int4 e = lane < kV2Rec ? __ldcg(v.rec + (size_t)k * kV2Rec + lane) : make_int4(kV2Empty, 0, 0, 0);
         const unsigned hit = __ballot_sync(0xffffffffu, e.x == p);
@@ -364,27 +451,7 @@ __device__ int2 h263v2_eval(const V263& v, Lattice& lt, int k, int mbr, int mbc,
             return make_int2(__shfl_sync(0xffffffffu, e.y, f), __shfl_sync(0xffffffffu, e.z, f));
         }
     }
-    const int px = mv_x(p), py = mv_y(p);
-    int pl[6];
-    h263_levels(px, py, pl);
-    MbSearch s;
-    bool reuse = !ghost;
-    if (!ghost) {
-        const int4 s0 = __ldcg(v.s0 + k);
-        s.mvx = mv_x(s0.x);
-        s.mvy = mv_y(s0.x);
-        s.min_d = s0.y;
-        s.zero_d = s0.z;
-        s.tie = s0.w;
-        for (int l = 0; l < 3; l++)
-            if ((s.tie & (TIE_L0 >> l)) && (pl[2 * l] || pl[2 * l + 1])) reuse = false;
-    }
-    if (!reuse) s = h263v2_search(v.m, lt, mbr, mbc, pl, lane, bad);
-    int pv;
-    const int pd = h263v2_pred_d(v.m, mbr, mbc, px, py, lane, bad, &pv);
-    const int2 r = h263v2_choose(s, pv, pd);
-    if (!ghost && lane == 0) v.rec[(size_t)k * kV2Rec + rec_slot(p)] = make_int4(p, r.x, r.y, 0);
-    return r;
+    return h263v2_compute(v, lt, k, mbr, mbc, p, s0, ghost, lane, bad, misses, searches);
 }
 
 // Prediction of macroblock k from the vector words s, read by ld (left, above, above-right).
@@ -397,12 +464,13 @@ __device__ __forceinline__ int h263v2_pred(int k, int cols, Ld&& ld)
     return h263_median(false, a, ld(k - cols), c + 1 < cols ? ld(k - cols + 1) : 0);
 }
 
-// The search at prediction (0, 0) of every macroblock and its choice there: the first state.
+// The search at prediction (0, 0) of every macroblock (a partial bottom row's too) and its choice
+// there: the first state.
 __global__ void __launch_bounds__(256) k_v263_search(V263 v)
 {
     __shared__ Lattice lt;  // never touched by the H.263 search (no sub-pel lattice)
     const int lane = threadIdx.x & 31, k = blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (k >= v.m.nmb) return;
+    if (k >= v.m.cols * v.m.rows_all) return;
     bool bad = false;
     const int pl[6] = {0, 0, 0, 0, 0, 0};
     const int mbr = k / v.m.cols, mbc = k - mbr * v.m.cols;
@@ -412,33 +480,69 @@ __global__ void __launch_bounds__(256) k_v263_search(V263 v)
     if (lane == 0) {
         if (bad) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
         v.s0[k] = make_int4(pack_mv(s.mvx, s.mvy), s.min_d, s.zero_d, s.tie);
-        v.state[k] = r.x;
-        v.rec[(size_t)k * kV2Rec + rec_slot(0)] = make_int4(0, r.x, r.y, 0);
+        if (s.tie) v.tie_list[atomicAdd(&v.m.ctrl->tie_mbs, 1)] = k;
+        if (k < v.m.nmb) {
+            v.state[k] = r.x;
+            v.rec[(size_t)k * kV2Rec + rec_slot(0)] = make_int4(0, r.x, r.y, 0);
+        }
     }
 }
 
-// One relaxation sweep: every macroblock at the prediction of the current vectors (updated in place);
-// a sweep after one that changed nothing returns at once.
+// The tie trees of the macroblocks whose search met a tie: warp r of a block makes run r.
+__global__ void __launch_bounds__(V2_TIE_RUNS * 32) k_v263_tietree(V263 v)
+{
+    __shared__ Lattice lt;
+    const int lane = threadIdx.x & 31, run = threadIdx.x >> 5;
+    const int n = __ldcg(&v.m.ctrl->tie_mbs);
+    bool bad = false;
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        const int k = __ldcg(v.tie_list + i), mbr = k / v.m.cols;
+        h263v2_run(v.m, lt, mbr, k - mbr * v.m.cols, run, v.runs + (size_t)k * V2_TIE_RUNS + run, lane, bad);
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
+}
+
+constexpr int kListLen = 32;  // offset of the work-list lengths in V263::changed
+
+// One relaxation sweep over the macroblocks whose prediction may have moved: every macroblock in the
+// first sweep, then those a vector change of the previous sweep reaches (its right, below-left and
+// below neighbours, queued once each), each at the prediction of the current vectors (updated in
+// place).  A sweep in which nothing changed leaves every macroblock evaluated at its current
+// prediction: the fixed point.  A sweep after one that changed nothing returns at once.
 __global__ void __launch_bounds__(256) k_v263_sweep(V263 v, int sweep)
 {
     __shared__ Lattice lt;
     if (sweep > 0 && __ldcg(v.changed + sweep - 1) == 0) return;
-    const int lane = threadIdx.x & 31;
-    int changed = 0;
+    const int lane = threadIdx.x & 31, cols = v.m.cols, rows = v.m.nmb / cols;
+    const int n = sweep == 0 ? v.m.nmb : __ldcg(v.changed + kListLen + sweep - 1);
+    const int* in = v.lists + (size_t)((sweep - 1) & 1) * v.m.nmb;
+    int* out = v.lists + (size_t)(sweep & 1) * v.m.nmb;
+    int* mark = v.lists + 2 * (size_t)v.m.nmb;
+    int changed = 0, evals = 0, misses = 0, searches = 0;
     bool bad = false;
-    for (int k = blockIdx.x * 8 + (threadIdx.x >> 5); k < v.m.nmb; k += gridDim.x * 8) {
-        const int p = h263v2_pred(k, v.m.cols, [&](int i) { return __ldcg(v.state + i); });
-        const int mbr = k / v.m.cols;
-        const int2 r = h263v2_eval(v, lt, k, mbr, k - mbr * v.m.cols, p, false, lane, bad);
+    for (int i = blockIdx.x * 8 + (threadIdx.x >> 5); i < n; i += gridDim.x * 8) {
+        const int k = sweep == 0 ? i : __ldcg(in + i);
+        const int p = h263v2_pred(k, cols, [&](int j) { return __ldcg(v.state + j); });
+        const int mbr = k / cols, mbc = k - mbr * cols;
+        const int2 r = h263v2_eval(v, lt, k, mbr, mbc, p, false, lane, bad, misses, searches);
+        evals++;
         if (lane == 0 && r.x != __ldcg(v.state + k)) {
             __stcg(v.state + k, r.x);
             changed++;
+            const int nb[3] = {mbc + 1 < cols ? k + 1 : -1, (mbr + 1 < rows && mbc > 0) ? k + cols - 1 : -1,
+                               mbr + 1 < rows ? k + cols : -1};
+            for (int e = 0; e < 3; e++)
+                if (nb[e] >= 0 && atomicExch(mark + nb[e], sweep) != sweep)
+                    out[atomicAdd(v.changed + kListLen + sweep, 1)] = nb[e];
         }
     }
     bad = __any_sync(0xffffffffu, bad);
     if (lane == 0) {
         if (bad) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
         if (changed) atomicAdd(v.changed + sweep, changed);
+        atomicAdd(&v.m.ctrl->relax_evals, evals);
+        if (misses) atomicAdd(&v.m.ctrl->relax_miss, misses);
+        if (searches) atomicAdd(&v.m.ctrl->ntie, searches);
     }
 }
 
@@ -447,48 +551,121 @@ __device__ __forceinline__ bool v263_relaxed(const V263& v)
     return v.sweeps > 0 && __ldcg(v.changed + v.sweeps - 1) == 0;
 }
 
-// The exact result by dataflow over the anti-diagonal order (c + 2r; every neighbour a prediction reads
-// has a lower ticket, and a ticket is only taken by a running warp, so every wait ends).  A warp takes
-// the next ticket, waits for the neighbours' published vectors (lanes 0..2, bounded, giving up at once
-// when another warp gave up), evaluates (a record from the sweeps when the prediction was met there)
-// and publishes its vector.
-__global__ void __launch_bounds__(128) k_v263_wave(V263 v)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
 {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// The exact result in one CTA: thread r owns macroblock row r and at step t takes column t - 2r, so a
+// step is an anti-diagonal c + 2r = t whose predictions read only earlier steps: the row's previous
+// vector (a register) and the row above's last vectors (a four-slot ring per row in shared memory; the
+// slot row r writes in step t is none of the two row r + 1 reads then).  Each row's records and search
+// at (0, 0) arrive by cp.async kDiagDepth - 1 steps ahead; a record gives the result for the
+// prediction, and the macroblocks that find none are listed in shared memory and evaluated by every
+// warp of the CTA, one macroblock per warp.  Up to three block barriers per step, no waits.
+constexpr int kDiagThreads = 512;  // rows of at most 512 macroblocks (pictures up to 8192 lines)
+constexpr int kDiagDepth = 4;      // steps of records in flight per row
+constexpr int kDiagPre = kV2Rec + 1;  // 16-byte words per row and step: the records, then the search at (0, 0)
+__host__ __device__ constexpr size_t diag_smem(int rows)
+{
+    return 16 * ((size_t)rows * kDiagDepth * kDiagPre + (size_t)rows + 1) + sizeof(int) * 7 * (size_t)rows;
+}
+__global__ void __launch_bounds__(kDiagThreads, 1) k_v263_diag(V263 v)
+{
+    extern __shared__ __align__(16) int4 dsm4[];  // prefetch slots, search-at-(0, 0) list, then the int arrays
     __shared__ Lattice lt;
+    __shared__ int s_nmiss[2];
     if (v263_relaxed(v)) return;
-    const int lane = threadIdx.x & 31, cols = v.m.cols, nmb = v.m.nmb;
-    volatile int* status = &v.m.ctrl->status;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int cols = v.m.cols, rows = v.m.nmb / cols;
+    int4* pre = dsm4;                                                  // rows x kDiagDepth x kDiagPre
+    int4* miss_s0 = pre + (size_t)rows * kDiagDepth * kDiagPre;        // rows (+1 spare)
+    int* ring = reinterpret_cast<int*>(miss_s0 + rows + 1);            // 4 per row
+    int* miss_k = ring + 4 * rows;
+    int* miss_p = miss_k + rows;
+    int* miss_v = miss_p + rows;
+    const int r = threadIdx.x;
+    const bool row_ok = r < rows;
+    int4* mine = pre + (size_t)(row_ok ? r : 0) * kDiagDepth * kDiagPre;
+    auto issue = [&](int t) {  // the records and search of this row's macroblock of step t
+        const int c = t - 2 * r;
+        if (row_ok && c >= 0 && c < cols) {
+            const size_t k = (size_t)r * cols + c;
+            int4* slot = mine + (t % kDiagDepth) * kDiagPre;
+#pragma unroll
+            for (int e = 0; e < kV2Rec; e++) cp_async16(slot + e, v.rec + k * kV2Rec + e);
+            cp_async16(slot + kV2Rec, v.s0 + k);
+        }
+        cp_async_commit();
+    };
+    if (threadIdx.x < 2) s_nmiss[threadIdx.x] = 0;
+    for (int t = 0; t < kDiagDepth - 1; t++) issue(t);
+    __syncthreads();
+    int left = 0, misses = 0, searches = 0;
     bool bad = false;
-    while (true) {
-        int t = 0;
-        if (lane == 0) t = atomicAdd(&v.m.ctrl->ticket, 1);
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= nmb) break;
-        const int k = __ldg(v.order + t), r = k / cols, c = k - r * cols;
-        int nb = -1;
-        if (lane == 0 && c > 0) nb = k - 1;
-        if (lane == 1 && r > 0) nb = k - cols;
-        if (lane == 2 && r > 0 && c + 1 < cols) nb = k - cols + 1;
-        int w = 0;
-        if (nb >= 0) {
-            long long it = 0;
-            while ((w = ld_relaxed_b32(v.wave + nb)) == kV2Empty) {
-                if ((++it & 63) == 0 && ((*status & ST_TIMEOUT) || it > v.spin_limit)) {
-                    atomicOr(&v.m.ctrl->status, ST_TIMEOUT);
-                    w = 0;
-                    break;
+    const int steps = cols + 2 * (rows - 1);
+    for (int t = 0; t < steps; t++) {
+        issue(t + kDiagDepth - 1);
+        cp_async_wait<kDiagDepth - 1>();  // this thread's copies of step t have landed
+        const int c = t - 2 * r;
+        const bool act = row_ok && c >= 0 && c < cols;
+        const int k = r * cols + c;
+        int mv = 0, slot = -1;
+        if (act) {
+            const int4* cur = mine + (t % kDiagDepth) * kDiagPre;
+            const int b = r > 0 ? ring[(r - 1) * 4 + (c & 3)] : 0;
+            const int cc = (r > 0 && c + 1 < cols) ? ring[(r - 1) * 4 + ((c + 1) & 3)] : 0;
+            const int p = h263_median(r == 0, c > 0 ? left : 0, b, cc);
+            bool hit = false;
+#pragma unroll
+            for (int e = 0; e < kV2Rec; e++) {
+                const int4 rec = cur[e];
+                if (!hit && rec.x == p) {
+                    hit = true;
+                    mv = rec.y;
                 }
-                __nanosleep(32);
+            }
+            if (!hit) {
+                slot = atomicAdd(&s_nmiss[t & 1], 1);
+                miss_k[slot] = k;
+                miss_p[slot] = p;
+                miss_s0[slot] = cur[kV2Rec];
             }
         }
-        const int a = __shfl_sync(0xffffffffu, w, 0), b = __shfl_sync(0xffffffffu, w, 1),
-                  cc = __shfl_sync(0xffffffffu, w, 2);
-        const int p = h263_median(r == 0, a, b, cc);
-        const int2 res = h263v2_eval(v, lt, k, r, c, p, false, lane, bad);
-        if (lane == 0) st_relaxed_b32(v.wave + k, res.x);
-        __syncwarp();
+        __syncthreads();
+        const int n = s_nmiss[t & 1];
+        if (threadIdx.x == 0) s_nmiss[(t + 1) & 1] = 0;  // untouched until after this step's last barrier
+        if (n) {
+            for (int i = wid; i < n; i += nw) {
+                const int kk = miss_k[i], mbr = kk / cols;
+                const int2 res = h263v2_compute(v, lt, kk, mbr, kk - mbr * cols, miss_p[i], miss_s0[i], false, lane,
+                                                bad, misses, searches);
+                if (lane == 0) miss_v[i] = res.x;
+            }
+            __syncthreads();
+            if (slot >= 0) mv = miss_v[slot];
+        }
+        if (act) {
+            left = mv;
+            ring[r * 4 + (c & 3)] = mv;
+            __stcg(v.wave + k, mv);
+        }
+        __syncthreads();
     }
-    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
+    cp_async_wait<0>();
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        if (bad) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
+        if (misses) atomicAdd(&v.m.ctrl->wave_miss, misses);
+        if (searches) atomicAdd(&v.m.ctrl->ntie, searches);
+    }
 }
 
 // Outputs: every macroblock's vector and distortion at its final prediction (a record), the
@@ -514,7 +691,8 @@ __global__ void __launch_bounds__(256) k_v263_outputs(V263 v)
         p = h263v2_pred(k, cols, [&](int i) { return __ldcg(fin + i); });
     }
     const int mbr = k / cols;
-    const int2 r = h263v2_eval(v, lt, k, mbr, k - mbr * cols, p, ghost, lane, bad);
+    int misses = 0, searches = 0;
+    const int2 r = h263v2_eval(v, lt, k, mbr, k - mbr * cols, p, ghost, lane, bad, misses, searches);
     bad = __any_sync(0xffffffffu, bad);
     if (lane == 0) {
         if (bad) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
@@ -526,7 +704,7 @@ __global__ void __launch_bounds__(256) k_v263_outputs(V263 v)
             atomicAdd(reinterpret_cast<unsigned long long*>(&v.m.ctrl->total), (unsigned long long)(long long)r.y);
             atomicAdd(&v.m.ctrl->count, 1);
         }
-        if (k == 0) {  // sweeps to the fixed point, or 1000 + the sweeps run when the dataflow pass decided
+        if (k == 0) {  // sweeps to the fixed point, or 1000 + the sweeps run when the exact pass decided
             int used = 1000 + v.sweeps;
             for (int s = 0; s < v.sweeps; s++)
                 if (__ldcg(v.changed + s) == 0) {
@@ -666,6 +844,13 @@ int mrc2_launch(vppgpu_ctx* ctx, int est, int mode, unsigned char* scratch, cons
     return full_resolve_launch(ctx, args, 0, est);
 }
 
+int h263v2_prepare()
+{
+    VPP_CUDA(cudaFuncSetAttribute(k_v263_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)diag_smem(kDiagThreads)));
+    return VPPGPU_OK;
+}
+
 int h263v2_launch(vppgpu_ctx* ctx, const H263V2Job& j)
 {
     MrcArgs m = mrc_args(j.W, j.H, 2 * j.motion_range, j.mode, j.scratch);
@@ -683,20 +868,24 @@ int h263v2_launch(vppgpu_ctx* ctx, const H263V2Job& j)
     v.wave = j.wave;
     v.rec = j.rec;
     v.changed = j.changed;
-    v.order = j.order;
+    v.lists = j.lists;
+    v.tie_list = j.tie_list;
+    v.runs = static_cast<V2TieRun*>(j.tie_runs);
     v.sweeps = j.sweeps;
-    v.spin_limit = 20000000LL;  // ~2 s of polling before a wait gives up
     VPP_CUDA(cudaMemsetAsync(j.rec, 0x7f, sizeof(int4) * kV2Rec * (size_t)m.nmb, ctx->stream));
-    VPP_CUDA(cudaMemsetAsync(j.wave, 0x7f, sizeof(int) * (size_t)m.nmb, ctx->stream));
-    VPP_CUDA(cudaMemsetAsync(j.changed, 0, sizeof(int) * (size_t)(j.sweeps > 0 ? j.sweeps : 1), ctx->stream));
-    const int blocks = (m.nmb + 7) / 8;
-    k_v263_search<<<blocks, 256, 0, ctx->stream>>>(v);
+    VPP_CUDA(cudaMemsetAsync(j.changed, 0, sizeof(int) * (size_t)(kListLen + UMHS_SWEEPS), ctx->stream));
+    VPP_CUDA(cudaMemsetAsync(j.lists + 2 * (size_t)m.nmb, 0xff, sizeof(int) * (size_t)m.nmb, ctx->stream));
+    // later sweeps walk short work lists: a grid of a few CTAs per SM strides over them
+    const int blocks = min((m.nmb + 7) / 8, 4 * ctx->sm_count);
+    k_v263_search<<<(m.cols * m.rows_all + 7) / 8, 256, 0, ctx->stream>>>(v);
+    VPP_CHECK_LAUNCH(ctx);
+    k_v263_tietree<<<j.tree_grid, V2_TIE_RUNS * 32, 0, ctx->stream>>>(v);
     VPP_CHECK_LAUNCH(ctx);
     for (int s = 0; s < j.sweeps; s++) {
         k_v263_sweep<<<blocks, 256, 0, ctx->stream>>>(v, s);
         VPP_CHECK_LAUNCH(ctx);
     }
-    k_v263_wave<<<j.wave_grid, 128, 0, ctx->stream>>>(v);
+    k_v263_diag<<<1, kDiagThreads, diag_smem(m.nmb / m.cols), ctx->stream>>>(v);
     VPP_CHECK_LAUNCH(ctx);
     k_v263_outputs<<<(m.cols * m.rows_all + 7) / 8, 256, 0, ctx->stream>>>(v);
     VPP_CHECK_LAUNCH(ctx);

@@ -391,6 +391,30 @@ public:
     }
 };
 
+// MotionEstimatorH263ImplMultiresCrossVer2 (src/CodecUtils/MotionEstimatorH263ImplMultiresCrossVer2.cpp):
+// motionRange (at most 64) and the vectors in half pels.  The reference asks its predictor
+// (an H263MotionVectorPredictorImpl1) for the H.263 median of the vectors it has written; the device
+// computes that median itself, so pMVPred is taken for the signature and not called (the reference
+// never sets vectors on it either).
+class GpuMotionEstimatorH263ImplMultiresCrossVer2 : public GpuMotionEstimatorH264Base {
+public:
+    GpuMotionEstimatorH263ImplMultiresCrossVer2(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                                int motionRange, IMotionVectorPredictor* pMVPred)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_H263_MULTIRES_CROSS_V2, pSrc, pRef, imgWidth, imgHeight, motionRange,
+                                     NULL, NULL)
+    {
+        (void)pMVPred;
+    }
+    GpuMotionEstimatorH263ImplMultiresCrossVer2(const void* pSrc, const void* pRef, int imgWidth, int imgHeight,
+                                                int motionRange, IMotionVectorPredictor* pMVPred,
+                                                void* pDistortionIncluded)
+        : GpuMotionEstimatorH264Base(VPPGPU_ME_H263_MULTIRES_CROSS_V2, pSrc, pRef, imgWidth, imgHeight, motionRange,
+                                     NULL, pDistortionIncluded)
+    {
+        (void)pMVPred;
+    }
+};
+
 // The integer-pel stage of MotionEstimatorH264ImplFull with its MEH264IF_ABS_DIFF
 // distortion (MotionEstimatorH264ImplFull.cpp:341-446, OverlayMem2Dv2::Tad16x16 /
 // Tad16x16LessThan): full-pel winners in quarter pels, their SAD as distortion.
