@@ -9,7 +9,7 @@
 // and the zero vector (:356-378).  There is no predictor, so every block is
 // independent: one warp per block, its search window (rows and columns
 // -R-1 .. R+B of the padded reference) and template staged in shared memory,
-// one lane per candidate.  The reference's raster scan keeps the first
+// one lane per candidate column.  The reference's raster scan keeps the first
 // strictly smaller distortion, i.e. the smallest (distortion, raster index)
 // pair below the zero vector's distortion: a warp argmin on that pair.
 #include "me_full_common.cuh"
@@ -131,14 +131,77 @@ __global__ void __launch_bounds__(32 * kWarps) k_impl1(Impl1Args g)
         for (int r = 0; r < BH; r++) acc = row_sd<BW>(p + r * kWinStride, tmpl + 4 * r, acc);
         return (int)acc;
     };
-    // full search: lane-strided raster candidates, the smallest (distortion, index)
-    const int side = 2 * R, ncand = side * side;
+    // full search, the smallest (distortion, raster index): lane l takes the candidate columns
+    // x = -R + l (+ 32) and eight candidate rows at a time.  SSD = A^2 + B^2 - 2 sum(ab): the cross
+    // terms one dp4a per four pixels, B^2 of each candidate from the energies of its window rows,
+    // A^2 once per block.  Each window row is aligned once for the lane's column (funnel shifts)
+    // into a ring of eight rows, its energy added to the candidates that cover it; template row r
+    // then scores the eight candidates of rows y .. y+7 against ring rows y+r .. y+r+7.  Rows and
+    // columns past the range are scored from bytes inside the slot and dropped.
+    const int side = 2 * R;
+    constexpr int WPR = BW / 4;  // words per block row
+    unsigned a2u = 0u;
+#pragma unroll
+    for (int r = 0; r < BH; r++)
+#pragma unroll
+        for (int w = 0; w < WPR; w++) a2u = __dp4a(tmpl[4 * r + w], tmpl[4 * r + w], a2u);
+    const int a2 = (int)a2u;
     int best_d = 0x7fffffff, best_c = 0x7fffffff;
-    for (int c = lane; c < ncand; c += 32) {
-        const int d = block_sd(c % side - R, c / side - R);
-        if (d < best_d) {  // a lane's candidates rise in index: strict keeps its first minimum
-            best_d = d;
-            best_c = c;
+    for (int xc = 0; xc < side; xc += 32) {
+        const int x = xc + lane - R;
+        const unsigned char* col = base + x;
+        const unsigned* wp = reinterpret_cast<const unsigned*>(reinterpret_cast<uintptr_t>(col) & ~(uintptr_t)3);
+        const unsigned sh = (unsigned)(reinterpret_cast<uintptr_t>(col) & 3) * 8;
+        constexpr int kStrideW = kWinStride / 4;
+        for (int yc = 0; yc < side; yc += 8) {
+            const int y0 = yc - R;
+            unsigned al[8][WPR], acc[8], en[8];
+            // window row y0 + row at the lane's column into dst; its energy to the candidates on it
+            auto load_row = [&](unsigned* dst, int row) {
+                const unsigned* q = wp + (y0 + row) * kStrideW;
+                unsigned e = 0u;
+#pragma unroll
+                for (int i = 0; i < WPR; i++) {
+                    dst[i] = __funnelshift_r(q[i], q[i + 1], sh);
+                    e = __dp4a(dst[i], dst[i], e);
+                }
+#pragma unroll
+                for (int i = 0; i < 8; i++)
+                    if (i <= row && row - i < BH) en[i] += e;
+            };
+#pragma unroll
+            for (int i = 0; i < 8; i++) acc[i] = en[i] = 0u;
+#pragma unroll
+            for (int i = 0; i < 8; i++) load_row(al[i], i);
+#pragma unroll
+            for (int r0 = 0; r0 < BH; r0 += 8) {
+#pragma unroll
+                for (int ru = 0; ru < 8; ru++) {
+                    const int r = r0 + ru;
+                    unsigned t[WPR];
+#pragma unroll
+                    for (int i = 0; i < WPR; i++) t[i] = tmpl[4 * r + i];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        const unsigned* B = al[(i + ru) % 8];
+                        unsigned c = acc[i];
+#pragma unroll
+                        for (int w = 0; w < WPR; w++) c = __dp4a(t[w], B[w], c);
+                        acc[i] = c;
+                    }
+                    if (r < BH - 1) load_row(al[ru], r + 8);  // row r is done: the ring takes row r + 8
+                }
+            }
+            if (x < R) {
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    const int c = (yc + i) * side + (x + R), d = a2 + (int)en[i] - 2 * (int)acc[i];
+                    if (yc + i < side && (d < best_d || (d == best_d && c < best_c))) {
+                        best_d = d;
+                        best_c = c;
+                    }
+                }
+            }
         }
     }
 #pragma unroll
