@@ -390,10 +390,14 @@ class MotionEstimatorH263ImplMultiresCrossVer2(MotionEstimatorH264ImplMultiresCr
     the clamped prediction and the zero vector against the searched vector;
     motionRange (at most 64) and vectors in half pels.  The prediction comes
     from the vectors the estimate writes, so pMVPred (an
-    H263MotionVectorPredictorImpl1 in the reference) is not consulted; an
-    object with Set16x16MotionVector still receives every vector."""
+    H263MotionVectorPredictorImpl1 in the reference, which only reads the
+    vector list) is neither consulted nor written."""
 
     KIND = _lib.ME_H263_MULTIRES_CROSS_V2
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        self._pred = None  # the reference sets no vectors on its predictor
 
 
 class MotionEstimatorH264ImplMultires(MotionEstimatorH264ImplMultiresCross):

@@ -5,7 +5,7 @@
 // pair.bin holds the source then the reference luma plane (int16).  The
 // program estimates with GpuMotionEstimatorH264ImplFull (or, by the optional
 // last argument, ...Multires, ...MultiresCross, ...MultiresCrossVer2 or
-// ...Cross, ...UMHS, ...FHS: "multires", "mrc", "mrc2", "cross", "sad", "umhs",
+// ...Cross, ...UMHS, ...FHS, H263ImplMultiresCrossVer2: "multires", "mrc", "mrc2", "cross", "sad", "umhs", "h263mrc2",
 // "fhs"; "impl1" / "impl2" are MotionEstimatorImpl1 / Impl2 with 16x16 blocks, a +-16 pel range and SetMode(0),
 // its half-pel char vectors widened to the output's shorts; "mrc2lam" is Ver2's Lagrangian Estimate(long*, void*) with lambda 2.5;
 // UMHS gets the previous frame's vectors from a first estimate of the same
@@ -46,7 +46,7 @@ int main(int argc, char** argv)
 {
     if (argc != 6 && argc != 7) {
         fprintf(stderr, "usage: %s pair.bin width height motionRange out.bin "
-                        "[full|multires|mrc|mrc2|mrc2lam|cross|sad|umhs|fhs|impl1|impl2]\n", argv[0]);
+                        "[full|multires|mrc|mrc2|mrc2lam|h263mrc2|cross|sad|umhs|fhs|impl1|impl2]\n", argv[0]);
         return 2;
     }
     const std::string kind = argc == 7 ? argv[6] : "full";
@@ -90,6 +90,8 @@ int main(int argc, char** argv)
         me = new GpuMotionEstimatorH264ImplMultires(src.data(), ref.data(), w, h, range, &pred, incl);
     else if (kind == "mrc")
         me = new GpuMotionEstimatorH264ImplMultiresCross(src.data(), ref.data(), w, h, range, incl);
+    else if (kind == "h263mrc2")  // half-pel range 64: the same +-31 pels as the quarter-pel 128
+        me = new GpuMotionEstimatorH263ImplMultiresCrossVer2(src.data(), ref.data(), w, h, range / 2, &pred, incl);
     else if (kind == "mrc2" || kind == "mrc2lam")
         me = new GpuMotionEstimatorH264ImplMultiresCrossVer2(src.data(), ref.data(), w, h, range, &pred, incl);
     else if (kind == "cross")

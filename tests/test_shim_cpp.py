@@ -35,7 +35,7 @@ def test_shim_compiles_against_vpp_interfaces():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("kind", ["full", "multires", "mrc", "mrc2", "mrc2lam", "cross", "sad", "umhs", "fhs", "impl1",
-                                  "impl2"])
+                                  "impl2", "h263mrc2"])
 def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
     from imagecodingutils_gb300 import build
     exe = tmp_path / "example_estimate"
@@ -76,6 +76,8 @@ def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
         mv_o, _, avg_o = orc.me_multires(fr[1], fr[0], mr, mode=0, dist_incl=ones)
     elif kind == "mrc":
         mv_o, _, avg_o = orc.me_multires_cross(fr[1], fr[0], mr, mode=0, dist_incl=ones)
+    elif kind == "h263mrc2":  # half pels, the predictor object is not called
+        mv_o, _, avg_o = orc.me_h263_multires_cross_ver2(fr[1], fr[0], mr // 2, mode=0, dist_incl=ones)
     elif kind == "cross":
         mv_o, _, avg_o = orc.me_cross(fr[1], fr[0], mr, mode=0, dist_incl=ones)
     elif kind == "mrc2lam":
@@ -95,7 +97,7 @@ def test_codec_style_program_on_gpu(tmp_path, vpp, orc, kind):
         mv_o, _, avg_o = orc.me_multires_cross_v2(fr[1], fr[0], mr, mode=0, dist_incl=ones)
     np.testing.assert_array_equal(mv, mv_o)
     assert avg == avg_o
-    if kind != "mrc":  # MultiresCross has no predictor
+    if kind not in ("mrc", "h263mrc2"):  # MultiresCross has no predictor, the H.263 one sets none
         np.testing.assert_array_equal(pred, mv_o.astype(np.int32))
     res = (fr[1][:16].astype(np.int32) - fr[0][:16]).astype(np.int16)
     blocks = res.reshape(4, 4, w // 4, 4).transpose(0, 2, 1, 3).reshape(-1, 16)
