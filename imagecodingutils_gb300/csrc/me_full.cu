@@ -205,7 +205,8 @@ __device__ __forceinline__ unsigned sad4_add(unsigned a, unsigned b, unsigned c)
 // template rows in two passes of the ring's period (a loop body small enough
 // for the instruction cache; the full 16-step unroll stalled on instruction
 // fetch, 0.179 against 0.167 ms), at 3 CTAs per SM, where the loop needs no
-// spills (4 CTAs with a 96-register cap: the same time).
+// spills (4 CTAs with a 96-register cap: the same time; 4 candidate rows per
+// thread, i.e. 8 compute warps, took 0.182 ms at 3 CTAs and 0.190 ms at 2).
 constexpr int SEARCH_ROWS = 8;    // candidate rows per thread (the window-row ring's period)
 constexpr int SEARCH_UNROLL = 8;  // template rows per unrolled loop body (a multiple of SEARCH_ROWS)
 constexpr int SEARCH_WARPS = 64 / (2 * SEARCH_ROWS);  // compute warps: 2 row groups of a warp each
