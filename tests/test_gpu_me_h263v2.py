@@ -104,6 +104,19 @@ def test_sequence_through_one_handle(vpp, ctx, orc):
         assert avg == avg_o
 
 
+@pytest.mark.parametrize("seed,w,h,mr,gen", [(121, 48, 2048, 32, "pan"), (122, 3840, 2160, 64, "noisy"),
+                                              (123, 16, 512, 16, "shift")])
+def test_tall_and_4k_frames(vpp, ctx, orc, seed, w, h, mr, gen):
+    """The exact pass keeps a thread and a ring per macroblock row: 128 and
+    135 rows, and a single column."""
+    fr = umhs_frames(seed, w, h, gen)
+    mv_o, dist_o, avg_o = orc.me_h263_multires_cross_ver2(fr[1], fr[0], mr, mode=0)
+    mv, dist, avg, _ = estimate(vpp, ctx, fr[1], fr[0], mr, 0, sweeps=2)
+    np.testing.assert_array_equal(mv, mv_o)
+    np.testing.assert_array_equal(dist, dist_o)
+    assert avg == avg_o
+
+
 def test_range_limit(vpp, ctx):
     fr = synth.pan_sequence(100, 64, 48, 2)
     me = vpp.MotionEstimatorH263ImplMultiresCrossVer2(fr[1], fr[0], 64, 48, 66, ctx=ctx)
