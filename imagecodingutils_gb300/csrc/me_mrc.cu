@@ -30,6 +30,11 @@
 //                  minimum.  The sub-pel window's lattice (G, h, b,
 //                  j at 22x22 points, with the window's unwritten and
 //                  unscaled edge samples) is built per warp in shared memory.
+//
+// The same file holds the searches of the predictor multi-resolution estimators at prediction
+// (0, 0) with their tie trees (MultiresCrossVer2, Multires; their resolve is me_full_resolve.cu),
+// and MotionEstimatorH263ImplMultiresCrossVer2 whole (k_v263_*: search, tie trees, relaxation
+// sweeps over work lists, the one-CTA exact pass, outputs).
 #include "me_full_common.cuh"
 #include "me_mrc_search.cuh"
 
