@@ -493,8 +493,8 @@ int vppgpu_me_create(vppgpu_ctx* ctx, int kind, int width, int height, int motio
         // planes, the searches at prediction (0, 0) and tie trees, relaxation and exact-pass vectors,
         // records, the sweeps' work lists
         const size_t nall = (size_t)me->cols * ((height + 15) / 16);  // a partial bottom row searched too
-        me->relax_sweeps = vppgpu::UMHS_SWEEPS;
-        if (me->sweep_limit < 32 + vppgpu::UMHS_SWEEPS) me->sweep_limit = 32 + vppgpu::UMHS_SWEEPS;
+        me->relax_sweeps = vppgpu::UMHS_SWEEPS;  // 24: past it the sweeps cost more than the misses they save
+        if (me->sweep_limit < 64 + vppgpu::H263V2_SWEEPS) me->sweep_limit = 64 + vppgpu::H263V2_SWEEPS;
         if ((rc = dalloc(&me->d_src16, npix)) || (rc = dalloc(&me->d_ref16, npix)) ||
             (rc = dalloc(&me->d_mrc, vppgpu::mrc_scratch_bytes(width, height))) ||
             (rc = dalloc(&me->spec, 4 * nall)) || (rc = dalloc(&me->state, 2 * (size_t)me->nmb)) ||
@@ -804,9 +804,9 @@ int vppgpu_me_last_sweeps(vppgpu_me* me, int* sweeps)
 extern "C" int vppgpu_me_set_relax_sweeps(vppgpu_me* me, int sweeps)
 {
     if (!me || sweeps < 0 ||
-        sweeps > ((searches_from_prediction(me->kind) || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2)
-                      ? vppgpu::UMHS_SWEEPS
-                      : vppgpu::RELAX_SWEEPS))
+        sweeps > (me->kind == VPPGPU_ME_H263_MULTIRES_CROSS_V2
+                      ? vppgpu::H263V2_SWEEPS
+                      : (searches_from_prediction(me->kind) ? vppgpu::UMHS_SWEEPS : vppgpu::RELAX_SWEEPS)))
         return VPPGPU_ERR_INVALID_ARG;
     if (me->kind == VPPGPU_ME_MULTIRES_CROSS || me->kind == VPPGPU_ME_H263_MULTIRES_CROSS ||
         me->kind == VPPGPU_ME_FULL_SAD || me->kind == VPPGPU_ME_IMPL1 || me->kind == VPPGPU_ME_IMPL2)

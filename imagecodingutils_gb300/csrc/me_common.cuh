@@ -240,4 +240,27 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* map, int x, i
         : "memory");
 }
 
+// H.263 half-pel samples of four bytes (OverlayMem2Dv2::HalfRead) from the
+// samples a (the block's), b (beside it), c (below or above it) and d (both):
+// the rounded mean of a and its one neighbour on the horizontal or vertical
+// lines, (a + b + c + d + 2) / 4 on the diagonals, evaluated in 16-bit lanes.
+__device__ __forceinline__ unsigned half4(unsigned a, unsigned b, unsigned c, unsigned d, int hx, int hy)
+{
+    if (!hy) return __vavgu4(a, b);
+    if (!hx) return __vavgu4(a, c);
+    const unsigned m = 0x00ff00ffu;
+    const unsigned lo = (a & m) + (b & m) + (c & m) + (d & m) + 0x00020002u;
+    const unsigned hi = ((a >> 8) & m) + ((b >> 8) & m) + ((c >> 8) & m) + ((d >> 8) & m) + 0x00020002u;
+    return ((lo >> 2) & m) | (((hi >> 2) & m) << 8);
+}
+
+// Four bytes at any offset of a row (shared or global memory: the aligned word after the
+// one holding p must be readable).
+__device__ __forceinline__ unsigned word_at(const unsigned char* p)
+{
+    const unsigned* w = reinterpret_cast<const unsigned*>(reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)3);
+    const unsigned sh = (unsigned)(reinterpret_cast<uintptr_t>(p) & 3) * 8;
+    return __funnelshift_r(w[0], w[1], sh);
+}
+
 }  // namespace vppgpu

@@ -46,28 +46,6 @@ __device__ __forceinline__ unsigned row_sd(const unsigned char* p, const unsigne
     return acc;
 }
 
-// H.263 half-pel samples of four bytes (OverlayMem2Dv2::HalfRead) from the
-// samples a (the block's), b (beside it), c (below or above it) and d (both):
-// the rounded mean of a and its one neighbour on the horizontal or vertical
-// lines, (a + b + c + d + 2) / 4 on the diagonals, evaluated in 16-bit lanes.
-__device__ __forceinline__ unsigned half4(unsigned a, unsigned b, unsigned c, unsigned d, int hx, int hy)
-{
-    if (!hy) return __vavgu4(a, b);
-    if (!hx) return __vavgu4(a, c);
-    const unsigned m = 0x00ff00ffu;
-    const unsigned lo = (a & m) + (b & m) + (c & m) + (d & m) + 0x00020002u;
-    const unsigned hi = ((a >> 8) & m) + ((b >> 8) & m) + ((c >> 8) & m) + ((d >> 8) & m) + 0x00020002u;
-    return ((lo >> 2) & m) | (((hi >> 2) & m) << 8);
-}
-
-// Four bytes at any offset of a shared-memory row.
-__device__ __forceinline__ unsigned word_at(const unsigned char* p)
-{
-    const unsigned* w = reinterpret_cast<const unsigned*>(reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)3);
-    const unsigned sh = (unsigned)(reinterpret_cast<uintptr_t>(p) & 3) * 8;
-    return __funnelshift_r(w[0], w[1], sh);
-}
-
 // GetHalfPelSearchStruct (MotionEstimatorImpl1.cpp:445-515): candidate k of
 // the half-pel neighbours left inside the range at (x, y), in the reference's
 // order; their number.

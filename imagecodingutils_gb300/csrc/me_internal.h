@@ -124,6 +124,7 @@ int mrc_launch(vppgpu_ctx* ctx, int W, int H, int motion_range, int mode, const 
 // (H + 15) / 16 rows), relaxation and exact-pass vectors, records (H263V2_RECORDS per MB), per-sweep
 // change counts and work lists; motion_range in half pels.
 constexpr int H263V2_RECORDS = 4;
+constexpr int H263V2_SWEEPS = 48;  // most relaxation sweeps
 struct H263V2Job {
     int W, H, motion_range, mode, sweeps;
     const short* src16;
@@ -138,7 +139,7 @@ struct H263V2Job {
     int* state;
     int* wave;
     int4* rec;
-    int* changed;    // at least 32 + UMHS_SWEEPS entries
+    int* changed;    // at least 64 + H263V2_SWEEPS entries
     int* lists;      // 3 * N_MB: the sweeps' work lists and queue marks
     int* tie_list;   // macroblocks whose search at (0, 0) met a tie
     void* tie_runs;  // their tie trees (mrc_tie_runs_bytes() per MB)

@@ -288,7 +288,10 @@ __device__ __forceinline__ MbSearch h263v2_search(const MrcArgs& a, Lattice& lt,
 
 // Distortion at the prediction (…:1012-1050): its full-pel part clamped to one macroblock outside the
 // picture, OverlayMem2Dv2::HalfRead for its half-pel part, against the input block; one warp, eight
-// samples per lane.  *pv: the clamped half-pel vector.
+// samples (a row half) per lane.  Within the border-19 copy, which the clamp guarantees except for a
+// partial bottom row's block pushed to the copy's last rows, the samples are packed words: HalfRead
+// as byte means (half4), the squares by __vabsdiffu4 and dp4a.  Otherwise every sample is a checked
+// flat read, as the reference reads past its copy there.  *pv: the clamped half-pel vector.
 __device__ int h263v2_pred_d(const MrcArgs& a, int mbr, int mbc, int px, int py, int lane, bool& bad, int* pv)
 {
     const int n = 16 * mbc, m = 16 * mbr;
@@ -302,21 +305,39 @@ __device__ int h263v2_pred_d(const MrcArgs& a, int mbr, int mbc, int px, int py,
     const Org oi = origin(a.in0, 16, 16, 0, n, m), oe = origin(a.e0, 16, 16, 19, x0 + n, y0 + m);
     const int r = oe.y + (lane >> 1), ri = oi.y + (lane >> 1), cb = (lane & 1) * 8;
     int acc = 0;
+    const bool inside = oe.y + (hy < 0 ? -1 : 0) >= 0 && oe.y + 15 + (hy > 0 ? 1 : 0) < a.e0.h && oe.x >= 1 &&
+                        oe.x + 17 < a.e0.w;  // warp-uniform
+    if (inside) {
+        const unsigned char* q = a.e0.p + (size_t)r * a.e0.w + oe.x + cb;
+        const unsigned char* qv = q + hy * a.e0.w;
+        const uint2 in = __ldg(reinterpret_cast<const uint2*>(a.in0.p + (size_t)ri * a.in0.w + oi.x + cb));
+        unsigned u = 0u;
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-        const int c = oe.x + cb + j + (hx < 0 ? -1 : 0);
-        int v;
-        if (hx && hy)
-            v = (rd(a.e0, r, c, bad) + rd(a.e0, r + hy, c, bad) + rd(a.e0, r, c + 1, bad) + rd(a.e0, r + hy, c + 1, bad) +
-                 2) >> 2;
-        else if (hx)
-            v = (rd(a.e0, r, c, bad) + rd(a.e0, r, c + 1, bad) + 1) >> 1;
-        else if (hy)
-            v = (rd(a.e0, r, c, bad) + rd(a.e0, r + hy, c, bad) + 1) >> 1;
-        else
-            v = rd(a.e0, r, c, bad);
-        const int d = rd(a.in0, ri, oi.x + cb + j, bad) - v;
-        acc += d * d;
+        for (int w = 0; w < 2; w++) {
+            const unsigned s = (hx || hy) ? half4(word_at(q + 4 * w), word_at(q + 4 * w + hx), word_at(qv + 4 * w),
+                                                  word_at(qv + 4 * w + hx), hx, hy)
+                                          : word_at(q + 4 * w);
+            const unsigned d = __vabsdiffu4(s, w ? in.y : in.x);
+            u = __dp4a(d, d, u);
+        }
+        acc = (int)u;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int c = oe.x + cb + j + (hx < 0 ? -1 : 0);
+            int v;
+            if (hx && hy)
+                v = (rd(a.e0, r, c, bad) + rd(a.e0, r + hy, c, bad) + rd(a.e0, r, c + 1, bad) +
+                     rd(a.e0, r + hy, c + 1, bad) + 2) >> 2;
+            else if (hx)
+                v = (rd(a.e0, r, c, bad) + rd(a.e0, r, c + 1, bad) + 1) >> 1;
+            else if (hy)
+                v = (rd(a.e0, r, c, bad) + rd(a.e0, r + hy, c, bad) + 1) >> 1;
+            else
+                v = rd(a.e0, r, c, bad);
+            const int d = rd(a.in0, ri, oi.x + cb + j, bad) - v;
+            acc += d * d;
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -507,7 +528,8 @@ __global__ void __launch_bounds__(V2_TIE_RUNS * 32) k_v263_tietree(V263 v)
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&v.m.ctrl->status, ST_OUT_OF_BOUNDS);
 }
 
-constexpr int kListLen = 32;  // offset of the work-list lengths in V263::changed
+constexpr int kListLen = 64;  // offset of the work-list lengths in V263::changed (after the change counts)
+static_assert(H263V2_SWEEPS <= kListLen, "change counts and list lengths must not overlap");
 
 // One relaxation sweep over the macroblocks whose prediction may have moved: every macroblock in the
 // first sweep, then those a vector change of the previous sweep reaches (its right, below-left and
@@ -573,8 +595,9 @@ __device__ __forceinline__ void cp_async_wait()
 // vector (a register) and the row above's last vectors (a four-slot ring per row in shared memory; the
 // slot row r writes in step t is none of the two row r + 1 reads then).  Each row's records and search
 // at (0, 0) arrive by cp.async kDiagDepth - 1 steps ahead; a record gives the result for the
-// prediction, and the macroblocks that find none are listed in shared memory and evaluated by every
-// warp of the CTA, one macroblock per warp.  Up to three block barriers per step, no waits.
+// prediction and is published at once; the macroblocks that find none are listed in shared memory
+// and evaluated by every warp of the CTA, one macroblock per warp.  One block barrier per step, three
+// when a step has misses; no waits.
 constexpr int kDiagThreads = 512;  // rows of at most 512 macroblocks (pictures up to 8192 lines)
 constexpr int kDiagDepth = 4;      // steps of records in flight per row
 constexpr int kDiagPre = kV2Rec + 1;  // 16-byte words per row and step: the records, then the search at (0, 0)
@@ -637,17 +660,23 @@ __global__ void __launch_bounds__(kDiagThreads, 1) k_v263_diag(V263 v)
                     mv = rec.y;
                 }
             }
-            if (!hit) {
+            if (hit) {  // published now: no row reads this slot in this step
+                left = mv;
+                ring[r * 4 + (c & 3)] = mv;
+                __stcg(v.wave + k, mv);
+            } else {
                 slot = atomicAdd(&s_nmiss[t & 1], 1);
                 miss_k[slot] = k;
                 miss_p[slot] = p;
                 miss_s0[slot] = cur[kV2Rec];
             }
         }
+        // the next step's counter: last read in step t-1 before that step's last barrier (or it is
+        // zero already), first incremented after this step's first barrier
+        if (threadIdx.x == 0) s_nmiss[(t + 1) & 1] = 0;
         __syncthreads();
         const int n = s_nmiss[t & 1];
-        if (threadIdx.x == 0) s_nmiss[(t + 1) & 1] = 0;  // untouched until after this step's last barrier
-        if (n) {
+        if (n) {  // the misses, one warp each; then their rows publish and the step ends
             for (int i = wid; i < n; i += nw) {
                 const int kk = miss_k[i], mbr = kk / cols;
                 const int2 res = h263v2_compute(v, lt, kk, mbr, kk - mbr * cols, miss_p[i], miss_s0[i], false, lane,
@@ -655,14 +684,14 @@ __global__ void __launch_bounds__(kDiagThreads, 1) k_v263_diag(V263 v)
                 if (lane == 0) miss_v[i] = res.x;
             }
             __syncthreads();
-            if (slot >= 0) mv = miss_v[slot];
+            if (slot >= 0) {
+                mv = miss_v[slot];
+                left = mv;
+                ring[r * 4 + (c & 3)] = mv;
+                __stcg(v.wave + k, mv);
+            }
+            __syncthreads();
         }
-        if (act) {
-            left = mv;
-            ring[r * 4 + (c & 3)] = mv;
-            __stcg(v.wave + k, mv);
-        }
-        __syncthreads();
     }
     cp_async_wait<0>();
     bad = __any_sync(0xffffffffu, bad);
@@ -878,7 +907,7 @@ int h263v2_launch(vppgpu_ctx* ctx, const H263V2Job& j)
     v.runs = static_cast<V2TieRun*>(j.tie_runs);
     v.sweeps = j.sweeps;
     VPP_CUDA(cudaMemsetAsync(j.rec, 0x7f, sizeof(int4) * kV2Rec * (size_t)m.nmb, ctx->stream));
-    VPP_CUDA(cudaMemsetAsync(j.changed, 0, sizeof(int) * (size_t)(kListLen + UMHS_SWEEPS), ctx->stream));
+    VPP_CUDA(cudaMemsetAsync(j.changed, 0, sizeof(int) * (size_t)(kListLen + H263V2_SWEEPS), ctx->stream));
     VPP_CUDA(cudaMemsetAsync(j.lists + 2 * (size_t)m.nmb, 0xff, sizeof(int) * (size_t)m.nmb, ctx->stream));
     // later sweeps walk short work lists: a grid of a few CTAs per SM strides over them
     const int blocks = min((m.nmb + 7) / 8, 4 * ctx->sm_count);
