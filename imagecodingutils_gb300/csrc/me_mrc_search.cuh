@@ -68,6 +68,10 @@ __device__ __forceinline__ int rd(const Buf& b, int r, int c, bool& bad)
     return __ldg(b.p + f);
 }
 
+// A read inside a block that origin() placed in its buffer (every row and column of the block lies
+// within the copy, as the clamp guarantees): no check needed.
+__device__ __forceinline__ int rdb(const Buf& b, int r, int c) { return __ldg(b.p + (size_t)r * b.w + c); }
+
 // GetMotionRange of the multi-resolution estimators (…MultiresCross.cpp:1195-1262).
 struct Level {
     int boundary, width, height, vec_range;
@@ -116,13 +120,14 @@ __device__ __forceinline__ void phase_coords(int lane, int& r0, int& c0)
     c0 = kPhaseCol[p];
 }
 
-// Full n x n SSD of two overlays, one warp (lane per column/row chunk).
+// Full n x n SSD of two overlays placed by origin(), one warp (lane per column/row chunk).
 __device__ __forceinline__ int full_ssd(const Buf& a, Org oa, const Buf& b, Org ob, int n, int lane, bool& bad)
 {
+    (void)bad;  // both blocks lie inside their copies
     int acc = 0;
     for (int i = lane; i < n * n; i += 32) {
         const int r = i / n, c = i - r * n;
-        const int d = rd(a, oa.y + r, oa.x + c, bad) - rd(b, ob.y + r, ob.x + c, bad);
+        const int d = rdb(a, oa.y + r, oa.x + c) - rdb(b, ob.y + r, ob.x + c);
         acc += d * d;
     }
     return warp_sum(acc);
@@ -309,12 +314,12 @@ __device__ MbSearch search_mb_with(const MrcArgs& a, Lattice& LT, int mbr, int m
     phase_coords<8>(lane, r1, c1);
     int cur1[2];
 #pragma unroll
-    for (int j = 0; j < 2; j++) cur1[j] = rd(a.in1, oin1.y + r1, oin1.x + c1 + 4 * j, bad);
+    for (int j = 0; j < 2; j++) cur1[j] = rdb(a.in1, oin1.y + r1, oin1.x + c1 + 4 * j);
     auto part8 = [&](Org o) {
         int acc = 0;
 #pragma unroll
         for (int j = 0; j < 2; j++) {
-            const int d = cur1[j] - rd(a.e1, o.y + r1, o.x + c1 + 4 * j, bad);
+            const int d = cur1[j] - rdb(a.e1, o.y + r1, o.x + c1 + 4 * j);
             acc += d * d;
         }
         return acc;
@@ -361,14 +366,14 @@ __device__ MbSearch search_mb_with(const MrcArgs& a, Lattice& LT, int mbr, int m
 #pragma unroll
     for (int i = 0; i < 2; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) cur0[4 * i + j] = rd(a.in0, oin0.y + r0 + 4 * i, oin0.x + c0 + 4 * j, bad);
+        for (int j = 0; j < 4; j++) cur0[4 * i + j] = rdb(a.in0, oin0.y + r0 + 4 * i, oin0.x + c0 + 4 * j);
     auto part16 = [&](Org o) {
         int acc = 0;
 #pragma unroll
         for (int i = 0; i < 2; i++)
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const int d = cur0[4 * i + j] - rd(a.e0, o.y + r0 + 4 * i, o.x + c0 + 4 * j, bad);
+                const int d = cur0[4 * i + j] - rdb(a.e0, o.y + r0 + 4 * i, o.x + c0 + 4 * j);
                 acc += d * d;
             }
         return acc;
@@ -521,7 +526,7 @@ __device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int m
         const int sub = lane >> 2, br = lane & 3;
         int cur2[4];
 #pragma unroll
-        for (int c = 0; c < 4; c++) cur2[c] = rd(a.in2, oin2.y + br, oin2.x + c, bad);
+        for (int c = 0; c < 4; c++) cur2[c] = rdb(a.in2, oin2.y + br, oin2.x + c);
         int min2 = full_ssd(a.in2, oin2, a.e2, origin(a.e2, 4, 4, 5, ll, kk), 4, lane, bad);
         mr_range(L2, ll, kk, 0, 0, l2_range - 1, xl, xr, yu, yd);
         for (int i = yu; i <= yd; i++)
@@ -531,7 +536,7 @@ __device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int m
                     const Org o = origin(a.e2, 4, 4, 5, ll + j0 + sub, kk + i);
 #pragma unroll
                     for (int c = 0; c < 4; c++) {
-                        const int e = cur2[c] - rd(a.e2, o.y + br, o.x + c, bad);
+                        const int e = cur2[c] - rdb(a.e2, o.y + br, o.x + c);
                         d += e * e;
                     }
                 }
@@ -560,7 +565,7 @@ __device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int m
     phase_coords<8>(lane, r1, c1);
     int cur1[2];
 #pragma unroll
-    for (int j = 0; j < 2; j++) cur1[j] = rd(a.in1, oin1.y + r1, oin1.x + c1 + 4 * j, bad);
+    for (int j = 0; j < 2; j++) cur1[j] = rdb(a.in1, oin1.y + r1, oin1.x + c1 + 4 * j);
     int min1 = full_ssd(a.in1, oin1, a.e1, origin(a.e1, 8, 8, 9, mx + q, my + p), 8, lane, bad);
     int rmx = 0, rmy = 0;
     mr_range(L1, q, p, mx, my, lcl_l1_range, xl, xr, yu, yd);
@@ -571,7 +576,7 @@ __device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int m
             int acc = 0;
 #pragma unroll
             for (int t = 0; t < 2; t++) {
-                const int e = cur1[t] - rd(a.e1, o.y + r1, o.x + c1 + 4 * t, bad);
+                const int e = cur1[t] - rdb(a.e1, o.y + r1, o.x + c1 + 4 * t);
                 acc += e * e;
             }
             const int d = warp_sum(acc);
@@ -594,14 +599,14 @@ __device__ MbSearch search_mr_with(const MrcArgs& a, Lattice& LT, int mbr, int m
 #pragma unroll
     for (int i = 0; i < 2; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) cur0[4 * i + j] = rd(a.in0, oin0.y + r0 + 4 * i, oin0.x + c0 + 4 * j, bad);
+        for (int j = 0; j < 4; j++) cur0[4 * i + j] = rdb(a.in0, oin0.y + r0 + 4 * i, oin0.x + c0 + 4 * j);
     auto ssd16 = [&](Org o) {
         int acc = 0;
 #pragma unroll
         for (int i = 0; i < 2; i++)
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const int e = cur0[4 * i + j] - rd(a.e0, o.y + r0 + 4 * i, o.x + c0 + 4 * j, bad);
+                const int e = cur0[4 * i + j] - rdb(a.e0, o.y + r0 + 4 * i, o.x + c0 + 4 * j);
                 acc += e * e;
             }
         return warp_sum(acc);
@@ -790,12 +795,12 @@ __device__ MbSearch search_lambda(const MrcArgs& a, Lattice& LT, int mbr, int mb
     phase_coords<8>(lane, r1, c1);
     int cur1[2];
 #pragma unroll
-    for (int j = 0; j < 2; j++) cur1[j] = rd(a.in1, oin1.y + r1, oin1.x + c1 + 4 * j, bad);
+    for (int j = 0; j < 2; j++) cur1[j] = rdb(a.in1, oin1.y + r1, oin1.x + c1 + 4 * j);
     auto part8 = [&](Org o) {
         int acc = 0;
 #pragma unroll
         for (int j = 0; j < 2; j++) {
-            const int d = cur1[j] - rd(a.e1, o.y + r1, o.x + c1 + 4 * j, bad);
+            const int d = cur1[j] - rdb(a.e1, o.y + r1, o.x + c1 + 4 * j);
             acc += d * d;
         }
         return acc;
@@ -843,14 +848,14 @@ __device__ MbSearch search_lambda(const MrcArgs& a, Lattice& LT, int mbr, int mb
 #pragma unroll
     for (int i = 0; i < 2; i++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) cur0[4 * i + j] = rd(a.in0, oin0.y + r0 + 4 * i, oin0.x + c0 + 4 * j, bad);
+        for (int j = 0; j < 4; j++) cur0[4 * i + j] = rdb(a.in0, oin0.y + r0 + 4 * i, oin0.x + c0 + 4 * j);
     auto part16 = [&](Org o) {
         int acc = 0;
 #pragma unroll
         for (int i = 0; i < 2; i++)
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const int d = cur0[4 * i + j] - rd(a.e0, o.y + r0 + 4 * i, o.x + c0 + 4 * j, bad);
+                const int d = cur0[4 * i + j] - rdb(a.e0, o.y + r0 + 4 * i, o.x + c0 + 4 * j);
                 acc += d * d;
             }
         return acc;
