@@ -71,7 +71,7 @@ def test_against_oracle(vpp, ctx, orc, seed, w, h, mr, mode, gen):
         assert avg == avg_o
 
 
-@pytest.mark.parametrize("sweeps", [0, 1, 3, 8, 24])
+@pytest.mark.parametrize("sweeps", [0, 1, 3, 8, 24, 48])
 def test_result_independent_of_sweeps(vpp, ctx, orc, sweeps):
     """Relaxation either reaches the fixed point (the sequential result) or
     hands over to the one-CTA exact pass: every setting gives the same vectors."""
